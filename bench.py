@@ -1,0 +1,311 @@
+"""Benchmark of the COLA particle-mesh step on GB300.
+
+Workload (default): nDGP, rc*H0 = 1, density screening on (Gaussian filter,
+Rsmooth 1 Mpc/h), 512^3 particles on a 1024^3 mesh, Box 1024 Mpc/h, 50
+linear-in-a steps from z = 19, seed 5003, amplitude-fixed 2LPT initial
+conditions, P(k) every step in 512 linear bins over [2 pi/Box, k_Nyquist].
+A step is one KDK step: CIC deposit, R2C, P(k) binning, fifth force (smoothing
+C2R, screening, R2C), force k-space pass, three C2R, fused interpolation +
+kick + drift.  Inputs are synthetic (generated by the IC on the device);
+the working set (~50 GB) is far larger than L2, so no L2 flush is needed.
+
+value: Mparticle-steps/s with the particle state resident in HBM.
+e2e:   the same metric through the host-buffer C-ABI call mgp_step_host
+       (pinned host particle arrays copied in and out every step).
+--impl reference: the FP64 CPU oracle (restatement of the reference's C
+       code) timed on the host cores on a bounded sample of the workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "mg-picola-public_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mparticle-steps/s at 512^3 / 1024^3 mesh; P(k) rel. err vs FP64 oracle"
+UNIT = "Mparticle-steps/s"
+
+CONFIGS = {
+    # name: (Ns, N, Box, model, nsteps_total, seed)
+    "ndgp_512_1024": dict(Ns=512, N=1024, Box=1024.0, model="dgp", nsteps=50, seed=5003, fixed=1, nbins=512),
+    "ndgp_256_512": dict(Ns=256, N=512, Box=512.0, model="dgp", nsteps=50, seed=5003, fixed=1, nbins=256),
+    "lcdm_64_128": dict(Ns=64, N=128, Box=256.0, model="lcdm", nsteps=10, seed=5001, fixed=0, nbins=64),
+}
+
+
+def make_params(M, cfg):
+    kw = dict(Nmesh=cfg["N"], Nsample=cfg["Ns"], Box=cfg["Box"], Seed=cfg["seed"], Init_Redshift=19.0,
+              amplitude_fixed_initial_condition=cfg["fixed"], pofk_compute_every_step=1, pofk_nbins=cfg["nbins"],
+              pofk_bintype=0, pofk_kmin=2 * np.pi / cfg["Box"], pofk_kmax=np.pi * cfg["N"] / cfg["Box"],
+              pofk_subtract_shotnoise=1, Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8,
+              PrimordialIndex=0.96, WhichSpectrum=2, UseCOLA=1)
+    if cfg["model"] == "dgp":
+        kw.update(model=M.MODEL_DGP, modified_gravity_active=1, include_screening=1, rcH0_DGP=1.0, Rsmooth=1.0,
+                  smoothing_filter=M.FILTER_GAUSSIAN, input_pofk_is_for_lcdm=1, input_sigma8_is_for_lcdm=1)
+    return M.default_params(**kw)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                f = [x.strip() for x in out.stdout.strip().split(",")]
+                if len(f) == 7:
+                    self.samples.append(f)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def algorithmic_bytes(N, Np, kernel):
+    """Minimum HBM bytes per launch of each stage (FP32)."""
+    NH = N // 2 + 1
+    nreal = N * N * 2 * NH
+    ncomplex = N * N * NH
+    return {
+        "cic": 12 * Np + 4 * N ** 3,                 # read s, write the mesh once
+        "pofk": 8 * ncomplex,                         # read delta(k)
+        "forces": 2 * 8 * ncomplex + 3 * 8 * ncomplex,  # read delta, MG source; write 3 complex grids
+        "interp_kick_drift": 12 * N ** 3 + 72 * Np,   # force grids once; s,v,D1,D2 in, s,v out
+        "mg": 8 * ncomplex + 4 * nreal + 8 * nreal,   # smoothing pass + screening pass (excl. FFTs)
+    }[kernel]
+
+
+def run_gpu(args):
+    import mgpicola as M
+
+    cfg = CONFIGS[args.config]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    p = make_params(M, cfg)
+    Np = cfg["Ns"] ** 3
+    N = cfg["N"]
+    ctx = M.Context(p, device=local if world > 1 else 0)
+    ctx.displacement_fields()
+    A0 = 1.0 / (1.0 + p.Init_Redshift)
+    da = (1.0 - A0) / cfg["nsteps"]
+    state = {"A": A0, "AI": A0}
+
+    def step():
+        A, AI = state["A"], state["AI"]
+        AF, AFF = A + 0.5 * da, A + da
+        ctx.step(A, AI, AF, AFF)
+        state["A"], state["AI"] = AFF, AF
+
+    def sync():
+        # mgp_kernel_ms synchronises the context stream on its last event
+        ctx.kernel_ms("interp_kick_drift")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    ctx.set_timing(True)
+    sync()
+    barrier()
+    launches0 = ctx.launches()
+    stage_ms = {k: 0.0 for k in ["cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift"]}
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        dev_ms = 0.0
+        for _ in range(args.steps):
+            step()
+            dev_ms += ctx.kernel_ms("step")  # CUDA events around the whole step
+            for k in stage_ms:
+                v = ctx.kernel_ms(k)
+                if v > 0:
+                    stage_ms[k] += v
+        wall = time.perf_counter() - t0
+    elapsed = dev_ms * 1e-3
+    launches = ctx.launches() - launches0
+    barrier()
+    if dist is not None:
+        import torch
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    ms_per_step = elapsed / args.steps * 1e3
+    value = world * Np * args.steps / elapsed / 1e6
+
+    # e2e through the host-buffer C-ABI entry point, pinned host memory
+    ctx.set_timing(False)
+    pos, vel, d1, d2 = ctx.get_particles()
+    for a in (pos, vel, d1, d2):
+        M.pin(a)
+    e2e_steps = max(1, min(args.steps, 5))
+    barrier()
+    te = time.perf_counter()
+    for _ in range(e2e_steps):
+        A, AI = state["A"], state["AI"]
+        AF, AFF = A + 0.5 * da, A + da
+        ctx.step_host(A, AI, AF, AFF, pos, vel, d1, d2)
+        state["A"], state["AI"] = AFF, AF
+    e2e_t = time.perf_counter() - te
+    for a in (pos, vel, d1, d2):
+        M.unpin(a)
+    e2e_val = world * Np * e2e_steps / e2e_t / 1e6
+    k, pk, km, n = ctx.pofk()
+    ctx.close()
+
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+    own = {k: v / args.steps for k, v in stage_ms.items() if k not in ("r2c", "c2r")}
+    dom = max(own, key=own.get)
+    abytes = algorithmic_bytes(N, Np, dom)
+    achieved = abytes / (own[dom] * 1e-3) / 1e9
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (2LPT IC generated on the device, seed 5003)",
+        "config": {"workload": args.config, "particles": Np, "mesh": N, "box_mpc_h": cfg["Box"],
+                   "model": "nDGP rcH0=1 screening (Gaussian, Rsmooth=1)" if cfg["model"] == "dgp" else "LCDM",
+                   "pofk_every_step": True, "pofk_bins": cfg["nbins"], "l2": "inputs larger than L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": round(e2e_val, 3), "unit": UNIT, "h2d_bytes_per_step": 4 * 12 * Np,
+                "d2h_bytes_per_step": 2 * 12 * Np, "api": "mgp_step_host"},
+        "gpu_launches": int(launches),
+        "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stage_ms.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "algorithmic_bytes_per_launch": abytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def oracle_params(O, cfg):
+    rp = O.RunParams()
+    if cfg["model"] == "dgp":
+        rp.mg = O.make_mg(O.DGP, 0.267, rcH0=1.0, rsmooth=1.0)
+    else:
+        rp.mg = O.make_mg(O.LCDM, 0.267)
+    rp.pw = O.make_power(omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sigma8=0.8)
+    rp.ic = O.ICParams(cfg["N"], cfg["Ns"], cfg["Box"], cfg["seed"], 0, cfg["fixed"], 0, 1.0)
+    rp.init_redshift = 19.0
+    rp.nsteps = cfg["nsteps"]
+    rp.final_redshift = 0.0
+    rp.pofk_nbins, rp.pofk_bintype, rp.pofk_subtract_shotnoise = cfg["nbins"], 0, 1
+    rp.pofk_kmin, rp.pofk_kmax = 2 * np.pi / cfg["Box"], np.pi * cfg["N"] / cfg["Box"]
+    rp.usecola = 1
+    return rp
+
+
+SAMPLE = {"ndgp_512_1024": "ndgp_128_256", "ndgp_256_512": "ndgp_128_256", "lcdm_64_128": "lcdm_64_128"}
+CONFIGS["ndgp_128_256"] = dict(Ns=128, N=256, Box=256.0, model="dgp", nsteps=50, seed=5003, fixed=1, nbins=128)
+
+
+def cpu_baseline(args, nsteps=1):
+    from oracle import oracle as O
+
+    name = SAMPLE[args.config]
+    cfg = CONFIGS[name]
+    dt = O.lib().orc_time_steps(oracle_params(O, cfg), nsteps)
+    Np = cfg["Ns"] ** 3
+    return {"value": round(Np / dt / 1e6, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d full FP64 KDK step(s) of the same model at %d^3 particles / %d^3 mesh (Box %g), "
+                      "OpenMP FFTs on all host cores, serial CIC/interp as the reference; per-particle cost at "
+                      "512^3/1024^3 is higher (FFT ~ N^3 log N)" % (nsteps, cfg["Ns"], cfg["N"], cfg["Box"])}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    name = SAMPLE[args.config]
+    cfg = CONFIGS[name]
+    rp = oracle_params(O, cfg)
+    if args.warmup > 0:
+        O.lib().orc_time_steps(rp, 1)
+    dt = O.lib().orc_time_steps(rp, max(1, args.steps))
+    Np = cfg["Ns"] ** 3
+    v = Np / dt / 1e6
+    cb = {"value": round(v, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+          "sample": "FP64 oracle KDK steps at %d^3 particles / %d^3 mesh, same model" % (cfg["Ns"], cfg["N"])}
+    print(json.dumps({"metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+                      "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": args.config, "sample": name}, "impl": "reference",
+                      "cpu_baseline": cb,
+                      "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="ndgp_512_1024", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

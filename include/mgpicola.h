@@ -1,0 +1,244 @@
+/*
+ * mgpicola.h -- C ABI of the GB300 COLA particle-mesh step and 2LPT IC path.
+ *
+ * Drop-in boundary for MG-PICOLA's hot path.  Every entry point is extern "C",
+ * takes plain pointers and sizes, and returns an int status (MGP_OK = 0,
+ * negative MGP_E* on failure; mgp_last_error() gives the message).  The
+ * reference aborts the whole MPI job instead (FatalError, src/auxPM.c:668-673).
+ *
+ * Ownership: the library owns all device memory of a context; the caller owns
+ * every host buffer it passes.  One context per host thread; each context
+ * owns one CUDA stream and every call is stream-ordered and synchronous on
+ * return unless stated otherwise.
+ *
+ * Reference interfaces replaced (paths within MG-PICOLA-PUBLIC):
+ *   mgp_params                 <- parameter-file globals, src/vars.h:60-472,
+ *                                 read by read_parameterfile src/read_param.c:107-445
+ *   mgp_read_parameterfile     <- read_parameterfile + read_mg_parameters
+ *                                 (src/read_param.c:107-445,
+ *                                 src/user_defined_functions.h:227-406)
+ *   mgp_create                 <- the start-up of main (src/main.c:33-200):
+ *                                 set_units, initialize_powerspectrum,
+ *                                 initialize_ffts, init_modified_version
+ *   mgp_displacement_fields    <- displacement_fields (src/2LPT.c:185-1519) +
+ *                                 the particle assignment of src/main.c:231-309
+ *   mgp_get_displacements      <- GetDisplacements (src/auxPM.c:37-103):
+ *                                 PtoMesh + ComputeFifthForce + Forces
+ *   mgp_kick_drift             <- MtoParticles (src/auxPM.c:560-644) +
+ *                                 Kick (src/main.c:688-742) + Drift
+ *                                 (src/main.c:747-787), fused
+ *   mgp_pofk                   <- compute_power_spectrum (src/compute_pofk.c:71-271)
+ *   mgp_run                    <- the time loop of main (src/main.c:394-611)
+ *   mgp_get_particles          <- the particle data read by Output
+ *                                 (src/main.c:792-1061)
+ */
+#ifndef MGPICOLA_H
+#define MGPICOLA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status */
+#define MGP_OK 0
+#define MGP_EINVAL -1       /* invalid argument or parameter value */
+#define MGP_ECUDA -2        /* CUDA runtime error */
+#define MGP_ECUFFT -3       /* cuFFT error */
+#define MGP_ENOMEM -4       /* allocation failed */
+#define MGP_EIO -5          /* file could not be read or written */
+#define MGP_EPARAM -6       /* parameter file: unknown, duplicate or missing key */
+#define MGP_ESTATE -7       /* call out of order (e.g. forces before density) */
+#define MGP_ENUMERIC -8     /* ODE / numerical failure */
+
+/* ------------------------------------------------------------ models */
+/* The reference picks the model at compile time (Makefile:61-106). */
+#define MGP_MODEL_LCDM 0
+#define MGP_MODEL_FOFR 1        /* Hu-Sawicki f(R), potential screening */
+#define MGP_MODEL_DGP 2         /* normal-branch DGP, density screening */
+#define MGP_MODEL_BRANSDICKE 3  /* JBD: Geff(a) rescaling of the density */
+#define MGP_MODEL_MBETA 4       /* general m(a), beta(a) (symmetron example) */
+
+#define MGP_FILTER_NONE 0
+#define MGP_FILTER_GAUSSIAN 1
+#define MGP_FILTER_TOPHAT 2
+#define MGP_FILTER_SHARPK 3
+
+/* Run parameters.  Field names are the parameter-file keys of the
+ * reference (src/read_param.c:167-265, src/user_defined_functions.h:233-405,
+ * paramfiles/additions_compute_pofk.txt). */
+typedef struct mgp_params {
+  /* model selection (compile-time in the reference) */
+  int model;
+  int smoothing_filter;            /* GAUSSIANFILTER etc. (src/mg.h:318-338) */
+  int use_w0wa;                    /* EQUATIONOFSTATE_PARAMETRIZATION */
+  int scaledependent;              /* SCALEDEPENDENT build */
+
+  /* modified gravity */
+  int modified_gravity_active;
+  int include_screening;
+  int use_lcdm_growth_factors;
+  int input_pofk_is_for_lcdm;
+  int input_sigma8_is_for_lcdm;
+  int inverted_initial_condition;
+  int amplitude_fixed_initial_condition;
+  double fofr0, nfofr;             /* FOFR */
+  double Rsmooth, rcH0_DGP;        /* DGP */
+  double wBD, Omegah2, Omegarh2, Omegavh2;   /* BRANSDICKE */
+  double range_symm, assb_symm, beta_symm;  /* MBETA */
+  double w_0, w_a;
+
+  /* P(k) */
+  int pofk_compute_every_step;
+  int pofk_compute_rsd_pofk;
+  int pofk_nbins;
+  int pofk_bintype;
+  int pofk_subtract_shotnoise;
+  double pofk_kmin, pofk_kmax;
+
+  /* outputs */
+  char OutputDir[500];
+  char FileBase[500];
+  char OutputRedshiftFile[500];
+  int NumFilesWrittenInParallel;
+
+  /* simulation */
+  int UseCOLA;
+  double Buffer;
+  int Nmesh;
+  int Nsample;
+  double Box;
+  double Init_Redshift;
+  int Seed;
+  int SphereMode;
+  int WhichSpectrum;
+  int WhichTransfer;
+  char FileWithInputSpectrum[500];
+  char FileWithInputTransfer[500];
+
+  /* cosmology */
+  double Omega;
+  double OmegaBaryon;
+  double HubbleParam;
+  double Sigma8;
+  double PrimordialIndex;
+
+  /* units */
+  double UnitLength_in_cm;
+  double UnitMass_in_g;
+  double UnitVelocity_in_cm_per_s;
+  double InputSpectrum_UnitLength_in_cm;
+
+  /* output list (read_outputs, src/read_param.c:32-89); descending z */
+  int Noutputs;
+  double output_redshift[64];
+  int output_nsteps[64];
+} mgp_params;
+
+typedef struct mgp_ctx mgp_ctx;
+
+/* Fill *p with the defaults used by the reference's example parameter
+ * files (paramfiles/example_*.txt). */
+int mgp_params_default(mgp_params *p);
+
+/* read_parameterfile (src/read_param.c:107-445) for `model`: every key the
+ * reference registers for that model is mandatory, unknown or repeated keys
+ * are errors, '%' starts a comment.  Also reads OutputRedshiftFile
+ * (read_outputs, src/read_param.c:32-89) unless read_outputs == 0, and the
+ * tabulated spectrum for WhichSpectrum == 1 at mgp_create time. */
+int mgp_read_parameterfile(const char *fname, int model, int pofk_keys, int read_outputs, mgp_params *p);
+
+/* Start-up: validate parameters, solve the growth ODEs, normalise the power
+ * spectrum, allocate device memory on `device` and plan the FFTs. */
+int mgp_create(const mgp_params *p, int device, mgp_ctx **out);
+int mgp_destroy(mgp_ctx *ctx);
+const char *mgp_last_error(void);
+
+/* 2LPT initial conditions on the device (displacement_fields + the particle
+ * assignment of main.c:231-309): afterwards the context holds positions at
+ * a_init = 1/(1+Init_Redshift), zero COLA velocities and the Lagrangian
+ * displacements D1 (ZA) and D2 (2LPT, times -3/7). */
+int mgp_displacement_fields(mgp_ctx *ctx);
+
+/* GetDisplacements at scale factor A: CIC density, forward FFT, optional
+ * P(k) (pofk_compute_every_step), fifth force, and the force grids. */
+int mgp_get_displacements(mgp_ctx *ctx, double A);
+
+/* Fused MtoParticles + Kick (AI -> AF at A) [+ Drift A -> AFF].  Requires a
+ * preceding mgp_get_displacements at the same A. */
+int mgp_kick_drift(mgp_ctx *ctx, double AI, double AF, double A, double AFF, int do_drift);
+
+/* One KDK step (main.c:410-602 body for a non-output step). */
+int mgp_step(mgp_ctx *ctx, double A, double AI, double AF, double AFF);
+
+/* Full time loop with outputs (main.c:394-611).  Writes snapshot files
+ * (GADGET-1 when gadget != 0, else ASCII) and pofk_* files to OutputDir. */
+int mgp_run(mgp_ctx *ctx, int gadget);
+
+/* P(k) of the most recent density (compute_power_spectrum).  Arrays of
+ * capacity `cap`; *nbins receives the bin count after the reference's
+ * parameter adjustment (compute_pofk.c:758-805).  k = k_from_index,
+ * kmean = mean |k| of the modes, n = mode count (weights as the reference). */
+int mgp_pofk(mgp_ctx *ctx, int cap, int *nbins, double *k, double *pk, double *kmean, double *n);
+
+/* RSD multipoles P0/P2/P4 for LOS y and z (compute_RSD_powerspectrum,
+ * src/compute_pofk.c:403-512) at the current particle state.  The seven
+ * output arrays (k, P0, P2, P4 averaged over y and z, and the sigma
+ * columns) have capacity `cap`. */
+int mgp_pofk_rsd(mgp_ctx *ctx, double A, int cap, int *nbins, double *k, double *P0, double *P2,
+                 double *P4, double *s0, double *s2, double *s4, double *n);
+
+/* Particle state, host buffers of [np][3] floats (AoS, the order of
+ * struct part_data's Pos/Vel/D/D2, src/vars.h:292-321).  Positions are
+ * wrapped to [0, Box); velocities are the internal COLA velocities
+ * (Vel - <Vel> is what Drift uses).  Any pointer may be NULL. */
+int mgp_get_particles(mgp_ctx *ctx, float *pos, float *vel, float *D1, float *D2, size_t np);
+int mgp_set_particles(mgp_ctx *ctx, const float *pos, const float *vel, const float *D1,
+                      const float *D2, size_t np);
+
+/* Host-buffer step for drop-in callers that keep particles in host memory:
+ * copies pos/vel/D1/D2 in, runs mgp_step, copies pos/vel back. */
+int mgp_step_host(mgp_ctx *ctx, double A, double AI, double AF, double AFF, float *pos, float *vel,
+                  const float *D1, const float *D2, size_t np);
+
+/* Growth factors and COLA coefficients of the context's cosmology
+ * (src/cosmo.c:318-403, 1114-1160). which: 0 D, 1 dD/dy, 2 d2D/dy2,
+ * 3 D2, 4 dD2/dy, 5 d2D2/dy2, 6 D_LCDM. */
+double mgp_growth(mgp_ctx *ctx, int which, double a);
+double mgp_Sq(mgp_ctx *ctx, double ai, double af, double aref);
+double mgp_Sphi(mgp_ctx *ctx, double ai, double af, double aref);
+double mgp_power_spectrum(mgp_ctx *ctx, double k);
+
+/* Host-only cosmology of a parameter set (no device needed): which 0-6 as
+ * mgp_growth, 7 the linear P(k) at x = k (h/Mpc); mgp_cosmo_coeff gives Sq
+ * (kind 0) or Sphi (kind 1) for n triples (ai, af, aref). */
+int mgp_cosmo_eval(const mgp_params *p, int which, const double *x, int n, double *out);
+int mgp_cosmo_coeff(const mgp_params *p, int kind, const double *ai, const double *af, const double *aref, int n,
+                    double *out);
+
+/* Copy an internal grid to a host buffer (diagnostics and parity tests).
+ * which: 0 density (real padded [N][N][2(N/2+1)] float), 1 delta(k)
+ * (complex [N][N][N/2+1] float pairs), 2..4 force grids x,y,z (real
+ * padded), 5 MG source (complex).  `count` is the number of floats. */
+int mgp_copy_grid(mgp_ctx *ctx, int which, float *host, size_t count);
+
+/* Kernel timing: CUDA-event milliseconds of the named kernels launched by
+ * the last call (names: "cic", "r2c", "pofk", "forces", "c2r", "interp_kick_drift",
+ * "mg", "step" = the whole mgp_step); returns -1 if not timed.  Timing is on when enable != 0. */
+int mgp_set_timing(mgp_ctx *ctx, int enable);
+double mgp_kernel_ms(mgp_ctx *ctx, const char *name);
+/* Process-wide number of this library's own kernel launches so far (cuFFT
+ * launches are not included). */
+long long mgp_launch_count(mgp_ctx *ctx);
+
+/* Page-lock (pin) a caller-owned host buffer for fast copies, and release it
+ * (cudaHostRegister / cudaHostUnregister). */
+int mgp_host_register(void *ptr, size_t bytes);
+int mgp_host_unregister(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

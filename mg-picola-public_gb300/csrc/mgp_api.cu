@@ -1,0 +1,686 @@
+// C ABI of the GB300 COLA library: context set-up, the PM step, the 2LPT IC
+// and particle I/O.  See include/mgpicola.h for the reference interface each
+// entry point replaces.
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "mgp_internal.h"
+#include "mgp_rng.h"
+
+static thread_local char g_err[1024] = "";
+
+extern "C" int mgp_set_error(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+extern "C" const char *mgp_last_error(void) { return g_err; }
+
+#define RET_IF(x)          \
+  do {                     \
+    int rc_ = (x);         \
+    if (rc_ != MGP_OK) return rc_; \
+  } while (0)
+
+// ----------------------------------------------------------------- timing
+static const char *k_timer_names[MGP_NTIMERS] = {"cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "step"};
+
+static void tstart(mgp_ctx *c, int t) {
+  if (c->timing) cudaEventRecord(c->ev[t][0], c->stream);
+}
+static void tstop(mgp_ctx *c, int t) {
+  if (c->timing) {
+    cudaEventRecord(c->ev[t][1], c->stream);
+    c->timed[t] = 1;
+  }
+}
+
+extern "C" int mgp_set_timing(mgp_ctx *c, int enable) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  c->timing = enable ? 1 : 0;
+  for (int t = 0; t < MGP_NTIMERS; t++) c->timed[t] = 0;
+  return MGP_OK;
+}
+
+extern "C" double mgp_kernel_ms(mgp_ctx *c, const char *name) {
+  if (!c || !name) return -1.0;
+  for (int t = 0; t < MGP_NTIMERS; t++) {
+    if (strcmp(name, k_timer_names[t]) == 0) {
+      if (!c->timed[t]) return -1.0;
+      float ms = 0.f;
+      cudaEventSynchronize(c->ev[t][1]);
+      if (cudaEventElapsedTime(&ms, c->ev[t][0], c->ev[t][1]) != cudaSuccess) return -1.0;
+      return ms;
+    }
+  }
+  return -1.0;
+}
+
+extern "C" long long mgp_launch_count(mgp_ctx *c) { return c ? mgp_kernel_launches() : -1; }
+
+// ----------------------------------------------------------- P(k) tables
+// adjust_pofk_parameters (src/compute_pofk.c:758-805) in integer k units.
+static void adjust_pofk(int N, int *nbins, int *bintype, int *sub, double *kmin, double *kmax) {
+  if (!(*bintype == 0 || *bintype == 1)) *bintype = 0;
+  if (!(*sub == 0 || *sub == 1)) *sub = 1;
+  if (*nbins <= 0) *nbins = N;
+  if (*kmax <= *kmin) {
+    if (*bintype == 0) *kmin = 0.0;
+    if (*bintype == 1) *kmin = 1.0;
+    *kmax = (double)N;
+  }
+  if (*kmin < 0.0) {
+    if (*bintype == 0) *kmin = 0.0;
+    if (*bintype == 1) *kmin = 1.0;
+  }
+  if (*bintype == 1 && *kmin == 0.0) *kmin = 1.0;
+  if (*kmax > sqrt(3.0) * (double)N) *kmax = (double)N;
+}
+
+// pofk_bin_index (src/compute_pofk.c:30-46)
+static int pofk_bin_index(double kmag, double kmin, double kmax, int nbins, int bintype) {
+  if (bintype == 0) return (int)((kmag - kmin) / (kmax - kmin) * nbins + 0.5);
+  if (bintype == 1) {
+    if (kmag <= 0.0) return -1;
+    return (int)(log(kmag / kmin) / log(kmax / kmin) * nbins + 0.5);
+  }
+  return 0;
+}
+
+// k_from_index (src/compute_pofk.c:51-64)
+static double k_from_index(int index, double kmin, double kmax, int nbins, int bintype, double box) {
+  if (bintype == 0) return (kmin + (kmax - kmin) / (double)nbins * index) * 2.0 * M_PI / box;
+  return exp(log(kmin) + log(kmax / kmin) / (double)nbins * index) * 2.0 * M_PI / box;
+}
+
+static int setup_pofk(mgp_ctx *c) {
+  const int N = c->g.N;
+  int nbins = c->p.pofk_nbins, bt = c->p.pofk_bintype, sub = c->p.pofk_subtract_shotnoise;
+  double kmin = c->p.pofk_kmin * c->p.Box / (2.0 * M_PI), kmax = c->p.pofk_kmax * c->p.Box / (2.0 * M_PI);
+  adjust_pofk(N, &nbins, &bt, &sub, &kmin, &kmax);
+  if (nbins > 12288) return mgp_set_error(MGP_EINVAL, "pofk_nbins = %d exceeds 12288", nbins);
+  c->pk_nbins = nbins;
+  c->pk_bintype = bt;
+  c->pk_sub = sub;
+  c->pk_kmin = kmin;
+  c->pk_kmax = kmax;
+  const int h = N / 2;
+  const int rkmax = 3 * h * h;
+  std::vector<int> rkb(rkmax + 1);
+  for (int rk = 0; rk <= rkmax; rk++) {
+    int nk = pofk_bin_index(sqrt((double)rk), kmin, kmax, nbins, bt);
+    rkb[rk] = (nk >= 0 && nk < nbins) ? nk : -1;
+  }
+  std::vector<float> win(h + 1);
+  for (int d = 0; d <= h; d++) {
+    double g = d == 0 ? 1.0 : sin((M_PI * d) / (double)N) / ((M_PI * d) / (double)N);
+    win[d] = (float)(1.0 / pow(g, 4.0));
+  }
+  c->pk_n = (double *)calloc(nbins, sizeof(double));
+  c->pk_k = (double *)calloc(nbins, sizeof(double));
+  c->pk_host = (double *)calloc(nbins, sizeof(double));
+  // geometric mode counts and |k| sums with the reference's weights
+  for (int d0 = 0; d0 <= h; d0++) {
+    double m0 = (d0 == 0 || d0 == h) ? 1.0 : 2.0;
+    for (int d1 = 0; d1 <= h; d1++) {
+      double m1 = (d1 == 0 || d1 == h) ? 1.0 : 2.0;
+      for (int d2 = 0; d2 <= h; d2++) {
+        int rk = d0 * d0 + d1 * d1 + d2 * d2;
+        int b = rkb[rk];
+        if (b < 0) continue;
+        double w = m0 * m1 * ((d2 == 0 || d2 == h) ? 1.0 : 2.0);
+        c->pk_n[b] += w;
+        c->pk_k[b] += w * sqrt((double)rk);
+      }
+    }
+  }
+  MGP_CUDA(cudaMalloc(&c->rk_bin, sizeof(int) * (rkmax + 1)));
+  MGP_CUDA(cudaMemcpy(c->rk_bin, rkb.data(), sizeof(int) * (rkmax + 1), cudaMemcpyHostToDevice));
+  MGP_CUDA(cudaMalloc(&c->win1d, sizeof(float) * (h + 1)));
+  MGP_CUDA(cudaMemcpy(c->win1d, win.data(), sizeof(float) * (h + 1), cudaMemcpyHostToDevice));
+  long long nb = (c->g.ncomplex + 65535) / 65536;
+  if (nb > 8192) nb = 8192;
+  if (nb < 1) nb = 1;
+  c->pk_blocks = (int)nb;
+  MGP_CUDA(cudaMalloc(&c->pk_block, sizeof(float) * (size_t)nb * nbins));
+  MGP_CUDA(cudaMalloc(&c->pk_sum, sizeof(double) * nbins));
+  return MGP_OK;
+}
+
+// ------------------------------------------------------------- lifecycle
+static int make_plans(mgp_ctx *c) {
+  const int N = c->g.N;
+  long long n[3] = {N, N, N};
+  long long rembed[3] = {N, N, c->g.P};
+  long long cembed[3] = {N, N, c->g.NH};
+  long long rdist = c->g.nreal, cdist = c->g.ncomplex;
+  size_t ws[4] = {0, 0, 0, 0};
+  cufftHandle *plans[4] = {&c->plan_r2c_oop, &c->plan_r2c_ip, &c->plan_c2r_1, &c->plan_c2r_3};
+  for (int i = 0; i < 4; i++) {
+    MGP_CUFFT(cufftCreate(plans[i]));
+    MGP_CUFFT(cufftSetAutoAllocation(*plans[i], 0));
+  }
+  MGP_CUFFT(cufftMakePlanMany64(c->plan_r2c_oop, 3, n, rembed, 1, rdist, cembed, 1, cdist, CUFFT_R2C, 1, &ws[0]));
+  MGP_CUFFT(cufftMakePlanMany64(c->plan_r2c_ip, 3, n, rembed, 1, rdist, cembed, 1, cdist, CUFFT_R2C, 1, &ws[1]));
+  MGP_CUFFT(cufftMakePlanMany64(c->plan_c2r_1, 3, n, cembed, 1, cdist, rembed, 1, rdist, CUFFT_C2R, 1, &ws[2]));
+  MGP_CUFFT(cufftMakePlanMany64(c->plan_c2r_3, 3, n, cembed, 1, cdist, rembed, 1, rdist, CUFFT_C2R, 3, &ws[3]));
+  size_t w = 0;
+  for (int i = 0; i < 4; i++) w = ws[i] > w ? ws[i] : w;
+  c->fft_work_bytes = w;
+  if (w) MGP_CUDA(cudaMalloc(&c->fft_work, w));
+  for (int i = 0; i < 4; i++) {
+    MGP_CUFFT(cufftSetWorkArea(*plans[i], c->fft_work));
+    MGP_CUFFT(cufftSetStream(*plans[i], c->stream));
+  }
+  return MGP_OK;
+}
+
+static int needs_mg1(const mgp_params *p) {
+  if (!p->modified_gravity_active) return 0;
+  if ((p->model == MGP_MODEL_FOFR || p->model == MGP_MODEL_MBETA)) return 1;
+  if (p->model == MGP_MODEL_DGP && p->include_screening) return 1;
+  return 0;
+}
+
+static int validate(const mgp_params *p) {
+  if (p->Nmesh < 4 || p->Nmesh % 2) return mgp_set_error(MGP_EINVAL, "Nmesh = %d must be even and >= 4", p->Nmesh);
+  if (p->Nmesh > 4096) return mgp_set_error(MGP_EINVAL, "Nmesh = %d exceeds 4096", p->Nmesh);
+  if (p->Nsample < 1 || p->Nsample > 2048) return mgp_set_error(MGP_EINVAL, "Nsample = %d out of range", p->Nsample);
+  if (!(p->Box > 0)) return mgp_set_error(MGP_EINVAL, "Box must be positive");
+  if (p->model < 0 || p->model > 4) return mgp_set_error(MGP_EINVAL, "unknown model %d", p->model);
+  if (p->model == MGP_MODEL_MBETA && p->modified_gravity_active)
+    return mgp_set_error(MGP_EINVAL, "MBETA model is not available in this build");
+  if (p->model == MGP_MODEL_BRANSDICKE && p->modified_gravity_active)
+    return mgp_set_error(MGP_EINVAL, "BRANSDICKE model is not available in this build");
+  if (p->scaledependent) return mgp_set_error(MGP_EINVAL, "SCALEDEPENDENT growth is not available in this build");
+  if ((p->WhichSpectrum != 0) && (p->WhichTransfer != 0))
+    return mgp_set_error(MGP_EINVAL, "can't run with both power spectrum and transfer function");
+  if ((p->WhichSpectrum == 0) && (p->WhichTransfer == 0))
+    return mgp_set_error(MGP_EINVAL, "can't run with neither power spectrum nor transfer function");
+  return MGP_OK;
+}
+
+extern "C" int mgp_destroy(mgp_ctx *c) {
+  if (!c) return MGP_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cufftHandle plans[4] = {c->plan_r2c_oop, c->plan_r2c_ip, c->plan_c2r_1, c->plan_c2r_3};
+  for (int i = 0; i < 4; i++)
+    if (plans[i]) cufftDestroy(plans[i]);
+  void *bufs[] = {c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
+                  c->fft_work, c->rk_bin, c->win1d, c->pk_block, c->pk_sum};
+  for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
+    if (bufs[i]) cudaFree(bufs[i]);
+  for (int t = 0; t < MGP_NTIMERS; t++) {
+    if (c->ev[t][0]) cudaEventDestroy(c->ev[t][0]);
+    if (c->ev[t][1]) cudaEventDestroy(c->ev[t][1]);
+  }
+  if (c->stream) cudaStreamDestroy(c->stream);
+  free(c->pk_n);
+  free(c->pk_k);
+  free(c->pk_host);
+  mgp_cosmo_free(&c->cosmo);
+  free(c);
+  return MGP_OK;
+}
+
+extern "C" int mgp_create(const mgp_params *p, int device, mgp_ctx **out) {
+  if (!p || !out) return mgp_set_error(MGP_EINVAL, "null argument");
+  *out = NULL;
+  RET_IF(validate(p));
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+    return mgp_set_error(MGP_ECUDA, "no CUDA device available: the library has no CPU path");
+  if (device < 0 || device >= ndev) return mgp_set_error(MGP_EINVAL, "device %d out of range", device);
+  mgp_ctx *c = (mgp_ctx *)calloc(1, sizeof(mgp_ctx));
+  c->p = *p;
+  c->device = device;
+  char err[512] = "";
+  int rc = mgp_cosmo_init(&c->cosmo, p, err, sizeof(err));
+  if (rc) {
+    free(c);
+    return mgp_set_error(rc, "%s", err);
+  }
+#define TRY(x)            \
+  do {                    \
+    int r_ = (x);         \
+    if (r_ != MGP_OK) {   \
+      std::string e_ = g_err; \
+      mgp_destroy(c);     \
+      mgp_set_error(r_, "%s", e_.c_str()); \
+      return r_;          \
+    }                     \
+  } while (0)
+#define TRYCUDA(x) TRY([&]() -> int { MGP_CUDA(x); return MGP_OK; }())
+  TRYCUDA(cudaSetDevice(device));
+  TRYCUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  for (int t = 0; t < MGP_NTIMERS; t++) {
+    TRYCUDA(cudaEventCreate(&c->ev[t][0]));
+    TRYCUDA(cudaEventCreate(&c->ev[t][1]));
+  }
+  const int N = p->Nmesh;
+  c->g.N = N;
+  c->g.NH = N / 2 + 1;
+  c->g.P = 2LL * (N / 2 + 1);
+  c->g.nreal = (long long)N * N * c->g.P;
+  c->g.ncomplex = (long long)N * N * c->g.NH;
+  c->Ns = p->Nsample;
+  c->np = (long long)p->Nsample * p->Nsample * p->Nsample;
+  const size_t pbytes = sizeof(float) * 3 * (size_t)c->np;
+  TRYCUDA(cudaMalloc(&c->s, pbytes));
+  TRYCUDA(cudaMalloc(&c->v, pbytes));
+  TRYCUDA(cudaMalloc(&c->D1, pbytes));
+  TRYCUDA(cudaMalloc(&c->D2, pbytes));
+  TRYCUDA(cudaMemset(c->s, 0, pbytes));
+  TRYCUDA(cudaMemset(c->v, 0, pbytes));
+  TRYCUDA(cudaMemset(c->D1, 0, pbytes));
+  TRYCUDA(cudaMemset(c->D2, 0, pbytes));
+  TRYCUDA(cudaMalloc(&c->dstate, sizeof(mgp_dstate)));
+  TRYCUDA(cudaMemset(c->dstate, 0, sizeof(mgp_dstate)));
+  c->max_blocks = mgp_ikd_blocks(c->np) > 4096 ? mgp_ikd_blocks(c->np) : 4096;
+  TRYCUDA(cudaMalloc(&c->partials, sizeof(double) * 6 * (size_t)c->max_blocks));
+  const size_t gbytes = sizeof(float) * (size_t)c->g.nreal;
+  TRYCUDA(cudaMalloc(&c->rho, gbytes));
+  TRYCUDA(cudaMalloc(&c->dk, gbytes));
+  TRYCUDA(cudaMalloc(&c->frc, 3 * gbytes));
+  if (needs_mg1(p)) TRYCUDA(cudaMalloc(&c->mg1, gbytes));
+  TRY(make_plans(c));
+  TRY(setup_pofk(c));
+#undef TRYCUDA
+#undef TRY
+  *out = c;
+  return MGP_OK;
+}
+
+// ---------------------------------------------------------------- IC
+extern "C" int mgp_displacement_fields(mgp_ctx *c) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  MGP_CUDA(cudaSetDevice(c->device));
+  const int N = c->g.N, Ns = c->Ns, h = N / 2;
+  const double box = c->p.Box;
+  // seed table, src/2LPT.c:262-271
+  std::vector<uint32_t> seeds((size_t)N * N);
+  {
+    uint64_t n = 0;
+    uint32_t sd = (uint32_t)c->p.Seed;
+    auto draw = [&]() { return (uint32_t)(0x7fffffff * mgp_uniform(sd, n++)); };
+    for (int i = 0; i < N / 2; i++) {
+      for (int j = 0; j < i; j++) seeds[(size_t)i * N + j] = draw();
+      for (int j = 0; j < i + 1; j++) seeds[(size_t)j * N + i] = draw();
+      for (int j = 0; j < i; j++) seeds[(size_t)(N - 1 - i) * N + j] = draw();
+      for (int j = 0; j < i + 1; j++) seeds[(size_t)(N - 1 - j) * N + i] = draw();
+      for (int j = 0; j < i; j++) seeds[(size_t)i * N + (N - 1 - j)] = draw();
+      for (int j = 0; j < i + 1; j++) seeds[(size_t)j * N + (N - 1 - i)] = draw();
+      for (int j = 0; j < i; j++) seeds[(size_t)(N - 1 - i) * N + (N - 1 - j)] = draw();
+      for (int j = 0; j < i + 1; j++) seeds[(size_t)(N - 1 - j) * N + (N - 1 - i)] = draw();
+    }
+  }
+  // P(k) rescaling for MG runs whose input spectrum is LCDM (2LPT.c:323-327,
+  // 395-407); scale-independent growth, so it is one number.
+  double rescale = 1.0;
+  if (c->p.modified_gravity_active && c->p.input_pofk_is_for_lcdm) {
+    rescale *= mgp_cosmo_pofk_ratio(&c->cosmo, 1.0);
+    if (!c->p.input_sigma8_is_for_lcdm) {
+      double e = mgp_cosmo_sigma8_enh(&c->cosmo, 1.0);
+      rescale /= e * e;
+    }
+  }
+  // amplitude per integer |k|^2 (k in h/Mpc = 2 pi/Box sqrt(RK))
+  const int rkmax = 3 * h * h;
+  std::vector<double> amp(rkmax + 1);
+  for (int rk = 0; rk <= rkmax; rk++) {
+    double k = 2.0 * M_PI / box * sqrt((double)rk);
+    double pk = rk == 0 ? 0.0 : mgp_cosmo_power(&c->cosmo, k) * rescale;
+    amp[rk] = pow(box, -1.5) * sqrt(pk);
+  }
+  // cube cut of 2LPT.c:383-386 with the reference's double expression
+  std::vector<unsigned char> cut(h + 1);
+  for (int d = 0; d <= h; d++) {
+    double kv = d * 2 * 3.14159265358979323846 / box;
+    cut[d] = (fabs(kv) * box / (2 * 3.14159265358979323846) > Ns / 2) ? 1 : 0;
+  }
+  uint32_t *d_seeds = NULL;
+  double *d_amp = NULL;
+  unsigned char *d_cut = NULL;
+  float *g6 = NULL;
+  int rc = MGP_OK;
+  const long long gf = c->g.nreal;
+  const double Di = mgp_cosmo_growth(&c->cosmo, 0, 1.0 / (1.0 + c->p.Init_Redshift));
+  const double Di2 = mgp_cosmo_growth(&c->cosmo, 3, 1.0 / (1.0 + c->p.Init_Redshift));
+  const int nblk = mgp_ikd_blocks(c->np);
+#define CK(x)                      \
+  do {                             \
+    rc = (x);                      \
+    if (rc != MGP_OK) goto cleanup; \
+  } while (0)
+#define CKC(x)                                                                                           \
+  do {                                                                                                   \
+    cudaError_t e_ = (x);                                                                                \
+    if (e_ != cudaSuccess) {                                                                             \
+      rc = mgp_set_error(MGP_ECUDA, "%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_));   \
+      goto cleanup;                                                                                      \
+    }                                                                                                    \
+  } while (0)
+#define CKF(x)                                                                                         \
+  do {                                                                                                 \
+    cufftResult r_ = (x);                                                                              \
+    if (r_ != CUFFT_SUCCESS) {                                                                         \
+      rc = mgp_set_error(MGP_ECUFFT, "%s:%d %s: cufft error %d", __FILE__, __LINE__, #x, (int)r_);   \
+      goto cleanup;                                                                                    \
+    }                                                                                                  \
+  } while (0)
+  CKC(cudaMalloc(&d_seeds, sizeof(uint32_t) * seeds.size()));
+  CKC(cudaMalloc(&d_amp, sizeof(double) * amp.size()));
+  CKC(cudaMalloc(&d_cut, cut.size()));
+  // six scratch grids for the displacement gradients and the six
+  // displacement fields (2LPT.c:1214-1219, 1300-1306)
+  CKC(cudaMalloc(&g6, sizeof(float) * 6 * (size_t)gf));
+  CKC(cudaMemcpyAsync(d_seeds, seeds.data(), sizeof(uint32_t) * seeds.size(), cudaMemcpyHostToDevice, c->stream));
+  CKC(cudaMemcpyAsync(d_amp, amp.data(), sizeof(double) * amp.size(), cudaMemcpyHostToDevice, c->stream));
+  CKC(cudaMemcpyAsync(d_cut, cut.data(), cut.size(), cudaMemcpyHostToDevice, c->stream));
+  CKC(cudaMemsetAsync(c->dk, 0, sizeof(float) * (size_t)gf, c->stream));
+  CK(mgp_launch_ic_delta(d_seeds, d_amp, d_cut, N, Ns, box, c->p.amplitude_fixed_initial_condition,
+                         c->p.inverted_initial_condition, c->p.SphereMode == 1, c->dk, c->stream));
+  CK(mgp_launch_ic_grad6(c->dk, g6, gf, N, c->stream));
+  CKF(cufftExecC2R(c->plan_c2r_3, (cufftComplex *)g6, (cufftReal *)g6));
+  CKF(cufftExecC2R(c->plan_c2r_3, (cufftComplex *)(g6 + 3 * gf), (cufftReal *)(g6 + 3 * gf)));
+  CK(mgp_launch_ic_source(g6, gf, N, c->g.P, c->stream));
+  CKF(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)(g6 + 3 * gf), (cufftComplex *)(g6 + 3 * gf)));
+  CK(mgp_launch_ic_disp(c->dk, g6 + 3 * gf, g6, gf, N, box, c->stream));
+  CKF(cufftExecC2R(c->plan_c2r_3, (cufftComplex *)g6, (cufftReal *)g6));
+  CKF(cufftExecC2R(c->plan_c2r_3, (cufftComplex *)(g6 + 3 * gf), (cufftReal *)(g6 + 3 * gf)));
+  CK(mgp_launch_ic_readout(g6, gf, N, c->g.P, Ns, c->D1, c->D2, c->partials, nblk, c->stream));
+  CK(mgp_launch_ic_finish(c->D1, c->D2, c->s, c->v, c->np, c->partials, nblk, (float)Di, (float)Di2, 0.0, c->stream));
+  CKC(cudaMemsetAsync(c->dstate, 0, sizeof(mgp_dstate), c->stream));
+  CKC(cudaStreamSynchronize(c->stream));
+  c->have_density = c->have_forces = 0;
+cleanup:
+  if (d_seeds) cudaFree(d_seeds);
+  if (d_amp) cudaFree(d_amp);
+  if (d_cut) cudaFree(d_cut);
+  if (g6) cudaFree(g6);
+#undef CK
+#undef CKC
+#undef CKF
+  return rc;
+}
+
+// ------------------------------------------------------------ PM step
+static int require_particles(mgp_ctx *c) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  MGP_CUDA(cudaSetDevice(c->device));
+  return MGP_OK;
+}
+
+// MG fifth force (ComputeFifthForce, src/user_defined_functions.h:687-719 and
+// src/mg.h) given delta(x) in rho and delta(k) in dk.  Leaves the MG source
+// for the force pass in rho (as complex) and returns the fused k-space mode.
+static int fifth_force(mgp_ctx *c, double A, int *mg_kind, float *coupling, float *mass2) {
+  const mgp_params *p = &c->p;
+  const int N = c->g.N;
+  *mg_kind = 0;
+  *coupling = 0.f;
+  *mass2 = 0.f;
+  if (!p->modified_gravity_active) return MGP_OK;
+  const long long nr = c->g.nreal;
+  if (p->model == MGP_MODEL_FOFR || p->model == MGP_MODEL_MBETA) {
+    // ComputeFifthForce_PotentialScreening, src/mg.h:147-189
+    if (p->include_screening) {
+      double norm = 1.0 / pow((double)N, 3) * 1.5 * p->Omega / A * pow(p->Box / 2997.92458 / (2.0 * M_PI), 2);
+      RET_IF(mgp_launch_div_laplacian(c->dk, c->mg1, N, (float)norm, c->stream));
+      MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+      RET_IF(mgp_launch_screen_potential(c->rho, c->mg1, nr, (float)mgp_phicrit(&c->cosmo, A), c->stream));
+    }
+    MGP_CUFFT(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
+    *mg_kind = 1;
+    *coupling = (float)mgp_coupling(&c->cosmo, A);
+    *mass2 = (float)(A * A * mgp_mass2_of_a(&c->cosmo, A) / pow(2.0 * M_PI * 2997.92458 / p->Box, 2));
+  } else if (p->model == MGP_MODEL_DGP) {
+    // ComputeFifthForce_DensityScreening, src/mg.h:197-260
+    double coupling_d = mgp_coupling(&c->cosmo, A);
+    if (!p->include_screening) {
+      *mg_kind = 3;
+      *coupling = (float)coupling_d;
+      return MGP_OK;
+    }
+    double kR1 = 2.0 * M_PI / p->Box * p->Rsmooth;
+    RET_IF(mgp_launch_smooth(c->dk, c->mg1, N, p->smoothing_filter, (float)kR1, (float)(1.0 / pow((double)N, 3)),
+                             c->stream));
+    MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+    RET_IF(mgp_launch_screen_density(c->rho, c->mg1, nr, (float)coupling_d,
+                                     (float)mgp_dgp_screen_prefactor(&c->cosmo, A), c->stream));
+    MGP_CUFFT(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
+    *mg_kind = 2;
+  }
+  return MGP_OK;
+}
+
+static int pofk_now(mgp_ctx *c) {
+  RET_IF(mgp_launch_pofk(c->dk, c->g.N, c->rk_bin, c->win1d, c->pk_nbins, c->pk_block, c->pk_blocks, c->pk_sum,
+                         c->stream));
+  return MGP_OK;
+}
+
+extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
+  RET_IF(require_particles(c));
+  const int N = c->g.N;
+  // PtoMesh, src/auxPM.c:280-432
+  tstart(c, T_CIC);
+  RET_IF(mgp_launch_fill(c->rho, c->g.nreal, -1.0f, c->stream));
+  double wpar = pow((double)N / (double)c->Ns, 3);
+  RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, c->p.Box, (float)wpar, c->rho, c->g.P, c->stream));
+  tstop(c, T_CIC);
+  tstart(c, T_R2C);
+  MGP_CUFFT(cufftExecR2C(c->plan_r2c_oop, (cufftReal *)c->rho, (cufftComplex *)c->dk));
+  tstop(c, T_R2C);
+  c->have_density = 1;
+  c->last_density_a = A;
+  if (c->p.pofk_compute_every_step) {
+    tstart(c, T_POFK);
+    RET_IF(pofk_now(c));
+    tstop(c, T_POFK);
+  }
+  int mg_kind = 0;
+  float coupling = 0.f, mass2 = 0.f;
+  tstart(c, T_MG);
+  RET_IF(fifth_force(c, A, &mg_kind, &coupling, &mass2));
+  tstop(c, T_MG);
+  // Forces, src/auxPM.c:437-555
+  tstart(c, T_FORCES);
+  RET_IF(mgp_launch_forces(c->dk, c->rho, coupling, mass2, mg_kind, N, c->p.Box, c->frc, c->g.nreal, c->stream));
+  tstop(c, T_FORCES);
+  tstart(c, T_C2R);
+  MGP_CUFFT(cufftExecC2R(c->plan_c2r_3, (cufftComplex *)c->frc, (cufftReal *)c->frc));
+  tstop(c, T_C2R);
+  c->have_forces = 1;
+  return MGP_OK;
+}
+
+static void kd_args(mgp_ctx *c, double AI, double AF, double A, double AFF, int do_drift, mgp_kd_args *a) {
+  const mgp_cosmo *cs = &c->cosmo;
+  const double om = c->p.Omega, cola = c->p.UseCOLA ? 1.0 : 0.0;
+  double dda = mgp_cosmo_Sphi(cs, AI, AF, A);  // StdDA = 0 (main.c:696-697)
+  memset(a, 0, sizeof(*a));
+  a->scale = (float)(c->g.N / c->p.Box);
+  a->inv_scale = (float)(c->p.Box / c->g.N);
+  a->kick_disp = (float)(-1.5 * om * dda);
+  a->kick_d1 = (float)(-cola * mgp_cosmo_growth(cs, 2, A) / A * dda);
+  a->kick_d2 = (float)(-cola * mgp_cosmo_growth(cs, 5, A) / A * dda);
+  a->dda_omega = 1.5 * om * dda;
+  a->do_drift = do_drift;
+  if (do_drift) {
+    double dyyy = mgp_cosmo_Sq(cs, A, AFF, AF);
+    a->dyyy = (float)dyyy;
+    a->dyyy_d = dyyy;
+    a->dD1 = (float)(cola * (mgp_cosmo_growth(cs, 0, AFF) - mgp_cosmo_growth(cs, 0, A)));
+    a->dD2 = (float)(cola * (mgp_cosmo_growth(cs, 3, AFF) - mgp_cosmo_growth(cs, 3, A)));
+  }
+}
+
+extern "C" int mgp_kick_drift(mgp_ctx *c, double AI, double AF, double A, double AFF, int do_drift) {
+  RET_IF(require_particles(c));
+  if (!c->have_forces) return mgp_set_error(MGP_ESTATE, "mgp_kick_drift before mgp_get_displacements");
+  mgp_kd_args a;
+  kd_args(c, AI, AF, A, AFF, do_drift, &a);
+  int nblk = mgp_ikd_blocks(c->np);
+  tstart(c, T_IKD);
+  RET_IF(mgp_launch_ikd(c->frc, c->g.nreal, c->g.N, c->g.P, c->Ns, c->np, c->s, c->v, c->D1, c->D2, c->dstate,
+                        c->partials, nblk, &a, c->stream));
+  tstop(c, T_IKD);
+  if (do_drift) c->have_density = 0;
+  return MGP_OK;
+}
+
+extern "C" int mgp_step(mgp_ctx *c, double A, double AI, double AF, double AFF) {
+  RET_IF(require_particles(c));
+  tstart(c, T_MISC);
+  RET_IF(mgp_get_displacements(c, A));
+  RET_IF(mgp_kick_drift(c, AI, AF, A, AFF, 1));
+  tstop(c, T_MISC);
+  return MGP_OK;
+}
+
+extern "C" int mgp_pofk(mgp_ctx *c, int cap, int *nbins, double *k, double *pk, double *kmean, double *n) {
+  RET_IF(require_particles(c));
+  if (!c->have_density) return mgp_set_error(MGP_ESTATE, "no density: call mgp_get_displacements first");
+  if (!c->p.pofk_compute_every_step) RET_IF(pofk_now(c));
+  const int nb = c->pk_nbins;
+  if (nbins) *nbins = nb;
+  if (cap < nb) return mgp_set_error(MGP_EINVAL, "P(k) capacity %d < %d bins", cap, nb);
+  MGP_CUDA(cudaMemcpyAsync(c->pk_host, c->pk_sum, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
+  MGP_CUDA(cudaStreamSynchronize(c->stream));
+  const double N = c->g.N, box = c->p.Box;
+  const double norm = pow(box, 3) / pow(N, 6), shot = pow(box / (double)c->Ns, 3);
+  for (int b = 0; b < nb; b++) {
+    double P = 0.0, K = 0.0;
+    if (c->pk_n[b] > 0) {
+      P = c->pk_host[b] / c->pk_n[b] * norm;
+      if (c->pk_sub) P -= shot;
+      K = c->pk_k[b] / c->pk_n[b] * 2.0 * M_PI / box;
+    }
+    if (k) k[b] = k_from_index(b, c->pk_kmin, c->pk_kmax, nb, c->pk_bintype, box);
+    if (pk) pk[b] = P;
+    if (kmean) kmean[b] = K;
+    if (n) n[b] = c->pk_n[b];
+  }
+  return MGP_OK;
+}
+
+extern "C" int mgp_pofk_rsd(mgp_ctx *c, double A, int cap, int *nbins, double *k, double *P0, double *P2, double *P4,
+                            double *s0, double *s2, double *s4, double *n) {
+  (void)A; (void)cap; (void)nbins; (void)k; (void)P0; (void)P2; (void)P4; (void)s0; (void)s2; (void)s4; (void)n;
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  return mgp_set_error(MGP_EINVAL, "RSD multipoles are not available in this build");
+}
+
+// ---------------------------------------------------------- particles
+static int ensure_stage(mgp_ctx *c) {
+  if (!c->stage) MGP_CUDA(cudaMalloc(&c->stage, sizeof(float) * 6 * (size_t)c->np));
+  return MGP_OK;
+}
+
+extern "C" int mgp_get_particles(mgp_ctx *c, float *pos, float *vel, float *D1, float *D2, size_t np) {
+  RET_IF(require_particles(c));
+  if ((long long)np != c->np) return mgp_set_error(MGP_EINVAL, "np = %zu, context holds %lld", np, c->np);
+  RET_IF(ensure_stage(c));
+  const size_t bytes = sizeof(float) * 3 * np;
+  float *dpos = c->stage, *dvel = c->stage + 3 * np;
+  if (pos || vel) {
+    RET_IF(mgp_launch_positions(c->s, c->dstate, c->np, c->Ns, c->p.Box, pos ? dpos : NULL, vel ? dvel : NULL, c->v,
+                                c->stream));
+    if (pos) MGP_CUDA(cudaMemcpyAsync(pos, dpos, bytes, cudaMemcpyDeviceToHost, c->stream));
+    if (vel) MGP_CUDA(cudaMemcpyAsync(vel, dvel, bytes, cudaMemcpyDeviceToHost, c->stream));
+  }
+  MGP_CUDA(cudaStreamSynchronize(c->stream));
+  // D1/D2 SoA -> AoS on the host
+  const float *srcs[2] = {c->D1, c->D2};
+  float *dsts[2] = {D1, D2};
+  std::vector<float> h;
+  for (int q = 0; q < 2; q++) {
+    if (!dsts[q]) continue;
+    h.resize(3 * np);
+    MGP_CUDA(cudaMemcpy(h.data(), srcs[q], bytes, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < np; i++)
+      for (int a = 0; a < 3; a++) dsts[q][3 * i + a] = h[a * np + i];
+  }
+  return MGP_OK;
+}
+
+extern "C" int mgp_set_particles(mgp_ctx *c, const float *pos, const float *vel, const float *D1, const float *D2,
+                                 size_t np) {
+  RET_IF(require_particles(c));
+  if ((long long)np != c->np) return mgp_set_error(MGP_EINVAL, "np = %zu, context holds %lld", np, c->np);
+  RET_IF(ensure_stage(c));
+  const size_t bytes = sizeof(float) * 3 * np;
+  float *a = c->stage, *b = c->stage + 3 * np;
+  if (pos) MGP_CUDA(cudaMemcpyAsync(a, pos, bytes, cudaMemcpyHostToDevice, c->stream));
+  if (vel) MGP_CUDA(cudaMemcpyAsync(b, vel, bytes, cudaMemcpyHostToDevice, c->stream));
+  if (pos || vel) {
+    RET_IF(mgp_launch_set_state(c->s, c->v, pos ? a : NULL, vel ? b : NULL, c->np, c->Ns, c->p.Box, c->stream));
+    // absolute state: offsets restart from zero
+    MGP_CUDA(cudaMemsetAsync(c->dstate, 0, sizeof(mgp_dstate), c->stream));
+  }
+  const float *srcs[2] = {D1, D2};
+  float *dsts[2] = {c->D1, c->D2};
+  for (int q = 0; q < 2; q++) {
+    if (!srcs[q]) continue;
+    float *st = q == 0 ? a : b;
+    MGP_CUDA(cudaMemcpyAsync(st, srcs[q], bytes, cudaMemcpyHostToDevice, c->stream));
+    RET_IF(mgp_launch_aos_to_soa(st, dsts[q], c->np, c->stream));
+  }
+  MGP_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_density = c->have_forces = 0;
+  return MGP_OK;
+}
+
+extern "C" int mgp_host_register(void *ptr, size_t bytes) {
+  MGP_CUDA(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  return MGP_OK;
+}
+
+extern "C" int mgp_host_unregister(void *ptr) {
+  MGP_CUDA(cudaHostUnregister(ptr));
+  return MGP_OK;
+}
+
+extern "C" int mgp_step_host(mgp_ctx *c, double A, double AI, double AF, double AFF, float *pos, float *vel,
+                             const float *D1, const float *D2, size_t np) {
+  RET_IF(mgp_set_particles(c, pos, vel, D1, D2, np));
+  RET_IF(mgp_step(c, A, AI, AF, AFF));
+  RET_IF(mgp_get_particles(c, pos, vel, NULL, NULL, np));
+  return MGP_OK;
+}
+
+extern "C" int mgp_copy_grid(mgp_ctx *c, int which, float *host, size_t count) {
+  RET_IF(require_particles(c));
+  const float *src = NULL;
+  switch (which) {
+    case 0: src = c->rho; break;
+    case 1: src = c->dk; break;
+    case 2: case 3: case 4: src = c->frc + (which - 2) * c->g.nreal; break;
+    case 5: src = c->rho; break;
+    case 6: src = c->mg1; break;
+    default: return mgp_set_error(MGP_EINVAL, "unknown grid %d", which);
+  }
+  if (!src) return mgp_set_error(MGP_ESTATE, "grid %d is not allocated", which);
+  if ((long long)count > c->g.nreal) return mgp_set_error(MGP_EINVAL, "count %zu exceeds grid size", count);
+  MGP_CUDA(cudaStreamSynchronize(c->stream));
+  MGP_CUDA(cudaMemcpy(host, src, sizeof(float) * count, cudaMemcpyDeviceToHost));
+  return MGP_OK;
+}
+
+extern "C" double mgp_growth(mgp_ctx *c, int which, double a) { return c ? mgp_cosmo_growth(&c->cosmo, which, a) : NAN; }
+extern "C" double mgp_Sq(mgp_ctx *c, double ai, double af, double aref) { return c ? mgp_cosmo_Sq(&c->cosmo, ai, af, aref) : NAN; }
+extern "C" double mgp_Sphi(mgp_ctx *c, double ai, double af, double aref) { return c ? mgp_cosmo_Sphi(&c->cosmo, ai, af, aref) : NAN; }
+extern "C" double mgp_power_spectrum(mgp_ctx *c, double k) { return c ? mgp_cosmo_power(&c->cosmo, k) : NAN; }

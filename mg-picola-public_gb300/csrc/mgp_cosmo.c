@@ -1,0 +1,503 @@
+/*
+ * Host FP64 cosmology for the GB300 COLA library.
+ *
+ * Growth factors: the coupled first/second-order growth ODEs of
+ * src/cosmo.c:206-268 in x = ln a, from z = max(200, z_init) to z = -0.5,
+ * stored at 1000 knots and interpolated by natural cubic splines with clamped
+ * lookup (src/cosmo.c:409-520, src/wrappers.c:102-167).  The reference uses
+ * GSL's rk2 driver at eps 1e-7; here an adaptive Dormand-Prince 5(4) pair
+ * (J. R. Dormand, P. J. Prince, J. Comp. Appl. Math. 6 (1980) 19) at a
+ * relative tolerance of 1e-11 integrates between knots.
+ *
+ * Quadratures (COLA Sq, sigma_8 normalisation) use adaptive 16-point
+ * Gauss-Legendre bisection; nodes are computed by Newton iteration on the
+ * Legendre polynomial.
+ */
+#include "mgp_cosmo.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define INVERSE_H0_MPCH 2997.92458 /* 1/H0 in Mpc/h, src/vars.h:65 */
+
+int mgp_set_error(int code, const char *fmt, ...);
+
+/* ------------------------------------------------------------------ hooks */
+double mgp_hubble(const mgp_cosmo *c, double a) {
+  const double om = c->p.Omega;
+  if (c->p.use_w0wa)
+    return sqrt(om / (a * a * a) + (1.0 - om) * exp(3.0 * c->p.w_a * (a - 1) - 3 * (1 + c->p.w_0 + c->p.w_a) * log(a)));
+  return sqrt(om / (a * a * a) + 1.0 - om);
+}
+
+double mgp_dhubbleda(const mgp_cosmo *c, double a) {
+  const double om = c->p.Omega;
+  double rhs = -3.0 * om / (a * a * a * a);
+  if (c->p.use_w0wa) rhs += -3.0 * (1.0 - om) * (1.0 + c->p.w_0 + c->p.w_a * (1 - a)) / a;
+  return rhs / (2.0 * mgp_hubble(c, a));
+}
+
+double mgp_beta_dgp(const mgp_cosmo *c, double a) {
+  return 1.0 + 2.0 * c->p.rcH0_DGP * (mgp_hubble(c, a) + a * mgp_dhubbleda(c, a) / 3.0);
+}
+
+double mgp_beta_of_a(const mgp_cosmo *c, double a) {
+  switch (c->p.model) {
+    case MGP_MODEL_FOFR: return 1.0 / sqrt(6.0);
+    case MGP_MODEL_MBETA: {
+      double r = c->p.assb_symm / a;
+      return a > c->p.assb_symm ? c->p.beta_symm * sqrt(1.0 - r * r * r) : 0.0;
+    }
+    default: return 0.0;
+  }
+}
+
+double mgp_mass2_of_a(const mgp_cosmo *c, double a) {
+  if (c->p.model == MGP_MODEL_FOFR) {
+    const double om = c->p.Omega, n = c->p.nfofr;
+    double fac = om / (a * a * a) + 4.0 * (1.0 - om);
+    double fac0 = om + 4.0 * (1.0 - om);
+    return fac0 * pow(fac / fac0, n + 2.0) / ((1.0 + n) * c->p.fofr0);
+  }
+  if (c->p.model == MGP_MODEL_MBETA) {
+    double r = c->p.assb_symm / a;
+    if (a > c->p.assb_symm) return 0.5 * pow(2998.0 / c->p.range_symm, 2) * (1.0 - r * r * r);
+    return 1.0;
+  }
+  return 0.0;
+}
+
+double mgp_coupling(const mgp_cosmo *c, double a) {
+  switch (c->p.model) {
+    case MGP_MODEL_FOFR:
+    case MGP_MODEL_MBETA: {
+      double b = mgp_beta_of_a(c, a);
+      return 2.0 * b * b;
+    }
+    case MGP_MODEL_DGP: return 1.0 / (3.0 * mgp_beta_dgp(c, a));
+    default: return 0.0;
+  }
+}
+
+double mgp_geff(const mgp_cosmo *c, double a, double k) {
+  if (!c->p.modified_gravity_active || c->p.use_lcdm_growth_factors) return 1.0;
+  switch (c->p.model) {
+    case MGP_MODEL_FOFR:
+    case MGP_MODEL_MBETA: {
+      double k2 = (k * INVERSE_H0_MPCH) * (k * INVERSE_H0_MPCH);
+      if (k2 == 0) return 1.0;
+      double b = mgp_beta_of_a(c, a);
+      return 1.0 + 2.0 * b * b * k2 / (k2 + a * a * mgp_mass2_of_a(c, a));
+    }
+    case MGP_MODEL_DGP: return 1.0 + 1.0 / (3.0 * mgp_beta_dgp(c, a));
+    default: return 1.0;
+  }
+}
+
+double mgp_factor_2lpt(const mgp_cosmo *c, double a) {
+  if (!c->p.modified_gravity_active || c->p.use_lcdm_growth_factors) return 1.0;
+  if (c->p.model == MGP_MODEL_DGP) {
+    double b = mgp_beta_dgp(c, a), r = c->p.rcH0_DGP;
+    return 1.0 - (2.0 * r * r * c->p.Omega) / (9.0 * a * a * a * b * b * b * (1 + 1.0 / (3.0 * b)));
+  }
+  return 1.0;
+}
+
+double mgp_phicrit(const mgp_cosmo *c, double a) {
+  const double om = c->p.Omega;
+  return 1.5 * c->p.fofr0 * pow((om + 4.0 * (1.0 - om)) / (om / (a * a * a) + 4.0 * (1.0 - om)), c->p.nfofr + 1.0);
+}
+
+double mgp_dgp_screen_prefactor(const mgp_cosmo *c, double a) {
+  double r = c->p.rcH0_DGP / mgp_beta_dgp(c, a);
+  return 8.0 / 9.0 * c->p.Omega * r * r;
+}
+
+/* ---------------------------------------------------------------- splines */
+static void spline_init(mgp_spline *s, const double *x, const double *y, int n) {
+  s->n = n;
+  s->x = (double *)malloc(sizeof(double) * n);
+  s->y = (double *)malloc(sizeof(double) * n);
+  s->y2 = (double *)calloc(n, sizeof(double));
+  double *u = (double *)calloc(n, sizeof(double));
+  memcpy(s->x, x, sizeof(double) * n);
+  memcpy(s->y, y, sizeof(double) * n);
+  for (int i = 1; i + 1 < n; i++) {
+    double sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+    double pp = sig * s->y2[i - 1] + 2.0;
+    double d = (y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]);
+    s->y2[i] = (sig - 1.0) / pp;
+    u[i] = (6.0 * d / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / pp;
+  }
+  for (int k = n - 2; k >= 0; k--) s->y2[k] = s->y2[k] * s->y2[k + 1] + u[k];
+  free(u);
+}
+
+static double spline_eval(const mgp_spline *s, double x) {
+  if (x < s->x[0]) x = s->x[0];
+  if (x > s->x[s->n - 1]) x = s->x[s->n - 1];
+  int lo = 0, hi = s->n - 1;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (s->x[mid] > x) hi = mid; else lo = mid;
+  }
+  double h = s->x[hi] - s->x[lo], A = (s->x[hi] - x) / h, B = 1.0 - A;
+  return A * s->y[lo] + B * s->y[hi] + ((A * A * A - A) * s->y2[lo] + (B * B * B - B) * s->y2[hi]) * h * h / 6.0;
+}
+
+static void spline_free(mgp_spline *s) {
+  free(s->x); free(s->y); free(s->y2);
+  memset(s, 0, sizeof(*s));
+}
+
+/* ------------------------------------------------------------- quadrature */
+static double gx[8], gw[8];
+static int g_ready = 0;
+static void gl16_init(void) {
+  if (g_ready) return;
+  for (int i = 0; i < 8; i++) {
+    double x = cos(M_PI * (i + 0.75) / 16.5), dp = 1.0;
+    for (int it = 0; it < 50; it++) {
+      double p0 = 1.0, p1 = x;
+      for (int n = 2; n <= 16; n++) { double p2 = ((2 * n - 1) * x * p1 - (n - 1) * p0) / n; p0 = p1; p1 = p2; }
+      dp = 16 * (x * p1 - p0) / (x * x - 1.0);
+      double dx = p1 / dp;
+      x -= dx;
+      if (fabs(dx) < 1e-16) break;
+    }
+    gx[i] = x;
+    gw[i] = 2.0 / ((1.0 - x * x) * dp * dp);
+  }
+  g_ready = 1;
+}
+typedef double (*qfn)(double, const void *);
+static double gl16(qfn f, const void *par, double a, double b) {
+  double m = 0.5 * (a + b), h = 0.5 * (b - a), s = 0.0;
+  for (int i = 0; i < 8; i++) s += gw[i] * (f(m - h * gx[i], par) + f(m + h * gx[i], par));
+  return s * h;
+}
+static double qadapt(qfn f, const void *par, double a, double b, double whole, double tol, int depth) {
+  double m = 0.5 * (a + b), l = gl16(f, par, a, m), r = gl16(f, par, m, b);
+  if (depth >= 18 || fabs(l + r - whole) <= tol) return l + r;
+  return qadapt(f, par, a, m, l, 0.5 * tol, depth + 1) + qadapt(f, par, m, b, r, 0.5 * tol, depth + 1);
+}
+static double quad(qfn f, const void *par, double a, double b, int panels) {
+  gl16_init();
+  double tot = 0.0, s = 0.0;
+  double *est = (double *)malloc(sizeof(double) * panels);
+  for (int i = 0; i < panels; i++) {
+    est[i] = gl16(f, par, a + (b - a) * i / panels, a + (b - a) * (i + 1) / panels);
+    tot += fabs(est[i]);
+  }
+  double tol = 1e-13 * tot / panels + 1e-300;
+  for (int i = 0; i < panels; i++)
+    s += qadapt(f, par, a + (b - a) * i / panels, a + (b - a) * (i + 1) / panels, est[i], tol, 0);
+  free(est);
+  return s;
+}
+
+/* ------------------------------------------------------------ growth ODE */
+typedef struct { const mgp_cosmo *c; int lcdm; } ode_par;
+
+static void growth_rhs(const ode_par *op, double x, const double *y, double *f) {
+  const mgp_cosmo *c = op->c;
+  double a = exp(x), H = mgp_hubble(c, a), dH = mgp_dhubbleda(c, a);
+  double mu = op->lcdm ? 1.0 : mgp_geff(c, a, 1e-3);
+  double beta = 1.5 * c->p.Omega * mu / (a * a * a * H * H);
+  double alpha = 2.0 + a * dH / H;
+  double mod = op->lcdm ? 1.0 : mgp_factor_2lpt(c, a);
+  f[0] = y[1];
+  f[1] = -alpha * y[1] + beta * y[0];
+  f[2] = y[3];
+  f[3] = -alpha * y[3] + beta * (y[2] - mod * y[0] * y[0]);
+}
+
+/* Dormand-Prince 5(4) coefficients (Dormand & Prince 1980, Table 2). */
+static const double DP_C[7] = {0, 1.0 / 5, 3.0 / 10, 4.0 / 5, 8.0 / 9, 1, 1};
+static const double DP_A[7][6] = {
+    {0, 0, 0, 0, 0, 0},
+    {1.0 / 5, 0, 0, 0, 0, 0},
+    {3.0 / 40, 9.0 / 40, 0, 0, 0, 0},
+    {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0, 0},
+    {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0, 0},
+    {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656, 0},
+    {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84}};
+static const double DP_B5[7] = {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84, 0};
+static const double DP_B4[7] = {5179.0 / 57600, 0, 7571.0 / 16695, 393.0 / 640, -92097.0 / 339200, 187.0 / 2100, 1.0 / 40};
+
+/* Integrate y from x0 to x1 (adaptive); returns 0 on success. */
+static int dp45(const ode_par *op, double x0, double x1, double *y, double *hguess) {
+  double x = x0, h = *hguess;
+  int steps = 0;
+  while (x < x1) {
+    if (x + h > x1) h = x1 - x;
+    double k[7][4], yt[4], y5[4], err = 0.0;
+    for (int s = 0; s < 7; s++) {
+      for (int i = 0; i < 4; i++) {
+        double acc = y[i];
+        for (int j = 0; j < s; j++) acc += h * DP_A[s][j] * k[j][i];
+        yt[i] = acc;
+      }
+      growth_rhs(op, x + DP_C[s] * h, yt, k[s]);
+    }
+    for (int i = 0; i < 4; i++) {
+      double s5 = y[i], s4 = y[i];
+      for (int s = 0; s < 7; s++) { s5 += h * DP_B5[s] * k[s][i]; s4 += h * DP_B4[s] * k[s][i]; }
+      y5[i] = s5;
+      double sc = 1e-11 * (fabs(y[i]) > fabs(s5) ? fabs(y[i]) : fabs(s5)) + 1e-14;
+      double e = fabs(s5 - s4) / sc;
+      if (e > err) err = e;
+    }
+    if (err <= 1.0) {
+      x += h;
+      memcpy(y, y5, sizeof(y5));
+    }
+    double fac = err > 0 ? 0.9 * pow(err, -0.2) : 5.0;
+    if (fac > 5.0) fac = 5.0;
+    if (fac < 0.2) fac = 0.2;
+    h *= fac;
+    if (++steps > 10000000 || !(h > 1e-14)) return -1;
+  }
+  *hguess = h;
+  return 0;
+}
+
+static double Qfactor(const mgp_cosmo *c, double a) { return mgp_hubble(c, a) * a * a * a; }
+
+static int solve_growth(mgp_cosmo *c, char *err, size_t errlen) {
+  const int npts = 1000;
+  double zini = c->p.Init_Redshift > 200.0 ? c->p.Init_Redshift : 200.0;
+  double xini = log(1.0 / (1.0 + zini)), xend = log(1.0 / (1.0 - 0.5));
+  double dx = (xend - xini) / (double)(npts - 1);
+  double *buf = (double *)malloc(sizeof(double) * npts * 13);
+  double *x = buf, *v[12];
+  for (int i = 0; i < 12; i++) v[i] = buf + npts * (i + 1);
+  double y[4] = {1.0, 1.0, -3.0 / 7.0, -6.0 / 7.0}, yl[4] = {1.0, 1.0, -3.0 / 7.0, -6.0 / 7.0};
+  double h = 1e-4, hl = 1e-4;
+  ode_par op = {c, 0}, opl = {c, 1};
+  for (int i = 0; i < npts; i++) {
+    double xn = xini + i * dx;
+    if (i > 0) {
+      if (dp45(&op, xini + (i - 1) * dx, xn, y, &h) || dp45(&opl, xini + (i - 1) * dx, xn, yl, &hl)) {
+        snprintf(err, errlen, "growth ODE integration failed at x = %f", xn);
+        free(buf);
+        return MGP_ENUMERIC;
+      }
+    }
+    double a = exp(xn), mu = mgp_geff(c, a, 1e-3), qa = Qfactor(c, a) / a, om = c->p.Omega;
+    x[i] = xn;
+    v[0][i] = y[0];
+    v[1][i] = y[1] * qa;
+    v[2][i] = 1.5 * mu * om * a * y[0];
+    v[3][i] = y[2];
+    v[4][i] = y[3] * qa;
+    v[5][i] = 1.5 * mu * om * a * (y[2] - y[0] * y[0] * mgp_factor_2lpt(c, a));
+    v[6][i] = yl[0];
+    v[7][i] = yl[1] * qa;
+    v[8][i] = 1.5 * om * a * yl[0];
+    v[9][i] = yl[2];
+    v[10][i] = yl[3] * qa;
+    v[11][i] = 1.5 * om * a * (yl[2] - yl[0] * yl[0]);
+  }
+  mgp_spline *sp[12] = {&c->D, &c->dDdy, &c->ddDddy, &c->D2, &c->dD2dy, &c->ddD2ddy,
+                        &c->DL, &c->dDLdy, &c->ddDLddy, &c->D2L, &c->dD2Ldy, &c->ddD2Lddy};
+  for (int i = 0; i < 12; i++) spline_init(sp[i], x, v[i], npts);
+  free(buf);
+  return MGP_OK;
+}
+
+double mgp_cosmo_growth(const mgp_cosmo *c, int which, double a) {
+  double la = log(a);
+  switch (which) {
+    case 0: return spline_eval(&c->D, la) / spline_eval(&c->D, 0.0);
+    case 1: return spline_eval(&c->dDdy, la) / spline_eval(&c->D, 0.0);
+    case 2: return spline_eval(&c->ddDddy, la) / spline_eval(&c->D, 0.0);
+    case 3: return spline_eval(&c->D2, la) / spline_eval(&c->D2, 0.0);
+    case 4: return spline_eval(&c->dD2dy, la) / spline_eval(&c->D2, 0.0);
+    case 5: return spline_eval(&c->ddD2ddy, la) / spline_eval(&c->D2, 0.0);
+    case 6: return spline_eval(&c->DL, la) / spline_eval(&c->DL, 0.0);
+    default: return NAN;
+  }
+}
+
+/* COLA: gpQ(a) = a^nLPT with nLPT = -2.5 and fullT = 1 (src/main.c:82-85,
+ * src/cosmo.c:1114-1160). */
+static double sq_integrand(double a, const void *par) {
+  return pow(a, -2.5) / Qfactor((const mgp_cosmo *)par, a);
+}
+double mgp_cosmo_Sq(const mgp_cosmo *c, double ai, double af, double aref) {
+  return quad(sq_integrand, c, ai, af, 4) / pow(aref, -2.5);
+}
+double mgp_cosmo_Sphi(const mgp_cosmo *c, double ai, double af, double aref) {
+  return (pow(af, -2.5) - pow(ai, -2.5)) * aref / Qfactor(c, aref) / (-2.5 * pow(aref, -3.5));
+}
+
+/* -------------------------------------------------------- power spectrum */
+/* Eisenstein & Hu no-wiggle transfer function (src/power.c:447-476). */
+static double transfer_eh(const mgp_cosmo *c, double k) {
+  const double h = c->p.HubbleParam, om = c->p.Omega;
+  double ombh2 = c->p.OmegaBaryon * h * h;
+  if (c->p.OmegaBaryon == 0) ombh2 = 0.04 * h * h;
+  k *= 3.085678e24 / c->p.UnitLength_in_cm;
+  double theta = 2.728 / 2.7, ommh2 = om * h * h;
+  double s = 44.5 * log(9.83 / ommh2) / sqrt(1. + 10. * exp(0.75 * log(ombh2))) * h;
+  double fb = ombh2 / ommh2;
+  double alpha = 1. - 0.328 * log(431. * ommh2) * fb + 0.380 * log(22.3 * ommh2) * fb * fb;
+  double gamma = (alpha + (1. - alpha) / (1. + exp(4 * log(0.43 * k * s)))) * om * h;
+  double q = k * theta * theta / gamma;
+  double L0 = log(2. * exp(1.) + 1.8 * q), C0 = 14.2 + 731. / (1. + 62.5 * q);
+  return L0 / (L0 + C0 * q * q);
+}
+
+static double table_interp(const mgp_cosmo *c, double k) {
+  double lk = log10(k * (c->p.InputSpectrum_UnitLength_in_cm / c->p.UnitLength_in_cm));
+  if (c->ntab < 2 || lk < c->tab_logk[0] || lk > c->tab_logk[c->ntab - 1]) return 0.0;
+  int lo = 0, hi = c->ntab - 1;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (lk < c->tab_logk[mid]) hi = mid; else lo = mid;
+  }
+  double u = (lk - c->tab_logk[lo]) / (c->tab_logk[hi] - c->tab_logk[lo]);
+  return pow(10.0, (1 - u) * c->tab_logv[lo] + u * c->tab_logv[hi]);
+}
+
+double mgp_cosmo_power(const mgp_cosmo *c, double k) {
+  switch (c->p.WhichSpectrum) {
+    case 0: {
+      double T = c->p.WhichTransfer == 1 ? table_interp(c, k) : transfer_eh(c, k);
+      return c->norm * pow(k, c->p.PrimordialIndex) * T * T;
+    }
+    case 1: return c->norm * table_interp(c, k);
+    default: {
+      double T = transfer_eh(c, k);
+      return c->norm * pow(k, c->p.PrimordialIndex) * T * T;
+    }
+  }
+}
+
+typedef struct { const mgp_cosmo *c; double R; } th_par;
+static double sigma2_integrand(double k, const void *v) {
+  const th_par *t = (const th_par *)v;
+  double kr = t->R * k;
+  if (kr < 1e-8) return 0.0;
+  double w = 3 * (sin(kr) / (kr * kr * kr) - cos(kr) / (kr * kr));
+  return k * k * w * w * mgp_cosmo_power(t->c, k);
+}
+
+static int read_table(mgp_cosmo *c, const char *fname, int transfer, char *err, size_t errlen) {
+  FILE *fd = fopen(fname, "r");
+  if (!fd) {
+    snprintf(err, errlen, "can't read input %s in file '%s'", transfer ? "transfer function" : "power spectrum", fname);
+    return MGP_EIO;
+  }
+  int cap = 1024, n = 0;
+  double *lk = (double *)malloc(sizeof(double) * cap), *lv = (double *)malloc(sizeof(double) * cap);
+  double k, v;
+  while (fscanf(fd, " %lg %lg ", &k, &v) == 2) {
+    if (n == cap) {
+      cap *= 2;
+      lk = (double *)realloc(lk, sizeof(double) * cap);
+      lv = (double *)realloc(lv, sizeof(double) * cap);
+    }
+    lk[n] = log10(k);
+    lv[n] = log10(v);
+    n++;
+  }
+  fclose(fd);
+  /* insertion sort by log k (src/power.c:337, 125) */
+  for (int i = 1; i < n; i++) {
+    double a = lk[i], b = lv[i];
+    int j = i - 1;
+    while (j >= 0 && lk[j] > a) { lk[j + 1] = lk[j]; lv[j + 1] = lv[j]; j--; }
+    lk[j + 1] = a;
+    lv[j + 1] = b;
+  }
+  if (transfer && n > 0) {
+    double t0 = lv[0];
+    for (int i = 0; i < n; i++) lv[i] -= t0; /* src/power.c:144-145 */
+  }
+  if (n < 2) {
+    snprintf(err, errlen, "table '%s' has fewer than two rows", fname);
+    free(lk); free(lv);
+    return MGP_EIO;
+  }
+  c->ntab = n;
+  c->tab_logk = lk;
+  c->tab_logv = lv;
+  return MGP_OK;
+}
+
+double mgp_cosmo_pofk_ratio(const mgp_cosmo *c, double a) {
+  if (!c->p.modified_gravity_active) return 1.0;
+  double r = spline_eval(&c->D, log(a)) / spline_eval(&c->DL, log(a));
+  return r * r;
+}
+double mgp_cosmo_sigma8_enh(const mgp_cosmo *c, double a) {
+  if (!c->p.modified_gravity_active) return 1.0;
+  return spline_eval(&c->D, log(a)) / spline_eval(&c->DL, log(a));
+}
+
+int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen) {
+  memset(c, 0, sizeof(*c));
+  c->p = *p;
+  int rc;
+  if (p->WhichSpectrum == 1) {
+    if ((rc = read_table(c, p->FileWithInputSpectrum, 0, err, errlen))) return rc;
+  } else if (p->WhichSpectrum == 0 && p->WhichTransfer == 1) {
+    if ((rc = read_table(c, p->FileWithInputTransfer, 1, err, errlen))) return rc;
+  }
+  /* Norm = sigma8^2 / sigma^2(R8) (src/power.c:226-257) */
+  c->norm = 1.0;
+  th_par t = {c, 8.0 * (3.085678e24 / p->UnitLength_in_cm)};
+  double s2 = quad(sigma2_integrand, &t, 0.0, 500.0 / t.R, 256) / (2.0 * M_PI * M_PI);
+  if (!(s2 > 0)) {
+    snprintf(err, errlen, "sigma8 normalisation integral is not positive (%g)", s2);
+    return MGP_ENUMERIC;
+  }
+  c->norm = p->Sigma8 * p->Sigma8 / s2;
+  return solve_growth(c, err, errlen);
+}
+
+void mgp_cosmo_free(mgp_cosmo *c) {
+  mgp_spline *sp[12] = {&c->D, &c->dDdy, &c->ddDddy, &c->D2, &c->dD2dy, &c->ddD2ddy,
+                        &c->DL, &c->dDLdy, &c->ddDLddy, &c->D2L, &c->dD2Ldy, &c->ddD2Lddy};
+  for (int i = 0; i < 12; i++)
+    if (sp[i]->x) spline_free(sp[i]);
+  free(c->tab_logk);
+  free(c->tab_logv);
+  c->tab_logk = c->tab_logv = NULL;
+}
+
+/* Host-only evaluation of the cosmology of a parameter set (no GPU needed):
+ * which 0-6 as mgp_growth, 7 the linear power spectrum P(x) (x = k in h/Mpc).
+ * Sq/Sphi are available through mgp_cosmo_coeff. */
+int mgp_cosmo_eval(const mgp_params *p, int which, const double *x, int n, double *out) {
+  char err[512] = "";
+  mgp_cosmo c;
+  int rc = mgp_cosmo_init(&c, p, err, sizeof(err));
+  if (rc) {
+    mgp_cosmo_free(&c);
+    return mgp_set_error(rc, "%s", err);
+  }
+  for (int i = 0; i < n; i++) out[i] = which == 7 ? mgp_cosmo_power(&c, x[i]) : mgp_cosmo_growth(&c, which, x[i]);
+  mgp_cosmo_free(&c);
+  return MGP_OK;
+}
+
+/* COLA coefficients for triples (ai, af, aref): kind 0 Sq, 1 Sphi. */
+int mgp_cosmo_coeff(const mgp_params *p, int kind, const double *ai, const double *af, const double *aref, int n,
+                    double *out) {
+  char err[512] = "";
+  mgp_cosmo c;
+  int rc = mgp_cosmo_init(&c, p, err, sizeof(err));
+  if (rc) {
+    mgp_cosmo_free(&c);
+    return mgp_set_error(rc, "%s", err);
+  }
+  for (int i = 0; i < n; i++)
+    out[i] = kind == 0 ? mgp_cosmo_Sq(&c, ai[i], af[i], aref[i]) : mgp_cosmo_Sphi(&c, ai[i], af[i], aref[i]);
+  mgp_cosmo_free(&c);
+  return MGP_OK;
+}

@@ -1,0 +1,63 @@
+/*
+ * Host FP64 cosmology of the GB300 library: model hooks, growth factors,
+ * COLA time-step coefficients and the linear power spectrum.  Everything here
+ * runs on the host in double precision; kernels receive per-step scalars.
+ */
+#ifndef MGP_COSMO_H
+#define MGP_COSMO_H
+#include "mgpicola.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  int n;
+  double *x, *y, *y2;
+} mgp_spline;
+
+typedef struct mgp_cosmo {
+  mgp_params p;
+  /* growth splines over x = ln a (src/cosmo.c:54-95) */
+  mgp_spline D, dDdy, ddDddy, D2, dD2dy, ddD2ddy;
+  mgp_spline DL, dDLdy, ddDLddy, D2L, dD2Ldy, ddD2Lddy;
+  /* power spectrum */
+  double norm;
+  int ntab;
+  double *tab_logk, *tab_logv; /* log10 k and log10 P (or T) */
+} mgp_cosmo;
+
+int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen);
+void mgp_cosmo_free(mgp_cosmo *c);
+
+/* hooks, src/user_defined_functions.h:413-904 */
+double mgp_hubble(const mgp_cosmo *c, double a);
+double mgp_dhubbleda(const mgp_cosmo *c, double a);
+double mgp_beta_dgp(const mgp_cosmo *c, double a);
+double mgp_beta_of_a(const mgp_cosmo *c, double a);
+double mgp_mass2_of_a(const mgp_cosmo *c, double a);
+double mgp_coupling(const mgp_cosmo *c, double a);
+double mgp_geff(const mgp_cosmo *c, double a, double k);
+double mgp_factor_2lpt(const mgp_cosmo *c, double a);
+/* phi_crit(a) of screening_factor_potential (user_defined_functions.h:725-750) */
+double mgp_phicrit(const mgp_cosmo *c, double a);
+/* prefactor C(a) with fac = C(a)(1+delta) in screening_factor_density
+ * (user_defined_functions.h:757-773) */
+double mgp_dgp_screen_prefactor(const mgp_cosmo *c, double a);
+
+/* growth lookups (src/cosmo.c:318-403), normalised at a = 1 */
+double mgp_cosmo_growth(const mgp_cosmo *c, int which, double a);
+double mgp_cosmo_Sq(const mgp_cosmo *c, double ai, double af, double aref);
+double mgp_cosmo_Sphi(const mgp_cosmo *c, double ai, double af, double aref);
+
+/* PowerSpec (src/power.c:373-394) in (Mpc/h)^3, k in h/Mpc */
+double mgp_cosmo_power(const mgp_cosmo *c, double k);
+/* mg_pofk_ratio(k, 1) and mg_sigma8_enhancement(1) for scale-independent
+ * growth (src/cosmo.c:688-756) */
+double mgp_cosmo_pofk_ratio(const mgp_cosmo *c, double a);
+double mgp_cosmo_sigma8_enh(const mgp_cosmo *c, double a);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,182 @@
+/*
+ * Internal state of an mgp_ctx and the kernel launchers of the GB300 COLA
+ * library.  Not part of the public ABI.
+ *
+ * HBM layout (N = Nmesh, Ns = Nsample, P = 2(N/2+1), NH = N/2+1):
+ *   particles, SoA float, lattice order p = (i*Ns + j)*Ns + k:
+ *     s[3][Np]   displacement from the Lagrangian point q = (i,j,k) Box/Ns
+ *     v[3][Np]   COLA velocity minus the running offset `cv`
+ *     D1[3][Np]  ZA displacement, D2[3][Np] 2LPT displacement (times -3/7)
+ *   true position x = wrap(q + s + cx), true velocity = v + cv, where cx, cv
+ *   are FP64 3-vectors in `dstate` updated on the device after every kick.
+ *   grids, FP32 (FFTW/cuFFT padded layout):
+ *     rho  [N][N][P]      density (real) / MG effective density (in place)
+ *     dk   [N][N][NH]c    delta(k)
+ *     frc  3 x [N][N][P]  force grids (complex in, real out, batched C2R)
+ *     mg1  [N][N][P]      MG scratch: Phi_N(k)->Phi_N(x) or smoothed delta
+ */
+#ifndef MGP_INTERNAL_H
+#define MGP_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "mgp_cosmo.h"
+#include "mgpicola.h"
+
+/* FP64 device-side running state (one per context). */
+typedef struct {
+  double cx[3];        /* position offset (Mpc/h) */
+  double cv[3];        /* velocity offset */
+  double mean_disp[3]; /* sumDxyz of the last MtoParticles */
+  double mean_v[3];    /* mean of the stored v after the last kick */
+} mgp_dstate;
+
+#define MGP_NTIMERS 8
+
+typedef struct mgp_grid_geom {
+  int N, NH;
+  long long P;          /* padded row length in floats */
+  long long nreal;      /* N*N*P floats */
+  long long ncomplex;   /* N*N*NH complex values */
+} mgp_grid_geom;
+
+struct mgp_ctx {
+  mgp_params p;
+  mgp_cosmo cosmo;
+  int device;
+  cudaStream_t stream;
+  mgp_grid_geom g;
+  long long np;
+  int Ns;
+
+  /* particles */
+  float *s, *v, *D1, *D2;  /* each 3*np */
+  mgp_dstate *dstate;      /* device */
+  double *partials;        /* per-block reduction scratch (double) */
+  float *stage;            /* host-interface staging, 6*np floats (lazy) */
+  int max_blocks;
+
+  /* grids */
+  float *rho, *dk, *frc, *mg1;
+  void *fft_work;
+  size_t fft_work_bytes;
+  cufftHandle plan_r2c_oop, plan_r2c_ip, plan_c2r_1, plan_c2r_3;
+
+  /* P(k) */
+  int pk_nbins, pk_bintype, pk_sub;
+  double pk_kmin, pk_kmax;  /* integer-k units, adjusted */
+  int *rk_bin;              /* device: bin index per integer |k|^2 (or -1) */
+  float *win1d;             /* device: 1/sinc^4 per |d| in [0, N/2] */
+  float *pk_block;          /* device: per-block FP32 bin partials */
+  double *pk_sum;           /* device: FP64 bin sums */
+  double *pk_n, *pk_k;      /* host: mode counts and k sums per bin */
+  double *pk_host;          /* host: last P(k) sums */
+  int pk_blocks;
+  int have_density, have_forces;
+  double last_density_a;
+
+  /* timing */
+  int timing;
+  cudaEvent_t ev[MGP_NTIMERS][2];
+  float ms[MGP_NTIMERS];
+  int timed[MGP_NTIMERS];
+  long long launches;
+};
+
+enum { T_CIC = 0, T_R2C, T_POFK, T_MG, T_FORCES, T_C2R, T_IKD, T_MISC };
+
+/* error plumbing (C linkage: also called from the C sources) */
+#ifdef __cplusplus
+extern "C" {
+#endif
+int mgp_set_error(int code, const char *fmt, ...);
+#ifdef __cplusplus
+}
+#endif
+
+#define MGP_CUDA(call)                                                                      \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return mgp_set_error(MGP_ECUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,            \
+                           cudaGetErrorString(e_));                                         \
+  } while (0)
+#define MGP_CUFFT(call)                                                                     \
+  do {                                                                                      \
+    cufftResult r_ = (call);                                                                \
+    if (r_ != CUFFT_SUCCESS)                                                                \
+      return mgp_set_error(MGP_ECUFFT, "%s:%d %s: cufft error %d", __FILE__, __LINE__, #call, \
+                           (int)r_);                                                        \
+  } while (0)
+#define MGP_CHECK_LAUNCH()                                                                  \
+  do {                                                                                      \
+    cudaError_t e_ = cudaGetLastError();                                                    \
+    if (e_ != cudaSuccess)                                                                  \
+      return mgp_set_error(MGP_ECUDA, "%s:%d kernel launch: %s", __FILE__, __LINE__,        \
+                           cudaGetErrorString(e_));                                         \
+  } while (0)
+
+/* ------------------------------------------------------------ launchers */
+/* Per-launch scalars of the fused MtoParticles + Kick + Drift kernel. */
+typedef struct {
+  float scale;        /* N / Box */
+  float inv_scale;    /* Box / N */
+  float kick_disp;    /* -1.5 * Omega * dda */
+  float kick_d1;      /* -UseCOLA * ddD(A) / A * dda */
+  float kick_d2;      /* -UseCOLA * ddD2(A) / A * dda */
+  float dyyy;         /* Sq(A, AFF, AF) */
+  float dD1;          /* UseCOLA * (D(AFF) - D(A)) */
+  float dD2;          /* UseCOLA * (D2(AFF) - D2(A)) */
+  int do_drift;
+  double dda_omega;   /* 1.5 * Omega * dda for the velocity offset */
+  double dyyy_d;
+} mgp_kd_args;
+
+int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st);
+int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box,
+                   float wpar, float *rho, long long P, cudaStream_t stream);
+int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins,
+                    float *block_part, int nblocks, double *sums, cudaStream_t st);
+int mgp_launch_forces(const float *dk, const float *mgk, float mg_coupling, float mg_mass2, int mg_kind,
+                      int N, double box, float *frc, long long grid_floats, cudaStream_t st);
+int mgp_launch_ikd(const float *frc, long long grid_floats, int N, long long P, int Ns, long long np,
+                   float *s, float *v, const float *D1, const float *D2, mgp_dstate *dst,
+                   double *partials, int nblocks, const mgp_kd_args *a, cudaStream_t st);
+int mgp_ikd_blocks(long long np);
+long long mgp_kernel_launches(void);
+
+/* MG real-space and k-space passes */
+int mgp_launch_div_laplacian(const float *dk, float *out, int N, float norm, cudaStream_t st);
+int mgp_launch_smooth(const float *dk, float *out, int N, int filter, float kR_per_sqrtRK, float norm, cudaStream_t st);
+int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float phicrit, cudaStream_t st);
+int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float coupling, float pref,
+                              cudaStream_t st);
+int mgp_launch_scale_complex(float *c, long long ncomplex, float factor, cudaStream_t st);
+
+/* IC */
+int mgp_launch_ic_delta(const uint32_t *seedtable, const double *amp_rk, const unsigned char *cut1d,
+                        int N, int Ns, double box, int fixed, int inverted, int sphere, float *dk,
+                        cudaStream_t st);
+int mgp_launch_ic_grad6(const float *dk, float *out6, long long grid_floats, int N, cudaStream_t st);
+int mgp_launch_ic_source(float *g6, long long grid_floats, int N, long long P, cudaStream_t st);
+int mgp_launch_ic_disp(const float *dk, const float *src, float *out6, long long grid_floats, int N, double box,
+                       cudaStream_t st);
+int mgp_launch_aos_to_soa(const float *in, float *out, long long np, cudaStream_t st);
+int mgp_launch_output(const float *s, const float *v, const float *D1, const float *D2, const mgp_dstate *dst,
+                      long long np, int Ns, double box, double lengthfac, double vfac, double dDdy, double dD2dy,
+                      double cola, float *pos, float *vel, cudaStream_t st);
+int mgp_launch_ic_readout(const float *g6, long long grid_floats, int N, long long P, int Ns,
+                          float *D1, float *D2, double *partials, int nblocks, cudaStream_t st);
+int mgp_launch_ic_finish(float *D1, float *D2, float *s, float *v, long long np, const double *partials,
+                         int nblocks, float Di, float Di2, double inv_n3, cudaStream_t st);
+int mgp_launch_finalize_kd(mgp_dstate *dst, const double *partials, int nblocks, long long np,
+                           double dda_omega, double dyyy, int do_drift, cudaStream_t st);
+int mgp_launch_positions(const float *s, const mgp_dstate *dst, long long np, int Ns, double box,
+                         float *out_pos, float *out_vel, const float *v, cudaStream_t st);
+int mgp_launch_set_state(float *s, float *v, const float *pos, const float *vel, long long np, int Ns,
+                         double box, cudaStream_t st);
+
+#endif

@@ -1,0 +1,853 @@
+// CUDA kernels of the GB300 COLA particle-mesh step and 2LPT IC path
+// (sm_103a).  Every kernel restates one loop of the reference and cites it;
+// paths are relative to the MG-PICOLA-PUBLIC tree.
+//
+// All kernels are HBM-bound streaming or gather/scatter passes: none of them
+// is GEMM-shaped, so there is no tensor-core path here.  Grids are sized in
+// multiples of the SM count (152 on GB300) times resident blocks.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "mgp_internal.h"
+#include "mgp_rng.h"
+
+#define MGP_THREADS 256
+
+// Process-wide count of this library's own kernel launches (cuFFT not
+// included); read by mgp_launch_count.
+static long long g_kernel_launches = 0;
+long long mgp_kernel_launches(void) { return g_kernel_launches; }
+
+static int g_sm_count = 0;
+static int sm_count() {
+  if (g_sm_count == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sm_count <= 0) g_sm_count = 152;
+  }
+  return g_sm_count;
+}
+
+static int blocks_for(long long n, int per_sm) {
+  long long b = (n + MGP_THREADS - 1) / MGP_THREADS;
+  long long cap = (long long)sm_count() * per_sm;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+// -------------------------------------------------------------- helpers
+// Lattice coordinates of particle p (src/main.c:257-262 ordering).
+__device__ __forceinline__ void lattice_ijk(long long p, int Ns, int &i, int &j, int &k) {
+  long long ns2 = (long long)Ns * Ns;
+  i = (int)(p / ns2);
+  long long r = p - (long long)i * ns2;
+  j = (int)(r / Ns);
+  k = (int)(r - (long long)j * Ns);
+}
+
+// Cell index and CIC fraction along one axis for the particle at lattice
+// index `li` with displacement `s` (Mpc/h) and global offset `off_cells`.
+// Position in cells = li*N/Ns + s*N/Box + off; the lattice part is split into
+// integer and fractional parts exactly so the small displacement keeps full
+// FP32 precision.
+__device__ __forceinline__ void cell_frac(int li, float s, float off_cells, int N, int Ns, float scale,
+                                          int &idx, float &frac) {
+  long long qn = (long long)li * N;
+  int qi = (int)(qn / Ns);
+  float qf = (float)(qn - (long long)qi * Ns) / (float)Ns;
+  float w = fmaf(s, scale, off_cells) + qf;
+  float fl = floorf(w);
+  float fr = w - fl;
+  if (fr >= 1.0f) { fr -= 1.0f; fl += 1.0f; }
+  int ic = (qi + (int)fl) % N;
+  if (ic < 0) ic += N;
+  idx = ic;
+  frac = fr;
+}
+
+__global__ void k_fill(float *__restrict__ p, long long n, float v) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = v;
+}
+
+int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st) {
+  k_fill<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>(p, n, value);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// ------------------------------------------------------------- CIC deposit
+// PtoMesh (src/auxPM.c:280-357): every particle adds its cloud-in-cell
+// weights, with WPAR = (N/Ns)^3 folded into the y factors (auxPM.c:316-317),
+// to a density grid pre-set to -1; periodic in all three axes (the ghost
+// x-slice exchange of auxPM.c:350-356 is the x wrap).
+__global__ void __launch_bounds__(MGP_THREADS) k_cic(const float *__restrict__ s, const mgp_dstate *__restrict__ st,
+                                                     long long np, int Ns, int N, float scale, float wpar,
+                                                     float *__restrict__ rho, long long P) {
+  const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
+  const float *sx = s, *sy = s + np, *sz = s + 2 * np;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    int i, j, k;
+    lattice_ijk(p, Ns, i, j, k);
+    int ix, iy, iz;
+    float DX, DY, DZ;
+    cell_frac(i, sx[p], ox, N, Ns, scale, ix, DX);
+    cell_frac(j, sy[p], oy, N, Ns, scale, iy, DY);
+    cell_frac(k, sz[p], oz, N, Ns, scale, iz, DZ);
+    float TX = 1.0f - DX, TY = (1.0f - DY) * wpar, TZ = 1.0f - DZ;
+    DY *= wpar;
+    int ixn = ix + 1 == N ? 0 : ix + 1, iyn = iy + 1 == N ? 0 : iy + 1, izn = iz + 1 == N ? 0 : iz + 1;
+    long long r00 = ((long long)ix * N + iy) * P, r01 = ((long long)ix * N + iyn) * P;
+    long long r10 = ((long long)ixn * N + iy) * P, r11 = ((long long)ixn * N + iyn) * P;
+    atomicAdd(rho + r00 + iz, TX * TY * TZ);
+    atomicAdd(rho + r00 + izn, TX * TY * DZ);
+    atomicAdd(rho + r01 + iz, TX * DY * TZ);
+    atomicAdd(rho + r01 + izn, TX * DY * DZ);
+    atomicAdd(rho + r10 + iz, DX * TY * TZ);
+    atomicAdd(rho + r10 + izn, DX * TY * DZ);
+    atomicAdd(rho + r11 + iz, DX * DY * TZ);
+    atomicAdd(rho + r11 + izn, DX * DY * DZ);
+  }
+}
+
+int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box, float wpar,
+                   float *rho, long long P, cudaStream_t stream) {
+  k_cic<<<blocks_for(np, 8), MGP_THREADS, 0, stream>>>(s, st, np, Ns, N, (float)(N / box), wpar, rho, P);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// ------------------------------------------------------------- P(k) bins
+// compute_power_spectrum (src/compute_pofk.c:71-271): every stored mode
+// (i, j, kz), kz in [0, N/2], contributes |delta|^2 / (sinc_x sinc_y sinc_z)^4
+// with weight 1 on the kz = 0 and kz = N/2 planes and 2 elsewhere; the
+// y-mirror loop of the reference visits exactly the stored j range.  The bin
+// of a mode depends only on its integer |k|^2, looked up in rk_bin (computed
+// on the host in double exactly as pofk_bin_index, compute_pofk.c:30-46).
+// Mode counts and k sums are geometric and also precomputed on the host.
+__global__ void __launch_bounds__(MGP_THREADS) k_pofk(const float2 *__restrict__ dk, int N, const int *__restrict__ rk_bin,
+                                                      const float *__restrict__ win, int nbins,
+                                                      float *__restrict__ block_part, long long chunk) {
+  extern __shared__ float sh[];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) sh[b] = 0.0f;
+  __syncthreads();
+  const int NH = N / 2 + 1;
+  const long long total = (long long)N * N * NH;
+  long long lo = (long long)blockIdx.x * chunk, hi = lo + chunk;
+  if (hi > total) hi = total;
+  for (long long c = lo + threadIdx.x; c < hi; c += blockDim.x) {
+    int kz = (int)(c % NH);
+    long long r = c / NH;
+    int j = (int)(r % N), i = (int)(r / N);
+    int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
+    int rk = d0 * d0 + d1 * d1 + kz * kz;
+    int bin = rk_bin[rk];
+    if (bin < 0) continue;
+    float2 z = dk[c];
+    float w = (kz == 0 || 2 * kz == N) ? 1.0f : 2.0f;
+    float pk = (z.x * z.x + z.y * z.y) * (win[d0] * win[d1] * win[kz] * w);
+    atomicAdd(&sh[bin], pk);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) block_part[(long long)blockIdx.x * nbins + b] = sh[b];
+}
+
+// Deterministic cross-block sum in FP64 (the MPI_Allreduce of compute_pofk.c:225).
+__global__ void k_pofk_reduce(const float *__restrict__ block_part, int nblocks, int nbins, double *__restrict__ sums) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  double s = 0.0;
+  for (int k = 0; k < nblocks; k++) s += (double)block_part[(long long)k * nbins + b];
+  sums[b] = s;
+}
+
+int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins, float *block_part,
+                    int nblocks, double *sums, cudaStream_t st) {
+  const long long total = (long long)N * N * (N / 2 + 1);
+  long long chunk = (total + nblocks - 1) / nblocks;
+  size_t shmem = sizeof(float) * (size_t)nbins;
+  if (shmem > 48 * 1024) {
+    cudaFuncSetAttribute(k_pofk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem);
+  }
+  k_pofk<<<nblocks, MGP_THREADS, shmem, st>>>((const float2 *)dk, N, rk_bin, win, nbins, block_part, chunk);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  k_pofk_reduce<<<(nbins + 127) / 128, 128, 0, st>>>(block_part, nblocks, nbins, sums);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// ------------------------------------------------------------ force grids
+// Forces (src/auxPM.c:437-535): F_a(k) = i k_a/k^2 * S(k) / N^3 with
+// S = delta(k) [+ MG source], no CIC deconvolution, k = 0 zeroed.  Wave
+// numbers: x index i > N/2 -> i - N (N/2 stays +N/2), y index j > N/2 is the
+// reference's mirrored j (dd = -(N - j)), kz >= 0.
+// MG source (auxPM.c:450-455): mg_kind 1 adds coupling * RK/(RK + m^2) *
+// delta_eff(k) (EffDensitykToPhiofk, src/mg.h:74-116, fused here); mg_kind 2
+// adds delta_eff(k) as is (density screening, src/mg.h:197-260); mg_kind 3
+// scales delta by (1 + coupling) (DGP without screening, src/mg.h:209-215).
+// On the kz = 0 and kz = N/2 planes a component whose own index sits on the
+// Nyquist plane is odd under k -> -k with the same stored index, so it has no
+// Hermitian partner; a real-output inverse FFT keeps only the Hermitian part
+// there, which is zero.  Those entries are written as zero so that cuFFT and
+// FFTW give the same real field.
+__global__ void __launch_bounds__(MGP_THREADS) k_forces(const float2 *__restrict__ dk, const float2 *__restrict__ mgk,
+                                                        float mg_coupling, float mg_mass2, int mg_kind, int N,
+                                                        float cfac, float2 *__restrict__ fx, float2 *__restrict__ fy,
+                                                        float2 *__restrict__ fz) {
+  const int NH = N / 2 + 1;
+  const long long total = (long long)N * N * NH;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += stride) {
+    int kz = (int)(c % NH);
+    long long r = c / NH;
+    int j = (int)(r % N), i = (int)(r / N);
+    int dx = i > N / 2 ? i - N : i, dy = j > N / 2 ? j - N : j, dz = kz;
+    int rk = dx * dx + dy * dy + dz * dz;
+    float2 S = dk[c];
+    if (mg_kind == 1) {
+      float2 m = mgk[c];
+      float f = mg_coupling * (float)rk / ((float)rk + mg_mass2);
+      S.x = fmaf(f, m.x, S.x);
+      S.y = fmaf(f, m.y, S.y);
+    } else if (mg_kind == 2) {
+      float2 m = mgk[c];
+      S.x += m.x;
+      S.y += m.y;
+    } else if (mg_kind == 3) {
+      S.x *= 1.0f + mg_coupling;
+      S.y *= 1.0f + mg_coupling;
+    }
+    float g = rk == 0 ? 0.0f : cfac / (float)rk;  // = -1/(RK N^3 Scale)
+    float ax = g * (float)dx, ay = g * (float)dy, az = g * (float)dz;
+    if (kz == 0 || 2 * kz == N) {
+      if (2 * i == N) ax = 0.0f;
+      if (2 * j == N) ay = 0.0f;
+      az = 0.0f;
+    }
+    fx[c] = make_float2(-ax * S.y, ax * S.x);
+    fy[c] = make_float2(-ay * S.y, ay * S.x);
+    fz[c] = make_float2(-az * S.y, az * S.x);
+  }
+}
+
+int mgp_launch_forces(const float *dk, const float *mgk, float mg_coupling, float mg_mass2, int mg_kind, int N,
+                      double box, float *frc, long long grid_floats, cudaStream_t st) {
+  const long long total = (long long)N * N * (N / 2 + 1);
+  double scale = 2.0 * M_PI / box;
+  float cfac = (float)(-1.0 / ((double)N * N * N * scale));
+  float2 *fx = (float2 *)frc, *fy = (float2 *)(frc + grid_floats), *fz = (float2 *)(frc + 2 * grid_floats);
+  k_forces<<<blocks_for(total, 8), MGP_THREADS, 0, st>>>((const float2 *)dk, (const float2 *)mgk, mg_coupling,
+                                                         mg_mass2, mg_kind, N, cfac, fx, fy, fz);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// ------------------------------------ fused MtoParticles + Kick + Drift
+// MtoParticles (src/auxPM.c:560-644): trilinear interpolation of the three
+// force grids at the particle; Kick (src/main.c:688-742):
+//   v += dda * (-1.5 Omega (Disp - <Disp>) - UseCOLA (D1 ddD + D2 ddD2)/A);
+// Drift (src/main.c:747-787):
+//   x += (v - <v>) dyyy + UseCOLA (D1 dD + D2 dD2).
+// The global means only shift all velocities (or all positions) by one
+// vector, so the kernel applies the particle-local part and carries the
+// uniform part in the FP64 offsets cv / cx (k_finalize_kd), which removes
+// the two extra passes over the particles the reference makes.
+__device__ __forceinline__ double block_sum_d(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[k];
+  return s;
+}
+
+__global__ void __launch_bounds__(MGP_THREADS) k_interp_kick_drift(
+    const float *__restrict__ frc, long long gf, int N, long long P, int Ns, long long np, float *__restrict__ s,
+    float *__restrict__ v, const float *__restrict__ D1, const float *__restrict__ D2,
+    const mgp_dstate *__restrict__ st, double *__restrict__ partials, mgp_kd_args a) {
+  __shared__ double sh[MGP_THREADS / 32];
+  const float ox = (float)(st->cx[0] * a.scale), oy = (float)(st->cx[1] * a.scale), oz = (float)(st->cx[2] * a.scale);
+  const float *F0 = frc, *F1 = frc + gf, *F2 = frc + 2 * gf;
+  float accD[3] = {0.f, 0.f, 0.f}, accV[3] = {0.f, 0.f, 0.f};
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    int i, j, k;
+    lattice_ijk(p, Ns, i, j, k);
+    float sp[3] = {s[p], s[np + p], s[2 * np + p]};
+    int ix, iy, iz;
+    float DX, DY, DZ;
+    cell_frac(i, sp[0], ox, N, Ns, a.scale, ix, DX);
+    cell_frac(j, sp[1], oy, N, Ns, a.scale, iy, DY);
+    cell_frac(k, sp[2], oz, N, Ns, a.scale, iz, DZ);
+    float TX = 1.0f - DX, TY = 1.0f - DY, TZ = 1.0f - DZ;
+    int ixn = ix + 1 == N ? 0 : ix + 1, iyn = iy + 1 == N ? 0 : iy + 1, izn = iz + 1 == N ? 0 : iz + 1;
+    long long r00 = ((long long)ix * N + iy) * P, r01 = ((long long)ix * N + iyn) * P;
+    long long r10 = ((long long)ixn * N + iy) * P, r11 = ((long long)ixn * N + iyn) * P;
+    float w000 = TX * TY * TZ, w001 = TX * TY * DZ, w010 = TX * DY * TZ, w011 = TX * DY * DZ;
+    float w100 = DX * TY * TZ, w101 = DX * TY * DZ, w110 = DX * DY * TZ, w111 = DX * DY * DZ;
+    float disp[3];
+    const float *Fa[3] = {F0, F1, F2};
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+      const float *F = Fa[ax];
+      disp[ax] = __ldg(F + r00 + iz) * w000 + __ldg(F + r00 + izn) * w001 + __ldg(F + r01 + iz) * w010 +
+                 __ldg(F + r01 + izn) * w011 + __ldg(F + r10 + iz) * w100 + __ldg(F + r10 + izn) * w101 +
+                 __ldg(F + r11 + iz) * w110 + __ldg(F + r11 + izn) * w111;
+    }
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+      long long o = ax * np + p;
+      float d1 = D1[o], d2 = D2[o];
+      float vn = v[o] + a.kick_disp * disp[ax] + a.kick_d1 * d1 + a.kick_d2 * d2;
+      v[o] = vn;
+      if (a.do_drift) s[o] = sp[ax] + vn * a.dyyy + a.dD1 * d1 + a.dD2 * d2;
+      accD[ax] += disp[ax];
+      accV[ax] += vn;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    double t = block_sum_d((double)accD[q], sh);
+    if (threadIdx.x == 0) partials[(long long)blockIdx.x * 6 + q] = t;
+    t = block_sum_d((double)accV[q], sh);
+    if (threadIdx.x == 0) partials[(long long)blockIdx.x * 6 + 3 + q] = t;
+  }
+}
+
+// Means over all particles and offset update (one block, fixed order).
+__global__ void k_finalize_kd(mgp_dstate *st, const double *__restrict__ partials, int nblocks, double inv_np,
+                              double dda_omega, double dyyy, int do_drift) {
+  __shared__ double sh[6][MGP_THREADS / 32];
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+    for (int q = 0; q < 6; q++) acc[q] += partials[(long long)b * 6 + q];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int q = 0; q < 6; q++) {
+    double x = acc[q];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[q][w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[6];
+    for (int q = 0; q < 6; q++) {
+      t[q] = 0.0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); k++) t[q] += sh[q][k];
+    }
+    for (int ax = 0; ax < 3; ax++) {
+      double mD = t[ax] * inv_np, mV = t[3 + ax] * inv_np;
+      st->mean_disp[ax] = mD;
+      st->cv[ax] += dda_omega * mD;
+      st->mean_v[ax] = mV;
+      if (do_drift) st->cx[ax] -= mV * dyyy;
+    }
+  }
+}
+
+int mgp_ikd_blocks(long long np) { return blocks_for(np, 8); }
+
+int mgp_launch_ikd(const float *frc, long long gf, int N, long long P, int Ns, long long np, float *s, float *v,
+                   const float *D1, const float *D2, mgp_dstate *dst, double *partials, int nblocks,
+                   const mgp_kd_args *a, cudaStream_t st) {
+  k_interp_kick_drift<<<nblocks, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  k_finalize_kd<<<1, MGP_THREADS, 0, st>>>(dst, partials, nblocks, 1.0 / (double)np, a->dda_omega, a->dyyy_d,
+                                           a->do_drift);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+int mgp_launch_finalize_kd(mgp_dstate *dst, const double *partials, int nblocks, long long np, double dda_omega,
+                           double dyyy, int do_drift, cudaStream_t st) {
+  k_finalize_kd<<<1, MGP_THREADS, 0, st>>>(dst, partials, nblocks, 1.0 / (double)np, dda_omega, dyyy, do_drift);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// --------------------------------------------------------- MG passes
+// DivideByLaplacian (src/mg.h:21-64): Phi_N(k) = -norm * delta(k) / RK.
+__global__ void k_div_laplacian(const float2 *__restrict__ dk, float2 *__restrict__ out, int N, float norm) {
+  const int NH = N / 2 + 1;
+  const long long total = (long long)N * N * NH;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += stride) {
+    int kz = (int)(c % NH);
+    long long r = c / NH;
+    int j = (int)(r % N), i = (int)(r / N);
+    int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
+    int rk = d0 * d0 + d1 * d1 + kz * kz;
+    float2 z = dk[c];
+    float f = rk == 0 ? 0.0f : -norm / (float)rk;
+    out[c] = make_float2(f * z.x, f * z.y);
+  }
+}
+
+int mgp_launch_div_laplacian(const float *dk, float *out, int N, float norm, cudaStream_t st) {
+  const long long total = (long long)N * N * (N / 2 + 1);
+  k_div_laplacian<<<blocks_for(total, 8), MGP_THREADS, 0, st>>>((const float2 *)dk, (float2 *)out, N, norm);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// SmoothDensityField (src/mg.h:268-309) with smoothing_filter (mg.h:318-338).
+__global__ void k_smooth(const float2 *__restrict__ dk, float2 *__restrict__ out, int N, int filter, float kR1,
+                         float norm) {
+  const int NH = N / 2 + 1;
+  const long long total = (long long)N * N * NH;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += stride) {
+    int kz = (int)(c % NH);
+    long long r = c / NH;
+    int j = (int)(r % N), i = (int)(r / N);
+    int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
+    int rk = d0 * d0 + d1 * d1 + kz * kz;
+    float kR = sqrtf((float)rk) * kR1, f = 1.0f;
+    if (filter == MGP_FILTER_GAUSSIAN) f = expf(-0.5f * kR * kR);
+    else if (filter == MGP_FILTER_TOPHAT) f = kR < 1e-5f ? 1.0f : 3.0f / (kR * kR * kR) * (sinf(kR) - kR * cosf(kR));
+    else if (filter == MGP_FILTER_SHARPK) f = kR < 1.0f ? 1.0f : 0.0f;
+    f *= norm;
+    float2 z = dk[c];
+    out[c] = make_float2(f * z.x, f * z.y);
+  }
+}
+
+int mgp_launch_smooth(const float *dk, float *out, int N, int filter, float kR1, float norm, cudaStream_t st) {
+  const long long total = (long long)N * N * (N / 2 + 1);
+  k_smooth<<<blocks_for(total, 8), MGP_THREADS, 0, st>>>((const float2 *)dk, (float2 *)out, N, filter, kR1, norm);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Potential screening (src/mg.h:174-176, screening_factor_potential at
+// src/user_defined_functions.h:725-750): rho *= min(1, |phicrit / Phi_N|)
+// where Phi_N < 0, else 1.  Padding entries are included as in the reference.
+__global__ void k_screen_potential(float *__restrict__ rho, const float *__restrict__ phi, long long n, float phicrit) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    float ph = phi[i], f = 1.0f;
+    if (ph < 0.0f) {
+      f = fabsf(phicrit / ph);
+      if (f > 1.0f) f = 1.0f;
+    }
+    rho[i] *= f;
+  }
+}
+
+int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float phicrit, cudaStream_t st) {
+  k_screen_potential<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>(rho, phi, n, phicrit);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Density screening (src/mg.h:241-250, screening_factor_density at
+// src/user_defined_functions.h:757-773): rho *= coupling * 2(sqrt(1+f)-1)/f,
+// f = pref (1 + delta_R), factor 1 when f < 1e-5.
+__global__ void k_screen_density(float *__restrict__ rho, const float *__restrict__ dsm, long long n, float coupling,
+                                 float pref) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    float fac = pref * (1.0f + dsm[i]);
+    float sc = fac < 1e-5f ? 1.0f : 2.0f * (sqrtf(1.0f + fac) - 1.0f) / fac;
+    rho[i] *= coupling * sc;
+  }
+}
+
+int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float coupling, float pref, cudaStream_t st) {
+  k_screen_density<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>(rho, dsm, n, coupling, pref);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// ComputeFifthForce_TimeDepGeffModels (src/mg.h:127-137): P3D *= Geff/G.
+__global__ void k_scale(float *__restrict__ c, long long n, float f) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) c[i] *= f;
+}
+
+int mgp_launch_scale_complex(float *c, long long ncomplex, float factor, cudaStream_t st) {
+  k_scale<<<blocks_for(2 * ncomplex, 8), MGP_THREADS, 0, st>>>(c, 2 * ncomplex, factor);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// ------------------------------------------------------------------ IC
+// displacement_fields, Gaussian branch (src/2LPT.c:276-495): one thread per
+// (i, j) column of the k grid replays that column's white-noise stream
+// (seeded by seedtable[i N + j], 2LPT.c:344) in the reference's draw order --
+// phase, then amplitude unless amplitude-fixed -- and writes delta(k) for
+// kz < N/2, including the Hermitian partners on the kz = 0 plane.
+// amp_rk[RK] = Box^-1.5 sqrt(P(k) * rescale) is tabulated on the host in FP64;
+// cut1d[|d|] is the cube cut of 2LPT.c:383-386 evaluated on the host with the
+// reference's exact double expression.
+__global__ void __launch_bounds__(MGP_THREADS) k_ic_delta(const uint32_t *__restrict__ seedtable,
+                                                          const double *__restrict__ amp_rk,
+                                                          const unsigned char *__restrict__ cut1d, int N, int Ns,
+                                                          double box, int fixed, int inverted, int sphere,
+                                                          float2 *__restrict__ dk) {
+  long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= (long long)N * N) return;
+  const int NH = N / 2 + 1;
+  int i = (int)(col / N), j = (int)(col % N);
+  uint32_t seed = seedtable[col];
+  uint64_t n = 0;
+  const double twopi = 2 * 3.14159265358979323846;
+  for (int k = 0; k < N / 2; k++) {
+    double phase = mgp_uniform(seed, n++);
+    double ampl = 1.0;
+    if (!fixed) {
+      do { ampl = mgp_uniform(seed, n++); } while (ampl == 0.0);
+    }
+    if (2 * i == N || 2 * j == N) continue;
+    if (i == 0 && j == 0 && k == 0) continue;
+    int di = i < N / 2 ? i : i - N, dj = j < N / 2 ? j : j - N, dkz = k;
+    int ai = di < 0 ? -di : di, aj = dj < 0 ? -dj : dj;
+    if (sphere) {
+      double kx = (di < 0 ? -(N - i) * 2 * 3.14159265358979323846 / box : i * 2 * 3.14159265358979323846 / box);
+      double ky = (dj < 0 ? -(N - j) * 2 * 3.14159265358979323846 / box : j * 2 * 3.14159265358979323846 / box);
+      double kzv = k * 2 * 3.14159265358979323846 / box;
+      double km = sqrt(kx * kx + ky * ky + kzv * kzv);
+      if (km * box / twopi > Ns / 2) continue;
+    } else {
+      if (cut1d[ai] || cut1d[aj] || cut1d[dkz]) continue;
+    }
+    int rk = ai * ai + aj * aj + dkz * dkz;
+    double delta = amp_rk[rk];
+    if (!fixed) delta *= sqrt(-log(ampl));
+    if (inverted) delta = -delta;
+    float sn, cs;
+    sincospif((float)(2.0 * phase), &sn, &cs);
+    float re = (float)delta * cs, im = (float)delta * sn;
+    if (k > 0) {
+      dk[((long long)i * N + j) * NH + k] = make_float2(re, im);
+    } else if (i == 0) {
+      if (j >= N / 2) continue;
+      dk[((long long)j) * NH] = make_float2(re, im);
+      dk[((long long)(N - j)) * NH] = make_float2(re, -im);
+    } else {
+      if (i >= N / 2) continue;
+      int ii = N - i, jj = (N - j) % N;
+      dk[((long long)i * N + j) * NH] = make_float2(re, im);
+      dk[((long long)ii * N + jj) * NH] = make_float2(re, -im);
+    }
+  }
+  (void)twopi;
+}
+
+int mgp_launch_ic_delta(const uint32_t *seedtable, const double *amp_rk, const unsigned char *cut1d, int N, int Ns,
+                        double box, int fixed, int inverted, int sphere, float *dk, cudaStream_t st) {
+  long long cols = (long long)N * N;
+  int nb = (int)((cols + MGP_THREADS - 1) / MGP_THREADS);
+  k_ic_delta<<<nb, MGP_THREADS, 0, st>>>(seedtable, amp_rk, cut1d, N, Ns, box, fixed, inverted, sphere, (float2 *)dk);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Integer wave number of index idx in the IC convention (2LPT.c:359-375):
+// idx < N/2 -> idx, else idx - N (so N/2 maps to -N/2).
+__device__ __forceinline__ int ic_d(int idx, int N) { return idx < N / 2 ? idx : idx - N; }
+
+// Displacement gradients (src/2LPT.c:1224-1270): psi_ab(k) = i k_b * Psi_a(k)
+// = -k_a k_b / k^2 delta(k); order (00, 01, 02, 11, 12, 22).
+__global__ void k_ic_grad6(const float2 *__restrict__ dk, float *__restrict__ out, long long gf, int N) {
+  const int NH = N / 2 + 1;
+  const long long total = (long long)N * N * NH;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += stride) {
+    int kz = (int)(c % NH);
+    long long r = c / NH;
+    int j = (int)(r % N), i = (int)(r / N);
+    int d[3] = {ic_d(i, N), ic_d(j, N), ic_d(kz, N)};
+    int rk = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    float2 z = dk[c];
+    float inv = rk == 0 ? 0.0f : -1.0f / (float)rk;
+    const int A[6] = {0, 0, 0, 1, 1, 2}, B[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int g = 0; g < 6; g++) {
+      float f = inv * (float)(d[A[g]] * d[B[g]]);
+      ((float2 *)(out + g * gf))[c] = make_float2(f * z.x, f * z.y);
+    }
+  }
+}
+
+int mgp_launch_ic_grad6(const float *dk, float *out6, long long gf, int N, cudaStream_t st) {
+  const long long total = (long long)N * N * (N / 2 + 1);
+  k_ic_grad6<<<blocks_for(total, 8), MGP_THREADS, 0, st>>>((const float2 *)dk, out6, gf, N);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Second-order source in real space (src/2LPT.c:1282-1290), written over
+// the psi_11 grid.
+__global__ void k_ic_source(float *__restrict__ g, long long gf, long long n) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    float p00 = g[i], p01 = g[gf + i], p02 = g[2 * gf + i], p11 = g[3 * gf + i], p12 = g[4 * gf + i],
+          p22 = g[5 * gf + i];
+    g[3 * gf + i] = p00 * (p11 + p22) + p11 * p22 - p01 * p01 - p02 * p02 - p12 * p12;
+  }
+}
+
+int mgp_launch_ic_source(float *g6, long long gf, int N, long long P, cudaStream_t st) {
+  long long n = (long long)N * N * P;
+  k_ic_source<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>(g6, gf, n);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// ZA and 2LPT displacement fields in k space (src/2LPT.c:406-425,
+// 1343-1355): Psi1_a = i k_a/k^2 delta, Psi2_a = -i k_a/k^2 S2, k in
+// physical units (Box/2pi factor), IC sign convention.  Derivative-type
+// Nyquist entries of the kz = 0 / N/2 planes are zeroed (see k_forces).
+__global__ void k_ic_disp(const float2 *__restrict__ dk, const float *__restrict__ src_grid, float *__restrict__ out,
+                          long long gf, int N, float box_over_2pi) {
+  const int NH = N / 2 + 1;
+  const long long total = (long long)N * N * NH;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += stride) {
+    int kz = (int)(c % NH);
+    long long r = c / NH;
+    int j = (int)(r % N), i = (int)(r / N);
+    int d[3] = {ic_d(i, N), ic_d(j, N), ic_d(kz, N)};
+    int rk = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    float2 z = dk[c];
+    float2 S = ((const float2 *)src_grid)[c];
+    float inv = rk == 0 ? 0.0f : box_over_2pi / (float)rk;
+    bool edge = (kz == 0 || 2 * kz == N);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      float f = inv * (float)d[a];
+      if (edge && ((a == 0 && 2 * i == N) || (a == 1 && 2 * j == N) || a == 2)) f = 0.0f;
+      ((float2 *)(out + a * gf))[c] = make_float2(-f * z.y, f * z.x);
+      ((float2 *)(out + (3 + a) * gf))[c] = make_float2(f * S.y, -f * S.x);
+    }
+  }
+}
+
+int mgp_launch_ic_disp(const float *dk, const float *src, float *out6, long long gf, int N, double box,
+                       cudaStream_t st) {
+  // out6 must not alias dk; the source grid may be one of the six outputs:
+  // each thread reads it before writing the same element.
+  const long long total = (long long)N * N * (N / 2 + 1);
+  k_ic_disp<<<blocks_for(total, 8), MGP_THREADS, 0, st>>>((const float2 *)dk, src, out6, gf, N,
+                                                          (float)(box / (2.0 * M_PI)));
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Read-out of the six real displacement grids at the Lagrangian lattice
+// (src/2LPT.c:1424-1491): trilinear with exact lattice fractions.
+__global__ void __launch_bounds__(MGP_THREADS) k_ic_readout(const float *__restrict__ g, long long gf, int N, long long P,
+                                                            int Ns, float *__restrict__ D1, float *__restrict__ D2,
+                                                            float d2fac, double *__restrict__ partials) {
+  __shared__ double sh[MGP_THREADS / 32];
+  const long long np = (long long)Ns * Ns * Ns;
+  float acc[6] = {0, 0, 0, 0, 0, 0};
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    int li[3];
+    lattice_ijk(p, Ns, li[0], li[1], li[2]);
+    int c0[3], c1[3];
+    float f[3];
+    for (int a = 0; a < 3; a++) {
+      long long qn = (long long)li[a] * N;
+      int q = (int)(qn / Ns);
+      f[a] = (float)(qn - (long long)q * Ns) / (float)Ns;
+      if (q == N) q = N - 1;
+      c0[a] = q;
+      c1[a] = q + 1 >= N ? q + 1 - N : q + 1;
+    }
+    float w[8];
+    long long id[8];
+    for (int t = 0; t < 8; t++) {
+      int bx = (t >> 2) & 1, by = (t >> 1) & 1, bz = t & 1;
+      w[t] = (bx ? f[0] : 1.0f - f[0]) * (by ? f[1] : 1.0f - f[1]) * (bz ? f[2] : 1.0f - f[2]);
+      id[t] = ((long long)(bx ? c1[0] : c0[0]) * N + (by ? c1[1] : c0[1])) * P + (bz ? c1[2] : c0[2]);
+    }
+    for (int a = 0; a < 3; a++) {
+      float d1 = 0.f, d2 = 0.f;
+      for (int t = 0; t < 8; t++) {
+        d1 += g[a * gf + id[t]] * w[t];
+        d2 += g[(3 + a) * gf + id[t]] * w[t];
+      }
+      d2 *= d2fac;
+      D1[a * np + p] = d1;
+      D2[a * np + p] = d2;
+      acc[a] += d1;
+      acc[3 + a] += d2;
+    }
+  }
+  for (int q = 0; q < 6; q++) {
+    double t = block_sum_d((double)acc[q], sh);
+    if (threadIdx.x == 0) partials[(long long)blockIdx.x * 6 + q] = t;
+  }
+}
+
+int mgp_launch_ic_readout(const float *g6, long long gf, int N, long long P, int Ns, float *D1, float *D2,
+                          double *partials, int nblocks, cudaStream_t st) {
+  float d2fac = (float)(-3.0 / 7.0 / ((double)N * N * N));
+  k_ic_readout<<<nblocks, MGP_THREADS, 0, st>>>(g6, gf, N, P, Ns, D1, D2, d2fac, partials);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Mean removal (2LPT.c:1493-1508) and initial COLA state (main.c:257-309):
+// s = D1 Di + D2 Di2 (displacement from q), v = 0.
+__global__ void k_ic_finish(float *__restrict__ D1, float *__restrict__ D2, float *__restrict__ s, float *__restrict__ v,
+                            long long np, const double *__restrict__ partials, int nblocks, float Di, float Di2) {
+  __shared__ float mean[6];
+  if (threadIdx.x < 6) {
+    double t = 0.0;
+    for (int b = 0; b < nblocks; b++) t += partials[(long long)b * 6 + threadIdx.x];
+    mean[threadIdx.x] = (float)(t / (double)np);
+  }
+  __syncthreads();
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    for (int a = 0; a < 3; a++) {
+      long long o = a * np + p;
+      float d1 = D1[o] - mean[a], d2 = D2[o] - mean[3 + a];
+      D1[o] = d1;
+      D2[o] = d2;
+      s[o] = d1 * Di + d2 * Di2;
+      v[o] = 0.0f;
+    }
+  }
+}
+
+int mgp_launch_ic_finish(float *D1, float *D2, float *s, float *v, long long np, const double *partials, int nblocks,
+                         float Di, float Di2, double inv_n3, cudaStream_t st) {
+  (void)inv_n3;
+  k_ic_finish<<<blocks_for(np, 8), MGP_THREADS, 0, st>>>(D1, D2, s, v, np, partials, nblocks, Di, Di2);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// ---------------------------------------------------- particle export
+// Absolute positions wrap(q + s + cx) and velocities v + cv, AoS [np][3].
+__global__ void k_positions(const float *__restrict__ s, const float *__restrict__ v, const mgp_dstate *__restrict__ st,
+                            long long np, int Ns, double box, float *__restrict__ pos, float *__restrict__ vel) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  const double dq = box / (double)Ns;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    int li[3];
+    lattice_ijk(p, Ns, li[0], li[1], li[2]);
+    for (int a = 0; a < 3; a++) {
+      if (pos) {
+        double x = li[a] * dq + (double)s[a * np + p] + st->cx[a];
+        x -= box * floor(x / box);
+        float xf = (float)x;
+        if (xf >= (float)box) xf = 0.0f;
+        pos[3 * p + a] = xf;
+      }
+      if (vel) vel[3 * p + a] = (float)((double)v[a * np + p] + st->cv[a]);
+    }
+  }
+}
+
+int mgp_launch_positions(const float *s, const mgp_dstate *dst, long long np, int Ns, double box, float *out_pos,
+                         float *out_vel, const float *v, cudaStream_t st) {
+  k_positions<<<blocks_for(np, 4), MGP_THREADS, 0, st>>>(s, v, dst, np, Ns, box, out_pos, out_vel);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Import absolute AoS positions/velocities: s = nearest-image (pos - q).
+__global__ void k_set_state(float *__restrict__ s, float *__restrict__ v, const float *__restrict__ pos,
+                            const float *__restrict__ vel, long long np, int Ns, double box) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  const double dq = box / (double)Ns;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    int li[3];
+    lattice_ijk(p, Ns, li[0], li[1], li[2]);
+    for (int a = 0; a < 3; a++) {
+      if (pos) {
+        double d = (double)pos[3 * p + a] - li[a] * dq;
+        d -= box * rint(d / box);
+        s[a * np + p] = (float)d;
+      }
+      if (vel) v[a * np + p] = vel[3 * p + a];
+    }
+  }
+}
+
+int mgp_launch_set_state(float *s, float *v, const float *pos, const float *vel, long long np, int Ns, double box,
+                         cudaStream_t st) {
+  k_set_state<<<blocks_for(np, 4), MGP_THREADS, 0, st>>>(s, v, pos, vel, np, Ns, box);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// AoS [np][3] <-> SoA [3][np] for the host particle interface.
+__global__ void k_aos_to_soa(const float *__restrict__ in, float *__restrict__ out, long long np) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride)
+    for (int a = 0; a < 3; a++) out[a * np + p] = in[3 * p + a];
+}
+int mgp_launch_aos_to_soa(const float *in, float *out, long long np, cudaStream_t st) {
+  k_aos_to_soa<<<blocks_for(np, 4), MGP_THREADS, 0, st>>>(in, out, np);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Particle data as written by Output (src/main.c:913-977): positions times
+// lengthfac, velocities velfac * Hubble/A^1.5 * (Vel - <Vel> + UseCOLA (D1
+// dD/dy + D2 dD2/dy)).  Vel - <Vel> equals the stored v minus its mean.
+__global__ void k_output(const float *__restrict__ s, const float *__restrict__ v, const float *__restrict__ D1,
+                         const float *__restrict__ D2, const mgp_dstate *__restrict__ st, long long np, int Ns,
+                         double box, double lengthfac, double vfac, double dDdy, double dD2dy, double cola,
+                         float *__restrict__ pos, float *__restrict__ vel) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  const double dq = box / (double)Ns;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    int li[3];
+    lattice_ijk(p, Ns, li[0], li[1], li[2]);
+    for (int a = 0; a < 3; a++) {
+      long long o = a * np + p;
+      double x = li[a] * dq + (double)s[o] + st->cx[a];
+      x -= box * floor(x / box);
+      if (x >= box) x = 0.0;
+      pos[3 * p + a] = (float)(lengthfac * x);
+      double vv = (double)v[o] - st->mean_v[a] + cola * ((double)D1[o] * dDdy + (double)D2[o] * dD2dy);
+      vel[3 * p + a] = (float)(vfac * vv);
+    }
+  }
+}
+
+int mgp_launch_output(const float *s, const float *v, const float *D1, const float *D2, const mgp_dstate *dst,
+                      long long np, int Ns, double box, double lengthfac, double vfac, double dDdy, double dD2dy,
+                      double cola, float *pos, float *vel, cudaStream_t st) {
+  k_output<<<blocks_for(np, 4), MGP_THREADS, 0, st>>>(s, v, D1, D2, dst, np, Ns, box, lengthfac, vfac, dDdy, dD2dy,
+                                                      cola, pos, vel);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}

@@ -1,0 +1,263 @@
+"""Python host binding of libmgpicola.so (the GB300 COLA library).
+
+Thin ctypes layer over the C ABI declared in include/mgpicola.h; it mirrors
+the reference's run-parameter names and raises on every non-zero status.
+There is no CPU fallback: loading fails loudly when the shared library is
+missing, and mgp_create fails when no CUDA device is present.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libmgpicola.so")
+
+MODEL_LCDM, MODEL_FOFR, MODEL_DGP, MODEL_BRANSDICKE, MODEL_MBETA = 0, 1, 2, 3, 4
+FILTER_NONE, FILTER_GAUSSIAN, FILTER_TOPHAT, FILTER_SHARPK = 0, 1, 2, 3
+
+# exported symbols of include/mgpicola.h
+EXPORTS = [
+    "mgp_params_default", "mgp_read_parameterfile", "mgp_create", "mgp_destroy", "mgp_last_error",
+    "mgp_displacement_fields", "mgp_get_displacements", "mgp_kick_drift", "mgp_step", "mgp_run", "mgp_pofk",
+    "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
+    "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_launch_count",
+    "mgp_host_register", "mgp_host_unregister",
+]
+
+
+class Params(C.Structure):
+    """struct mgp_params (include/mgpicola.h); field names are the
+    reference's parameter-file keys."""
+    _fields_ = [
+        ("model", C.c_int), ("smoothing_filter", C.c_int), ("use_w0wa", C.c_int), ("scaledependent", C.c_int),
+        ("modified_gravity_active", C.c_int), ("include_screening", C.c_int),
+        ("use_lcdm_growth_factors", C.c_int), ("input_pofk_is_for_lcdm", C.c_int),
+        ("input_sigma8_is_for_lcdm", C.c_int), ("inverted_initial_condition", C.c_int),
+        ("amplitude_fixed_initial_condition", C.c_int),
+        ("fofr0", C.c_double), ("nfofr", C.c_double), ("Rsmooth", C.c_double), ("rcH0_DGP", C.c_double),
+        ("wBD", C.c_double), ("Omegah2", C.c_double), ("Omegarh2", C.c_double), ("Omegavh2", C.c_double),
+        ("range_symm", C.c_double), ("assb_symm", C.c_double), ("beta_symm", C.c_double),
+        ("w_0", C.c_double), ("w_a", C.c_double),
+        ("pofk_compute_every_step", C.c_int), ("pofk_compute_rsd_pofk", C.c_int), ("pofk_nbins", C.c_int),
+        ("pofk_bintype", C.c_int), ("pofk_subtract_shotnoise", C.c_int),
+        ("pofk_kmin", C.c_double), ("pofk_kmax", C.c_double),
+        ("OutputDir", C.c_char * 500), ("FileBase", C.c_char * 500), ("OutputRedshiftFile", C.c_char * 500),
+        ("NumFilesWrittenInParallel", C.c_int),
+        ("UseCOLA", C.c_int), ("Buffer", C.c_double), ("Nmesh", C.c_int), ("Nsample", C.c_int),
+        ("Box", C.c_double), ("Init_Redshift", C.c_double), ("Seed", C.c_int), ("SphereMode", C.c_int),
+        ("WhichSpectrum", C.c_int), ("WhichTransfer", C.c_int),
+        ("FileWithInputSpectrum", C.c_char * 500), ("FileWithInputTransfer", C.c_char * 500),
+        ("Omega", C.c_double), ("OmegaBaryon", C.c_double), ("HubbleParam", C.c_double), ("Sigma8", C.c_double),
+        ("PrimordialIndex", C.c_double),
+        ("UnitLength_in_cm", C.c_double), ("UnitMass_in_g", C.c_double), ("UnitVelocity_in_cm_per_s", C.c_double),
+        ("InputSpectrum_UnitLength_in_cm", C.c_double),
+        ("Noutputs", C.c_int), ("output_redshift", C.c_double * 64), ("output_nsteps", C.c_int * 64),
+    ]
+
+
+class MGPError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("mgp error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load libmgpicola.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError("libmgpicola.so not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L.mgp_last_error.restype = C.c_char_p
+        L.mgp_params_default.argtypes = [C.POINTER(Params)]
+        L.mgp_read_parameterfile.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(Params)]
+        L.mgp_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
+        L.mgp_destroy.argtypes = [vp]
+        L.mgp_displacement_fields.argtypes = [vp]
+        L.mgp_get_displacements.argtypes = [vp, C.c_double]
+        L.mgp_kick_drift.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+        L.mgp_step.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
+        L.mgp_run.argtypes = [vp, C.c_int]
+        dp = C.POINTER(C.c_double)
+        L.mgp_pofk.argtypes = [vp, C.c_int, C.POINTER(C.c_int), dp, dp, dp, dp]
+        L.mgp_pofk_rsd.argtypes = [vp, C.c_double, C.c_int, C.POINTER(C.c_int)] + [dp] * 8
+        L.mgp_get_particles.argtypes = [vp, vp, vp, vp, vp, C.c_size_t]
+        L.mgp_set_particles.argtypes = [vp, vp, vp, vp, vp, C.c_size_t]
+        L.mgp_step_host.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, vp, vp, vp, vp, C.c_size_t]
+        for f in ("mgp_growth",):
+            getattr(L, f).argtypes = [vp, C.c_int, C.c_double]
+            getattr(L, f).restype = C.c_double
+        for f in ("mgp_Sq", "mgp_Sphi"):
+            getattr(L, f).argtypes = [vp, C.c_double, C.c_double, C.c_double]
+            getattr(L, f).restype = C.c_double
+        L.mgp_cosmo_eval.argtypes = [C.POINTER(Params), C.c_int, dp, C.c_int, dp]
+        L.mgp_cosmo_coeff.argtypes = [C.POINTER(Params), C.c_int, dp, dp, dp, C.c_int, dp]
+        L.mgp_power_spectrum.argtypes = [vp, C.c_double]
+        L.mgp_power_spectrum.restype = C.c_double
+        L.mgp_copy_grid.argtypes = [vp, C.c_int, fp, C.c_size_t]
+        L.mgp_set_timing.argtypes = [vp, C.c_int]
+        L.mgp_kernel_ms.argtypes = [vp, C.c_char_p]
+        L.mgp_kernel_ms.restype = C.c_double
+        L.mgp_launch_count.argtypes = [vp]
+        L.mgp_launch_count.restype = C.c_longlong
+        L.mgp_host_register.argtypes = [vp, C.c_size_t]
+        L.mgp_host_unregister.argtypes = [vp]
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise MGPError(rc, lib().mgp_last_error().decode(errors="replace"))
+
+
+def default_params(**kw):
+    p = Params()
+    _check(lib().mgp_params_default(C.byref(p)))
+    for k, v in kw.items():
+        if isinstance(getattr(p, k), bytes):
+            v = v.encode() if isinstance(v, str) else v
+        setattr(p, k, v)
+    return p
+
+
+def read_parameterfile(fname, model=MODEL_LCDM, pofk_keys=True, read_outputs=True, use_w0wa=False):
+    """read_parameterfile + read_outputs of the reference."""
+    p = Params()
+    p.use_w0wa = 1 if use_w0wa else 0
+    _check(lib().mgp_read_parameterfile(fname.encode(), model, 1 if pofk_keys else 0, 1 if read_outputs else 0,
+                                        C.byref(p)))
+    return p
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def cosmo_eval(params, which, x):
+    """Host-only growth factors (which 0-6) or P(k) (which 7)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros_like(x)
+    _check(lib().mgp_cosmo_eval(C.byref(params), which, _dptr(x), x.size, _dptr(out)))
+    return out
+
+
+def cosmo_coeff(params, kind, ai, af, aref):
+    """COLA Sq (kind 0) / Sphi (kind 1) on the host."""
+    ai, af, aref = (np.ascontiguousarray(v, dtype=np.float64) for v in (ai, af, aref))
+    out = np.zeros_like(ai)
+    _check(lib().mgp_cosmo_coeff(C.byref(params), kind, _dptr(ai), _dptr(af), _dptr(aref), ai.size, _dptr(out)))
+    return out
+
+
+def pin(arr):
+    """Page-lock a numpy array for fast host<->device copies."""
+    _check(lib().mgp_host_register(arr.ctypes.data, arr.nbytes))
+
+
+def unpin(arr):
+    _check(lib().mgp_host_unregister(arr.ctypes.data))
+
+
+class Context:
+    """One simulation box on one GPU (mgp_ctx)."""
+
+    def __init__(self, params, device=0):
+        self.params = params
+        self.h = C.c_void_p()
+        _check(lib().mgp_create(C.byref(params), device, C.byref(self.h)))
+        self.N = params.Nmesh
+        self.Ns = params.Nsample
+        self.np = params.Nsample ** 3
+
+    def close(self):
+        if self.h:
+            lib().mgp_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # reference entry points
+    def displacement_fields(self):
+        _check(lib().mgp_displacement_fields(self.h))
+
+    def get_displacements(self, A):
+        _check(lib().mgp_get_displacements(self.h, A))
+
+    def kick_drift(self, AI, AF, A, AFF, drift=True):
+        _check(lib().mgp_kick_drift(self.h, AI, AF, A, AFF, 1 if drift else 0))
+
+    def step(self, A, AI, AF, AFF):
+        _check(lib().mgp_step(self.h, A, AI, AF, AFF))
+
+    def run(self, gadget=True):
+        _check(lib().mgp_run(self.h, 1 if gadget else 0))
+
+    def pofk(self):
+        cap = max(self.params.pofk_nbins, self.N, 1)
+        k, pk, km, n = (np.zeros(cap) for _ in range(4))
+        nb = C.c_int(0)
+        _check(lib().mgp_pofk(self.h, cap, C.byref(nb), _dptr(k), _dptr(pk), _dptr(km), _dptr(n)))
+        m = nb.value
+        return k[:m], pk[:m], km[:m], n[:m]
+
+    def get_particles(self):
+        pos = np.zeros((self.np, 3), np.float32)
+        vel = np.zeros((self.np, 3), np.float32)
+        d1 = np.zeros((self.np, 3), np.float32)
+        d2 = np.zeros((self.np, 3), np.float32)
+        _check(lib().mgp_get_particles(self.h, pos.ctypes.data, vel.ctypes.data, d1.ctypes.data, d2.ctypes.data,
+                                       self.np))
+        return pos, vel, d1, d2
+
+    def set_particles(self, pos=None, vel=None, d1=None, d2=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32) for a in (pos, vel, d1, d2)]
+        ptrs = [None if a is None else a.ctypes.data for a in arrs]
+        _check(lib().mgp_set_particles(self.h, *ptrs, self.np))
+
+    def step_host(self, A, AI, AF, AFF, pos, vel, d1, d2):
+        _check(lib().mgp_step_host(self.h, A, AI, AF, AFF, pos.ctypes.data, vel.ctypes.data, d1.ctypes.data,
+                                   d2.ctypes.data, self.np))
+
+    def grid(self, which):
+        n = self.N * self.N * 2 * (self.N // 2 + 1)
+        out = np.zeros(n, np.float32)
+        _check(lib().mgp_copy_grid(self.h, which, out, n))
+        return out.reshape(self.N, self.N, 2 * (self.N // 2 + 1))
+
+    def growth(self, which, a):
+        return lib().mgp_growth(self.h, which, a)
+
+    def Sq(self, ai, af, aref):
+        return lib().mgp_Sq(self.h, ai, af, aref)
+
+    def Sphi(self, ai, af, aref):
+        return lib().mgp_Sphi(self.h, ai, af, aref)
+
+    def power(self, k):
+        return lib().mgp_power_spectrum(self.h, k)
+
+    def set_timing(self, on=True):
+        _check(lib().mgp_set_timing(self.h, 1 if on else 0))
+
+    def kernel_ms(self, name):
+        return lib().mgp_kernel_ms(self.h, name.encode())
+
+    def launches(self):
+        return lib().mgp_launch_count(self.h)

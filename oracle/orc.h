@@ -1,0 +1,190 @@
+/*
+ * FP64 CPU oracle for the MG-PICOLA COLA particle-mesh step and 2LPT initial
+ * conditions.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links, loads or
+ * calls this code; it is the checker that the CUDA path is compared against
+ * (tests/, __graft_entry__.smoke() and the cpu_baseline / reference legs of
+ * bench.py).  Every routine restates one reference routine in double
+ * precision and cites it (paths are relative to the MG-PICOLA-PUBLIC tree).
+ *
+ * Conventions shared with the reference (src/vars.h:292-353 with MEMORY_MODE
+ * off, SINGLE_PRECISION off):
+ *   - particle arrays are AoS [np][3] doubles (P[i].Pos[3] etc.);
+ *   - real grids use the FFTW in-place padded layout [N][N][2(N/2+1)];
+ *   - complex grids are [N][N][N/2+1] interleaved (re, im);
+ *   - FFTs are unnormalised, forward sign -1, backward sign +1.
+ *
+ * Parity status: pinned against the reference's own sources compiled with
+ * project-written single-rank shims (oracle/ref_shim, output in oracle/_ref)
+ * where that build succeeds; see tests/golden/make_golden.py.
+ */
+#ifndef MGP_ORACLE_H
+#define MGP_ORACLE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- RNG */
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).  Used as the
+ * project-defined stand-in for gsl_rng_ranlxd1 in the IC generator. */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* One uniform double in [0,1): draw number `n` of the stream seeded by `seed`. */
+double orc_stream_uniform(uint32_t seed, uint64_t n);
+
+/* ---------------------------------------------------------------- FFT */
+/* In-place 3D real FFTs on an [N][N][2(N/2+1)] double grid, FFTW semantics.
+ * Backward (c2r) uses only Re of the kz=0 and kz=N/2 entries after the x/y
+ * passes, as a real-output half-complex transform does. */
+void orc_fft_r2c(int N, double *grid);
+void orc_fft_c2r(int N, double *grid);
+/* 1D complex FFT helper for tests (sign -1 forward, +1 backward). */
+void orc_fft1d(int n, double *data_interleaved, int sign);
+
+/* ------------------------------------------------------------ PM step */
+/* PtoMesh (src/auxPM.c:280-357): density = -1 + CIC(pos) * (N/Ns)^3. */
+void orc_cic(const double *pos, long np, int N, int Ns, double box, double *grid);
+/* CIC with positions taken as q + disp (lattice q) -- same arithmetic as
+ * orc_cic on pos = wrap(q + disp); convenience for tests. */
+void orc_lattice_positions(const double *disp, int Ns, double box, double *pos);
+
+/* Forces k-space pass (src/auxPM.c:437-535): from delta(k) (+ optional MG
+ * source added first, auxPM.c:450-455) produce the three complex force grids. */
+void orc_forces_kspace(const double *deltak, const double *mgk, int N, double box,
+                       double *f1, double *f2, double *f3);
+/* MtoParticles (src/auxPM.c:560-644); returns per-particle Disp and mean. */
+void orc_interp(const double *f1, const double *f2, const double *f3, int N, double box,
+                const double *pos, long np, double *disp, double mean_out[3]);
+/* Kick (src/main.c:688-742) for scale-independent growth. */
+void orc_kick(long np, double *vel, double *disp, const double *D1, const double *D2,
+              const double sumD[3], double omega, double dda, double ddD, double ddD2,
+              double A, int usecola, double sumv_out[3]);
+/* Drift (src/main.c:747-787) for scale-independent growth. */
+void orc_drift(long np, double *pos, const double *vel, const double *D1, const double *D2,
+               const double sumv[3], double dyyy, double dD, double dD2, int usecola, double box);
+double orc_periodic_wrap(double x, double box);
+
+/* compute_power_spectrum (src/compute_pofk.c:71-271).  kmin/kmax in h/Mpc as
+ * in the parameter file; the k_bin/P/k_mean/n arrays have `nbins` entries
+ * (after adjust_pofk_parameters, compute_pofk.c:758-805, which may change
+ * nbins: pass capacity in *nbins_io, get the used count back). */
+int orc_pofk(const double *deltak, int N, int Ns, double box, int *nbins_io, int bintype,
+             int subtract_shotnoise, double kmin_hmpc, double kmax_hmpc,
+             double *kbin, double *pk, double *kmean, double *nmodes);
+
+/* RSD multipoles of one line of sight (compute_pofk.c:518-753).  The
+ * LOS axis must be 1 (y) or 2 (z).  vel_los_extra is the per-particle LPT
+ * velocity added for COLA (main.c:959-967 form), may be NULL. */
+int orc_pofk_rsd_axis(const double *pos, const double *vel, const double *vel_extra, long np,
+                      int axis, int N, int Ns, double box, double vnorm,
+                      int *nbins_io, int bintype, int subtract_shotnoise,
+                      double kmin_hmpc, double kmax_hmpc,
+                      double *k, double *P0, double *P2, double *P4, double *n);
+
+/* ------------------------------------------------------- MG screening */
+/* Model ids (compile-time MODEL switch in the reference Makefile:61-106). */
+enum { ORC_LCDM = 0, ORC_FOFR = 1, ORC_DGP = 2, ORC_JBD_GEFF = 3, ORC_MBETA = 4 };
+
+typedef struct {
+  int model;
+  int mg_active, include_screening, use_lcdm_growth;
+  double omega;            /* Omega_m */
+  double fofr0, nfofr;     /* Hu-Sawicki (user_defined_functions.h:490-500) */
+  double rcH0, rsmooth;    /* nDGP (user_defined_functions.h:453, mg.h:197-260) */
+  double geff_const;       /* Geff/G(a) for the time-dependent-Geff path */
+  double w0, wa; int use_w0wa;
+  /* m(a)/beta(a) symmetron example (user_defined_functions.h:462-484) */
+  double beta_symm, assb_symm, range_symm;
+  int smoothing_filter;    /* 0 none, 1 gaussian, 2 tophat, 3 sharpk */
+} orc_mg;
+
+double orc_hubble(const orc_mg *m, double a);
+double orc_dhubbleda(const orc_mg *m, double a);
+double orc_beta_dgp(const orc_mg *m, double a);
+double orc_beta_of_a(const orc_mg *m, double a);
+double orc_mass2_of_a(const orc_mg *m, double a);
+double orc_coupling(const orc_mg *m, double a);
+double orc_geff(const orc_mg *m, double a, double k);
+double orc_factor_2lpt(const orc_mg *m, double a);
+double orc_screen_potential(const orc_mg *m, double a, double phinewton);
+double orc_screen_density(const orc_mg *m, double a, double density);
+
+/* ComputeFifthForce (user_defined_functions.h:687-719 + src/mg.h).
+ * density_x: real-space density copy (CopyDensityArray), deltak: P3D.
+ * Writes the complex MG source to mgk (P3D_mgarray_two) when the model uses
+ * MG arrays; multiplies deltak in place for the time-dependent Geff path. */
+void orc_fifth_force(const orc_mg *m, double a, int N, double box,
+                     const double *density_x, double *deltak, double *mgk);
+
+/* ----------------------------------------------------------- cosmology */
+typedef struct orc_cosmo orc_cosmo;
+/* Growth ODEs (src/cosmo.c:206-643) on a fine fixed-step RK4 grid. */
+orc_cosmo *orc_cosmo_create(const orc_mg *m, double init_redshift);
+void orc_cosmo_free(orc_cosmo *c);
+double orc_growth_D(orc_cosmo *c, double a);
+double orc_growth_dDdy(orc_cosmo *c, double a);
+double orc_growth_ddDddy(orc_cosmo *c, double a);
+double orc_growth_D2(orc_cosmo *c, double a);
+double orc_growth_dD2dy(orc_cosmo *c, double a);
+double orc_growth_ddD2ddy(orc_cosmo *c, double a);
+double orc_growth_DLCDM(orc_cosmo *c, double a);
+/* COLA coefficients (src/cosmo.c:1114-1160), nLPT = -2.5, fullT = 1. */
+double orc_Sq(orc_cosmo *c, double ai, double af, double aref);
+double orc_Sphi(orc_cosmo *c, double ai, double af, double aref);
+/* LCDM fitting functions (src/cosmo.c:1291-1398) -- known-answer checks. */
+double orc_growthD_fit(double omega, double a);
+
+/* Linear power spectrum (src/power.c:373-498). */
+typedef struct {
+  int which_spectrum;       /* 0 transfer-function, 1 tabulated, else EH */
+  double omega, omega_b, h, ns, sigma8;
+  int ntab; const double *tab_logk, *tab_logP;   /* log10 table for type 1 */
+  double norm;              /* filled by orc_power_init */
+} orc_power;
+void orc_power_init(orc_power *p);
+double orc_power_spec(const orc_power *p, double k);
+double orc_tophat_sigma2(const orc_power *p, double R);
+double orc_transfer_eh(const orc_power *p, double k);
+
+/* ------------------------------------------------------------------ IC */
+typedef struct {
+  int N, Ns; double box; uint32_t seed; int sphere_mode;
+  int fixed_amplitude, inverted;
+  double pofk_rescale;      /* mg_pofk_ratio * sigma8 factor, scale-independent */
+} orc_ic_params;
+/* Seed table exactly in the order of src/2LPT.c:262-271. */
+void orc_seedtable(int N, uint32_t seed, uint32_t *table);
+/* displacement_fields() Gaussian + 2LPT (src/2LPT.c:185-495,1209-1519):
+ * writes ZA (D1) and 2LPT (D2, already times -3/7) displacements per
+ * particle [Ns^3][3], means removed.  Also returns delta(k) and the 2LPT
+ * source(k) (cdelta_cdm / cdelta_cdm2 of the SCALEDEPENDENT build) if the
+ * pointers are non-NULL. */
+void orc_ic_2lpt(const orc_ic_params *ip, const orc_power *pw, double *D1, double *D2,
+                 double *deltak_out, double *source2k_out);
+
+/* --------------------------------------------------------- full run */
+typedef struct {
+  orc_mg mg; orc_power pw; orc_ic_params ic;
+  double init_redshift;
+  int nsteps; double final_redshift;       /* one output at the end */
+  int pofk_nbins, pofk_bintype, pofk_subtract_shotnoise;
+  double pofk_kmin, pofk_kmax;
+  int usecola;
+} orc_run_params;
+/* Runs IC + the KDK loop of src/main.c:394-611 for one output redshift.
+ * pos/vel out [Ns^3][3] at the final time (vel incl. LPT part as written by
+ * Output, main.c:959-967, in code units before velfac*fac); pk arrays sized
+ * pofk_nbins.  Returns number of P(k) bins. */
+int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
+            double *kbin, double *pk, double *kmean, double *nmodes);
+
+/* CPU baseline timing: seconds per KDK step after an untimed IC. */
+double orc_time_steps(const orc_run_params *rp, int nsteps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,426 @@
+/*
+ * Oracle cosmology (test infrastructure only): model hooks of
+ * src/user_defined_functions.h, growth ODEs of src/cosmo.c, COLA time-step
+ * coefficients and the linear power spectrum of src/power.c, all FP64.
+ *
+ * Third-party numerics the reference takes from GSL are replaced here by
+ * textbook methods: the growth ODE (GSL odeiv2 rk2, eps 1e-7, cosmo.c:460-463)
+ * is integrated with a fixed-step classical RK4 at 64 sub-steps per knot;
+ * quadratures (GSL qag) use adaptive 20-point Gauss-Legendre bisection to a
+ * 1e-12 relative tolerance; splines are natural cubic (GSL cspline).
+ */
+#include "orc.h"
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define INVERSE_H0_MPCH 2997.92458 /* src/vars.h:65 */
+
+/* ---------------------------------------------------------------- hooks */
+/* hubble: user_defined_functions.h:413-429 */
+double orc_hubble(const orc_mg *m, double a) {
+  if (m->use_w0wa)
+    return sqrt(m->omega / (a * a * a) + (1.0 - m->omega) * exp(3.0 * m->wa * (a - 1) - 3 * (1 + m->w0 + m->wa) * log(a)));
+  return sqrt(m->omega / (a * a * a) + 1.0 - m->omega);
+}
+/* dhubbleda: user_defined_functions.h:431-447 */
+double orc_dhubbleda(const orc_mg *m, double a) {
+  if (m->use_w0wa)
+    return 1.0 / (2.0 * orc_hubble(m, a)) *
+           (-3.0 * m->omega / (a * a * a * a) - 3.0 * (1.0 - m->omega) * (1.0 + m->w0 + m->wa * (1 - a)) / a);
+  return 1.0 / (2.0 * orc_hubble(m, a)) * (-3.0 * m->omega / (a * a * a * a));
+}
+/* beta_DGP: user_defined_functions.h:453-455 */
+double orc_beta_dgp(const orc_mg *m, double a) {
+  return 1.0 + 2.0 * m->rcH0 * (orc_hubble(m, a) + a * orc_dhubbleda(m, a) / 3.0);
+}
+/* beta_of_a: user_defined_functions.h:462-484 */
+double orc_beta_of_a(const orc_mg *m, double a) {
+  if (m->model == ORC_FOFR) return 1.0 / sqrt(6.0);
+  if (m->model == ORC_MBETA) {
+    if (a > m->assb_symm) return m->beta_symm * sqrt(1.0 - pow(m->assb_symm / a, 3));
+    return 0.0;
+  }
+  return 0.0;
+}
+/* mass2_of_a: user_defined_functions.h:490-522 */
+double orc_mass2_of_a(const orc_mg *m, double a) {
+  if (m->model == ORC_FOFR) {
+    double a3 = a * a * a;
+    double fac = m->omega / a3 + 4.0 * (1.0 - m->omega);
+    double fac0 = m->omega + 4.0 * (1.0 - m->omega);
+    return fac0 * pow(fac / fac0, m->nfofr + 2.0) / ((1.0 + m->nfofr) * m->fofr0);
+  }
+  if (m->model == ORC_MBETA) {
+    if (a > m->assb_symm) return 0.5 * pow(2998.0 / m->range_symm, 2) * (1.0 - pow(m->assb_symm / a, 3));
+    return 1.0;
+  }
+  return 0.0;
+}
+/* coupling_function: user_defined_functions.h:587-611 */
+double orc_coupling(const orc_mg *m, double a) {
+  if (m->model == ORC_FOFR || m->model == ORC_MBETA) return 2.0 * orc_beta_of_a(m, a) * orc_beta_of_a(m, a);
+  if (m->model == ORC_DGP) return 1.0 / (3.0 * orc_beta_dgp(m, a));
+  if (m->model == ORC_JBD_GEFF) return m->geff_const - 1.0;
+  return 0.0;
+}
+/* GeffoverG: user_defined_functions.h:618-652 */
+double orc_geff(const orc_mg *m, double a, double k) {
+  double mu = 1.0;
+  if (!m->mg_active) return mu;
+  if (m->use_lcdm_growth) return mu;
+  if (m->model == ORC_FOFR || m->model == ORC_MBETA) {
+    double mass2a2 = a * a * orc_mass2_of_a(m, a);
+    double k2 = pow(k * INVERSE_H0_MPCH, 2);
+    if (k2 == 0) return mu;
+    mu *= 1.0 + 2.0 * orc_beta_of_a(m, a) * orc_beta_of_a(m, a) * k2 / (k2 + mass2a2);
+    return mu;
+  }
+  if (m->model == ORC_DGP) return mu * (1.0 + 1.0 / (3.0 * orc_beta_dgp(m, a)));
+  if (m->model == ORC_JBD_GEFF) return mu * (1.0 + orc_coupling(m, a));
+  return mu;
+}
+/* Factor_2LPT: user_defined_functions.h:814-838 */
+double orc_factor_2lpt(const orc_mg *m, double a) {
+  if (!m->mg_active || m->use_lcdm_growth) return 1.0;
+  if (m->model == ORC_DGP) {
+    double b = orc_beta_dgp(m, a);
+    return 1.0 - (2.0 * m->rcH0 * m->rcH0 * m->omega) / (9.0 * a * a * a * pow(b, 3) * (1 + 1.0 / (3.0 * b)));
+  }
+  return 1.0;
+}
+/* screening_factor_potential: user_defined_functions.h:725-750 (f(R)) */
+double orc_screen_potential(const orc_mg *m, double a, double phinewton) {
+  if (!m->include_screening) return 1.0;
+  if (phinewton >= 0.0) return 1.0;
+  if (m->model == ORC_FOFR) {
+    double phicrit = 1.5 * m->fofr0 *
+                     pow((m->omega + 4.0 * (1.0 - m->omega)) / (1.0 / (a * a * a) * m->omega + 4.0 * (1.0 - m->omega)), m->nfofr + 1.0);
+    double s = fabs(phicrit / phinewton);
+    return s > 1.0 ? 1.0 : s;
+  }
+  return 1.0;
+}
+/* screening_factor_density: user_defined_functions.h:757-773 (nDGP) */
+double orc_screen_density(const orc_mg *m, double a, double density) {
+  if (!m->include_screening) return 1.0;
+  if (m->model == ORC_DGP) {
+    double fac = 8.0 / 9.0 * m->omega * pow(m->rcH0 / orc_beta_dgp(m, a), 2) * (1.0 + density);
+    if (fac < 1e-5) return 1.0;
+    return 2.0 * (sqrt(1.0 + fac) - 1.0) / fac;
+  }
+  return 1.0;
+}
+
+/* ------------------------------------------------------------- splines */
+typedef struct { int n; double *x, *y, *y2; } spline1;
+
+static void spline_init(spline1 *s, const double *x, const double *y, int n) {
+  s->n = n;
+  s->x = malloc(8 * n); s->y = malloc(8 * n); s->y2 = calloc(n, 8);
+  memcpy(s->x, x, 8 * n); memcpy(s->y, y, 8 * n);
+  double *u = calloc(n, 8);
+  /* natural cubic spline, tridiagonal solve */
+  for (int i = 1; i < n - 1; i++) {
+    double sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+    double p = sig * s->y2[i - 1] + 2.0;
+    s->y2[i] = (sig - 1.0) / p;
+    u[i] = (y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]);
+    u[i] = (6.0 * u[i] / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / p;
+  }
+  s->y2[n - 1] = 0.0;
+  for (int k = n - 2; k >= 0; k--) s->y2[k] = s->y2[k] * s->y2[k + 1] + u[k];
+  free(u);
+}
+
+/* Clamped lookup as Lookup_GSL_Spline (src/wrappers.c:162-167). */
+static double spline_eval(const spline1 *s, double x) {
+  if (x < s->x[0]) x = s->x[0];
+  if (x > s->x[s->n - 1]) x = s->x[s->n - 1];
+  int lo = 0, hi = s->n - 1;
+  while (hi - lo > 1) { int mid = (hi + lo) / 2; if (s->x[mid] > x) hi = mid; else lo = mid; }
+  double h = s->x[hi] - s->x[lo];
+  double A = (s->x[hi] - x) / h, B = (x - s->x[lo]) / h;
+  return A * s->y[lo] + B * s->y[hi] + ((A * A * A - A) * s->y2[lo] + (B * B * B - B) * s->y2[hi]) * (h * h) / 6.0;
+}
+static void spline_free(spline1 *s) { free(s->x); free(s->y); free(s->y2); }
+
+/* ---------------------------------------------------------- quadrature */
+static const double GL20_X[10] = {0.0765265211334973, 0.2277858511416451, 0.3737060887154195,
+                                  0.5108670019508271, 0.6360536807265150, 0.7463319064601508,
+                                  0.8391169718222188, 0.9122344282513259, 0.9639719272779138,
+                                  0.9931285991850949};
+static const double GL20_W[10] = {0.1527533871307258, 0.1491729864726037, 0.1420961093183820,
+                                  0.1316886384491766, 0.1181945319615184, 0.1019301198172404,
+                                  0.0832767415767048, 0.0626720483341091, 0.0406014298003869,
+                                  0.0176140071391521};
+/* Nodes above are printed to 16 digits; refine them by Newton on P_20. */
+static double glx[10], glw[10];
+static int gl_ready = 0;
+static void gl_init(void) {
+  if (gl_ready) return;
+  for (int i = 0; i < 10; i++) {
+    double x = GL20_X[i], dp = 0;
+    for (int it = 0; it < 8; it++) {
+      double p0 = 1.0, p1 = x;
+      for (int n = 2; n <= 20; n++) { double p2 = ((2 * n - 1) * x * p1 - (n - 1) * p0) / n; p0 = p1; p1 = p2; }
+      dp = 20 * (x * p1 - p0) / (x * x - 1.0);
+      x -= p1 / dp;
+    }
+    glx[i] = x;
+    glw[i] = 2.0 / ((1.0 - x * x) * dp * dp);
+  }
+  (void)GL20_W;
+  gl_ready = 1;
+}
+typedef double (*fn1)(double, void *);
+static double gl20(fn1 f, void *par, double a, double b) {
+  double c = 0.5 * (a + b), h = 0.5 * (b - a), s = 0;
+  for (int i = 0; i < 10; i++) s += glw[i] * (f(c - h * glx[i], par) + f(c + h * glx[i], par));
+  return s * h;
+}
+static double adapt(fn1 f, void *par, double a, double b, double whole, double abstol, int depth) {
+  double c = 0.5 * (a + b);
+  double l = gl20(f, par, a, c), r = gl20(f, par, c, b);
+  if (depth >= 16 || fabs(l + r - whole) <= abstol) return l + r;
+  return adapt(f, par, a, c, l, 0.5 * abstol, depth + 1) + adapt(f, par, c, b, r, 0.5 * abstol, depth + 1);
+}
+static double integrate(fn1 f, void *par, double a, double b) {
+  gl_init();
+  /* 8 starting panels so oscillatory integrands are resolved; the absolute
+   * tolerance is 1e-13 of the first estimate of the whole integral */
+  double est[8], tot = 0;
+  for (int i = 0; i < 8; i++) {
+    est[i] = gl20(f, par, a + (b - a) * i / 8.0, a + (b - a) * (i + 1) / 8.0);
+    tot += fabs(est[i]);
+  }
+  double s = 0, tol = 1e-13 * tot / 8.0 + 1e-300;
+  for (int i = 0; i < 8; i++)
+    s += adapt(f, par, a + (b - a) * i / 8.0, a + (b - a) * (i + 1) / 8.0, est[i], tol, 0);
+  return s;
+}
+
+/* --------------------------------------------------------- growth ODEs */
+struct orc_cosmo {
+  orc_mg m;
+  spline1 D, dDdy, ddDddy, D2, dD2dy, ddD2ddy, DLCDM;
+};
+
+/* ode_growth_D (cosmo.c:206-239), non-SCALEDEPENDENT modfac = Factor_2LPT;
+ * lcdm = 1 gives ode_growth_DLCDM (cosmo.c:245-268). k = 1e-3 h/Mpc as in
+ * solve_for_growth_factors (cosmo.c:456). */
+static void growth_rhs(const orc_mg *m, int lcdm, double x, const double *D, double *dD) {
+  double a = exp(x);
+  double k = 1e-3;
+  double mu = lcdm ? 1.0 : orc_geff(m, a, k);
+  double H = orc_hubble(m, a), dH = orc_dhubbleda(m, a);
+  double betafac = 1.5 * m->omega * mu / (a * a * a * H * H);
+  double alphafac = 2.0 + a * dH / H;
+  double modfac = lcdm ? 1.0 : orc_factor_2lpt(m, a);
+  dD[0] = D[1];
+  dD[1] = -alphafac * D[1] + betafac * D[0];
+  dD[2] = D[3];
+  dD[3] = -alphafac * D[3] + betafac * (D[2] - modfac * D[0] * D[0]);
+}
+
+static void rk4(const orc_mg *m, int lcdm, double x0, double x1, int nsub, double *y) {
+  double h = (x1 - x0) / nsub;
+  for (int s = 0; s < nsub; s++) {
+    double x = x0 + s * h, k1[4], k2[4], k3[4], k4[4], t[4];
+    growth_rhs(m, lcdm, x, y, k1);
+    for (int i = 0; i < 4; i++) t[i] = y[i] + 0.5 * h * k1[i];
+    growth_rhs(m, lcdm, x + 0.5 * h, t, k2);
+    for (int i = 0; i < 4; i++) t[i] = y[i] + 0.5 * h * k2[i];
+    growth_rhs(m, lcdm, x + 0.5 * h, t, k3);
+    for (int i = 0; i < 4; i++) t[i] = y[i] + h * k3[i];
+    growth_rhs(m, lcdm, x + h, t, k4);
+    for (int i = 0; i < 4; i++) y[i] += h / 6.0 * (k1[i] + 2 * k2[i] + 2 * k3[i] + k4[i]);
+  }
+}
+
+static double Qfactor(const orc_mg *m, double a) { return orc_hubble(m, a) * a * a * a; }
+
+/* solve_for_growth_factors (cosmo.c:409-643) */
+orc_cosmo *orc_cosmo_create(const orc_mg *m, double init_redshift) {
+  orc_cosmo *c = calloc(1, sizeof(orc_cosmo));
+  c->m = *m;
+  const int npts = 1000;
+  double zini = init_redshift > 200.0 ? init_redshift : 200.0, zend = -0.5;
+  double aini = 1.0 / (1.0 + zini), xini = log(aini), xend = log(1.0 / (1.0 + zend));
+  double dx = (xend - xini) / (double)(npts - 1);
+  double *x = malloc(8 * npts), *D = malloc(8 * npts), *dD = malloc(8 * npts), *ddD = malloc(8 * npts);
+  double *D2 = malloc(8 * npts), *dD2 = malloc(8 * npts), *ddD2 = malloc(8 * npts), *DL = malloc(8 * npts);
+  double y[4] = {1.0, 1.0, -3.0 / 7.0, -6.0 / 7.0}, yl[4] = {1.0, 1.0, -3.0 / 7.0, -6.0 / 7.0};
+  for (int i = 0; i < npts; i++) {
+    double xnow = xini + i * dx;
+    if (i > 0) {
+      rk4(m, 0, xini + (i - 1) * dx, xnow, 64, y);
+      rk4(m, 1, xini + (i - 1) * dx, xnow, 64, yl);
+    }
+    double anow = exp(xnow), mu = orc_geff(m, anow, 1e-3);
+    x[i] = xnow;
+    D[i] = y[0];
+    dD[i] = y[1] * Qfactor(m, anow) / anow;
+    ddD[i] = 1.5 * mu * m->omega * anow * y[0];
+    D2[i] = y[2];
+    dD2[i] = y[3] * Qfactor(m, anow) / anow;
+    ddD2[i] = 1.5 * mu * m->omega * anow * (y[2] - y[0] * y[0] * orc_factor_2lpt(m, anow));
+    DL[i] = yl[0];
+  }
+  spline_init(&c->D, x, D, npts); spline_init(&c->dDdy, x, dD, npts); spline_init(&c->ddDddy, x, ddD, npts);
+  spline_init(&c->D2, x, D2, npts); spline_init(&c->dD2dy, x, dD2, npts); spline_init(&c->ddD2ddy, x, ddD2, npts);
+  spline_init(&c->DLCDM, x, DL, npts);
+  free(x); free(D); free(dD); free(ddD); free(D2); free(dD2); free(ddD2); free(DL);
+  return c;
+}
+void orc_cosmo_free(orc_cosmo *c) {
+  if (!c) return;
+  spline_free(&c->D); spline_free(&c->dDdy); spline_free(&c->ddDddy);
+  spline_free(&c->D2); spline_free(&c->dD2dy); spline_free(&c->ddD2ddy); spline_free(&c->DLCDM);
+  free(c);
+}
+/* growth_* lookups (cosmo.c:318-403), normalised at a = 1 */
+double orc_growth_D(orc_cosmo *c, double a) { return spline_eval(&c->D, log(a)) / spline_eval(&c->D, 0.0); }
+double orc_growth_dDdy(orc_cosmo *c, double a) { return spline_eval(&c->dDdy, log(a)) / spline_eval(&c->D, 0.0); }
+double orc_growth_ddDddy(orc_cosmo *c, double a) { return spline_eval(&c->ddDddy, log(a)) / spline_eval(&c->D, 0.0); }
+double orc_growth_D2(orc_cosmo *c, double a) { return spline_eval(&c->D2, log(a)) / spline_eval(&c->D2, 0.0); }
+double orc_growth_dD2dy(orc_cosmo *c, double a) { return spline_eval(&c->dD2dy, log(a)) / spline_eval(&c->D2, 0.0); }
+double orc_growth_ddD2ddy(orc_cosmo *c, double a) { return spline_eval(&c->ddD2ddy, log(a)) / spline_eval(&c->D2, 0.0); }
+double orc_growth_DLCDM(orc_cosmo *c, double a) { return spline_eval(&c->DLCDM, log(a)) / spline_eval(&c->DLCDM, 0.0); }
+
+/* COLA coefficients, cosmo.c:1114-1160 with nLPT = -2.5, fullT = 1
+ * (main.c:82-85). */
+static double gpQ(double a) { return pow(a, -2.5); }
+static double DERgpQ(double a) { return -2.5 * pow(a, -3.5); }
+static double sq_integrand(double a, void *p) { return gpQ(a) / Qfactor((const orc_mg *)p, a); }
+double orc_Sq(orc_cosmo *c, double ai, double af, double aref) {
+  return integrate(sq_integrand, &c->m, ai, af) / gpQ(aref);
+}
+double orc_Sphi(orc_cosmo *c, double ai, double af, double aref) {
+  return (gpQ(af) - gpQ(ai)) * aref / Qfactor(&c->m, aref) / DERgpQ(aref);
+}
+
+/* Gauss hypergeometric series 2F1(a,b;c;z), |z| < 1. */
+static double hyp2f1(double a, double b, double c, double z) {
+  double term = 1.0, sum = 1.0;
+  for (int n = 0; n < 2000000; n++) {
+    term *= (a + n) * (b + n) / ((c + n) * (n + 1.0)) * z;
+    sum += term;
+    if (fabs(term) < 1e-17 * fabs(sum)) break;
+  }
+  return sum;
+}
+/* growthDtemp, cosmo.c:1307-1356 (LCDM closed form). */
+static double growthDtemp(double Omega, double a) {
+  double hyperP = 0.0, hyperM = 0.0;
+  double x = -Omega / (Omega - 1.0) / (a * a * a);
+  if (fabs(x - 1.0) < 1.e-3) {
+    double t = -1.0 + x;
+    hyperP = 0.859596768064608 - 0.1016599912520404 * t + 0.025791094277821357 * pow(t, 2) -
+             0.008194025861121475 * pow(t, 3) + 0.0029076305993447644 * pow(t, 4) -
+             0.0011025426387159761 * pow(t, 5) + 0.00043707304964624546 * pow(t, 6) -
+             0.0001788889964687831 * pow(t, 7);
+    hyperM = 1.1765206505266006 + 0.15846194123099624 * t - 0.014200487494738975 * pow(t, 2) +
+             0.002801728034399257 * pow(t, 3) - 0.0007268267888593511 * pow(t, 4) +
+             0.00021801569226706922 * pow(t, 5) - 0.00007163321597397065 * pow(t, 6) +
+             0.000025063737576245116 * pow(t, 7);
+  } else {
+    if (x < 1.0) {
+      hyperP = hyp2f1(1.0 / 2.0, 2.0 / 3.0, 5.0 / 3.0, -x);
+      hyperM = hyp2f1(-1.0 / 2.0, 2.0 / 3.0, 5.0 / 3.0, -x);
+    }
+    x = 1.0 / x;
+    if ((x < 1.0) && (x > 1.0 / 30.0)) {
+      hyperP = hyp2f1(-1.0 / 6.0, 0.5, 5.0 / 6.0, -x);
+      hyperP *= 4 * sqrt(x);
+      hyperP += -3.4494794123063873799 * pow(x, 2.0 / 3.0);
+      hyperM = hyp2f1(-7.0 / 6.0, -0.5, -1.0 / 6.0, -x);
+      hyperM *= 4.0 / 7.0 / sqrt(x);
+      hyperM += pow(x, 2.0 / 3.0) * (-1.4783483195598803057);
+    }
+    if (x <= 1.0 / 30.0) {
+      hyperP = 4.0 * sqrt(x) - 3.4494794123063865 * pow(x, 2.0 / 3.0) + 0.4 * pow(x, 1.5) -
+               0.13636363636363635 * pow(x, 2.5) + 0.07352941176470587 * pow(x, 3.5) -
+               0.04755434782608695 * pow(x, 4.5) + 0.033943965517241374 * pow(x, 5.5) -
+               0.02578125 * pow(x, 6.5) + 0.020436356707317072 * pow(x, 7.5) -
+               0.01671324384973404 * pow(x, 8.5) + 0.013997779702240564 * pow(x, 9.5) -
+               0.011945562847590041 * pow(x, 10.5) + 0.01035003662109375 * pow(x, 11.5) -
+               0.009080577904069926 * pow(x, 12.5);
+      hyperM = 0.5714285714285715 / sqrt(x) + 2.0 * sqrt(x) - 1.4783483195598794 * pow(x, 2.0 / 3.0) +
+               0.1 * pow(x, 1.5) - 0.022727272727272735 * pow(x, 2.5) + 0.009191176470588237 * pow(x, 3.5) -
+               0.004755434782608697 * pow(x, 4.5) + 0.002828663793103449 * pow(x, 5.5) -
+               0.0018415178571428578 * pow(x, 6.5) + 0.0012772722942073172 * pow(x, 7.5) -
+               0.0009285135472074472 * pow(x, 8.5) + 0.0006998889851120285 * pow(x, 9.5) -
+               0.0005429801294359111 * pow(x, 10.5) + 0.0004312515258789064 * pow(x, 11.5) -
+               0.00034925299631038194 * pow(x, 12.5);
+    }
+  }
+  if (a > 0.2) {
+    return sqrt(1.0 + (-1.0 + pow(a, -3)) * Omega) *
+           (3.4494794123063873799 * pow(-1.0 + 1.0 / Omega, 2.0 / 3.0) +
+            (hyperP * (4 * pow(a, 3) * (-1.0 + Omega) - Omega) - 7.0 * pow(a, 3) * hyperM * (-1.0 + Omega)) /
+                (pow(a, 5) * (-1.0 + Omega) - pow(a, 2) * Omega));
+  }
+  return (a * pow(1 - Omega, 1.5) *
+          (1291467969 * pow(a, 12) * pow(-1 + Omega, 4) + 1956769650 * pow(a, 9) * pow(-1 + Omega, 3) * Omega +
+           8000000000 * pow(a, 3) * (-1 + Omega) * pow(Omega, 3) + 37490640625 * pow(Omega, 4))) /
+         (1.5625e10 * pow(Omega, 5));
+}
+double orc_growthD_fit(double omega, double a) { return growthDtemp(omega, a) / growthDtemp(omega, 1.0); }
+
+/* -------------------------------------------------------- power spectrum */
+/* TransferFunc_EH, src/power.c:447-476 (UnitLength = Mpc/h). */
+double orc_transfer_eh(const orc_power *p, double k) {
+  double hubble = p->h, omegam = p->omega, ombh2 = p->omega_b * p->h * p->h;
+  if (p->omega_b == 0) ombh2 = 0.04 * p->h * p->h;
+  double theta = 2.728 / 2.7;
+  double ommh2 = omegam * hubble * hubble;
+  double s = 44.5 * log(9.83 / ommh2) / sqrt(1. + 10. * exp(0.75 * log(ombh2))) * hubble;
+  double a = 1. - 0.328 * log(431. * ommh2) * ombh2 / ommh2 + 0.380 * log(22.3 * ommh2) * (ombh2 / ommh2) * (ombh2 / ommh2);
+  double gamma = a + (1. - a) / (1. + exp(4 * log(0.43 * k * s)));
+  gamma *= omegam * hubble;
+  double q = k * theta * theta / gamma;
+  double L0 = log(2. * exp(1.) + 1.8 * q);
+  double C0 = 14.2 + 731. / (1. + 62.5 * q);
+  return L0 / (L0 + C0 * q * q);
+}
+/* PowerSpec_Tabulated, src/power.c:399-435 */
+static double pk_tab(const orc_power *p, double k) {
+  double logk = log10(k);
+  if (logk < p->tab_logk[0] || logk > p->tab_logk[p->ntab - 1]) return 0;
+  int lo = 0, hi = p->ntab - 1;
+  while (hi - lo > 1) { int mid = (hi + lo) / 2; if (logk < p->tab_logk[mid]) hi = mid; else lo = mid; }
+  double u = (logk - p->tab_logk[lo]) / (p->tab_logk[hi] - p->tab_logk[lo]);
+  return p->norm * pow(10.0, (1 - u) * p->tab_logP[lo] + u * p->tab_logP[hi]);
+}
+/* PowerSpec, src/power.c:373-394 */
+double orc_power_spec(const orc_power *p, double k) {
+  if (p->which_spectrum == 1) return pk_tab(p, k);
+  double T = orc_transfer_eh(p, k);
+  return p->norm * pow(k, p->ns) * T * T;
+}
+struct th_par { const orc_power *p; double R; };
+/* sigma2_int, src/power.c:503-516 */
+static double sigma2_int(double k, void *v) {
+  struct th_par *t = v;
+  double kr = t->R * k, kr2 = kr * kr, kr3 = kr2 * kr;
+  if (kr < 1e-8) return 0;
+  double w = 3 * (sin(kr) / kr3 - cos(kr) / kr2);
+  return k * k * w * w * orc_power_spec(t->p, k);
+}
+/* TopHatSigma2, src/power.c:481-498 */
+double orc_tophat_sigma2(const orc_power *p, double R) {
+  struct th_par t = {p, R};
+  /* split [0, 500/R] into many panels: the integrand oscillates */
+  double s = 0, b = 500.0 / R;
+  int np = 256;
+  for (int i = 0; i < np; i++) s += integrate(sigma2_int, &t, b * i / np, b * (i + 1) / np);
+  return s / (2.0 * M_PI * M_PI);
+}
+/* initialize_powerspectrum, src/power.c:226-257 */
+void orc_power_init(orc_power *p) {
+  p->norm = 1.0;
+  double res = orc_tophat_sigma2(p, 8.0);
+  p->norm = p->sigma8 * p->sigma8 / res;
+}

@@ -1,0 +1,155 @@
+/*
+ * Oracle end-to-end run (test infrastructure only): 2LPT IC + the KDK loop of
+ * src/main.c:394-611 for one output redshift, scale-independent growth.
+ */
+#include "orc.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
+            double *kbin, double *pk, double *kmean, double *nmodes) {
+  const int N = rp->ic.N, Ns = rp->ic.Ns, NH = N / 2 + 1;
+  const double Box = rp->ic.box;
+  const long np = (long)Ns * Ns * Ns;
+  const size_t tot = (size_t)N * N * NH;
+  orc_cosmo *c = orc_cosmo_create(&rp->mg, rp->init_redshift);
+  double *D1 = malloc(8 * 3 * np), *D2 = malloc(8 * 3 * np), *pos = malloc(8 * 3 * np), *vel = calloc(3 * np, 8);
+  double *disp = malloc(8 * 3 * np);
+  orc_ic_2lpt(&rp->ic, &rp->pw, D1, D2, NULL, NULL);
+
+  double A = 1.0 / (1.0 + rp->init_redshift);
+  double Di = orc_growth_D(c, A), Di2 = orc_growth_D2(c, A);
+  /* main.c:289-307 (non-SCALEDEPENDENT) */
+  for (long p = 0; p < np; p++) {
+    long i = p / ((long)Ns * Ns), j = (p / Ns) % Ns, k = p % Ns;
+    long q[3] = {i, j, k};
+    for (int a = 0; a < 3; a++)
+      pos[3 * p + a] = orc_periodic_wrap(q[a] * (Box / (double)Ns) + D1[3 * p + a] * Di + D2[3 * p + a] * Di2, Box);
+  }
+  double AI = A, AF = A, AFF = A, da = 0;
+  double *grid = malloc(sizeof(double) * 2 * tot), *dens_x = malloc(sizeof(double) * 2 * tot);
+  double *mgk = malloc(sizeof(double) * 2 * tot);
+  double *f[3];
+  for (int a = 0; a < 3; a++) f[a] = malloc(sizeof(double) * 2 * tot);
+  double sumv[3] = {0, 0, 0};
+  int nb = rp->pofk_nbins;
+  int uses_mgk = rp->mg.mg_active && (rp->mg.model == ORC_FOFR || rp->mg.model == ORC_MBETA || rp->mg.model == ORC_DGP);
+  const int Noutputs = 1;
+  for (int io = 0; io <= Noutputs; io++) {
+    int nsteps;
+    if (io == Noutputs) nsteps = 1;
+    else {
+      nsteps = rp->nsteps;
+      double ao = 1.0 / (1.0 + rp->final_redshift);
+      da = (ao - A) / (double)nsteps;
+    }
+    for (int ts = 0; ts < nsteps; ts++) {
+      if (ts == 0 && io != 0) AF = A;
+      else AF = A + da * 0.5;
+      AFF = A + da;
+      /* GetDisplacements (auxPM.c:37-103) */
+      orc_cic(pos, np, N, Ns, Box, grid);
+      memcpy(dens_x, grid, sizeof(double) * 2 * tot);
+      orc_fft_r2c(N, grid);
+      nb = rp->pofk_nbins;
+      orc_pofk(grid, N, Ns, Box, &nb, rp->pofk_bintype, rp->pofk_subtract_shotnoise, rp->pofk_kmin,
+               rp->pofk_kmax, kbin, pk, kmean, nmodes);
+      if (rp->mg.mg_active) orc_fifth_force(&rp->mg, A, N, Box, dens_x, grid, mgk);
+      orc_forces_kspace(grid, uses_mgk ? mgk : NULL, N, Box, f[0], f[1], f[2]);
+      for (int a = 0; a < 3; a++) orc_fft_c2r(N, f[a]);
+      double sumD[3];
+      orc_interp(f[0], f[1], f[2], N, Box, pos, np, disp, sumD);
+      /* Kick (main.c:688-742) */
+      double dda = orc_Sphi(c, AI, AF, A);
+      orc_kick(np, vel, disp, D1, D2, sumD, rp->mg.omega, dda, orc_growth_ddDddy(c, A), orc_growth_ddD2ddy(c, A), A,
+               rp->usecola, sumv);
+      if (ts == 0 && io != 0) {
+        /* output step (main.c:516-549): the last output ends the run */
+        double dDdy = orc_growth_dDdy(c, A), dD2dy = orc_growth_dD2dy(c, A);
+        for (long p = 0; p < np; p++)
+          for (int a = 0; a < 3; a++) {
+            pos_out[3 * p + a] = pos[3 * p + a];
+            vel_out[3 * p + a] = vel[3 * p + a] - sumv[a] + (D1[3 * p + a] * dDdy + D2[3 * p + a] * dD2dy) * rp->usecola;
+          }
+        goto done;
+      }
+      /* Drift (main.c:747-787) */
+      double dyyy = orc_Sq(c, A, AFF, AF);
+      double dD = orc_growth_D(c, AFF) - Di, dD2 = orc_growth_D2(c, AFF) - Di2;
+      orc_drift(np, pos, vel, D1, D2, sumv, dyyy, dD, dD2, rp->usecola, Box);
+      A = AFF;
+      AI = AF;
+      Di = orc_growth_D(c, A);
+      Di2 = orc_growth_D2(c, A);
+    }
+  }
+done:
+  for (int a = 0; a < 3; a++) free(f[a]);
+  free(grid); free(dens_x); free(mgk); free(D1); free(D2); free(pos); free(vel); free(disp);
+  orc_cosmo_free(c);
+  return nb;
+}
+
+/* CPU baseline: IC (untimed) then `nsteps` KDK steps of the same loop body,
+ * timed with the wall clock.  Returns seconds per step, or -1. */
+#include <sys/time.h>
+static double now_s(void) {
+  struct timeval tv;
+  gettimeofday(&tv, NULL);
+  return tv.tv_sec + 1e-6 * tv.tv_usec;
+}
+
+double orc_time_steps(const orc_run_params *rp, int nsteps) {
+  const int N = rp->ic.N, Ns = rp->ic.Ns, NH = N / 2 + 1;
+  const double Box = rp->ic.box;
+  const long np = (long)Ns * Ns * Ns;
+  const size_t tot = (size_t)N * N * NH;
+  orc_cosmo *c = orc_cosmo_create(&rp->mg, rp->init_redshift);
+  double *D1 = malloc(8 * 3 * np), *D2 = malloc(8 * 3 * np), *pos = malloc(8 * 3 * np), *vel = calloc(3 * np, 8);
+  double *disp = malloc(8 * 3 * np);
+  orc_ic_2lpt(&rp->ic, &rp->pw, D1, D2, NULL, NULL);
+  double A = 1.0 / (1.0 + rp->init_redshift);
+  double Di = orc_growth_D(c, A), Di2 = orc_growth_D2(c, A);
+  for (long p = 0; p < np; p++) {
+    long q[3] = {p / ((long)Ns * Ns), (p / Ns) % Ns, p % Ns};
+    for (int a = 0; a < 3; a++)
+      pos[3 * p + a] = orc_periodic_wrap(q[a] * (Box / (double)Ns) + D1[3 * p + a] * Di + D2[3 * p + a] * Di2, Box);
+  }
+  double *grid = malloc(sizeof(double) * 2 * tot), *dens_x = malloc(sizeof(double) * 2 * tot);
+  double *mgk = malloc(sizeof(double) * 2 * tot), *f[3];
+  for (int a = 0; a < 3; a++) f[a] = malloc(sizeof(double) * 2 * tot);
+  int cap = rp->pofk_nbins > N ? rp->pofk_nbins : N;
+  double *kb = malloc(8 * cap), *pk = malloc(8 * cap), *km = malloc(8 * cap), *nm = malloc(8 * cap);
+  int uses_mgk = rp->mg.mg_active && (rp->mg.model == ORC_FOFR || rp->mg.model == ORC_MBETA || rp->mg.model == ORC_DGP);
+  double da = (1.0 / (1.0 + rp->final_redshift) - A) / (double)rp->nsteps, AI = A, sumv[3];
+  double t0 = now_s();
+  for (int ts = 0; ts < nsteps; ts++) {
+    double AF = A + 0.5 * da, AFF = A + da;
+    orc_cic(pos, np, N, Ns, Box, grid);
+    memcpy(dens_x, grid, sizeof(double) * 2 * tot);
+    orc_fft_r2c(N, grid);
+    int nb = rp->pofk_nbins;
+    orc_pofk(grid, N, Ns, Box, &nb, rp->pofk_bintype, rp->pofk_subtract_shotnoise, rp->pofk_kmin, rp->pofk_kmax, kb, pk,
+             km, nm);
+    if (rp->mg.mg_active) orc_fifth_force(&rp->mg, A, N, Box, dens_x, grid, mgk);
+    orc_forces_kspace(grid, uses_mgk ? mgk : NULL, N, Box, f[0], f[1], f[2]);
+    for (int a = 0; a < 3; a++) orc_fft_c2r(N, f[a]);
+    double sumD[3];
+    orc_interp(f[0], f[1], f[2], N, Box, pos, np, disp, sumD);
+    orc_kick(np, vel, disp, D1, D2, sumD, rp->mg.omega, orc_Sphi(c, AI, AF, A), orc_growth_ddDddy(c, A),
+             orc_growth_ddD2ddy(c, A), A, rp->usecola, sumv);
+    orc_drift(np, pos, vel, D1, D2, sumv, orc_Sq(c, A, AFF, AF), orc_growth_D(c, AFF) - Di, orc_growth_D2(c, AFF) - Di2,
+              rp->usecola, Box);
+    A = AFF;
+    AI = AF;
+    Di = orc_growth_D(c, A);
+    Di2 = orc_growth_D2(c, A);
+  }
+  double dt = (now_s() - t0) / (nsteps > 0 ? nsteps : 1);
+  for (int a = 0; a < 3; a++) free(f[a]);
+  free(grid); free(dens_x); free(mgk); free(D1); free(D2); free(pos); free(vel); free(disp);
+  free(kb); free(pk); free(km); free(nm);
+  orc_cosmo_free(c);
+  return dt;
+}

@@ -1,0 +1,227 @@
+"""Parity of the CUDA path (through the C ABI) against the FP64 oracle.
+
+Tolerances: the CUDA path computes in FP32 (grids, FFTs, particles) and the
+oracle in FP64, so comparisons are relative rms / max errors with the bound
+stated at each assert.  Bin indices, mode counts and lattice bookkeeping are
+integer work and compared exactly.
+"""
+import numpy as np
+import pytest
+
+import mgpicola as M
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def params(N=32, Ns=16, box=128.0, **kw):
+    d = dict(Nmesh=N, Nsample=Ns, Box=box, Seed=5001, Init_Redshift=19.0, pofk_nbins=16, pofk_bintype=0,
+             pofk_kmin=0.0, pofk_kmax=0.0, pofk_compute_every_step=1, pofk_subtract_shotnoise=0)
+    d.update(kw)
+    return M.default_params(**d)
+
+
+def power_for(p):
+    return O.make_power(omega=p.Omega, omega_b=p.OmegaBaryon, h=p.HubbleParam, ns=p.PrimordialIndex,
+                        sigma8=p.Sigma8)
+
+
+def rel_rms(a, b):
+    return float(np.sqrt(np.mean((np.asarray(a, np.float64) - b) ** 2) / np.mean(np.asarray(b) ** 2)))
+
+
+def random_particles(Ns, box, seed=1, spread=0.3):
+    """Lattice + random displacement (as COLA particles), plus D1/D2/vel."""
+    rng = np.random.default_rng(seed)
+    n = Ns ** 3
+    q = np.stack(np.meshgrid(*(np.arange(Ns),) * 3, indexing="ij"), -1).reshape(-1, 3) * (box / Ns)
+    disp = rng.normal(0, spread * box / Ns, (n, 3))
+    pos = np.mod(q + disp, box).astype(np.float32)
+    pos[pos >= box] = 0.0
+    vel = rng.normal(0, 10.0, (n, 3)).astype(np.float32)
+    d1 = rng.normal(0, 2.0, (n, 3)).astype(np.float32)
+    d2 = rng.normal(0, 0.5, (n, 3)).astype(np.float32)
+    return pos, vel, d1, d2
+
+
+@pytest.mark.parametrize("N,Ns,fixed,inverted", [(32, 16, 0, 0), (32, 32, 1, 0), (32, 16, 0, 1), (24, 12, 0, 0)])
+def test_ic_displacements_match_oracle(N, Ns, fixed, inverted):
+    box = 100.0
+    p = params(N, Ns, box, amplitude_fixed_initial_condition=fixed, inverted_initial_condition=inverted, Seed=777)
+    with M.Context(p) as ctx:
+        ctx.displacement_fields()
+        pos, vel, d1, d2 = ctx.get_particles()
+        Di = ctx.growth(0, 1 / 20.0)
+        Di2 = ctx.growth(3, 1 / 20.0)
+    D1, D2 = O.ic_2lpt(N, Ns, box, 777, power_for(p), fixed=fixed, inverted=inverted)
+    # FP32 FFTs of an FP64 field: relative rms bound 1e-5 (ZA) and 1e-4 (2LPT)
+    assert rel_rms(d1, D1) < 1e-5
+    assert rel_rms(d2, D2) < 1e-4
+    assert np.all(vel == 0)
+    q = np.stack(np.meshgrid(*(np.arange(Ns),) * 3, indexing="ij"), -1).reshape(-1, 3) * (box / Ns)
+    ref = np.mod(q + D1 * Di + D2 * Di2, box)
+    dx = np.abs(pos - ref)
+    dx = np.minimum(dx, box - dx)
+    assert dx.max() < 1e-4 * box / Ns
+
+
+def test_cic_density_matches_oracle():
+    N, Ns, box = 32, 16, 64.0
+    p = params(N, Ns, box)
+    pos, vel, d1, d2 = random_particles(Ns, box, seed=3)
+    # edge cases: particles on the box boundary, on cell corners and at 0
+    pos[0] = [0.0, 0.0, 0.0]
+    pos[1] = [np.nextafter(np.float32(box), np.float32(0))] * 3
+    pos[2] = [2.0, 4.0, 6.0]  # exact grid points (cell = 2 Mpc/h)
+    with M.Context(p) as ctx:
+        ctx.set_particles(pos, vel, d1, d2)
+        ctx.get_displacements(0.5)
+        rho = ctx.grid(0)
+    ref = O.cic(pos.astype(np.float64), N, Ns, box)
+    # mass conservation of the deposit: mean of delta is zero
+    assert abs(rho[:, :, :N].astype(np.float64).mean()) < 1e-6
+    err = np.abs(rho[:, :, :N] - ref[:, :, :N]).max()
+    assert err < 2e-5 * np.abs(ref[:, :, :N]).max()
+
+
+@pytest.mark.parametrize("bintype,nbins,kmin,kmax", [(0, 16, 0.0, 0.0), (1, 12, 0.05, 1.5), (0, 40, 0.1, 0.9)])
+def test_pofk_matches_oracle(bintype, nbins, kmin, kmax):
+    N, Ns, box = 32, 16, 64.0
+    p = params(N, Ns, box, pofk_bintype=bintype, pofk_nbins=nbins, pofk_kmin=kmin, pofk_kmax=kmax,
+               pofk_subtract_shotnoise=1)
+    pos, vel, d1, d2 = random_particles(Ns, box, seed=4, spread=0.8)
+    with M.Context(p) as ctx:
+        ctx.set_particles(pos, vel, d1, d2)
+        ctx.get_displacements(0.5)
+        k, pk, km, n = ctx.pofk()
+    g = O.cic(pos.astype(np.float64), N, Ns, box)
+    O.lib().orc_fft_r2c(N, g)
+    kb, pko, kmo, no = O.pofk(g, N, Ns, box, nbins, bintype, 1, kmin, kmax)
+    assert len(k) == len(kb)
+    np.testing.assert_array_equal(n, no)          # integer mode counts, exact
+    np.testing.assert_allclose(k, kb, rtol=1e-14)  # bin k values
+    np.testing.assert_allclose(km[n > 0], kmo[no > 0], rtol=1e-12)
+    m = no > 0
+    # P(k) includes shot-noise subtraction: compare the raw power
+    shot = (box / Ns) ** 3
+    assert np.max(np.abs((pk[m] + shot) - (pko[m] + shot)) / (pko[m] + shot)) < 1e-5
+
+
+def test_forces_match_oracle():
+    N, Ns, box = 32, 16, 64.0
+    p = params(N, Ns, box)
+    pos, vel, d1, d2 = random_particles(Ns, box, seed=5, spread=0.6)
+    with M.Context(p) as ctx:
+        ctx.set_particles(pos, vel, d1, d2)
+        ctx.get_displacements(0.5)
+        f = [ctx.grid(w)[:, :, :N] for w in (2, 3, 4)]
+    g = O.cic(pos.astype(np.float64), N, Ns, box)
+    O.lib().orc_fft_r2c(N, g)
+    fo = O.forces_kspace(g, N, box)
+    for a in range(3):
+        O.lib().orc_fft_c2r(N, fo[a])
+        assert rel_rms(f[a], fo[a][:, :, :N]) < 1e-5
+
+
+def test_kick_drift_matches_oracle():
+    N, Ns, box = 32, 16, 64.0
+    p = params(N, Ns, box)
+    pos, vel, d1, d2 = random_particles(Ns, box, seed=6, spread=0.4)
+    A, AI, AF, AFF = 0.30, 0.28, 0.32, 0.34
+    with M.Context(p) as ctx:
+        ctx.set_particles(pos, vel, d1, d2)
+        ctx.get_displacements(A)
+        ctx.kick_drift(AI, AF, A, AFF, drift=True)
+        pos2, vel2, _, _ = ctx.get_particles()
+    mg = O.make_mg(O.LCDM, p.Omega)
+    cos = O.Cosmo(mg, p.Init_Redshift)
+    g = O.cic(pos.astype(np.float64), N, Ns, box)
+    O.lib().orc_fft_r2c(N, g)
+    fo = O.forces_kspace(g, N, box)
+    for a in range(3):
+        O.lib().orc_fft_c2r(N, fo[a])
+    P = pos.astype(np.float64).copy()
+    V = vel.astype(np.float64).copy()
+    D1 = d1.astype(np.float64)
+    D2 = d2.astype(np.float64)
+    disp, sD = O.interp(fo, N, box, P)
+    sumv = np.zeros(3)
+    O.lib().orc_kick(P.shape[0], V, disp, D1, D2, sD, p.Omega, cos.Sphi(AI, AF, A), cos.growth_ddDddy(A),
+                     cos.growth_ddD2ddy(A), A, 1, sumv)
+    O.lib().orc_drift(P.shape[0], P, V, D1, D2, sumv, cos.Sq(A, AFF, AF), cos.growth_D(AFF) - cos.growth_D(A),
+                      cos.growth_D2(AFF) - cos.growth_D2(A), 1, box)
+    assert rel_rms(vel2, V) < 1e-5
+    dx = np.abs(pos2 - P)
+    dx = np.minimum(dx, box - dx)
+    assert np.sqrt(np.mean(dx ** 2)) < 1e-5 * box / Ns
+
+
+def _gpu_run(p, nsteps, zf=0.0):
+    """The KDK loop of src/main.c:394-611 for one output, through the C ABI."""
+    with M.Context(p) as ctx:
+        ctx.displacement_fields()
+        A = 1.0 / (1.0 + p.Init_Redshift)
+        AI = A
+        ao = 1.0 / (1.0 + zf)
+        da = (ao - A) / nsteps
+        for ts in range(nsteps):
+            AF, AFF = A + 0.5 * da, A + da
+            ctx.get_displacements(A)
+            ctx.kick_drift(AI, AF, A, AFF, drift=True)
+            A, AI = AFF, AF
+        ctx.get_displacements(A)
+        pk = ctx.pofk()
+        ctx.kick_drift(AI, A, A, A, drift=False)
+        pos, vel, d1, d2 = ctx.get_particles()
+        dDdy, dD2dy = ctx.growth(1, A), ctx.growth(4, A)
+    return pos, vel, d1, d2, pk, dDdy, dD2dy
+
+
+def _oracle_run(p, mg, nsteps, zf=0.0):
+    rp = O.RunParams()
+    rp.mg = mg
+    rp.pw = power_for(p)
+    rp.ic = O.ICParams(p.Nmesh, p.Nsample, p.Box, p.Seed, p.SphereMode, p.amplitude_fixed_initial_condition,
+                       p.inverted_initial_condition, 1.0)
+    rp.init_redshift = p.Init_Redshift
+    rp.nsteps = nsteps
+    rp.final_redshift = zf
+    rp.pofk_nbins, rp.pofk_bintype, rp.pofk_subtract_shotnoise = p.pofk_nbins, p.pofk_bintype, 0
+    rp.pofk_kmin, rp.pofk_kmax = p.pofk_kmin, p.pofk_kmax
+    rp.usecola = 1
+    n = p.Nsample ** 3
+    pos, vel = np.zeros((n, 3)), np.zeros((n, 3))
+    cap = max(p.pofk_nbins, p.Nmesh)
+    kb, pk, km, nm = (np.zeros(cap) for _ in range(4))
+    nb = O.lib().orc_run(rp, pos, vel, kb, pk, km, nm)
+    return pos, vel, (kb[:nb], pk[:nb], km[:nb], nm[:nb])
+
+
+@pytest.mark.parametrize("model", ["lcdm", "fofr", "dgp"])
+def test_short_run_matches_oracle(model):
+    N, Ns, box, nsteps = 32, 16, 128.0, 5
+    kw = dict(Seed=4242)
+    if model == "fofr":
+        kw.update(model=M.MODEL_FOFR, modified_gravity_active=1, include_screening=1, fofr0=1e-5, nfofr=1.0,
+                  input_pofk_is_for_lcdm=0)
+        mg = O.make_mg(O.FOFR, 0.267, fofr0=1e-5, nfofr=1.0)
+    elif model == "dgp":
+        kw.update(model=M.MODEL_DGP, modified_gravity_active=1, include_screening=1, rcH0_DGP=1.0, Rsmooth=1.0,
+                  smoothing_filter=M.FILTER_GAUSSIAN, input_pofk_is_for_lcdm=0)
+        mg = O.make_mg(O.DGP, 0.267, rcH0=1.0, rsmooth=1.0)
+    else:
+        mg = O.make_mg(O.LCDM, 0.267)
+    p = params(N, Ns, box, **kw)
+    pos, vel, d1, d2, (k, pk, km, n), dDdy, dD2dy = _gpu_run(p, nsteps)
+    opos, ovel, (kb, pko, kmo, no) = _oracle_run(p, mg, nsteps)
+    np.testing.assert_array_equal(n, no)
+    m = no > 0
+    # P(k) of the final density: FP32 path vs FP64 oracle within 1e-3
+    assert np.max(np.abs(pk[m] - pko[m]) / pko[m]) < 1e-3
+    dx = np.abs(pos - opos)
+    dx = np.minimum(dx, box - dx)
+    # particle positions: rms below 1e-3 of the particle spacing
+    assert np.sqrt(np.mean(dx ** 2)) < 1e-3 * box / Ns
+    v64 = vel.astype(np.float64)
+    vout = v64 - v64.mean(0) + d1 * dDdy + d2 * dD2dy
+    assert rel_rms(vout, ovel) < 1e-3
