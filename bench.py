@@ -196,7 +196,6 @@ def run_gpu(args):
     for a in (pos, vel, d1, d2):
         M.unpin(a)
     e2e_val = world * Np * e2e_steps / e2e_t / 1e6
-    k, pk, km, n = ctx.pofk()
     ctx.close()
 
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(

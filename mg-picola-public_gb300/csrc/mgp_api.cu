@@ -109,7 +109,7 @@ static int setup_pofk(mgp_ctx *c) {
   int nbins = c->p.pofk_nbins, bt = c->p.pofk_bintype, sub = c->p.pofk_subtract_shotnoise;
   double kmin = c->p.pofk_kmin * c->p.Box / (2.0 * M_PI), kmax = c->p.pofk_kmax * c->p.Box / (2.0 * M_PI);
   adjust_pofk(N, &nbins, &bt, &sub, &kmin, &kmax);
-  if (nbins > 12288) return mgp_set_error(MGP_EINVAL, "pofk_nbins = %d exceeds 12288", nbins);
+  if (nbins > 24576) return mgp_set_error(MGP_EINVAL, "pofk_nbins = %d exceeds 24576", nbins);
   c->pk_nbins = nbins;
   c->pk_bintype = bt;
   c->pk_sub = sub;
@@ -153,7 +153,7 @@ static int setup_pofk(mgp_ctx *c) {
   if (nb > 8192) nb = 8192;
   if (nb < 1) nb = 1;
   c->pk_blocks = (int)nb;
-  MGP_CUDA(cudaMalloc(&c->pk_block, sizeof(float) * (size_t)nb * nbins));
+  MGP_CUDA(cudaMalloc(&c->pk_block, sizeof(double) * (size_t)nb * nbins));
   MGP_CUDA(cudaMalloc(&c->pk_sum, sizeof(double) * nbins));
   return MGP_OK;
 }

@@ -70,7 +70,7 @@ struct mgp_ctx {
   double pk_kmin, pk_kmax;  /* integer-k units, adjusted */
   int *rk_bin;              /* device: bin index per integer |k|^2 (or -1) */
   float *win1d;             /* device: 1/sinc^4 per |d| in [0, N/2] */
-  float *pk_block;          /* device: per-block FP32 bin partials */
+  double *pk_block;         /* device: per-block FP64 bin partials */
   double *pk_sum;           /* device: FP64 bin sums */
   double *pk_n, *pk_k;      /* host: mode counts and k sums per bin */
   double *pk_host;          /* host: last P(k) sums */
@@ -139,7 +139,7 @@ int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st);
 int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box,
                    float wpar, float *rho, long long P, cudaStream_t stream);
 int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins,
-                    float *block_part, int nblocks, double *sums, cudaStream_t st);
+                    double *block_part, int nblocks, double *sums, cudaStream_t st);
 int mgp_launch_forces(const float *dk, const float *mgk, float mg_coupling, float mg_mass2, int mg_kind,
                       int N, double box, float *frc, long long grid_floats, cudaStream_t st);
 int mgp_launch_ikd(const float *frc, long long grid_floats, int N, long long P, int Ns, long long np,

@@ -131,47 +131,73 @@ int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, i
 // of a mode depends only on its integer |k|^2, looked up in rk_bin (computed
 // on the host in double exactly as pofk_bin_index, compute_pofk.c:30-46).
 // Mode counts and k sums are geometric and also precomputed on the host.
+//
+// Accumulation: a warp reads 32 consecutive modes (coalesced); lanes with the
+// same bin are contiguous (|k| grows along kz), so a segmented warp scan sums
+// each run in FP32 and the last lane of a run adds it to an FP64 shared-memory
+// bin; blocks write FP64 partials that k_pofk_reduce sums in fixed order.
 __global__ void __launch_bounds__(MGP_THREADS) k_pofk(const float2 *__restrict__ dk, int N, const int *__restrict__ rk_bin,
                                                       const float *__restrict__ win, int nbins,
-                                                      float *__restrict__ block_part, long long chunk) {
-  extern __shared__ float sh[];
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) sh[b] = 0.0f;
+                                                      double *__restrict__ block_part, long long chunk) {
+  extern __shared__ double shd[];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) shd[b] = 0.0;
   __syncthreads();
   const int NH = N / 2 + 1;
   const long long total = (long long)N * N * NH;
+  const int lane = threadIdx.x & 31;
   long long lo = (long long)blockIdx.x * chunk, hi = lo + chunk;
   if (hi > total) hi = total;
-  for (long long c = lo + threadIdx.x; c < hi; c += blockDim.x) {
-    int kz = (int)(c % NH);
-    long long r = c / NH;
-    int j = (int)(r % N), i = (int)(r / N);
-    int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
-    int rk = d0 * d0 + d1 * d1 + kz * kz;
-    int bin = rk_bin[rk];
-    if (bin < 0) continue;
-    float2 z = dk[c];
-    float w = (kz == 0 || 2 * kz == N) ? 1.0f : 2.0f;
-    float pk = (z.x * z.x + z.y * z.y) * (win[d0] * win[d1] * win[kz] * w);
-    atomicAdd(&sh[bin], pk);
+  // every lane of a warp runs the same number of iterations
+  for (long long base = lo + (threadIdx.x & ~31); base < hi; base += blockDim.x) {
+    long long c = base + lane;
+    int bin = -1;
+    float pk = 0.0f;
+    if (c < hi) {
+      int kz = (int)(c % NH);
+      long long r = c / NH;
+      int j = (int)(r % N), i = (int)(r / N);
+      int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
+      bin = rk_bin[d0 * d0 + d1 * d1 + kz * kz];
+      if (bin >= 0) {
+        float2 z = dk[c];
+        float w = (kz == 0 || 2 * kz == N) ? 1.0f : 2.0f;
+        pk = (z.x * z.x + z.y * z.y) * (win[d0] * win[d1] * win[kz] * w);
+      }
+    }
+    // segmented inclusive scan over runs of equal bin
+    int prev = __shfl_up_sync(0xffffffffu, bin, 1);
+    bool head = lane == 0 || prev != bin;
+    unsigned heads = __ballot_sync(0xffffffffu, head);
+    // start lane of this lane's segment
+    unsigned below = heads & ((2u << lane) - 1u);
+    int seg0 = 31 - __clz(below);
+    float acc = pk;
+    for (int o = 1; o < 32; o <<= 1) {
+      float t = __shfl_up_sync(0xffffffffu, acc, o);
+      if (lane - o >= seg0) acc += t;
+    }
+    int nbin = __shfl_down_sync(0xffffffffu, bin, 1);
+    bool tail = lane == 31 || nbin != bin;
+    if (tail && bin >= 0) atomicAdd(&shd[bin], (double)acc);
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) block_part[(long long)blockIdx.x * nbins + b] = sh[b];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) block_part[(long long)blockIdx.x * nbins + b] = shd[b];
 }
 
 // Deterministic cross-block sum in FP64 (the MPI_Allreduce of compute_pofk.c:225).
-__global__ void k_pofk_reduce(const float *__restrict__ block_part, int nblocks, int nbins, double *__restrict__ sums) {
+__global__ void k_pofk_reduce(const double *__restrict__ block_part, int nblocks, int nbins, double *__restrict__ sums) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nbins) return;
   double s = 0.0;
-  for (int k = 0; k < nblocks; k++) s += (double)block_part[(long long)k * nbins + b];
+  for (int k = 0; k < nblocks; k++) s += block_part[(long long)k * nbins + b];
   sums[b] = s;
 }
 
-int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins, float *block_part,
+int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins, double *block_part,
                     int nblocks, double *sums, cudaStream_t st) {
   const long long total = (long long)N * N * (N / 2 + 1);
   long long chunk = (total + nblocks - 1) / nblocks;
-  size_t shmem = sizeof(float) * (size_t)nbins;
+  size_t shmem = sizeof(double) * (size_t)nbins;
   if (shmem > 48 * 1024) {
     cudaFuncSetAttribute(k_pofk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem);
   }
