@@ -149,8 +149,12 @@ static int setup_pofk(mgp_ctx *c) {
   MGP_CUDA(cudaMemcpy(c->rk_bin, rkb.data(), sizeof(int) * (rkmax + 1), cudaMemcpyHostToDevice));
   MGP_CUDA(cudaMalloc(&c->win1d, sizeof(float) * (h + 1)));
   MGP_CUDA(cudaMemcpy(c->win1d, win.data(), sizeof(float) * (h + 1), cudaMemcpyHostToDevice));
-  long long nb = (c->g.ncomplex + 65535) / 65536;
-  if (nb > 8192) nb = 8192;
+  // enough warps to cover the SMs; each warp owns whole (i, j) rows
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  long long nb = (long long)sms * 4;
+  long long rows_blocks = ((long long)N * N + 7) / 8;
+  if (nb > rows_blocks) nb = rows_blocks;
   if (nb < 1) nb = 1;
   c->pk_blocks = (int)nb;
   MGP_CUDA(cudaMalloc(&c->pk_block, sizeof(double) * (size_t)nb * nbins));
@@ -165,21 +169,22 @@ static int make_plans(mgp_ctx *c) {
   long long rembed[3] = {N, N, c->g.P};
   long long cembed[3] = {N, N, c->g.NH};
   long long rdist = c->g.nreal, cdist = c->g.ncomplex;
-  size_t ws[4] = {0, 0, 0, 0};
-  cufftHandle *plans[4] = {&c->plan_r2c_oop, &c->plan_r2c_ip, &c->plan_c2r_1, &c->plan_c2r_3};
-  for (int i = 0; i < 4; i++) {
+  size_t ws[3] = {0, 0, 0};
+  // single-grid plans only: a batch of three in-place C2R runs markedly
+  // slower per grid (and needs a 3-grid work area) than three single calls
+  cufftHandle *plans[3] = {&c->plan_r2c_oop, &c->plan_r2c_ip, &c->plan_c2r_1};
+  for (int i = 0; i < 3; i++) {
     MGP_CUFFT(cufftCreate(plans[i]));
     MGP_CUFFT(cufftSetAutoAllocation(*plans[i], 0));
   }
   MGP_CUFFT(cufftMakePlanMany64(c->plan_r2c_oop, 3, n, rembed, 1, rdist, cembed, 1, cdist, CUFFT_R2C, 1, &ws[0]));
   MGP_CUFFT(cufftMakePlanMany64(c->plan_r2c_ip, 3, n, rembed, 1, rdist, cembed, 1, cdist, CUFFT_R2C, 1, &ws[1]));
   MGP_CUFFT(cufftMakePlanMany64(c->plan_c2r_1, 3, n, cembed, 1, cdist, rembed, 1, rdist, CUFFT_C2R, 1, &ws[2]));
-  MGP_CUFFT(cufftMakePlanMany64(c->plan_c2r_3, 3, n, cembed, 1, cdist, rembed, 1, rdist, CUFFT_C2R, 3, &ws[3]));
   size_t w = 0;
-  for (int i = 0; i < 4; i++) w = ws[i] > w ? ws[i] : w;
+  for (int i = 0; i < 3; i++) w = ws[i] > w ? ws[i] : w;
   c->fft_work_bytes = w;
   if (w) MGP_CUDA(cudaMalloc(&c->fft_work, w));
-  for (int i = 0; i < 4; i++) {
+  for (int i = 0; i < 3; i++) {
     MGP_CUFFT(cufftSetWorkArea(*plans[i], c->fft_work));
     MGP_CUFFT(cufftSetStream(*plans[i], c->stream));
   }
@@ -215,8 +220,8 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   if (!c) return MGP_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  cufftHandle plans[4] = {c->plan_r2c_oop, c->plan_r2c_ip, c->plan_c2r_1, c->plan_c2r_3};
-  for (int i = 0; i < 4; i++)
+  cufftHandle plans[3] = {c->plan_r2c_oop, c->plan_r2c_ip, c->plan_c2r_1};
+  for (int i = 0; i < 3; i++)
     if (plans[i]) cufftDestroy(plans[i]);
   void *bufs[] = {c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
                   c->fft_work, c->rk_bin, c->win1d, c->pk_block, c->pk_sum};
@@ -393,13 +398,13 @@ extern "C" int mgp_displacement_fields(mgp_ctx *c) {
   CK(mgp_launch_ic_delta(d_seeds, d_amp, d_cut, N, Ns, box, c->p.amplitude_fixed_initial_condition,
                          c->p.inverted_initial_condition, c->p.SphereMode == 1, c->dk, c->stream));
   CK(mgp_launch_ic_grad6(c->dk, g6, gf, N, c->stream));
-  CKF(cufftExecC2R(c->plan_c2r_3, (cufftComplex *)g6, (cufftReal *)g6));
-  CKF(cufftExecC2R(c->plan_c2r_3, (cufftComplex *)(g6 + 3 * gf), (cufftReal *)(g6 + 3 * gf)));
+  for (int g = 0; g < 3; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
+  for (int g = 3; g < 6; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
   CK(mgp_launch_ic_source(g6, gf, N, c->g.P, c->stream));
   CKF(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)(g6 + 3 * gf), (cufftComplex *)(g6 + 3 * gf)));
   CK(mgp_launch_ic_disp(c->dk, g6 + 3 * gf, g6, gf, N, box, c->stream));
-  CKF(cufftExecC2R(c->plan_c2r_3, (cufftComplex *)g6, (cufftReal *)g6));
-  CKF(cufftExecC2R(c->plan_c2r_3, (cufftComplex *)(g6 + 3 * gf), (cufftReal *)(g6 + 3 * gf)));
+  for (int g = 0; g < 3; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
+  for (int g = 3; g < 6; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
   CK(mgp_launch_ic_readout(g6, gf, N, c->g.P, Ns, c->D1, c->D2, c->partials, nblk, c->stream));
   CK(mgp_launch_ic_finish(c->D1, c->D2, c->s, c->v, c->np, c->partials, nblk, (float)Di, (float)Di2, 0.0, c->stream));
   CKC(cudaMemsetAsync(c->dstate, 0, sizeof(mgp_dstate), c->stream));
@@ -501,7 +506,8 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   RET_IF(mgp_launch_forces(c->dk, c->rho, coupling, mass2, mg_kind, N, c->p.Box, c->frc, c->g.nreal, c->stream));
   tstop(c, T_FORCES);
   tstart(c, T_C2R);
-  MGP_CUFFT(cufftExecC2R(c->plan_c2r_3, (cufftComplex *)c->frc, (cufftReal *)c->frc));
+  for (int g = 0; g < 3; g++)
+    MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(c->frc + g * c->g.nreal), (cufftReal *)(c->frc + g * c->g.nreal)));
   tstop(c, T_C2R);
   c->have_forces = 1;
   return MGP_OK;

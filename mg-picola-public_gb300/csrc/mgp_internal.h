@@ -63,7 +63,7 @@ struct mgp_ctx {
   float *rho, *dk, *frc, *mg1;
   void *fft_work;
   size_t fft_work_bytes;
-  cufftHandle plan_r2c_oop, plan_r2c_ip, plan_c2r_1, plan_c2r_3;
+  cufftHandle plan_r2c_oop, plan_r2c_ip, plan_c2r_1;
 
   /* P(k) */
   int pk_nbins, pk_bintype, pk_sub;

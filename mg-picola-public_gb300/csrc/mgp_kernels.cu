@@ -136,52 +136,64 @@ int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, i
 // same bin are contiguous (|k| grows along kz), so a segmented warp scan sums
 // each run in FP32 and the last lane of a run adds it to an FP64 shared-memory
 // bin; blocks write FP64 partials that k_pofk_reduce sums in fixed order.
+// priv != 0: every warp owns a private FP64 copy of the bins (the run tails
+// of one warp always hit distinct bins, so plain adds suffice); otherwise
+// the block shares one copy updated with FP64 shared-memory atomics.
 __global__ void __launch_bounds__(MGP_THREADS) k_pofk(const float2 *__restrict__ dk, int N, const int *__restrict__ rk_bin,
-                                                      const float *__restrict__ win, int nbins,
-                                                      double *__restrict__ block_part, long long chunk) {
+                                                      const float *__restrict__ win, int nbins, int priv,
+                                                      double *__restrict__ block_part) {
   extern __shared__ double shd[];
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) shd[b] = 0.0;
+  const int nwb = priv ? (int)(blockDim.x >> 5) : 1;
+  for (int b = threadIdx.x; b < nbins * nwb; b += blockDim.x) shd[b] = 0.0;
   __syncthreads();
+  double *mybins = priv ? shd + (threadIdx.x >> 5) * nbins : shd;
   const int NH = N / 2 + 1;
-  const long long total = (long long)N * N * NH;
   const int lane = threadIdx.x & 31;
-  long long lo = (long long)blockIdx.x * chunk, hi = lo + chunk;
-  if (hi > total) hi = total;
-  // every lane of a warp runs the same number of iterations
-  for (long long base = lo + (threadIdx.x & ~31); base < hi; base += blockDim.x) {
-    long long c = base + lane;
-    int bin = -1;
-    float pk = 0.0f;
-    if (c < hi) {
-      int kz = (int)(c % NH);
-      long long r = c / NH;
-      int j = (int)(r % N), i = (int)(r / N);
-      int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
-      bin = rk_bin[d0 * d0 + d1 * d1 + kz * kz];
-      if (bin >= 0) {
-        float2 z = dk[c];
-        float w = (kz == 0 || 2 * kz == N) ? 1.0f : 2.0f;
-        pk = (z.x * z.x + z.y * z.y) * (win[d0] * win[d1] * win[kz] * w);
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  // one warp per (i, j) row; all lanes run the same number of chunks
+  for (long long r = wid; r < (long long)N * N; r += nw) {
+    const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+    const int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
+    const int rk01 = d0 * d0 + d1 * d1;
+    const float w01 = win[d0] * win[d1];
+    for (int k0 = 0; k0 < NH; k0 += 32) {
+      const int kz = k0 + lane;
+      int bin = -1;
+      float pk = 0.0f;
+      if (kz < NH) {
+        bin = rk_bin[rk01 + kz * kz];
+        if (bin >= 0) {
+          float2 z = dk[r * NH + kz];
+          float w = (kz == 0 || 2 * kz == N) ? 1.0f : 2.0f;
+          pk = (z.x * z.x + z.y * z.y) * (w01 * win[kz] * w);
+        }
+      }
+      // segmented inclusive scan over runs of equal bin (|k| grows with kz)
+      int prev = __shfl_up_sync(0xffffffffu, bin, 1);
+      bool head = lane == 0 || prev != bin;
+      unsigned heads = __ballot_sync(0xffffffffu, head);
+      unsigned below = heads & ((2u << lane) - 1u);
+      int seg0 = 31 - __clz(below);
+      float acc = pk;
+      for (int o = 1; o < 32; o <<= 1) {
+        float t = __shfl_up_sync(0xffffffffu, acc, o);
+        if (lane - o >= seg0) acc += t;
+      }
+      int nbin = __shfl_down_sync(0xffffffffu, bin, 1);
+      bool tail = lane == 31 || nbin != bin;
+      if (tail && bin >= 0) {
+        if (priv) mybins[bin] += (double)acc;
+        else atomicAdd(&mybins[bin], (double)acc);
       }
     }
-    // segmented inclusive scan over runs of equal bin
-    int prev = __shfl_up_sync(0xffffffffu, bin, 1);
-    bool head = lane == 0 || prev != bin;
-    unsigned heads = __ballot_sync(0xffffffffu, head);
-    // start lane of this lane's segment
-    unsigned below = heads & ((2u << lane) - 1u);
-    int seg0 = 31 - __clz(below);
-    float acc = pk;
-    for (int o = 1; o < 32; o <<= 1) {
-      float t = __shfl_up_sync(0xffffffffu, acc, o);
-      if (lane - o >= seg0) acc += t;
-    }
-    int nbin = __shfl_down_sync(0xffffffffu, bin, 1);
-    bool tail = lane == 31 || nbin != bin;
-    if (tail && bin >= 0) atomicAdd(&shd[bin], (double)acc);
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) block_part[(long long)blockIdx.x * nbins + b] = shd[b];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
+    double t = 0.0;
+    for (int w = 0; w < nwb; w++) t += shd[w * nbins + b];
+    block_part[(long long)blockIdx.x * nbins + b] = t;
+  }
 }
 
 // Deterministic cross-block sum in FP64 (the MPI_Allreduce of compute_pofk.c:225).
@@ -195,13 +207,12 @@ __global__ void k_pofk_reduce(const double *__restrict__ block_part, int nblocks
 
 int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins, double *block_part,
                     int nblocks, double *sums, cudaStream_t st) {
-  const long long total = (long long)N * N * (N / 2 + 1);
-  long long chunk = (total + nblocks - 1) / nblocks;
-  size_t shmem = sizeof(double) * (size_t)nbins;
+  int priv = (size_t)nbins * (MGP_THREADS / 32) * sizeof(double) <= 64 * 1024;
+  size_t shmem = sizeof(double) * (size_t)nbins * (priv ? MGP_THREADS / 32 : 1);
   if (shmem > 48 * 1024) {
     cudaFuncSetAttribute(k_pofk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem);
   }
-  k_pofk<<<nblocks, MGP_THREADS, shmem, st>>>((const float2 *)dk, N, rk_bin, win, nbins, block_part, chunk);
+  k_pofk<<<nblocks, MGP_THREADS, shmem, st>>>((const float2 *)dk, N, rk_bin, win, nbins, priv, block_part);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   k_pofk_reduce<<<(nbins + 127) / 128, 128, 0, st>>>(block_part, nblocks, nbins, sums);
@@ -230,11 +241,15 @@ __global__ void __launch_bounds__(MGP_THREADS) k_forces(const float2 *__restrict
                                                         float2 *__restrict__ fz) {
   const int NH = N / 2 + 1;
   const long long total = (long long)N * N * NH;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += stride) {
-    int kz = (int)(c % NH);
-    long long r = c / NH;
-    int j = (int)(r % N), i = (int)(r / N);
+  (void)total;
+  const int lane = threadIdx.x & 31;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  // one warp per (i, j) row of the half-complex grid, lanes along kz
+  for (long long r = wid; r < (long long)N * N; r += nw) {
+    const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+    for (int kz = lane; kz < NH; kz += 32) {
+    const long long c = r * NH + kz;
     int dx = i > N / 2 ? i - N : i, dy = j > N / 2 ? j - N : j, dz = kz;
     int rk = dx * dx + dy * dy + dz * dz;
     float2 S = dk[c];
@@ -261,6 +276,7 @@ __global__ void __launch_bounds__(MGP_THREADS) k_forces(const float2 *__restrict
     fx[c] = make_float2(-ax * S.y, ax * S.x);
     fy[c] = make_float2(-ay * S.y, ay * S.x);
     fz[c] = make_float2(-az * S.y, az * S.x);
+  }
   }
 }
 
@@ -410,16 +426,21 @@ int mgp_launch_finalize_kd(mgp_dstate *dst, const double *partials, int nblocks,
 __global__ void k_div_laplacian(const float2 *__restrict__ dk, float2 *__restrict__ out, int N, float norm) {
   const int NH = N / 2 + 1;
   const long long total = (long long)N * N * NH;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += stride) {
-    int kz = (int)(c % NH);
-    long long r = c / NH;
-    int j = (int)(r % N), i = (int)(r / N);
+  (void)total;
+  const int lane = threadIdx.x & 31;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  // one warp per (i, j) row of the half-complex grid, lanes along kz
+  for (long long r = wid; r < (long long)N * N; r += nw) {
+    const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+    for (int kz = lane; kz < NH; kz += 32) {
+    const long long c = r * NH + kz;
     int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
     int rk = d0 * d0 + d1 * d1 + kz * kz;
     float2 z = dk[c];
     float f = rk == 0 ? 0.0f : -norm / (float)rk;
     out[c] = make_float2(f * z.x, f * z.y);
+  }
   }
 }
 
@@ -436,11 +457,15 @@ __global__ void k_smooth(const float2 *__restrict__ dk, float2 *__restrict__ out
                          float norm) {
   const int NH = N / 2 + 1;
   const long long total = (long long)N * N * NH;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += stride) {
-    int kz = (int)(c % NH);
-    long long r = c / NH;
-    int j = (int)(r % N), i = (int)(r / N);
+  (void)total;
+  const int lane = threadIdx.x & 31;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  // one warp per (i, j) row of the half-complex grid, lanes along kz
+  for (long long r = wid; r < (long long)N * N; r += nw) {
+    const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+    for (int kz = lane; kz < NH; kz += 32) {
+    const long long c = r * NH + kz;
     int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
     int rk = d0 * d0 + d1 * d1 + kz * kz;
     float kR = sqrtf((float)rk) * kR1, f = 1.0f;
@@ -450,6 +475,7 @@ __global__ void k_smooth(const float2 *__restrict__ dk, float2 *__restrict__ out
     f *= norm;
     float2 z = dk[c];
     out[c] = make_float2(f * z.x, f * z.y);
+  }
   }
 }
 
@@ -598,11 +624,15 @@ __device__ __forceinline__ int ic_d(int idx, int N) { return idx < N / 2 ? idx :
 __global__ void k_ic_grad6(const float2 *__restrict__ dk, float *__restrict__ out, long long gf, int N) {
   const int NH = N / 2 + 1;
   const long long total = (long long)N * N * NH;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += stride) {
-    int kz = (int)(c % NH);
-    long long r = c / NH;
-    int j = (int)(r % N), i = (int)(r / N);
+  (void)total;
+  const int lane = threadIdx.x & 31;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  // one warp per (i, j) row of the half-complex grid, lanes along kz
+  for (long long r = wid; r < (long long)N * N; r += nw) {
+    const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+    for (int kz = lane; kz < NH; kz += 32) {
+    const long long c = r * NH + kz;
     int d[3] = {ic_d(i, N), ic_d(j, N), ic_d(kz, N)};
     int rk = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
     float2 z = dk[c];
@@ -613,6 +643,7 @@ __global__ void k_ic_grad6(const float2 *__restrict__ dk, float *__restrict__ ou
       float f = inv * (float)(d[A[g]] * d[B[g]]);
       ((float2 *)(out + g * gf))[c] = make_float2(f * z.x, f * z.y);
     }
+  }
   }
 }
 
@@ -651,11 +682,15 @@ __global__ void k_ic_disp(const float2 *__restrict__ dk, const float *__restrict
                           long long gf, int N, float box_over_2pi) {
   const int NH = N / 2 + 1;
   const long long total = (long long)N * N * NH;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += stride) {
-    int kz = (int)(c % NH);
-    long long r = c / NH;
-    int j = (int)(r % N), i = (int)(r / N);
+  (void)total;
+  const int lane = threadIdx.x & 31;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  // one warp per (i, j) row of the half-complex grid, lanes along kz
+  for (long long r = wid; r < (long long)N * N; r += nw) {
+    const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+    for (int kz = lane; kz < NH; kz += 32) {
+    const long long c = r * NH + kz;
     int d[3] = {ic_d(i, N), ic_d(j, N), ic_d(kz, N)};
     int rk = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
     float2 z = dk[c];
@@ -669,6 +704,7 @@ __global__ void k_ic_disp(const float2 *__restrict__ dk, const float *__restrict
       ((float2 *)(out + a * gf))[c] = make_float2(-f * z.y, f * z.x);
       ((float2 *)(out + (3 + a) * gf))[c] = make_float2(f * S.y, -f * S.x);
     }
+  }
   }
 }
 
