@@ -229,6 +229,24 @@ int mgp_copy_grid(mgp_ctx *ctx, int which, float *host, size_t count);
  * "mg", "step" = the whole mgp_step); returns -1 if not timed.  Timing is on when enable != 0. */
 int mgp_set_timing(mgp_ctx *ctx, int enable);
 double mgp_kernel_ms(mgp_ctx *ctx, const char *name);
+/* P(k) binning for callers that cannot allocate (no counterpart in the
+ * reference): for code running inside another framework's memory pool or
+ * allocator hooks, or that must not let cudaMalloc/cudaFree synchronise the
+ * device.  Bins the caller's delta(k) grid (device pointer, complex
+ * [Nmesh][Nmesh][Nmesh/2+1] float pairs, the R2C of a CIC density) exactly as
+ * mgp_pofk does, with every scratch buffer in one fixed-size device array
+ * owned by the library (about 8 MB, held on each device that loads the
+ * library until exit); it calls no cudaMalloc, cudaFree or other allocating
+ * routine.  Limits: even Nmesh <= 1024, at most 2048 bins after the
+ * reference's parameter adjustment; larger requests return MGP_EINVAL.  Runs
+ * on the current device and on `stream` (NULL = legacy default stream) and
+ * returns after the results are in the host arrays.  The first call on a
+ * device looks up the array's device address.  All calls share the array:
+ * calls whose GPU work overlaps race and must be serialised by the caller. */
+int mgp_pofk_noalloc(const float *d_deltak, int Nmesh, int Nsample, double Box, int nbins, int bintype,
+                     int subtract_shotnoise, double kmin, double kmax, int cap, int *nbins_out, double *k,
+                     double *pk, double *kmean, double *n, void *stream);
+
 /* Process-wide number of this library's own kernel launches so far (cuFFT
  * launches are not included). */
 long long mgp_launch_count(mgp_ctx *ctx);

@@ -22,7 +22,7 @@ EXPORTS = [
     "mgp_displacement_fields", "mgp_get_displacements", "mgp_kick_drift", "mgp_step", "mgp_run", "mgp_pofk",
     "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
     "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_launch_count",
-    "mgp_host_register", "mgp_host_unregister",
+    "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc",
 ]
 
 
@@ -108,6 +108,8 @@ def lib():
         L.mgp_launch_count.restype = C.c_longlong
         L.mgp_host_register.argtypes = [vp, C.c_size_t]
         L.mgp_host_unregister.argtypes = [vp]
+        L.mgp_pofk_noalloc.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double,
+                                       C.c_double, C.c_int, C.POINTER(C.c_int), dp, dp, dp, dp, vp]
         _lib = L
     return _lib
 
@@ -154,6 +156,18 @@ def cosmo_coeff(params, kind, ai, af, aref):
     out = np.zeros_like(ai)
     _check(lib().mgp_cosmo_coeff(C.byref(params), kind, _dptr(ai), _dptr(af), _dptr(aref), ai.size, _dptr(out)))
     return out
+
+
+def pofk_noalloc(d_deltak, Nmesh, Nsample, Box, nbins, bintype, subtract_shotnoise, kmin, kmax, stream=None):
+    """Allocation-free P(k) of a caller-owned device delta(k) grid (see
+    mgp_pofk_noalloc in include/mgpicola.h)."""
+    cap = max(nbins, Nmesh, 1)
+    k, pk, km, n = (np.zeros(cap) for _ in range(4))
+    nb = C.c_int(0)
+    _check(lib().mgp_pofk_noalloc(d_deltak, Nmesh, Nsample, Box, nbins, bintype, subtract_shotnoise, kmin, kmax,
+                                  cap, C.byref(nb), _dptr(k), _dptr(pk), _dptr(km), _dptr(n), stream))
+    m = nb.value
+    return k[:m], pk[:m], km[:m], n[:m]
 
 
 def pin(arr):
