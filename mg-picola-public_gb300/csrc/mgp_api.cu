@@ -147,6 +147,28 @@ static int setup_pofk(mgp_ctx *c) {
   }
   MGP_CUDA(cudaMalloc(&c->rk_bin, sizeof(int) * (rkmax + 1)));
   MGP_CUDA(cudaMemcpy(c->rk_bin, rkb.data(), sizeof(int) * (rkmax + 1), cudaMemcpyHostToDevice));
+  // first |k|^2 of each bin: the bin index is monotone in |k|^2 over one
+  // contiguous range [rlo, rhi) and -1 outside it
+  {
+    int rlo = -1, rhi = 0;
+    for (int rk = 0; rk <= rkmax; rk++)
+      if (rkb[rk] >= 0) {
+        if (rlo < 0) rlo = rk;
+        rhi = rk + 1;
+      }
+    if (rlo < 0) rlo = rhi = 0;
+    std::vector<int> thr(nbins + 1);
+    int rk = rlo;
+    for (int b = 0; b < nbins; b++) {
+      while (rk < rhi && rkb[rk] < b) rk++;
+      thr[b] = rk;
+    }
+    thr[nbins] = rhi;
+    for (int q = rlo; q < rhi; q++)
+      if (rkb[q] < 0) return mgp_set_error(MGP_EINVAL, "P(k) binning is not monotone in |k|");
+    MGP_CUDA(cudaMalloc(&c->pk_thr, sizeof(int) * (nbins + 1)));
+    MGP_CUDA(cudaMemcpy(c->pk_thr, thr.data(), sizeof(int) * (nbins + 1), cudaMemcpyHostToDevice));
+  }
   MGP_CUDA(cudaMalloc(&c->win1d, sizeof(float) * (h + 1)));
   MGP_CUDA(cudaMemcpy(c->win1d, win.data(), sizeof(float) * (h + 1), cudaMemcpyHostToDevice));
   // enough warps to cover the SMs; each warp owns whole (i, j) rows
@@ -204,10 +226,6 @@ static int validate(const mgp_params *p) {
   if (p->Nsample < 1 || p->Nsample > 2048) return mgp_set_error(MGP_EINVAL, "Nsample = %d out of range", p->Nsample);
   if (!(p->Box > 0)) return mgp_set_error(MGP_EINVAL, "Box must be positive");
   if (p->model < 0 || p->model > 4) return mgp_set_error(MGP_EINVAL, "unknown model %d", p->model);
-  if (p->model == MGP_MODEL_MBETA && p->modified_gravity_active)
-    return mgp_set_error(MGP_EINVAL, "MBETA model is not available in this build");
-  if (p->model == MGP_MODEL_BRANSDICKE && p->modified_gravity_active)
-    return mgp_set_error(MGP_EINVAL, "BRANSDICKE model is not available in this build");
   if (p->scaledependent) return mgp_set_error(MGP_EINVAL, "SCALEDEPENDENT growth is not available in this build");
   if ((p->WhichSpectrum != 0) && (p->WhichTransfer != 0))
     return mgp_set_error(MGP_EINVAL, "can't run with both power spectrum and transfer function");
@@ -224,7 +242,7 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   for (int i = 0; i < 3; i++)
     if (plans[i]) cufftDestroy(plans[i]);
   void *bufs[] = {c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
-                  c->fft_work, c->rk_bin, c->win1d, c->pk_block, c->pk_sum};
+                  c->fft_work, c->rk_bin, c->pk_thr, c->win1d, c->pk_block, c->pk_sum};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
     if (bufs[i]) cudaFree(bufs[i]);
   for (int t = 0; t < MGP_NTIMERS; t++) {
@@ -257,6 +275,10 @@ extern "C" int mgp_create(const mgp_params *p, int device, mgp_ctx **out) {
     free(c);
     return mgp_set_error(rc, "%s", err);
   }
+  // the Brans-Dicke background solve replaces Omega and h (init_modified_version,
+  // src/user_defined_functions.h:135-143); the time step uses the new values
+  c->p.Omega = c->cosmo.p.Omega;
+  c->p.HubbleParam = c->cosmo.p.HubbleParam;
 #define TRY(x)            \
   do {                    \
     int r_ = (x);         \
@@ -431,7 +453,7 @@ static int require_particles(mgp_ctx *c) {
 // MG fifth force (ComputeFifthForce, src/user_defined_functions.h:687-719 and
 // src/mg.h) given delta(x) in rho and delta(k) in dk.  Leaves the MG source
 // for the force pass in rho (as complex) and returns the fused k-space mode.
-static int fifth_force(mgp_ctx *c, double A, int *mg_kind, float *coupling, float *mass2) {
+static int fifth_force(mgp_ctx *c, double A, int filtered, int *mg_kind, float *coupling, float *mass2) {
   const mgp_params *p = &c->p;
   const int N = c->g.N;
   *mg_kind = 0;
@@ -443,7 +465,7 @@ static int fifth_force(mgp_ctx *c, double A, int *mg_kind, float *coupling, floa
     // ComputeFifthForce_PotentialScreening, src/mg.h:147-189
     if (p->include_screening) {
       double norm = 1.0 / pow((double)N, 3) * 1.5 * p->Omega / A * pow(p->Box / 2997.92458 / (2.0 * M_PI), 2);
-      RET_IF(mgp_launch_div_laplacian(c->dk, c->mg1, N, (float)norm, c->stream));
+      if (!filtered) RET_IF(mgp_launch_div_laplacian(c->dk, c->mg1, N, (float)norm, c->stream));
       MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
       RET_IF(mgp_launch_screen_potential(c->rho, c->mg1, nr, (float)mgp_phicrit(&c->cosmo, A), c->stream));
     }
@@ -460,20 +482,46 @@ static int fifth_force(mgp_ctx *c, double A, int *mg_kind, float *coupling, floa
       return MGP_OK;
     }
     double kR1 = 2.0 * M_PI / p->Box * p->Rsmooth;
-    RET_IF(mgp_launch_smooth(c->dk, c->mg1, N, p->smoothing_filter, (float)kR1, (float)(1.0 / pow((double)N, 3)),
-                             c->stream));
+    if (!filtered)
+      RET_IF(mgp_launch_smooth(c->dk, c->mg1, N, p->smoothing_filter, (float)kR1, (float)(1.0 / pow((double)N, 3)),
+                               c->stream));
     MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
     RET_IF(mgp_launch_screen_density(c->rho, c->mg1, nr, (float)coupling_d,
                                      (float)mgp_dgp_screen_prefactor(&c->cosmo, A), c->stream));
     MGP_CUFFT(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
     *mg_kind = 2;
+  } else if (p->model == MGP_MODEL_BRANSDICKE) {
+    // ComputeFifthForce_TimeDepGeffModels (src/mg.h:127-137): the source
+    // is delta(k) Geff/G(a), applied inside the force pass
+    *mg_kind = 3;
+    *coupling = (float)(mgp_geff(&c->cosmo, A, 0.0) - 1.0);
   }
   return MGP_OK;
 }
 
-static int pofk_now(mgp_ctx *c) {
-  RET_IF(mgp_launch_pofk(c->dk, c->g.N, c->rk_bin, c->win1d, c->pk_nbins, c->pk_block, c->pk_blocks, c->pk_sum,
-                         c->stream));
+// k-space filter of the fifth force that can ride on the P(k) pass
+// (both read delta(k) once): 1 smoothing for density screening, 2 inverse
+// Laplacian for potential screening; 0 none.
+static int mg_filter_kind(const mgp_params *p) {
+  if (!p->modified_gravity_active || !p->include_screening) return 0;
+  if (p->model == MGP_MODEL_DGP) return 1;
+  if (p->model == MGP_MODEL_FOFR || p->model == MGP_MODEL_MBETA) return 2;
+  return 0;
+}
+
+static int pofk_now(mgp_ctx *c, int fuse_kind, double A) {
+  const mgp_params *p = &c->p;
+  const int N = c->g.N;
+  float fa = 0.f, fb = 0.f;
+  if (fuse_kind == 1) {
+    fa = (float)(2.0 * M_PI / p->Box * p->Rsmooth);
+    fb = (float)(1.0 / pow((double)N, 3));
+  } else if (fuse_kind == 2) {
+    fb = (float)(1.0 / pow((double)N, 3) * 1.5 * p->Omega / A * pow(p->Box / 2997.92458 / (2.0 * M_PI), 2));
+  }
+  RET_IF(mgp_launch_pofk_thr(c->dk, N, c->pk_thr, c->win1d, c->pk_nbins, c->pk_bintype, c->pk_kmin, c->pk_kmax,
+                             c->pk_block, c->pk_blocks, c->pk_sum, fuse_kind, p->smoothing_filter,
+                             fuse_kind ? c->mg1 : NULL, fa, fb, c->stream));
   return MGP_OK;
 }
 
@@ -491,15 +539,17 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   tstop(c, T_R2C);
   c->have_density = 1;
   c->last_density_a = A;
+  int fused = 0;
   if (c->p.pofk_compute_every_step) {
+    fused = mg_filter_kind(&c->p);
     tstart(c, T_POFK);
-    RET_IF(pofk_now(c));
+    RET_IF(pofk_now(c, fused, A));
     tstop(c, T_POFK);
   }
   int mg_kind = 0;
   float coupling = 0.f, mass2 = 0.f;
   tstart(c, T_MG);
-  RET_IF(fifth_force(c, A, &mg_kind, &coupling, &mass2));
+  RET_IF(fifth_force(c, A, fused, &mg_kind, &coupling, &mass2));
   tstop(c, T_MG);
   // Forces, src/auxPM.c:437-555
   tstart(c, T_FORCES);
@@ -560,7 +610,7 @@ extern "C" int mgp_step(mgp_ctx *c, double A, double AI, double AF, double AFF) 
 extern "C" int mgp_pofk(mgp_ctx *c, int cap, int *nbins, double *k, double *pk, double *kmean, double *n) {
   RET_IF(require_particles(c));
   if (!c->have_density) return mgp_set_error(MGP_ESTATE, "no density: call mgp_get_displacements first");
-  if (!c->p.pofk_compute_every_step) RET_IF(pofk_now(c));
+  if (!c->p.pofk_compute_every_step) RET_IF(pofk_now(c, 0, c->last_density_a));
   const int nb = c->pk_nbins;
   if (nbins) *nbins = nb;
   if (cap < nb) return mgp_set_error(MGP_EINVAL, "P(k) capacity %d < %d bins", cap, nb);

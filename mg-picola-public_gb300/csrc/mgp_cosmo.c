@@ -24,9 +24,12 @@
 
 int mgp_set_error(int code, const char *fmt, ...);
 
+static double spline_eval(const mgp_spline *s, double x);
+
 /* ------------------------------------------------------------------ hooks */
 double mgp_hubble(const mgp_cosmo *c, double a) {
   const double om = c->p.Omega;
+  if (c->have_jbd) return spline_eval(&c->jbdH, log(a));
   if (c->p.use_w0wa)
     return sqrt(om / (a * a * a) + (1.0 - om) * exp(3.0 * c->p.w_a * (a - 1) - 3 * (1 + c->p.w_0 + c->p.w_a) * log(a)));
   return sqrt(om / (a * a * a) + 1.0 - om);
@@ -34,6 +37,7 @@ double mgp_hubble(const mgp_cosmo *c, double a) {
 
 double mgp_dhubbleda(const mgp_cosmo *c, double a) {
   const double om = c->p.Omega;
+  if (c->have_jbd) return spline_eval(&c->jbddH, log(a));
   double rhs = -3.0 * om / (a * a * a * a);
   if (c->p.use_w0wa) rhs += -3.0 * (1.0 - om) * (1.0 + c->p.w_0 + c->p.w_a * (1 - a)) / a;
   return rhs / (2.0 * mgp_hubble(c, a));
@@ -77,6 +81,7 @@ double mgp_coupling(const mgp_cosmo *c, double a) {
       return 2.0 * b * b;
     }
     case MGP_MODEL_DGP: return 1.0 / (3.0 * mgp_beta_dgp(c, a));
+    case MGP_MODEL_BRANSDICKE: return c->have_jbd ? spline_eval(&c->jbdG, log(a)) - 1.0 : 0.0;
     default: return 0.0;
   }
 }
@@ -92,6 +97,7 @@ double mgp_geff(const mgp_cosmo *c, double a, double k) {
       return 1.0 + 2.0 * b * b * k2 / (k2 + a * a * mgp_mass2_of_a(c, a));
     }
     case MGP_MODEL_DGP: return 1.0 + 1.0 / (3.0 * mgp_beta_dgp(c, a));
+    case MGP_MODEL_BRANSDICKE: return 1.0 + mgp_coupling(c, a);
     default: return 1.0;
   }
 }
@@ -107,6 +113,7 @@ double mgp_factor_2lpt(const mgp_cosmo *c, double a) {
 
 double mgp_phicrit(const mgp_cosmo *c, double a) {
   const double om = c->p.Omega;
+  if (c->p.model == MGP_MODEL_MBETA) return c->have_phia ? spline_eval(&c->phia, log(a)) : 0.0;
   return 1.5 * c->p.fofr0 * pow((om + 4.0 * (1.0 - om)) / (om / (a * a * a) + 4.0 * (1.0 - om)), c->p.nfofr + 1.0);
 }
 
@@ -439,6 +446,144 @@ double mgp_cosmo_sigma8_enh(const mgp_cosmo *c, double a) {
   return spline_eval(&c->D, log(a)) / spline_eval(&c->DL, log(a));
 }
 
+/* ------------------------------------------------ Brans-Dicke background */
+/* JBD_Solve_Background (src/jbd.c): y = ln(phi/phi0) and z over x = ln a
+ * from z = 1e6 to a = 1 (10000 points), phi_ini found by bisection so that
+ * phi(a=1) = phi0 to 1e-6; Geff/G = e^-y, H from the modified Friedmann
+ * equation.  Integrated here with the Dormand-Prince pair. */
+typedef struct { double w, om, orr, ov; } jbd_par;
+
+static double jbd_H(const jbd_par *g, double x, double y, double dy) {
+  return sqrt(exp(-y) * (g->orr * exp(-4 * x) + g->om * exp(-3 * x) + g->ov) / (1.0 + dy - g->w / 6 * dy * dy));
+}
+static double jbd_dHdx(const jbd_par *g, double x, double y, double dy) {
+  double H = jbd_H(g, x, y, dy);
+  double om = g->om * exp(-y - 3.0 * x) / (H * H), ov = g->ov * exp(-y) / (H * H);
+  double ora = g->orr * exp(-y - 4.0 * x) / (H * H);
+  return H / 2.0 * (-3.0 - ora - g->w / 2.0 * dy * dy + dy - 3.0 * (om + 4.0 * ov) / (3.0 + 2.0 * g->w) + 3.0 * ov);
+}
+static double jbd_H_of_z(const jbd_par *g, double x, double y, double z) {
+  return sqrt(exp(-y) * (g->orr * exp(-4 * x) + g->om * exp(-3 * x) + g->ov) +
+              z * z / 12.0 * (2.0 * g->w + 3.0) * exp(-2 * y - 6 * x)) -
+         z / 2.0 * exp(-y - 3 * x);
+}
+static void jbd_rhs(const jbd_par *g, double x, const double *u, double *f) {
+  double hubb = jbd_H_of_z(g, x, u[0], u[1]);
+  f[0] = u[1] * exp(-u[0] - 3 * x) / hubb;
+  f[1] = 3.0 * exp(3.0 * x) / (2 * g->w + 3) / hubb * (g->om * exp(-3 * x) + 4.0 * g->ov);
+}
+/* generic 2-component Dormand-Prince step driver */
+static int dp45_2(const jbd_par *g, double x0, double x1, double *u, double *hguess) {
+  double x = x0, h = *hguess;
+  int steps = 0;
+  while (x < x1) {
+    if (x + h > x1) h = x1 - x;
+    double k[7][2], ut[2], u5[2], err = 0.0;
+    for (int s = 0; s < 7; s++) {
+      for (int i = 0; i < 2; i++) {
+        double acc = u[i];
+        for (int j = 0; j < s; j++) acc += h * DP_A[s][j] * k[j][i];
+        ut[i] = acc;
+      }
+      jbd_rhs(g, x + DP_C[s] * h, ut, k[s]);
+    }
+    for (int i = 0; i < 2; i++) {
+      double s5 = u[i], s4 = u[i];
+      for (int s = 0; s < 7; s++) { s5 += h * DP_B5[s] * k[s][i]; s4 += h * DP_B4[s] * k[s][i]; }
+      u5[i] = s5;
+      double sc = 1e-11 * (fabs(u[i]) > fabs(s5) ? fabs(u[i]) : fabs(s5)) + 1e-13;
+      double e = fabs(s5 - s4) / sc;
+      if (e > err) err = e;
+    }
+    if (err <= 1.0) { x += h; u[0] = u5[0]; u[1] = u5[1]; }
+    double fac = err > 0 ? 0.9 * pow(err, -0.2) : 5.0;
+    if (fac > 5.0) fac = 5.0;
+    if (fac < 0.2) fac = 0.2;
+    h *= fac;
+    if (++steps > 10000000 || !(h > 1e-15)) return -1;
+  }
+  *hguess = h;
+  return 0;
+}
+
+static int jbd_solve(mgp_cosmo *c, char *err, size_t errlen) {
+  const int npts = 10000;
+  jbd_par g = {c->p.wBD, c->p.Omegah2, c->p.Omegarh2, c->p.Omegavh2};
+  double xini = log(1.0 / (1.0 + 1e6)), dx = (0.0 - xini) / (double)(npts - 1);
+  double *x = (double *)malloc(sizeof(double) * npts * 4), *y = x + npts, *dy = y + npts, *t = dy + npts;
+  double lo = 0.0, hi = 1.0;
+  int ok = 0;
+  for (int it = 0; it < 200; it++) {
+    double phinow = 0.5 * (lo + hi), yi = log(phinow);
+    double u[2] = {yi, jbd_H(&g, xini, yi, 0.0) * exp(3.0 * xini + yi) * 0.0}, h = 1e-4;
+    x[0] = xini; y[0] = u[0]; dy[0] = u[1];
+    int bad = 0;
+    for (int i = 1; i < npts && !bad; i++) {
+      double xn = xini + i * dx;
+      if (dp45_2(&g, xini + (i - 1) * dx, xn, u, &h)) bad = 1;
+      x[i] = xn;
+      y[i] = u[0];
+      dy[i] = u[1] / jbd_H_of_z(&g, xn, u[0], u[1]) * exp(-3.0 * xn - u[0]);
+    }
+    if (bad) break;
+    double r = exp(y[npts - 1]);
+    if (fabs(r - 1.0) < 1e-6) { ok = 1; break; }
+    if (r < 1.0) lo = phinow; else hi = phinow;
+  }
+  if (!ok) {
+    free(x);
+    snprintf(err, errlen, "Brans-Dicke background: no phi_ini gives phi(a=1) = phi0");
+    return MGP_ENUMERIC;
+  }
+  double h = jbd_H(&g, 0.0, y[npts - 1], dy[npts - 1]);
+  double *G = (double *)malloc(sizeof(double) * npts * 3), *H = G + npts, *dH = H + npts;
+  for (int i = 0; i < npts; i++) {
+    G[i] = exp(-y[i]);
+    H[i] = jbd_H(&g, x[i], y[i], dy[i]) / h;
+    dH[i] = jbd_dHdx(&g, x[i], y[i], dy[i]) / h * exp(-x[i]);
+  }
+  spline_init(&c->jbdG, x, G, npts);
+  spline_init(&c->jbdH, x, H, npts);
+  spline_init(&c->jbddH, x, dH, npts);
+  (void)t;
+  free(x);
+  free(G);
+  c->have_jbd = 1;
+  /* init_modified_version (user_defined_functions.h:135-143) */
+  c->p.HubbleParam = h;
+  c->p.Omega = c->p.Omegah2 / (h * h);
+  return MGP_OK;
+}
+
+/* compute_phi_of_a (src/cosmo.c:104-190): phi(a) = int 9 Omega beta /
+ * (m^2 a^3) dln a from z = max(200, z_init), then phi_crit = phi / (2 beta). */
+static double phia_integrand(double x, const void *par) {
+  const mgp_cosmo *c = (const mgp_cosmo *)par;
+  double a = exp(x), beta = mgp_beta_of_a(c, a), m2 = mgp_mass2_of_a(c, a);
+  if (beta == 0.0) return 0.0;
+  return 9.0 * c->p.Omega * beta / (m2 * a * a * a);
+}
+static int phia_solve(mgp_cosmo *c) {
+  const int npts = 1000;
+  double zini = c->p.Init_Redshift > 200.0 ? c->p.Init_Redshift : 200.0;
+  double xmin = log(1.0 / (1.0 + zini)), xmax = log(1.0 / (1.0 - 0.5)), dx = (xmax - xmin) / (double)(npts - 1);
+  double *x = (double *)malloc(sizeof(double) * npts * 2), *ph = x + npts;
+  x[0] = xmin;
+  ph[0] = 0.0;
+  for (int i = 1; i < npts; i++) {
+    x[i] = xmin + i * dx;
+    ph[i] = ph[i - 1] + quad(phia_integrand, c, xmin + (i - 1) * dx, x[i], 1);
+  }
+  for (int i = 0; i < npts; i++) {
+    double b = mgp_beta_of_a(c, exp(x[i]));
+    if (b != 0.0) ph[i] /= 2.0 * b;
+  }
+  spline_init(&c->phia, x, ph, npts);
+  free(x);
+  c->have_phia = 1;
+  return MGP_OK;
+}
+
 int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen) {
   memset(c, 0, sizeof(*c));
   c->p = *p;
@@ -457,10 +602,17 @@ int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen) 
     return MGP_ENUMERIC;
   }
   c->norm = p->Sigma8 * p->Sigma8 / s2;
+  /* init_modified_version runs after initialize_powerspectrum in main.c
+   * (main.c:186-196), so the normalisation above uses the file's Omega/h */
+  if (p->model == MGP_MODEL_BRANSDICKE && (rc = jbd_solve(c, err, errlen))) return rc;
+  if (p->model == MGP_MODEL_MBETA && p->modified_gravity_active) phia_solve(c);
   return solve_growth(c, err, errlen);
 }
 
 void mgp_cosmo_free(mgp_cosmo *c) {
+  mgp_spline *ex[4] = {&c->jbdH, &c->jbddH, &c->jbdG, &c->phia};
+  for (int i = 0; i < 4; i++)
+    if (ex[i]->x) spline_free(ex[i]);
   mgp_spline *sp[12] = {&c->D, &c->dDdy, &c->ddDddy, &c->D2, &c->dD2dy, &c->ddD2ddy,
                         &c->DL, &c->dDLdy, &c->ddDLddy, &c->D2L, &c->dD2Ldy, &c->ddD2Lddy};
   for (int i = 0; i < 12; i++)

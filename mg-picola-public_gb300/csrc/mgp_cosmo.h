@@ -21,6 +21,12 @@ typedef struct mgp_cosmo {
   /* growth splines over x = ln a (src/cosmo.c:54-95) */
   mgp_spline D, dDdy, ddDddy, D2, dD2dy, ddD2ddy;
   mgp_spline DL, dDLdy, ddDLddy, D2L, dD2Ldy, ddD2Lddy;
+  /* Brans-Dicke background (src/jbd.c): H(a)/H0, dH/da, Geff/G over ln a */
+  int have_jbd;
+  mgp_spline jbdH, jbddH, jbdG;
+  /* m(a), beta(a) models: phi_crit(a) over ln a (src/cosmo.c:104-190) */
+  int have_phia;
+  mgp_spline phia;
   /* power spectrum */
   double norm;
   int ntab;

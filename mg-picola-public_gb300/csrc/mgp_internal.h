@@ -69,6 +69,7 @@ struct mgp_ctx {
   int pk_nbins, pk_bintype, pk_sub;
   double pk_kmin, pk_kmax;  /* integer-k units, adjusted */
   int *rk_bin;              /* device: bin index per integer |k|^2 (or -1) */
+  int *pk_thr;              /* device: first |k|^2 of each bin, [nbins] = end */
   float *win1d;             /* device: 1/sinc^4 per |d| in [0, N/2] */
   double *pk_block;         /* device: per-block FP64 bin partials */
   double *pk_sum;           /* device: FP64 bin sums */
@@ -140,6 +141,9 @@ int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, i
                    float wpar, float *rho, long long P, cudaStream_t stream);
 int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins,
                     double *block_part, int nblocks, double *sums, cudaStream_t st);
+int mgp_launch_pofk_thr(const float *dk, int N, const int *thr, const float *win, int nbins, int bintype, double kmin,
+                        double kmax, double *block_part, int nblocks, double *sums, int fuse_kind, int filter,
+                        float *fuse_out, float fuse_a, float fuse_b, cudaStream_t st);
 int mgp_launch_forces(const float *dk, const float *mgk, float mg_coupling, float mg_mass2, int mg_kind,
                       int N, double box, float *frc, long long grid_floats, cudaStream_t st);
 int mgp_launch_ikd(const float *frc, long long grid_floats, int N, long long P, int Ns, long long np,

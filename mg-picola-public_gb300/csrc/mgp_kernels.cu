@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "mgp_internal.h"
 #include "mgp_rng.h"
@@ -70,7 +71,11 @@ __device__ __forceinline__ void cell_frac(int li, float s, float off_cells, int 
 
 __global__ void k_fill(float *__restrict__ p, long long n, float v) {
   long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = v;
+  long long n4 = n >> 2;  // grids are 256-byte aligned; n % 4 tail handled below
+  float4 v4 = make_float4(v, v, v, v);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride)
+    reinterpret_cast<float4 *>(p)[i] = v4;
+  for (long long i = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = v;
 }
 
 int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st) {
@@ -136,37 +141,88 @@ int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, i
 // same bin are contiguous (|k| grows along kz), so a segmented warp scan sums
 // each run in FP32 and the last lane of a run adds it to an FP64 shared-memory
 // bin; blocks write FP64 partials that k_pofk_reduce sums in fixed order.
-// priv != 0: every warp owns a private FP64 copy of the bins (the run tails
-// of one warp always hit distinct bins, so plain adds suffice); otherwise
-// the block shares one copy updated with FP64 shared-memory atomics.
-__global__ void __launch_bounds__(MGP_THREADS) k_pofk(const float2 *__restrict__ dk, int N, const int *__restrict__ rk_bin,
-                                                      const float *__restrict__ win, int nbins, int priv,
-                                                      double *__restrict__ block_part) {
-  extern __shared__ double shd[];
-  const int nwb = priv ? (int)(blockDim.x >> 5) : 1;
-  for (int b = threadIdx.x; b < nbins * nwb; b += blockDim.x) shd[b] = 0.0;
+// Bin lookup: with `thr` (first |k|^2 of every bin, thr[nbins] = end of the
+// binned range; bins are monotone in |k|^2) a float estimate of the bin is
+// corrected against the exact integer thresholds held in shared memory, which
+// reproduces the host's double-precision pofk_bin_index for every mode;
+// without it the per-|k|^2 table rk_bin is read from global memory.
+// Fused k-space output (one read of delta(k) serves both): fuse_kind 1 writes
+// delta(k) W(kR) norm (SmoothDensityField, src/mg.h:268-309), 2 writes
+// -norm delta(k)/RK (DivideByLaplacian, src/mg.h:21-64).
+struct mgp_pofk_kargs {
+  const float2 *dk;
+  int N, nbins, bintype;
+  const int *rk_bin;   // used when thr == NULL
+  const int *thr;      // nbins + 1 thresholds, or NULL
+  const float *win;
+  float kmin, kmax;    // integer-k units (estimate only)
+  double *block_part;
+  int fuse_kind, filter;
+  float2 *fuse_out;
+  float fuse_a, fuse_b;
+};
+
+// Bin sums: native FP32 shared-memory atomics made exact to second order by
+// a compensated (TwoSum) split: the atomic returns the old value, so the
+// rounding error of every addition is recovered and added to a second FP32
+// array; hi + lo carries about twice FP32's precision.
+__global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
+  extern __shared__ float shf[];
+  const int N = a.N, nbins = a.nbins, NH = N / 2 + 1, h = N / 2;
+  float *shi = shf, *slo = shf + nbins;
+  int *sthr = (int *)(slo + nbins);
+  float *swin = (float *)(sthr + (a.thr ? nbins + 1 : 0));
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) shi[b] = slo[b] = 0.0f;
+  if (a.thr)
+    for (int b = threadIdx.x; b <= nbins; b += blockDim.x) sthr[b] = a.thr[b];
+  for (int d = threadIdx.x; d <= h; d += blockDim.x) swin[d] = a.win[d];
   __syncthreads();
-  double *mybins = priv ? shd + (threadIdx.x >> 5) * nbins : shd;
-  const int NH = N / 2 + 1;
   const int lane = threadIdx.x & 31;
   const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const float inv_span = (float)nbins / (a.kmax - a.kmin);
+  const float inv_logspan = a.bintype ? (float)nbins / logf(a.kmax / a.kmin) : 0.0f;
+  const int lo = a.thr ? sthr[0] : 0, hi = a.thr ? sthr[nbins] : 0;
   // one warp per (i, j) row; all lanes run the same number of chunks
   for (long long r = wid; r < (long long)N * N; r += nw) {
     const int i = (int)(r / N), j = (int)(r - (long long)i * N);
-    const int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
+    const int d0 = i > h ? N - i : i, d1 = j > h ? N - j : j;
     const int rk01 = d0 * d0 + d1 * d1;
-    const float w01 = win[d0] * win[d1];
+    const float w01 = swin[d0] * swin[d1];
     for (int k0 = 0; k0 < NH; k0 += 32) {
       const int kz = k0 + lane;
       int bin = -1;
       float pk = 0.0f;
       if (kz < NH) {
-        bin = rk_bin[rk01 + kz * kz];
+        const int rk = rk01 + kz * kz;
+        if (a.thr) {
+          if (rk >= lo && rk < hi) {
+            float km = sqrtf((float)rk);
+            float x = a.bintype ? logf(km / a.kmin) * inv_logspan : (km - a.kmin) * inv_span;
+            int b = (int)floorf(x + 0.5f);
+            b = b < 0 ? 0 : (b >= nbins ? nbins - 1 : b);
+            while (b > 0 && sthr[b] > rk) b--;
+            while (b + 1 < nbins && sthr[b + 1] <= rk) b++;
+            bin = b;
+          }
+        } else {
+          bin = a.rk_bin[rk];
+        }
+        float2 z = a.dk[r * NH + kz];
         if (bin >= 0) {
-          float2 z = dk[r * NH + kz];
           float w = (kz == 0 || 2 * kz == N) ? 1.0f : 2.0f;
-          pk = (z.x * z.x + z.y * z.y) * (w01 * win[kz] * w);
+          pk = (z.x * z.x + z.y * z.y) * (w01 * swin[kz] * w);
+        }
+        if (a.fuse_kind == 1) {
+          float kR = sqrtf((float)rk) * a.fuse_a, f = 1.0f;
+          if (a.filter == MGP_FILTER_GAUSSIAN) f = expf(-0.5f * kR * kR);
+          else if (a.filter == MGP_FILTER_TOPHAT) f = kR < 1e-5f ? 1.0f : 3.0f / (kR * kR * kR) * (sinf(kR) - kR * cosf(kR));
+          else if (a.filter == MGP_FILTER_SHARPK) f = kR < 1.0f ? 1.0f : 0.0f;
+          f *= a.fuse_b;
+          a.fuse_out[r * NH + kz] = make_float2(f * z.x, f * z.y);
+        } else if (a.fuse_kind == 2) {
+          float f = rk == 0 ? 0.0f : -a.fuse_b / (float)rk;
+          a.fuse_out[r * NH + kz] = make_float2(f * z.x, f * z.y);
         }
       }
       // segmented inclusive scan over runs of equal bin (|k| grows with kz)
@@ -183,17 +239,15 @@ __global__ void __launch_bounds__(MGP_THREADS) k_pofk(const float2 *__restrict__
       int nbin = __shfl_down_sync(0xffffffffu, bin, 1);
       bool tail = lane == 31 || nbin != bin;
       if (tail && bin >= 0) {
-        if (priv) mybins[bin] += (double)acc;
-        else atomicAdd(&mybins[bin], (double)acc);
+        float old = atomicAdd(&shi[bin], acc);
+        float sum = old + acc, bp = sum - old;
+        atomicAdd(&slo[bin], (old - (sum - bp)) + (acc - bp));
       }
     }
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
-    double t = 0.0;
-    for (int w = 0; w < nwb; w++) t += shd[w * nbins + b];
-    block_part[(long long)blockIdx.x * nbins + b] = t;
-  }
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+    a.block_part[(long long)blockIdx.x * nbins + b] = (double)shi[b] + (double)slo[b];
 }
 
 // Deterministic cross-block sum in FP64 (the MPI_Allreduce of compute_pofk.c:225).
@@ -205,20 +259,56 @@ __global__ void k_pofk_reduce(const double *__restrict__ block_part, int nblocks
   sums[b] = s;
 }
 
-int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins, double *block_part,
-                    int nblocks, double *sums, cudaStream_t st) {
-  int priv = (size_t)nbins * (MGP_THREADS / 32) * sizeof(double) <= 64 * 1024;
-  size_t shmem = sizeof(double) * (size_t)nbins * (priv ? MGP_THREADS / 32 : 1);
+static int launch_pofk(const mgp_pofk_kargs &ka, int nblocks, double *sums, cudaStream_t st) {
+  const int h = ka.N / 2;
+  size_t shmem = 2 * sizeof(float) * (size_t)ka.nbins + (ka.thr ? sizeof(int) * (size_t)(ka.nbins + 1) : 0) +
+                 sizeof(float) * (size_t)(h + 1);
   if (shmem > 48 * 1024) {
-    cudaFuncSetAttribute(k_pofk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem);
+    if (cudaFuncSetAttribute(k_pofk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem) != cudaSuccess)
+      return mgp_set_error(MGP_EINVAL, "P(k) needs %zu bytes of shared memory", shmem);
   }
-  k_pofk<<<nblocks, MGP_THREADS, shmem, st>>>((const float2 *)dk, N, rk_bin, win, nbins, priv, block_part);
+  k_pofk<<<nblocks, MGP_THREADS, shmem, st>>>(ka);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
-  k_pofk_reduce<<<(nbins + 127) / 128, 128, 0, st>>>(block_part, nblocks, nbins, sums);
+  k_pofk_reduce<<<(ka.nbins + 127) / 128, 128, 0, st>>>(ka.block_part, nblocks, ka.nbins, sums);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
+}
+
+int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins, double *block_part,
+                    int nblocks, double *sums, cudaStream_t st) {
+  mgp_pofk_kargs ka;
+  memset(&ka, 0, sizeof(ka));
+  ka.dk = (const float2 *)dk;
+  ka.N = N;
+  ka.nbins = nbins;
+  ka.rk_bin = rk_bin;
+  ka.win = win;
+  ka.block_part = block_part;
+  return launch_pofk(ka, nblocks, sums, st);
+}
+
+int mgp_launch_pofk_thr(const float *dk, int N, const int *thr, const float *win, int nbins, int bintype, double kmin,
+                        double kmax, double *block_part, int nblocks, double *sums, int fuse_kind, int filter,
+                        float *fuse_out, float fuse_a, float fuse_b, cudaStream_t st) {
+  mgp_pofk_kargs ka;
+  memset(&ka, 0, sizeof(ka));
+  ka.dk = (const float2 *)dk;
+  ka.N = N;
+  ka.nbins = nbins;
+  ka.bintype = bintype;
+  ka.thr = thr;
+  ka.win = win;
+  ka.kmin = (float)kmin;
+  ka.kmax = (float)kmax;
+  ka.block_part = block_part;
+  ka.fuse_kind = fuse_kind;
+  ka.filter = filter;
+  ka.fuse_out = (float2 *)fuse_out;
+  ka.fuse_a = fuse_a;
+  ka.fuse_b = fuse_b;
+  return launch_pofk(ka, nblocks, sums, st);
 }
 
 // ------------------------------------------------------------ force grids
@@ -248,6 +338,7 @@ __global__ void __launch_bounds__(MGP_THREADS) k_forces(const float2 *__restrict
   // one warp per (i, j) row of the half-complex grid, lanes along kz
   for (long long r = wid; r < (long long)N * N; r += nw) {
     const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+#pragma unroll 4
     for (int kz = lane; kz < NH; kz += 32) {
     const long long c = r * NH + kz;
     int dx = i > N / 2 ? i - N : i, dy = j > N / 2 ? j - N : j, dz = kz;
@@ -315,13 +406,17 @@ __device__ __forceinline__ double block_sum_d(double v, double *sh) {
   return s;
 }
 
-__global__ void __launch_bounds__(MGP_THREADS) k_interp_kick_drift(
+// IDX is the grid offset type: 32-bit when the padded grid has < 2^31
+// floats (N <= 1024), which keeps the 24-point gather in fewer registers.
+template <typename IDX>
+__global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
     const float *__restrict__ frc, long long gf, int N, long long P, int Ns, long long np, float *__restrict__ s,
     float *__restrict__ v, const float *__restrict__ D1, const float *__restrict__ D2,
     const mgp_dstate *__restrict__ st, double *__restrict__ partials, mgp_kd_args a) {
   __shared__ double sh[MGP_THREADS / 32];
   const float ox = (float)(st->cx[0] * a.scale), oy = (float)(st->cx[1] * a.scale), oz = (float)(st->cx[2] * a.scale);
   const float *F0 = frc, *F1 = frc + gf, *F2 = frc + 2 * gf;
+  const IDX Pi = (IDX)P, NPi = (IDX)N * (IDX)P;
   float accD[3] = {0.f, 0.f, 0.f}, accV[3] = {0.f, 0.f, 0.f};
   long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
@@ -333,20 +428,21 @@ __global__ void __launch_bounds__(MGP_THREADS) k_interp_kick_drift(
     cell_frac(i, sp[0], ox, N, Ns, a.scale, ix, DX);
     cell_frac(j, sp[1], oy, N, Ns, a.scale, iy, DY);
     cell_frac(k, sp[2], oz, N, Ns, a.scale, iz, DZ);
-    float TX = 1.0f - DX, TY = 1.0f - DY, TZ = 1.0f - DZ;
-    int ixn = ix + 1 == N ? 0 : ix + 1, iyn = iy + 1 == N ? 0 : iy + 1, izn = iz + 1 == N ? 0 : iz + 1;
-    long long r00 = ((long long)ix * N + iy) * P, r01 = ((long long)ix * N + iyn) * P;
-    long long r10 = ((long long)ixn * N + iy) * P, r11 = ((long long)ixn * N + iyn) * P;
-    float w000 = TX * TY * TZ, w001 = TX * TY * DZ, w010 = TX * DY * TZ, w011 = TX * DY * DZ;
-    float w100 = DX * TY * TZ, w101 = DX * TY * DZ, w110 = DX * DY * TZ, w111 = DX * DY * DZ;
+    const float TX = 1.0f - DX, TY = 1.0f - DY, TZ = 1.0f - DZ;
+    const IDX x0 = (IDX)ix * NPi, x1 = (ix + 1 == N ? 0 : (IDX)(ix + 1) * NPi);
+    const IDX y0 = (IDX)iy * Pi, y1 = (iy + 1 == N ? 0 : (IDX)(iy + 1) * Pi);
+    const IDX z0 = (IDX)iz, z1 = (iz + 1 == N ? 0 : (IDX)(iz + 1));
+    const IDX o000 = x0 + y0 + z0, o001 = x0 + y0 + z1, o010 = x0 + y1 + z0, o011 = x0 + y1 + z1;
+    const IDX o100 = x1 + y0 + z0, o101 = x1 + y0 + z1, o110 = x1 + y1 + z0, o111 = x1 + y1 + z1;
+    const float w000 = TX * TY * TZ, w001 = TX * TY * DZ, w010 = TX * DY * TZ, w011 = TX * DY * DZ;
+    const float w100 = DX * TY * TZ, w101 = DX * TY * DZ, w110 = DX * DY * TZ, w111 = DX * DY * DZ;
     float disp[3];
     const float *Fa[3] = {F0, F1, F2};
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
       const float *F = Fa[ax];
-      disp[ax] = __ldg(F + r00 + iz) * w000 + __ldg(F + r00 + izn) * w001 + __ldg(F + r01 + iz) * w010 +
-                 __ldg(F + r01 + izn) * w011 + __ldg(F + r10 + iz) * w100 + __ldg(F + r10 + izn) * w101 +
-                 __ldg(F + r11 + iz) * w110 + __ldg(F + r11 + izn) * w111;
+      disp[ax] = __ldg(F + o000) * w000 + __ldg(F + o001) * w001 + __ldg(F + o010) * w010 + __ldg(F + o011) * w011 +
+                 __ldg(F + o100) * w100 + __ldg(F + o101) * w101 + __ldg(F + o110) * w110 + __ldg(F + o111) * w111;
     }
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
@@ -403,7 +499,11 @@ int mgp_ikd_blocks(long long np) { return blocks_for(np, 8); }
 int mgp_launch_ikd(const float *frc, long long gf, int N, long long P, int Ns, long long np, float *s, float *v,
                    const float *D1, const float *D2, mgp_dstate *dst, double *partials, int nblocks,
                    const mgp_kd_args *a, cudaStream_t st) {
-  k_interp_kick_drift<<<nblocks, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a);
+  if (gf < (1LL << 31))
+    k_interp_kick_drift<int><<<nblocks, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a);
+  else
+    k_interp_kick_drift<long long><<<nblocks, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials,
+                                                                   *a);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   k_finalize_kd<<<1, MGP_THREADS, 0, st>>>(dst, partials, nblocks, 1.0 / (double)np, a->dda_omega, a->dyyy_d,
@@ -433,6 +533,7 @@ __global__ void k_div_laplacian(const float2 *__restrict__ dk, float2 *__restric
   // one warp per (i, j) row of the half-complex grid, lanes along kz
   for (long long r = wid; r < (long long)N * N; r += nw) {
     const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+#pragma unroll 4
     for (int kz = lane; kz < NH; kz += 32) {
     const long long c = r * NH + kz;
     int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
@@ -464,6 +565,7 @@ __global__ void k_smooth(const float2 *__restrict__ dk, float2 *__restrict__ out
   // one warp per (i, j) row of the half-complex grid, lanes along kz
   for (long long r = wid; r < (long long)N * N; r += nw) {
     const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+#pragma unroll 4
     for (int kz = lane; kz < NH; kz += 32) {
     const long long c = r * NH + kz;
     int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
@@ -490,16 +592,27 @@ int mgp_launch_smooth(const float *dk, float *out, int N, int filter, float kR1,
 // Potential screening (src/mg.h:174-176, screening_factor_potential at
 // src/user_defined_functions.h:725-750): rho *= min(1, |phicrit / Phi_N|)
 // where Phi_N < 0, else 1.  Padding entries are included as in the reference.
+__device__ __forceinline__ float screen_pot(float ph, float phicrit) {
+  float f = 1.0f;
+  if (ph < 0.0f) {
+    f = fabsf(phicrit / ph);
+    if (f > 1.0f) f = 1.0f;
+  }
+  return f;
+}
 __global__ void k_screen_potential(float *__restrict__ rho, const float *__restrict__ phi, long long n, float phicrit) {
   long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    float ph = phi[i], f = 1.0f;
-    if (ph < 0.0f) {
-      f = fabsf(phicrit / ph);
-      if (f > 1.0f) f = 1.0f;
-    }
-    rho[i] *= f;
+  long long n4 = n >> 2;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+    float4 r = reinterpret_cast<float4 *>(rho)[i], ph = reinterpret_cast<const float4 *>(phi)[i];
+    r.x *= screen_pot(ph.x, phicrit);
+    r.y *= screen_pot(ph.y, phicrit);
+    r.z *= screen_pot(ph.z, phicrit);
+    r.w *= screen_pot(ph.w, phicrit);
+    reinterpret_cast<float4 *>(rho)[i] = r;
   }
+  for (long long i = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    rho[i] *= screen_pot(phi[i], phicrit);
 }
 
 int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float phicrit, cudaStream_t st) {
@@ -512,14 +625,24 @@ int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float
 // Density screening (src/mg.h:241-250, screening_factor_density at
 // src/user_defined_functions.h:757-773): rho *= coupling * 2(sqrt(1+f)-1)/f,
 // f = pref (1 + delta_R), factor 1 when f < 1e-5.
+__device__ __forceinline__ float screen_den(float dsm, float pref) {
+  float fac = pref * (1.0f + dsm);
+  return fac < 1e-5f ? 1.0f : 2.0f * (sqrtf(1.0f + fac) - 1.0f) / fac;
+}
 __global__ void k_screen_density(float *__restrict__ rho, const float *__restrict__ dsm, long long n, float coupling,
                                  float pref) {
   long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    float fac = pref * (1.0f + dsm[i]);
-    float sc = fac < 1e-5f ? 1.0f : 2.0f * (sqrtf(1.0f + fac) - 1.0f) / fac;
-    rho[i] *= coupling * sc;
+  long long n4 = n >> 2;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+    float4 r = reinterpret_cast<float4 *>(rho)[i], d = reinterpret_cast<const float4 *>(dsm)[i];
+    r.x *= coupling * screen_den(d.x, pref);
+    r.y *= coupling * screen_den(d.y, pref);
+    r.z *= coupling * screen_den(d.z, pref);
+    r.w *= coupling * screen_den(d.w, pref);
+    reinterpret_cast<float4 *>(rho)[i] = r;
   }
+  for (long long i = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    rho[i] *= coupling * screen_den(dsm[i], pref);
 }
 
 int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float coupling, float pref, cudaStream_t st) {
@@ -631,6 +754,7 @@ __global__ void k_ic_grad6(const float2 *__restrict__ dk, float *__restrict__ ou
   // one warp per (i, j) row of the half-complex grid, lanes along kz
   for (long long r = wid; r < (long long)N * N; r += nw) {
     const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+#pragma unroll 4
     for (int kz = lane; kz < NH; kz += 32) {
     const long long c = r * NH + kz;
     int d[3] = {ic_d(i, N), ic_d(j, N), ic_d(kz, N)};
@@ -689,6 +813,7 @@ __global__ void k_ic_disp(const float2 *__restrict__ dk, const float *__restrict
   // one warp per (i, j) row of the half-complex grid, lanes along kz
   for (long long r = wid; r < (long long)N * N; r += nw) {
     const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+#pragma unroll 4
     for (int kz = lane; kz < NH; kz += 32) {
     const long long c = r * NH + kz;
     int d[3] = {ic_d(i, N), ic_d(j, N), ic_d(kz, N)};
@@ -812,22 +937,26 @@ int mgp_launch_ic_finish(float *D1, float *D2, float *s, float *v, long long np,
 
 // ---------------------------------------------------- particle export
 // Absolute positions wrap(q + s + cx) and velocities v + cv, AoS [np][3].
+// FP32 arithmetic: the outputs are FP32 and the wrap needs no division.
+__device__ __forceinline__ float wrap_box(float x, float box) {
+  x -= box * floorf(x / box);  // no loop: bounded work for any input
+  if (x >= box) x -= box;
+  if (x < 0.0f) x += box;
+  return (x >= box || x < 0.0f) ? 0.0f : x;
+}
+
 __global__ void k_positions(const float *__restrict__ s, const float *__restrict__ v, const mgp_dstate *__restrict__ st,
                             long long np, int Ns, double box, float *__restrict__ pos, float *__restrict__ vel) {
   long long stride = (long long)gridDim.x * blockDim.x;
-  const double dq = box / (double)Ns;
+  const float dq = (float)(box / (double)Ns), fbox = (float)box;
+  const float cx[3] = {(float)st->cx[0], (float)st->cx[1], (float)st->cx[2]};
+  const float cv[3] = {(float)st->cv[0], (float)st->cv[1], (float)st->cv[2]};
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
     int li[3];
     lattice_ijk(p, Ns, li[0], li[1], li[2]);
     for (int a = 0; a < 3; a++) {
-      if (pos) {
-        double x = li[a] * dq + (double)s[a * np + p] + st->cx[a];
-        x -= box * floor(x / box);
-        float xf = (float)x;
-        if (xf >= (float)box) xf = 0.0f;
-        pos[3 * p + a] = xf;
-      }
-      if (vel) vel[3 * p + a] = (float)((double)v[a * np + p] + st->cv[a]);
+      if (pos) pos[3 * p + a] = wrap_box((float)li[a] * dq + (s[a * np + p] + cx[a]), fbox);
+      if (vel) vel[3 * p + a] = v[a * np + p] + cv[a];
     }
   }
 }
@@ -844,15 +973,16 @@ int mgp_launch_positions(const float *s, const mgp_dstate *dst, long long np, in
 __global__ void k_set_state(float *__restrict__ s, float *__restrict__ v, const float *__restrict__ pos,
                             const float *__restrict__ vel, long long np, int Ns, double box) {
   long long stride = (long long)gridDim.x * blockDim.x;
-  const double dq = box / (double)Ns;
+  const float dq = (float)(box / (double)Ns), fbox = (float)box, half = 0.5f * (float)box;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
     int li[3];
     lattice_ijk(p, Ns, li[0], li[1], li[2]);
     for (int a = 0; a < 3; a++) {
       if (pos) {
-        double d = (double)pos[3 * p + a] - li[a] * dq;
-        d -= box * rint(d / box);
-        s[a * np + p] = (float)d;
+        float d = pos[3 * p + a] - (float)li[a] * dq;
+        if (d > half) d -= fbox;
+        if (d < -half) d += fbox;
+        s[a * np + p] = d;
       }
       if (vel) v[a * np + p] = vel[3 * p + a];
     }
@@ -888,18 +1018,17 @@ __global__ void k_output(const float *__restrict__ s, const float *__restrict__ 
                          double box, double lengthfac, double vfac, double dDdy, double dD2dy, double cola,
                          float *__restrict__ pos, float *__restrict__ vel) {
   long long stride = (long long)gridDim.x * blockDim.x;
-  const double dq = box / (double)Ns;
+  const float dq = (float)(box / (double)Ns), fbox = (float)box, lf = (float)lengthfac, vf = (float)vfac;
+  const float g1 = (float)(cola * dDdy), g2 = (float)(cola * dD2dy);
+  const float cx[3] = {(float)st->cx[0], (float)st->cx[1], (float)st->cx[2]};
+  const float mv[3] = {(float)st->mean_v[0], (float)st->mean_v[1], (float)st->mean_v[2]};
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
     int li[3];
     lattice_ijk(p, Ns, li[0], li[1], li[2]);
     for (int a = 0; a < 3; a++) {
       long long o = a * np + p;
-      double x = li[a] * dq + (double)s[o] + st->cx[a];
-      x -= box * floor(x / box);
-      if (x >= box) x = 0.0;
-      pos[3 * p + a] = (float)(lengthfac * x);
-      double vv = (double)v[o] - st->mean_v[a] + cola * ((double)D1[o] * dDdy + (double)D2[o] * dD2dy);
-      vel[3 * p + a] = (float)(vfac * vv);
+      pos[3 * p + a] = lf * wrap_box((float)li[a] * dq + (s[o] + cx[a]), fbox);
+      vel[3 * p + a] = vf * ((v[o] - mv[a]) + D1[o] * g1 + D2[o] * g2);
     }
   }
 }

@@ -24,7 +24,8 @@ class MG(C.Structure):
                 ("nfofr", C.c_double), ("rcH0", C.c_double), ("rsmooth", C.c_double),
                 ("geff_const", C.c_double), ("w0", C.c_double), ("wa", C.c_double), ("use_w0wa", C.c_int),
                 ("beta_symm", C.c_double), ("assb_symm", C.c_double), ("range_symm", C.c_double),
-                ("smoothing_filter", C.c_int)]
+                ("smoothing_filter", C.c_int), ("wBD", C.c_double), ("Omegah2", C.c_double),
+                ("Omegarh2", C.c_double), ("Omegavh2", C.c_double)]
 
 
 class Power(C.Structure):
@@ -108,6 +109,11 @@ def lib():
         L.orc_tophat_sigma2.restype = C.c_double
         L.orc_seedtable.argtypes = [C.c_int, C.c_uint32, u32ptr]
         L.orc_ic_2lpt.argtypes = [C.POINTER(ICParams), C.POINTER(Power), dptr, dptr, C.c_void_p, C.c_void_p]
+        L.orc_jbd_solve.argtypes = [C.POINTER(MG)]
+        L.orc_jbd_solve.restype = C.c_double
+        L.orc_phia_solve.argtypes = [C.POINTER(MG), C.c_double]
+        L.orc_phicrit.argtypes = [C.POINTER(MG), C.c_double]
+        L.orc_phicrit.restype = C.c_double
         L.orc_run.argtypes = [C.POINTER(RunParams), dptr, dptr, dptr, dptr, dptr, dptr]
         L.orc_run.restype = C.c_int
         L.orc_time_steps.argtypes = [C.POINTER(RunParams), C.c_int]
@@ -205,6 +211,14 @@ def make_mg(model=LCDM, omega=0.267, **kw):
     m.assb_symm = kw.get("assb_symm", 0.5)
     m.range_symm = kw.get("range_symm", 1.0)
     m.smoothing_filter = kw.get("smoothing_filter", 1 if model == DGP else 0)
+    m.wBD = kw.get("wBD", 100.0)
+    m.Omegah2 = kw.get("Omegah2", 0.14)
+    m.Omegarh2 = kw.get("Omegarh2", 4.0e-5)
+    m.Omegavh2 = kw.get("Omegavh2", 0.36)
+    if model == JBD_GEFF:
+        lib().orc_jbd_solve(C.byref(m))
+    if model == MBETA and m.mg_active:
+        lib().orc_phia_solve(C.byref(m), kw.get("init_redshift", 19.0))
     return m
 
 

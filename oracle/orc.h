@@ -99,7 +99,16 @@ typedef struct {
   /* m(a)/beta(a) symmetron example (user_defined_functions.h:462-484) */
   double beta_symm, assb_symm, range_symm;
   int smoothing_filter;    /* 0 none, 1 gaussian, 2 tophat, 3 sharpk */
+  /* Brans-Dicke background parameters (src/jbd.c) */
+  double wBD, Omegah2, Omegarh2, Omegavh2;
 } orc_mg;
+
+/* Brans-Dicke background (src/jbd.c) and the m(a), beta(a) phi_crit(a)
+ * integral (src/cosmo.c:104-190): solved into oracle-global splines used by
+ * the hooks below; orc_jbd_solve returns h and writes Omega = Omegah2/h^2. */
+double orc_jbd_solve(orc_mg *m);
+void orc_phia_solve(const orc_mg *m, double init_redshift);
+double orc_phicrit(const orc_mg *m, double a);
 
 double orc_hubble(const orc_mg *m, double a);
 double orc_dhubbleda(const orc_mg *m, double a);

@@ -17,15 +17,24 @@
 
 #define INVERSE_H0_MPCH 2997.92458 /* src/vars.h:65 */
 
+/* ---------------------------------------------------- JBD / phi(a) state */
+typedef struct { int n; double *x, *y, *y2; } spl;
+static void spl_init(spl *s, const double *x, const double *y, int n);
+static double spl_eval(const spl *s, double x);
+static int g_jbd = 0, g_phia = 0;
+static spl g_jbdH, g_jbddH, g_jbdG, g_phia_s;
+
 /* ---------------------------------------------------------------- hooks */
 /* hubble: user_defined_functions.h:413-429 */
 double orc_hubble(const orc_mg *m, double a) {
+  if (m->model == ORC_JBD_GEFF && g_jbd) return spl_eval(&g_jbdH, log(a));
   if (m->use_w0wa)
     return sqrt(m->omega / (a * a * a) + (1.0 - m->omega) * exp(3.0 * m->wa * (a - 1) - 3 * (1 + m->w0 + m->wa) * log(a)));
   return sqrt(m->omega / (a * a * a) + 1.0 - m->omega);
 }
 /* dhubbleda: user_defined_functions.h:431-447 */
 double orc_dhubbleda(const orc_mg *m, double a) {
+  if (m->model == ORC_JBD_GEFF && g_jbd) return spl_eval(&g_jbddH, log(a));
   if (m->use_w0wa)
     return 1.0 / (2.0 * orc_hubble(m, a)) *
            (-3.0 * m->omega / (a * a * a * a) - 3.0 * (1.0 - m->omega) * (1.0 + m->w0 + m->wa * (1 - a)) / a);
@@ -62,7 +71,7 @@ double orc_mass2_of_a(const orc_mg *m, double a) {
 double orc_coupling(const orc_mg *m, double a) {
   if (m->model == ORC_FOFR || m->model == ORC_MBETA) return 2.0 * orc_beta_of_a(m, a) * orc_beta_of_a(m, a);
   if (m->model == ORC_DGP) return 1.0 / (3.0 * orc_beta_dgp(m, a));
-  if (m->model == ORC_JBD_GEFF) return m->geff_const - 1.0;
+  if (m->model == ORC_JBD_GEFF) return g_jbd ? spl_eval(&g_jbdG, log(a)) - 1.0 : m->geff_const - 1.0;
   return 0.0;
 }
 /* GeffoverG: user_defined_functions.h:618-652 */
@@ -98,6 +107,10 @@ double orc_screen_potential(const orc_mg *m, double a, double phinewton) {
     double phicrit = 1.5 * m->fofr0 *
                      pow((m->omega + 4.0 * (1.0 - m->omega)) / (1.0 / (a * a * a) * m->omega + 4.0 * (1.0 - m->omega)), m->nfofr + 1.0);
     double s = fabs(phicrit / phinewton);
+    return s > 1.0 ? 1.0 : s;
+  }
+  if (m->model == ORC_MBETA) {
+    double s = fabs(orc_phicrit(m, a) / phinewton);
     return s > 1.0 ? 1.0 : s;
   }
   return 1.0;
@@ -423,4 +436,125 @@ void orc_power_init(orc_power *p) {
   p->norm = 1.0;
   double res = orc_tophat_sigma2(p, 8.0);
   p->norm = p->sigma8 * p->sigma8 / res;
+}
+
+/* ------------------------------------------------------------ splines */
+static void spl_init(spl *s, const double *x, const double *y, int n) {
+  s->n = n;
+  s->x = malloc(8 * n); s->y = malloc(8 * n); s->y2 = calloc(n, 8);
+  memcpy(s->x, x, 8 * n); memcpy(s->y, y, 8 * n);
+  double *u = calloc(n, 8);
+  for (int i = 1; i < n - 1; i++) {
+    double sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+    double p = sig * s->y2[i - 1] + 2.0;
+    s->y2[i] = (sig - 1.0) / p;
+    u[i] = (y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]);
+    u[i] = (6.0 * u[i] / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / p;
+  }
+  for (int k = n - 2; k >= 0; k--) s->y2[k] = s->y2[k] * s->y2[k + 1] + u[k];
+  free(u);
+}
+static double spl_eval(const spl *s, double x) {
+  if (x < s->x[0]) x = s->x[0];
+  if (x > s->x[s->n - 1]) x = s->x[s->n - 1];
+  int lo = 0, hi = s->n - 1;
+  while (hi - lo > 1) { int mid = (hi + lo) / 2; if (s->x[mid] > x) hi = mid; else lo = mid; }
+  double h = s->x[hi] - s->x[lo], A = (s->x[hi] - x) / h, B = (x - s->x[lo]) / h;
+  return A * s->y[lo] + B * s->y[hi] + ((A * A * A - A) * s->y2[lo] + (B * B * B - B) * s->y2[hi]) * (h * h) / 6.0;
+}
+static void spl_free(spl *s) { free(s->x); free(s->y); free(s->y2); s->x = s->y = s->y2 = NULL; }
+
+/* ----------------------------------------- JBD background, src/jbd.c */
+static double jw, jom, jor, jov;
+static double jH(double x, double y, double dy) {
+  return sqrt(exp(-y) * (jor * exp(-4 * x) + jom * exp(-3 * x) + jov) / (1.0 + dy - jw / 6 * dy * dy));
+}
+static double jdHdx(double x, double y, double dy) {
+  double H = jH(x, y, dy);
+  double om = jom * exp(-y - 3.0 * x) / (H * H), ov = jov * exp(-y) / (H * H), ora = jor * exp(-y - 4.0 * x) / (H * H);
+  return H / 2.0 * (-3.0 - ora - jw / 2.0 * dy * dy + dy - 3.0 * (om + 4.0 * ov) / (3.0 + 2.0 * jw) + 3.0 * ov);
+}
+static double jHz(double x, double y, double z) {
+  return sqrt(exp(-y) * (jor * exp(-4 * x) + jom * exp(-3 * x) + jov) + z * z / 12.0 * (2.0 * jw + 3.0) * exp(-2 * y - 6 * x)) -
+         z / 2.0 * exp(-y - 3 * x);
+}
+static void jrhs(double x, const double *u, double *f) {
+  double hubb = jHz(x, u[0], u[1]);
+  f[0] = u[1] * exp(-u[0] - 3 * x) / hubb;
+  f[1] = 3.0 * exp(3.0 * x) / (2 * jw + 3) / hubb * (jom * exp(-3 * x) + 4.0 * jov);
+}
+double orc_jbd_solve(orc_mg *m) {
+  const int npts = 10000, nsub = 16;
+  jw = m->wBD; jom = m->Omegah2; jor = m->Omegarh2; jov = m->Omegavh2;
+  double xini = log(1.0 / (1.0 + 1e6)), dx = -xini / (double)(npts - 1);
+  double *x = malloc(8 * npts), *y = malloc(8 * npts), *dy = malloc(8 * npts);
+  double lo = 0.0, hi = 1.0;
+  for (int it = 0; it < 200; it++) {
+    double ph = 0.5 * (lo + hi), u[2] = {log(ph), 0.0};
+    x[0] = xini; y[0] = u[0]; dy[0] = 0.0;
+    for (int i = 1; i < npts; i++) {
+      double h = dx / nsub;
+      for (int s = 0; s < nsub; s++) {
+        double xx = xini + (i - 1) * dx + s * h, k1[2], k2[2], k3[2], k4[2], t[2];
+        jrhs(xx, u, k1);
+        for (int q = 0; q < 2; q++) t[q] = u[q] + 0.5 * h * k1[q];
+        jrhs(xx + 0.5 * h, t, k2);
+        for (int q = 0; q < 2; q++) t[q] = u[q] + 0.5 * h * k2[q];
+        jrhs(xx + 0.5 * h, t, k3);
+        for (int q = 0; q < 2; q++) t[q] = u[q] + h * k3[q];
+        jrhs(xx + h, t, k4);
+        for (int q = 0; q < 2; q++) u[q] += h / 6.0 * (k1[q] + 2 * k2[q] + 2 * k3[q] + k4[q]);
+      }
+      double xn = xini + i * dx;
+      x[i] = xn; y[i] = u[0];
+      dy[i] = u[1] / jHz(xn, u[0], u[1]) * exp(-3.0 * xn - u[0]);
+    }
+    double r = exp(y[npts - 1]);
+    if (fabs(r - 1.0) < 1e-6) break;
+    if (r < 1.0) lo = ph; else hi = ph;
+  }
+  double h = jH(0.0, y[npts - 1], dy[npts - 1]);
+  double *G = malloc(8 * npts), *H = malloc(8 * npts), *dH = malloc(8 * npts);
+  for (int i = 0; i < npts; i++) {
+    G[i] = exp(-y[i]);
+    H[i] = jH(x[i], y[i], dy[i]) / h;
+    dH[i] = jdHdx(x[i], y[i], dy[i]) / h * exp(-x[i]);
+  }
+  if (g_jbd) { spl_free(&g_jbdG); spl_free(&g_jbdH); spl_free(&g_jbddH); }
+  spl_init(&g_jbdG, x, G, npts); spl_init(&g_jbdH, x, H, npts); spl_init(&g_jbddH, x, dH, npts);
+  g_jbd = 1;
+  free(x); free(y); free(dy); free(G); free(H); free(dH);
+  m->omega = m->Omegah2 / (h * h);
+  return h;
+}
+
+/* ------------------------------------- phi_crit(a), src/cosmo.c:104-190 */
+static double phia_int(double x, void *p) {
+  const orc_mg *m = p;
+  double a = exp(x), b = orc_beta_of_a(m, a);
+  if (b == 0.0) return 0.0;
+  return 9.0 * m->omega * b / (orc_mass2_of_a(m, a) * a * a * a);
+}
+void orc_phia_solve(const orc_mg *m, double init_redshift) {
+  const int npts = 1000;
+  double zini = init_redshift > 200.0 ? init_redshift : 200.0;
+  double xmin = log(1.0 / (1.0 + zini)), xmax = log(1.0 / (1.0 - 0.5)), dx = (xmax - xmin) / (npts - 1);
+  double *x = malloc(8 * npts), *ph = malloc(8 * npts);
+  x[0] = xmin; ph[0] = 0.0;
+  for (int i = 1; i < npts; i++) {
+    x[i] = xmin + i * dx;
+    ph[i] = ph[i - 1] + integrate(phia_int, (void *)m, xmin + (i - 1) * dx, x[i]);
+  }
+  for (int i = 0; i < npts; i++) {
+    double b = orc_beta_of_a(m, exp(x[i]));
+    if (b != 0.0) ph[i] /= 2.0 * b;
+  }
+  if (g_phia) spl_free(&g_phia_s);
+  spl_init(&g_phia_s, x, ph, npts);
+  g_phia = 1;
+  free(x); free(ph);
+}
+double orc_phicrit(const orc_mg *m, double a) {
+  (void)m;
+  return g_phia ? spl_eval(&g_phia_s, log(a)) : 0.0;
 }

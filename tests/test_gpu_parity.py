@@ -179,10 +179,16 @@ def _gpu_run(p, nsteps, zf=0.0):
     return pos, vel, d1, d2, pk, dDdy, dD2dy
 
 
-def _oracle_run(p, mg, nsteps, zf=0.0):
+def _oracle_run(p, mg, nsteps, zf=0.0, pw_fix=None):
     rp = O.RunParams()
     rp.mg = mg
     rp.pw = power_for(p)
+    if pw_fix is not None:
+        # Brans-Dicke: the spectrum is normalised with the parameter file's
+        # Omega/h before the background solve replaces them (main.c:186-196)
+        import ctypes as C
+        h = float(np.sqrt(mg.Omegah2 / mg.omega))
+        rp.pw.omega, rp.pw.h = mg.omega, h
     rp.ic = O.ICParams(p.Nmesh, p.Nsample, p.Box, p.Seed, p.SphereMode, p.amplitude_fixed_initial_condition,
                        p.inverted_initial_condition, 1.0)
     rp.init_redshift = p.Init_Redshift
@@ -199,10 +205,11 @@ def _oracle_run(p, mg, nsteps, zf=0.0):
     return pos, vel, (kb[:nb], pk[:nb], km[:nb], nm[:nb])
 
 
-@pytest.mark.parametrize("model", ["lcdm", "fofr", "dgp"])
+@pytest.mark.parametrize("model", ["lcdm", "fofr", "dgp", "jbd", "mbeta", "w0wa", "fofr_noscreen", "dgp_noscreen"])
 def test_short_run_matches_oracle(model):
     N, Ns, box, nsteps = 32, 16, 128.0, 5
     kw = dict(Seed=4242)
+    pw_fix = None
     if model == "fofr":
         kw.update(model=M.MODEL_FOFR, modified_gravity_active=1, include_screening=1, fofr0=1e-5, nfofr=1.0,
                   input_pofk_is_for_lcdm=0)
@@ -211,11 +218,31 @@ def test_short_run_matches_oracle(model):
         kw.update(model=M.MODEL_DGP, modified_gravity_active=1, include_screening=1, rcH0_DGP=1.0, Rsmooth=1.0,
                   smoothing_filter=M.FILTER_GAUSSIAN, input_pofk_is_for_lcdm=0)
         mg = O.make_mg(O.DGP, 0.267, rcH0=1.0, rsmooth=1.0)
+    elif model == "jbd":
+        kw.update(model=M.MODEL_BRANSDICKE, modified_gravity_active=1, wBD=100.0, Omegah2=0.14, Omegarh2=4e-5,
+                  Omegavh2=0.36, input_pofk_is_for_lcdm=0)
+        mg = O.make_mg(O.JBD_GEFF, 0.267, wBD=100.0, Omegah2=0.14, Omegarh2=4e-5, Omegavh2=0.36)
+        pw_fix = (mg.omega, None)
+    elif model == "mbeta":
+        kw.update(model=M.MODEL_MBETA, modified_gravity_active=1, include_screening=1, assb_symm=0.5,
+                  beta_symm=1.0, range_symm=1.0, input_pofk_is_for_lcdm=0)
+        mg = O.make_mg(O.MBETA, 0.267, assb_symm=0.5, beta_symm=1.0, range_symm=1.0)
+    elif model == "w0wa":
+        kw.update(use_w0wa=1, w_0=-0.9, w_a=0.2)
+        mg = O.make_mg(O.LCDM, 0.267, use_w0wa=1, w0=-0.9, wa=0.2)
+    elif model == "fofr_noscreen":
+        kw.update(model=M.MODEL_FOFR, modified_gravity_active=1, include_screening=0, fofr0=1e-5, nfofr=1.0,
+                  input_pofk_is_for_lcdm=0)
+        mg = O.make_mg(O.FOFR, 0.267, fofr0=1e-5, nfofr=1.0, include_screening=0)
+    elif model == "dgp_noscreen":
+        kw.update(model=M.MODEL_DGP, modified_gravity_active=1, include_screening=0, rcH0_DGP=1.0, Rsmooth=1.0,
+                  smoothing_filter=M.FILTER_GAUSSIAN, input_pofk_is_for_lcdm=0)
+        mg = O.make_mg(O.DGP, 0.267, rcH0=1.0, rsmooth=1.0, include_screening=0)
     else:
         mg = O.make_mg(O.LCDM, 0.267)
     p = params(N, Ns, box, **kw)
     pos, vel, d1, d2, (k, pk, km, n), dDdy, dD2dy = _gpu_run(p, nsteps)
-    opos, ovel, (kb, pko, kmo, no) = _oracle_run(p, mg, nsteps)
+    opos, ovel, (kb, pko, kmo, no) = _oracle_run(p, mg, nsteps, pw_fix=pw_fix)
     np.testing.assert_array_equal(n, no)
     m = no > 0
     m[0] = False  # bin 0 holds only the k = 0 mode

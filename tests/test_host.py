@@ -161,3 +161,26 @@ def test_create_fails_loudly_without_device_or_bad_params():
     p = M.default_params(Nmesh=7)
     with pytest.raises(M.MGPError):
         M.Context(p)
+
+
+def test_host_cosmology_jbd_and_mbeta_and_w0wa():
+    # Brans-Dicke: background solved by shooting (src/jbd.c); Omega and h are
+    # replaced by the solution (user_defined_functions.h:135-143)
+    p = M.default_params(model=M.MODEL_BRANSDICKE, modified_gravity_active=1, wBD=100.0, Omegah2=0.14,
+                         Omegarh2=4e-5, Omegavh2=0.36)
+    mg = O.make_mg(O.JBD_GEFF, 0.267, wBD=100.0, Omegah2=0.14, Omegarh2=4e-5, Omegavh2=0.36)
+    cos = O.Cosmo(mg, 19.0)
+    a = np.array([0.05, 0.2, 0.6, 1.0])
+    np.testing.assert_allclose(M.cosmo_eval(p, 0, a), [cos.growth_D(x) for x in a], rtol=1e-7)
+    np.testing.assert_allclose(M.cosmo_eval(p, 3, a), [cos.growth_D2(x) for x in a], rtol=1e-7)
+    # symmetron-type m(a), beta(a): growth only changes through Geff(k = 1e-3)
+    p = M.default_params(model=M.MODEL_MBETA, modified_gravity_active=1, assb_symm=0.5, beta_symm=1.0,
+                         range_symm=1.0)
+    mg = O.make_mg(O.MBETA, 0.267, assb_symm=0.5, beta_symm=1.0, range_symm=1.0)
+    cos = O.Cosmo(mg, 19.0)
+    np.testing.assert_allclose(M.cosmo_eval(p, 0, a), [cos.growth_D(x) for x in a], rtol=1e-9)
+    # w0/wa background
+    p = M.default_params(use_w0wa=1, w_0=-0.9, w_a=0.2)
+    mg = O.make_mg(O.LCDM, 0.267, use_w0wa=1, w0=-0.9, wa=0.2)
+    cos = O.Cosmo(mg, 19.0)
+    np.testing.assert_allclose(M.cosmo_eval(p, 0, a), [cos.growth_D(x) for x in a], rtol=1e-9)
