@@ -242,7 +242,7 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   for (int i = 0; i < 3; i++)
     if (plans[i]) cufftDestroy(plans[i]);
   void *bufs[] = {c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
-                  c->fft_work, c->rk_bin, c->pk_thr, c->win1d, c->pk_block, c->pk_sum};
+                  c->fft_work, c->rk_bin, c->pk_thr, c->win1d, c->pk_block, c->pk_sum, c->rsd_block, c->rsd_sum};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
     if (bufs[i]) cudaFree(bufs[i]);
   for (int t = 0; t < MGP_NTIMERS; t++) {
@@ -633,11 +633,62 @@ extern "C" int mgp_pofk(mgp_ctx *c, int cap, int *nbins, double *k, double *pk, 
   return MGP_OK;
 }
 
+// compute_RSD_powerspectrum (src/compute_pofk.c:403-512): redshift-space
+// deposits with the y and z axes as line of sight, P0/P2/P4 per axis, their
+// mean and |difference|/sqrt(2).  Uses the force grids as scratch.
 extern "C" int mgp_pofk_rsd(mgp_ctx *c, double A, int cap, int *nbins, double *k, double *P0, double *P2, double *P4,
                             double *s0, double *s2, double *s4, double *n) {
-  (void)A; (void)cap; (void)nbins; (void)k; (void)P0; (void)P2; (void)P4; (void)s0; (void)s2; (void)s4; (void)n;
-  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
-  return mgp_set_error(MGP_EINVAL, "RSD multipoles are not available in this build");
+  RET_IF(require_particles(c));
+  const int nb = c->pk_nbins, N = c->g.N;
+  if (nbins) *nbins = nb;
+  if (cap < nb) return mgp_set_error(MGP_EINVAL, "RSD capacity %d < %d bins", cap, nb);
+  if (!c->rsd_block) {
+    MGP_CUDA(cudaMalloc(&c->rsd_block, sizeof(double) * 3 * (size_t)nb * c->pk_blocks));
+    MGP_CUDA(cudaMalloc(&c->rsd_sum, sizeof(double) * 3 * (size_t)nb));
+  }
+  const mgp_params *p = &c->p;
+  // velfac = Hubble/A with Hubble = HUBBLE * UnitTime (src/2LPT.c:35-42)
+  const double hub = 3.2407789e-18 * (p->UnitLength_in_cm / p->UnitVelocity_in_cm_per_s);
+  const double vnorm = (hub / A) / (100.0 * A * mgp_hubble(&c->cosmo, A)) * (double)N / p->Box;
+  const double cola = p->UseCOLA ? 1.0 : 0.0;
+  const float g1 = (float)(cola * mgp_cosmo_growth(&c->cosmo, 1, A)), g2 = (float)(cola * mgp_cosmo_growth(&c->cosmo, 4, A));
+  const double wpar = pow((double)N / (double)c->Ns, 3);
+  float *dens = c->frc, *dkr = c->frc + c->g.nreal;
+  std::vector<double> sums(3 * (size_t)nb), res[2][3];
+  const double norm = pow(p->Box, 3) / pow((double)N, 6), shot = c->pk_sub ? pow(p->Box / (double)c->Ns, 3) : 0.0;
+  for (int ax = 0; ax < 2; ax++) {
+    RET_IF(mgp_launch_fill(dens, c->g.nreal, -1.0f, c->stream));
+    RET_IF(mgp_launch_cic_rsd(c->s, c->v, c->D1, c->D2, c->dstate, c->np, c->Ns, N, p->Box, (float)wpar, ax + 1,
+                              (float)vnorm, g1, g2, dens, c->g.P, c->stream));
+    MGP_CUFFT(cufftExecR2C(c->plan_r2c_oop, (cufftReal *)dens, (cufftComplex *)dkr));
+    RET_IF(mgp_launch_pofk_mu(dkr, N, c->rk_bin, c->win1d, nb, c->rsd_block, c->pk_blocks, c->rsd_sum, c->stream));
+    MGP_CUDA(cudaMemcpyAsync(sums.data(), c->rsd_sum, sizeof(double) * 3 * nb, cudaMemcpyDeviceToHost, c->stream));
+    MGP_CUDA(cudaStreamSynchronize(c->stream));
+    for (int q = 0; q < 3; q++) res[ax][q].assign(nb, 0.0);
+    for (int b = 0; b < nb; b++) {
+      double nn = c->pk_n[b];
+      if (!(nn > 0)) continue;
+      double p0 = sums[b] / nn * norm, p2 = sums[nb + b] / nn * norm, p4 = sums[2 * nb + b] / nn * norm;
+      p4 = 9.0 * (35.0 * p4 - 30.0 * p2 + 3.0 * p0) / 8.0;  // order as compute_pofk.c:704-706
+      p2 = 5.0 * (3.0 * p2 - 1.0 * p0) / 2.0;
+      res[ax][0][b] = p0 - shot;
+      res[ax][1][b] = p2 - shot;
+      res[ax][2][b] = p4 - shot;
+    }
+  }
+  c->have_forces = 0;
+  for (int b = 0; b < nb; b++) {
+    double nn = c->pk_n[b];
+    if (k) k[b] = nn > 0 ? k_from_index(b, c->pk_kmin, c->pk_kmax, nb, c->pk_bintype, p->Box) : 0.0;
+    if (P0) P0[b] = (res[0][0][b] + res[1][0][b]) / 2.0;
+    if (P2) P2[b] = (res[0][1][b] + res[1][1][b]) / 2.0;
+    if (P4) P4[b] = (res[0][2][b] + res[1][2][b]) / 2.0;
+    if (s0) s0[b] = fabs(res[0][0][b] - res[1][0][b]) / sqrt(2.0);
+    if (s2) s2[b] = fabs(res[0][1][b] - res[1][1][b]) / sqrt(2.0);
+    if (s4) s4[b] = fabs(res[0][2][b] - res[1][2][b]) / sqrt(2.0);
+    if (n) n[b] = nn;
+  }
+  return MGP_OK;
 }
 
 // ---------------------------------------------------------- particles

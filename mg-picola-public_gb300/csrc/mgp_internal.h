@@ -73,6 +73,7 @@ struct mgp_ctx {
   float *win1d;             /* device: 1/sinc^4 per |d| in [0, N/2] */
   double *pk_block;         /* device: per-block FP64 bin partials */
   double *pk_sum;           /* device: FP64 bin sums */
+  double *rsd_block, *rsd_sum; /* device: RSD moment partials and sums (lazy) */
   double *pk_n, *pk_k;      /* host: mode counts and k sums per bin */
   double *pk_host;          /* host: last P(k) sums */
   int pk_blocks;
@@ -168,6 +169,11 @@ int mgp_launch_ic_grad6(const float *dk, float *out6, long long grid_floats, int
 int mgp_launch_ic_source(float *g6, long long grid_floats, int N, long long P, cudaStream_t st);
 int mgp_launch_ic_disp(const float *dk, const float *src, float *out6, long long grid_floats, int N, double box,
                        cudaStream_t st);
+int mgp_launch_cic_rsd(const float *s, const float *v, const float *D1, const float *D2, const mgp_dstate *st,
+                       long long np, int Ns, int N, double box, float wpar, int axis, float vnorm, float g1, float g2,
+                       float *rho, long long P, cudaStream_t stream);
+int mgp_launch_pofk_mu(const float *dk, int N, const int *rk_bin, const float *win, int nbins, double *block_part,
+                       int nblocks, double *sums, cudaStream_t st);
 int mgp_launch_aos_to_soa(const float *in, float *out, long long np, cudaStream_t st);
 int mgp_launch_output(const float *s, const float *v, const float *D1, const float *D2, const mgp_dstate *dst,
                       long long np, int Ns, double box, double lengthfac, double vfac, double dDdy, double dD2dy,

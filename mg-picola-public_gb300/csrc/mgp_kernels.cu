@@ -1042,3 +1042,105 @@ int mgp_launch_output(const float *s, const float *v, const float *D1, const flo
   g_kernel_launches++;
   return MGP_OK;
 }
+
+// ------------------------------------------------------ RSD multipoles
+// PtoMesh_RSD (src/compute_pofk.c:280-393): CIC in redshift space with the
+// line of sight mapped onto the grid's third axis (y LOS: grid axes (x, z, y);
+// z LOS: (x, y, z)); the LOS coordinate moves by V * vnorm cells with
+// V = Vel + UseCOLA (D1 dD/dy + D2 dD2/dy) (the reference does not subtract
+// the mean velocity here) and wraps periodically.
+__global__ void __launch_bounds__(MGP_THREADS) k_cic_rsd(const float *__restrict__ s, const float *__restrict__ v,
+                                                         const float *__restrict__ D1, const float *__restrict__ D2,
+                                                         const mgp_dstate *__restrict__ st, long long np, int Ns,
+                                                         int N, float scale, float wpar, int axis, float vnorm,
+                                                         float g1, float g2, float *__restrict__ rho, long long P) {
+  const int map[2][3] = {{0, 2, 1}, {0, 1, 2}};  // grid axis g takes particle axis map[.][g]
+  const int *m = map[axis == 1 ? 0 : 1];
+  float off[3];
+  for (int g = 0; g < 3; g++) off[g] = (float)(st->cx[m[g]] * scale);
+  const float cvl = (float)st->cv[m[2]];
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    int li[3];
+    lattice_ijk(p, Ns, li[0], li[1], li[2]);
+    const long long ol = m[2] * np + p;
+    float V = (v[ol] + cvl) + D1[ol] * g1 + D2[ol] * g2;
+    int ix, iy, iz;
+    float DX, DY, DZ;
+    cell_frac(li[m[0]], s[m[0] * np + p], off[0], N, Ns, scale, ix, DX);
+    cell_frac(li[m[1]], s[m[1] * np + p], off[1], N, Ns, scale, iy, DY);
+    cell_frac(li[m[2]], s[ol], off[2] + V * vnorm, N, Ns, scale, iz, DZ);
+    float TX = 1.0f - DX, TY = (1.0f - DY) * wpar, TZ = 1.0f - DZ;
+    DY *= wpar;
+    int ixn = ix + 1 == N ? 0 : ix + 1, iyn = iy + 1 == N ? 0 : iy + 1, izn = iz + 1 == N ? 0 : iz + 1;
+    long long r00 = ((long long)ix * N + iy) * P, r01 = ((long long)ix * N + iyn) * P;
+    long long r10 = ((long long)ixn * N + iy) * P, r11 = ((long long)ixn * N + iyn) * P;
+    atomicAdd(rho + r00 + iz, TX * TY * TZ);
+    atomicAdd(rho + r00 + izn, TX * TY * DZ);
+    atomicAdd(rho + r01 + iz, TX * DY * TZ);
+    atomicAdd(rho + r01 + izn, TX * DY * DZ);
+    atomicAdd(rho + r10 + iz, DX * TY * TZ);
+    atomicAdd(rho + r10 + izn, DX * TY * DZ);
+    atomicAdd(rho + r11 + iz, DX * DY * TZ);
+    atomicAdd(rho + r11 + izn, DX * DY * DZ);
+  }
+}
+
+int mgp_launch_cic_rsd(const float *s, const float *v, const float *D1, const float *D2, const mgp_dstate *st,
+                       long long np, int Ns, int N, double box, float wpar, int axis, float vnorm, float g1, float g2,
+                       float *rho, long long P, cudaStream_t stream) {
+  k_cic_rsd<<<blocks_for(np, 8), MGP_THREADS, 0, stream>>>(s, v, D1, D2, st, np, Ns, N, (float)(N / box), wpar, axis,
+                                                           vnorm, g1, g2, rho, P);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// bin_up_RSD_power_spectrum (src/compute_pofk.c:518-753): sums of P, P mu^2
+// and P mu^4 per bin with mu = kz/|k| (kz is the LOS index), mu = 0 for the
+// k = 0 mode; FP64 shared-memory bins (used at output time only).
+__global__ void __launch_bounds__(MGP_THREADS) k_pofk_mu(const float2 *__restrict__ dk, int N,
+                                                         const int *__restrict__ rk_bin, const float *__restrict__ win,
+                                                         int nbins, double *__restrict__ block_part) {
+  extern __shared__ double smu[];
+  const int NH = N / 2 + 1, h = N / 2;
+  for (int b = threadIdx.x; b < 3 * nbins; b += blockDim.x) smu[b] = 0.0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = wid; r < (long long)N * N; r += nw) {
+    const int i = (int)(r / N), j = (int)(r - (long long)i * N);
+    const int d0 = i > h ? N - i : i, d1 = j > h ? N - j : j;
+    for (int kz = lane; kz < NH; kz += 32) {
+      const int rk = d0 * d0 + d1 * d1 + kz * kz;
+      const int bin = rk_bin[rk];
+      if (bin < 0) continue;
+      float2 z = dk[r * NH + kz];
+      double w = (kz == 0 || 2 * kz == N) ? 1.0 : 2.0;
+      double pk = (double)(z.x * z.x + z.y * z.y) * (double)(win[d0] * win[d1] * win[kz]) * w;
+      double mu2 = rk == 0 ? 0.0 : (double)(kz * kz) / (double)rk;
+      atomicAdd(&smu[bin], pk);
+      atomicAdd(&smu[nbins + bin], pk * mu2);
+      atomicAdd(&smu[2 * nbins + bin], pk * mu2 * mu2);
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < 3 * nbins; b += blockDim.x) block_part[(long long)blockIdx.x * 3 * nbins + b] = smu[b];
+}
+
+int mgp_launch_pofk_mu(const float *dk, int N, const int *rk_bin, const float *win, int nbins, double *block_part,
+                       int nblocks, double *sums, cudaStream_t st) {
+  size_t shmem = sizeof(double) * 3 * (size_t)nbins;
+  if (shmem > 48 * 1024) {
+    if (cudaFuncSetAttribute(k_pofk_mu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem) != cudaSuccess)
+      return mgp_set_error(MGP_EINVAL, "RSD P(k) needs %zu bytes of shared memory", shmem);
+  }
+  k_pofk_mu<<<nblocks, MGP_THREADS, shmem, st>>>((const float2 *)dk, N, rk_bin, win, nbins, block_part);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  k_pofk_reduce<<<(3 * nbins + 127) / 128, 128, 0, st>>>(block_part, nblocks, 3 * nbins, sums);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}

@@ -18,7 +18,12 @@
   } while (0)
 
 // Output (src/main.c:792-1061) at scale factor A for output redshift z.
+static int write_rsd_now(mgp_ctx *c, double A);
+
 static int output(mgp_ctx *c, double A, double z, int gadget) {
+  // RSD multipoles at output (src/main.c:875-880), not for the IC output
+  int first_step = fabs(c->p.Init_Redshift - z) / c->p.Init_Redshift <= 1.0E-6;
+  if (c->p.pofk_compute_rsd_pofk >= 1 && !first_step) RET_IF(write_rsd_now(c, A));
   mgp_units u;
   mgp_units_init(&c->p, &u);
   const size_t np = (size_t)c->np, bytes = sizeof(float) * 3 * np;
@@ -42,6 +47,15 @@ static int output(mgp_ctx *c, double A, double z, int gadget) {
   RET_IF(gadget ? mgp_write_gadget(fn, &c->p, A, pos.data(), vel.data(), np)
                 : mgp_write_ascii(fn, pos.data(), vel.data(), np));
   return mgp_write_info(&c->p, A, np);
+}
+
+static int write_rsd_now(mgp_ctx *c, double A) {
+  int nb = c->pk_nbins;
+  std::vector<double> k(nb), P0(nb), P2(nb), P4(nb), s0(nb), s2(nb), s4(nb), n(nb);
+  RET_IF(mgp_pofk_rsd(c, A, nb, &nb, k.data(), P0.data(), P2.data(), P4.data(), s0.data(), s2.data(), s4.data(),
+                      n.data()));
+  return mgp_write_pofk_rsd(&c->p, A, nb, k.data(), P0.data(), P2.data(), P4.data(), s0.data(), s2.data(), s4.data(),
+                            n.data());
 }
 
 static int write_pofk_now(mgp_ctx *c, double A, const char *label) {
@@ -76,12 +90,16 @@ extern "C" int mgp_run(mgp_ctx *c, int gadget) {
       int output_step = (ts == 0) && (i != NoutputStart);
       AF = output_step ? A : A + da * 0.5;
       AFF = A + da;
+      // RSD every step except at outputs (src/compute_pofk.c call in auxPM.c:376-381)
+      if (c->p.pofk_compute_rsd_pofk == 1 && !output_step) RET_IF(write_rsd_now(c, A));
       RET_IF(mgp_get_displacements(c, A));
       if (p->pofk_compute_every_step) RET_IF(write_pofk_now(c, A, "CDM"));
       if (output_step) {
         RET_IF(mgp_kick_drift(c, AI, AF, A, AFF, 0));
         RET_IF(output(c, A, p->output_redshift[i - 1], gadget));
         if (i == Noutputs) return MGP_OK;
+        // the RSD deposits used the force grids as scratch: rebuild them at A
+        if (!c->have_forces) RET_IF(mgp_get_displacements(c, A));
         AI = A;
         AF = A + da * 0.5;
         RET_IF(mgp_kick_drift(c, AI, AF, A, AFF, 1));

@@ -231,6 +231,16 @@ class Context:
         m = nb.value
         return k[:m], pk[:m], km[:m], n[:m]
 
+    def pofk_rsd(self, A):
+        """RSD multipoles (compute_RSD_powerspectrum): k, P0, P2, P4, sigma0,
+        sigma2, sigma4, n."""
+        cap = max(self.params.pofk_nbins, self.N, 1)
+        arrs = [np.zeros(cap) for _ in range(8)]
+        nb = C.c_int(0)
+        _check(lib().mgp_pofk_rsd(self.h, A, cap, C.byref(nb), *[_dptr(a) for a in arrs]))
+        m = nb.value
+        return tuple(a[:m] for a in arrs)
+
     def get_particles(self):
         pos = np.zeros((self.np, 3), np.float32)
         vel = np.zeros((self.np, 3), np.float32)

@@ -255,3 +255,72 @@ def test_short_run_matches_oracle(model):
     v64 = vel.astype(np.float64)
     vout = v64 - v64.mean(0) + d1 * dDdy + d2 * dD2dy
     assert rel_rms(vout, ovel) < 1e-3
+
+
+def test_rsd_multipoles_match_oracle():
+    N, Ns, box = 32, 16, 64.0
+    p = params(N, Ns, box, pofk_nbins=12, pofk_bintype=0, pofk_kmin=0.0, pofk_kmax=0.0, pofk_subtract_shotnoise=1)
+    pos, vel, d1, d2 = random_particles(Ns, box, seed=8, spread=0.5)
+    A = 0.6
+    with M.Context(p) as ctx:
+        ctx.set_particles(pos, vel, d1, d2)
+        k, P0, P2, P4, s0, s2, s4, n = ctx.pofk_rsd(A)
+        dDdy, dD2dy = ctx.growth(1, A), ctx.growth(4, A)
+        Hubble = 3.2407789e-18 * (3.085678e24 / 1e5)
+        cos = O.Cosmo(O.make_mg(O.LCDM, p.Omega), p.Init_Redshift)
+    import ctypes as C
+    H = O.lib().orc_hubble(C.byref(O.make_mg(O.LCDM, p.Omega)), A)
+    vnorm = (Hubble / A) / (100.0 * A * H) * N / box
+    extra = (d1.astype(np.float64) * dDdy + d2.astype(np.float64) * dD2dy)
+    res = []
+    for axis in (1, 2):
+        out = [np.zeros(N) for _ in range(5)]
+        nb = C.c_int(12)
+        O.lib().orc_pofk_rsd_axis(pos.astype(np.float64), vel.astype(np.float64), extra.ctypes.data, Ns ** 3, axis, N,
+                                  Ns, box, vnorm, C.byref(nb), 0, 1, 0.0, 0.0, *out)
+        res.append([o[:nb.value] for o in out])
+    (ky, y0, y2, y4, ny), (kz, z0, z2, z4, nz) = res
+    np.testing.assert_array_equal(n, ny)
+    m = ny > 0
+    np.testing.assert_allclose(k[m], ky[m], rtol=1e-14)
+    shot = (box / Ns) ** 3
+    for got, a, b in ((P0, y0, z0), (P2, y2, z2), (P4, y4, z4)):
+        ref = 0.5 * (a + b)
+        scale = np.abs(0.5 * (y0 + z0) + shot)
+        assert np.max(np.abs(got[m] - ref[m]) / scale[m]) < 1e-5
+    np.testing.assert_allclose(s0[m], np.abs(y0 - z0)[m] / np.sqrt(2), atol=1e-5 * np.abs(y0 + shot).max())
+
+
+def test_run_writes_reference_formats(tmp_path):
+    """mgp_run: GADGET-1 snapshot, info file and pofk files (src/main.c:792-1149,
+    src/compute_pofk.c:238-478) with the reference's names and layouts."""
+    N, Ns, box = 32, 16, 128.0
+    out = str(tmp_path)
+    p = params(N, Ns, box, pofk_compute_rsd_pofk=2, pofk_nbins=8, OutputDir=out, FileBase="snap", Noutputs=2)
+    p.output_redshift[0], p.output_nsteps[0] = 1.0, 3
+    p.output_redshift[1], p.output_nsteps[1] = 0.0, 3
+    with M.Context(p) as ctx:
+        ctx.run(gadget=True)
+    import os
+    import struct
+    names = sorted(os.listdir(out))
+    assert "snap_z1p000.0" in names and "snap_z0p000.0" in names
+    assert "info_snap_z0p000.txt" in names and "pofk_RSD_snap_z0.000.txt" in names
+    assert any(nm.startswith("pofk_snap_z0.000_CDM") for nm in names)
+    raw = open(os.path.join(out, "snap_z0p000.0"), "rb").read()
+    n = Ns ** 3
+    assert len(raw) == 4 + 256 + 4 + 2 * (4 + 12 * n + 4)
+    assert struct.unpack("<i", raw[:4])[0] == 256 and struct.unpack("<i", raw[260:264])[0] == 256
+    npart = struct.unpack("<6I", raw[4:28])
+    assert npart[1] == n
+    mass = struct.unpack("<6d", raw[28:76])
+    t, z = struct.unpack("<2d", raw[76:92])
+    assert abs(t - 1.0) < 1e-12 and abs(z) < 1e-12 and mass[1] > 0
+    boxsize = struct.unpack("<d", raw[4 + 128:4 + 136])[0]
+    assert boxsize == box
+    blk = struct.unpack("<i", raw[264:268])[0]
+    assert blk == 12 * n
+    posf = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3)
+    assert posf.min() >= 0 and posf.max() < box
+    lines = [l for l in open(os.path.join(out, "pofk_RSD_snap_z0.000.txt")) if not l.startswith("#")]
+    assert len(lines) >= 4 and len(lines[0].split()) == 7
