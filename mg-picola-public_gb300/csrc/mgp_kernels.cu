@@ -160,19 +160,25 @@ struct mgp_pofk_kargs {
   int fuse_kind, filter;
   float2 *fuse_out;
   float fuse_a, fuse_b;
+  int priv;
 };
 
 // Bin sums: native FP32 shared-memory atomics made exact to second order by
 // a compensated (TwoSum) split: the atomic returns the old value, so the
 // rounding error of every addition is recovered and added to a second FP32
 // array; hi + lo carries about twice FP32's precision.
+// priv != 0: every warp owns its own hi/lo bin arrays (the run tails of one
+// warp always hit distinct bins), so the sums need no atomics at all.
 __global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
   extern __shared__ float shf[];
   const int N = a.N, nbins = a.nbins, NH = N / 2 + 1, h = N / 2;
-  float *shi = shf, *slo = shf + nbins;
-  int *sthr = (int *)(slo + nbins);
+  const int nwb = a.priv ? (int)(blockDim.x >> 5) : 1;
+  float *shi0 = shf, *slo0 = shf + nwb * nbins;
+  int *sthr = (int *)(slo0 + nwb * nbins);
   float *swin = (float *)(sthr + (a.thr ? nbins + 1 : 0));
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) shi[b] = slo[b] = 0.0f;
+  for (int b = threadIdx.x; b < nwb * nbins; b += blockDim.x) shi0[b] = slo0[b] = 0.0f;
+  const int wslot = a.priv ? (int)(threadIdx.x >> 5) : 0;
+  float *shi = shi0 + wslot * nbins, *slo = slo0 + wslot * nbins;
   if (a.thr)
     for (int b = threadIdx.x; b <= nbins; b += blockDim.x) sthr[b] = a.thr[b];
   for (int d = threadIdx.x; d <= h; d += blockDim.x) swin[d] = a.win[d];
@@ -239,15 +245,23 @@ __global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
       int nbin = __shfl_down_sync(0xffffffffu, bin, 1);
       bool tail = lane == 31 || nbin != bin;
       if (tail && bin >= 0) {
-        float old = atomicAdd(&shi[bin], acc);
-        float sum = old + acc, bp = sum - old;
-        atomicAdd(&slo[bin], (old - (sum - bp)) + (acc - bp));
+        float old = a.priv ? shi[bin] : atomicAdd(&shi[bin], acc);
+        float sum = old + acc, bp = sum - old, err = (old - (sum - bp)) + (acc - bp);
+        if (a.priv) {
+          shi[bin] = sum;
+          slo[bin] += err;
+        } else {
+          atomicAdd(&slo[bin], err);
+        }
       }
     }
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
-    a.block_part[(long long)blockIdx.x * nbins + b] = (double)shi[b] + (double)slo[b];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
+    double t = 0.0;
+    for (int w = 0; w < nwb; w++) t += (double)shi0[w * nbins + b] + (double)slo0[w * nbins + b];
+    a.block_part[(long long)blockIdx.x * nbins + b] = t;
+  }
 }
 
 // Deterministic cross-block sum in FP64 (the MPI_Allreduce of compute_pofk.c:225).
@@ -259,10 +273,11 @@ __global__ void k_pofk_reduce(const double *__restrict__ block_part, int nblocks
   sums[b] = s;
 }
 
-static int launch_pofk(const mgp_pofk_kargs &ka, int nblocks, double *sums, cudaStream_t st) {
+static int launch_pofk(mgp_pofk_kargs ka, int nblocks, double *sums, cudaStream_t st) {
   const int h = ka.N / 2;
-  size_t shmem = 2 * sizeof(float) * (size_t)ka.nbins + (ka.thr ? sizeof(int) * (size_t)(ka.nbins + 1) : 0) +
-                 sizeof(float) * (size_t)(h + 1);
+  ka.priv = (size_t)ka.nbins * (MGP_THREADS / 32) * 2 * sizeof(float) <= 96 * 1024;
+  size_t shmem = 2 * sizeof(float) * (size_t)ka.nbins * (ka.priv ? MGP_THREADS / 32 : 1) +
+                 (ka.thr ? sizeof(int) * (size_t)(ka.nbins + 1) : 0) + sizeof(float) * (size_t)(h + 1);
   if (shmem > 48 * 1024) {
     if (cudaFuncSetAttribute(k_pofk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem) != cudaSuccess)
       return mgp_set_error(MGP_EINVAL, "P(k) needs %zu bytes of shared memory", shmem);
