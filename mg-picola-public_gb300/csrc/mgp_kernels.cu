@@ -189,12 +189,18 @@ __global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
   const float inv_span = (float)nbins / (a.kmax - a.kmin);
   const float inv_logspan = a.bintype ? (float)nbins / logf(a.kmax / a.kmin) : 0.0f;
   const int lo = a.thr ? sthr[0] : 0, hi = a.thr ? sthr[nbins] : 0;
-  // one warp per (i, j) row; all lanes run the same number of chunks
-  for (long long r = wid; r < (long long)N * N; r += nw) {
-    const int i = (int)(r / N), j = (int)(r - (long long)i * N);
-    const int d0 = i > h ? N - i : i, d1 = j > h ? N - j : j;
+  // One warp per (|d0|, |d1|) pair: the up to four stored rows (i, j) with
+  // i in {d0, N-d0}, j in {d1, N-d1} share |k|^2 along kz, hence the bins,
+  // window and filter; their powers are summed before the warp scan.
+  const long long npair = (long long)(h + 1) * (h + 1);
+  for (long long q = wid; q < npair; q += nw) {
+    const int d0 = (int)(q / (h + 1)), d1 = (int)(q - (long long)d0 * (h + 1));
     const int rk01 = d0 * d0 + d1 * d1;
     const float w01 = swin[d0] * swin[d1];
+    const bool mi = !(d0 == 0 || d0 == h), mj = !(d1 == 0 || d1 == h);
+    const long long rows[4] = {(long long)d0 * N + d1, (long long)d0 * N + (N - d1), (long long)(N - d0) * N + d1,
+                               (long long)(N - d0) * N + (N - d1)};
+    const bool use[4] = {true, mj, mi, mi && mj};
     for (int k0 = 0; k0 < NH; k0 += 32) {
       const int kz = k0 + lane;
       int bin = -1;
@@ -214,21 +220,31 @@ __global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
         } else {
           bin = a.rk_bin[rk];
         }
-        float2 z = a.dk[r * NH + kz];
-        if (bin >= 0) {
-          float w = (kz == 0 || 2 * kz == N) ? 1.0f : 2.0f;
-          pk = (z.x * z.x + z.y * z.y) * (w01 * swin[kz] * w);
-        }
+        float f = 0.0f;
         if (a.fuse_kind == 1) {
-          float kR = sqrtf((float)rk) * a.fuse_a, f = 1.0f;
+          float kR = sqrtf((float)rk) * a.fuse_a;
+          f = 1.0f;
           if (a.filter == MGP_FILTER_GAUSSIAN) f = expf(-0.5f * kR * kR);
           else if (a.filter == MGP_FILTER_TOPHAT) f = kR < 1e-5f ? 1.0f : 3.0f / (kR * kR * kR) * (sinf(kR) - kR * cosf(kR));
           else if (a.filter == MGP_FILTER_SHARPK) f = kR < 1.0f ? 1.0f : 0.0f;
           f *= a.fuse_b;
-          a.fuse_out[r * NH + kz] = make_float2(f * z.x, f * z.y);
         } else if (a.fuse_kind == 2) {
-          float f = rk == 0 ? 0.0f : -a.fuse_b / (float)rk;
-          a.fuse_out[r * NH + kz] = make_float2(f * z.x, f * z.y);
+          f = rk == 0 ? 0.0f : -a.fuse_b / (float)rk;
+        }
+        float2 z[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++)
+          if (use[t]) z[t] = a.dk[rows[t] * NH + kz];
+        float p2 = 0.0f;
+#pragma unroll
+        for (int t = 0; t < 4; t++)
+          if (use[t]) {
+            p2 += z[t].x * z[t].x + z[t].y * z[t].y;
+            if (a.fuse_kind) a.fuse_out[rows[t] * NH + kz] = make_float2(f * z[t].x, f * z[t].y);
+          }
+        if (bin >= 0) {
+          float w = (kz == 0 || 2 * kz == N) ? 1.0f : 2.0f;
+          pk = p2 * (w01 * swin[kz] * w);
         }
       }
       // segmented inclusive scan over runs of equal bin (|k| grows with kz)

@@ -1,0 +1,61 @@
+"""Recipe: compile MG-PICOLA's own C sources, unmodified, into single-rank
+checker binaries (test infrastructure only).
+
+The reference needs FFTW3-MPI, GSL and MPI, which this image does not have;
+the sources are compiled against the project-written shims in
+oracle/ref_shim (single-rank MPI, the oracle's FFTW-convention FFTs, GSL
+calls restated from their documentation).  Sources are read in place from
+the reference tree; outputs go to oracle/_ref/ only.  Built in double
+precision (MEMORY_MODE and SINGLE_PRECISION off) with GAUSSIAN, COMPUTE_POFK
+and GADGET_STYLE, one binary per model as the reference Makefile does.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SRC = os.environ.get("MGP_REFERENCE_SRC", "/root/reference/src")
+OUT = os.path.join(HERE, "_ref")
+SOURCES = ["main.c", "auxPM.c", "2LPT.c", "cosmo.c", "power.c", "compute_pofk.c", "read_param.c", "vars.c",
+           "wrappers.c", "timer.c", "msg.c", "jbd.c"]
+SHIM = [os.path.join(HERE, "ref_shim", "ref_shim.c"), os.path.join(HERE, "orc_fft.c"), os.path.join(HERE, "orc_rng.c")]
+COMMON = ["-DGAUSSIAN", "-DCOMPUTE_POFK", "-DGADGET_STYLE"]
+# model -> preprocessor flags (Makefile:61-106)
+MODELS = {
+    "FOFR_LCDM": ["-DFOFRGRAVITY"],
+    "DGP": ["-DDGPGRAVITY", "-DGAUSSIANFILTER"],
+    "BRANSDICKE": ["-DBRANSDICKE"],
+    "MBETA_LCDM": ["-DMBETAMODEL"],
+    "FOFR": ["-DFOFRGRAVITY", "-DSCALEDEPENDENT"],
+}
+
+
+def available():
+    return os.path.isdir(REF_SRC) and all(os.path.exists(os.path.join(REF_SRC, s)) for s in SOURCES)
+
+
+def binary(model):
+    return os.path.join(OUT, "MG_PICOLA_" + model)
+
+
+def build(models=None, verbose=False):
+    if not available():
+        raise RuntimeError("reference sources not found at " + REF_SRC)
+    os.makedirs(OUT, exist_ok=True)
+    inc = ["-I" + os.path.join(HERE, "ref_shim", "include"), "-I" + REF_SRC]
+    srcs = [os.path.join(REF_SRC, s) for s in SOURCES] + SHIM
+    newest = max(os.path.getmtime(s) for s in srcs)
+    for model in models or MODELS:
+        out = binary(model)
+        if os.path.exists(out) and os.path.getmtime(out) >= newest:
+            continue
+        cmd = (["gcc", "-O2", "-std=gnu99", "-fopenmp", "-w", "-o", out] + COMMON + MODELS[model] + inc + srcs +
+               ["-lm"])
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.check_call(cmd)
+    return OUT
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,1 @@
+#include "ref_gsl.h"

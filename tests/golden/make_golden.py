@@ -1,0 +1,105 @@
+"""Generate golden fixtures from MG-PICOLA's own code (run here).
+
+Builds the reference's unmodified C sources against the single-rank shims
+(oracle/ref_build.py), runs small COLA simulations for each model and stores
+the final P(k) table and a subsample of the final GADGET snapshot in
+tests/golden/ref_<case>.npz.  tests/test_golden.py checks the FP64 oracle
+against these files.  The white-noise stream in both is the project's Philox
+stand-in for GSL's ranlxd1 (the shim's gsl_rng_uniform), so the runs share
+identical initial conditions.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from oracle import ref_build  # noqa: E402
+
+BASE = dict(Nmesh=32, Nsample=16, Box=128.0, Init_Redshift=19.0, Seed=4242, nsteps=5)
+
+CASES = {
+    # case: (binary model, MG keys)
+    "lcdm": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1)),
+    "fofr": ("FOFR_LCDM", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1)),
+    "fofr_nosc": ("FOFR_LCDM", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=0)),
+    "dgp": ("DGP", dict(modified_gravity_active=1, rcH0_DGP=1.0, Rsmooth=1.0, include_screening=1)),
+    "jbd": ("BRANSDICKE", dict(modified_gravity_active=1, wBD=100.0, Omegah2=0.14, Omegar2=4e-5, Omegav2=0.36,
+                               include_screening=1)),
+    "mbeta": ("MBETA_LCDM", dict(modified_gravity_active=1, range_symm=1.0, assb_symm=0.5, beta_symm=1.0,
+                                 include_screening=1)),
+    "lcdm_fixed_inv": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1,
+                                         amplitude_fixed_initial_condition=1, inverted_initial_condition=1)),
+}
+
+STD = """use_lcdm_growth_factors  0
+input_pofk_is_for_lcdm   0
+input_sigma8_is_for_lcdm 1
+pofk_compute_every_step   1
+pofk_compute_rsd_pofk     0
+pofk_nbins                16
+pofk_bintype              0
+pofk_subtract_shotnoise   0
+pofk_kmin                 0.0
+pofk_kmax                 0.0
+OutputDir                   {out}
+FileBase                    run
+OutputRedshiftFile          {out}/outputs.txt
+NumFilesWrittenInParallel   1
+UseCOLA          1
+Buffer           1.5
+Nmesh            {Nmesh}
+Nsample          {Nsample}
+Box              {Box}
+Init_Redshift    {Init_Redshift}
+Seed             {Seed}
+SphereMode       0
+WhichSpectrum    2
+WhichTransfer    0
+FileWithInputSpectrum  none
+FileWithInputTransfer  none
+Omega            0.267
+OmegaBaryon      0.049
+HubbleParam      0.71
+Sigma8           0.8
+PrimordialIndex  0.96
+UnitLength_in_cm                3.085678e24
+UnitMass_in_g                   1.989e43
+UnitVelocity_in_cm_per_s        1e5
+InputSpectrum_UnitLength_in_cm  3.085678e24
+"""
+
+
+def run_case(name, model, mg):
+    with tempfile.TemporaryDirectory() as d:
+        with open(os.path.join(d, "outputs.txt"), "w") as f:
+            f.write("0, %d\n" % BASE["nsteps"])
+        mgd = dict(inverted_initial_condition=0, amplitude_fixed_initial_condition=0)
+        mgd.update(mg)
+        txt = STD.format(out=d, **BASE) + "".join("%s %s\n" % kv for kv in mgd.items())
+        pf = os.path.join(d, "params.txt")
+        with open(pf, "w") as f:
+            f.write(txt)
+        log = subprocess.run([ref_build.binary(model), pf], capture_output=True, text=True)
+        if log.returncode != 0:
+            raise RuntimeError(name + ": " + log.stdout[-2000:] + log.stderr[-2000:])
+        pk = np.loadtxt(os.path.join(d, "pofk_run_z0.000_CDM.txt"))
+        raw = open(os.path.join(d, "run_z0p000.0"), "rb").read()
+        n = BASE["Nsample"] ** 3
+        pos = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3)
+        vel = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3)
+        idx = np.arange(0, n, 8)
+        np.savez(os.path.join(ROOT, "tests", "golden", "ref_%s.npz" % name), pk=pk, idx=idx, pos=pos[idx],
+                 vel=vel[idx], model=model, **{k: float(v) for k, v in mgd.items()}, **BASE)
+        print(name, "bins", pk.shape[0])
+
+
+if __name__ == "__main__":
+    ref_build.build()
+    for name, (model, mg) in CASES.items():
+        run_case(name, model, mg)
