@@ -25,7 +25,8 @@ class MG(C.Structure):
                 ("geff_const", C.c_double), ("w0", C.c_double), ("wa", C.c_double), ("use_w0wa", C.c_int),
                 ("beta_symm", C.c_double), ("assb_symm", C.c_double), ("range_symm", C.c_double),
                 ("smoothing_filter", C.c_int), ("wBD", C.c_double), ("Omegah2", C.c_double),
-                ("Omegarh2", C.c_double), ("Omegavh2", C.c_double)]
+                ("Omegarh2", C.c_double), ("Omegavh2", C.c_double), ("scaledependent", C.c_int),
+                ("sd_nk", C.c_int), ("sd_kmin", C.c_double), ("sd_kmax", C.c_double)]
 
 
 class Power(C.Structure):
@@ -90,6 +91,21 @@ def lib():
         L.orc_screen_density.restype = C.c_double
         L.orc_cosmo_create.argtypes = [C.POINTER(MG), C.c_double]
         L.orc_cosmo_create.restype = C.c_void_p
+        L.orc_cosmo_create_sd.argtypes = [C.POINTER(MG), C.c_double, C.c_double, C.c_int]
+        L.orc_cosmo_create_sd.restype = C.c_void_p
+        L.orc_growth_sd.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double]
+        L.orc_growth_sd.restype = C.c_double
+        L.orc_mg_pofk_ratio.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        L.orc_mg_pofk_ratio.restype = C.c_double
+        L.orc_mg_sigma8_enh.argtypes = [C.c_void_p, C.POINTER(Power), C.c_double]
+        L.orc_mg_sigma8_enh.restype = C.c_double
+        L.orc_dmass2_of_ada.argtypes = [C.POINTER(MG), C.c_double]
+        L.orc_dmass2_of_ada.restype = C.c_double
+        L.orc_second_order_kernel.argtypes = [C.POINTER(MG), C.c_double, C.c_double, C.c_double, C.c_double,
+                                              C.c_double]
+        L.orc_second_order_kernel.restype = C.c_double
+        L.orc_sd_field.argtypes = [C.c_void_p, dptr, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                   C.c_int, C.c_int, dptr]
         L.orc_cosmo_free.argtypes = [C.c_void_p]
         for name in ["orc_growth_D", "orc_growth_dDdy", "orc_growth_ddDddy", "orc_growth_D2", "orc_growth_dD2dy",
                      "orc_growth_ddD2ddy", "orc_growth_DLCDM"]:
@@ -178,9 +194,9 @@ def interp(f, N, box, pos):
 
 
 class Cosmo:
-    def __init__(self, mg, init_redshift):
+    def __init__(self, mg, init_redshift, box=0.0, nmesh=0):
         self.mg = mg
-        self.h = lib().orc_cosmo_create(C.byref(mg), init_redshift)
+        self.h = lib().orc_cosmo_create_sd(C.byref(mg), init_redshift, box, nmesh)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -215,6 +231,10 @@ def make_mg(model=LCDM, omega=0.267, **kw):
     m.Omegah2 = kw.get("Omegah2", 0.14)
     m.Omegarh2 = kw.get("Omegarh2", 4.0e-5)
     m.Omegavh2 = kw.get("Omegavh2", 0.36)
+    m.scaledependent = kw.get("scaledependent", 0)
+    m.sd_nk = kw.get("sd_nk", 0)
+    m.sd_kmin = kw.get("sd_kmin", 0.0)
+    m.sd_kmax = kw.get("sd_kmax", 0.0)
     if model == JBD_GEFF:
         lib().orc_jbd_solve(C.byref(m))
     if model == MBETA and m.mg_active:
@@ -241,3 +261,14 @@ def ic_2lpt(N, Ns, box, seed, pw, fixed=0, inverted=0, sphere=0, rescale=1.0, wa
     lib().orc_ic_2lpt(C.byref(ip), C.byref(pw), D1, D2, None if dk is None else dk.ctypes.data,
                       None if s2 is None else s2.ctypes.data)
     return (D1, D2, dk, s2) if want_k else (D1, D2)
+
+
+FIELD_D, FIELD_dDdy, FIELD_ddDddy, FIELD_deltaD = 0, 1, 2, 3
+
+
+def sd_field(cosmo, stored_k, N, Ns, box, A, AFF, fieldtype, order):
+    """from_cdisp_store_to_ZA for one LPT order; stored_k is a padded complex
+    grid (delta(k) for order 1, -source(k) for order 2)."""
+    out = np.zeros((Ns ** 3, 3))
+    lib().orc_sd_field(cosmo.h, np.ascontiguousarray(stored_k), N, Ns, box, A, AFF, fieldtype, order, out)
+    return out

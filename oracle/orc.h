@@ -101,6 +101,13 @@ typedef struct {
   int smoothing_filter;    /* 0 none, 1 gaussian, 2 tophat, 3 sharpk */
   /* Brans-Dicke background parameters (src/jbd.c) */
   double wBD, Omegah2, Omegarh2, Omegavh2;
+  /* SCALEDEPENDENT build: growth factors D(k, a) from 2D tables
+   * (src/cosmo.c:798-1010).  sd_nk/sd_kmin/sd_kmax (h/Mpc) override the
+   * reference's k grid (1000 points in [pi/Box, 4 pi sqrt(3) N/Box]) when
+   * nonzero. */
+  int scaledependent;
+  int sd_nk;
+  double sd_kmin, sd_kmax;
 } orc_mg;
 
 /* Brans-Dicke background (src/jbd.c) and the m(a), beta(a) phi_crit(a)
@@ -118,6 +125,10 @@ double orc_mass2_of_a(const orc_mg *m, double a);
 double orc_coupling(const orc_mg *m, double a);
 double orc_geff(const orc_mg *m, double a, double k);
 double orc_factor_2lpt(const orc_mg *m, double a);
+/* dmass2_of_ada (user_defined_functions.h:527-560) and the second-order
+ * kernel gamma_2(k, k1, k2, cos theta, a) (user_defined_functions.h:848-904) */
+double orc_dmass2_of_ada(const orc_mg *m, double a);
+double orc_second_order_kernel(const orc_mg *m, double k, double k1, double k2, double costheta, double a);
 double orc_screen_potential(const orc_mg *m, double a, double phinewton);
 double orc_screen_density(const orc_mg *m, double a, double density);
 
@@ -128,7 +139,18 @@ double orc_screen_density(const orc_mg *m, double a, double density);
 void orc_fifth_force(const orc_mg *m, double a, int N, double box,
                      const double *density_x, double *deltak, double *mgk);
 
+/* ------------------------------------------------- 2D bicubic tables */
+/* GSL gsl_interp2d_bicubic restated (orc_interp2d.c); z[j * nx + i]. */
+typedef struct {
+  int nx, ny;
+  double *x, *y, *z, *zx, *zy, *zxy;
+} orc_bicubic;
+void orc_bicubic_init(orc_bicubic *b, const double *x, const double *y, const double *z, int nx, int ny);
+double orc_bicubic_eval(const orc_bicubic *b, double x, double y);
+void orc_bicubic_free(orc_bicubic *b);
+
 /* ----------------------------------------------------------- cosmology */
+struct orc_power_s;
 typedef struct orc_cosmo orc_cosmo;
 /* Growth ODEs (src/cosmo.c:206-643) on a fine fixed-step RK4 grid. */
 orc_cosmo *orc_cosmo_create(const orc_mg *m, double init_redshift);
@@ -140,6 +162,18 @@ double orc_growth_D2(orc_cosmo *c, double a);
 double orc_growth_dD2dy(orc_cosmo *c, double a);
 double orc_growth_ddD2ddy(orc_cosmo *c, double a);
 double orc_growth_DLCDM(orc_cosmo *c, double a);
+/* Scale-dependent build: the growth ODEs per k on the reference's k grid
+ * (needs Box and Nmesh for that grid).  orc_cosmo_create is this with the
+ * tables off. */
+orc_cosmo *orc_cosmo_create_sd(const orc_mg *m, double init_redshift, double box, int nmesh);
+/* growth_*_scaledependent (src/cosmo.c:987-1010): which 0 D, 1 dDdy,
+ * 2 ddDddy, 3 D2, 4 dD2dy, 5 ddD2ddy; k in h/Mpc, normalised at a = 1 per k. */
+double orc_growth_sd(orc_cosmo *c, int which, double k, double a);
+/* mg_pofk_ratio (src/cosmo.c:688-706) and mg_sigma8_enhancement
+ * (src/cosmo.c:713-756), both build variants. */
+double orc_mg_pofk_ratio(orc_cosmo *c, double k, double a);
+double orc_mg_sigma8_enh(orc_cosmo *c, const struct orc_power_s *pw, double a);
+
 /* COLA coefficients (src/cosmo.c:1114-1160), nLPT = -2.5, fullT = 1. */
 double orc_Sq(orc_cosmo *c, double ai, double af, double aref);
 double orc_Sphi(orc_cosmo *c, double ai, double af, double aref);
@@ -147,7 +181,7 @@ double orc_Sphi(orc_cosmo *c, double ai, double af, double aref);
 double orc_growthD_fit(double omega, double a);
 
 /* Linear power spectrum (src/power.c:373-498). */
-typedef struct {
+typedef struct orc_power_s {
   int which_spectrum;       /* 0 transfer-function, 1 tabulated, else EH */
   double omega, omega_b, h, ns, sigma8;
   int ntab; const double *tab_logk, *tab_logP;   /* log10 table for type 1 */
@@ -173,6 +207,16 @@ void orc_seedtable(int N, uint32_t seed, uint32_t *table);
  * pointers are non-NULL. */
 void orc_ic_2lpt(const orc_ic_params *ip, const orc_power *pw, double *D1, double *D2,
                  double *deltak_out, double *source2k_out);
+
+/* Scale-dependent displacement fields (SCALEDEPENDENT build).  Field types
+ * as src/proto.h:153-158. */
+enum { ORC_FIELD_D = 0, ORC_FIELD_dDdy = 1, ORC_FIELD_ddDddy = 2, ORC_FIELD_deltaD = 3 };
+/* from_cdisp_store_to_ZA (src/2LPT.c:1539-1735) for one LPT order (1 or 2):
+ * disp(k) = i k/k^2 stored(k) G(k), three c2r, trilinear read-out at the
+ * Lagrangian lattice, mean removed.  stored is delta(k) for order 1 and
+ * -source(k) for order 2 (orc_ic_2lpt outputs).  out [Ns^3][3]. */
+void orc_sd_field(orc_cosmo *c, const double *stored, int N, int Ns, double box, double A, double AFF,
+                  int fieldtype, int order, double *out);
 
 /* --------------------------------------------------------- full run */
 typedef struct {

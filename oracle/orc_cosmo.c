@@ -99,6 +99,56 @@ double orc_factor_2lpt(const orc_mg *m, double a) {
   }
   return 1.0;
 }
+/* dmass2_of_ada: user_defined_functions.h:527-560 (dm^2/da / H0^2) */
+double orc_dmass2_of_ada(const orc_mg *m, double a) {
+  if (m->model == ORC_FOFR) {
+    double a3 = a * a * a;
+    double fac = m->omega / a3 + 4.0 * (1.0 - m->omega);
+    double fac0 = m->omega + 4.0 * (1.0 - m->omega);
+    double mass2 = fac0 * (m->nfofr + 2.0) * pow(fac / fac0, m->nfofr + 1.0) / ((1.0 + m->nfofr) * m->fofr0 * fac0);
+    return mass2 * (-3.0 * m->omega / a3 / a);
+  }
+  if (m->model == ORC_MBETA) {
+    if (a > m->assb_symm) return 0.5 * pow(2998.0 / m->range_symm, 2) * (3.0 * pow(m->assb_symm / a, 3) / a);
+    return 0.0;
+  }
+  return 0.0;
+}
+/* fofr_pi_factor: user_defined_functions.h:848-854 */
+static double fofr_pi(const orc_mg *m, double k, double a) {
+  double a3 = a * a * a;
+  double fac = m->omega / a3 + 4.0 * (1.0 - m->omega);
+  double fac0 = m->omega + 4.0 * (1.0 - m->omega);
+  return pow(k * INVERSE_H0_MPCH / a, 2) + fac0 * pow(fac / fac0, m->nfofr + 2.0) / (1.0 + m->nfofr) / m->fofr0;
+}
+/* second_order_kernel: user_defined_functions.h:862-904 */
+double orc_second_order_kernel(const orc_mg *m, double k, double k1, double k2, double cost, double a) {
+  if (!m->mg_active || m->use_lcdm_growth) return 0.0;
+  double g = 0.0, H = orc_hubble(m, a), a3 = a * a * a;
+  if (m->model == ORC_FOFR) {
+    double fac = m->omega / a3 + 4.0 * (1.0 - m->omega);
+    double fac0 = m->omega + 4.0 * (1.0 - m->omega);
+    double n = m->nfofr;
+    g = -(3.0 * (n + 2.0) / (12.0 * (1.0 + n) * (1.0 + n))) * pow(k * INVERSE_H0_MPCH / (a * H), 2) *
+        pow(m->omega / a3, 2) * fac0 * pow(fac / fac0, 2.0 * n + 3.0) / pow(m->fofr0, 2);
+    g /= fofr_pi(m, k, a) * fofr_pi(m, k1, a) * fofr_pi(m, k2, a);
+  } else if (m->model == ORC_DGP) {
+    g = -1.0 / 6.0 / pow(orc_beta_dgp(m, a), 3) * pow(m->rcH0 / H, 2) * pow(m->omega / a3, 2) * (1.0 - cost * cost);
+  } else if (m->model == ORC_MBETA) {
+    double m2 = orc_mass2_of_a(m, a), dm2da = orc_dmass2_of_ada(m, a);
+    double pk = pow(k * INVERSE_H0_MPCH / a, 2) + m2;
+    double pk1 = pow(k1 * INVERSE_H0_MPCH / a, 2) + m2;
+    double pk2 = pow(k2 * INVERSE_H0_MPCH / a, 2) + m2;
+    double b = orc_beta_of_a(m, a);
+    g = (dm2da / m2) * b * b * m->omega / (2.0 * a * a) * (m2 / pk1) * (m2 / pk2) * (1.0 - m2 / pk) / (H * H);
+  }
+  if (k2 > 1e-3 && k1 > 1e-3) {
+    double mk = orc_geff(m, a, k);
+    g += 1.5 * m->omega / (a3 * H * H) *
+         ((mk - orc_geff(m, a, k1)) * (k1 / k2) + (mk - orc_geff(m, a, k2)) * (k2 / k1)) * cost / 2.0;
+  }
+  return g;
+}
 /* screening_factor_potential: user_defined_functions.h:725-750 (f(R)) */
 double orc_screen_potential(const orc_mg *m, double a, double phinewton) {
   if (!m->include_screening) return 1.0;
@@ -218,44 +268,105 @@ static double integrate(fn1 f, void *par, double a, double b) {
 struct orc_cosmo {
   orc_mg m;
   spline1 D, dDdy, ddDddy, D2, dD2dy, ddD2ddy, DLCDM;
+  /* SCALEDEPENDENT: D, dDdy, ddDddy, D2, dD2dy, ddD2ddy over (ln a, ln k) */
+  int sd;
+  orc_bicubic tab[6];
 };
 
-/* ode_growth_D (cosmo.c:206-239), non-SCALEDEPENDENT modfac = Factor_2LPT;
- * lcdm = 1 gives ode_growth_DLCDM (cosmo.c:245-268). k = 1e-3 h/Mpc as in
- * solve_for_growth_factors (cosmo.c:456). */
-static void growth_rhs(const orc_mg *m, int lcdm, double x, const double *D, double *dD) {
+/* ode_growth_D (cosmo.c:206-239); lcdm = 1 gives ode_growth_DLCDM
+ * (cosmo.c:245-268).  modfac is Factor_2LPT(a) in the scale-independent
+ * build and 1 + 2 (a^2 H)^2 gamma_2(k, k/sqrt2, k/sqrt2, 0, a) / (1.5 Omega a
+ * mu) in the SCALEDEPENDENT build (cosmo.c:215-223).  The 1D tables use
+ * k = 1e-3 h/Mpc (solve_for_growth_factors, cosmo.c:456). */
+static void growth_rhs(const orc_mg *m, int lcdm, double k, double x, const double *D, double *dD) {
   double a = exp(x);
-  double k = 1e-3;
   double mu = lcdm ? 1.0 : orc_geff(m, a, k);
   double H = orc_hubble(m, a), dH = orc_dhubbleda(m, a);
   double betafac = 1.5 * m->omega * mu / (a * a * a * H * H);
   double alphafac = 2.0 + a * dH / H;
-  double modfac = lcdm ? 1.0 : orc_factor_2lpt(m, a);
+  double modfac = 1.0;
+  if (!lcdm) {
+    if (m->scaledependent)
+      modfac = 1.0 + 2.0 * pow(a * a * H, 2) * orc_second_order_kernel(m, k, k / sqrt(2.0), k / sqrt(2.0), 0.0, a) /
+                         (1.5 * m->omega * a * mu);
+    else
+      modfac = orc_factor_2lpt(m, a);
+  }
   dD[0] = D[1];
   dD[1] = -alphafac * D[1] + betafac * D[0];
   dD[2] = D[3];
   dD[3] = -alphafac * D[3] + betafac * (D[2] - modfac * D[0] * D[0]);
 }
 
-static void rk4(const orc_mg *m, int lcdm, double x0, double x1, int nsub, double *y) {
+static void rk4(const orc_mg *m, int lcdm, double k, double x0, double x1, int nsub, double *y) {
   double h = (x1 - x0) / nsub;
   for (int s = 0; s < nsub; s++) {
     double x = x0 + s * h, k1[4], k2[4], k3[4], k4[4], t[4];
-    growth_rhs(m, lcdm, x, y, k1);
+    growth_rhs(m, lcdm, k, x, y, k1);
     for (int i = 0; i < 4; i++) t[i] = y[i] + 0.5 * h * k1[i];
-    growth_rhs(m, lcdm, x + 0.5 * h, t, k2);
+    growth_rhs(m, lcdm, k, x + 0.5 * h, t, k2);
     for (int i = 0; i < 4; i++) t[i] = y[i] + 0.5 * h * k2[i];
-    growth_rhs(m, lcdm, x + 0.5 * h, t, k3);
+    growth_rhs(m, lcdm, k, x + 0.5 * h, t, k3);
     for (int i = 0; i < 4; i++) t[i] = y[i] + h * k3[i];
-    growth_rhs(m, lcdm, x + h, t, k4);
+    growth_rhs(m, lcdm, k, x + h, t, k4);
     for (int i = 0; i < 4; i++) y[i] += h / 6.0 * (k1[i] + 2 * k2[i] + 2 * k3[i] + k4[i]);
   }
 }
 
 static double Qfactor(const orc_mg *m, double a) { return orc_hubble(m, a) * a * a * a; }
 
-/* solve_for_growth_factors (cosmo.c:409-643) */
+/* calculate_scale_dependent_growth_factor (cosmo.c:798-981): the growth
+ * ODEs for each of nk log-spaced k, stored as 2D tables over (ln a, ln k). */
+static void solve_sd(orc_cosmo *c, double xini, double xend, int npts, double box, int nmesh) {
+  const orc_mg *m = &c->m;
+  int nk = m->sd_nk > 0 ? m->sd_nk : 1000;
+  double kmin = m->sd_kmin > 0 ? m->sd_kmin : 2.0 * M_PI / box * 0.5;
+  double kmax = m->sd_kmax > 0 ? m->sd_kmax : 2.0 * M_PI / box * nmesh * sqrt(3.0) * 2.0;
+  double *logk = malloc(8 * nk), *x = malloc(8 * npts);
+  double *T[6];
+  for (int f = 0; f < 6; f++) T[f] = malloc(sizeof(double) * npts * nk);
+  for (int i = 0; i < nk; i++) logk[i] = log(kmin) + log(kmax / kmin) * i / (double)(nk - 1);
+  for (int i = 0; i < npts; i++) x[i] = xini + (xend - xini) * i / (double)(npts - 1);
+#pragma omp parallel for schedule(dynamic)
+  for (int ik = 0; ik < nk; ik++) {
+    double know = exp(log(kmin) + log(kmax / kmin) * ik / (double)(nk - 1));
+    double y[4] = {1.0, 1.0, -3.0 / 7.0, -6.0 / 7.0};
+    for (int i = 0; i < npts; i++) {
+      if (i > 0) rk4(m, 0, know, x[i - 1], x[i], 16, y);
+      double anow = exp(x[i]), mu = orc_geff(m, anow, know);
+      size_t c0 = (size_t)ik * npts + i;
+      T[0][c0] = y[0];
+      T[1][c0] = y[1] * Qfactor(m, anow) / anow;
+      T[2][c0] = 1.5 * mu * m->omega * anow * y[0];
+      T[3][c0] = y[2];
+      T[4][c0] = y[3] * Qfactor(m, anow) / anow;
+      T[5][c0] = 1.5 * mu * m->omega * anow * (y[2] - y[0] * y[0]);
+    }
+  }
+  for (int f = 0; f < 6; f++) {
+    orc_bicubic_init(&c->tab[f], x, logk, T[f], npts, nk);
+    free(T[f]);
+  }
+  free(logk);
+  free(x);
+  c->sd = 1;
+}
+
+/* Lookup_GSL_2D_Spline (src/wrappers.c:129-136): clamp, then evaluate */
+static double lookup2d(const orc_bicubic *b, double x, double y) {
+  if (x < b->x[0]) x = b->x[0];
+  if (x > b->x[b->nx - 1]) x = b->x[b->nx - 1];
+  if (y < b->y[0]) y = b->y[0];
+  if (y > b->y[b->ny - 1]) y = b->y[b->ny - 1];
+  return orc_bicubic_eval(b, x, y);
+}
+
 orc_cosmo *orc_cosmo_create(const orc_mg *m, double init_redshift) {
+  return orc_cosmo_create_sd(m, init_redshift, 0.0, 0);
+}
+
+/* solve_for_growth_factors (cosmo.c:409-643) */
+orc_cosmo *orc_cosmo_create_sd(const orc_mg *m, double init_redshift, double box, int nmesh) {
   orc_cosmo *c = calloc(1, sizeof(orc_cosmo));
   c->m = *m;
   const int npts = 1000;
@@ -268,8 +379,8 @@ orc_cosmo *orc_cosmo_create(const orc_mg *m, double init_redshift) {
   for (int i = 0; i < npts; i++) {
     double xnow = xini + i * dx;
     if (i > 0) {
-      rk4(m, 0, xini + (i - 1) * dx, xnow, 64, y);
-      rk4(m, 1, xini + (i - 1) * dx, xnow, 64, yl);
+      rk4(m, 0, 1e-3, xini + (i - 1) * dx, xnow, 64, y);
+      rk4(m, 1, 1e-3, xini + (i - 1) * dx, xnow, 64, yl);
     }
     double anow = exp(xnow), mu = orc_geff(m, anow, 1e-3);
     x[i] = xnow;
@@ -285,13 +396,47 @@ orc_cosmo *orc_cosmo_create(const orc_mg *m, double init_redshift) {
   spline_init(&c->D2, x, D2, npts); spline_init(&c->dD2dy, x, dD2, npts); spline_init(&c->ddD2ddy, x, ddD2, npts);
   spline_init(&c->DLCDM, x, DL, npts);
   free(x); free(D); free(dD); free(ddD); free(D2); free(dD2); free(ddD2); free(DL);
+  if (m->scaledependent && box > 0 && nmesh > 0) solve_sd(c, xini, xend, npts, box, nmesh);
   return c;
 }
 void orc_cosmo_free(orc_cosmo *c) {
   if (!c) return;
   spline_free(&c->D); spline_free(&c->dDdy); spline_free(&c->ddDddy);
   spline_free(&c->D2); spline_free(&c->dD2dy); spline_free(&c->ddD2ddy); spline_free(&c->DLCDM);
+  if (c->sd)
+    for (int f = 0; f < 6; f++) orc_bicubic_free(&c->tab[f]);
   free(c);
+}
+/* growth_*_scaledependent (cosmo.c:987-1010) */
+double orc_growth_sd(orc_cosmo *c, int which, double k, double a) {
+  const orc_bicubic *norm = &c->tab[which < 3 ? 0 : 3];
+  return lookup2d(&c->tab[which], log(a), log(k)) / lookup2d(norm, 0.0, log(k));
+}
+/* mg_pofk_ratio (cosmo.c:688-706), no massive neutrinos */
+double orc_mg_pofk_ratio(orc_cosmo *c, double k, double a) {
+  if (!c->m.mg_active) return 1.0;
+  double r = c->sd ? lookup2d(&c->tab[0], log(a), log(k)) / spline_eval(&c->DLCDM, log(a))
+                   : spline_eval(&c->D, log(a)) / spline_eval(&c->DLCDM, log(a));
+  return r * r;
+}
+/* mg_sigma8_enhancement (cosmo.c:713-756) */
+double orc_mg_sigma8_enh(orc_cosmo *c, const struct orc_power_s *pw, double a) {
+  if (!c->m.mg_active) return 1.0;
+  if (!c->sd) return spline_eval(&c->D, log(a)) / spline_eval(&c->DLCDM, log(a));
+  const double kmin = 0.001, kmax = 100.0;
+  const int npts = 1000;
+  double s = 0.0, sl = 0.0, dlogk = log(kmax / kmin) / (double)(npts - 1);
+  for (int i = 0; i < npts; i++) {
+    double know = exp(log(kmin) + log(kmax / kmin) * i / (double)(npts - 1));
+    double kR8 = know * 8.0;
+    double w = 3.0 / (kR8 * kR8 * kR8) * (sin(kR8) - kR8 * cos(kR8));
+    double D = lookup2d(&c->tab[0], log(a), log(know));
+    double DL = spline_eval(&c->DLCDM, log(a));
+    double power = orc_power_spec((const orc_power *)pw, know);
+    s += power * w * w * D * D * know * know * know * dlogk / (2.0 * M_PI * M_PI);
+    sl += power * w * w * DL * DL * know * know * know * dlogk / (2.0 * M_PI * M_PI);
+  }
+  return sqrt(s) / sqrt(sl);
 }
 /* growth_* lookups (cosmo.c:318-403), normalised at a = 1 */
 double orc_growth_D(orc_cosmo *c, double a) { return spline_eval(&c->D, log(a)) / spline_eval(&c->D, 0.0); }

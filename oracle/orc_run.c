@@ -13,19 +13,43 @@ int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
   const double Box = rp->ic.box;
   const long np = (long)Ns * Ns * Ns;
   const size_t tot = (size_t)N * N * NH;
-  orc_cosmo *c = orc_cosmo_create(&rp->mg, rp->init_redshift);
+  const int sd = rp->mg.scaledependent;
+  orc_cosmo *c = orc_cosmo_create_sd(&rp->mg, rp->init_redshift, Box, N);
   double *D1 = malloc(8 * 3 * np), *D2 = malloc(8 * 3 * np), *pos = malloc(8 * 3 * np), *vel = calloc(3 * np, 8);
   double *disp = malloc(8 * 3 * np);
-  orc_ic_2lpt(&rp->ic, &rp->pw, D1, D2, NULL, NULL);
+  /* SCALEDEPENDENT: the stored delta(k) and -source(k) (2LPT.c:301-309,
+   * 1336-1344) and the particle fields dDdy/dD2dy (vars.h:303-311); D1/D2
+   * then play P.D/P.D2, which hold D at the IC and ddDddy in the loop */
+  double *cdelta = NULL, *cdelta2 = NULL, *V1 = NULL, *V2 = NULL;
+  if (sd) {
+    cdelta = malloc(sizeof(double) * 2 * tot);
+    cdelta2 = malloc(sizeof(double) * 2 * tot);
+    V1 = malloc(8 * 3 * np);
+    V2 = malloc(8 * 3 * np);
+  }
+  orc_ic_2lpt(&rp->ic, &rp->pw, D1, D2, cdelta, cdelta2);
 
   double A = 1.0 / (1.0 + rp->init_redshift);
   double Di = orc_growth_D(c, A), Di2 = orc_growth_D2(c, A);
-  /* main.c:289-307 (non-SCALEDEPENDENT) */
+  if (sd) {
+    /* main.c:244-251 */
+    orc_sd_field(c, cdelta, N, Ns, Box, A, A, ORC_FIELD_D, 1, D1);
+    orc_sd_field(c, cdelta2, N, Ns, Box, A, A, ORC_FIELD_D, 2, D2);
+    orc_sd_field(c, cdelta, N, Ns, Box, A, A, ORC_FIELD_dDdy, 1, V1);
+    orc_sd_field(c, cdelta2, N, Ns, Box, A, A, ORC_FIELD_dDdy, 2, V2);
+  }
+  /* main.c:256-307: x = q + D Di + D2 Di2, or q + D + D2 when scale dependent;
+   * v = 0 for COLA, else the 2LPT velocity */
+  double fD = sd ? 1.0 : Di, fD2 = sd ? 1.0 : Di2;
   for (long p = 0; p < np; p++) {
     long i = p / ((long)Ns * Ns), j = (p / Ns) % Ns, k = p % Ns;
     long q[3] = {i, j, k};
-    for (int a = 0; a < 3; a++)
-      pos[3 * p + a] = orc_periodic_wrap(q[a] * (Box / (double)Ns) + D1[3 * p + a] * Di + D2[3 * p + a] * Di2, Box);
+    for (int a = 0; a < 3; a++) {
+      pos[3 * p + a] = orc_periodic_wrap(q[a] * (Box / (double)Ns) + D1[3 * p + a] * fD + D2[3 * p + a] * fD2, Box);
+      if (!rp->usecola)
+        vel[3 * p + a] = sd ? V1[3 * p + a] + V2[3 * p + a]
+                            : D1[3 * p + a] * orc_growth_dDdy(c, A) + D2[3 * p + a] * orc_growth_dD2dy(c, A);
+    }
   }
   double AI = A, AF = A, AFF = A, da = 0;
   double *grid = malloc(sizeof(double) * 2 * tot), *dens_x = malloc(sizeof(double) * 2 * tot);
@@ -60,24 +84,43 @@ int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
       for (int a = 0; a < 3; a++) orc_fft_c2r(N, f[a]);
       double sumD[3];
       orc_interp(f[0], f[1], f[2], N, Box, pos, np, disp, sumD);
-      /* Kick (main.c:688-742) */
+      if (sd) {
+        /* main.c:487-503: [deltaD] into dDdy/dD2dy, [ddDddy] into D/D2 */
+        orc_sd_field(c, cdelta, N, Ns, Box, A, AFF, ORC_FIELD_deltaD, 1, V1);
+        orc_sd_field(c, cdelta2, N, Ns, Box, A, AFF, ORC_FIELD_deltaD, 2, V2);
+        orc_sd_field(c, cdelta, N, Ns, Box, A, AFF, ORC_FIELD_ddDddy, 1, D1);
+        orc_sd_field(c, cdelta2, N, Ns, Box, A, AFF, ORC_FIELD_ddDddy, 2, D2);
+      }
+      /* Kick (main.c:688-742); the scale-dependent Kick uses D + D2 */
       double dda = orc_Sphi(c, AI, AF, A);
-      orc_kick(np, vel, disp, D1, D2, sumD, rp->mg.omega, dda, orc_growth_ddDddy(c, A), orc_growth_ddD2ddy(c, A), A,
-               rp->usecola, sumv);
+      orc_kick(np, vel, disp, D1, D2, sumD, rp->mg.omega, dda, sd ? 1.0 : orc_growth_ddDddy(c, A),
+               sd ? 1.0 : orc_growth_ddD2ddy(c, A), A, rp->usecola, sumv);
       if (ts == 0 && io != 0) {
-        /* output step (main.c:516-549): the last output ends the run */
+        /* output step (main.c:516-549): the last output ends the run; the
+         * scale-dependent Output first puts [dDdy] into dDdy/dD2dy
+         * (main.c:807-823) */
+        if (sd) {
+          orc_sd_field(c, cdelta, N, Ns, Box, A, AFF, ORC_FIELD_dDdy, 1, V1);
+          orc_sd_field(c, cdelta2, N, Ns, Box, A, AFF, ORC_FIELD_dDdy, 2, V2);
+        }
         double dDdy = orc_growth_dDdy(c, A), dD2dy = orc_growth_dD2dy(c, A);
         for (long p = 0; p < np; p++)
           for (int a = 0; a < 3; a++) {
             pos_out[3 * p + a] = pos[3 * p + a];
-            vel_out[3 * p + a] = vel[3 * p + a] - sumv[a] + (D1[3 * p + a] * dDdy + D2[3 * p + a] * dD2dy) * rp->usecola;
+            double lpt = sd ? V1[3 * p + a] + V2[3 * p + a] : D1[3 * p + a] * dDdy + D2[3 * p + a] * dD2dy;
+            vel_out[3 * p + a] = vel[3 * p + a] - sumv[a] + lpt * rp->usecola;
           }
         goto done;
       }
-      /* Drift (main.c:747-787) */
+      /* Drift (main.c:747-787); the scale-dependent Drift adds dDdy + dD2dy,
+       * which hold [deltaD] here */
       double dyyy = orc_Sq(c, A, AFF, AF);
-      double dD = orc_growth_D(c, AFF) - Di, dD2 = orc_growth_D2(c, AFF) - Di2;
-      orc_drift(np, pos, vel, D1, D2, sumv, dyyy, dD, dD2, rp->usecola, Box);
+      if (sd) {
+        orc_drift(np, pos, vel, V1, V2, sumv, dyyy, 1.0, 1.0, rp->usecola, Box);
+      } else {
+        double dD = orc_growth_D(c, AFF) - Di, dD2 = orc_growth_D2(c, AFF) - Di2;
+        orc_drift(np, pos, vel, D1, D2, sumv, dyyy, dD, dD2, rp->usecola, Box);
+      }
       A = AFF;
       AI = AF;
       Di = orc_growth_D(c, A);
@@ -87,6 +130,7 @@ int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
 done:
   for (int a = 0; a < 3; a++) free(f[a]);
   free(grid); free(dens_x); free(mgk); free(D1); free(D2); free(pos); free(vel); free(disp);
+  free(cdelta); free(cdelta2); free(V1); free(V2);
   orc_cosmo_free(c);
   return nb;
 }

@@ -18,7 +18,8 @@ REF_SRC = os.environ.get("MGP_REFERENCE_SRC", "/root/reference/src")
 OUT = os.path.join(HERE, "_ref")
 SOURCES = ["main.c", "auxPM.c", "2LPT.c", "cosmo.c", "power.c", "compute_pofk.c", "read_param.c", "vars.c",
            "wrappers.c", "timer.c", "msg.c", "jbd.c"]
-SHIM = [os.path.join(HERE, "ref_shim", "ref_shim.c"), os.path.join(HERE, "orc_fft.c"), os.path.join(HERE, "orc_rng.c")]
+SHIM = [os.path.join(HERE, "ref_shim", "ref_shim.c"), os.path.join(HERE, "orc_fft.c"), os.path.join(HERE, "orc_rng.c"),
+        os.path.join(HERE, "orc_interp2d.c")]
 COMMON = ["-DGAUSSIAN", "-DCOMPUTE_POFK", "-DGADGET_STYLE"]
 # model -> preprocessor flags (Makefile:61-106)
 MODELS = {
@@ -27,6 +28,7 @@ MODELS = {
     "BRANSDICKE": ["-DBRANSDICKE"],
     "MBETA_LCDM": ["-DMBETAMODEL"],
     "FOFR": ["-DFOFRGRAVITY", "-DSCALEDEPENDENT"],
+    "MBETA": ["-DMBETAMODEL", "-DSCALEDEPENDENT"],
 }
 
 
@@ -44,7 +46,9 @@ def build(models=None, verbose=False):
     os.makedirs(OUT, exist_ok=True)
     inc = ["-I" + os.path.join(HERE, "ref_shim", "include"), "-I" + REF_SRC]
     srcs = [os.path.join(REF_SRC, s) for s in SOURCES] + SHIM
-    newest = max(os.path.getmtime(s) for s in srcs)
+    headers = [os.path.join(HERE, "orc.h")] + [os.path.join(d, f) for d, _, fs in os.walk(os.path.join(HERE, "ref_shim"))
+                                              for f in fs if f.endswith(".h")]
+    newest = max(os.path.getmtime(s) for s in srcs + headers)
     for model in models or MODELS:
         out = binary(model)
         if os.path.exists(out) and os.path.getmtime(out) >= newest:

@@ -48,7 +48,7 @@ extern const gsl_interp_type *gsl_interp_cspline;
 extern const gsl_interp2d_type *gsl_interp2d_bicubic;
 typedef struct { size_t cache; } gsl_interp_accel;
 typedef struct { size_t n; double *x, *y, *y2; } gsl_spline;
-typedef struct { size_t nx, ny; double *x, *y, *z; } gsl_spline2d;
+typedef struct { size_t nx, ny; void *impl; } gsl_spline2d;
 gsl_interp_accel *gsl_interp_accel_alloc(void);
 void gsl_interp_accel_free(gsl_interp_accel *a);
 gsl_spline *gsl_spline_alloc(const gsl_interp_type *T, size_t n);

@@ -270,47 +270,28 @@ double gsl_spline_eval(const gsl_spline *s, double x, gsl_interp_accel *a) {
   return A * s->y[lo] + B * s->y[hi] + ((A * A * A - A) * s->y2[lo] + (B * B * B - B) * s->y2[hi]) * h * h / 6.0;
 }
 void gsl_spline_free(gsl_spline *s) { if (!s) return; free(s->x); free(s->y); free(s->y2); free(s); }
+/* gsl_interp2d_bicubic: the oracle's restatement (oracle/orc_interp2d.c) */
 gsl_spline2d *gsl_spline2d_alloc(const gsl_interp2d_type *T, size_t nx, size_t ny) {
   (void)T;
   gsl_spline2d *s = calloc(1, sizeof(*s));
   s->nx = nx; s->ny = ny;
-  s->x = malloc(8 * nx); s->y = malloc(8 * ny); s->z = malloc(8 * nx * ny);
+  s->impl = calloc(1, sizeof(orc_bicubic));
   return s;
 }
 int gsl_spline2d_init(gsl_spline2d *s, const double x[], const double y[], const double z[], size_t nx, size_t ny) {
-  memcpy(s->x, x, 8 * nx); memcpy(s->y, y, 8 * ny); memcpy(s->z, z, 8 * nx * ny);
+  orc_bicubic_init((orc_bicubic *)s->impl, x, y, z, (int)nx, (int)ny);
   return GSL_SUCCESS;
-}
-static void keys_w(double t, double w[4]) {
-  /* cubic convolution kernel with a = -1/2 */
-  w[0] = ((-0.5 * t + 1.0) * t - 0.5) * t;
-  w[1] = (1.5 * t - 2.5) * t * t + 1.0;
-  w[2] = ((-1.5 * t + 2.0) * t + 0.5) * t;
-  w[3] = (0.5 * t - 0.5) * t * t;
 }
 double gsl_spline2d_eval(const gsl_spline2d *s, double x, double y, gsl_interp_accel *xa, gsl_interp_accel *ya) {
   (void)xa; (void)ya;
-  long i = (long)find_lo(s->x, s->nx, x), j = (long)find_lo(s->y, s->ny, y);
-  double tx = (x - s->x[i]) / (s->x[i + 1] - s->x[i]), ty = (y - s->y[j]) / (s->y[j + 1] - s->y[j]);
-  double wx[4], wy[4], r = 0.0;
-  keys_w(tx, wx);
-  keys_w(ty, wy);
-  for (int b = 0; b < 4; b++) {
-    long jj = j - 1 + b;
-    if (jj < 0) jj = 0;
-    if (jj >= (long)s->ny) jj = (long)s->ny - 1;
-    double row = 0.0;
-    for (int a = 0; a < 4; a++) {
-      long ii = i - 1 + a;
-      if (ii < 0) ii = 0;
-      if (ii >= (long)s->nx) ii = (long)s->nx - 1;
-      row += wx[a] * s->z[jj * s->nx + ii];
-    }
-    r += wy[b] * row;
-  }
-  return r;
+  return orc_bicubic_eval((const orc_bicubic *)s->impl, x, y);
 }
-void gsl_spline2d_free(gsl_spline2d *s) { if (!s) return; free(s->x); free(s->y); free(s->z); free(s); }
+void gsl_spline2d_free(gsl_spline2d *s) {
+  if (!s) return;
+  orc_bicubic_free((orc_bicubic *)s->impl);
+  free(s->impl);
+  free(s);
+}
 
 /* ---------------------------------------------------------------- roots */
 static const gsl_root_fsolver_type brent_t = {3};

@@ -35,6 +35,10 @@ CASES = {
                                  include_screening=1)),
     "lcdm_fixed_inv": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1,
                                          amplitude_fixed_initial_condition=1, inverted_initial_condition=1)),
+    # SCALEDEPENDENT builds: growth factors D(k, a) from 2D tables
+    "fofr_sd": ("FOFR", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1)),
+    "mbeta_sd": ("MBETA", dict(modified_gravity_active=1, range_symm=1.0, assb_symm=0.5, beta_symm=1.0,
+                               include_screening=1)),
 }
 
 STD = """use_lcdm_growth_factors  0
@@ -101,5 +105,8 @@ def run_case(name, model, mg):
 
 if __name__ == "__main__":
     ref_build.build()
+    # optional case names on the command line regenerate only those
     for name, (model, mg) in CASES.items():
+        if len(sys.argv) > 1 and name not in sys.argv[1:]:
+            continue
         run_case(name, model, mg)

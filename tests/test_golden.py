@@ -28,10 +28,11 @@ def oracle_run(g):
                        Omegarh2=float(g["Omegar2"]), Omegavh2=float(g["Omegav2"]))
     elif model.startswith("MBETA"):
         mg = O.make_mg(O.MBETA, 0.267, mg_active=active, include_screening=scr, assb_symm=float(g["assb_symm"]),
-                       beta_symm=float(g["beta_symm"]), range_symm=float(g["range_symm"]))
+                       beta_symm=float(g["beta_symm"]), range_symm=float(g["range_symm"]),
+                       scaledependent=int(model == "MBETA"))
     else:
         mg = O.make_mg(O.FOFR, 0.267, mg_active=active, include_screening=scr, fofr0=float(g["fofr0"]),
-                       nfofr=float(g["nfofr"]))
+                       nfofr=float(g["nfofr"]), scaledependent=int(model == "FOFR"))
     N, Ns, box = int(g["Nmesh"]), int(g["Nsample"]), float(g["Box"])
     rp = O.RunParams()
     rp.mg = mg
