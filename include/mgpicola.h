@@ -135,6 +135,13 @@ typedef struct mgp_params {
   int Noutputs;
   double output_redshift[64];
   int output_nsteps[64];
+
+  /* k grid of the scale-dependent growth tables (not parameter-file keys;
+   * src/cosmo.c:803-805 hard-codes them): number of log-spaced k and the
+   * range in h/Mpc.  0 selects the reference's grid, 1000 points in
+   * [pi/Box, 4 pi sqrt(3) Nmesh/Box]. */
+  int sd_nk;
+  double sd_kmin, sd_kmax;
 } mgp_params;
 
 typedef struct mgp_ctx mgp_ctx;
@@ -170,8 +177,27 @@ int mgp_get_displacements(mgp_ctx *ctx, double A);
  * preceding mgp_get_displacements at the same A. */
 int mgp_kick_drift(mgp_ctx *ctx, double AI, double AF, double A, double AFF, int do_drift);
 
-/* One KDK step (main.c:410-602 body for a non-output step). */
+/* One KDK step (main.c:410-602 body for a non-output step); with
+ * scale-dependent growth it also assigns that step's ddDddy and deltaD
+ * fields (main.c:487-503). */
 int mgp_step(mgp_ctx *ctx, double A, double AI, double AF, double AFF);
+
+/* Scale-dependent growth (contexts created with scaledependent = 1, the
+ * reference's SCALEDEPENDENT build): assign_displacment_field_to_particles
+ * (src/2LPT.c:1758-2005) with from_cdisp_store_to_ZA (src/2LPT.c:1539-1735)
+ * for `n` (1-3) field types at once, each for both LPT orders.  Field types
+ * as src/proto.h:155-158.  The context keeps one particle slot per role, as
+ * the reference's P[] members: D and ddDddy go to the slot the Kick reads
+ * (P.D/P.D2), deltaD to the one the Drift reads (P.dDdy/P.dD2dy), dDdy to a
+ * velocity slot for outputs and RSD (the reference puts it into P.dDdy and
+ * restores deltaD afterwards, src/main.c:1051-1053, compute_pofk.c:409-500),
+ * so two types of one slot in a call are MGP_EINVAL.  deltaD uses
+ * D(k, AFF) - D(k, A).  Requires Nmesh to be a multiple of Nsample. */
+#define MGP_FIELD_D 0
+#define MGP_FIELD_dDdy 1
+#define MGP_FIELD_ddDddy 2
+#define MGP_FIELD_deltaD 3
+int mgp_assign_displacement_fields(mgp_ctx *ctx, double A, double AFF, int n, const int *fieldtypes);
 
 /* Full time loop with outputs (main.c:394-611).  Writes snapshot files
  * (GADGET-1 when gadget != 0, else ASCII) and pofk_* files to OutputDir. */
@@ -215,6 +241,10 @@ double mgp_power_spectrum(mgp_ctx *ctx, double k);
  * mgp_growth, 7 the linear P(k) at x = k (h/Mpc); mgp_cosmo_coeff gives Sq
  * (kind 0) or Sphi (kind 1) for n triples (ai, af, aref). */
 int mgp_cosmo_eval(const mgp_params *p, int which, const double *x, int n, double *out);
+/* growth_*_scaledependent(k, a) (src/cosmo.c:987-1010) of a parameter set
+ * with scaledependent = 1, host only: which 0 D, 1 dD/dy, 2 d2D/dy2, 3 D2,
+ * 4 dD2/dy, 5 d2D2/dy2 at n pairs (k in h/Mpc, a), normalised at a = 1 per k. */
+int mgp_growth_scaledependent(const mgp_params *p, int which, const double *k, const double *a, int n, double *out);
 int mgp_cosmo_coeff(const mgp_params *p, int kind, const double *ai, const double *af, const double *aref, int n,
                     double *out);
 

@@ -34,7 +34,8 @@ extern "C" const char *mgp_last_error(void) { return g_err; }
   } while (0)
 
 // ----------------------------------------------------------------- timing
-static const char *k_timer_names[MGP_NTIMERS] = {"cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "step"};
+static const char *k_timer_names[MGP_NTIMERS] = {"cic",    "r2c",  "pofk",          "mg",         "forces",
+                                                   "c2r",    "interp_kick_drift", "step", "lpt_fields"};
 
 static void tstart(mgp_ctx *c, int t) {
   if (c->timing) cudaEventRecord(c->ev[t][0], c->stream);
@@ -226,7 +227,10 @@ static int validate(const mgp_params *p) {
   if (p->Nsample < 1 || p->Nsample > 2048) return mgp_set_error(MGP_EINVAL, "Nsample = %d out of range", p->Nsample);
   if (!(p->Box > 0)) return mgp_set_error(MGP_EINVAL, "Box must be positive");
   if (p->model < 0 || p->model > 4) return mgp_set_error(MGP_EINVAL, "unknown model %d", p->model);
-  if (p->scaledependent) return mgp_set_error(MGP_EINVAL, "SCALEDEPENDENT growth is not available in this build");
+  if (p->scaledependent && (p->Nmesh % p->Nsample != 0 || p->Nsample % 2))
+    return mgp_set_error(MGP_EINVAL,
+                         "scale-dependent growth needs an even Nsample that divides Nmesh (Nmesh = %d, Nsample = %d)",
+                         p->Nmesh, p->Nsample);
   if ((p->WhichSpectrum != 0) && (p->WhichTransfer != 0))
     return mgp_set_error(MGP_EINVAL, "can't run with both power spectrum and transfer function");
   if ((p->WhichSpectrum == 0) && (p->WhichTransfer == 0))
@@ -241,6 +245,7 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   cufftHandle plans[3] = {c->plan_r2c_oop, c->plan_r2c_ip, c->plan_c2r_1};
   for (int i = 0; i < 3; i++)
     if (plans[i]) cufftDestroy(plans[i]);
+  mgp_sd_free(c);
   void *bufs[] = {c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
                   c->fft_work, c->rk_bin, c->pk_thr, c->win1d, c->pk_block, c->pk_sum, c->rsd_block, c->rsd_sum};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
@@ -307,12 +312,15 @@ extern "C" int mgp_create(const mgp_params *p, int device, mgp_ctx **out) {
   const size_t pbytes = sizeof(float) * 3 * (size_t)c->np;
   TRYCUDA(cudaMalloc(&c->s, pbytes));
   TRYCUDA(cudaMalloc(&c->v, pbytes));
-  TRYCUDA(cudaMalloc(&c->D1, pbytes));
-  TRYCUDA(cudaMalloc(&c->D2, pbytes));
   TRYCUDA(cudaMemset(c->s, 0, pbytes));
   TRYCUDA(cudaMemset(c->v, 0, pbytes));
-  TRYCUDA(cudaMemset(c->D1, 0, pbytes));
-  TRYCUDA(cudaMemset(c->D2, 0, pbytes));
+  if (!p->scaledependent) {
+    // scale-dependent runs keep their LPT fields in the lattice slots instead
+    TRYCUDA(cudaMalloc(&c->D1, pbytes));
+    TRYCUDA(cudaMalloc(&c->D2, pbytes));
+    TRYCUDA(cudaMemset(c->D1, 0, pbytes));
+    TRYCUDA(cudaMemset(c->D2, 0, pbytes));
+  }
   TRYCUDA(cudaMalloc(&c->dstate, sizeof(mgp_dstate)));
   TRYCUDA(cudaMemset(c->dstate, 0, sizeof(mgp_dstate)));
   c->max_blocks = mgp_ikd_blocks(c->np) > 4096 ? mgp_ikd_blocks(c->np) : 4096;
@@ -324,6 +332,7 @@ extern "C" int mgp_create(const mgp_params *p, int device, mgp_ctx **out) {
   if (needs_mg1(p)) TRYCUDA(cudaMalloc(&c->mg1, gbytes));
   TRY(make_plans(c));
   TRY(setup_pofk(c));
+  if (p->scaledependent) TRY(mgp_sd_alloc(c));
 #undef TRYCUDA
 #undef TRY
   *out = c;
@@ -353,22 +362,22 @@ extern "C" int mgp_displacement_fields(mgp_ctx *c) {
       for (int j = 0; j < i + 1; j++) seeds[(size_t)(N - 1 - j) * N + (N - 1 - i)] = draw();
     }
   }
+  // amplitude per integer |k|^2 (k in h/Mpc = 2 pi/Box sqrt(RK)), with the
   // P(k) rescaling for MG runs whose input spectrum is LCDM (2LPT.c:323-327,
-  // 395-407); scale-independent growth, so it is one number.
-  double rescale = 1.0;
+  // 395-407): mg_pofk_ratio(k, 1), per k when the growth is scale dependent
+  const int rkmax = 3 * h * h;
+  std::vector<double> amp(rkmax + 1), kk(rkmax + 1), ratio(rkmax + 1, 1.0);
+  for (int rk = 0; rk <= rkmax; rk++) kk[rk] = 2.0 * M_PI / box * sqrt((double)rk);
+  double s8fac = 1.0;
   if (c->p.modified_gravity_active && c->p.input_pofk_is_for_lcdm) {
-    rescale *= mgp_cosmo_pofk_ratio(&c->cosmo, 1.0);
+    mgp_cosmo_pofk_ratio_many(&c->cosmo, 1.0, rkmax, kk.data() + 1, ratio.data() + 1);
     if (!c->p.input_sigma8_is_for_lcdm) {
       double e = mgp_cosmo_sigma8_enh(&c->cosmo, 1.0);
-      rescale /= e * e;
+      s8fac = 1.0 / (e * e);
     }
   }
-  // amplitude per integer |k|^2 (k in h/Mpc = 2 pi/Box sqrt(RK))
-  const int rkmax = 3 * h * h;
-  std::vector<double> amp(rkmax + 1);
   for (int rk = 0; rk <= rkmax; rk++) {
-    double k = 2.0 * M_PI / box * sqrt((double)rk);
-    double pk = rk == 0 ? 0.0 : mgp_cosmo_power(&c->cosmo, k) * rescale;
+    double pk = rk == 0 ? 0.0 : mgp_cosmo_power(&c->cosmo, kk[rk]) * ratio[rk] * s8fac;
     amp[rk] = pow(box, -1.5) * sqrt(pk);
   }
   // cube cut of 2LPT.c:383-386 with the reference's double expression
@@ -424,6 +433,19 @@ extern "C" int mgp_displacement_fields(mgp_ctx *c) {
   for (int g = 3; g < 6; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
   CK(mgp_launch_ic_source(g6, gf, N, c->g.P, c->stream));
   CKF(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)(g6 + 3 * gf), (cufftComplex *)(g6 + 3 * gf)));
+  if (c->sd) {
+    // SCALEDEPENDENT: keep delta(k) and the source (2LPT.c:1336-1344), then
+    // x = q + D + D2 and v = dDdy + dD2dy (or 0) at a_i (main.c:244-307)
+    const double Ai = 1.0 / (1.0 + c->p.Init_Redshift);
+    const int types[2] = {MGP_FIELD_D, MGP_FIELD_dDdy};
+    CK(mgp_sd_store(c, c->dk, g6 + 3 * gf));
+    CK(mgp_sd_fields(c, Ai, Ai, 2, types));
+    CK(mgp_sd_init_particles(c));
+    CKC(cudaMemsetAsync(c->dstate, 0, sizeof(mgp_dstate), c->stream));
+    CKC(cudaStreamSynchronize(c->stream));
+    c->have_density = c->have_forces = 0;
+    goto cleanup;
+  }
   CK(mgp_launch_ic_disp(c->dk, g6 + 3 * gf, g6, gf, N, box, c->stream));
   for (int g = 0; g < 3; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
   for (int g = 3; g < 6; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
@@ -571,27 +593,52 @@ static void kd_args(mgp_ctx *c, double AI, double AF, double A, double AFF, int 
   a->scale = (float)(c->g.N / c->p.Box);
   a->inv_scale = (float)(c->p.Box / c->g.N);
   a->kick_disp = (float)(-1.5 * om * dda);
-  a->kick_d1 = (float)(-cola * mgp_cosmo_growth(cs, 2, A) / A * dda);
-  a->kick_d2 = (float)(-cola * mgp_cosmo_growth(cs, 5, A) / A * dda);
   a->dda_omega = 1.5 * om * dda;
   a->do_drift = do_drift;
+  if (c->sd) {
+    // scale-dependent Kick/Drift (main.c:703-719, 758-770): D1 is the slot of
+    // P.D + P.D2 (= the ddDddy fields), D2 the slot of P.dDdy + P.dD2dy
+    // (= the deltaD fields), both already multiplied by their growth factors
+    a->kick_d1 = (float)(-cola / A * dda);
+    a->kick_d2 = 0.0f;
+    a->lpt_stride = c->sd_grid;
+    a->lpt_pitch = c->sd_pitch;
+  } else {
+    a->kick_d1 = (float)(-cola * mgp_cosmo_growth(cs, 2, A) / A * dda);
+    a->kick_d2 = (float)(-cola * mgp_cosmo_growth(cs, 5, A) / A * dda);
+    a->lpt_stride = c->np;
+    a->lpt_pitch = c->Ns;
+  }
   if (do_drift) {
     double dyyy = mgp_cosmo_Sq(cs, A, AFF, AF);
     a->dyyy = (float)dyyy;
     a->dyyy_d = dyyy;
-    a->dD1 = (float)(cola * (mgp_cosmo_growth(cs, 0, AFF) - mgp_cosmo_growth(cs, 0, A)));
-    a->dD2 = (float)(cola * (mgp_cosmo_growth(cs, 3, AFF) - mgp_cosmo_growth(cs, 3, A)));
+    if (c->sd) {
+      a->dD1 = 0.0f;
+      a->dD2 = (float)cola;
+    } else {
+      a->dD1 = (float)(cola * (mgp_cosmo_growth(cs, 0, AFF) - mgp_cosmo_growth(cs, 0, A)));
+      a->dD2 = (float)(cola * (mgp_cosmo_growth(cs, 3, AFF) - mgp_cosmo_growth(cs, 3, A)));
+    }
   }
 }
 
 extern "C" int mgp_kick_drift(mgp_ctx *c, double AI, double AF, double A, double AFF, int do_drift) {
   RET_IF(require_particles(c));
   if (!c->have_forces) return mgp_set_error(MGP_ESTATE, "mgp_kick_drift before mgp_get_displacements");
+  if (c->sd) {
+    if (c->sd_kind[0] != MGP_FIELD_ddDddy || c->sd_a[0] != A)
+      return mgp_set_error(MGP_ESTATE, "scale-dependent kick at a = %g needs the ddDddy fields at that a "
+                                       "(mgp_assign_displacement_fields)", A);
+    if (do_drift && (c->sd_kind[1] != MGP_FIELD_deltaD || c->sd_a[1] != A || c->sd_aff[1] != AFF))
+      return mgp_set_error(MGP_ESTATE, "scale-dependent drift %g -> %g needs the deltaD fields of that step", A, AFF);
+  }
   mgp_kd_args a;
   kd_args(c, AI, AF, A, AFF, do_drift, &a);
   int nblk = mgp_ikd_blocks(c->np);
+  const float *D1 = c->sd ? c->sd_slot[0] : c->D1, *D2 = c->sd ? c->sd_slot[1] : c->D2;
   tstart(c, T_IKD);
-  RET_IF(mgp_launch_ikd(c->frc, c->g.nreal, c->g.N, c->g.P, c->Ns, c->np, c->s, c->v, c->D1, c->D2, c->dstate,
+  RET_IF(mgp_launch_ikd(c->frc, c->g.nreal, c->g.N, c->g.P, c->Ns, c->np, c->s, c->v, D1, D2, c->dstate,
                         c->partials, nblk, &a, c->stream));
   tstop(c, T_IKD);
   if (do_drift) c->have_density = 0;
@@ -602,6 +649,13 @@ extern "C" int mgp_step(mgp_ctx *c, double A, double AI, double AF, double AFF) 
   RET_IF(require_particles(c));
   tstart(c, T_MISC);
   RET_IF(mgp_get_displacements(c, A));
+  if (c->sd) {
+    // main.c:487-503: [deltaD] and [ddDddy] for this step
+    const int types[2] = {MGP_FIELD_ddDddy, MGP_FIELD_deltaD};
+    tstart(c, T_SD);
+    RET_IF(mgp_sd_fields(c, A, AFF, 2, types));
+    tstop(c, T_SD);
+  }
   RET_IF(mgp_kick_drift(c, AI, AF, A, AFF, 1));
   tstop(c, T_MISC);
   return MGP_OK;
@@ -651,15 +705,31 @@ extern "C" int mgp_pofk_rsd(mgp_ctx *c, double A, int cap, int *nbins, double *k
   const double hub = 3.2407789e-18 * (p->UnitLength_in_cm / p->UnitVelocity_in_cm_per_s);
   const double vnorm = (hub / A) / (100.0 * A * mgp_hubble(&c->cosmo, A)) * (double)N / p->Box;
   const double cola = p->UseCOLA ? 1.0 : 0.0;
-  const float g1 = (float)(cola * mgp_cosmo_growth(&c->cosmo, 1, A)), g2 = (float)(cola * mgp_cosmo_growth(&c->cosmo, 4, A));
+  float g1 = (float)(cola * mgp_cosmo_growth(&c->cosmo, 1, A)), g2 = (float)(cola * mgp_cosmo_growth(&c->cosmo, 4, A));
+  const float *L1 = c->D1, *L2 = c->D2;
+  long long lstride = c->np;
+  int lpitch = c->Ns;
+  if (c->sd) {
+    // V = Vel + dDdy + dD2dy with the scale-dependent fields at A
+    // (compute_pofk.c:323-325, 409-429)
+    if (c->sd_kind[2] != MGP_FIELD_dDdy || c->sd_a[2] != A) {
+      const int t = MGP_FIELD_dDdy;
+      RET_IF(mgp_sd_fields(c, A, A, 1, &t));
+    }
+    L1 = L2 = c->sd_slot[2];
+    g1 = (float)cola;
+    g2 = 0.0f;
+    lstride = c->sd_grid;
+    lpitch = c->sd_pitch;
+  }
   const double wpar = pow((double)N / (double)c->Ns, 3);
   float *dens = c->frc, *dkr = c->frc + c->g.nreal;
   std::vector<double> sums(3 * (size_t)nb), res[2][3];
   const double norm = pow(p->Box, 3) / pow((double)N, 6), shot = c->pk_sub ? pow(p->Box / (double)c->Ns, 3) : 0.0;
   for (int ax = 0; ax < 2; ax++) {
     RET_IF(mgp_launch_fill(dens, c->g.nreal, -1.0f, c->stream));
-    RET_IF(mgp_launch_cic_rsd(c->s, c->v, c->D1, c->D2, c->dstate, c->np, c->Ns, N, p->Box, (float)wpar, ax + 1,
-                              (float)vnorm, g1, g2, dens, c->g.P, c->stream));
+    RET_IF(mgp_launch_cic_rsd(c->s, c->v, L1, L2, lstride, lpitch, c->dstate, c->np, c->Ns, N, p->Box, (float)wpar,
+                              ax + 1, (float)vnorm, g1, g2, dens, c->g.P, c->stream));
     MGP_CUFFT(cufftExecR2C(c->plan_r2c_oop, (cufftReal *)dens, (cufftComplex *)dkr));
     RET_IF(mgp_launch_pofk_mu(dkr, N, c->rk_bin, c->win1d, nb, c->rsd_block, c->pk_blocks, c->rsd_sum, c->stream));
     MGP_CUDA(cudaMemcpyAsync(sums.data(), c->rsd_sum, sizeof(double) * 3 * nb, cudaMemcpyDeviceToHost, c->stream));
@@ -710,14 +780,22 @@ extern "C" int mgp_get_particles(mgp_ctx *c, float *pos, float *vel, float *D1, 
     if (vel) MGP_CUDA(cudaMemcpyAsync(vel, dvel, bytes, cudaMemcpyDeviceToHost, c->stream));
   }
   MGP_CUDA(cudaStreamSynchronize(c->stream));
-  // D1/D2 SoA -> AoS on the host
-  const float *srcs[2] = {c->D1, c->D2};
+  // D1/D2 SoA -> AoS on the host; with scale-dependent growth the two slots
+  // the kick and the drift read (lattice rows of pitch Ps)
+  const float *srcs[2] = {c->sd ? c->sd_slot[0] : c->D1, c->sd ? c->sd_slot[1] : c->D2};
   float *dsts[2] = {D1, D2};
   std::vector<float> h;
   for (int q = 0; q < 2; q++) {
     if (!dsts[q]) continue;
     h.resize(3 * np);
-    MGP_CUDA(cudaMemcpy(h.data(), srcs[q], bytes, cudaMemcpyDeviceToHost));
+    if (c->sd) {
+      for (int a = 0; a < 3; a++)
+        MGP_CUDA(cudaMemcpy2D(h.data() + a * np, sizeof(float) * c->Ns, srcs[q] + a * c->sd_grid,
+                              sizeof(float) * c->sd_pitch, sizeof(float) * c->Ns, (size_t)c->Ns * c->Ns,
+                              cudaMemcpyDeviceToHost));
+    } else {
+      MGP_CUDA(cudaMemcpy(h.data(), srcs[q], bytes, cudaMemcpyDeviceToHost));
+    }
     for (size_t i = 0; i < np; i++)
       for (int a = 0; a < 3; a++) dsts[q][3 * i + a] = h[a * np + i];
   }
@@ -738,7 +816,9 @@ extern "C" int mgp_set_particles(mgp_ctx *c, const float *pos, const float *vel,
     // absolute state: offsets restart from zero
     MGP_CUDA(cudaMemsetAsync(c->dstate, 0, sizeof(mgp_dstate), c->stream));
   }
-  const float *srcs[2] = {D1, D2};
+  // with scale-dependent growth the LPT fields are recomputed from the stored
+  // delta(k) before every use, so D1/D2 are not read
+  const float *srcs[2] = {c->sd ? NULL : D1, c->sd ? NULL : D2};
   float *dsts[2] = {c->D1, c->D2};
   for (int q = 0; q < 2; q++) {
     if (!srcs[q]) continue;

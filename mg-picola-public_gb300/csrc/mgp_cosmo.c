@@ -111,6 +111,107 @@ double mgp_factor_2lpt(const mgp_cosmo *c, double a) {
   return 1.0;
 }
 
+/* dm^2/da / H0^2 (user_defined_functions.h:527-560) */
+double mgp_dmass2_of_ada(const mgp_cosmo *c, double a) {
+  const double om = c->p.Omega;
+  if (c->p.model == MGP_MODEL_FOFR) {
+    double a3 = a * a * a, fac = om / a3 + 4.0 * (1.0 - om), fac0 = om + 4.0 * (1.0 - om), n = c->p.nfofr;
+    double m2 = fac0 * (n + 2.0) * pow(fac / fac0, n + 1.0) / ((1.0 + n) * c->p.fofr0 * fac0);
+    return m2 * (-3.0 * om / a3 / a);
+  }
+  if (c->p.model == MGP_MODEL_MBETA) {
+    if (a > c->p.assb_symm) {
+      double r = 2998.0 / c->p.range_symm, q = c->p.assb_symm / a;
+      return 0.5 * r * r * (3.0 * q * q * q / a);
+    }
+    return 0.0;
+  }
+  return 0.0;
+}
+
+/* The a-dependent factors of GeffoverG(a, k) and second_order_kernel(k, k1,
+ * k2, cos theta, a) (user_defined_functions.h:618-652, 848-904), split so that
+ * the scale-dependent growth ODE evaluates them once per a for all k. */
+typedef struct {
+  double H, alpha, beta0;  /* H/H0, 2 + a H'/H, 1.5 Omega / (a^3 H^2) */
+  double geff_const;       /* mu for k-independent models */
+  int kdep;                /* mu(k) = 1 + mu_b k2 / (k2 + mu_m) with k2 = (k c/H0)^2 */
+  double mu_b, mu_m;
+  int g2kind;              /* 0 none, 1 f(R), 2 DGP, 3 m(a)/beta(a) */
+  double g2_pref, g2_pi0;  /* f(R): prefactor and pi(k) = (k c/(H0 a))^2 + pi0; MBETA: pi0 = m2 */
+  double inv_a2;           /* (c/H0 / a)^2 multiplier of k^2 in pi(k) */
+} mgp_sd_apart;
+
+static void sd_apart(const mgp_cosmo *c, double a, mgp_sd_apart *o) {
+  const double om = c->p.Omega, a3 = a * a * a;
+  memset(o, 0, sizeof(*o));
+  o->H = mgp_hubble(c, a);
+  o->alpha = 2.0 + a * mgp_dhubbleda(c, a) / o->H;
+  o->beta0 = 1.5 * om / (a3 * o->H * o->H);
+  o->geff_const = 1.0;
+  o->inv_a2 = (INVERSE_H0_MPCH / a) * (INVERSE_H0_MPCH / a);
+  if (!c->p.modified_gravity_active || c->p.use_lcdm_growth_factors) return;
+  switch (c->p.model) {
+    case MGP_MODEL_FOFR:
+    case MGP_MODEL_MBETA: {
+      double b = mgp_beta_of_a(c, a);
+      o->kdep = 1;
+      o->mu_b = 2.0 * b * b;
+      o->mu_m = a * a * mgp_mass2_of_a(c, a);
+      if (c->p.model == MGP_MODEL_FOFR) {
+        double fac = om / a3 + 4.0 * (1.0 - om), fac0 = om + 4.0 * (1.0 - om), n = c->p.nfofr;
+        double cH = INVERSE_H0_MPCH / (a * o->H);
+        o->g2kind = 1;
+        o->g2_pref = -(3.0 * (n + 2.0) / (12.0 * (1.0 + n) * (1.0 + n))) * cH * cH * (om / a3) * (om / a3) * fac0 *
+                     pow(fac / fac0, 2.0 * n + 3.0) / (c->p.fofr0 * c->p.fofr0);
+        o->g2_pi0 = fac0 * pow(fac / fac0, n + 2.0) / (1.0 + n) / c->p.fofr0;
+      } else {
+        double m2 = mgp_mass2_of_a(c, a);
+        o->g2kind = 3;
+        o->g2_pi0 = m2;
+        o->g2_pref = (mgp_dmass2_of_ada(c, a) / m2) * b * b * om / (2.0 * a * a) / (o->H * o->H);
+      }
+      break;
+    }
+    case MGP_MODEL_DGP: {
+      double bd = mgp_beta_dgp(c, a), r = c->p.rcH0_DGP / o->H;
+      o->geff_const = mgp_geff(c, a, 1.0);
+      o->g2kind = 2;
+      o->g2_pref = -1.0 / 6.0 / (bd * bd * bd) * r * r * (om / a3) * (om / a3);
+      break;
+    }
+    default: o->geff_const = mgp_geff(c, a, 1.0); break;
+  }
+}
+
+static double sd_mu(const mgp_sd_apart *o, double k) {
+  if (!o->kdep) return o->geff_const;
+  double k2 = (k * INVERSE_H0_MPCH) * (k * INVERSE_H0_MPCH);
+  if (k2 == 0) return 1.0;
+  return 1.0 + o->mu_b * k2 / (k2 + o->mu_m);
+}
+
+/* second_order_kernel(k, k/sqrt2, k/sqrt2, 0, a): the cos(theta) term of the
+ * reference vanishes at cos(theta) = 0. */
+static double sd_gamma2(const mgp_sd_apart *o, double k) {
+  double k2 = k * k * o->inv_a2, k12 = 0.5 * k2;
+  switch (o->g2kind) {
+    case 1: return o->g2_pref * k * k / ((k2 + o->g2_pi0) * (k12 + o->g2_pi0) * (k12 + o->g2_pi0));
+    case 2: return o->g2_pref;
+    case 3: {
+      double m2 = o->g2_pi0, p1 = k12 + m2;
+      return o->g2_pref * (m2 / p1) * (m2 / p1) * (1.0 - m2 / (k2 + m2));
+    }
+    default: return 0.0;
+  }
+}
+
+/* modfac of ode_growth_D in the SCALEDEPENDENT build (src/cosmo.c:215-219) */
+static double sd_modfac(const mgp_sd_apart *o, double a, double k, double mu, double omega) {
+  double a2H = a * a * o->H;
+  return 1.0 + 2.0 * a2H * a2H * sd_gamma2(o, k) / (1.5 * omega * a * mu);
+}
+
 double mgp_phicrit(const mgp_cosmo *c, double a) {
   const double om = c->p.Omega;
   if (c->p.model == MGP_MODEL_MBETA) return c->have_phia ? spline_eval(&c->phia, log(a)) : 0.0;
@@ -214,7 +315,16 @@ static void growth_rhs(const ode_par *op, double x, const double *y, double *f) 
   double mu = op->lcdm ? 1.0 : mgp_geff(c, a, 1e-3);
   double beta = 1.5 * c->p.Omega * mu / (a * a * a * H * H);
   double alpha = 2.0 + a * dH / H;
-  double mod = op->lcdm ? 1.0 : mgp_factor_2lpt(c, a);
+  double mod = 1.0;
+  if (!op->lcdm) {
+    if (c->p.scaledependent) {
+      mgp_sd_apart o;
+      sd_apart(c, a, &o);
+      mod = sd_modfac(&o, a, 1e-3, mu, c->p.Omega);
+    } else {
+      mod = mgp_factor_2lpt(c, a);
+    }
+  }
   f[0] = y[1];
   f[1] = -alpha * y[1] + beta * y[0];
   f[2] = y[3];
@@ -313,6 +423,237 @@ static int solve_growth(mgp_cosmo *c, char *err, size_t errlen) {
   for (int i = 0; i < 12; i++) spline_init(sp[i], x, v[i], npts);
   free(buf);
   return MGP_OK;
+}
+
+/* ------------------------------------------- scale-dependent growth tables */
+/* Bicubic interpolation on the (ln a, ln k) grid as GSL's
+ * gsl_interp2d_bicubic (src/wrappers.c:101-136): node derivatives from
+ * natural cubic splines along the grid lines (z_x along x, z_y along y,
+ * z_xy = d/dx of z_y), tensor-product cubic Hermite cells. */
+static void node_derivs(const double *x, const double *y, long ys, int n, double *d, long ds, double *M, double *u) {
+  M[0] = u[0] = 0.0;
+  for (int i = 1; i < n - 1; i++) {
+    double sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]), p = sig * M[i - 1] + 2.0;
+    M[i] = (sig - 1.0) / p;
+    double r = (y[(i + 1) * ys] - y[i * ys]) / (x[i + 1] - x[i]) - (y[i * ys] - y[(i - 1) * ys]) / (x[i] - x[i - 1]);
+    u[i] = (6.0 * r / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / p;
+  }
+  M[n - 1] = 0.0;
+  for (int k = n - 2; k >= 0; k--) M[k] = M[k] * M[k + 1] + u[k];
+  for (int i = 0; i < n - 1; i++) {
+    double h = x[i + 1] - x[i];
+    d[i * ds] = (y[(i + 1) * ys] - y[i * ys]) / h - h * (2.0 * M[i] + M[i + 1]) / 6.0;
+  }
+  double h = x[n - 1] - x[n - 2];
+  d[(n - 1) * ds] = (y[(n - 1) * ys] - y[(n - 2) * ys]) / h + h * (M[n - 2] + 2.0 * M[n - 1]) / 6.0;
+}
+
+static void bicubic_init(mgp_bicubic *b, const double *x, const double *y, double *z, int nx, int ny) {
+  size_t nn = (size_t)nx * ny;
+  b->nx = nx;
+  b->ny = ny;
+  b->x = (double *)malloc(sizeof(double) * nx);
+  b->y = (double *)malloc(sizeof(double) * ny);
+  memcpy(b->x, x, sizeof(double) * nx);
+  memcpy(b->y, y, sizeof(double) * ny);
+  b->z = z;
+  b->zx = (double *)malloc(sizeof(double) * nn);
+  b->zy = (double *)malloc(sizeof(double) * nn);
+  b->zxy = (double *)malloc(sizeof(double) * nn);
+  int m = nx > ny ? nx : ny;
+  double *M = (double *)malloc(sizeof(double) * 2 * m);
+  for (int j = 0; j < ny; j++) node_derivs(b->x, z + (size_t)j * nx, 1, nx, b->zx + (size_t)j * nx, 1, M, M + m);
+  for (int i = 0; i < nx; i++) node_derivs(b->y, z + i, nx, ny, b->zy + i, nx, M, M + m);
+  for (int j = 0; j < ny; j++)
+    node_derivs(b->x, b->zy + (size_t)j * nx, 1, nx, b->zxy + (size_t)j * nx, 1, M, M + m);
+  free(M);
+}
+
+static void bicubic_free(mgp_bicubic *b) {
+  free(b->x); free(b->y); free(b->z); free(b->zx); free(b->zy); free(b->zxy);
+  memset(b, 0, sizeof(*b));
+}
+
+static int grid_cell(const double *x, int n, double v) {
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    int m = (lo + hi) / 2;
+    if (x[m] > v) hi = m;
+    else lo = m;
+  }
+  return lo;
+}
+
+/* value and d/dy of the bicubic along x = xv (clamped) at every y node: the
+ * cubic Hermite in x of z and z_y (exact restriction of the bicubic) */
+static void bicubic_column(const mgp_bicubic *b, double xv, double *val, double *dval) {
+  if (xv < b->x[0]) xv = b->x[0];
+  if (xv > b->x[b->nx - 1]) xv = b->x[b->nx - 1];
+  int i = grid_cell(b->x, b->nx, xv);
+  double dx = b->x[i + 1] - b->x[i], t = (xv - b->x[i]) / dx;
+  double h0 = (1 + 2 * t) * (1 - t) * (1 - t), h1 = t * t * (3 - 2 * t), g0 = t * (1 - t) * (1 - t) * dx,
+         g1 = t * t * (t - 1) * dx;
+  for (int j = 0; j < b->ny; j++) {
+    size_t c0 = (size_t)j * b->nx + i, c1 = c0 + 1;
+    val[j] = h0 * b->z[c0] + h1 * b->z[c1] + g0 * b->zx[c0] + g1 * b->zx[c1];
+    dval[j] = h0 * b->zy[c0] + h1 * b->zy[c1] + g0 * b->zxy[c0] + g1 * b->zxy[c1];
+  }
+}
+
+/* cubic Hermite in y of a column (val, dval on the y nodes), y clamped */
+static double column_eval(const mgp_bicubic *b, const double *val, const double *dval, double yv) {
+  if (yv < b->y[0]) yv = b->y[0];
+  if (yv > b->y[b->ny - 1]) yv = b->y[b->ny - 1];
+  int j = grid_cell(b->y, b->ny, yv);
+  double dy = b->y[j + 1] - b->y[j], u = (yv - b->y[j]) / dy;
+  return (1 + 2 * u) * (1 - u) * (1 - u) * val[j] + u * u * (3 - 2 * u) * val[j + 1] +
+         u * (1 - u) * (1 - u) * dy * dval[j] + u * u * (u - 1) * dy * dval[j + 1];
+}
+
+/* Dormand-Prince 5(4) over all k at once with one shared step size (the
+ * a-dependent parts of the right-hand side are evaluated once per stage). */
+typedef struct {
+  const mgp_cosmo *c;
+  int nk;
+  const double *k;
+} sd_ode;
+
+static void sd_rhs(const sd_ode *o, double x, const double *y, double *f) {
+  double a = exp(x), om = o->c->p.Omega;
+  mgp_sd_apart ap;
+  sd_apart(o->c, a, &ap);
+  for (int q = 0; q < o->nk; q++) {
+    const double *Y = y + 4 * q;
+    double *F = f + 4 * q;
+    double mu = sd_mu(&ap, o->k[q]);
+    double beta = ap.beta0 * mu, mod = sd_modfac(&ap, a, o->k[q], mu, om);
+    F[0] = Y[1];
+    F[1] = -ap.alpha * Y[1] + beta * Y[0];
+    F[2] = Y[3];
+    F[3] = -ap.alpha * Y[3] + beta * (Y[2] - mod * Y[0] * Y[0]);
+  }
+}
+
+static int sd_dp45(const sd_ode *o, double x0, double x1, double *y, double *hguess, double *work) {
+  const int n = 4 * o->nk;
+  double *K[7], *yt = work + 7 * n, *y5 = work + 8 * n;
+  for (int s = 0; s < 7; s++) K[s] = work + s * n;
+  double x = x0, h = *hguess;
+  int steps = 0;
+  while (x < x1) {
+    if (x + h > x1) h = x1 - x;
+    for (int s = 0; s < 7; s++) {
+      for (int i = 0; i < n; i++) {
+        double acc = y[i];
+        for (int j = 0; j < s; j++) acc += h * DP_A[s][j] * K[j][i];
+        yt[i] = acc;
+      }
+      sd_rhs(o, x + DP_C[s] * h, yt, K[s]);
+    }
+    double err = 0.0;
+    for (int i = 0; i < n; i++) {
+      double s5 = y[i], s4 = y[i];
+      for (int s = 0; s < 7; s++) {
+        s5 += h * DP_B5[s] * K[s][i];
+        s4 += h * DP_B4[s] * K[s][i];
+      }
+      y5[i] = s5;
+      double sc = 1e-10 * (fabs(y[i]) > fabs(s5) ? fabs(y[i]) : fabs(s5)) + 1e-14;
+      double e = fabs(s5 - s4) / sc;
+      if (e > err) err = e;
+    }
+    if (err <= 1.0) {
+      x += h;
+      memcpy(y, y5, sizeof(double) * n);
+    }
+    double fac = err > 0 ? 0.9 * pow(err, -0.2) : 5.0;
+    if (fac > 5.0) fac = 5.0;
+    if (fac < 0.2) fac = 0.2;
+    h *= fac;
+    if (++steps > 1000000 || !(h > 1e-14)) return -1;
+  }
+  *hguess = h;
+  return 0;
+}
+
+/* calculate_scale_dependent_growth_factor (src/cosmo.c:798-981) */
+static int solve_growth_sd(mgp_cosmo *c, char *err, size_t errlen) {
+  const int npts = 1000;
+  const int nk = c->p.sd_nk > 0 ? c->p.sd_nk : 1000;
+  const double kmin = c->p.sd_kmin > 0 ? c->p.sd_kmin : 2.0 * M_PI / c->p.Box * 0.5;
+  const double kmax = c->p.sd_kmax > 0 ? c->p.sd_kmax : 2.0 * M_PI / c->p.Box * c->p.Nmesh * sqrt(3.0) * 2.0;
+  if (nk < 4 || !(kmax > kmin) || !(kmin > 0)) {
+    snprintf(err, errlen, "scale-dependent k grid: nk = %d, kmin = %g, kmax = %g", nk, kmin, kmax);
+    return MGP_EPARAM;
+  }
+  double zini = c->p.Init_Redshift > 200.0 ? c->p.Init_Redshift : 200.0;
+  double xini = log(1.0 / (1.0 + zini)), xend = log(1.0 / (1.0 - 0.5));
+  double *x = (double *)malloc(sizeof(double) * npts), *logk = (double *)malloc(sizeof(double) * nk);
+  double *kk = (double *)malloc(sizeof(double) * nk);
+  double *y = (double *)malloc(sizeof(double) * 4 * nk), *work = (double *)malloc(sizeof(double) * 9 * 4 * nk);
+  double *T[6];
+  for (int f = 0; f < 6; f++) T[f] = (double *)malloc(sizeof(double) * (size_t)npts * nk);
+  for (int i = 0; i < npts; i++) x[i] = xini + (xend - xini) * i / (double)(npts - 1);
+  for (int q = 0; q < nk; q++) {
+    logk[q] = log(kmin) + log(kmax / kmin) * q / (double)(nk - 1);
+    kk[q] = exp(logk[q]);
+    y[4 * q] = 1.0;
+    y[4 * q + 1] = 1.0;
+    y[4 * q + 2] = -3.0 / 7.0;
+    y[4 * q + 3] = -6.0 / 7.0;
+  }
+  sd_ode o = {c, nk, kk};
+  double h = 1e-4;
+  int rc = MGP_OK;
+  for (int i = 0; i < npts && rc == MGP_OK; i++) {
+    if (i > 0 && sd_dp45(&o, x[i - 1], x[i], y, &h, work)) {
+      snprintf(err, errlen, "scale-dependent growth ODE integration failed at x = %f", x[i]);
+      rc = MGP_ENUMERIC;
+      break;
+    }
+    double a = exp(x[i]), qa = Qfactor(c, a) / a, om = c->p.Omega;
+    mgp_sd_apart ap;
+    sd_apart(c, a, &ap);
+    for (int q = 0; q < nk; q++) {
+      const double *Y = y + 4 * q;
+      double mu = sd_mu(&ap, kk[q]);
+      size_t cc = (size_t)q * npts + i;
+      T[0][cc] = Y[0];
+      T[1][cc] = Y[1] * qa;
+      T[2][cc] = 1.5 * mu * om * a * Y[0];
+      T[3][cc] = Y[2];
+      T[4][cc] = Y[3] * qa;
+      T[5][cc] = 1.5 * mu * om * a * (Y[2] - Y[0] * Y[0]);
+    }
+  }
+  if (rc == MGP_OK) {
+    for (int f = 0; f < 6; f++) bicubic_init(&c->sd_tab[f], x, logk, T[f], npts, nk);
+    c->sd = 1;
+  } else {
+    for (int f = 0; f < 6; f++) free(T[f]);
+  }
+  free(x); free(logk); free(kk); free(y); free(work);
+  return rc;
+}
+
+int mgp_cosmo_sd_column(const mgp_cosmo *c, int which, double a, double *val, double *dval) {
+  if (!c->sd || which < 0 || which > 5) return MGP_ESTATE;
+  bicubic_column(&c->sd_tab[which], log(a), val, dval);
+  return MGP_OK;
+}
+
+/* growth_*_scaledependent (src/cosmo.c:987-1010): which 0-5 as
+ * D, dDdy, ddDddy, D2, dD2dy, ddD2ddy, normalised at a = 1 per k. */
+double mgp_cosmo_growth_sd(const mgp_cosmo *c, int which, double k, double a) {
+  if (!c->sd || which < 0 || which > 5) return NAN;
+  const mgp_bicubic *b = &c->sd_tab[which], *nb = &c->sd_tab[which < 3 ? 0 : 3];
+  int ny = b->ny;
+  double *col = (double *)malloc(sizeof(double) * 4 * ny);
+  bicubic_column(b, log(a), col, col + ny);
+  bicubic_column(nb, 0.0, col + 2 * ny, col + 3 * ny);
+  double r = column_eval(b, col, col + ny, log(k)) / column_eval(nb, col + 2 * ny, col + 3 * ny, log(k));
+  free(col);
+  return r;
 }
 
 double mgp_cosmo_growth(const mgp_cosmo *c, int which, double a) {
@@ -436,14 +777,65 @@ static int read_table(mgp_cosmo *c, const char *fname, int transfer, char *err, 
   return MGP_OK;
 }
 
-double mgp_cosmo_pofk_ratio(const mgp_cosmo *c, double a) {
+/* mg_pofk_ratio(k, a) (src/cosmo.c:688-706): (D/D_LCDM)^2 with the raw
+ * (unnormalised) tables; D(k, a) in the scale-dependent build. */
+double mgp_cosmo_pofk_ratio(const mgp_cosmo *c, double k, double a) {
   if (!c->p.modified_gravity_active) return 1.0;
-  double r = spline_eval(&c->D, log(a)) / spline_eval(&c->DL, log(a));
+  double D;
+  if (c->sd) {
+    const mgp_bicubic *b = &c->sd_tab[0];
+    double *col = (double *)malloc(sizeof(double) * 2 * b->ny);
+    bicubic_column(b, log(a), col, col + b->ny);
+    D = column_eval(b, col, col + b->ny, log(k));
+    free(col);
+  } else {
+    D = spline_eval(&c->D, log(a));
+  }
+  double r = D / spline_eval(&c->DL, log(a));
   return r * r;
 }
+void mgp_cosmo_pofk_ratio_many(const mgp_cosmo *c, double a, int n, const double *k, double *out) {
+  if (!c->p.modified_gravity_active) {
+    for (int i = 0; i < n; i++) out[i] = 1.0;
+    return;
+  }
+  double DL = spline_eval(&c->DL, log(a));
+  if (!c->sd) {
+    double r = spline_eval(&c->D, log(a)) / DL;
+    for (int i = 0; i < n; i++) out[i] = r * r;
+    return;
+  }
+  const mgp_bicubic *b = &c->sd_tab[0];
+  double *col = (double *)malloc(sizeof(double) * 2 * b->ny);
+  bicubic_column(b, log(a), col, col + b->ny);
+  for (int i = 0; i < n; i++) {
+    double r = column_eval(b, col, col + b->ny, log(k[i])) / DL;
+    out[i] = r * r;
+  }
+  free(col);
+}
+
+/* mg_sigma8_enhancement(a) (src/cosmo.c:713-756): the ratio of growth
+ * factors, or in the scale-dependent build the ratio of the sigma_8
+ * integrals over 1000 log-spaced k in [1e-3, 100] h/Mpc. */
 double mgp_cosmo_sigma8_enh(const mgp_cosmo *c, double a) {
   if (!c->p.modified_gravity_active) return 1.0;
-  return spline_eval(&c->D, log(a)) / spline_eval(&c->DL, log(a));
+  if (!c->sd) return spline_eval(&c->D, log(a)) / spline_eval(&c->DL, log(a));
+  const double kmin = 0.001, kmax = 100.0;
+  const int npts = 1000;
+  const mgp_bicubic *b = &c->sd_tab[0];
+  double *col = (double *)malloc(sizeof(double) * 2 * b->ny);
+  bicubic_column(b, log(a), col, col + b->ny);
+  double DL = spline_eval(&c->DL, log(a)), dlogk = log(kmax / kmin) / (double)(npts - 1), s = 0.0, sl = 0.0;
+  for (int i = 0; i < npts; i++) {
+    double k = exp(log(kmin) + log(kmax / kmin) * i / (double)(npts - 1)), kR8 = k * 8.0;
+    double w = 3.0 / (kR8 * kR8 * kR8) * (sin(kR8) - kR8 * cos(kR8));
+    double D = column_eval(b, col, col + b->ny, log(k)), pk = mgp_cosmo_power(c, k);
+    s += pk * w * w * D * D * k * k * k * dlogk / (2.0 * M_PI * M_PI);
+    sl += pk * w * w * DL * DL * k * k * k * dlogk / (2.0 * M_PI * M_PI);
+  }
+  free(col);
+  return sqrt(s) / sqrt(sl);
 }
 
 /* ------------------------------------------------ Brans-Dicke background */
@@ -606,7 +998,9 @@ int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen) 
    * (main.c:186-196), so the normalisation above uses the file's Omega/h */
   if (p->model == MGP_MODEL_BRANSDICKE && (rc = jbd_solve(c, err, errlen))) return rc;
   if (p->model == MGP_MODEL_MBETA && p->modified_gravity_active) phia_solve(c);
-  return solve_growth(c, err, errlen);
+  if ((rc = solve_growth(c, err, errlen))) return rc;
+  if (p->scaledependent) return solve_growth_sd(c, err, errlen);
+  return MGP_OK;
 }
 
 void mgp_cosmo_free(mgp_cosmo *c) {
@@ -617,6 +1011,9 @@ void mgp_cosmo_free(mgp_cosmo *c) {
                         &c->DL, &c->dDLdy, &c->ddDLddy, &c->D2L, &c->dD2Ldy, &c->ddD2Lddy};
   for (int i = 0; i < 12; i++)
     if (sp[i]->x) spline_free(sp[i]);
+  if (c->sd)
+    for (int f = 0; f < 6; f++) bicubic_free(&c->sd_tab[f]);
+  c->sd = 0;
   free(c->tab_logk);
   free(c->tab_logv);
   c->tab_logk = c->tab_logv = NULL;
@@ -634,6 +1031,21 @@ int mgp_cosmo_eval(const mgp_params *p, int which, const double *x, int n, doubl
     return mgp_set_error(rc, "%s", err);
   }
   for (int i = 0; i < n; i++) out[i] = which == 7 ? mgp_cosmo_power(&c, x[i]) : mgp_cosmo_growth(&c, which, x[i]);
+  mgp_cosmo_free(&c);
+  return MGP_OK;
+}
+
+int mgp_growth_scaledependent(const mgp_params *p, int which, const double *k, const double *a, int n, double *out) {
+  if (!p || !p->scaledependent) return mgp_set_error(MGP_EINVAL, "parameters without scaledependent = 1");
+  if (which < 0 || which > 5) return mgp_set_error(MGP_EINVAL, "which = %d out of range", which);
+  char err[512] = "";
+  mgp_cosmo c;
+  int rc = mgp_cosmo_init(&c, p, err, sizeof(err));
+  if (rc) {
+    mgp_cosmo_free(&c);
+    return mgp_set_error(rc, "%s", err);
+  }
+  for (int i = 0; i < n; i++) out[i] = mgp_cosmo_growth_sd(&c, which, k[i], a[i]);
   mgp_cosmo_free(&c);
   return MGP_OK;
 }

@@ -16,6 +16,12 @@ typedef struct {
   double *x, *y, *y2;
 } mgp_spline;
 
+/* bicubic table over (x, y), z[j * nx + i], with node derivatives */
+typedef struct {
+  int nx, ny;
+  double *x, *y, *z, *zx, *zy, *zxy;
+} mgp_bicubic;
+
 typedef struct mgp_cosmo {
   mgp_params p;
   /* growth splines over x = ln a (src/cosmo.c:54-95) */
@@ -27,6 +33,10 @@ typedef struct mgp_cosmo {
   /* m(a), beta(a) models: phi_crit(a) over ln a (src/cosmo.c:104-190) */
   int have_phia;
   mgp_spline phia;
+  /* scale-dependent growth (src/cosmo.c:798-1010): D, dDdy, ddDddy, D2,
+   * dD2dy, ddD2ddy over (ln a, ln k) */
+  int sd;
+  mgp_bicubic sd_tab[6];
   /* power spectrum */
   double norm;
   int ntab;
@@ -58,10 +68,17 @@ double mgp_cosmo_Sphi(const mgp_cosmo *c, double ai, double af, double aref);
 
 /* PowerSpec (src/power.c:373-394) in (Mpc/h)^3, k in h/Mpc */
 double mgp_cosmo_power(const mgp_cosmo *c, double k);
-/* mg_pofk_ratio(k, 1) and mg_sigma8_enhancement(1) for scale-independent
- * growth (src/cosmo.c:688-756) */
-double mgp_cosmo_pofk_ratio(const mgp_cosmo *c, double a);
+/* mg_pofk_ratio(k, a) and mg_sigma8_enhancement(a) (src/cosmo.c:688-756) */
+double mgp_cosmo_pofk_ratio(const mgp_cosmo *c, double k, double a);
+void mgp_cosmo_pofk_ratio_many(const mgp_cosmo *c, double a, int n, const double *k, double *out);
 double mgp_cosmo_sigma8_enh(const mgp_cosmo *c, double a);
+/* Scale-dependent growth: growth_*_scaledependent (src/cosmo.c:987-1010),
+ * which 0-5 = D, dDdy, ddDddy, D2, dD2dy, ddD2ddy, k in h/Mpc; and the
+ * table restricted to x = ln a (clamped): value and d/d ln k at the ln k
+ * nodes sd_tab[which].y. */
+double mgp_cosmo_growth_sd(const mgp_cosmo *c, int which, double k, double a);
+int mgp_cosmo_sd_column(const mgp_cosmo *c, int which, double a, double *val, double *dval);
+double mgp_dmass2_of_ada(const mgp_cosmo *c, double a);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,7 @@ typedef struct {
   double mean_v[3];    /* mean of the stored v after the last kick */
 } mgp_dstate;
 
-#define MGP_NTIMERS 8
+#define MGP_NTIMERS 9
 
 typedef struct mgp_grid_geom {
   int N, NH;
@@ -80,6 +80,27 @@ struct mgp_ctx {
   int have_density, have_forces;
   double last_density_a;
 
+  /* scale-dependent growth (SCALEDEPENDENT build).  The particles carry no
+   * D1/D2 arrays; the LPT fields live on the Lagrangian lattice as three
+   * padded real [Ns][Ns][Ps] grids per slot (Ps = 2(Ns/2+1)), which is the
+   * particle order with a row pitch of Ps:
+   *   slot 0 "D"     FIELD_D at the IC, FIELD_ddDddy in the loop (P.D + P.D2)
+   *   slot 1 "dDdy"  FIELD_deltaD (P.dDdy + P.dD2dy as Drift reads them)
+   *   slot 2 "vel"   FIELD_dDdy for outputs, RSD and the non-COLA IC velocity
+   * each the sum of the 1LPT and 2LPT fields (every reader adds them). */
+  int sd;
+  int sd_fold;              /* Nmesh / Nsample (alias count per axis) */
+  float *sd_dk[2];          /* delta(k), -source(k): complex [N][N][NH] */
+  float *sd_slot[3];        /* 3 components x sd_grid floats each */
+  long long sd_grid;        /* Ns*Ns*Ps floats */
+  int sd_pitch;             /* Ps */
+  int sd_kind[3];           /* field type held by each slot, -1 none */
+  double sd_a[3], sd_aff[3];
+  cufftHandle plan_c2r_s;   /* Ns^3 in-place C2R */
+  double *sd_cols;          /* device: growth-table columns for the current call */
+  float *sd_tab;            /* device: float4 per integer |k|^2 */
+  long long sd_nmax;        /* largest integer |k|^2 = 3 (N/2)^2 */
+
   /* timing */
   int timing;
   cudaEvent_t ev[MGP_NTIMERS][2];
@@ -88,7 +109,7 @@ struct mgp_ctx {
   long long launches;
 };
 
-enum { T_CIC = 0, T_R2C, T_POFK, T_MG, T_FORCES, T_C2R, T_IKD, T_MISC };
+enum { T_CIC = 0, T_R2C, T_POFK, T_MG, T_FORCES, T_C2R, T_IKD, T_MISC, T_SD };
 
 /* error plumbing (C linkage: also called from the C sources) */
 #ifdef __cplusplus
@@ -135,7 +156,26 @@ typedef struct {
   int do_drift;
   double dda_omega;   /* 1.5 * Omega * dda for the velocity offset */
   double dyyy_d;
+  /* layout of D1/D2: component c of particle (i, j, k) is at
+   * c * lpt_stride + (i*Ns + j) * lpt_pitch + k (Np and Ns for the particle
+   * arrays, the slot grid size and Ps for the scale-dependent slots) */
+  long long lpt_stride;
+  int lpt_pitch;
 } mgp_kd_args;
+
+extern long long g_kernel_launches;
+int mgp_blocks_for(long long n, int per_sm);
+
+/* scale-dependent growth (mgp_sd.cu) */
+int mgp_sd_alloc(mgp_ctx *c);
+void mgp_sd_free(mgp_ctx *c);
+/* keep delta(k) and the complex 2LPT source S(k) of the IC (stored as
+ * delta and -S, src/2LPT.c:301-309, 1336-1344) */
+int mgp_sd_store(mgp_ctx *c, const float *deltak, const float *source2k);
+/* fields of `types` (one per slot) at A (and AFF for deltaD) */
+int mgp_sd_fields(mgp_ctx *c, double A, double AFF, int n, const int *types);
+/* IC particle state from the D (slot 0) and dDdy (slot 2) fields */
+int mgp_sd_init_particles(mgp_ctx *c);
 
 int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st);
 int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box,
@@ -169,15 +209,15 @@ int mgp_launch_ic_grad6(const float *dk, float *out6, long long grid_floats, int
 int mgp_launch_ic_source(float *g6, long long grid_floats, int N, long long P, cudaStream_t st);
 int mgp_launch_ic_disp(const float *dk, const float *src, float *out6, long long grid_floats, int N, double box,
                        cudaStream_t st);
-int mgp_launch_cic_rsd(const float *s, const float *v, const float *D1, const float *D2, const mgp_dstate *st,
-                       long long np, int Ns, int N, double box, float wpar, int axis, float vnorm, float g1, float g2,
-                       float *rho, long long P, cudaStream_t stream);
+int mgp_launch_cic_rsd(const float *s, const float *v, const float *D1, const float *D2, long long lpt_stride,
+                       int lpt_pitch, const mgp_dstate *st, long long np, int Ns, int N, double box, float wpar,
+                       int axis, float vnorm, float g1, float g2, float *rho, long long P, cudaStream_t stream);
 int mgp_launch_pofk_mu(const float *dk, int N, const int *rk_bin, const float *win, int nbins, double *block_part,
                        int nblocks, double *sums, cudaStream_t st);
 int mgp_launch_aos_to_soa(const float *in, float *out, long long np, cudaStream_t st);
-int mgp_launch_output(const float *s, const float *v, const float *D1, const float *D2, const mgp_dstate *dst,
-                      long long np, int Ns, double box, double lengthfac, double vfac, double dDdy, double dD2dy,
-                      double cola, float *pos, float *vel, cudaStream_t st);
+int mgp_launch_output(const float *s, const float *v, const float *D1, const float *D2, long long lpt_stride,
+                      int lpt_pitch, const mgp_dstate *dst, long long np, int Ns, double box, double lengthfac,
+                      double vfac, double dDdy, double dD2dy, double cola, float *pos, float *vel, cudaStream_t st);
 int mgp_launch_ic_readout(const float *g6, long long grid_floats, int N, long long P, int Ns,
                           float *D1, float *D2, double *partials, int nblocks, cudaStream_t st);
 int mgp_launch_ic_finish(float *D1, float *D2, float *s, float *v, long long np, const double *partials,

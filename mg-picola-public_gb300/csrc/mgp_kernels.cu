@@ -17,7 +17,7 @@
 
 // Process-wide count of this library's own kernel launches (cuFFT not
 // included); read by mgp_launch_count.
-static long long g_kernel_launches = 0;
+long long g_kernel_launches = 0;
 long long mgp_kernel_launches(void) { return g_kernel_launches; }
 
 static int g_sm_count = 0;
@@ -38,6 +38,7 @@ static int blocks_for(long long n, int per_sm) {
   if (b < 1) b = 1;
   return (int)b;
 }
+int mgp_blocks_for(long long n, int per_sm) { return blocks_for(n, per_sm); }
 
 // -------------------------------------------------------------- helpers
 // Lattice coordinates of particle p (src/main.c:257-262 ordering).
@@ -475,10 +476,11 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
       disp[ax] = __ldg(F + o000) * w000 + __ldg(F + o001) * w001 + __ldg(F + o010) * w010 + __ldg(F + o011) * w011 +
                  __ldg(F + o100) * w100 + __ldg(F + o101) * w101 + __ldg(F + o110) * w110 + __ldg(F + o111) * w111;
     }
+    const long long od = ((long long)i * Ns + j) * a.lpt_pitch + k;
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
       long long o = ax * np + p;
-      float d1 = D1[o], d2 = D2[o];
+      float d1 = D1[ax * a.lpt_stride + od], d2 = D2[ax * a.lpt_stride + od];
       float vn = v[o] + a.kick_disp * disp[ax] + a.kick_d1 * d1 + a.kick_d2 * d2;
       v[o] = vn;
       if (a.do_drift) s[o] = sp[ax] + vn * a.dyyy + a.dD1 * d1 + a.dD2 * d2;
@@ -1045,9 +1047,10 @@ int mgp_launch_aos_to_soa(const float *in, float *out, long long np, cudaStream_
 // lengthfac, velocities velfac * Hubble/A^1.5 * (Vel - <Vel> + UseCOLA (D1
 // dD/dy + D2 dD2/dy)).  Vel - <Vel> equals the stored v minus its mean.
 __global__ void k_output(const float *__restrict__ s, const float *__restrict__ v, const float *__restrict__ D1,
-                         const float *__restrict__ D2, const mgp_dstate *__restrict__ st, long long np, int Ns,
-                         double box, double lengthfac, double vfac, double dDdy, double dD2dy, double cola,
-                         float *__restrict__ pos, float *__restrict__ vel) {
+                         const float *__restrict__ D2, long long lstride, int lpitch,
+                         const mgp_dstate *__restrict__ st, long long np, int Ns, double box, double lengthfac,
+                         double vfac, double dDdy, double dD2dy, double cola, float *__restrict__ pos,
+                         float *__restrict__ vel) {
   long long stride = (long long)gridDim.x * blockDim.x;
   const float dq = (float)(box / (double)Ns), fbox = (float)box, lf = (float)lengthfac, vf = (float)vfac;
   const float g1 = (float)(cola * dDdy), g2 = (float)(cola * dD2dy);
@@ -1056,19 +1059,20 @@ __global__ void k_output(const float *__restrict__ s, const float *__restrict__ 
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
     int li[3];
     lattice_ijk(p, Ns, li[0], li[1], li[2]);
+    const long long od = ((long long)li[0] * Ns + li[1]) * lpitch + li[2];
     for (int a = 0; a < 3; a++) {
       long long o = a * np + p;
       pos[3 * p + a] = lf * wrap_box((float)li[a] * dq + (s[o] + cx[a]), fbox);
-      vel[3 * p + a] = vf * ((v[o] - mv[a]) + D1[o] * g1 + D2[o] * g2);
+      vel[3 * p + a] = vf * ((v[o] - mv[a]) + D1[a * lstride + od] * g1 + D2[a * lstride + od] * g2);
     }
   }
 }
 
-int mgp_launch_output(const float *s, const float *v, const float *D1, const float *D2, const mgp_dstate *dst,
-                      long long np, int Ns, double box, double lengthfac, double vfac, double dDdy, double dD2dy,
-                      double cola, float *pos, float *vel, cudaStream_t st) {
-  k_output<<<blocks_for(np, 4), MGP_THREADS, 0, st>>>(s, v, D1, D2, dst, np, Ns, box, lengthfac, vfac, dDdy, dD2dy,
-                                                      cola, pos, vel);
+int mgp_launch_output(const float *s, const float *v, const float *D1, const float *D2, long long lpt_stride,
+                      int lpt_pitch, const mgp_dstate *dst, long long np, int Ns, double box, double lengthfac,
+                      double vfac, double dDdy, double dD2dy, double cola, float *pos, float *vel, cudaStream_t st) {
+  k_output<<<blocks_for(np, 4), MGP_THREADS, 0, st>>>(s, v, D1, D2, lpt_stride, lpt_pitch, dst, np, Ns, box,
+                                                      lengthfac, vfac, dDdy, dD2dy, cola, pos, vel);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -1082,6 +1086,7 @@ int mgp_launch_output(const float *s, const float *v, const float *D1, const flo
 // the mean velocity here) and wraps periodically.
 __global__ void __launch_bounds__(MGP_THREADS) k_cic_rsd(const float *__restrict__ s, const float *__restrict__ v,
                                                          const float *__restrict__ D1, const float *__restrict__ D2,
+                                                         long long lstride, int lpitch,
                                                          const mgp_dstate *__restrict__ st, long long np, int Ns,
                                                          int N, float scale, float wpar, int axis, float vnorm,
                                                          float g1, float g2, float *__restrict__ rho, long long P) {
@@ -1095,7 +1100,8 @@ __global__ void __launch_bounds__(MGP_THREADS) k_cic_rsd(const float *__restrict
     int li[3];
     lattice_ijk(p, Ns, li[0], li[1], li[2]);
     const long long ol = m[2] * np + p;
-    float V = (v[ol] + cvl) + D1[ol] * g1 + D2[ol] * g2;
+    const long long od = m[2] * lstride + ((long long)li[0] * Ns + li[1]) * lpitch + li[2];
+    float V = (v[ol] + cvl) + D1[od] * g1 + D2[od] * g2;
     int ix, iy, iz;
     float DX, DY, DZ;
     cell_frac(li[m[0]], s[m[0] * np + p], off[0], N, Ns, scale, ix, DX);
@@ -1117,11 +1123,11 @@ __global__ void __launch_bounds__(MGP_THREADS) k_cic_rsd(const float *__restrict
   }
 }
 
-int mgp_launch_cic_rsd(const float *s, const float *v, const float *D1, const float *D2, const mgp_dstate *st,
-                       long long np, int Ns, int N, double box, float wpar, int axis, float vnorm, float g1, float g2,
-                       float *rho, long long P, cudaStream_t stream) {
-  k_cic_rsd<<<blocks_for(np, 8), MGP_THREADS, 0, stream>>>(s, v, D1, D2, st, np, Ns, N, (float)(N / box), wpar, axis,
-                                                           vnorm, g1, g2, rho, P);
+int mgp_launch_cic_rsd(const float *s, const float *v, const float *D1, const float *D2, long long lpt_stride,
+                       int lpt_pitch, const mgp_dstate *st, long long np, int Ns, int N, double box, float wpar,
+                       int axis, float vnorm, float g1, float g2, float *rho, long long P, cudaStream_t stream) {
+  k_cic_rsd<<<blocks_for(np, 8), MGP_THREADS, 0, stream>>>(s, v, D1, D2, lpt_stride, lpt_pitch, st, np, Ns, N,
+                                                           (float)(N / box), wpar, axis, vnorm, g1, g2, rho, P);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;

@@ -29,11 +29,26 @@ static int output(mgp_ctx *c, double A, double z, int gadget) {
   const size_t np = (size_t)c->np, bytes = sizeof(float) * 3 * np;
   double fac = u.Hubble / pow(A, 1.5);
   double dDdy = mgp_cosmo_growth(&c->cosmo, 1, A), dD2dy = mgp_cosmo_growth(&c->cosmo, 4, A);
+  const float *L1 = c->D1, *L2 = c->D2;
+  long long lstride = c->np;
+  int lpitch = c->Ns;
+  if (c->sd) {
+    // the scale-dependent Output first assigns [dDdy] (main.c:807-823)
+    if (c->sd_kind[2] != MGP_FIELD_dDdy || c->sd_a[2] != A) {
+      const int t = MGP_FIELD_dDdy;
+      RET_IF(mgp_sd_fields(c, A, A, 1, &t));
+    }
+    L1 = L2 = c->sd_slot[2];
+    dDdy = 1.0;
+    dD2dy = 0.0;
+    lstride = c->sd_grid;
+    lpitch = c->sd_pitch;
+  }
   float *d = NULL;
   MGP_CUDA(cudaMalloc(&d, 2 * bytes));
   std::vector<float> pos(3 * np), vel(3 * np);
-  int rc = mgp_launch_output(c->s, c->v, c->D1, c->D2, c->dstate, c->np, c->Ns, c->p.Box, u.lengthfac, u.velfac * fac,
-                             dDdy, dD2dy, c->p.UseCOLA ? 1.0 : 0.0, d, d + 3 * np, c->stream);
+  int rc = mgp_launch_output(c->s, c->v, L1, L2, lstride, lpitch, c->dstate, c->np, c->Ns, c->p.Box, u.lengthfac,
+                             u.velfac * fac, dDdy, dD2dy, c->p.UseCOLA ? 1.0 : 0.0, d, d + 3 * np, c->stream);
   if (!rc) {
     cudaError_t e = cudaMemcpyAsync(pos.data(), d, bytes, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(vel.data(), d + 3 * np, bytes, cudaMemcpyDeviceToHost, c->stream);
@@ -94,6 +109,11 @@ extern "C" int mgp_run(mgp_ctx *c, int gadget) {
       if (c->p.pofk_compute_rsd_pofk == 1 && !output_step) RET_IF(write_rsd_now(c, A));
       RET_IF(mgp_get_displacements(c, A));
       if (p->pofk_compute_every_step) RET_IF(write_pofk_now(c, A, "CDM"));
+      if (c->sd) {
+        // scale-dependent fields of this step (main.c:487-503)
+        const int types[2] = {MGP_FIELD_ddDddy, MGP_FIELD_deltaD};
+        RET_IF(mgp_sd_fields(c, A, AFF, 2, types));
+      }
       if (output_step) {
         RET_IF(mgp_kick_drift(c, AI, AF, A, AFF, 0));
         RET_IF(output(c, A, p->output_redshift[i - 1], gadget));

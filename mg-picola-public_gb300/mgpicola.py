@@ -22,8 +22,12 @@ EXPORTS = [
     "mgp_displacement_fields", "mgp_get_displacements", "mgp_kick_drift", "mgp_step", "mgp_run", "mgp_pofk",
     "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
     "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_launch_count",
-    "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc",
+    "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
+    "mgp_growth_scaledependent",
 ]
+
+# field types of mgp_assign_displacement_fields (src/proto.h:155-158)
+FIELD_D, FIELD_dDdy, FIELD_ddDddy, FIELD_deltaD = 0, 1, 2, 3
 
 
 class Params(C.Structure):
@@ -53,6 +57,7 @@ class Params(C.Structure):
         ("UnitLength_in_cm", C.c_double), ("UnitMass_in_g", C.c_double), ("UnitVelocity_in_cm_per_s", C.c_double),
         ("InputSpectrum_UnitLength_in_cm", C.c_double),
         ("Noutputs", C.c_int), ("output_redshift", C.c_double * 64), ("output_nsteps", C.c_int * 64),
+        ("sd_nk", C.c_int), ("sd_kmin", C.c_double), ("sd_kmax", C.c_double),
     ]
 
 
@@ -98,6 +103,8 @@ def lib():
             getattr(L, f).restype = C.c_double
         L.mgp_cosmo_eval.argtypes = [C.POINTER(Params), C.c_int, dp, C.c_int, dp]
         L.mgp_cosmo_coeff.argtypes = [C.POINTER(Params), C.c_int, dp, dp, dp, C.c_int, dp]
+        L.mgp_growth_scaledependent.argtypes = [C.POINTER(Params), C.c_int, dp, dp, C.c_int, dp]
+        L.mgp_assign_displacement_fields.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_int)]
         L.mgp_power_spectrum.argtypes = [vp, C.c_double]
         L.mgp_power_spectrum.restype = C.c_double
         L.mgp_copy_grid.argtypes = [vp, C.c_int, fp, C.c_size_t]
@@ -147,6 +154,15 @@ def cosmo_eval(params, which, x):
     x = np.ascontiguousarray(x, dtype=np.float64)
     out = np.zeros_like(x)
     _check(lib().mgp_cosmo_eval(C.byref(params), which, _dptr(x), x.size, _dptr(out)))
+    return out
+
+
+def growth_scaledependent(params, which, k, a):
+    """growth_*_scaledependent(k, a) of a parameter set (scaledependent = 1)."""
+    k = np.ascontiguousarray(k, dtype=np.float64)
+    a = np.ascontiguousarray(np.broadcast_to(a, k.shape), dtype=np.float64)
+    out = np.zeros_like(k)
+    _check(lib().mgp_growth_scaledependent(C.byref(params), which, _dptr(k), _dptr(a), k.size, _dptr(out)))
     return out
 
 
@@ -216,6 +232,10 @@ class Context:
 
     def kick_drift(self, AI, AF, A, AFF, drift=True):
         _check(lib().mgp_kick_drift(self.h, AI, AF, A, AFF, 1 if drift else 0))
+
+    def assign_fields(self, A, AFF, *types):
+        t = (C.c_int * len(types))(*types)
+        _check(lib().mgp_assign_displacement_fields(self.h, A, AFF, len(types), t))
 
     def step(self, A, AI, AF, AFF):
         _check(lib().mgp_step(self.h, A, AI, AF, AFF))
