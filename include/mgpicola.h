@@ -248,6 +248,38 @@ int mgp_growth_scaledependent(const mgp_params *p, int which, const double *k, c
 int mgp_cosmo_coeff(const mgp_params *p, int kind, const double *ai, const double *af, const double *aref, int n,
                     double *out);
 
+/* Batches of independent boxes (no counterpart in the reference, which runs
+ * one box per MPI job: a parameter sweep is many runs of main).  All boxes
+ * share Nmesh, Nsample, Box, the model, its switches and the background;
+ * each has its own seed, IC flags and, for f(R) / nDGP, its own |fR0| /
+ * rcH0 (values <= 0 keep the common one).  Every kernel and FFT of the PM
+ * step covers all boxes at once, and mgp_batch_run captures the whole KDK
+ * loop of main.c:394-611 (one output at z_final, nsteps steps, P(k) at
+ * every step when pofk_compute_every_step) into one CUDA graph launch.
+ * Scale-independent growth only.  The context returned works only with the
+ * mgp_batch_* calls and mgp_destroy. */
+typedef struct mgp_box_params {
+  int Seed;
+  int inverted_initial_condition;
+  int amplitude_fixed_initial_condition;
+  double fofr0;
+  double rcH0_DGP;
+} mgp_box_params;
+int mgp_batch_create(const mgp_params *p, int nbox, const mgp_box_params *boxes, int device, mgp_ctx **out);
+/* 2LPT ICs of every box, then the captured loop (built on the first call
+ * for this nsteps / z_final and replayed afterwards). */
+int mgp_batch_run(mgp_ctx *ctx, int nsteps, double z_final);
+/* P(k) of box `box` at step `step` (0 .. nsteps; step nsteps is z_final),
+ * arrays as mgp_pofk. */
+int mgp_batch_pofk(mgp_ctx *ctx, int box, int step, int cap, int *nbins, double *k, double *pk, double *kmean,
+                   double *n);
+/* Final particles of one box, as mgp_get_particles. */
+int mgp_batch_get_particles(mgp_ctx *ctx, int box, float *pos, float *vel, size_t np);
+/* CUDA-event milliseconds of the last mgp_batch_run: what 0 = the captured
+ * loop (one graph launch), 1 = the ICs; and the captured graph's node count. */
+double mgp_batch_ms(mgp_ctx *ctx, int what);
+int mgp_batch_graph_nodes(mgp_ctx *ctx);
+
 /* Copy an internal grid to a host buffer (diagnostics and parity tests).
  * which: 0 density (real padded [N][N][2(N/2+1)] float), 1 delta(k)
  * (complex [N][N][N/2+1] float pairs), 2..4 force grids x,y,z (real

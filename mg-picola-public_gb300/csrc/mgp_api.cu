@@ -175,13 +175,14 @@ static int setup_pofk(mgp_ctx *c) {
   // enough warps to cover the SMs; each warp owns whole (i, j) rows
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-  long long nb = (long long)sms * 4;
+  // (a batch shares that budget among its boxes)
+  long long nb = ((long long)sms * 4 + c->nbox - 1) / c->nbox;
   long long rows_blocks = ((long long)N * N + 7) / 8;
   if (nb > rows_blocks) nb = rows_blocks;
   if (nb < 1) nb = 1;
   c->pk_blocks = (int)nb;
-  MGP_CUDA(cudaMalloc(&c->pk_block, sizeof(double) * (size_t)nb * nbins));
-  MGP_CUDA(cudaMalloc(&c->pk_sum, sizeof(double) * nbins));
+  MGP_CUDA(cudaMalloc(&c->pk_block, sizeof(double) * (size_t)nb * nbins * c->nbox));
+  MGP_CUDA(cudaMalloc(&c->pk_sum, sizeof(double) * nbins * c->nbox));
   return MGP_OK;
 }
 
@@ -205,11 +206,32 @@ static int make_plans(mgp_ctx *c) {
   MGP_CUFFT(cufftMakePlanMany64(c->plan_c2r_1, 3, n, cembed, 1, cdist, rembed, 1, rdist, CUFFT_C2R, 1, &ws[2]));
   size_t w = 0;
   for (int i = 0; i < 3; i++) w = ws[i] > w ? ws[i] : w;
+  // a batch also transforms all boxes per call (the force grids of one box
+  // are three consecutive grids, so their batch stride is 3 grids)
+  cufftHandle *bplans[4] = {&c->plan_r2c_oop_b, &c->plan_r2c_ip_b, &c->plan_c2r_b, &c->plan_c2r_frc_b};
+  const int nbp = c->nbox > 1 ? 4 : 0;
+  for (int i = 0; i < nbp; i++) {
+    size_t wb = 0;
+    MGP_CUFFT(cufftCreate(bplans[i]));
+    MGP_CUFFT(cufftSetAutoAllocation(*bplans[i], 0));
+    if (i < 2)
+      MGP_CUFFT(cufftMakePlanMany64(*bplans[i], 3, n, rembed, 1, rdist, cembed, 1, cdist, CUFFT_R2C, c->nbox, &wb));
+    else if (i == 2)
+      MGP_CUFFT(cufftMakePlanMany64(*bplans[i], 3, n, cembed, 1, cdist, rembed, 1, rdist, CUFFT_C2R, c->nbox, &wb));
+    else
+      MGP_CUFFT(cufftMakePlanMany64(*bplans[i], 3, n, cembed, 1, 3 * cdist, rembed, 1, 3 * rdist, CUFFT_C2R, c->nbox,
+                                    &wb));
+    w = wb > w ? wb : w;
+  }
   c->fft_work_bytes = w;
   if (w) MGP_CUDA(cudaMalloc(&c->fft_work, w));
   for (int i = 0; i < 3; i++) {
     MGP_CUFFT(cufftSetWorkArea(*plans[i], c->fft_work));
     MGP_CUFFT(cufftSetStream(*plans[i], c->stream));
+  }
+  for (int i = 0; i < nbp; i++) {
+    MGP_CUFFT(cufftSetWorkArea(*bplans[i], c->fft_work));
+    MGP_CUFFT(cufftSetStream(*bplans[i], c->stream));
   }
   return MGP_OK;
 }
@@ -242,10 +264,22 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   if (!c) return MGP_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  cufftHandle plans[3] = {c->plan_r2c_oop, c->plan_r2c_ip, c->plan_c2r_1};
-  for (int i = 0; i < 3; i++)
+  cufftHandle plans[7] = {c->plan_r2c_oop, c->plan_r2c_ip, c->plan_c2r_1, c->plan_r2c_oop_b, c->plan_r2c_ip_b,
+                          c->plan_c2r_b, c->plan_c2r_frc_b};
+  for (int i = 0; i < 7; i++)
     if (plans[i]) cufftDestroy(plans[i]);
   mgp_sd_free(c);
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  for (int q = 0; q < 2; q++)
+    if (c->bev[q]) cudaEventDestroy(c->bev[q]);
+  if (c->box_bs) cudaFree(c->box_bs);
+  if (c->pk_hist) cudaFree(c->pk_hist);
+  if (c->box_cosmo) {
+    for (int b = 1; b < c->nbox; b++) mgp_cosmo_free(&c->box_cosmo[b]);
+    free(c->box_cosmo);
+  }
+  free(c->box_p);
   void *bufs[] = {c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
                   c->fft_work, c->rk_bin, c->pk_thr, c->win1d, c->pk_block, c->pk_sum, c->rsd_block, c->rsd_sum};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
@@ -263,22 +297,57 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   return MGP_OK;
 }
 
-extern "C" int mgp_create(const mgp_params *p, int device, mgp_ctx **out) {
+// Parameters of box b of a batch: the common set with the box's overrides.
+static mgp_params box_params(const mgp_params *p, const mgp_box_params *bp) {
+  mgp_params q = *p;
+  q.Seed = bp->Seed;
+  q.inverted_initial_condition = bp->inverted_initial_condition;
+  q.amplitude_fixed_initial_condition = bp->amplitude_fixed_initial_condition;
+  if (bp->fofr0 > 0) q.fofr0 = bp->fofr0;
+  if (bp->rcH0_DGP > 0) q.rcH0_DGP = bp->rcH0_DGP;
+  return q;
+}
+
+static const mgp_cosmo *cosmo_of(const mgp_ctx *c, int b) { return b == 0 ? &c->cosmo : &c->box_cosmo[b]; }
+
+static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxes, int device, mgp_ctx **out) {
   if (!p || !out) return mgp_set_error(MGP_EINVAL, "null argument");
   *out = NULL;
   RET_IF(validate(p));
+  if (nbox < 1 || nbox > 65535) return mgp_set_error(MGP_EINVAL, "nbox = %d out of range", nbox);
+  if (nbox > 1 && p->scaledependent)
+    return mgp_set_error(MGP_EINVAL, "a batch of boxes runs scale-independent growth only");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
     return mgp_set_error(MGP_ECUDA, "no CUDA device available: the library has no CPU path");
   if (device < 0 || device >= ndev) return mgp_set_error(MGP_EINVAL, "device %d out of range", device);
   mgp_ctx *c = (mgp_ctx *)calloc(1, sizeof(mgp_ctx));
-  c->p = *p;
+  c->nbox = nbox;
+  c->box_p = (mgp_params *)calloc(nbox, sizeof(mgp_params));
+  for (int b = 0; b < nbox; b++) c->box_p[b] = boxes ? box_params(p, &boxes[b]) : *p;
+  c->p = c->box_p[0];
   c->device = device;
   char err[512] = "";
-  int rc = mgp_cosmo_init(&c->cosmo, p, err, sizeof(err));
+  int rc = mgp_cosmo_init(&c->cosmo, &c->box_p[0], err, sizeof(err));
   if (rc) {
+    free(c->box_p);
     free(c);
     return mgp_set_error(rc, "%s", err);
+  }
+  if (nbox > 1) {
+    c->box_cosmo = (mgp_cosmo *)calloc(nbox, sizeof(mgp_cosmo));
+    for (int b = 1; b < nbox && rc == MGP_OK; b++) {
+      rc = mgp_cosmo_init(&c->box_cosmo[b], &c->box_p[b], err, sizeof(err));
+      if (rc == MGP_OK && c->box_cosmo[b].p.Omega != c->cosmo.p.Omega) {
+        snprintf(err, sizeof(err), "the boxes of a batch must share the background (box %d)", b);
+        rc = MGP_EINVAL;
+      }
+    }
+    if (rc) {
+      std::string e = err;
+      mgp_destroy(c);
+      return mgp_set_error(rc, "%s", e.c_str());
+    }
   }
   // the Brans-Dicke background solve replaces Omega and h (init_modified_version,
   // src/user_defined_functions.h:135-143); the time step uses the new values
@@ -309,7 +378,7 @@ extern "C" int mgp_create(const mgp_params *p, int device, mgp_ctx **out) {
   c->g.ncomplex = (long long)N * N * c->g.NH;
   c->Ns = p->Nsample;
   c->np = (long long)p->Nsample * p->Nsample * p->Nsample;
-  const size_t pbytes = sizeof(float) * 3 * (size_t)c->np;
+  const size_t pbytes = sizeof(float) * 3 * (size_t)c->np * nbox;
   TRYCUDA(cudaMalloc(&c->s, pbytes));
   TRYCUDA(cudaMalloc(&c->v, pbytes));
   TRYCUDA(cudaMemset(c->s, 0, pbytes));
@@ -321,11 +390,11 @@ extern "C" int mgp_create(const mgp_params *p, int device, mgp_ctx **out) {
     TRYCUDA(cudaMemset(c->D1, 0, pbytes));
     TRYCUDA(cudaMemset(c->D2, 0, pbytes));
   }
-  TRYCUDA(cudaMalloc(&c->dstate, sizeof(mgp_dstate)));
-  TRYCUDA(cudaMemset(c->dstate, 0, sizeof(mgp_dstate)));
+  TRYCUDA(cudaMalloc(&c->dstate, sizeof(mgp_dstate) * nbox));
+  TRYCUDA(cudaMemset(c->dstate, 0, sizeof(mgp_dstate) * nbox));
   c->max_blocks = mgp_ikd_blocks(c->np) > 4096 ? mgp_ikd_blocks(c->np) : 4096;
-  TRYCUDA(cudaMalloc(&c->partials, sizeof(double) * 6 * (size_t)c->max_blocks));
-  const size_t gbytes = sizeof(float) * (size_t)c->g.nreal;
+  TRYCUDA(cudaMalloc(&c->partials, sizeof(double) * 6 * (size_t)c->max_blocks * nbox));
+  const size_t gbytes = sizeof(float) * (size_t)c->g.nreal * nbox;
   TRYCUDA(cudaMalloc(&c->rho, gbytes));
   TRYCUDA(cudaMalloc(&c->dk, gbytes));
   TRYCUDA(cudaMalloc(&c->frc, 3 * gbytes));
@@ -333,23 +402,41 @@ extern "C" int mgp_create(const mgp_params *p, int device, mgp_ctx **out) {
   TRY(make_plans(c));
   TRY(setup_pofk(c));
   if (p->scaledependent) TRY(mgp_sd_alloc(c));
+  if (nbox > 1) {
+    TRYCUDA(cudaEventCreate(&c->bev[0]));
+    TRYCUDA(cudaEventCreate(&c->bev[1]));
+  }
 #undef TRYCUDA
 #undef TRY
   *out = c;
   return MGP_OK;
 }
 
+extern "C" int mgp_create(const mgp_params *p, int device, mgp_ctx **out) {
+  return create_impl(p, 1, NULL, device, out);
+}
+
+extern "C" int mgp_batch_create(const mgp_params *p, int nbox, const mgp_box_params *boxes, int device,
+                                mgp_ctx **out) {
+  if (!boxes) return mgp_set_error(MGP_EINVAL, "null box list");
+  return create_impl(p, nbox, boxes, device, out);
+}
+
 // ---------------------------------------------------------------- IC
-extern "C" int mgp_displacement_fields(mgp_ctx *c) {
-  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
-  MGP_CUDA(cudaSetDevice(c->device));
+// displacement_fields + the particle assignment of main.c:231-309 for box b
+// (single-grid transforms; box b's particle arrays and state).
+static int ic_box(mgp_ctx *c, int bx) {
+  const mgp_params *pb = &c->box_p[bx];
+  const mgp_cosmo *cb = cosmo_of(c, bx);
+  float *dkb = c->dk + (size_t)bx * c->g.nreal;
+  const size_t po = (size_t)bx * 3 * c->np;
   const int N = c->g.N, Ns = c->Ns, h = N / 2;
-  const double box = c->p.Box;
+  const double box = pb->Box;
   // seed table, src/2LPT.c:262-271
   std::vector<uint32_t> seeds((size_t)N * N);
   {
     uint64_t n = 0;
-    uint32_t sd = (uint32_t)c->p.Seed;
+    uint32_t sd = (uint32_t)pb->Seed;
     auto draw = [&]() { return (uint32_t)(0x7fffffff * mgp_uniform(sd, n++)); };
     for (int i = 0; i < N / 2; i++) {
       for (int j = 0; j < i; j++) seeds[(size_t)i * N + j] = draw();
@@ -369,15 +456,15 @@ extern "C" int mgp_displacement_fields(mgp_ctx *c) {
   std::vector<double> amp(rkmax + 1), kk(rkmax + 1), ratio(rkmax + 1, 1.0);
   for (int rk = 0; rk <= rkmax; rk++) kk[rk] = 2.0 * M_PI / box * sqrt((double)rk);
   double s8fac = 1.0;
-  if (c->p.modified_gravity_active && c->p.input_pofk_is_for_lcdm) {
-    mgp_cosmo_pofk_ratio_many(&c->cosmo, 1.0, rkmax, kk.data() + 1, ratio.data() + 1);
-    if (!c->p.input_sigma8_is_for_lcdm) {
-      double e = mgp_cosmo_sigma8_enh(&c->cosmo, 1.0);
+  if (pb->modified_gravity_active && pb->input_pofk_is_for_lcdm) {
+    mgp_cosmo_pofk_ratio_many(cb, 1.0, rkmax, kk.data() + 1, ratio.data() + 1);
+    if (!pb->input_sigma8_is_for_lcdm) {
+      double e = mgp_cosmo_sigma8_enh(cb, 1.0);
       s8fac = 1.0 / (e * e);
     }
   }
   for (int rk = 0; rk <= rkmax; rk++) {
-    double pk = rk == 0 ? 0.0 : mgp_cosmo_power(&c->cosmo, kk[rk]) * ratio[rk] * s8fac;
+    double pk = rk == 0 ? 0.0 : mgp_cosmo_power(cb, kk[rk]) * ratio[rk] * s8fac;
     amp[rk] = pow(box, -1.5) * sqrt(pk);
   }
   // cube cut of 2LPT.c:383-386 with the reference's double expression
@@ -392,8 +479,8 @@ extern "C" int mgp_displacement_fields(mgp_ctx *c) {
   float *g6 = NULL;
   int rc = MGP_OK;
   const long long gf = c->g.nreal;
-  const double Di = mgp_cosmo_growth(&c->cosmo, 0, 1.0 / (1.0 + c->p.Init_Redshift));
-  const double Di2 = mgp_cosmo_growth(&c->cosmo, 3, 1.0 / (1.0 + c->p.Init_Redshift));
+  const double Di = mgp_cosmo_growth(cb, 0, 1.0 / (1.0 + pb->Init_Redshift));
+  const double Di2 = mgp_cosmo_growth(cb, 3, 1.0 / (1.0 + pb->Init_Redshift));
   const int nblk = mgp_ikd_blocks(c->np);
 #define CK(x)                      \
   do {                             \
@@ -425,10 +512,10 @@ extern "C" int mgp_displacement_fields(mgp_ctx *c) {
   CKC(cudaMemcpyAsync(d_seeds, seeds.data(), sizeof(uint32_t) * seeds.size(), cudaMemcpyHostToDevice, c->stream));
   CKC(cudaMemcpyAsync(d_amp, amp.data(), sizeof(double) * amp.size(), cudaMemcpyHostToDevice, c->stream));
   CKC(cudaMemcpyAsync(d_cut, cut.data(), cut.size(), cudaMemcpyHostToDevice, c->stream));
-  CKC(cudaMemsetAsync(c->dk, 0, sizeof(float) * (size_t)gf, c->stream));
-  CK(mgp_launch_ic_delta(d_seeds, d_amp, d_cut, N, Ns, box, c->p.amplitude_fixed_initial_condition,
-                         c->p.inverted_initial_condition, c->p.SphereMode == 1, c->dk, c->stream));
-  CK(mgp_launch_ic_grad6(c->dk, g6, gf, N, c->stream));
+  CKC(cudaMemsetAsync(dkb, 0, sizeof(float) * (size_t)gf, c->stream));
+  CK(mgp_launch_ic_delta(d_seeds, d_amp, d_cut, N, Ns, box, pb->amplitude_fixed_initial_condition,
+                         pb->inverted_initial_condition, pb->SphereMode == 1, dkb, c->stream));
+  CK(mgp_launch_ic_grad6(dkb, g6, gf, N, c->stream));
   for (int g = 0; g < 3; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
   for (int g = 3; g < 6; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
   CK(mgp_launch_ic_source(g6, gf, N, c->g.P, c->stream));
@@ -446,12 +533,13 @@ extern "C" int mgp_displacement_fields(mgp_ctx *c) {
     c->have_density = c->have_forces = 0;
     goto cleanup;
   }
-  CK(mgp_launch_ic_disp(c->dk, g6 + 3 * gf, g6, gf, N, box, c->stream));
+  CK(mgp_launch_ic_disp(dkb, g6 + 3 * gf, g6, gf, N, box, c->stream));
   for (int g = 0; g < 3; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
   for (int g = 3; g < 6; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
-  CK(mgp_launch_ic_readout(g6, gf, N, c->g.P, Ns, c->D1, c->D2, c->partials, nblk, c->stream));
-  CK(mgp_launch_ic_finish(c->D1, c->D2, c->s, c->v, c->np, c->partials, nblk, (float)Di, (float)Di2, 0.0, c->stream));
-  CKC(cudaMemsetAsync(c->dstate, 0, sizeof(mgp_dstate), c->stream));
+  CK(mgp_launch_ic_readout(g6, gf, N, c->g.P, Ns, c->D1 + po, c->D2 + po, c->partials, nblk, c->stream));
+  CK(mgp_launch_ic_finish(c->D1 + po, c->D2 + po, c->s + po, c->v + po, c->np, c->partials, nblk, (float)Di,
+                          (float)Di2, 0.0, c->stream));
+  CKC(cudaMemsetAsync(c->dstate + bx, 0, sizeof(mgp_dstate), c->stream));
   CKC(cudaStreamSynchronize(c->stream));
   c->have_density = c->have_forces = 0;
 cleanup:
@@ -465,9 +553,17 @@ cleanup:
   return rc;
 }
 
+extern "C" int mgp_displacement_fields(mgp_ctx *c) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  if (c->nbox != 1) return mgp_set_error(MGP_ESTATE, "single-box call on a batch of %d boxes", c->nbox);
+  MGP_CUDA(cudaSetDevice(c->device));
+  return ic_box(c, 0);
+}
+
 // ------------------------------------------------------------ PM step
 static int require_particles(mgp_ctx *c) {
   if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  if (c->nbox != 1) return mgp_set_error(MGP_ESTATE, "single-box call on a batch of %d boxes", c->nbox);
   MGP_CUDA(cudaSetDevice(c->device));
   return MGP_OK;
 }
@@ -871,3 +967,261 @@ extern "C" double mgp_growth(mgp_ctx *c, int which, double a) { return c ? mgp_c
 extern "C" double mgp_Sq(mgp_ctx *c, double ai, double af, double aref) { return c ? mgp_cosmo_Sq(&c->cosmo, ai, af, aref) : NAN; }
 extern "C" double mgp_Sphi(mgp_ctx *c, double ai, double af, double aref) { return c ? mgp_cosmo_Sphi(&c->cosmo, ai, af, aref) : NAN; }
 extern "C" double mgp_power_spectrum(mgp_ctx *c, double k) { return c ? mgp_cosmo_power(&c->cosmo, k) : NAN; }
+
+// ----------------------------------------------------------------- batches
+// A batch runs nbox independent boxes in lock step: every kernel of the PM
+// step covers all boxes (the box is blockIdx.y), every FFT is one batched
+// cuFFT call, and the whole KDK loop (src/main.c:394-611 for one output) is
+// captured once into a CUDA graph and replayed with one launch.  The
+// reference runs one box per MPI job; a sweep is many jobs.
+
+struct batch_step {
+  double A, AI, AF, AFF;
+  int drift;
+  mgp_kd_args kd;
+};
+
+// Time steps of main.c:394-611 for one output at z_final (stepDistr = 0):
+// nsteps kick+drift steps, then the output step's kick (AF = A, no drift).
+static void batch_schedule(const mgp_ctx *c, int nsteps, double zf, std::vector<batch_step> &st,
+                           std::vector<mgp_box_scalars> &bs) {
+  const mgp_params *p = &c->p;
+  const double A0 = 1.0 / (1.0 + p->Init_Redshift), ao = 1.0 / (1.0 + zf);
+  const double da = (ao - A0) / (double)nsteps, cola = p->UseCOLA ? 1.0 : 0.0, om = p->Omega;
+  st.assign(nsteps + 1, batch_step());
+  bs.assign((size_t)(nsteps + 1) * c->nbox, mgp_box_scalars());
+  double A = A0, AI = A0;
+  for (int t = 0; t <= nsteps; t++) {
+    batch_step &q = st[t];
+    q.drift = t < nsteps;
+    q.A = A;
+    q.AI = AI;
+    q.AF = q.drift ? A + 0.5 * da : A;
+    q.AFF = A + da;
+    const mgp_cosmo *c0 = &c->cosmo;
+    double dda = mgp_cosmo_Sphi(c0, q.AI, q.AF, A);
+    memset(&q.kd, 0, sizeof(q.kd));
+    q.kd.scale = (float)(c->g.N / p->Box);
+    q.kd.inv_scale = (float)(p->Box / c->g.N);
+    q.kd.kick_disp = (float)(-1.5 * om * dda);
+    q.kd.dda_omega = 1.5 * om * dda;
+    q.kd.do_drift = q.drift;
+    q.kd.lpt_stride = c->np;
+    q.kd.lpt_pitch = c->Ns;
+    if (q.drift) {
+      double dyyy = mgp_cosmo_Sq(c0, A, q.AFF, q.AF);
+      q.kd.dyyy = (float)dyyy;
+      q.kd.dyyy_d = dyyy;
+    }
+    for (int b = 0; b < c->nbox; b++) {
+      const mgp_cosmo *cb = cosmo_of(c, b);
+      const mgp_params *pb = &c->box_p[b];
+      mgp_box_scalars &o = bs[(size_t)t * c->nbox + b];
+      o.kick_d1 = (float)(-cola * mgp_cosmo_growth(cb, 2, A) / A * dda);
+      o.kick_d2 = (float)(-cola * mgp_cosmo_growth(cb, 5, A) / A * dda);
+      if (q.drift) {
+        o.dD1 = (float)(cola * (mgp_cosmo_growth(cb, 0, q.AFF) - mgp_cosmo_growth(cb, 0, A)));
+        o.dD2 = (float)(cola * (mgp_cosmo_growth(cb, 3, q.AFF) - mgp_cosmo_growth(cb, 3, A)));
+      }
+      if (!pb->modified_gravity_active) continue;
+      if (pb->model == MGP_MODEL_FOFR || pb->model == MGP_MODEL_MBETA) {
+        o.phicrit = (float)mgp_phicrit(cb, A);
+        o.coupling = (float)mgp_coupling(cb, A);
+        o.mass2 = (float)(A * A * mgp_mass2_of_a(cb, A) / pow(2.0 * M_PI * 2997.92458 / pb->Box, 2));
+      } else if (pb->model == MGP_MODEL_DGP) {
+        o.coupling = (float)mgp_coupling(cb, A);
+        o.pref = (float)mgp_dgp_screen_prefactor(cb, A);
+      } else if (pb->model == MGP_MODEL_BRANSDICKE) {
+        o.coupling = (float)(mgp_geff(cb, A, 0.0) - 1.0);
+      }
+    }
+    A = q.AFF;
+    AI = q.AF;
+  }
+}
+
+// One batched PM step (GetDisplacements + P(k) + Kick/Drift) for all boxes,
+// stream-ordered and free of host synchronisation (it is graph-captured).
+static int batch_step_launch(mgp_ctx *c, const batch_step &q, const mgp_box_scalars *bs, double *pk_sums) {
+  const mgp_params *p = &c->p;
+  const int N = c->g.N, B = c->nbox;
+  const long long gf = c->g.nreal;
+  // batched plans when there are several boxes (a single box uses its own)
+  const cufftHandle r2c_oop = B > 1 ? c->plan_r2c_oop_b : c->plan_r2c_oop;
+  const cufftHandle r2c_ip = B > 1 ? c->plan_r2c_ip_b : c->plan_r2c_ip;
+  const cufftHandle c2r = B > 1 ? c->plan_c2r_b : c->plan_c2r_1;
+  const cufftHandle c2r_frc = B > 1 ? c->plan_c2r_frc_b : c->plan_c2r_1;
+  RET_IF(mgp_launch_fill(c->rho, gf * B, -1.0f, c->stream));
+  const double wpar = pow((double)N / (double)c->Ns, 3);
+  RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, p->Box, (float)wpar, c->rho, c->g.P, c->stream, B, gf));
+  MGP_CUFFT(cufftExecR2C(r2c_oop, (cufftReal *)c->rho, (cufftComplex *)c->dk));
+  const int fused = p->pofk_compute_every_step ? mg_filter_kind(p) : 0;
+  const double n3 = pow((double)N, 3);
+  if (p->pofk_compute_every_step) {
+    float fa = 0.f, fb = 0.f;
+    if (fused == 1) {
+      fa = (float)(2.0 * M_PI / p->Box * p->Rsmooth);
+      fb = (float)(1.0 / n3);
+    } else if (fused == 2) {
+      fb = (float)(1.0 / n3 * 1.5 * p->Omega / q.A * pow(p->Box / 2997.92458 / (2.0 * M_PI), 2));
+    }
+    RET_IF(mgp_launch_pofk_thr(c->dk, N, c->pk_thr, c->win1d, c->pk_nbins, c->pk_bintype, c->pk_kmin, c->pk_kmax,
+                               c->pk_block, c->pk_blocks, pk_sums, fused, p->smoothing_filter, fused ? c->mg1 : NULL,
+                               fa, fb, c->stream, B, gf, c->pk_nbins));
+  }
+  int mg_kind = 0;
+  if (p->modified_gravity_active) {
+    if (p->model == MGP_MODEL_FOFR || p->model == MGP_MODEL_MBETA) {
+      if (p->include_screening) {
+        double norm = 1.0 / n3 * 1.5 * p->Omega / q.A * pow(p->Box / 2997.92458 / (2.0 * M_PI), 2);
+        if (!fused) RET_IF(mgp_launch_div_laplacian(c->dk, c->mg1, N, (float)norm, c->stream, B, gf));
+        MGP_CUFFT(cufftExecC2R(c2r, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+        RET_IF(mgp_launch_screen_potential(c->rho, c->mg1, gf, 0.f, c->stream, B, bs));
+      }
+      MGP_CUFFT(cufftExecR2C(r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
+      mg_kind = 1;
+    } else if (p->model == MGP_MODEL_DGP) {
+      if (p->include_screening) {
+        if (!fused)
+          RET_IF(mgp_launch_smooth(c->dk, c->mg1, N, p->smoothing_filter, (float)(2.0 * M_PI / p->Box * p->Rsmooth),
+                                   (float)(1.0 / n3), c->stream, B, gf));
+        MGP_CUFFT(cufftExecC2R(c2r, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+        RET_IF(mgp_launch_screen_density(c->rho, c->mg1, gf, 0.f, 0.f, c->stream, B, bs));
+        MGP_CUFFT(cufftExecR2C(r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
+        mg_kind = 2;
+      } else {
+        mg_kind = 3;
+      }
+    } else if (p->model == MGP_MODEL_BRANSDICKE) {
+      mg_kind = 3;
+    }
+  }
+  RET_IF(mgp_launch_forces(c->dk, c->rho, 0.f, 0.f, mg_kind, N, p->Box, c->frc, gf, c->stream, B, bs));
+  for (int g = 0; g < 3; g++)
+    MGP_CUFFT(cufftExecC2R(c2r_frc, (cufftComplex *)(c->frc + g * gf), (cufftReal *)(c->frc + g * gf)));
+  const int nblk = mgp_blocks_per_box(c->np, 8, B);
+  RET_IF(mgp_launch_ikd(c->frc, gf, N, c->g.P, c->Ns, c->np, c->s, c->v, c->D1, c->D2, c->dstate, c->partials, nblk,
+                        &q.kd, c->stream, B, bs));
+  return MGP_OK;
+}
+
+static int batch_build_graph(mgp_ctx *c, int nsteps, double zf) {
+  std::vector<batch_step> st;
+  std::vector<mgp_box_scalars> bs;
+  batch_schedule(c, nsteps, zf, st, bs);
+  if (nsteps + 1 > c->hist_steps) {
+    if (c->box_bs) cudaFree(c->box_bs);
+    if (c->pk_hist) cudaFree(c->pk_hist);
+    c->box_bs = NULL;
+    c->pk_hist = NULL;
+    c->hist_steps = 0;
+    MGP_CUDA(cudaMalloc(&c->box_bs, sizeof(mgp_box_scalars) * bs.size()));
+    MGP_CUDA(cudaMalloc(&c->pk_hist, sizeof(double) * (size_t)(nsteps + 1) * c->nbox * c->pk_nbins));
+    c->hist_steps = nsteps + 1;
+  }
+  MGP_CUDA(cudaMemcpy(c->box_bs, bs.data(), sizeof(mgp_box_scalars) * bs.size(), cudaMemcpyHostToDevice));
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = NULL;
+  c->graph = NULL;
+  MGP_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = MGP_OK;
+  for (int t = 0; t <= nsteps && rc == MGP_OK; t++)
+    rc = batch_step_launch(c, st[t], c->box_bs + (size_t)t * c->nbox,
+                           c->pk_hist + (size_t)t * c->nbox * c->pk_nbins);
+  cudaGraph_t g = NULL;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (rc != MGP_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return mgp_set_error(MGP_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+  c->graph = g;
+  MGP_CUDA(cudaGraphInstantiate(&c->graph_exec, g, 0));
+  c->graph_nsteps = nsteps;
+  c->graph_zf = zf;
+  return MGP_OK;
+}
+
+extern "C" int mgp_batch_run(mgp_ctx *c, int nsteps, double z_final) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  if (nsteps < 1) return mgp_set_error(MGP_EINVAL, "nsteps = %d", nsteps);
+  MGP_CUDA(cudaSetDevice(c->device));
+  if (c->nbox == 1 && !c->bev[0]) {
+    MGP_CUDA(cudaEventCreate(&c->bev[0]));
+    MGP_CUDA(cudaEventCreate(&c->bev[1]));
+  }
+  if (c->sd) return mgp_set_error(MGP_EINVAL, "batch runs use scale-independent growth");
+  // 2LPT ICs of every box (not captured: host-side seed tables)
+  MGP_CUDA(cudaEventRecord(c->bev[0], c->stream));
+  for (int b = 0; b < c->nbox; b++) RET_IF(ic_box(c, b));
+  MGP_CUDA(cudaEventRecord(c->bev[1], c->stream));
+  MGP_CUDA(cudaEventSynchronize(c->bev[1]));
+  MGP_CUDA(cudaEventElapsedTime(&c->batch_ic_ms, c->bev[0], c->bev[1]));
+  if (!c->graph_exec || c->graph_nsteps != nsteps || c->graph_zf != z_final) RET_IF(batch_build_graph(c, nsteps, z_final));
+  MGP_CUDA(cudaEventRecord(c->bev[0], c->stream));
+  MGP_CUDA(cudaGraphLaunch(c->graph_exec, c->stream));
+  MGP_CUDA(cudaEventRecord(c->bev[1], c->stream));
+  MGP_CUDA(cudaEventSynchronize(c->bev[1]));
+  MGP_CUDA(cudaEventElapsedTime(&c->batch_ms, c->bev[0], c->bev[1]));
+  c->have_density = c->have_forces = 0;
+  return MGP_OK;
+}
+
+extern "C" double mgp_batch_ms(mgp_ctx *c, int what) {
+  if (!c) return -1.0;
+  return what == 0 ? c->batch_ms : c->batch_ic_ms;
+}
+
+extern "C" int mgp_batch_graph_nodes(mgp_ctx *c) {
+  if (!c || !c->graph) return -1;
+  size_t n = 0;
+  if (cudaGraphGetNodes(c->graph, NULL, &n) != cudaSuccess) return -1;
+  return (int)n;
+}
+
+extern "C" int mgp_batch_pofk(mgp_ctx *c, int box, int step, int cap, int *nbins, double *k, double *pk,
+                              double *kmean, double *n) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  if (!c->pk_hist || !c->p.pofk_compute_every_step) return mgp_set_error(MGP_ESTATE, "no batch P(k) recorded");
+  if (box < 0 || box >= c->nbox || step < 0 || step > c->graph_nsteps)
+    return mgp_set_error(MGP_EINVAL, "box %d / step %d out of range", box, step);
+  const int nb = c->pk_nbins;
+  if (nbins) *nbins = nb;
+  if (cap < nb) return mgp_set_error(MGP_EINVAL, "P(k) capacity %d < %d bins", cap, nb);
+  MGP_CUDA(cudaSetDevice(c->device));
+  MGP_CUDA(cudaStreamSynchronize(c->stream));
+  MGP_CUDA(cudaMemcpy(c->pk_host, c->pk_hist + ((size_t)step * c->nbox + box) * nb, sizeof(double) * nb,
+                      cudaMemcpyDeviceToHost));
+  const double N = c->g.N, bx = c->p.Box;
+  const double norm = pow(bx, 3) / pow(N, 6), shot = pow(bx / (double)c->Ns, 3);
+  for (int b = 0; b < nb; b++) {
+    double P = 0.0, K = 0.0;
+    if (c->pk_n[b] > 0) {
+      P = c->pk_host[b] / c->pk_n[b] * norm;
+      if (c->pk_sub) P -= shot;
+      K = c->pk_k[b] / c->pk_n[b] * 2.0 * M_PI / bx;
+    }
+    if (k) k[b] = k_from_index(b, c->pk_kmin, c->pk_kmax, nb, c->pk_bintype, bx);
+    if (pk) pk[b] = P;
+    if (kmean) kmean[b] = K;
+    if (n) n[b] = c->pk_n[b];
+  }
+  return MGP_OK;
+}
+
+extern "C" int mgp_batch_get_particles(mgp_ctx *c, int box, float *pos, float *vel, size_t np) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  if (box < 0 || box >= c->nbox) return mgp_set_error(MGP_EINVAL, "box %d out of range", box);
+  if ((long long)np != c->np) return mgp_set_error(MGP_EINVAL, "np = %zu, a box holds %lld", np, c->np);
+  MGP_CUDA(cudaSetDevice(c->device));
+  RET_IF(ensure_stage(c));
+  const size_t bytes = sizeof(float) * 3 * np, po = (size_t)box * 3 * np;
+  float *dpos = c->stage, *dvel = c->stage + 3 * np;
+  RET_IF(mgp_launch_positions(c->s + po, c->dstate + box, c->np, c->Ns, c->p.Box, pos ? dpos : NULL,
+                              vel ? dvel : NULL, c->v + po, c->stream));
+  if (pos) MGP_CUDA(cudaMemcpyAsync(pos, dpos, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (vel) MGP_CUDA(cudaMemcpyAsync(vel, dvel, bytes, cudaMemcpyDeviceToHost, c->stream));
+  MGP_CUDA(cudaStreamSynchronize(c->stream));
+  return MGP_OK;
+}

@@ -43,6 +43,16 @@ typedef struct mgp_grid_geom {
   long long ncomplex;   /* N*N*NH complex values */
 } mgp_grid_geom;
 
+/* Per-box scalars of a batch of independent boxes (mgp_batch): one entry per
+ * box, read by the batched kernels in place of their by-value scalars. */
+typedef struct {
+  float kick_d1, kick_d2, dD1, dD2; /* growth-dependent Kick/Drift factors (mgp_kd_args) */
+  float phicrit;                    /* potential screening phi_crit(a) */
+  float mass2;                      /* a^2 m^2(a) in RK units (force pass, mg_kind 1) */
+  float coupling;                   /* force-pass or density-screening coupling */
+  float pref;                       /* density-screening prefactor */
+} mgp_box_scalars;
+
 struct mgp_ctx {
   mgp_params p;
   mgp_cosmo cosmo;
@@ -101,6 +111,24 @@ struct mgp_ctx {
   float *sd_tab;            /* device: float4 per integer |k|^2 */
   long long sd_nmax;        /* largest integer |k|^2 = 3 (N/2)^2 */
 
+  /* batch of independent boxes (mgp_batch_create; nbox = 1 otherwise).
+   * Every particle array and grid holds nbox boxes back to back; box b has
+   * its own parameters (seed, IC flags, f(R) fR0 or nDGP rcH0) and growth
+   * tables, all boxes share Nmesh, Nsample, Box and the background H(a). */
+  int nbox;
+  mgp_params *box_p;        /* host: per-box parameters (nbox) */
+  mgp_cosmo *box_cosmo;     /* host: per-box cosmologies for boxes 1..nbox-1 */
+  cufftHandle plan_r2c_oop_b, plan_r2c_ip_b, plan_c2r_b, plan_c2r_frc_b; /* batched over boxes */
+  mgp_box_scalars *box_bs;  /* device: [nsteps+1][nbox] per-step scalars */
+  double *pk_hist;          /* device: [nsteps+1][nbox][nbins] P(k) bin sums */
+  int hist_steps;           /* capacity of box_bs / pk_hist in steps */
+  cudaGraph_t graph;
+  cudaGraphExec_t graph_exec;
+  int graph_nsteps;
+  double graph_zf;
+  cudaEvent_t bev[2];
+  float batch_ms, batch_ic_ms;
+
   /* timing */
   int timing;
   cudaEvent_t ev[MGP_NTIMERS][2];
@@ -143,6 +171,11 @@ int mgp_set_error(int code, const char *fmt, ...);
   } while (0)
 
 /* ------------------------------------------------------------ launchers */
+/* Launchers that take `nbox` run the same kernel over nbox boxes laid out
+ * back to back (grids g_bs floats apart, particles 3 Np floats apart), the box
+ * being blockIdx.y; `bs` (device, nbox entries) replaces the by-value
+ * scalars when non-NULL. */
+int mgp_blocks_per_box(long long n_per_box, int per_sm, int nbox);
 /* Per-launch scalars of the fused MtoParticles + Kick + Drift kernel. */
 typedef struct {
   float scale;        /* N / Box */
@@ -179,26 +212,32 @@ int mgp_sd_init_particles(mgp_ctx *c);
 
 int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st);
 int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box,
-                   float wpar, float *rho, long long P, cudaStream_t stream);
+                   float wpar, float *rho, long long P, cudaStream_t stream, int nbox = 1, long long g_bs = 0);
 int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins,
                     double *block_part, int nblocks, double *sums, cudaStream_t st);
 int mgp_launch_pofk_thr(const float *dk, int N, const int *thr, const float *win, int nbins, int bintype, double kmin,
                         double kmax, double *block_part, int nblocks, double *sums, int fuse_kind, int filter,
-                        float *fuse_out, float fuse_a, float fuse_b, cudaStream_t st);
+                        float *fuse_out, float fuse_a, float fuse_b, cudaStream_t st, int nbox = 1,
+                        long long g_bs = 0, long long sum_bs = 0);
 int mgp_launch_forces(const float *dk, const float *mgk, float mg_coupling, float mg_mass2, int mg_kind,
-                      int N, double box, float *frc, long long grid_floats, cudaStream_t st);
+                      int N, double box, float *frc, long long grid_floats, cudaStream_t st, int nbox = 1,
+                      const mgp_box_scalars *bs = NULL);
 int mgp_launch_ikd(const float *frc, long long grid_floats, int N, long long P, int Ns, long long np,
                    float *s, float *v, const float *D1, const float *D2, mgp_dstate *dst,
-                   double *partials, int nblocks, const mgp_kd_args *a, cudaStream_t st);
+                   double *partials, int nblocks, const mgp_kd_args *a, cudaStream_t st, int nbox = 1,
+                   const mgp_box_scalars *bs = NULL);
 int mgp_ikd_blocks(long long np);
 long long mgp_kernel_launches(void);
 
 /* MG real-space and k-space passes */
-int mgp_launch_div_laplacian(const float *dk, float *out, int N, float norm, cudaStream_t st);
-int mgp_launch_smooth(const float *dk, float *out, int N, int filter, float kR_per_sqrtRK, float norm, cudaStream_t st);
-int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float phicrit, cudaStream_t st);
+int mgp_launch_div_laplacian(const float *dk, float *out, int N, float norm, cudaStream_t st, int nbox = 1,
+                             long long g_bs = 0);
+int mgp_launch_smooth(const float *dk, float *out, int N, int filter, float kR_per_sqrtRK, float norm, cudaStream_t st,
+                      int nbox = 1, long long g_bs = 0);
+int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float phicrit, cudaStream_t st,
+                                int nbox = 1, const mgp_box_scalars *bs = NULL);
 int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float coupling, float pref,
-                              cudaStream_t st);
+                              cudaStream_t st, int nbox = 1, const mgp_box_scalars *bs = NULL);
 int mgp_launch_scale_complex(float *c, long long ncomplex, float factor, cudaStream_t st);
 
 /* IC */

@@ -39,6 +39,16 @@ static int blocks_for(long long n, int per_sm) {
   return (int)b;
 }
 int mgp_blocks_for(long long n, int per_sm) { return blocks_for(n, per_sm); }
+// Grid over `nbox` independent boxes: blockIdx.y is the box, and the x
+// blocks of all boxes together stay near the single-box budget.
+static dim3 grid_boxes(long long n_per_box, int per_sm, int nbox) {
+  long long b = (n_per_box + MGP_THREADS - 1) / MGP_THREADS;
+  long long cap = ((long long)sm_count() * per_sm + nbox - 1) / nbox;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return dim3((unsigned)b, (unsigned)nbox);
+}
+int mgp_blocks_per_box(long long n_per_box, int per_sm, int nbox) { return (int)grid_boxes(n_per_box, per_sm, nbox).x; }
 
 // -------------------------------------------------------------- helpers
 // Lattice coordinates of particle p (src/main.c:257-262 ordering).
@@ -93,7 +103,11 @@ int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st) {
 // x-slice exchange of auxPM.c:350-356 is the x wrap).
 __global__ void __launch_bounds__(MGP_THREADS) k_cic(const float *__restrict__ s, const mgp_dstate *__restrict__ st,
                                                      long long np, int Ns, int N, float scale, float wpar,
-                                                     float *__restrict__ rho, long long P) {
+                                                     float *__restrict__ rho, long long P, long long g_bs) {
+  // box blockIdx.y of a batch: particles 3 np apart, grids g_bs floats apart
+  s += blockIdx.y * 3 * np;
+  st += blockIdx.y;
+  rho += blockIdx.y * g_bs;
   const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
   const float *sx = s, *sy = s + np, *sz = s + 2 * np;
   long long stride = (long long)gridDim.x * blockDim.x;
@@ -122,8 +136,8 @@ __global__ void __launch_bounds__(MGP_THREADS) k_cic(const float *__restrict__ s
 }
 
 int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box, float wpar,
-                   float *rho, long long P, cudaStream_t stream) {
-  k_cic<<<blocks_for(np, 8), MGP_THREADS, 0, stream>>>(s, st, np, Ns, N, (float)(N / box), wpar, rho, P);
+                   float *rho, long long P, cudaStream_t stream, int nbox, long long g_bs) {
+  k_cic<<<grid_boxes(np, 8, nbox), MGP_THREADS, 0, stream>>>(s, st, np, Ns, N, (float)(N / box), wpar, rho, P, g_bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -162,6 +176,8 @@ struct mgp_pofk_kargs {
   float2 *fuse_out;
   float fuse_a, fuse_b;
   int priv;
+  long long dk_bs;     // box stride of dk / fuse_out (complex values)
+  long long part_bs;   // box stride of block_part (doubles)
 };
 
 // Bin sums: native FP32 shared-memory atomics made exact to second order by
@@ -173,6 +189,9 @@ struct mgp_pofk_kargs {
 __global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
   extern __shared__ float shf[];
   const int N = a.N, nbins = a.nbins, NH = N / 2 + 1, h = N / 2;
+  const float2 *__restrict__ dkb = a.dk + blockIdx.y * a.dk_bs;
+  float2 *__restrict__ fob = a.fuse_out ? a.fuse_out + blockIdx.y * a.dk_bs : nullptr;
+  double *__restrict__ bpb = a.block_part + blockIdx.y * a.part_bs;
   const int nwb = a.priv ? (int)(blockDim.x >> 5) : 1;
   float *shi0 = shf, *slo0 = shf + nwb * nbins;
   int *sthr = (int *)(slo0 + nwb * nbins);
@@ -235,13 +254,13 @@ __global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
         float2 z[4];
 #pragma unroll
         for (int t = 0; t < 4; t++)
-          if (use[t]) z[t] = a.dk[rows[t] * NH + kz];
+          if (use[t]) z[t] = dkb[rows[t] * NH + kz];
         float p2 = 0.0f;
 #pragma unroll
         for (int t = 0; t < 4; t++)
           if (use[t]) {
             p2 += z[t].x * z[t].x + z[t].y * z[t].y;
-            if (a.fuse_kind) a.fuse_out[rows[t] * NH + kz] = make_float2(f * z[t].x, f * z[t].y);
+            if (a.fuse_kind) fob[rows[t] * NH + kz] = make_float2(f * z[t].x, f * z[t].y);
           }
         if (bin >= 0) {
           float w = (kz == 0 || 2 * kz == N) ? 1.0f : 2.0f;
@@ -277,12 +296,15 @@ __global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
   for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
     double t = 0.0;
     for (int w = 0; w < nwb; w++) t += (double)shi0[w * nbins + b] + (double)slo0[w * nbins + b];
-    a.block_part[(long long)blockIdx.x * nbins + b] = t;
+    bpb[(long long)blockIdx.x * nbins + b] = t;
   }
 }
 
 // Deterministic cross-block sum in FP64 (the MPI_Allreduce of compute_pofk.c:225).
-__global__ void k_pofk_reduce(const double *__restrict__ block_part, int nblocks, int nbins, double *__restrict__ sums) {
+__global__ void k_pofk_reduce(const double *__restrict__ block_part, int nblocks, int nbins, double *__restrict__ sums,
+                              long long part_bs, long long sum_bs) {
+  block_part += blockIdx.y * part_bs;
+  sums += blockIdx.y * sum_bs;
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nbins) return;
   double s = 0.0;
@@ -290,7 +312,9 @@ __global__ void k_pofk_reduce(const double *__restrict__ block_part, int nblocks
   sums[b] = s;
 }
 
-static int launch_pofk(mgp_pofk_kargs ka, int nblocks, double *sums, cudaStream_t st) {
+static int launch_pofk(mgp_pofk_kargs ka, int nblocks, double *sums, cudaStream_t st, int nbox = 1,
+                       long long sum_bs = 0) {
+  ka.part_bs = (long long)nblocks * ka.nbins;
   const int h = ka.N / 2;
   ka.priv = (size_t)ka.nbins * (MGP_THREADS / 32) * 2 * sizeof(float) <= 96 * 1024;
   size_t shmem = 2 * sizeof(float) * (size_t)ka.nbins * (ka.priv ? MGP_THREADS / 32 : 1) +
@@ -299,10 +323,11 @@ static int launch_pofk(mgp_pofk_kargs ka, int nblocks, double *sums, cudaStream_
     if (cudaFuncSetAttribute(k_pofk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem) != cudaSuccess)
       return mgp_set_error(MGP_EINVAL, "P(k) needs %zu bytes of shared memory", shmem);
   }
-  k_pofk<<<nblocks, MGP_THREADS, shmem, st>>>(ka);
+  k_pofk<<<dim3(nblocks, nbox), MGP_THREADS, shmem, st>>>(ka);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
-  k_pofk_reduce<<<(ka.nbins + 127) / 128, 128, 0, st>>>(ka.block_part, nblocks, ka.nbins, sums);
+  k_pofk_reduce<<<dim3((ka.nbins + 127) / 128, nbox), 128, 0, st>>>(ka.block_part, nblocks, ka.nbins, sums, ka.part_bs,
+                                                                   sum_bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -323,7 +348,8 @@ int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win,
 
 int mgp_launch_pofk_thr(const float *dk, int N, const int *thr, const float *win, int nbins, int bintype, double kmin,
                         double kmax, double *block_part, int nblocks, double *sums, int fuse_kind, int filter,
-                        float *fuse_out, float fuse_a, float fuse_b, cudaStream_t st) {
+                        float *fuse_out, float fuse_a, float fuse_b, cudaStream_t st, int nbox, long long g_bs,
+                        long long sum_bs) {
   mgp_pofk_kargs ka;
   memset(&ka, 0, sizeof(ka));
   ka.dk = (const float2 *)dk;
@@ -340,7 +366,8 @@ int mgp_launch_pofk_thr(const float *dk, int N, const int *thr, const float *win
   ka.fuse_out = (float2 *)fuse_out;
   ka.fuse_a = fuse_a;
   ka.fuse_b = fuse_b;
-  return launch_pofk(ka, nblocks, sums, st);
+  ka.dk_bs = g_bs / 2;
+  return launch_pofk(ka, nblocks, sums, st, nbox, sum_bs);
 }
 
 // ------------------------------------------------------------ force grids
@@ -360,7 +387,21 @@ int mgp_launch_pofk_thr(const float *dk, int N, const int *thr, const float *win
 __global__ void __launch_bounds__(MGP_THREADS) k_forces(const float2 *__restrict__ dk, const float2 *__restrict__ mgk,
                                                         float mg_coupling, float mg_mass2, int mg_kind, int N,
                                                         float cfac, float2 *__restrict__ fx, float2 *__restrict__ fy,
-                                                        float2 *__restrict__ fz) {
+                                                        float2 *__restrict__ fz, long long g_bs,
+                                                        const mgp_box_scalars *__restrict__ bs) {
+  {
+    // box blockIdx.y: input grids g_bs floats apart, the three force grids 3 g_bs
+    const long long o = blockIdx.y * (g_bs / 2);
+    dk += o;
+    if (mgk) mgk += o;
+    fx += 3 * o;
+    fy += 3 * o;
+    fz += 3 * o;
+    if (bs) {
+      mg_coupling = bs[blockIdx.y].coupling;
+      mg_mass2 = bs[blockIdx.y].mass2;
+    }
+  }
   const int NH = N / 2 + 1;
   const long long total = (long long)N * N * NH;
   (void)total;
@@ -404,13 +445,14 @@ __global__ void __launch_bounds__(MGP_THREADS) k_forces(const float2 *__restrict
 }
 
 int mgp_launch_forces(const float *dk, const float *mgk, float mg_coupling, float mg_mass2, int mg_kind, int N,
-                      double box, float *frc, long long grid_floats, cudaStream_t st) {
+                      double box, float *frc, long long grid_floats, cudaStream_t st, int nbox,
+                      const mgp_box_scalars *bs) {
   const long long total = (long long)N * N * (N / 2 + 1);
   double scale = 2.0 * M_PI / box;
   float cfac = (float)(-1.0 / ((double)N * N * N * scale));
   float2 *fx = (float2 *)frc, *fy = (float2 *)(frc + grid_floats), *fz = (float2 *)(frc + 2 * grid_floats);
-  k_forces<<<blocks_for(total, 8), MGP_THREADS, 0, st>>>((const float2 *)dk, (const float2 *)mgk, mg_coupling,
-                                                         mg_mass2, mg_kind, N, cfac, fx, fy, fz);
+  k_forces<<<grid_boxes(total, 8, nbox), MGP_THREADS, 0, st>>>((const float2 *)dk, (const float2 *)mgk, mg_coupling,
+                                                               mg_mass2, mg_kind, N, cfac, fx, fy, fz, grid_floats, bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -444,8 +486,26 @@ template <typename IDX>
 __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
     const float *__restrict__ frc, long long gf, int N, long long P, int Ns, long long np, float *__restrict__ s,
     float *__restrict__ v, const float *__restrict__ D1, const float *__restrict__ D2,
-    const mgp_dstate *__restrict__ st, double *__restrict__ partials, mgp_kd_args a) {
+    const mgp_dstate *__restrict__ st, double *__restrict__ partials, mgp_kd_args a,
+    const mgp_box_scalars *__restrict__ bs) {
   __shared__ double sh[MGP_THREADS / 32];
+  {
+    // box blockIdx.y of a batch: force grids 3 gf apart, particle arrays 3 np
+    const int bx = blockIdx.y;
+    frc += bx * 3 * gf;
+    s += bx * 3 * np;
+    v += bx * 3 * np;
+    D1 += bx * 3 * a.lpt_stride;
+    D2 += bx * 3 * a.lpt_stride;
+    st += bx;
+    partials += (long long)bx * gridDim.x * 6;
+    if (bs) {
+      a.kick_d1 = bs[bx].kick_d1;
+      a.kick_d2 = bs[bx].kick_d2;
+      a.dD1 = bs[bx].dD1;
+      a.dD2 = bs[bx].dD2;
+    }
+  }
   const float ox = (float)(st->cx[0] * a.scale), oy = (float)(st->cx[1] * a.scale), oz = (float)(st->cx[2] * a.scale);
   const float *F0 = frc, *F1 = frc + gf, *F2 = frc + 2 * gf;
   const IDX Pi = (IDX)P, NPi = (IDX)N * (IDX)P;
@@ -501,6 +561,8 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
 __global__ void k_finalize_kd(mgp_dstate *st, const double *__restrict__ partials, int nblocks, double inv_np,
                               double dda_omega, double dyyy, int do_drift) {
   __shared__ double sh[6][MGP_THREADS / 32];
+  st += blockIdx.x;  // one block per box
+  partials += (long long)blockIdx.x * nblocks * 6;
   double acc[6] = {0, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
     for (int q = 0; q < 6; q++) acc[q] += partials[(long long)b * 6 + q];
@@ -531,16 +593,17 @@ int mgp_ikd_blocks(long long np) { return blocks_for(np, 8); }
 
 int mgp_launch_ikd(const float *frc, long long gf, int N, long long P, int Ns, long long np, float *s, float *v,
                    const float *D1, const float *D2, mgp_dstate *dst, double *partials, int nblocks,
-                   const mgp_kd_args *a, cudaStream_t st) {
+                   const mgp_kd_args *a, cudaStream_t st, int nbox, const mgp_box_scalars *bs) {
+  const dim3 g(nblocks, nbox);
   if (gf < (1LL << 31))
-    k_interp_kick_drift<int><<<nblocks, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a);
+    k_interp_kick_drift<int><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a, bs);
   else
-    k_interp_kick_drift<long long><<<nblocks, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials,
-                                                                   *a);
+    k_interp_kick_drift<long long><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a,
+                                                             bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
-  k_finalize_kd<<<1, MGP_THREADS, 0, st>>>(dst, partials, nblocks, 1.0 / (double)np, a->dda_omega, a->dyyy_d,
-                                           a->do_drift);
+  k_finalize_kd<<<nbox, MGP_THREADS, 0, st>>>(dst, partials, nblocks, 1.0 / (double)np, a->dda_omega, a->dyyy_d,
+                                              a->do_drift);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -556,7 +619,10 @@ int mgp_launch_finalize_kd(mgp_dstate *dst, const double *partials, int nblocks,
 
 // --------------------------------------------------------- MG passes
 // DivideByLaplacian (src/mg.h:21-64): Phi_N(k) = -norm * delta(k) / RK.
-__global__ void k_div_laplacian(const float2 *__restrict__ dk, float2 *__restrict__ out, int N, float norm) {
+__global__ void k_div_laplacian(const float2 *__restrict__ dk, float2 *__restrict__ out, int N, float norm,
+                                long long g_bs) {
+  dk += blockIdx.y * (g_bs / 2);
+  out += blockIdx.y * (g_bs / 2);
   const int NH = N / 2 + 1;
   const long long total = (long long)N * N * NH;
   (void)total;
@@ -578,9 +644,10 @@ __global__ void k_div_laplacian(const float2 *__restrict__ dk, float2 *__restric
   }
 }
 
-int mgp_launch_div_laplacian(const float *dk, float *out, int N, float norm, cudaStream_t st) {
+int mgp_launch_div_laplacian(const float *dk, float *out, int N, float norm, cudaStream_t st, int nbox,
+                             long long g_bs) {
   const long long total = (long long)N * N * (N / 2 + 1);
-  k_div_laplacian<<<blocks_for(total, 8), MGP_THREADS, 0, st>>>((const float2 *)dk, (float2 *)out, N, norm);
+  k_div_laplacian<<<grid_boxes(total, 8, nbox), MGP_THREADS, 0, st>>>((const float2 *)dk, (float2 *)out, N, norm, g_bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -588,7 +655,9 @@ int mgp_launch_div_laplacian(const float *dk, float *out, int N, float norm, cud
 
 // SmoothDensityField (src/mg.h:268-309) with smoothing_filter (mg.h:318-338).
 __global__ void k_smooth(const float2 *__restrict__ dk, float2 *__restrict__ out, int N, int filter, float kR1,
-                         float norm) {
+                         float norm, long long g_bs) {
+  dk += blockIdx.y * (g_bs / 2);
+  out += blockIdx.y * (g_bs / 2);
   const int NH = N / 2 + 1;
   const long long total = (long long)N * N * NH;
   (void)total;
@@ -614,9 +683,11 @@ __global__ void k_smooth(const float2 *__restrict__ dk, float2 *__restrict__ out
   }
 }
 
-int mgp_launch_smooth(const float *dk, float *out, int N, int filter, float kR1, float norm, cudaStream_t st) {
+int mgp_launch_smooth(const float *dk, float *out, int N, int filter, float kR1, float norm, cudaStream_t st,
+                      int nbox, long long g_bs) {
   const long long total = (long long)N * N * (N / 2 + 1);
-  k_smooth<<<blocks_for(total, 8), MGP_THREADS, 0, st>>>((const float2 *)dk, (float2 *)out, N, filter, kR1, norm);
+  k_smooth<<<grid_boxes(total, 8, nbox), MGP_THREADS, 0, st>>>((const float2 *)dk, (float2 *)out, N, filter, kR1, norm,
+                                                               g_bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -633,7 +704,12 @@ __device__ __forceinline__ float screen_pot(float ph, float phicrit) {
   }
   return f;
 }
-__global__ void k_screen_potential(float *__restrict__ rho, const float *__restrict__ phi, long long n, float phicrit) {
+__global__ void k_screen_potential(float *__restrict__ rho, const float *__restrict__ phi, long long n, float phicrit,
+                                   const mgp_box_scalars *__restrict__ bs) {
+  // box blockIdx.y: grids n floats apart
+  rho += blockIdx.y * n;
+  phi += blockIdx.y * n;
+  if (bs) phicrit = bs[blockIdx.y].phicrit;
   long long stride = (long long)gridDim.x * blockDim.x;
   long long n4 = n >> 2;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
@@ -648,8 +724,9 @@ __global__ void k_screen_potential(float *__restrict__ rho, const float *__restr
     rho[i] *= screen_pot(phi[i], phicrit);
 }
 
-int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float phicrit, cudaStream_t st) {
-  k_screen_potential<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>(rho, phi, n, phicrit);
+int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float phicrit, cudaStream_t st, int nbox,
+                                const mgp_box_scalars *bs) {
+  k_screen_potential<<<grid_boxes(n, 8, nbox), MGP_THREADS, 0, st>>>(rho, phi, n, phicrit, bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -663,7 +740,14 @@ __device__ __forceinline__ float screen_den(float dsm, float pref) {
   return fac < 1e-5f ? 1.0f : 2.0f * (sqrtf(1.0f + fac) - 1.0f) / fac;
 }
 __global__ void k_screen_density(float *__restrict__ rho, const float *__restrict__ dsm, long long n, float coupling,
-                                 float pref) {
+                                 float pref, const mgp_box_scalars *__restrict__ bs) {
+  // box blockIdx.y: grids n floats apart
+  rho += blockIdx.y * n;
+  dsm += blockIdx.y * n;
+  if (bs) {
+    coupling = bs[blockIdx.y].coupling;
+    pref = bs[blockIdx.y].pref;
+  }
   long long stride = (long long)gridDim.x * blockDim.x;
   long long n4 = n >> 2;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
@@ -678,8 +762,9 @@ __global__ void k_screen_density(float *__restrict__ rho, const float *__restric
     rho[i] *= coupling * screen_den(dsm[i], pref);
 }
 
-int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float coupling, float pref, cudaStream_t st) {
-  k_screen_density<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>(rho, dsm, n, coupling, pref);
+int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float coupling, float pref, cudaStream_t st,
+                              int nbox, const mgp_box_scalars *bs) {
+  k_screen_density<<<grid_boxes(n, 8, nbox), MGP_THREADS, 0, st>>>(rho, dsm, n, coupling, pref, bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -1176,7 +1261,7 @@ int mgp_launch_pofk_mu(const float *dk, int N, const int *rk_bin, const float *w
   k_pofk_mu<<<nblocks, MGP_THREADS, shmem, st>>>((const float2 *)dk, N, rk_bin, win, nbins, block_part);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
-  k_pofk_reduce<<<(3 * nbins + 127) / 128, 128, 0, st>>>(block_part, nblocks, 3 * nbins, sums);
+  k_pofk_reduce<<<(3 * nbins + 127) / 128, 128, 0, st>>>(block_part, nblocks, 3 * nbins, sums, 0, 0);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;

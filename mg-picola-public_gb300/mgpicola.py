@@ -23,7 +23,8 @@ EXPORTS = [
     "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
     "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_launch_count",
     "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
-    "mgp_growth_scaledependent",
+    "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
+    "mgp_batch_ms", "mgp_batch_graph_nodes",
 ]
 
 # field types of mgp_assign_displacement_fields (src/proto.h:155-158)
@@ -59,6 +60,12 @@ class Params(C.Structure):
         ("Noutputs", C.c_int), ("output_redshift", C.c_double * 64), ("output_nsteps", C.c_int * 64),
         ("sd_nk", C.c_int), ("sd_kmin", C.c_double), ("sd_kmax", C.c_double),
     ]
+
+
+class BoxParams(C.Structure):
+    """struct mgp_box_params: the per-box overrides of a batch."""
+    _fields_ = [("Seed", C.c_int), ("inverted_initial_condition", C.c_int),
+                ("amplitude_fixed_initial_condition", C.c_int), ("fofr0", C.c_double), ("rcH0_DGP", C.c_double)]
 
 
 class MGPError(RuntimeError):
@@ -105,6 +112,13 @@ def lib():
         L.mgp_cosmo_coeff.argtypes = [C.POINTER(Params), C.c_int, dp, dp, dp, C.c_int, dp]
         L.mgp_growth_scaledependent.argtypes = [C.POINTER(Params), C.c_int, dp, dp, C.c_int, dp]
         L.mgp_assign_displacement_fields.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_int)]
+        L.mgp_batch_create.argtypes = [C.POINTER(Params), C.c_int, C.POINTER(BoxParams), C.c_int, C.POINTER(vp)]
+        L.mgp_batch_run.argtypes = [vp, C.c_int, C.c_double]
+        L.mgp_batch_pofk.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), dp, dp, dp, dp]
+        L.mgp_batch_get_particles.argtypes = [vp, C.c_int, vp, vp, C.c_size_t]
+        L.mgp_batch_ms.argtypes = [vp, C.c_int]
+        L.mgp_batch_ms.restype = C.c_double
+        L.mgp_batch_graph_nodes.argtypes = [vp]
         L.mgp_power_spectrum.argtypes = [vp, C.c_double]
         L.mgp_power_spectrum.restype = C.c_double
         L.mgp_copy_grid.argtypes = [vp, C.c_int, fp, C.c_size_t]
@@ -305,3 +319,55 @@ class Context:
 
     def launches(self):
         return lib().mgp_launch_count(self.h)
+
+
+class Batch:
+    """A batch of independent boxes run in lock step (mgp_batch_*)."""
+
+    def __init__(self, params, boxes, device=0):
+        self.p = params
+        arr = (BoxParams * len(boxes))()
+        for i, b in enumerate(boxes):
+            arr[i] = BoxParams(int(b.get("Seed", params.Seed)), int(b.get("inverted", 0)), int(b.get("fixed", 0)),
+                               float(b.get("fofr0", 0.0)), float(b.get("rcH0", 0.0)))
+        self.nbox = len(boxes)
+        self.h = C.c_void_p()
+        _check(lib().mgp_batch_create(C.byref(params), self.nbox, arr, device, C.byref(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mgp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def run(self, nsteps, z_final=0.0):
+        _check(lib().mgp_batch_run(self.h, nsteps, z_final))
+
+    def pofk(self, box, step):
+        cap = max(self.p.pofk_nbins, self.p.Nmesh) if self.p.pofk_nbins > 0 else self.p.Nmesh
+        k, pk, km, n = (np.zeros(cap) for _ in range(4))
+        nb = C.c_int(0)
+        _check(lib().mgp_batch_pofk(self.h, box, step, cap, C.byref(nb), _dptr(k), _dptr(pk), _dptr(km), _dptr(n)))
+        m = nb.value
+        return k[:m], pk[:m], km[:m], n[:m]
+
+    def particles(self, box):
+        n = self.p.Nsample ** 3
+        pos = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        _check(lib().mgp_batch_get_particles(self.h, box, pos.ctypes.data, vel.ctypes.data, n))
+        return pos, vel
+
+    def ms(self, what=0):
+        return lib().mgp_batch_ms(self.h, what)
+
+    def graph_nodes(self):
+        return lib().mgp_batch_graph_nodes(self.h)
