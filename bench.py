@@ -39,7 +39,22 @@ CONFIGS = {
     "ndgp_512_1024": dict(Ns=512, N=1024, Box=1024.0, model="dgp", nsteps=50, seed=5003, fixed=1, nbins=512),
     "ndgp_256_512": dict(Ns=256, N=512, Box=512.0, model="dgp", nsteps=50, seed=5003, fixed=1, nbins=256),
     "lcdm_64_128": dict(Ns=64, N=128, Box=256.0, model="lcdm", nsteps=10, seed=5001, fixed=0, nbins=64),
+    # 64 independent f(R) boxes (seeds 6001-6032, each normal + inverted,
+    # |fR0| log-uniform in [1e-6, 1e-4]) in one batch, one graph launch per run
+    "fofr_batch_64x64_128": dict(Ns=64, N=128, Box=256.0, model="fofr", nsteps=20, seed=6001, fixed=0, nbins=64,
+                                 batch=64),
 }
+
+# |fR0| of the batch: one value per seed pair, drawn log-uniform in [1e-6, 1e-4]
+# by numpy's PCG64 with this seed.
+BATCH_FR0_SEED = 20260604
+
+
+def batch_boxes(cfg):
+    rng = np.random.default_rng(BATCH_FR0_SEED)
+    f0 = 10 ** rng.uniform(-6.0, -4.0, cfg["batch"] // 2)
+    return [dict(Seed=cfg["seed"] + i, inverted=inv, fofr0=float(f0[i])) for i in range(cfg["batch"] // 2)
+            for inv in (0, 1)]
 
 
 def make_params(M, cfg):
@@ -51,7 +66,72 @@ def make_params(M, cfg):
     if cfg["model"] == "dgp":
         kw.update(model=M.MODEL_DGP, modified_gravity_active=1, include_screening=1, rcH0_DGP=1.0, Rsmooth=1.0,
                   smoothing_filter=M.FILTER_GAUSSIAN, input_pofk_is_for_lcdm=1, input_sigma8_is_for_lcdm=1)
+    elif cfg["model"] == "fofr":
+        kw.update(model=M.MODEL_FOFR, modified_gravity_active=1, include_screening=1, fofr0=1e-5, nfofr=1.0,
+                  input_pofk_is_for_lcdm=1, input_sigma8_is_for_lcdm=1)
     return M.default_params(**kw)
+
+
+def run_batch(args, cfg):
+    """A batch of independent boxes: each timed step is one graph launch that
+    runs the whole KDK loop of every box; value counts particle-steps of all
+    boxes (drift steps; the final output kick is included in the time)."""
+    import mgpicola as M
+
+    p = make_params(M, cfg)
+    boxes = batch_boxes(cfg)
+    B, Np, nst = len(boxes), cfg["Ns"] ** 3, cfg["nsteps"]
+    batch = M.Batch(p, boxes)
+    for _ in range(args.warmup):
+        batch.run(nst)
+    launches = batch.graph_kernels()
+    times, walls = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            batch.run(nst)
+            pk = [batch.pofk(b, nst)[1] for b in range(B)]  # the per-box results, read back every run
+            walls.append(time.perf_counter() - t0)
+            times.append(batch.ms(0))
+    ic_ms = batch.ms(1)
+    nodes = batch.graph_nodes()
+    batch.close()
+    ms = float(np.mean(times))
+    value = B * Np * nst / (ms * 1e-3) / 1e6
+    wall = float(np.mean(walls))
+    N = cfg["N"]
+    Nc = N ** 3
+    # minimum HBM bytes per box-step of the f(R) step with screening and P(k)
+    # (FP32): 84 Np particle traffic + 92 Nc grid traffic incl. the six FFTs
+    abytes = (84 * Np + 92 * Nc) * B
+    achieved = abytes / (ms * 1e-3 / nst) / 1e9
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    out = {
+        "metric": "Mparticle-steps/s of a batch of independent boxes", "value": round(value, 3), "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / nst, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (2LPT ICs generated on the device, seeds 6001-6032 normal + inverted)",
+        "config": {"workload": args.config, "boxes": B, "particles_per_box": Np, "mesh": N, "box_mpc_h": cfg["Box"],
+                   "model": "f(R) Hu-Sawicki n=1, screening, |fR0| log-uniform [1e-6, 1e-4] (seed %d)" % BATCH_FR0_SEED,
+                   "steps_per_run": nst, "pofk_every_step": True, "pofk_bins": cfg["nbins"],
+                   "l2": "working set %.1f GB > L2" % (B * (6 * 4 * N * N * 2 * (N // 2 + 1) + 48 * Np) / 1e9)},
+        "e2e": {"value": round(B * Np * nst / wall / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(B * cfg["nbins"] * 8 / nst), "api": "mgp_batch_run + mgp_batch_pofk",
+                "includes": "2LPT ICs of all boxes, graph launch, per-box P(k) read-back"},
+        "gpu_launches": int(launches * args.steps),
+        "graph": {"launches_per_run": 1, "nodes": nodes, "own_kernels": launches, "ic_ms": round(ic_ms, 3)},
+        "per_box_completion_ms": {"p50": round(ms, 3), "p99": round(ms, 3),
+                                  "note": "lock step: every box finishes with the graph"},
+        "roofline": {"bound": "hbm", "kernel": "whole step (FFTs included)", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "algorithmic_bytes_per_step": abytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args)
+    print(json.dumps(out))
 
 
 class ClockSampler:
@@ -131,6 +211,8 @@ def run_gpu(args):
     import mgpicola as M
 
     cfg = CONFIGS[args.config]
+    if cfg.get("batch"):
+        return run_batch(args, cfg)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -252,6 +334,8 @@ def oracle_params(O, cfg):
     rp = O.RunParams()
     if cfg["model"] == "dgp":
         rp.mg = O.make_mg(O.DGP, 0.267, rcH0=1.0, rsmooth=1.0)
+    elif cfg["model"] == "fofr":
+        rp.mg = O.make_mg(O.FOFR, 0.267, fofr0=1e-5, nfofr=1.0)
     else:
         rp.mg = O.make_mg(O.LCDM, 0.267)
     rp.pw = O.make_power(omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sigma8=0.8)
@@ -265,7 +349,9 @@ def oracle_params(O, cfg):
     return rp
 
 
-SAMPLE = {"ndgp_512_1024": "ndgp_128_256", "ndgp_256_512": "ndgp_128_256", "lcdm_64_128": "lcdm_64_128"}
+SAMPLE = {"ndgp_512_1024": "ndgp_128_256", "ndgp_256_512": "ndgp_128_256", "lcdm_64_128": "lcdm_64_128",
+          "fofr_batch_64x64_128": "fofr_64_128"}
+CONFIGS["fofr_64_128"] = dict(Ns=64, N=128, Box=256.0, model="fofr", nsteps=20, seed=6001, fixed=0, nbins=64)
 CONFIGS["ndgp_128_256"] = dict(Ns=128, N=256, Box=256.0, model="dgp", nsteps=50, seed=5003, fixed=1, nbins=128)
 
 

@@ -279,6 +279,8 @@ int mgp_batch_get_particles(mgp_ctx *ctx, int box, float *pos, float *vel, size_
  * loop (one graph launch), 1 = the ICs; and the captured graph's node count. */
 double mgp_batch_ms(mgp_ctx *ctx, int what);
 int mgp_batch_graph_nodes(mgp_ctx *ctx);
+/* this library's own kernels among them (the rest are cuFFT's) */
+int mgp_batch_graph_kernels(mgp_ctx *ctx);
 
 /* Copy an internal grid to a host buffer (diagnostics and parity tests).
  * which: 0 density (real padded [N][N][2(N/2+1)] float), 1 delta(k)

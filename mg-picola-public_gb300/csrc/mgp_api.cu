@@ -1125,6 +1125,7 @@ static int batch_build_graph(mgp_ctx *c, int nsteps, double zf) {
   c->graph_exec = NULL;
   c->graph = NULL;
   MGP_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  const long long k0 = g_kernel_launches;
   int rc = MGP_OK;
   for (int t = 0; t <= nsteps && rc == MGP_OK; t++)
     rc = batch_step_launch(c, st[t], c->box_bs + (size_t)t * c->nbox,
@@ -1137,6 +1138,7 @@ static int batch_build_graph(mgp_ctx *c, int nsteps, double zf) {
   }
   if (e != cudaSuccess) return mgp_set_error(MGP_ECUDA, "graph capture: %s", cudaGetErrorString(e));
   c->graph = g;
+  c->graph_kernels = (int)(g_kernel_launches - k0);
   MGP_CUDA(cudaGraphInstantiate(&c->graph_exec, g, 0));
   c->graph_nsteps = nsteps;
   c->graph_zf = zf;
@@ -1172,6 +1174,8 @@ extern "C" double mgp_batch_ms(mgp_ctx *c, int what) {
   if (!c) return -1.0;
   return what == 0 ? c->batch_ms : c->batch_ic_ms;
 }
+
+extern "C" int mgp_batch_graph_kernels(mgp_ctx *c) { return c && c->graph ? c->graph_kernels : -1; }
 
 extern "C" int mgp_batch_graph_nodes(mgp_ctx *c) {
   if (!c || !c->graph) return -1;

@@ -125,6 +125,7 @@ struct mgp_ctx {
   cudaGraph_t graph;
   cudaGraphExec_t graph_exec;
   int graph_nsteps;
+  int graph_kernels;        /* this library's kernels per graph launch */
   double graph_zf;
   cudaEvent_t bev[2];
   float batch_ms, batch_ic_ms;

@@ -24,7 +24,7 @@ EXPORTS = [
     "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_launch_count",
     "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
-    "mgp_batch_ms", "mgp_batch_graph_nodes",
+    "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels",
 ]
 
 # field types of mgp_assign_displacement_fields (src/proto.h:155-158)
@@ -119,6 +119,7 @@ def lib():
         L.mgp_batch_ms.argtypes = [vp, C.c_int]
         L.mgp_batch_ms.restype = C.c_double
         L.mgp_batch_graph_nodes.argtypes = [vp]
+        L.mgp_batch_graph_kernels.argtypes = [vp]
         L.mgp_power_spectrum.argtypes = [vp, C.c_double]
         L.mgp_power_spectrum.restype = C.c_double
         L.mgp_copy_grid.argtypes = [vp, C.c_int, fp, C.c_size_t]
@@ -371,3 +372,6 @@ class Batch:
 
     def graph_nodes(self):
         return lib().mgp_batch_graph_nodes(self.h)
+
+    def graph_kernels(self):
+        return lib().mgp_batch_graph_kernels(self.h)
