@@ -288,6 +288,9 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
     if (c->ev[t][0]) cudaEventDestroy(c->ev[t][0]);
     if (c->ev[t][1]) cudaEventDestroy(c->ev[t][1]);
   }
+  if (c->side) cudaStreamDestroy(c->side);
+  for (int q = 0; q < 2; q++)
+    if (c->ev_side[q]) cudaEventDestroy(c->ev_side[q]);
   if (c->stream) cudaStreamDestroy(c->stream);
   free(c->pk_n);
   free(c->pk_k);
@@ -722,6 +725,11 @@ static void kd_args(mgp_ctx *c, double AI, double AF, double A, double AFF, int 
 extern "C" int mgp_kick_drift(mgp_ctx *c, double AI, double AF, double A, double AFF, int do_drift) {
   RET_IF(require_particles(c));
   if (!c->have_forces) return mgp_set_error(MGP_ESTATE, "mgp_kick_drift before mgp_get_displacements");
+  if (c->side_pending) {
+    // velocities / LPT displacements still arriving on the side stream
+    MGP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_side[1], 0));
+    c->side_pending = 0;
+  }
   if (c->sd) {
     if (c->sd_kind[0] != MGP_FIELD_ddDddy || c->sd_a[0] != A)
       return mgp_set_error(MGP_ESTATE, "scale-dependent kick at a = %g needs the ddDddy fields at that a "
@@ -858,8 +866,18 @@ extern "C" int mgp_pofk_rsd(mgp_ctx *c, double A, int cap, int *nbins, double *k
 }
 
 // ---------------------------------------------------------- particles
-static int ensure_stage(mgp_ctx *c) {
-  if (!c->stage) MGP_CUDA(cudaMalloc(&c->stage, sizeof(float) * 6 * (size_t)c->np));
+static int ensure_stage(mgp_ctx *c, int arrays = 2) {
+  // `arrays` [np][3] float staging arrays
+  if (c->stage_arrays < arrays) {
+    if (c->stage) {
+      MGP_CUDA(cudaStreamSynchronize(c->stream));
+      cudaFree(c->stage);
+      c->stage = NULL;
+      c->stage_arrays = 0;
+    }
+    MGP_CUDA(cudaMalloc(&c->stage, sizeof(float) * 3 * arrays * (size_t)c->np));
+    c->stage_arrays = arrays;
+  }
   return MGP_OK;
 }
 
@@ -937,9 +955,45 @@ extern "C" int mgp_host_unregister(void *ptr) {
   return MGP_OK;
 }
 
+// The positions go first (the deposit needs them); the velocities and the
+// LPT displacements, which only the kick reads, are copied and converted on
+// a second stream while the deposit, the FFTs and the force pass run, and the
+// kick waits for them.
 extern "C" int mgp_step_host(mgp_ctx *c, double A, double AI, double AF, double AFF, float *pos, float *vel,
                              const float *D1, const float *D2, size_t np) {
-  RET_IF(mgp_set_particles(c, pos, vel, D1, D2, np));
+  RET_IF(require_particles(c));
+  if ((long long)np != c->np) return mgp_set_error(MGP_EINVAL, "np = %zu, context holds %lld", np, c->np);
+  if (c->sd) {
+    RET_IF(mgp_set_particles(c, pos, vel, D1, D2, np));
+  } else {
+    if (!c->side) {
+      MGP_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+      MGP_CUDA(cudaEventCreateWithFlags(&c->ev_side[0], cudaEventDisableTiming));
+      MGP_CUDA(cudaEventCreateWithFlags(&c->ev_side[1], cudaEventDisableTiming));
+    }
+    RET_IF(ensure_stage(c, 4));
+    const size_t bytes = sizeof(float) * 3 * np;
+    float *st[4] = {c->stage, c->stage + 3 * np, c->stage + 6 * np, c->stage + 9 * np};
+    if (pos) {
+      MGP_CUDA(cudaMemcpyAsync(st[0], pos, bytes, cudaMemcpyHostToDevice, c->stream));
+      RET_IF(mgp_launch_set_state(c->s, c->v, st[0], NULL, c->np, c->Ns, c->p.Box, c->stream));
+    }
+    MGP_CUDA(cudaMemsetAsync(c->dstate, 0, sizeof(mgp_dstate), c->stream));
+    // the side stream starts after everything queued so far (earlier readers
+    // of v, D1, D2 included)
+    MGP_CUDA(cudaEventRecord(c->ev_side[0], c->stream));
+    MGP_CUDA(cudaStreamWaitEvent(c->side, c->ev_side[0], 0));
+    const float *src[3] = {vel, D1, D2};
+    float *dst[3] = {c->v, c->D1, c->D2};
+    for (int q = 0; q < 3; q++) {
+      if (!src[q]) continue;
+      MGP_CUDA(cudaMemcpyAsync(st[1 + q], src[q], bytes, cudaMemcpyHostToDevice, c->side));
+      RET_IF(mgp_launch_aos_to_soa(st[1 + q], dst[q], c->np, c->side));
+    }
+    MGP_CUDA(cudaEventRecord(c->ev_side[1], c->side));
+    c->side_pending = 1;
+    c->have_density = c->have_forces = 0;
+  }
   RET_IF(mgp_step(c, A, AI, AF, AFF));
   RET_IF(mgp_get_particles(c, pos, vel, NULL, NULL, np));
   return MGP_OK;

@@ -66,7 +66,11 @@ struct mgp_ctx {
   float *s, *v, *D1, *D2;  /* each 3*np */
   mgp_dstate *dstate;      /* device */
   double *partials;        /* per-block reduction scratch (double) */
-  float *stage;            /* host-interface staging, 6*np floats (lazy) */
+  float *stage;            /* host-interface staging, stage_arrays x 3 np floats (lazy) */
+  int stage_arrays;
+  cudaStream_t side;       /* host-buffer step: copies that only the kick waits for */
+  cudaEvent_t ev_side[2];
+  int side_pending;
   int max_blocks;
 
   /* grids */
