@@ -282,6 +282,40 @@ int mgp_batch_graph_nodes(mgp_ctx *ctx);
 /* this library's own kernels among them (the rest are cuFFT's) */
 int mgp_batch_graph_kernels(mgp_ctx *ctx);
 
+/* Learned force closure (no counterpart in the reference): a 3D CNN on the
+ * PM mesh -- four periodic 3x3x3 convolutions, 16 channels, ReLU, BF16
+ * weights and activations with FP32 accumulation on the tensor cores --
+ * that maps [asinh(delta), asinh(Phi_N/1e-5), screening factor] to a
+ * residual force added to the mesh force.  Trained on the GPU against the
+ * force of a finer mesh for the same particles (Nmesh_fine = r Nmesh), with
+ * this library's forward and backward kernels and Adam.  Nmesh must be a
+ * multiple of 16.  Weight layout: w [4][27 taps][16 out][16 in], tap =
+ * 9 (di+1) + 3 (dj+1) + (dk+1), b [4][16]; the last layer has 3 live outputs. */
+typedef struct mgp_closure mgp_closure;
+int mgp_closure_create(int Nmesh, unsigned seed, int device, mgp_closure **out);
+int mgp_closure_destroy(mgp_closure *cl);
+int mgp_closure_get_weights(mgp_closure *cl, float *w, float *b, float *out_scale);
+int mgp_closure_set_weights(mgp_closure *cl, const float *w, const float *b, float out_scale);
+/* Working sample from the host ([V][3] features and targets, FP32; either
+ * may be NULL), forward pass (out [V][3] or NULL), loss and gradients
+ * without an update, one Adam step (returns the loss before it). */
+int mgp_closure_set_sample(mgp_closure *cl, const float *x, const float *t);
+int mgp_closure_get_sample(mgp_closure *cl, float *x, float *t);
+int mgp_closure_forward(mgp_closure *cl, float *out);
+int mgp_closure_gradients(mgp_closure *cl, double *loss, float *gw, float *gb);
+int mgp_closure_train_step(mgp_closure *cl, float lr, double *loss);
+/* Training data from contexts after mgp_get_displacements at scale factor A:
+ * features of the coarse context, and the target = fine force averaged onto
+ * the coarse mesh minus the coarse force (*rms its rms, may be NULL). */
+int mgp_closure_features(mgp_closure *cl, mgp_ctx *coarse, double A);
+int mgp_closure_target(mgp_closure *cl, mgp_ctx *fine, mgp_ctx *coarse, double *rms);
+/* Device training set: reserve n slots, store / load the working sample. */
+int mgp_closure_reserve(mgp_closure *cl, int n);
+int mgp_closure_store(mgp_closure *cl, int slot);
+int mgp_closure_load(mgp_closure *cl, int slot);
+/* Use the closure in every later mgp_get_displacements of ctx (NULL detaches). */
+int mgp_set_closure(mgp_ctx *ctx, mgp_closure *cl);
+
 /* Copy an internal grid to a host buffer (diagnostics and parity tests).
  * which: 0 density (real padded [N][N][2(N/2+1)] float), 1 delta(k)
  * (complex [N][N][N/2+1] float pairs), 2..4 force grids x,y,z (real

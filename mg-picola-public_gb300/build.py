@@ -19,7 +19,7 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libmgpicola.so")
 
-CU_SOURCES = ["mgp_kernels.cu", "mgp_api.cu", "mgp_run.cu", "mgp_noalloc.cu", "mgp_sd.cu"]
+CU_SOURCES = ["mgp_kernels.cu", "mgp_api.cu", "mgp_run.cu", "mgp_noalloc.cu", "mgp_sd.cu", "mgp_nn.cu"]
 C_SOURCES = ["mgp_cosmo.c", "mgp_param.c", "mgp_io.c"]
 HEADERS = ["mgp_internal.h", "mgp_cosmo.h", "mgp_rng.h", "mgp_io.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -35,7 +35,7 @@ extern "C" const char *mgp_last_error(void) { return g_err; }
 
 // ----------------------------------------------------------------- timing
 static const char *k_timer_names[MGP_NTIMERS] = {"cic",    "r2c",  "pofk",          "mg",         "forces",
-                                                   "c2r",    "interp_kick_drift", "step", "lpt_fields"};
+                                                   "c2r",    "interp_kick_drift", "step", "lpt_fields", "closure"};
 
 static void tstart(mgp_ctx *c, int t) {
   if (c->timing) cudaEventRecord(c->ev[t][0], c->stream);
@@ -680,6 +680,11 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   for (int g = 0; g < 3; g++)
     MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(c->frc + g * c->g.nreal), (cufftReal *)(c->frc + g * c->g.nreal)));
   tstop(c, T_C2R);
+  if (c->closure) {
+    tstart(c, T_NN);
+    RET_IF(mgp_closure_apply(c->closure, c, A));
+    tstop(c, T_NN);
+  }
   c->have_forces = 1;
   return MGP_OK;
 }

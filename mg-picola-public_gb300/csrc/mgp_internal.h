@@ -34,7 +34,7 @@ typedef struct {
   double mean_v[3];    /* mean of the stored v after the last kick */
 } mgp_dstate;
 
-#define MGP_NTIMERS 9
+#define MGP_NTIMERS 10
 
 typedef struct mgp_grid_geom {
   int N, NH;
@@ -134,6 +134,9 @@ struct mgp_ctx {
   cudaEvent_t bev[2];
   float batch_ms, batch_ic_ms;
 
+  /* learned force closure added to the force grids (mgp_set_closure) */
+  struct mgp_closure *closure;
+
   /* timing */
   int timing;
   cudaEvent_t ev[MGP_NTIMERS][2];
@@ -142,7 +145,7 @@ struct mgp_ctx {
   long long launches;
 };
 
-enum { T_CIC = 0, T_R2C, T_POFK, T_MG, T_FORCES, T_C2R, T_IKD, T_MISC, T_SD };
+enum { T_CIC = 0, T_R2C, T_POFK, T_MG, T_FORCES, T_C2R, T_IKD, T_MISC, T_SD, T_NN };
 
 /* error plumbing (C linkage: also called from the C sources) */
 #ifdef __cplusplus
@@ -203,6 +206,9 @@ typedef struct {
 
 extern long long g_kernel_launches;
 int mgp_blocks_for(long long n, int per_sm);
+
+/* learned force closure (mgp_nn.cu): adds its residual to the force grids */
+int mgp_closure_apply(struct mgp_closure *cl, mgp_ctx *c, double A);
 
 /* scale-dependent growth (mgp_sd.cu) */
 int mgp_sd_alloc(mgp_ctx *c);

@@ -24,7 +24,10 @@ EXPORTS = [
     "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_launch_count",
     "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
-    "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels",
+    "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_closure_create", "mgp_closure_destroy",
+    "mgp_closure_get_weights", "mgp_closure_set_weights", "mgp_closure_set_sample", "mgp_closure_get_sample",
+    "mgp_closure_forward", "mgp_closure_gradients", "mgp_closure_train_step", "mgp_closure_features",
+    "mgp_closure_target", "mgp_closure_reserve", "mgp_closure_store", "mgp_closure_load", "mgp_set_closure",
 ]
 
 # field types of mgp_assign_displacement_fields (src/proto.h:155-158)
@@ -120,6 +123,22 @@ def lib():
         L.mgp_batch_ms.restype = C.c_double
         L.mgp_batch_graph_nodes.argtypes = [vp]
         L.mgp_batch_graph_kernels.argtypes = [vp]
+        fpp = C.POINTER(C.c_float)
+        L.mgp_closure_create.argtypes = [C.c_int, C.c_uint, C.c_int, C.POINTER(vp)]
+        L.mgp_closure_destroy.argtypes = [vp]
+        L.mgp_closure_get_weights.argtypes = [vp, fpp, fpp, C.POINTER(C.c_float)]
+        L.mgp_closure_set_weights.argtypes = [vp, fpp, fpp, C.c_float]
+        L.mgp_closure_set_sample.argtypes = [vp, fpp, fpp]
+        L.mgp_closure_get_sample.argtypes = [vp, fpp, fpp]
+        L.mgp_closure_forward.argtypes = [vp, fpp]
+        L.mgp_closure_gradients.argtypes = [vp, C.POINTER(C.c_double), fpp, fpp]
+        L.mgp_closure_train_step.argtypes = [vp, C.c_float, C.POINTER(C.c_double)]
+        L.mgp_closure_features.argtypes = [vp, vp, C.c_double]
+        L.mgp_closure_target.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
+        L.mgp_closure_reserve.argtypes = [vp, C.c_int]
+        L.mgp_closure_store.argtypes = [vp, C.c_int]
+        L.mgp_closure_load.argtypes = [vp, C.c_int]
+        L.mgp_set_closure.argtypes = [vp, vp]
         L.mgp_power_spectrum.argtypes = [vp, C.c_double]
         L.mgp_power_spectrum.restype = C.c_double
         L.mgp_copy_grid.argtypes = [vp, C.c_int, fp, C.c_size_t]
@@ -375,3 +394,99 @@ class Batch:
 
     def graph_kernels(self):
         return lib().mgp_batch_graph_kernels(self.h)
+
+
+def _fptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Closure:
+    """Learned force closure (mgp_closure_*): a 4-layer 3x3x3 CNN on an
+    Nmesh^3 mesh predicting the finer-mesh force residual."""
+
+    NW = 4 * 27 * 16 * 16
+    NB = 4 * 16
+
+    def __init__(self, Nmesh, seed=1, device=0):
+        self.N = Nmesh
+        self.V = Nmesh ** 3
+        self.h = C.c_void_p()
+        _check(lib().mgp_closure_create(Nmesh, seed, device, C.byref(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mgp_closure_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def weights(self):
+        w = np.zeros(self.NW, np.float32)
+        b = np.zeros(self.NB, np.float32)
+        s = C.c_float(0)
+        _check(lib().mgp_closure_get_weights(self.h, _fptr(w), _fptr(b), C.byref(s)))
+        return w.reshape(4, 27, 16, 16), b.reshape(4, 16), s.value
+
+    def set_weights(self, w=None, b=None, scale=0.0):
+        w = None if w is None else np.ascontiguousarray(w, np.float32).reshape(-1)
+        b = None if b is None else np.ascontiguousarray(b, np.float32).reshape(-1)
+        _check(lib().mgp_closure_set_weights(self.h, _fptr(w), _fptr(b), float(scale)))
+
+    def set_sample(self, x=None, t=None):
+        x = None if x is None else np.ascontiguousarray(x, np.float32).reshape(-1)
+        t = None if t is None else np.ascontiguousarray(t, np.float32).reshape(-1)
+        _check(lib().mgp_closure_set_sample(self.h, _fptr(x), _fptr(t)))
+
+    def sample(self):
+        x = np.zeros((self.V, 3), np.float32)
+        t = np.zeros((self.V, 3), np.float32)
+        _check(lib().mgp_closure_get_sample(self.h, _fptr(x), _fptr(t)))
+        return x, t
+
+    def forward(self):
+        out = np.zeros((self.V, 3), np.float32)
+        _check(lib().mgp_closure_forward(self.h, _fptr(out)))
+        return out
+
+    def gradients(self):
+        gw = np.zeros(self.NW, np.float32)
+        gb = np.zeros(self.NB, np.float32)
+        loss = C.c_double(0)
+        _check(lib().mgp_closure_gradients(self.h, C.byref(loss), _fptr(gw), _fptr(gb)))
+        return loss.value, gw.reshape(4, 27, 16, 16), gb.reshape(4, 16)
+
+    def train_step(self, lr):
+        loss = C.c_double(0)
+        _check(lib().mgp_closure_train_step(self.h, float(lr), C.byref(loss)))
+        return loss.value
+
+    def features(self, ctx, A):
+        _check(lib().mgp_closure_features(self.h, ctx.h, float(A)))
+
+    def target(self, fine, coarse):
+        rms = C.c_double(0)
+        _check(lib().mgp_closure_target(self.h, fine.h, coarse.h, C.byref(rms)))
+        return rms.value
+
+    def reserve(self, n):
+        _check(lib().mgp_closure_reserve(self.h, n))
+
+    def store(self, slot):
+        _check(lib().mgp_closure_store(self.h, slot))
+
+    def load(self, slot):
+        _check(lib().mgp_closure_load(self.h, slot))
+
+    def attach(self, ctx):
+        _check(lib().mgp_set_closure(ctx.h, self.h))
+
+    @staticmethod
+    def detach(ctx):
+        _check(lib().mgp_set_closure(ctx.h, None))

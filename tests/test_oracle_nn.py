@@ -1,0 +1,41 @@
+"""The numpy restatement of the closure network (oracle/orc_nn.py): its
+backward pass against central finite differences in FP64 (no BF16
+rounding), on a small periodic grid."""
+import numpy as np
+
+from oracle import orc_nn as NN
+
+
+def test_closure_oracle_gradients_match_finite_differences():
+    N = 4
+    rng = np.random.default_rng(0)
+    X = np.zeros((N, N, N, 16))
+    X[..., :3] = rng.normal(0, 1, (N, N, N, 3))
+    Ws = rng.normal(0, 0.2, (4, 27, 16, 16))
+    Ws[3, :, 3:, :] = 0
+    bs = rng.normal(0, 0.1, (4, 16))
+    bs[3, 3:] = 0
+    T = rng.normal(0, 1, (N, N, N, 3))
+    loss, _, gw, gb = NN.loss_and_grads(X, Ws, bs, T, 1.5, bf16=False)
+    eps = 1e-6
+    for (l, t, o, c) in [(0, 4, 2, 1), (1, 13, 7, 5), (2, 26, 15, 0), (3, 0, 2, 9), (3, 20, 1, 3)]:
+        Wp, Wm = Ws.copy(), Ws.copy()
+        Wp[l, t, o, c] += eps
+        Wm[l, t, o, c] -= eps
+        fd = (NN.loss_and_grads(X, Wp, bs, T, 1.5, bf16=False)[0] -
+              NN.loss_and_grads(X, Wm, bs, T, 1.5, bf16=False)[0]) / (2 * eps)
+        assert abs(fd - gw[l][t, o, c]) < 1e-6 + 1e-4 * abs(fd), (l, t, o, c, fd, gw[l][t, o, c])
+    for (l, o) in [(0, 3), (2, 11), (3, 1)]:
+        bp, bm = bs.copy(), bs.copy()
+        bp[l, o] += eps
+        bm[l, o] -= eps
+        fd = (NN.loss_and_grads(X, Ws, bp, T, 1.5, bf16=False)[0] -
+              NN.loss_and_grads(X, Ws, bm, T, 1.5, bf16=False)[0]) / (2 * eps)
+        assert abs(fd - gb[l][o]) < 1e-6 + 1e-4 * abs(fd)
+
+
+def test_bf16_rounding_is_round_to_nearest_even():
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -9, -2.5, 3.14159265], np.float64)
+    r = NN.to_bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0 + 2 ** -7 and r[3] == -2.5
+    assert abs(r[4] - 3.140625) < 1e-12
