@@ -43,7 +43,17 @@ CONFIGS = {
     # |fR0| log-uniform in [1e-6, 1e-4]) in one batch, one graph launch per run
     "fofr_batch_64x64_128": dict(Ns=64, N=128, Box=256.0, model="fofr", nsteps=20, seed=6001, fixed=0, nbins=64,
                                  batch=64),
+    # COLA step with the learned force closure applied every step (256^3
+    # particles on the 256^3 mesh, Box 256 Mpc/h, 30 steps)
+    "closure_lcdm_256": dict(Ns=256, N=256, Box=256.0, model="lcdm", nsteps=30, seed=7017, fixed=0, nbins=128,
+                             closure=True),
 }
+
+
+def closure_flops(N):
+    """Algorithmic FLOPs of one closure forward: 2 x 27 x C_in x C_out per
+    voxel and layer over the live channels (3->16, 16->16, 16->16, 16->3)."""
+    return 2 * 27 * (3 * 16 + 16 * 16 + 16 * 16 + 16 * 3) * N ** 3
 
 # |fR0| of the batch: one value per seed pair, drawn log-uniform in [1e-6, 1e-4]
 # by numpy's PCG64 with this seed.
@@ -226,6 +236,10 @@ def run_gpu(args):
     Np = cfg["Ns"] ** 3
     N = cfg["N"]
     ctx = M.Context(p, device=local if world > 1 else 0)
+    closure = None
+    if cfg.get("closure"):
+        closure = M.Closure(N, seed=cfg["seed"], device=local if world > 1 else 0)  # He-normal init weights
+        closure.attach(ctx)
     ctx.displacement_fields()
     A0 = 1.0 / (1.0 + p.Init_Redshift)
     da = (1.0 - A0) / cfg["nsteps"]
@@ -251,7 +265,8 @@ def run_gpu(args):
     sync()
     barrier()
     launches0 = ctx.launches()
-    stage_ms = {k: 0.0 for k in ["cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift"]}
+    stage_ms = {k: 0.0 for k in ["cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "closure",
+                                 "closure_conv"]}
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         dev_ms = 0.0
@@ -297,6 +312,8 @@ def run_gpu(args):
         M.unpin(a)
     e2e_val = world * Np * e2e_steps / e2e_t / 1e6
     ctx.close()
+    if closure is not None:
+        closure.close()
 
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
@@ -307,13 +324,28 @@ def run_gpu(args):
     achieved = abytes / (own[dom] * 1e-3) / 1e9
     peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = measured_traffic(N, Np, dom)
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at 256^3 particles / "
+                              "512^3 mesh, scaled by particles and cells",
+            "algorithmic_bytes_per_launch": abytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+    if closure is not None:
+        conv_ms = stage_ms["closure_conv"] / args.steps
+        fl = closure_flops(N)
+        tf = fl / (conv_ms * 1e-3) / 1e12
+        bpeak = float(peaks.get("bf16_tflops_sustained", 1700.0))
+        roof = {"bound": "tensor", "kernel": "closure_conv (4 conv launches of one forward)", "achieved": round(tf, 2),
+                "peak": bpeak, "unit": "TFLOP/s", "frac": round(tf / bpeak, 4), "traffic": None,
+                "algorithmic_flops_per_forward": fl, "conv_ms_per_step": round(conv_ms, 4),
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed inside the step)"}
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (2LPT IC generated on the device, seed 5003)",
         "config": {"workload": args.config, "particles": Np, "mesh": N, "box_mpc_h": cfg["Box"],
-                   "model": "nDGP rcH0=1 screening (Gaussian, Rsmooth=1)" if cfg["model"] == "dgp" else "LCDM",
+                   "model": ("nDGP rcH0=1 screening (Gaussian, Rsmooth=1)" if cfg["model"] == "dgp" else "LCDM")
+                   + (" + learned force closure (4x 3^3 conv, 16 ch, BF16/FP32 acc)" if closure is not None else ""),
                    "pofk_every_step": True, "pofk_bins": cfg["nbins"], "l2": "inputs larger than L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": round(e2e_val, 3), "unit": UNIT, "h2d_bytes_per_step": 4 * 12 * Np,
@@ -321,11 +353,7 @@ def run_gpu(args):
                 "step_ms": [round(x, 2) for x in e2e_ms]},
         "gpu_launches": int(launches),
         "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stage_ms.items()},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at 256^3 particles / "
-                                       "512^3 mesh, scaled by particles and cells",
-                     "algorithmic_bytes_per_launch": abytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "roofline": roof,
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -356,8 +384,9 @@ def oracle_params(O, cfg):
 
 
 SAMPLE = {"ndgp_512_1024": "ndgp_128_256", "ndgp_256_512": "ndgp_128_256", "lcdm_64_128": "lcdm_64_128",
-          "fofr_batch_64x64_128": "fofr_64_128"}
+          "fofr_batch_64x64_128": "fofr_64_128", "closure_lcdm_256": "lcdm_128_128"}
 CONFIGS["fofr_64_128"] = dict(Ns=64, N=128, Box=256.0, model="fofr", nsteps=20, seed=6001, fixed=0, nbins=64)
+CONFIGS["lcdm_128_128"] = dict(Ns=128, N=128, Box=128.0, model="lcdm", nsteps=30, seed=7017, fixed=0, nbins=64)
 CONFIGS["ndgp_128_256"] = dict(Ns=128, N=256, Box=256.0, model="dgp", nsteps=50, seed=5003, fixed=1, nbins=128)
 
 

@@ -285,7 +285,7 @@ int mgp_batch_graph_kernels(mgp_ctx *ctx);
 /* Learned force closure (no counterpart in the reference): a 3D CNN on the
  * PM mesh -- four periodic 3x3x3 convolutions, 16 channels, ReLU, BF16
  * weights and activations with FP32 accumulation on the tensor cores --
- * that maps [asinh(delta), asinh(Phi_N/1e-5), screening factor] to a
+ * that maps [asinh(delta), Phi_N/1e-5, screening factor] to a
  * residual force added to the mesh force.  Trained on the GPU against the
  * force of a finer mesh for the same particles (Nmesh_fine = r Nmesh), with
  * this library's forward and backward kernels and Adam.  Nmesh must be a
@@ -309,8 +309,24 @@ int mgp_closure_train_step(mgp_closure *cl, float lr, double *loss);
  * the coarse mesh minus the coarse force (*rms its rms, may be NULL). */
 int mgp_closure_features(mgp_closure *cl, mgp_ctx *coarse, double A);
 int mgp_closure_target(mgp_closure *cl, mgp_ctx *fine, mgp_ctx *coarse, double *rms);
-/* Device training set: reserve n slots, store / load the working sample. */
-int mgp_closure_reserve(mgp_closure *cl, int n);
+/* Particle-level target (the loss a closure is trained with for use in a
+ * run): per particle, the fine context's force interpolated at the particle
+ * minus the coarse context's, r_p = F_fine(x_p) - F_coarse(x_p), with the
+ * particle's cell coordinates on the coarse mesh.  With such a sample the
+ * loss is the mean over particles and components of (out_scale u_p - r_p)^2,
+ * u_p the CIC interpolation of the network output at x_p, so the network
+ * learns the correction as the kick will use it; its gradient is the CIC
+ * deposit of the residuals.  The contexts hold the same particles.  band:
+ * restrict the fine force to the modes of the coarse mesh first (|k_i| below
+ * its Nyquist frequency), which drops the sub-grid force.  Host
+ * form: np particles, cells and t [np][3] (cells in mesh units, [0, Nmesh));
+ * get returns the working sample's np (0 for a grid target). */
+int mgp_closure_target_particles(mgp_closure *cl, mgp_ctx *fine, mgp_ctx *coarse, int band, double *rms);
+int mgp_closure_set_particle_sample(mgp_closure *cl, long long np, const float *cells, const float *t);
+int mgp_closure_get_particle_sample(mgp_closure *cl, long long *np, float *cells, float *t);
+/* Device training set: reserve n slots (np = 0: grid targets; np > 0:
+ * particle samples of np particles), store / load the working sample. */
+int mgp_closure_reserve(mgp_closure *cl, int n, long long np);
 int mgp_closure_store(mgp_closure *cl, int slot);
 int mgp_closure_load(mgp_closure *cl, int slot);
 /* Use the closure in every later mgp_get_displacements of ctx (NULL detaches). */

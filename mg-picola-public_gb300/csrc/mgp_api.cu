@@ -35,7 +35,8 @@ extern "C" const char *mgp_last_error(void) { return g_err; }
 
 // ----------------------------------------------------------------- timing
 static const char *k_timer_names[MGP_NTIMERS] = {"cic",    "r2c",  "pofk",          "mg",         "forces",
-                                                   "c2r",    "interp_kick_drift", "step", "lpt_fields", "closure"};
+                                                   "c2r",    "interp_kick_drift", "step", "lpt_fields", "closure",
+                                                   "closure_conv"};
 
 static void tstart(mgp_ctx *c, int t) {
   if (c->timing) cudaEventRecord(c->ev[t][0], c->stream);

@@ -10,6 +10,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include "mgp_device.cuh"
 #include "mgp_internal.h"
 #include "mgp_rng.h"
 
@@ -51,35 +52,6 @@ static dim3 grid_boxes(long long n_per_box, int per_sm, int nbox) {
 int mgp_blocks_per_box(long long n_per_box, int per_sm, int nbox) { return (int)grid_boxes(n_per_box, per_sm, nbox).x; }
 
 // -------------------------------------------------------------- helpers
-// Lattice coordinates of particle p (src/main.c:257-262 ordering).
-__device__ __forceinline__ void lattice_ijk(long long p, int Ns, int &i, int &j, int &k) {
-  long long ns2 = (long long)Ns * Ns;
-  i = (int)(p / ns2);
-  long long r = p - (long long)i * ns2;
-  j = (int)(r / Ns);
-  k = (int)(r - (long long)j * Ns);
-}
-
-// Cell index and CIC fraction along one axis for the particle at lattice
-// index `li` with displacement `s` (Mpc/h) and global offset `off_cells`.
-// Position in cells = li*N/Ns + s*N/Box + off; the lattice part is split into
-// integer and fractional parts exactly so the small displacement keeps full
-// FP32 precision.
-__device__ __forceinline__ void cell_frac(int li, float s, float off_cells, int N, int Ns, float scale,
-                                          int &idx, float &frac) {
-  long long qn = (long long)li * N;
-  int qi = (int)(qn / Ns);
-  float qf = (float)(qn - (long long)qi * Ns) / (float)Ns;
-  float w = fmaf(s, scale, off_cells) + qf;
-  float fl = floorf(w);
-  float fr = w - fl;
-  if (fr >= 1.0f) { fr -= 1.0f; fl += 1.0f; }
-  int ic = (qi + (int)fl) % N;
-  if (ic < 0) ic += N;
-  idx = ic;
-  frac = fr;
-}
-
 __global__ void k_fill(float *__restrict__ p, long long n, float v) {
   long long stride = (long long)gridDim.x * blockDim.x;
   long long n4 = n >> 2;  // grids are 256-byte aligned; n % 4 tail handled below

@@ -5,7 +5,8 @@
 // Network: four periodic 3x3x3 convolutions, 16 channels between layers,
 // ReLU after the first three, the last layer linear with 3 outputs (the
 // residual force components).  Inputs per cell (padded to 16 channels):
-// asinh(delta), asinh(Phi_N / 1e-5) and the screening factor
+// asinh(delta), Phi_N / 1e-5 (linear: the resolution correction is to
+// first order a linear filter of the potential) and the screening factor
 // min(1, |phi_crit / Phi_N|) for Phi_N < 0 (1 otherwise, and 1 for models
 // without potential screening).  Activations and weights are BF16, every
 // accumulation is FP32 on the tensor cores (mma.sync m16n8k16 bf16).
@@ -32,6 +33,7 @@
 
 #include <vector>
 
+#include "mgp_device.cuh"
 #include "mgp_internal.h"
 
 typedef __nv_bfloat16 bf16;
@@ -62,15 +64,27 @@ struct mgp_closure {
   float out_scale;                         // residual = out_scale * network output
   float *grid_a, *grid_b;                  // scratch real grids for the features
   long long P;                             // padded row of the scratch grids
-  // stored training samples: features (3 bf16) and targets (3 f32) per voxel
+  // particle-level target (pmode 1): cell coordinates on this mesh and
+  // r_p = F_fine(x_p) - F_coarse(x_p), SoA [3][np]; cur_* point at the
+  // working sample (own buffers or a stored slot)
+  int pmode;
+  long long np;                            // particles of the working sample
+  long long own_np;                        // capacity of pc / pt
+  float *pc, *pt;
+  const float *cur_pc, *cur_pt;
+  float *dout;                             // d loss / d out [V][4] (particle loss)
+  float *fscr;                             // band-limited fine force, 3 fine grids (lazy)
+  long long fscr_floats;
+  // stored training samples: features (3 bf16) per voxel and either grid
+  // targets (3 f32 per voxel, ds_np = 0) or particle samples (ds_np > 0)
   int nsamples, cap_samples;
+  long long ds_np;
   bf16 *ds_x;
-  float *ds_t;
+  float *ds_t, *ds_pc, *ds_pt;
 };
 
 namespace {
 
-constexpr int kThreadsConv = 128;  // 4 warps x 16 voxels = NN_SEG
 constexpr int kThreadsWg = 256;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -122,69 +136,136 @@ __device__ __forceinline__ void stage_rows(const bf16 *__restrict__ X, int N, in
   }
 }
 
-// Forward convolution.  mode 0: bf16 out, bias + ReLU; 1: bf16 out, no bias
-// (data gradient); 2: f32 out [V][4] (channels 0-3), bias; 3: add
-// scale * (out + bias) to the three force grids (channels 0-2).
-__global__ void __launch_bounds__(kThreadsConv) k_conv_fwd(const bf16 *__restrict__ X, const bf16 *__restrict__ W,
-                                                           const float *__restrict__ bias, int N, int mode,
-                                                           bf16 *__restrict__ Y16, float *__restrict__ Y32,
-                                                           float *__restrict__ frc, long long gstride, long long P,
-                                                           float scale) {
-  __shared__ __align__(16) bf16 ws[NN_WSIZE];
-  __shared__ __align__(16) bf16 xs[9][NN_SEG + 2][NN_CH];
-  const int nseg = (N + NN_SEG - 1) / NN_SEG;
-  const long long row = blockIdx.x / nseg;
-  const int seg = (int)(blockIdx.x - row * nseg);
-  const int i = (int)(row / N), j = (int)(row - (long long)i * N), k0 = seg * NN_SEG;
-  const int tid = threadIdx.x;
-  for (int c = tid; c < NN_WSIZE / 8; c += kThreadsConv)
-    reinterpret_cast<uint4 *>(ws)[c] = reinterpret_cast<const uint4 *>(W)[c];
-  stage_rows(X, N, i, j, k0, xs, tid, kThreadsConv);
-  __syncthreads();
-  const int warp = tid >> 5, lane = tid & 31;
-  const int kw = k0 + 16 * warp;  // first voxel of this warp
-  if (kw >= N) return;
-  float acc0[4] = {0.f, 0.f, 0.f, 0.f}, acc1[4] = {0.f, 0.f, 0.f, 0.f};
+// Forward convolution, persistent: a CTA keeps all weights in shared memory
+// and walks tiles of CT_I x CT_J output rows (i, j) by CT_SEG voxels (k).
+// For a tile it stages the (CT_I+2) x (CT_J+2) input rows around it, each
+// with one halo voxel on either side (cp.async), so a staged row serves up
+// to 9 output rows; warp w computes output row (i0 + w / CT_J, j0 + w % CT_J)
+// as 4 groups of 16 voxels, reusing each tap's B fragment for the 4 groups.
+// Shared-memory layout of a [voxel][16] bf16 row: the two 16-byte halves of
+// voxel q are swapped when bit 2 of q is set, so the 8 row addresses of any
+// ldmatrix (8 consecutive voxels or 8 consecutive output channels) fall in 8
+// distinct 16-byte bank groups.
+// mode 0: bf16 out, bias + ReLU; 1: bf16 out, no bias (data gradient); 2: f32
+// out [V][4] (channels 0-3), bias; 3: add scale * (out + bias) to the three
+// force grids (channels 0-2).
+constexpr int CT_I = 2, CT_J = 4, CT_SEG = 64;
+constexpr int CT_ROWS = (CT_I + 2) * (CT_J + 2);  // staged rows
+constexpr int CT_Q = CT_SEG + 2;                  // staged voxels per row
+constexpr int kThreadsConv = 32 * CT_I * CT_J;    // one warp per output row
+constexpr size_t kConvSmem = sizeof(bf16) * (NN_WSIZE + (size_t)CT_ROWS * CT_Q * NN_CH);
+
+__device__ __forceinline__ int swz_half(int q, int h) { return h ^ ((q >> 2) & 1); }
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kThreadsConv, 3) k_conv_fwd(const bf16 *__restrict__ X, const bf16 *__restrict__ W,
+                                                              const float *__restrict__ bias, int N, int mode,
+                                                              bf16 *__restrict__ Y16, float *__restrict__ Y32,
+                                                              float *__restrict__ frc, long long gstride, long long P,
+                                                              float scale) {
+  extern __shared__ __align__(16) unsigned char conv_smem[];
+  bf16(*ws)[NN_CH] = reinterpret_cast<bf16(*)[NN_CH]>(conv_smem);  // [tap * 16 + out][16 in]
+  bf16(*xs)[CT_Q][NN_CH] = reinterpret_cast<bf16(*)[CT_Q][NN_CH]>(conv_smem + sizeof(bf16) * NN_WSIZE);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int c = tid; c < NN_WSIZE / 8; c += kThreadsConv) {
+    const int row = c >> 1, h = c & 1;  // row = tap * 16 + out
+    cp_async16(&ws[row][8 * swz_half(row & 15, h)], W + (size_t)c * 8);
+  }
+  const int nseg = (N + CT_SEG - 1) / CT_SEG, tiles_j = N / CT_J;
+  const long long ntiles = (long long)(N / CT_I) * tiles_j * nseg;
+  const int wi = warp / CT_J, wj = warp % CT_J;
   // ldmatrix lane roles: A (16 voxels x 16 ch), B (16 out x 16 in)
   const int a_vox = (lane & 7) + 8 * ((lane >> 3) & 1), a_half = lane >> 4;
   const int b_out = (lane & 7) + 8 * (lane >> 4), b_half = (lane >> 3) & 1;
-#pragma unroll 1
-  for (int tap = 0; tap < NN_TAPS; tap++) {
-    const int r = tap / 3, dk = tap % 3;
-    uint32_t a0, a1, a2, a3, b0, b1, b2, b3;
-    ldsm_x4(smem_u32(&xs[r][16 * warp + dk + a_vox][8 * a_half]), a0, a1, a2, a3);
-    ldsm_x4(smem_u32(&ws[(tap * NN_CH + b_out) * NN_CH + 8 * b_half]), b0, b1, b2, b3);
-    mma16816(acc0, a0, a1, a2, a3, b0, b1);
-    mma16816(acc1, a0, a1, a2, a3, b2, b3);
-  }
-  // fragment: rows (voxels) lane/4 and lane/4 + 8, columns 2 (lane%4) + {0,1}
   const int vr = lane >> 2, cc = 2 * (lane & 3);
-  const long long vb = ((long long)i * N + j) * N + kw;
-#pragma unroll
-  for (int h = 0; h < 2; h++) {
-    const long long v = vb + vr + 8 * h;
-    float o[4] = {acc0[2 * h], acc0[2 * h + 1], acc1[2 * h], acc1[2 * h + 1]};  // ch cc, cc+1, cc+8, cc+9
-    if (mode != 1 && bias) {
-      o[0] += bias[cc];
-      o[1] += bias[cc + 1];
-      o[2] += bias[cc + 8];
-      o[3] += bias[cc + 9];
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int seg = (int)(t % nseg);
+    const long long rest = t / nseg;
+    const int i0 = (int)(rest / tiles_j) * CT_I, j0 = (int)(rest % tiles_j) * CT_J, k0 = seg * CT_SEG;
+    const int qmax = min(CT_SEG + 1, N - k0 + 1);  // staged voxels past qmax are zero
+    __syncthreads();  // the previous tile's reads of xs are done
+    for (int c = tid; c < CT_ROWS * CT_Q * 2; c += kThreadsConv) {
+      const int r = c / (CT_Q * 2), rem = c - r * (CT_Q * 2), q = rem >> 1, h = rem & 1;
+      bf16 *dst = &xs[r][q][8 * swz_half(q, h)];
+      if (q > qmax) {
+        *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+        continue;
+      }
+      int ii = i0 + r / (CT_J + 2) - 1, jj = j0 + r % (CT_J + 2) - 1, kk = k0 - 1 + q;
+      ii += ii < 0 ? N : 0;
+      ii -= ii >= N ? N : 0;
+      jj += jj < 0 ? N : 0;
+      jj -= jj >= N ? N : 0;
+      kk += kk < 0 ? N : 0;
+      kk -= kk >= N ? N : 0;
+      cp_async16(dst, X + (((long long)ii * N + jj) * N + kk) * NN_CH + 8 * h);
     }
-    if (mode <= 1) {
-      if (mode == 0)
+    cp_async_wait_all();
+    __syncthreads();
+    const int ng = min(4, (N - k0) / 16);  // valid 16-voxel groups (N is a multiple of 16)
+    float acc[4][2][4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) o[q] = fmaxf(o[q], 0.f);
-      reinterpret_cast<__nv_bfloat162 *>(Y16 + v * NN_CH + cc)[0] = __floats2bfloat162_rn(o[0], o[1]);
-      reinterpret_cast<__nv_bfloat162 *>(Y16 + v * NN_CH + cc + 8)[0] = __floats2bfloat162_rn(o[2], o[3]);
-    } else if (cc < 4) {
-      if (mode == 2) {
-        Y32[v * 4 + cc] = o[0];
-        Y32[v * 4 + cc + 1] = o[1];
-      } else {
-        const int kk = kw + vr + 8 * h;
-        const long long g = ((long long)i * N + j) * P + kk;
-        frc[cc * gstride + g] += scale * o[0];
-        if (cc + 1 < 3) frc[(cc + 1) * gstride + g] += scale * o[1];
+    for (int g = 0; g < 4; g++)
+#pragma unroll
+      for (int n = 0; n < 2; n++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[g][n][q] = 0.f;
+#pragma unroll 3
+    for (int tap = 0; tap < NN_TAPS; tap++) {
+      const int di = tap / 9, dj = (tap / 3) % 3, dk = tap % 3;
+      const int r = (wi + di) * (CT_J + 2) + (wj + dj);
+      uint32_t b0, b1, b2, b3;
+      ldsm_x4(smem_u32(&ws[tap * NN_CH + b_out][8 * swz_half(b_out, b_half)]), b0, b1, b2, b3);
+#pragma unroll
+      for (int g = 0; g < 4; g++) {
+        if (g < ng) {
+          const int q = 16 * g + a_vox + dk;
+          uint32_t a0, a1, a2, a3;
+          ldsm_x4(smem_u32(&xs[r][q][8 * swz_half(q, a_half)]), a0, a1, a2, a3);
+          mma16816(acc[g][0], a0, a1, a2, a3, b0, b1);
+          mma16816(acc[g][1], a0, a1, a2, a3, b2, b3);
+        }
+      }
+    }
+    // fragment: rows (voxels) lane/4 and lane/4 + 8, columns 2 (lane%4) + {0,1}
+    const int i = i0 + wi, j = j0 + wj;
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+      if (g >= ng) continue;
+      const int kw = k0 + 16 * g;
+      const long long vb = ((long long)i * N + j) * N + kw;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const long long v = vb + vr + 8 * h;
+        float o[4] = {acc[g][0][2 * h], acc[g][0][2 * h + 1], acc[g][1][2 * h], acc[g][1][2 * h + 1]};  // cc, cc+1, cc+8, cc+9
+        if (mode != 1 && bias) {
+          o[0] += bias[cc];
+          o[1] += bias[cc + 1];
+          o[2] += bias[cc + 8];
+          o[3] += bias[cc + 9];
+        }
+        if (mode <= 1) {
+          if (mode == 0)
+#pragma unroll
+            for (int q = 0; q < 4; q++) o[q] = fmaxf(o[q], 0.f);
+          reinterpret_cast<__nv_bfloat162 *>(Y16 + v * NN_CH + cc)[0] = __floats2bfloat162_rn(o[0], o[1]);
+          reinterpret_cast<__nv_bfloat162 *>(Y16 + v * NN_CH + cc + 8)[0] = __floats2bfloat162_rn(o[2], o[3]);
+        } else if (cc < 4) {
+          if (mode == 2) {
+            Y32[v * 4 + cc] = o[0];
+            Y32[v * 4 + cc + 1] = o[1];
+          } else {
+            const int kk = kw + vr + 8 * h;
+            const long long gi = ((long long)i * N + j) * P + kk;
+            frc[cc * gstride + gi] += scale * o[0];
+            if (cc + 1 < 3) frc[(cc + 1) * gstride + gi] += scale * o[1];
+          }
+        }
       }
     }
   }
@@ -346,7 +427,7 @@ __global__ void k_features(const float *__restrict__ ga, const float *__restrict
 #pragma unroll
     for (int c = 0; c < NN_CH; c++) rowv[c] = __float2bfloat16_rn(0.f);
     rowv[0] = __float2bfloat16_rn(asinhf(d));
-    rowv[1] = __float2bfloat16_rn(asinhf(ph * 1e5f));
+    rowv[1] = __float2bfloat16_rn(ph * 1e5f);
     rowv[2] = __float2bfloat16_rn(sc);
     reinterpret_cast<uint4 *>(X + v * NN_CH)[0] = reinterpret_cast<uint4 *>(rowv)[0];
     reinterpret_cast<uint4 *>(X + v * NN_CH)[1] = reinterpret_cast<uint4 *>(rowv)[1];
@@ -380,8 +461,8 @@ __global__ void k_target(const float *__restrict__ ff, long long fg, int Nf, lon
   }
 }
 
-// Training-set compaction: 3 feature channels (bf16) and 3 target
-// components (f32) per voxel.
+// Training-set compaction: 3 feature channels (bf16) and, for grid targets,
+// 3 target components (f32) per voxel (dt / t NULL: features only).
 __global__ void k_pack_sample(const bf16 *__restrict__ X, const float *__restrict__ t, long long V,
                               bf16 *__restrict__ dx, float *__restrict__ dt) {
   long long stride = (long long)gridDim.x * blockDim.x;
@@ -389,7 +470,7 @@ __global__ void k_pack_sample(const bf16 *__restrict__ X, const float *__restric
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       dx[v * 3 + c] = X[v * NN_CH + c];
-      dt[v * 3 + c] = t[v * 4 + c];
+      if (dt) dt[v * 3 + c] = t[v * 4 + c];
     }
 }
 __global__ void k_unpack_sample(const bf16 *__restrict__ dx, const float *__restrict__ dt, long long V,
@@ -400,13 +481,177 @@ __global__ void k_unpack_sample(const bf16 *__restrict__ dx, const float *__rest
 #pragma unroll
     for (int c = 0; c < NN_CH; c++) rowv[c] = __float2bfloat16_rn(0.f);
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      rowv[c] = dx[v * 3 + c];
-      t[v * 4 + c] = dt[v * 3 + c];
+    for (int c = 0; c < 3; c++) rowv[c] = dx[v * 3 + c];
+    if (dt) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) t[v * 4 + c] = dt[v * 3 + c];
+      t[v * 4 + 3] = 0.f;
     }
-    t[v * 4 + 3] = 0.f;
     reinterpret_cast<uint4 *>(X + v * NN_CH)[0] = reinterpret_cast<uint4 *>(rowv)[0];
     reinterpret_cast<uint4 *>(X + v * NN_CH)[1] = reinterpret_cast<uint4 *>(rowv)[1];
+  }
+}
+
+// Trilinear (CIC) interpolation of three force grids at a cell position, the
+// gather of the kick (MtoParticles, src/auxPM.c:560-644).
+__device__ __forceinline__ void cic_gather3(const float *__restrict__ F, long long gf, int N, long long P, int ix,
+                                            int iy, int iz, float dx, float dy, float dz, float out[3]) {
+  const long long NP = (long long)N * P;
+  const long long x0 = (long long)ix * NP, x1 = (ix + 1 == N ? 0 : (long long)(ix + 1) * NP);
+  const long long y0 = (long long)iy * P, y1 = (iy + 1 == N ? 0 : (long long)(iy + 1) * P);
+  const long long z0 = iz, z1 = (iz + 1 == N ? 0 : iz + 1);
+  const float tx = 1.f - dx, ty = 1.f - dy, tz = 1.f - dz;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    const float *G = F + q * gf;
+    out[q] = G[x0 + y0 + z0] * (tx * ty * tz) + G[x0 + y0 + z1] * (tx * ty * dz) + G[x0 + y1 + z0] * (tx * dy * tz) +
+             G[x0 + y1 + z1] * (tx * dy * dz) + G[x1 + y0 + z0] * (dx * ty * tz) + G[x1 + y0 + z1] * (dx * ty * dz) +
+             G[x1 + y1 + z0] * (dx * dy * tz) + G[x1 + y1 + z1] * (dx * dy * dz);
+  }
+}
+
+// Particle-level target: per particle, the fine context's interpolated force
+// minus the coarse context's (each at its own copy of the particle), and the
+// particle's coarse-mesh cell coordinates (cell + CIC fraction), SoA [3][np].
+__global__ void k_particle_target(const float *__restrict__ ff, long long fg, int Nf, long long Pf,
+                                  const float *__restrict__ sf, const mgp_dstate *__restrict__ stf,
+                                  const float *__restrict__ fc, long long cg, int N, long long P,
+                                  const float *__restrict__ sc, const mgp_dstate *__restrict__ stc, long long np,
+                                  int Ns, float scale_f, float scale_c, float *__restrict__ pc,
+                                  float *__restrict__ pt) {
+  const float oxf = (float)(stf->cx[0] * scale_f), oyf = (float)(stf->cx[1] * scale_f),
+              ozf = (float)(stf->cx[2] * scale_f);
+  const float oxc = (float)(stc->cx[0] * scale_c), oyc = (float)(stc->cx[1] * scale_c),
+              ozc = (float)(stc->cx[2] * scale_c);
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    int i, j, k, ix, iy, iz;
+    float dx, dy, dz, Ff[3], Fc[3];
+    lattice_ijk(p, Ns, i, j, k);
+    cell_frac(i, sf[p], oxf, Nf, Ns, scale_f, ix, dx);
+    cell_frac(j, sf[np + p], oyf, Nf, Ns, scale_f, iy, dy);
+    cell_frac(k, sf[2 * np + p], ozf, Nf, Ns, scale_f, iz, dz);
+    cic_gather3(ff, fg, Nf, Pf, ix, iy, iz, dx, dy, dz, Ff);
+    cell_frac(i, sc[p], oxc, N, Ns, scale_c, ix, dx);
+    cell_frac(j, sc[np + p], oyc, N, Ns, scale_c, iy, dy);
+    cell_frac(k, sc[2 * np + p], ozc, N, Ns, scale_c, iz, dz);
+    cic_gather3(fc, cg, N, P, ix, iy, iz, dx, dy, dz, Fc);
+    pc[p] = (float)ix + dx;
+    pc[np + p] = (float)iy + dy;
+    pc[2 * np + p] = (float)iz + dz;
+#pragma unroll
+    for (int q = 0; q < 3; q++) pt[q * np + p] = Ff[q] - Fc[q];
+  }
+}
+
+// Particle loss = sum over particles and components of (s u_p - r_p)^2 / (3 np),
+// u_p the CIC interpolation of the network output (out [V][4], channels 0-2)
+// at the particle; its gradient d loss / d out is the CIC deposit of
+// 2 s (s u_p - r_p) / (3 np), accumulated into dout [V][4] (float4 atomics).
+constexpr int kThreadsPl = 256;
+__global__ void __launch_bounds__(kThreadsPl) k_particle_loss(const float *__restrict__ out, int N, long long np,
+                                                              const float *__restrict__ pc,
+                                                              const float *__restrict__ pt, float s, float inv,
+                                                              float *__restrict__ dout, double *__restrict__ loss) {
+  __shared__ double sh[kThreadsPl / 32];
+  double acc = 0.0;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    int i0[3], i1[3];
+    float d[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const float w = pc[a * np + p], fl = floorf(w);
+      d[a] = w - fl;
+      int ic = (int)fl % N;
+      if (ic < 0) ic += N;
+      i0[a] = ic;
+      i1[a] = ic + 1 == N ? 0 : ic + 1;
+    }
+    long long v[8];
+    float wt[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const int bx = c >> 2, by = (c >> 1) & 1, bz = c & 1;
+      v[c] = ((long long)(bx ? i1[0] : i0[0]) * N + (by ? i1[1] : i0[1])) * N + (bz ? i1[2] : i0[2]);
+      wt[c] = (bx ? d[0] : 1.f - d[0]) * (by ? d[1] : 1.f - d[1]) * (bz ? d[2] : 1.f - d[2]);
+    }
+    float u0 = 0.f, u1 = 0.f, u2 = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const float4 o = __ldg(reinterpret_cast<const float4 *>(out) + v[c]);
+      u0 = fmaf(wt[c], o.x, u0);
+      u1 = fmaf(wt[c], o.y, u1);
+      u2 = fmaf(wt[c], o.z, u2);
+    }
+    const float e0 = s * u0 - pt[p], e1 = s * u1 - pt[np + p], e2 = s * u2 - pt[2 * np + p];
+    acc += (double)e0 * e0 + (double)e1 * e1 + (double)e2 * e2;
+    const float g = 2.f * s * inv;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const float gw = g * wt[c];
+      atomicAdd(reinterpret_cast<float4 *>(dout) + v[c], make_float4(gw * e0, gw * e1, gw * e2, 0.f));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kThreadsPl / 32; w++) t += sh[w];
+    atomicAdd(loss, t * (double)inv);
+  }
+}
+
+// dout [V][4] f32 -> the BF16 gradient [V][16] of the last layer (channels 0-2)
+__global__ void k_dout_to_bf16(const float *__restrict__ dout, long long V, bf16 *__restrict__ g) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += stride) {
+    const float4 d = reinterpret_cast<const float4 *>(dout)[v];
+    __align__(16) bf16 row[NN_CH];
+#pragma unroll
+    for (int c = 0; c < NN_CH; c++) row[c] = __float2bfloat16_rn(0.f);
+    row[0] = __float2bfloat16_rn(d.x);
+    row[1] = __float2bfloat16_rn(d.y);
+    row[2] = __float2bfloat16_rn(d.z);
+    reinterpret_cast<uint4 *>(g + v * NN_CH)[0] = reinterpret_cast<uint4 *>(row)[0];
+    reinterpret_cast<uint4 *>(g + v * NN_CH)[1] = reinterpret_cast<uint4 *>(row)[1];
+  }
+}
+
+// Keep the modes of a fine-mesh transform [Nf][Nf][Nf/2+1] that the coarse
+// mesh represents (|k_x|, |k_y|, k_z < kc in fine integer units), scaled by
+// norm (the 1/Nf^3 of the round trip); zero the rest.
+__global__ void k_band_limit(float2 *__restrict__ c, int Nf, int kc, float norm) {
+  const int NH = Nf / 2 + 1;
+  const long long n = (long long)Nf * Nf * NH;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+    const int kz = (int)(q % NH);
+    const long long r = q / NH;
+    const int j = (int)(r % Nf), i = (int)(r / Nf);
+    const int ki = i < Nf / 2 ? i : Nf - i, kj = j < Nf / 2 ? j : Nf - j;
+    const float f = (ki < kc && kj < kc && kz < kc) ? norm : 0.f;
+    float2 v = c[q];
+    v.x *= f;
+    v.y *= f;
+    c[q] = v;
+  }
+}
+
+// sum of squares of n floats into *out (FP64)
+__global__ void k_sumsq_flat(const float *__restrict__ a, long long n, double *__restrict__ out) {
+  __shared__ double sh[8];
+  double acc = 0.0;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+    acc += (double)a[q] * a[q];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+    atomicAdd(out, t);
   }
 }
 
@@ -421,9 +666,18 @@ __global__ void k_unpack_sample(const bf16 *__restrict__ dx, const float *__rest
 
 static int conv_fwd(mgp_closure *cl, const bf16 *X, const bf16 *W, const float *bias, int mode, bf16 *Y16, float *Y32,
                     float *frc, long long gstride, long long P, float scale) {
-  const int N = cl->N, nseg = (N + NN_SEG - 1) / NN_SEG;
-  const long long blocks = (long long)N * N * nseg;
-  k_conv_fwd<<<(unsigned)blocks, kThreadsConv, 0, cl->stream>>>(X, W, bias, N, mode, Y16, Y32, frc, gstride, P, scale);
+  static int grid = 0;  // resident CTAs of the persistent kernel (one device per process)
+  if (!grid) {
+    MGP_CUDA(cudaFuncSetAttribute(k_conv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kConvSmem));
+    int per_sm = 0, sms = 0;
+    MGP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_fwd, kThreadsConv, kConvSmem));
+    MGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cl->device));
+    grid = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  const int N = cl->N;
+  const long long tiles = (long long)(N / CT_I) * (N / CT_J) * ((N + CT_SEG - 1) / CT_SEG);
+  const unsigned blocks = (unsigned)(tiles < grid ? tiles : grid);
+  k_conv_fwd<<<blocks, kThreadsConv, kConvSmem, cl->stream>>>(X, W, bias, N, mode, Y16, Y32, frc, gstride, P, scale);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -452,9 +706,20 @@ static int closure_forward(mgp_closure *cl) {
 static int closure_backward(mgp_closure *cl) {
   const long long V = cl->V;
   MGP_CUDA(cudaMemsetAsync(cl->loss, 0, sizeof(double), cl->stream));
-  k_loss_grad<<<mgp_blocks_for(V, 4), 256, 0, cl->stream>>>(cl->out, cl->target, V, cl->out_scale, cl->g0, cl->loss);
-  MGP_CHECK_LAUNCH();
-  g_kernel_launches++;
+  if (cl->pmode) {
+    MGP_CUDA(cudaMemsetAsync(cl->dout, 0, sizeof(float) * 4 * V, cl->stream));
+    k_particle_loss<<<mgp_blocks_for(cl->np, 8), kThreadsPl, 0, cl->stream>>>(
+        cl->out, cl->N, cl->np, cl->cur_pc, cl->cur_pt, cl->out_scale, (float)(1.0 / (3.0 * (double)cl->np)), cl->dout,
+        cl->loss);
+    MGP_CHECK_LAUNCH();
+    k_dout_to_bf16<<<mgp_blocks_for(V, 4), 256, 0, cl->stream>>>(cl->dout, V, cl->g0);
+    MGP_CHECK_LAUNCH();
+    g_kernel_launches += 2;
+  } else {
+    k_loss_grad<<<mgp_blocks_for(V, 4), 256, 0, cl->stream>>>(cl->out, cl->target, V, cl->out_scale, cl->g0, cl->loss);
+    MGP_CHECK_LAUNCH();
+    g_kernel_launches++;
+  }
   bf16 *g = cl->g0, *gn = cl->g1;
   for (int l = NN_LAYERS - 1; l >= 0; l--) {
     MGP_CUDA(cudaMemsetAsync(cl->gw[l], 0, sizeof(float) * NN_WSIZE, cl->stream));
@@ -493,7 +758,8 @@ extern "C" int mgp_closure_destroy(mgp_closure *cl) {
     for (size_t q = 0; q < sizeof(b) / sizeof(b[0]); q++)
       if (b[q]) cudaFree(b[q]);
   }
-  void *b[] = {cl->wt16, cl->out, cl->target, cl->g0, cl->g1, cl->loss, cl->grid_a, cl->grid_b, cl->ds_x, cl->ds_t};
+  void *b[] = {cl->wt16, cl->out,  cl->target, cl->g0,   cl->g1,   cl->loss,  cl->grid_a, cl->grid_b,
+               cl->ds_x, cl->ds_t, cl->ds_pc,  cl->ds_pt, cl->pc,   cl->pt,    cl->dout, cl->fscr};
   for (size_t q = 0; q < sizeof(b) / sizeof(b[0]); q++)
     if (b[q]) cudaFree(b[q]);
   if (cl->own_stream && cl->stream) cudaStreamDestroy(cl->stream);
@@ -615,6 +881,7 @@ extern "C" int mgp_closure_set_sample(mgp_closure *cl, const float *x, const flo
     for (long long v = 0; v < V; v++)
       for (int c = 0; c < 3; c++) h[v * 4 + c] = t[v * 3 + c];
     MGP_CUDA(cudaMemcpy(cl->target, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice));
+    cl->pmode = 0;
   }
   return MGP_OK;
 }
@@ -752,6 +1019,7 @@ extern "C" int mgp_closure_target(mgp_closure *cl, mgp_ctx *fine, mgp_ctx *coars
                                                              coarse->g.nreal, N, coarse->g.P, Nf / N, cl->target);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
+  cl->pmode = 0;
   if (rms) {
     MGP_CUDA(cudaMemsetAsync(cl->loss, 0, sizeof(double), cl->stream));
     k_sumsq<<<mgp_blocks_for(cl->V, 4), 256, 0, cl->stream>>>(cl->target, cl->V, cl->loss);
@@ -765,41 +1033,196 @@ extern "C" int mgp_closure_target(mgp_closure *cl, mgp_ctx *fine, mgp_ctx *coars
   return MGP_OK;
 }
 
-// Training set on the device: `n` slots of (3 feature channels, 3 target
-// components) per voxel.
-extern "C" int mgp_closure_reserve(mgp_closure *cl, int n) {
-  if (!cl || n < 0) return mgp_set_error(MGP_EINVAL, "bad closure reserve");
+// Particle buffers (SoA [3][np]) and the f32 gradient grid for np particles.
+static int ensure_particles(mgp_closure *cl, long long np) {
+  if (np <= 0) return mgp_set_error(MGP_EINVAL, "particle sample needs np > 0");
+  if (cl->own_np != np) {
+    if (cl->pc) cudaFree(cl->pc);
+    if (cl->pt) cudaFree(cl->pt);
+    cl->pc = cl->pt = NULL;
+    cl->own_np = 0;
+    MGP_CUDA(cudaMalloc(&cl->pc, sizeof(float) * 3 * np));
+    MGP_CUDA(cudaMalloc(&cl->pt, sizeof(float) * 3 * np));
+    cl->own_np = np;
+  }
+  cl->np = np;
+  if (!cl->dout) MGP_CUDA(cudaMalloc(&cl->dout, sizeof(float) * 4 * cl->V));
+  return MGP_OK;
+}
+
+// Particle-level training target from a fine and a coarse context holding the
+// same particles, both after mgp_get_displacements at the same scale factor.
+// band != 0: the fine force is first restricted to the modes the coarse mesh
+// represents (three R2C / C2R pairs on the fine mesh), which drops the
+// sub-grid force that no coarse-mesh input can predict.
+extern "C" int mgp_closure_target_particles(mgp_closure *cl, mgp_ctx *fine, mgp_ctx *coarse, int band,
+                                            double *rms) {
+  NN_RET(check_ctx(cl, coarse));
+  if (!fine || fine->nbox != 1 || !fine->have_forces) return mgp_set_error(MGP_ESTATE, "fine context has no forces");
+  if (fine->np != coarse->np || fine->Ns != coarse->Ns || fine->p.Box != coarse->p.Box)
+    return mgp_set_error(MGP_EINVAL, "fine and coarse contexts hold different particle sets");
+  MGP_CUDA(cudaSetDevice(cl->device));
+  MGP_CUDA(cudaStreamSynchronize(fine->stream));
+  MGP_CUDA(cudaStreamSynchronize(coarse->stream));
+  NN_RET(ensure_particles(cl, coarse->np));
+  const float *ff = fine->frc;
+  if (band) {
+    const long long gf = fine->g.nreal;
+    if (cl->fscr_floats != 3 * gf) {
+      if (cl->fscr) cudaFree(cl->fscr);
+      cl->fscr = NULL;
+      cl->fscr_floats = 0;
+      MGP_CUDA(cudaMalloc(&cl->fscr, sizeof(float) * 3 * gf));
+      cl->fscr_floats = 3 * gf;
+    }
+    MGP_CUDA(cudaMemcpyAsync(cl->fscr, fine->frc, sizeof(float) * 3 * gf, cudaMemcpyDeviceToDevice, cl->stream));
+    MGP_CUFFT(cufftSetStream(fine->plan_r2c_ip, cl->stream));
+    MGP_CUFFT(cufftSetStream(fine->plan_c2r_1, cl->stream));
+    const int Nf = fine->g.N;
+    cufftResult r = CUFFT_SUCCESS;
+    for (int q = 0; q < 3 && r == CUFFT_SUCCESS; q++) {
+      float *g = cl->fscr + q * gf;
+      r = cufftExecR2C(fine->plan_r2c_ip, (cufftReal *)g, (cufftComplex *)g);
+      if (r != CUFFT_SUCCESS) break;
+      k_band_limit<<<mgp_blocks_for(fine->g.ncomplex, 4), 256, 0, cl->stream>>>(
+          (float2 *)g, Nf, coarse->g.N / 2, (float)(1.0 / ((double)Nf * Nf * Nf)));
+      g_kernel_launches++;
+      r = cufftExecC2R(fine->plan_c2r_1, (cufftComplex *)g, (cufftReal *)g);
+    }
+    cufftSetStream(fine->plan_r2c_ip, fine->stream);
+    cufftSetStream(fine->plan_c2r_1, fine->stream);
+    if (r != CUFFT_SUCCESS) return mgp_set_error(MGP_ECUFFT, "closure band-limited target transforms");
+    MGP_CHECK_LAUNCH();
+    ff = cl->fscr;
+  }
+  const double box = coarse->p.Box;
+  k_particle_target<<<mgp_blocks_for(cl->np, 8), 256, 0, cl->stream>>>(
+      ff, fine->g.nreal, fine->g.N, fine->g.P, fine->s, fine->dstate, coarse->frc, coarse->g.nreal,
+      coarse->g.N, coarse->g.P, coarse->s, coarse->dstate, cl->np, coarse->Ns, (float)(fine->g.N / box),
+      (float)(coarse->g.N / box), cl->pc, cl->pt);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  cl->cur_pc = cl->pc;
+  cl->cur_pt = cl->pt;
+  cl->pmode = 1;
+  if (rms) {
+    MGP_CUDA(cudaMemsetAsync(cl->loss, 0, sizeof(double), cl->stream));
+    k_sumsq_flat<<<mgp_blocks_for(3 * cl->np, 4), 256, 0, cl->stream>>>(cl->pt, 3 * cl->np, cl->loss);
+    MGP_CHECK_LAUNCH();
+    double ss = 0.0;
+    MGP_CUDA(cudaMemcpyAsync(&ss, cl->loss, sizeof(double), cudaMemcpyDeviceToHost, cl->stream));
+    MGP_CUDA(cudaStreamSynchronize(cl->stream));
+    *rms = sqrt(ss / (3.0 * (double)cl->np));
+  }
+  MGP_CUDA(cudaStreamSynchronize(cl->stream));
+  return MGP_OK;
+}
+
+// Host particle sample: cells [np][3] (mesh units, [0, Nmesh)), t [np][3].
+extern "C" int mgp_closure_set_particle_sample(mgp_closure *cl, long long np, const float *cells, const float *t) {
+  if (!cl || !cells || !t) return mgp_set_error(MGP_EINVAL, "null argument");
+  for (long long q = 0; q < 3 * np; q++)
+    if (!(cells[q] >= 0.f && cells[q] < (float)cl->N))
+      return mgp_set_error(MGP_EINVAL, "particle cell coordinate %g outside [0, %d)", cells[q], cl->N);
   MGP_CUDA(cudaSetDevice(cl->device));
   MGP_CUDA(cudaStreamSynchronize(cl->stream));
-  if (cl->ds_x) cudaFree(cl->ds_x);
-  if (cl->ds_t) cudaFree(cl->ds_t);
+  NN_RET(ensure_particles(cl, np));
+  std::vector<float> hc((size_t)3 * np), ht((size_t)3 * np);
+  for (long long p = 0; p < np; p++)
+    for (int a = 0; a < 3; a++) {
+      hc[a * np + p] = cells[p * 3 + a];
+      ht[a * np + p] = t[p * 3 + a];
+    }
+  MGP_CUDA(cudaMemcpy(cl->pc, hc.data(), sizeof(float) * hc.size(), cudaMemcpyHostToDevice));
+  MGP_CUDA(cudaMemcpy(cl->pt, ht.data(), sizeof(float) * ht.size(), cudaMemcpyHostToDevice));
+  cl->cur_pc = cl->pc;
+  cl->cur_pt = cl->pt;
+  cl->pmode = 1;
+  return MGP_OK;
+}
+
+extern "C" int mgp_closure_get_particle_sample(mgp_closure *cl, long long *np, float *cells, float *t) {
+  if (!cl) return mgp_set_error(MGP_EINVAL, "null closure");
+  if (np) *np = cl->pmode ? cl->np : 0;
+  if (!cl->pmode) return MGP_OK;
+  MGP_CUDA(cudaStreamSynchronize(cl->stream));
+  const long long n = cl->np;
+  std::vector<float> hc((size_t)3 * n), ht((size_t)3 * n);
+  MGP_CUDA(cudaMemcpy(hc.data(), cl->cur_pc, sizeof(float) * hc.size(), cudaMemcpyDeviceToHost));
+  MGP_CUDA(cudaMemcpy(ht.data(), cl->cur_pt, sizeof(float) * ht.size(), cudaMemcpyDeviceToHost));
+  for (long long p = 0; p < n; p++)
+    for (int a = 0; a < 3; a++) {
+      if (cells) cells[p * 3 + a] = hc[a * n + p];
+      if (t) t[p * 3 + a] = ht[a * n + p];
+    }
+  return MGP_OK;
+}
+
+// Training set on the device: `n` slots of 3 feature channels per voxel and
+// either grid targets (np = 0) or particle samples of np particles.
+extern "C" int mgp_closure_reserve(mgp_closure *cl, int n, long long np) {
+  if (!cl || n < 0 || np < 0) return mgp_set_error(MGP_EINVAL, "bad closure reserve");
+  MGP_CUDA(cudaSetDevice(cl->device));
+  MGP_CUDA(cudaStreamSynchronize(cl->stream));
+  void *b[] = {cl->ds_x, cl->ds_t, cl->ds_pc, cl->ds_pt};
+  for (size_t q = 0; q < sizeof(b) / sizeof(b[0]); q++)
+    if (b[q]) cudaFree(b[q]);
   cl->ds_x = NULL;
-  cl->ds_t = NULL;
+  cl->ds_t = cl->ds_pc = cl->ds_pt = NULL;
   cl->cap_samples = cl->nsamples = 0;
+  cl->ds_np = 0;
+  if (cl->pmode && cl->cur_pc != cl->pc) cl->pmode = 0;  // the working sample pointed into the old set
   if (n == 0) return MGP_OK;
   MGP_CUDA(cudaMalloc(&cl->ds_x, sizeof(bf16) * 3 * cl->V * n));
-  MGP_CUDA(cudaMalloc(&cl->ds_t, sizeof(float) * 3 * cl->V * n));
+  if (np > 0) {
+    MGP_CUDA(cudaMalloc(&cl->ds_pc, sizeof(float) * 3 * np * n));
+    MGP_CUDA(cudaMalloc(&cl->ds_pt, sizeof(float) * 3 * np * n));
+  } else {
+    MGP_CUDA(cudaMalloc(&cl->ds_t, sizeof(float) * 3 * cl->V * n));
+  }
+  cl->ds_np = np;
   cl->cap_samples = n;
   return MGP_OK;
 }
 
 extern "C" int mgp_closure_store(mgp_closure *cl, int slot) {
   if (!cl || slot < 0 || slot >= cl->cap_samples) return mgp_set_error(MGP_EINVAL, "bad closure slot %d", slot);
-  k_pack_sample<<<mgp_blocks_for(cl->V, 4), 256, 0, cl->stream>>>(cl->act[0], cl->target, cl->V,
-                                                                  cl->ds_x + (size_t)slot * 3 * cl->V,
-                                                                  cl->ds_t + (size_t)slot * 3 * cl->V);
+  if (cl->ds_np ? !(cl->pmode && cl->np == cl->ds_np) : cl->pmode)
+    return mgp_set_error(MGP_ESTATE, "working sample does not match the reserved set (particles %lld vs %lld)",
+                         cl->pmode ? cl->np : 0LL, cl->ds_np);
+  k_pack_sample<<<mgp_blocks_for(cl->V, 4), 256, 0, cl->stream>>>(
+      cl->act[0], cl->target, cl->V, cl->ds_x + (size_t)slot * 3 * cl->V,
+      cl->ds_np ? NULL : cl->ds_t + (size_t)slot * 3 * cl->V);
   MGP_CHECK_LAUNCH();
+  if (cl->ds_np) {
+    const size_t n3 = (size_t)3 * cl->ds_np;
+    MGP_CUDA(cudaMemcpyAsync(cl->ds_pc + slot * n3, cl->cur_pc, sizeof(float) * n3, cudaMemcpyDeviceToDevice,
+                             cl->stream));
+    MGP_CUDA(cudaMemcpyAsync(cl->ds_pt + slot * n3, cl->cur_pt, sizeof(float) * n3, cudaMemcpyDeviceToDevice,
+                             cl->stream));
+  }
   if (slot >= cl->nsamples) cl->nsamples = slot + 1;
   MGP_CUDA(cudaStreamSynchronize(cl->stream));
   return MGP_OK;
 }
 
+// Make a stored slot the working sample (particle samples are used in place).
 extern "C" int mgp_closure_load(mgp_closure *cl, int slot) {
   if (!cl || slot < 0 || slot >= cl->nsamples) return mgp_set_error(MGP_EINVAL, "bad closure slot %d", slot);
-  k_unpack_sample<<<mgp_blocks_for(cl->V, 4), 256, 0, cl->stream>>>(cl->ds_x + (size_t)slot * 3 * cl->V,
-                                                                    cl->ds_t + (size_t)slot * 3 * cl->V, cl->V,
-                                                                    cl->act[0], cl->target);
+  k_unpack_sample<<<mgp_blocks_for(cl->V, 4), 256, 0, cl->stream>>>(
+      cl->ds_x + (size_t)slot * 3 * cl->V, cl->ds_np ? NULL : cl->ds_t + (size_t)slot * 3 * cl->V, cl->V,
+      cl->act[0], cl->target);
   MGP_CHECK_LAUNCH();
+  if (cl->ds_np) {
+    if (!cl->dout) MGP_CUDA(cudaMalloc(&cl->dout, sizeof(float) * 4 * cl->V));
+    const size_t n3 = (size_t)3 * cl->ds_np;
+    cl->np = cl->ds_np;
+    cl->cur_pc = cl->ds_pc + slot * n3;
+    cl->cur_pt = cl->ds_pt + slot * n3;
+    cl->pmode = 1;
+  } else {
+    cl->pmode = 0;
+  }
   return MGP_OK;
 }
 
@@ -810,11 +1233,16 @@ int mgp_closure_apply(mgp_closure *cl, mgp_ctx *c, double A) {
   cudaStream_t keep = cl->stream;
   cl->stream = c->stream;
   int rc = closure_features(cl, c, A);
+  if (c->timing) cudaEventRecord(c->ev[T_NNCONV][0], c->stream);  // the four convolutions
   for (int l = 0; l < NN_LAYERS - 1 && rc == MGP_OK; l++)
     rc = conv_fwd(cl, cl->act[l], cl->w16[l], cl->b32[l], 0, cl->act[l + 1], NULL, NULL, 0, 0, 0.f);
   if (rc == MGP_OK)
     rc = conv_fwd(cl, cl->act[NN_LAYERS - 1], cl->w16[NN_LAYERS - 1], cl->b32[NN_LAYERS - 1], 3, NULL, NULL, c->frc,
                   c->g.nreal, c->g.P, cl->out_scale);
+  if (c->timing) {
+    cudaEventRecord(c->ev[T_NNCONV][1], c->stream);
+    c->timed[T_NNCONV] = 1;
+  }
   cl->stream = keep;
   return rc;
 }

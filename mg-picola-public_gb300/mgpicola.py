@@ -27,7 +27,8 @@ EXPORTS = [
     "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_closure_create", "mgp_closure_destroy",
     "mgp_closure_get_weights", "mgp_closure_set_weights", "mgp_closure_set_sample", "mgp_closure_get_sample",
     "mgp_closure_forward", "mgp_closure_gradients", "mgp_closure_train_step", "mgp_closure_features",
-    "mgp_closure_target", "mgp_closure_reserve", "mgp_closure_store", "mgp_closure_load", "mgp_set_closure",
+    "mgp_closure_target", "mgp_closure_target_particles", "mgp_closure_set_particle_sample",
+    "mgp_closure_get_particle_sample", "mgp_closure_reserve", "mgp_closure_store", "mgp_closure_load", "mgp_set_closure",
 ]
 
 # field types of mgp_assign_displacement_fields (src/proto.h:155-158)
@@ -135,7 +136,10 @@ def lib():
         L.mgp_closure_train_step.argtypes = [vp, C.c_float, C.POINTER(C.c_double)]
         L.mgp_closure_features.argtypes = [vp, vp, C.c_double]
         L.mgp_closure_target.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
-        L.mgp_closure_reserve.argtypes = [vp, C.c_int]
+        L.mgp_closure_target_particles.argtypes = [vp, vp, vp, C.c_int, C.POINTER(C.c_double)]
+        L.mgp_closure_set_particle_sample.argtypes = [vp, C.c_longlong, fpp, fpp]
+        L.mgp_closure_get_particle_sample.argtypes = [vp, C.POINTER(C.c_longlong), fpp, fpp]
+        L.mgp_closure_reserve.argtypes = [vp, C.c_int, C.c_longlong]
         L.mgp_closure_store.argtypes = [vp, C.c_int]
         L.mgp_closure_load.argtypes = [vp, C.c_int]
         L.mgp_set_closure.argtypes = [vp, vp]
@@ -475,8 +479,26 @@ class Closure:
         _check(lib().mgp_closure_target(self.h, fine.h, coarse.h, C.byref(rms)))
         return rms.value
 
-    def reserve(self, n):
-        _check(lib().mgp_closure_reserve(self.h, n))
+    def target_particles(self, fine, coarse, band=True):
+        rms = C.c_double(0)
+        _check(lib().mgp_closure_target_particles(self.h, fine.h, coarse.h, 1 if band else 0, C.byref(rms)))
+        return rms.value
+
+    def set_particle_sample(self, cells, t):
+        cells = np.ascontiguousarray(cells, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1, 3)
+        _check(lib().mgp_closure_set_particle_sample(self.h, len(cells), _fptr(cells), _fptr(t)))
+
+    def particle_sample(self):
+        n = C.c_longlong(0)
+        _check(lib().mgp_closure_get_particle_sample(self.h, C.byref(n), None, None))
+        cells = np.zeros((n.value, 3), np.float32)
+        t = np.zeros((n.value, 3), np.float32)
+        _check(lib().mgp_closure_get_particle_sample(self.h, C.byref(n), _fptr(cells), _fptr(t)))
+        return cells, t
+
+    def reserve(self, n, np_particles=0):
+        _check(lib().mgp_closure_reserve(self.h, n, np_particles))
 
     def store(self, slot):
         _check(lib().mgp_closure_store(self.h, slot))

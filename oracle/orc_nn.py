@@ -1,6 +1,7 @@
 """FP64 numpy restatement of the learned force closure's network (test
 infrastructure only): four periodic 3x3x3 convolutions, ReLU after the first
-three, MSE loss on the 3 residual components, and the exact backward pass.
+three, MSE loss on the 3 residual components (on the mesh, or at particles
+through the CIC interpolation), and the exact backward pass.
 
 The GPU kernels keep activations, weights and gradients in BF16 between
 layers and accumulate in FP32; `bf16=True` rounds at the same points so that
@@ -40,17 +41,9 @@ def forward(X, Ws, bs, bf16=True):
     return acts, out
 
 
-def loss_and_grads(X, Ws, bs, T, scale, bf16=True):
-    """Loss = sum over voxels and 3 components of (scale out - T)^2 / (3 V);
-    gradients of all weights [4][27][16][16] and biases [4][16]."""
+def backward(acts, g, Ws, bf16=True):
+    """Gradients of all weights and biases from d loss / d out (g, [N,N,N,16])."""
     r = to_bf16 if bf16 else (lambda a: a)
-    acts, out = forward(X, Ws, bs, bf16)
-    V = X.shape[0] * X.shape[1] * X.shape[2]
-    e = scale * out[..., :3] - T
-    loss = float(np.sum(e * e) / (3.0 * V))
-    g = np.zeros(out.shape)
-    g[..., :3] = 2.0 * e * scale / (3.0 * V)
-    g = r(g)
     gw, gb = [None] * 4, [None] * 4
     for l in range(3, -1, -1):
         Xl = acts[l]
@@ -64,4 +57,59 @@ def loss_and_grads(X, Ws, bs, T, scale, bf16=True):
             dx += shift(g @ W[t], (-d[0], -d[1], -d[2]))
         dx = r(dx)
         g = dx * (Xl > 0)
+    return gw, gb
+
+
+def loss_and_grads(X, Ws, bs, T, scale, bf16=True):
+    """Loss = sum over voxels and 3 components of (scale out - T)^2 / (3 V);
+    gradients of all weights [4][27][16][16] and biases [4][16]."""
+    r = to_bf16 if bf16 else (lambda a: a)
+    acts, out = forward(X, Ws, bs, bf16)
+    V = X.shape[0] * X.shape[1] * X.shape[2]
+    e = scale * out[..., :3] - T
+    loss = float(np.sum(e * e) / (3.0 * V))
+    g = np.zeros(out.shape)
+    g[..., :3] = 2.0 * e * scale / (3.0 * V)
+    gw, gb = backward(acts, r(g), Ws, bf16)
+    return loss, out, gw, gb
+
+
+def cic_corners(cells, N):
+    """The 8 (voxel index triple, weight) pairs of the trilinear interpolation
+    at cell coordinates `cells` [np][3] (mesh units) on a periodic N^3 mesh,
+    the weights of the PM gather (src/auxPM.c:560-644)."""
+    fl = np.floor(cells)
+    d = cells - fl
+    i0 = fl.astype(np.int64) % N
+    i1 = (i0 + 1) % N
+    out = []
+    for bx in (0, 1):
+        for by in (0, 1):
+            for bz in (0, 1):
+                idx = tuple(np.where(b, i1[:, a], i0[:, a]) for a, b in enumerate((bx, by, bz)))
+                w = np.ones(len(cells))
+                for a, b in enumerate((bx, by, bz)):
+                    w = w * (d[:, a] if b else 1.0 - d[:, a])
+                out.append((idx, w))
+    return out
+
+
+def loss_and_grads_particles(X, Ws, bs, cells, Tp, scale, bf16=True):
+    """Particle loss = sum over particles and components of
+    (scale u_p - Tp)^2 / (3 np), u_p the trilinear interpolation of the
+    network output at the particle; d loss / d out is the CIC deposit of the
+    residuals."""
+    r = to_bf16 if bf16 else (lambda a: a)
+    acts, out = forward(X, Ws, bs, bf16)
+    N, n = X.shape[0], len(cells)
+    corners = cic_corners(np.asarray(cells, np.float64), N)
+    u = np.zeros((n, 3))
+    for idx, w in corners:
+        u += w[:, None] * out[idx][:, :3]
+    e = scale * u - Tp
+    loss = float(np.sum(e * e) / (3.0 * n))
+    g = np.zeros(out.shape)
+    for idx, w in corners:
+        np.add.at(g, idx + (slice(0, 3),), (2.0 * scale / (3.0 * n)) * w[:, None] * e)
+    gw, gb = backward(acts, r(g), Ws, bf16)
     return loss, out, gw, gb
