@@ -9,22 +9,20 @@
 // first order a linear filter of the potential) and the screening factor
 // min(1, |phi_crit / Phi_N|) for Phi_N < 0 (1 otherwise, and 1 for models
 // without potential screening).  Activations and weights are BF16, every
-// accumulation is FP32 on the tensor cores (mma.sync m16n8k16 bf16).
+// accumulation is FP32 on the tensor cores.
 //
 // Layout: activations channel-last [V][16] bf16 with voxel v = (i N + j) N + k
 // (k fastest, as the mesh rows); weights [27 taps][16 out][16 in], tap =
 // 9 (di+1) + 3 (dj+1) + (dk+1) for offsets d in {-1, 0, 1}.
 //
-// Convolution as implicit GEMM: a block takes 64 consecutive voxels of one
-// (i, j) row; it stages the 9 neighbouring rows (i+di, j+dj), each with one
-// halo voxel on either side, and all weights in shared memory; warp w owns
-// 16 voxels and runs, for each tap, one 16x16x16 product as two m16n8k16
-// MMAs whose A fragment is the 16 voxels shifted by dk (ldmatrix), so every
-// staged row serves the three dk taps.  The data gradient is the same
-// convolution with the weights mirrored (tap -> 26 - tap) and transposed
-// (in <-> out); the weight gradient is, per tap, dY^T X over all voxels,
-// accumulated by persistent blocks in registers and reduced with one FP32
-// atomic per weight per block.
+// Convolution as implicit GEMM on tcgen05 (k_conv_fwd_tc): per 128-voxel
+// segment of an output row, 27 MMAs (M = 128 voxels, N = 16, K = 16) whose A
+// operand is a staged input row shifted by dk, accumulated in tensor memory.
+// The data gradient is the same convolution with the weights mirrored
+// (tap -> 26 - tap) and transposed (in <-> out).  The weight gradient is,
+// per tap, dY^T X over all voxels (M = N = 16 per tap, too small for the
+// 128-row tcgen05 MMA): persistent blocks accumulate it in registers with
+// mma.sync m16n8k16 and reduce it with one FP32 atomic per weight per block.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -90,11 +88,6 @@ constexpr int kThreadsWg = 256;
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
-__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-               : "r"(addr));
-}
 __device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
                : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
@@ -136,138 +129,257 @@ __device__ __forceinline__ void stage_rows(const bf16 *__restrict__ X, int N, in
   }
 }
 
-// Forward convolution, persistent: a CTA keeps all weights in shared memory
-// and walks tiles of CT_I x CT_J output rows (i, j) by CT_SEG voxels (k).
-// For a tile it stages the (CT_I+2) x (CT_J+2) input rows around it, each
-// with one halo voxel on either side (cp.async), so a staged row serves up
-// to 9 output rows; warp w computes output row (i0 + w / CT_J, j0 + w % CT_J)
-// as 4 groups of 16 voxels, reusing each tap's B fragment for the 4 groups.
-// Shared-memory layout of a [voxel][16] bf16 row: the two 16-byte halves of
-// voxel q are swapped when bit 2 of q is set, so the 8 row addresses of any
-// ldmatrix (8 consecutive voxels or 8 consecutive output channels) fall in 8
-// distinct 16-byte bank groups.
-// mode 0: bf16 out, bias + ReLU; 1: bf16 out, no bias (data gradient); 2: f32
-// out [V][4] (channels 0-3), bias; 3: add scale * (out + bias) to the three
-// force grids (channels 0-2).
-constexpr int CT_I = 2, CT_J = 4, CT_SEG = 64;
-constexpr int CT_ROWS = (CT_I + 2) * (CT_J + 2);  // staged rows
-constexpr int CT_Q = CT_SEG + 2;                  // staged voxels per row
-constexpr int kThreadsConv = 32 * CT_I * CT_J;    // one warp per output row
-constexpr size_t kConvSmem = sizeof(bf16) * (NN_WSIZE + (size_t)CT_ROWS * CT_Q * NN_CH);
-
-__device__ __forceinline__ int swz_half(int q, int h) { return h ^ ((q >> 2) & 1); }
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+
+// ------------------------------------------------- tcgen05 convolution
+// The same convolution on the 5th-generation tensor cores: per output row
+// segment of 128 voxels, D[128 x 16] (FP32, in tensor memory) accumulates 27
+// MMAs (M = 128 voxels, N = 16 output channels, K = 16 input channels), one
+// per tap, whose A operand is the staged input row (i+di, j+dj) shifted by dk
+// voxels and whose B operand is the tap's weights, both read from shared
+// memory through matrix descriptors.  A persistent CTA (one per SM) takes
+// tiles of TC_I x TC_J output rows (8 accumulators, 128 TMEM columns) and
+// stages the (TC_I+2) x (TC_J+2) input rows around a tile once.  Staging
+// buffers and accumulators are double-buffered: while the 216 MMAs of tile t
+// run (warp w issues the 27 of output row w; the eight warps'
+// tcgen05.commit arrivals complete an mbarrier), the
+// CTA's cp.async copies bring in tile t+1 and every warp reads its 32 TMEM
+// lanes of 4 accumulators of tile t-1 (tcgen05.ld) for the epilogue.
+// Shared layout (no swizzle, K-major core matrices of 8 rows x 16 bytes):
+//   staged row r: [half h][voxel q][8 channels], half planes TC_Q*16 bytes
+//     apart (leading byte offset), 8-voxel groups 128 bytes apart (stride
+//     byte offset); a dk shift moves the start address by 16 dk bytes.
+//   weights: [tap][half][out 16][8 in], 512 bytes per tap.
+constexpr int TC_I = 2, TC_J = 4, TC_M = 128;
+constexpr int TC_OUT = TC_I * TC_J;               // accumulators per tile
+constexpr int TC_ROWS = (TC_I + 2) * (TC_J + 2);  // staged rows
+constexpr int TC_Q = TC_M + 2;                    // staged voxels per row
+constexpr uint32_t TC_HALF_BYTES = TC_Q * 16;
+constexpr uint32_t TC_ROW_BYTES = 2 * TC_HALF_BYTES;
+constexpr uint32_t TC_W_BYTES = NN_TAPS * 512;
+constexpr uint32_t TC_BUF_BYTES = TC_ROWS * TC_ROW_BYTES;  // one staging buffer
+constexpr uint32_t TC_TMEM_COLS = 2 * TC_OUT * 16;          // two accumulator sets
+constexpr int kThreadsTc = 32 * TC_OUT;  // warp w issues and owns output row w
+constexpr size_t kTcSmem = TC_W_BYTES + 2 * (size_t)TC_BUF_BYTES + 64;  // + 2 mbarriers, TMEM address
+// kind::f16 instruction descriptor: D f32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+
+__device__ int g_conv_err;  // set when a tensor-core wait gave up
+
+// Shared-memory matrix descriptor: start, leading and stride byte offsets
+// (>> 4), bits 46-48 = 0b001, base offset 0, no swizzle.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
+}
+// Wait for the mbarrier phase with the given parity; gives up after about
+// 2e9 SM clocks (1-2 s) and returns false.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > 2000000000LL) return false;
+  }
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
 }
 
-__global__ void __launch_bounds__(kThreadsConv, 3) k_conv_fwd(const bf16 *__restrict__ X, const bf16 *__restrict__ W,
-                                                              const float *__restrict__ bias, int N, int mode,
-                                                              bf16 *__restrict__ Y16, float *__restrict__ Y32,
-                                                              float *__restrict__ frc, long long gstride, long long P,
-                                                              float scale) {
-  extern __shared__ __align__(16) unsigned char conv_smem[];
-  bf16(*ws)[NN_CH] = reinterpret_cast<bf16(*)[NN_CH]>(conv_smem);  // [tap * 16 + out][16 in]
-  bf16(*xs)[CT_Q][NN_CH] = reinterpret_cast<bf16(*)[CT_Q][NN_CH]>(conv_smem + sizeof(bf16) * NN_WSIZE);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int c = tid; c < NN_WSIZE / 8; c += kThreadsConv) {
-    const int row = c >> 1, h = c & 1;  // row = tap * 16 + out
-    cp_async16(&ws[row][8 * swz_half(row & 15, h)], W + (size_t)c * 8);
+// Stage the input rows of tile t into a buffer (cp.async, not waited for).
+__device__ __forceinline__ void tc_stage(const bf16 *__restrict__ X, int N, long long t, int nseg, int tiles_j,
+                                         unsigned char *buf, int tid) {
+  const int seg = (int)(t % nseg);
+  const long long rest = t / nseg;
+  const int i0 = (int)(rest / tiles_j) * TC_I, j0 = (int)(rest % tiles_j) * TC_J, k0 = seg * TC_M;
+  const int qmax = min(TC_M + 1, N - k0 + 1);  // staged voxels past qmax are zero
+  for (int c = tid; c < TC_ROWS * TC_Q * 2; c += kThreadsTc) {
+    const int r = c / (TC_Q * 2), rem = c - r * (TC_Q * 2), q = rem >> 1, h = rem & 1;
+    unsigned char *dst = buf + r * TC_ROW_BYTES + h * TC_HALF_BYTES + q * 16;
+    if (q > qmax) {
+      *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+      continue;
+    }
+    int ii = i0 + r / (TC_J + 2) - 1, jj = j0 + r % (TC_J + 2) - 1, kk = k0 - 1 + q;
+    ii += ii < 0 ? N : 0;
+    ii -= ii >= N ? N : 0;
+    jj += jj < 0 ? N : 0;
+    jj -= jj >= N ? N : 0;
+    kk += kk < 0 ? N : 0;
+    kk -= kk >= N ? N : 0;
+    cp_async16(dst, X + (((long long)ii * N + jj) * N + kk) * NN_CH + 8 * h);
   }
-  const int nseg = (N + CT_SEG - 1) / CT_SEG, tiles_j = N / CT_J;
-  const long long ntiles = (long long)(N / CT_I) * tiles_j * nseg;
-  const int wi = warp / CT_J, wj = warp % CT_J;
-  // ldmatrix lane roles: A (16 voxels x 16 ch), B (16 out x 16 in)
-  const int a_vox = (lane & 7) + 8 * ((lane >> 3) & 1), a_half = lane >> 4;
-  const int b_out = (lane & 7) + 8 * (lane >> 4), b_half = (lane >> 3) & 1;
-  const int vr = lane >> 2, cc = 2 * (lane & 3);
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int seg = (int)(t % nseg);
-    const long long rest = t / nseg;
-    const int i0 = (int)(rest / tiles_j) * CT_I, j0 = (int)(rest % tiles_j) * CT_J, k0 = seg * CT_SEG;
-    const int qmax = min(CT_SEG + 1, N - k0 + 1);  // staged voxels past qmax are zero
-    __syncthreads();  // the previous tile's reads of xs are done
-    for (int c = tid; c < CT_ROWS * CT_Q * 2; c += kThreadsConv) {
-      const int r = c / (CT_Q * 2), rem = c - r * (CT_Q * 2), q = rem >> 1, h = rem & 1;
-      bf16 *dst = &xs[r][q][8 * swz_half(q, h)];
-      if (q > qmax) {
-        *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
-        continue;
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// Epilogue of tile t from the accumulator set at TMEM column `acc`.
+__device__ __forceinline__ void tc_epilogue(long long t, int nseg, int tiles_j, int N, int mode, uint32_t tmem_acc,
+                                            int warp, int lane, const float (&bb)[16], bf16 *__restrict__ Y16,
+                                            float *__restrict__ Y32, float *__restrict__ frc, long long gstride,
+                                            long long P, float scale) {
+  const int seg = (int)(t % nseg);
+  const long long rest = t / nseg;
+  const int i0 = (int)(rest / tiles_j) * TC_I, j0 = (int)(rest % tiles_j) * TC_J, k0 = seg * TC_M;
+  const int lq = warp & 3, obase = (warp >> 2) * 4;  // TMEM lane quarter and 4 accumulators of this warp
+  const int kk = k0 + 32 * lq + lane;
+  for (int o4 = 0; o4 < 4; o4++) {
+    const int o = obase + o4;
+    float v[16];
+    tmem_ld16(tmem_acc + ((uint32_t)(32 * lq) << 16) + o * 16, v);
+    if (kk >= N) continue;
+    const int i = i0 + o / TC_J, j = j0 + o % TC_J;
+    const long long vx = ((long long)i * N + j) * N + kk;
+#pragma unroll
+    for (int q = 0; q < 16; q++) v[q] += bb[q];
+    if (mode <= 1) {
+      __align__(16) __nv_bfloat162 pk[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        float a = v[2 * q], b = v[2 * q + 1];
+        if (mode == 0) {
+          a = fmaxf(a, 0.f);
+          b = fmaxf(b, 0.f);
+        }
+        pk[q] = __floats2bfloat162_rn(a, b);
       }
-      int ii = i0 + r / (CT_J + 2) - 1, jj = j0 + r % (CT_J + 2) - 1, kk = k0 - 1 + q;
-      ii += ii < 0 ? N : 0;
-      ii -= ii >= N ? N : 0;
-      jj += jj < 0 ? N : 0;
-      jj -= jj >= N ? N : 0;
-      kk += kk < 0 ? N : 0;
-      kk -= kk >= N ? N : 0;
-      cp_async16(dst, X + (((long long)ii * N + jj) * N + kk) * NN_CH + 8 * h);
+      reinterpret_cast<uint4 *>(Y16 + vx * NN_CH)[0] = reinterpret_cast<uint4 *>(pk)[0];
+      reinterpret_cast<uint4 *>(Y16 + vx * NN_CH)[1] = reinterpret_cast<uint4 *>(pk)[1];
+    } else if (mode == 2) {
+      reinterpret_cast<float4 *>(Y32)[vx] = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+      const long long gi = ((long long)i * N + j) * P + kk;
+      frc[gi] += scale * v[0];
+      frc[gstride + gi] += scale * v[1];
+      frc[2 * gstride + gi] += scale * v[2];
     }
-    cp_async_wait_all();
+  }
+}
+
+__global__ void __launch_bounds__(kThreadsTc, 1) k_conv_fwd_tc(const bf16 *__restrict__ X, const bf16 *__restrict__ W,
+                                                               const float *__restrict__ bias, int N, int mode,
+                                                               bf16 *__restrict__ Y16, float *__restrict__ Y32,
+                                                               float *__restrict__ frc, long long gstride, long long P,
+                                                               float scale) {
+  extern __shared__ __align__(128) unsigned char tc_smem[];
+  unsigned char *ws = tc_smem;
+  unsigned char *xs = tc_smem + TC_W_BYTES;  // two staging buffers
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(xs + 2 * (size_t)TC_BUF_BYTES);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t ws_a = smem_u32(ws), xs_a = smem_u32(xs);
+  const uint32_t mbar0 = smem_u32(mbar);  // mbarrier of set b at mbar0 + 8 b
+  for (int c = tid; c < NN_WSIZE / 8; c += kThreadsTc) {
+    const int tap = c >> 5, o = (c >> 1) & 15, h = c & 1;
+    cp_async16(ws + tap * 512 + h * 256 + o * 16, W + (size_t)c * 8);
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tslot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(mbar0, TC_OUT);  // one tcgen05.commit per issuing warp
+    mbar_init(mbar0 + 8, TC_OUT);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const int nseg = (N + TC_M - 1) / TC_M, tiles_j = N / TC_J;
+  const long long ntiles = (long long)(N / TC_I) * tiles_j * nseg;
+  float bb[16];
+#pragma unroll
+  for (int q = 0; q < 16; q++) bb[q] = (mode != 1 && bias) ? bias[q] : 0.f;
+  uint32_t ph = 0u;  // bit b: phase parity of mbarrier b
+  long long prev = -1;
+  int it = 0;
+  bool ok = true;
+  if ((long long)blockIdx.x < ntiles) tc_stage(X, N, blockIdx.x, nseg, tiles_j, xs, tid);
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
+    const int b = it & 1;
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    fence_proxy_async();  // staged rows (and weights) visible to the tensor cores
+    tc_fence_before();    // TMEM reads of earlier epilogues ordered before the barrier
     __syncthreads();
-    const int ng = min(4, (N - k0) / 16);  // valid 16-voxel groups (N is a multiple of 16)
-    float acc[4][2][4];
+    if (lane == 0) {  // warp w issues the 27 MMAs of output row w (accumulator w of set b)
+      tc_fence_after();
+      const int wi = warp / TC_J, wj = warp % TC_J;
+      // descriptors of tap 0; a tap adds its byte offset >> 4 to the start-address field
+      const uint64_t da0 = umma_desc(xs_a + b * TC_BUF_BYTES + (wi * (TC_J + 2) + wj) * TC_ROW_BYTES, TC_HALF_BYTES, 128);
+      const uint64_t db0 = umma_desc(ws_a, 256, 128);
+      const uint32_t d = tmem + b * (TC_OUT * 16) + warp * 16;
 #pragma unroll
-    for (int g = 0; g < 4; g++)
-#pragma unroll
-      for (int n = 0; n < 2; n++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) acc[g][n][q] = 0.f;
-#pragma unroll 3
-    for (int tap = 0; tap < NN_TAPS; tap++) {
-      const int di = tap / 9, dj = (tap / 3) % 3, dk = tap % 3;
-      const int r = (wi + di) * (CT_J + 2) + (wj + dj);
-      uint32_t b0, b1, b2, b3;
-      ldsm_x4(smem_u32(&ws[tap * NN_CH + b_out][8 * swz_half(b_out, b_half)]), b0, b1, b2, b3);
-#pragma unroll
-      for (int g = 0; g < 4; g++) {
-        if (g < ng) {
-          const int q = 16 * g + a_vox + dk;
-          uint32_t a0, a1, a2, a3;
-          ldsm_x4(smem_u32(&xs[r][q][8 * swz_half(q, a_half)]), a0, a1, a2, a3);
-          mma16816(acc[g][0], a0, a1, a2, a3, b0, b1);
-          mma16816(acc[g][1], a0, a1, a2, a3, b2, b3);
-        }
+      for (int tap = 0; tap < NN_TAPS; tap++) {
+        const int di = tap / 9, dj = (tap / 3) % 3, dk = tap % 3;
+        const uint32_t offa = ((di * (TC_J + 2) + dj) * TC_ROW_BYTES + dk * 16) >> 4;
+        umma_bf16(d, da0 + offa, db0 + (uint32_t)(tap * 32), kTcIdesc, tap > 0 ? 1u : 0u);
       }
+      umma_commit(mbar0 + 8 * b);
     }
-    // fragment: rows (voxels) lane/4 and lane/4 + 8, columns 2 (lane%4) + {0,1}
-    const int i = i0 + wi, j = j0 + wj;
-#pragma unroll
-    for (int g = 0; g < 4; g++) {
-      if (g >= ng) continue;
-      const int kw = k0 + 16 * g;
-      const long long vb = ((long long)i * N + j) * N + kw;
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const long long v = vb + vr + 8 * h;
-        float o[4] = {acc[g][0][2 * h], acc[g][0][2 * h + 1], acc[g][1][2 * h], acc[g][1][2 * h + 1]};  // cc, cc+1, cc+8, cc+9
-        if (mode != 1 && bias) {
-          o[0] += bias[cc];
-          o[1] += bias[cc + 1];
-          o[2] += bias[cc + 8];
-          o[3] += bias[cc + 9];
-        }
-        if (mode <= 1) {
-          if (mode == 0)
-#pragma unroll
-            for (int q = 0; q < 4; q++) o[q] = fmaxf(o[q], 0.f);
-          reinterpret_cast<__nv_bfloat162 *>(Y16 + v * NN_CH + cc)[0] = __floats2bfloat162_rn(o[0], o[1]);
-          reinterpret_cast<__nv_bfloat162 *>(Y16 + v * NN_CH + cc + 8)[0] = __floats2bfloat162_rn(o[2], o[3]);
-        } else if (cc < 4) {
-          if (mode == 2) {
-            Y32[v * 4 + cc] = o[0];
-            Y32[v * 4 + cc + 1] = o[1];
-          } else {
-            const int kk = kw + vr + 8 * h;
-            const long long gi = ((long long)i * N + j) * P + kk;
-            frc[cc * gstride + gi] += scale * o[0];
-            if (cc + 1 < 3) frc[(cc + 1) * gstride + gi] += scale * o[1];
-          }
-        }
-      }
+    if (prev >= 0) {  // tile prev: its MMAs done -> buffer b^1 free, accumulators b^1 ready
+      ok = mbar_wait(mbar0 + 8 * (b ^ 1), (ph >> (b ^ 1)) & 1u);
+      if (!__syncthreads_and(ok)) break;
+      ph ^= 1u << (b ^ 1);
+      tc_fence_after();
     }
+    const long long next = t + gridDim.x;
+    if (next < ntiles) tc_stage(X, N, next, nseg, tiles_j, xs + (b ^ 1) * TC_BUF_BYTES, tid);
+    if (prev >= 0)
+      tc_epilogue(prev, nseg, tiles_j, N, mode, tmem + (b ^ 1) * (TC_OUT * 16), warp, lane, bb, Y16, Y32, frc, gstride,
+                  P, scale);
+    prev = t;
+  }
+  if (ok && prev >= 0) {
+    const int b = (it - 1) & 1;
+    ok = mbar_wait(mbar0 + 8 * b, (ph >> b) & 1u);
+    if (__syncthreads_and(ok)) {
+      tc_fence_after();
+      tc_epilogue(prev, nseg, tiles_j, N, mode, tmem + b * (TC_OUT * 16), warp, lane, bb, Y16, Y32, frc, gstride, P,
+                  scale);
+    }
+  }
+  if (!ok && tid == 0) atomicExch(&g_conv_err, 1);
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
   }
 }
 
@@ -668,18 +780,25 @@ static int conv_fwd(mgp_closure *cl, const bf16 *X, const bf16 *W, const float *
                     float *frc, long long gstride, long long P, float scale) {
   static int grid = 0;  // resident CTAs of the persistent kernel (one device per process)
   if (!grid) {
-    MGP_CUDA(cudaFuncSetAttribute(k_conv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kConvSmem));
-    int per_sm = 0, sms = 0;
-    MGP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_fwd, kThreadsConv, kConvSmem));
+    MGP_CUDA(cudaFuncSetAttribute(k_conv_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
+    int sms = 0;
     MGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cl->device));
-    grid = sms * (per_sm > 0 ? per_sm : 1);
+    grid = sms;  // one CTA per SM: 213 KB of shared memory, 256 TMEM columns
   }
   const int N = cl->N;
-  const long long tiles = (long long)(N / CT_I) * (N / CT_J) * ((N + CT_SEG - 1) / CT_SEG);
+  const long long tiles = (long long)(N / TC_I) * (N / TC_J) * ((N + TC_M - 1) / TC_M);
   const unsigned blocks = (unsigned)(tiles < grid ? tiles : grid);
-  k_conv_fwd<<<blocks, kThreadsConv, kConvSmem, cl->stream>>>(X, W, bias, N, mode, Y16, Y32, frc, gstride, P, scale);
+  k_conv_fwd_tc<<<blocks, kThreadsTc, kTcSmem, cl->stream>>>(X, W, bias, N, mode, Y16, Y32, frc, gstride, P, scale);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Error flag of the tensor-core waits (read after a synchronisation).
+static int conv_status() {
+  int e = 0;
+  MGP_CUDA(cudaMemcpyFromSymbol(&e, g_conv_err, sizeof(int)));
+  if (e) return mgp_set_error(MGP_ECUDA, "closure convolution: tensor-core completion wait timed out");
   return MGP_OK;
 }
 
@@ -800,6 +919,10 @@ extern "C" int mgp_closure_create(int Nmesh, unsigned seed, int device, mgp_clos
     }                                    \
   } while (0)
   CL_TRY(cudaStreamCreateWithFlags(&cl->stream, cudaStreamNonBlocking));
+  {
+    const int zero = 0;
+    CL_TRY(cudaMemcpyToSymbol(g_conv_err, &zero, sizeof(int)));
+  }
   cl->own_stream = 1;
   uint64_t st = 0x9E3779B97F4A7C15ULL ^ seed;
   for (int l = 0; l < NN_LAYERS; l++) {
@@ -892,6 +1015,7 @@ extern "C" int mgp_closure_forward(mgp_closure *cl, float *out) {
   MGP_CUDA(cudaSetDevice(cl->device));
   NN_RET(closure_forward(cl));
   MGP_CUDA(cudaStreamSynchronize(cl->stream));
+  NN_RET(conv_status());
   if (out) {
     std::vector<float> h((size_t)cl->V * 4);
     MGP_CUDA(cudaMemcpy(h.data(), cl->out, sizeof(float) * h.size(), cudaMemcpyDeviceToHost));
@@ -908,6 +1032,7 @@ extern "C" int mgp_closure_gradients(mgp_closure *cl, double *loss, float *gw, f
   NN_RET(closure_forward(cl));
   NN_RET(closure_backward(cl));
   MGP_CUDA(cudaStreamSynchronize(cl->stream));
+  NN_RET(conv_status());
   if (loss) MGP_CUDA(cudaMemcpy(loss, cl->loss, sizeof(double), cudaMemcpyDeviceToHost));
   for (int l = 0; l < NN_LAYERS; l++) {
     if (gw) MGP_CUDA(cudaMemcpy(gw + l * NN_WSIZE, cl->gw[l], sizeof(float) * NN_WSIZE, cudaMemcpyDeviceToHost));
@@ -937,6 +1062,7 @@ extern "C" int mgp_closure_train_step(mgp_closure *cl, float lr, double *loss) {
   if (loss) {
     MGP_CUDA(cudaMemcpyAsync(loss, cl->loss, sizeof(double), cudaMemcpyDeviceToHost, cl->stream));
     MGP_CUDA(cudaStreamSynchronize(cl->stream));
+    NN_RET(conv_status());
   }
   return MGP_OK;
 }
