@@ -316,7 +316,10 @@ int mgp_closure_target(mgp_closure *cl, mgp_ctx *fine, mgp_ctx *coarse, double *
  * loss is the mean over particles and components of (out_scale u_p - r_p)^2,
  * u_p the CIC interpolation of the network output at x_p, so the network
  * learns the correction as the kick will use it; its gradient is the CIC
- * deposit of the residuals.  The contexts hold the same particles.  band:
+ * deposit of the residuals.  A sample made from contexts takes its own rms
+ * as the scale and its loss relative to that rms squared (the network
+ * predicts the residual in units of its rms, so every time step weighs the
+ * same); host samples use out_scale and an unnormalised loss.  The contexts hold the same particles.  band:
  * restrict the fine force to the modes of the coarse mesh first (|k_i| below
  * its Nyquist frequency), which drops the sub-grid force.  Host
  * form: np particles, cells and t [np][3] (cells in mesh units, [0, Nmesh));
@@ -329,8 +332,21 @@ int mgp_closure_get_particle_sample(mgp_closure *cl, long long *np, float *cells
 int mgp_closure_reserve(mgp_closure *cl, int n, long long np);
 int mgp_closure_store(mgp_closure *cl, int slot);
 int mgp_closure_load(mgp_closure *cl, int slot);
-/* Use the closure in every later mgp_get_displacements of ctx (NULL detaches). */
+/* Use the closure in every later mgp_get_displacements of ctx (NULL detaches):
+ * the network output, high-passed (modes of wavelength >= lambda mesh cells
+ * and the mean removed; default lambda 0: the mean only) and scaled by
+ * out_scale, is added
+ * to the force transforms before their C2R.  The particle loss trains the
+ * same high-passed output; mgp_closure_forward returns the raw output. */
 int mgp_set_closure(mgp_ctx *ctx, mgp_closure *cl);
+int mgp_closure_set_highpass(mgp_closure *cl, double lambda_cells);
+/* The in-step output scale: a table of the residual rms s(a) of the training
+ * snapshots (n points, a increasing), interpolated log-log at the step's
+ * scale factor; without a table (n = 0) out_scale is used.  scale_at returns
+ * the value the step uses. */
+int mgp_closure_set_scale_table(mgp_closure *cl, int n, const double *a, const double *s);
+double mgp_closure_scale_at(mgp_closure *cl, double A);
+double mgp_closure_get_highpass(mgp_closure *cl);
 
 /* Copy an internal grid to a host buffer (diagnostics and parity tests).
  * which: 0 density (real padded [N][N][2(N/2+1)] float), 1 delta(k)

@@ -42,8 +42,9 @@ def schedule(nsteps, zi=19.0, zf=0.0):
 
 def collect(cl, seed, model, Nc, r, Ns, box, nsteps, snaps, slot, band=True):
     """Run the fine mesh for one seed and store a sample at each step in
-    `snaps`; returns the next free slot and the targets' rms values."""
-    rms = []
+    `snaps`; returns the next free slot, the targets' rms values and the
+    samples' scale factors."""
+    rms, avals = [], []
     with M.Context(run_params(Nc * r, Ns, box, seed, model, 64)) as fine, \
             M.Context(run_params(Nc, Ns, box, seed, model, 64)) as coarse:
         fine.displacement_fields()
@@ -56,10 +57,19 @@ def collect(cl, seed, model, Nc, r, Ns, box, nsteps, snaps, slot, band=True):
                 coarse.get_displacements(A)
                 cl.features(coarse, A)
                 rms.append(cl.target_particles(fine, coarse, band=band))
+                avals.append(A)
                 cl.store(slot)
                 slot += 1
             fine.kick_drift(AI, AF, A, AFF, drift=True)
-    return slot, rms
+    return slot, rms, avals
+
+
+def scale_table(rms, avals):
+    """Residual rms per snapshot scale factor (rms over the seeds)."""
+    a = np.asarray(avals)
+    r = np.asarray(rms)
+    ua = np.unique(a)
+    return ua, np.array([np.sqrt(np.mean(r[a == u] ** 2)) for u in ua])
 
 
 def train(cl, nsamples, epochs, lr0, seed=0, log=None):
@@ -134,35 +144,41 @@ def evaluate(cl, seed, model, Nc, r, Ns, box, nsteps, kmax=1.0):
 
 
 def run_c5(model, Nc=256, r=3, box=256.0, nsteps=30, train_seeds=range(7001, 7017), test_seeds=range(7017, 7021),
-           every=3, epochs=16, lr=2e-3, kmax=1.0, tol=0.01, band=True, net_seed=5, log=print, weights_out=None):
+           every=3, epochs=16, lr=2e-3, kmax=1.0, tol=0.01, band=True, net_seed=5, log=print, weights_out=None,
+           highpass=None):
     """Learned-closure workload: collect training samples from the fine and
     coarse meshes of `train_seeds`, train, and judge on `test_seeds` by the
     final P(k) against the fine mesh.  The closure is accepted up to the k
     where its error stays within `tol`; beyond that the plain force is the
     result."""
     Ns = Nc
-    snaps = set(range(every - 1, nsteps, every))
+    snaps = set(range(0, nsteps, every)) | {nsteps - 1}
     out = dict(model=model, Nmesh=Nc, Nmesh_fine=r * Nc, Nsample=Ns, Box=box, nsteps=nsteps, epochs=epochs, lr=lr,
                band_limited_target=band, train_seeds=list(train_seeds), test_seeds=list(test_seeds), tol=tol, kmax=kmax)
     with M.Closure(Nc, seed=net_seed) as cl:
+        if highpass is not None:
+            cl.set_highpass(highpass)
         cl.reserve(len(train_seeds) * len(snaps), Ns ** 3)
         t0 = time.perf_counter()
-        slot, rms = 0, []
+        slot, rms, avals = 0, [], []
         for sd in train_seeds:
-            slot, rr = collect(cl, sd, model, Nc, r, Ns, box, nsteps, snaps, slot, band=band)
+            slot, rr, aa = collect(cl, sd, model, Nc, r, Ns, box, nsteps, snaps, slot, band=band)
             rms += rr
+            avals += aa
         out["collect_s"] = time.perf_counter() - t0
         out["samples"] = slot
-        scale = float(np.sqrt(np.mean(np.square(rms))))
-        cl.set_weights(None, None, scale)
+        ta, ts = scale_table(rms, avals)
+        cl.set_scale_table(ta, ts)  # the step scales the output by the residual rms at its a
+        out["scale_table"] = [ta.tolist(), ts.tolist()]
         t0 = time.perf_counter()
         hist = train(cl, slot, epochs, lr, log=log)
         out["train_s"] = time.perf_counter() - t0
         out["train_steps"] = epochs * slot
-        out["loss_over_var"] = [h / scale ** 2 for h in hist]
+        out["loss_over_var"] = hist  # each sample's loss is relative to its own mean square target
+        out["highpass_lambda_cells"] = cl.highpass()
         if weights_out:
             w, b, sc = cl.weights()
-            np.savez(weights_out, w=w, b=b, scale=sc)
+            np.savez(weights_out, w=w, b=b, scale_a=ta, scale_s=ts, highpass_lambda_cells=cl.highpass())
         evs = []
         for sd in test_seeds:
             ev = evaluate(cl, sd, model, Nc, r, Ns, box, nsteps, kmax=kmax)
@@ -179,6 +195,24 @@ def run_c5(model, Nc=256, r=3, box=256.0, nsteps=30, train_seeds=range(7001, 701
     return out
 
 
+def kernel_probe(N, train=False, reps=3, seed=1):
+    """A fixed closure workload for profiling: random features on an N^3
+    mesh, then `reps` forward passes (or, with train, `reps` Adam steps on a
+    particle sample of N^3 random particles)."""
+    rng = np.random.default_rng(seed)
+    x = rng.normal(0, 1, (N ** 3, 3)).astype(np.float32)
+    with M.Closure(N, seed=3) as cl:
+        cl.set_sample(x, None)
+        if train:
+            cells = np.minimum(rng.uniform(0, N, (N ** 3, 3)).astype(np.float32), np.float32(N - 1e-3))
+            cl.set_particle_sample(cells, rng.normal(0, 1, (N ** 3, 3)).astype(np.float32))
+            for _ in range(reps):
+                cl.train_step(1e-4)
+        else:
+            for _ in range(reps):
+                cl.forward()
+
+
 def main(argv=None):
     import argparse
     import json
@@ -192,12 +226,19 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--every", type=int, default=3)
     ap.add_argument("--full-target", action="store_true", help="do not band-limit the fine force")
+    ap.add_argument("--highpass", type=float, default=None,
+                    help="cutoff wavelength (cells) of the closure output's high-pass")
     ap.add_argument("--out", default=None, help="JSON report")
     ap.add_argument("--weights", default=None, help=".npz for the trained weights")
+    ap.add_argument("--probe", type=int, default=0, help="profiling workload on an N^3 mesh instead of training")
+    ap.add_argument("--probe-train", action="store_true", help="the probe runs Adam steps")
     a = ap.parse_args(argv)
+    if a.probe:
+        kernel_probe(a.probe, train=a.probe_train)
+        return None
     rep = run_c5(a.model, Nc=a.nmesh, box=float(a.nmesh), train_seeds=range(7001, 7001 + a.ntrain),
                  test_seeds=range(7017, 7017 + a.ntest), every=a.every, epochs=a.epochs, lr=a.lr,
-                 band=not a.full_target, weights_out=a.weights)
+                 band=not a.full_target, weights_out=a.weights, highpass=a.highpass)
     if a.out:
         with open(a.out, "w") as f:
             json.dump(rep, f, indent=1)

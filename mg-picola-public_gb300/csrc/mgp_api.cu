@@ -677,15 +677,15 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   tstart(c, T_FORCES);
   RET_IF(mgp_launch_forces(c->dk, c->rho, coupling, mass2, mg_kind, N, c->p.Box, c->frc, c->g.nreal, c->stream));
   tstop(c, T_FORCES);
-  tstart(c, T_C2R);
-  for (int g = 0; g < 3; g++)
-    MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(c->frc + g * c->g.nreal), (cufftReal *)(c->frc + g * c->g.nreal)));
-  tstop(c, T_C2R);
-  if (c->closure) {
+  if (c->closure) {  // learned residual force, added to the force transforms
     tstart(c, T_NN);
     RET_IF(mgp_closure_apply(c->closure, c, A));
     tstop(c, T_NN);
   }
+  tstart(c, T_C2R);
+  for (int g = 0; g < 3; g++)
+    MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(c->frc + g * c->g.nreal), (cufftReal *)(c->frc + g * c->g.nreal)));
+  tstop(c, T_C2R);
   c->have_forces = 1;
   return MGP_OK;
 }

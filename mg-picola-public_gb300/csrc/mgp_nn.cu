@@ -9,20 +9,26 @@
 // first order a linear filter of the potential) and the screening factor
 // min(1, |phi_crit / Phi_N|) for Phi_N < 0 (1 otherwise, and 1 for models
 // without potential screening).  Activations and weights are BF16, every
-// accumulation is FP32 on the tensor cores.
+// accumulation is FP32 on the tensor cores (mma.sync m16n8k16 bf16).
 //
 // Layout: activations channel-last [V][16] bf16 with voxel v = (i N + j) N + k
 // (k fastest, as the mesh rows); weights [27 taps][16 out][16 in], tap =
 // 9 (di+1) + 3 (dj+1) + (dk+1) for offsets d in {-1, 0, 1}.
 //
-// Convolution as implicit GEMM on tcgen05 (k_conv_fwd_tc): per 128-voxel
-// segment of an output row, 27 MMAs (M = 128 voxels, N = 16, K = 16) whose A
-// operand is a staged input row shifted by dk, accumulated in tensor memory.
-// The data gradient is the same convolution with the weights mirrored
-// (tap -> 26 - tap) and transposed (in <-> out).  The weight gradient is,
-// per tap, dY^T X over all voxels (M = N = 16 per tap, too small for the
-// 128-row tcgen05 MMA): persistent blocks accumulate it in registers with
-// mma.sync m16n8k16 and reduce it with one FP32 atomic per weight per block.
+// Convolution as implicit GEMM (k_conv_fwd): persistent blocks keep all
+// weights in shared memory and walk tiles of 2 x 4 output rows (i, j) by 64
+// voxels; a tile stages the 4 x 6 input rows around it once (cp.async), and
+// warp w computes one output row as 4 groups of 16 voxels, each tap one
+// 16x16x16 product (two m16n8k16 MMAs) whose A fragment is the staged row
+// shifted by dk (ldmatrix).  With 16 channels the product per tap is N = 16
+// wide: a tcgen05 version (M = 128 voxels, N = 16, K = 16 per tap, TMEM
+// accumulators) measured 1.5x slower per layer on the same 192^3 input, its
+// MMAs bound by per-instruction operand fetch rather than the datapath, so
+// the register-blocked mma.sync kernel is the one used.  The data gradient is
+// the same convolution with the weights mirrored (tap -> 26 - tap) and
+// transposed (in <-> out); the weight gradient is, per tap, dY^T X over all
+// voxels, accumulated by persistent blocks in registers and reduced with one
+// FP32 atomic per weight per block.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -67,11 +73,20 @@ struct mgp_closure {
   // working sample (own buffers or a stored slot)
   int pmode;
   long long np;                            // particles of the working sample
+  float pscale;                            // output scale of the working particle sample
+  int pnorm;                               // 1: its loss is relative to pscale^2 (samples from contexts)
   long long own_np;                        // capacity of pc / pt
   float *pc, *pt;
   const float *cur_pc, *cur_pt;
-  float *dout;                             // d loss / d out [V][4] (particle loss)
+  // high-passed network output and its gradient (particle loss and the
+  // in-step path): three padded real grids each, [3][N][N][P]
+  float *ugrid, *dgrid;
+  cufftHandle plan_r2c, plan_c2r;          // in-place N^3 transforms of one grid
+  int have_plans;
+  float hp_lambda;                         // high-pass cutoff wavelength in cells (0: only the mean removed)
   float *fscr;                             // band-limited fine force, 3 fine grids (lazy)
+  float *wg_partial;                       // weight-gradient partial sums per block (lazy)
+  int wg_blocks;
   long long fscr_floats;
   // stored training samples: features (3 bf16) per voxel and either grid
   // targets (3 f32 per voxel, ds_np = 0) or particle samples (ds_np > 0)
@@ -79,14 +94,22 @@ struct mgp_closure {
   long long ds_np;
   bf16 *ds_x;
   float *ds_t, *ds_pc, *ds_pt;
+  float *ds_s;                             // host: output scale per stored particle sample
+  // residual scale vs scale factor for the in-step path (log-log table; n = 0: out_scale)
+  int scale_n;
+  double *scale_a, *scale_s;
 };
 
 namespace {
 
-constexpr int kThreadsWg = 256;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(addr));
 }
 __device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
@@ -102,360 +125,285 @@ __device__ __forceinline__ void mma16816(float (&d)[4], uint32_t a0, uint32_t a1
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// Stage the 9 rows (i+di, j+dj), voxels k0-1 .. k0+NN_SEG (periodic), of a
-// [V][16] bf16 tensor: xs[r][q] with r = 3 (di+1) + (dj+1), q = voxel - (k0-1).
-// A segment that ends before k0+NN_SEG (N not a multiple of NN_SEG) stages
-// voxels k0-1 .. N (the last one wraps to 0) and zeros after them, so every
-// read stays inside the tensor.
-__device__ __forceinline__ void stage_rows(const bf16 *__restrict__ X, int N, int i, int j, int k0,
-                                           bf16 (*xs)[NN_SEG + 2][NN_CH], int tid, int nthr) {
-  const int per_row = (NN_SEG + 2) * 2;  // 16-byte chunks per staged row
-  const int qmax = min(NN_SEG + 1, N - k0 + 1);
-  for (int c = tid; c < 9 * per_row; c += nthr) {
-    const int r = c / per_row, q = (c % per_row) >> 1, h = c & 1;
-    if (q > qmax) {
-      reinterpret_cast<uint4 *>(&xs[r][q][0])[h] = make_uint4(0, 0, 0, 0);
-      continue;
-    }
-    int ii = i + r / 3 - 1, jj = j + r % 3 - 1, kk = k0 - 1 + q;
-    ii += ii < 0 ? N : 0;
-    ii -= ii >= N ? N : 0;
-    jj += jj < 0 ? N : 0;
-    jj -= jj >= N ? N : 0;
-    kk += kk < 0 ? N : 0;
-    kk -= kk >= N ? N : 0;
-    const long long v = ((long long)ii * N + jj) * N + kk;
-    reinterpret_cast<uint4 *>(&xs[r][q][0])[h] = reinterpret_cast<const uint4 *>(X + v * NN_CH)[h];
-  }
-}
+// Forward convolution, persistent: a CTA keeps all weights in shared memory
+// and walks tiles of CT_I x CT_J output rows (i, j) by CT_SEG voxels (k).
+// For a tile it stages the (CT_I+2) x (CT_J+2) input rows around it, each
+// with one halo voxel on either side (cp.async), so a staged row serves up
+// to 9 output rows; warp w computes output row (i0 + w / CT_J, j0 + w % CT_J)
+// as 4 groups of 16 voxels, reusing each tap's B fragment for the 4 groups.
+// Shared-memory layout of a [voxel][16] bf16 row: the two 16-byte halves of
+// voxel q are swapped when bit 2 of q is set, so the 8 row addresses of any
+// ldmatrix (8 consecutive voxels or 8 consecutive output channels) fall in 8
+// distinct 16-byte bank groups.
+// mode 0: bf16 out, bias + ReLU; 1: bf16 out, no bias, times relu'(gate)
+// (data gradient through the previous layer's ReLU, gate = its output); 2: f32
+// out [V][4] (channels 0-3), bias; 3: out + bias into three padded real
+// grids (channels 0-2; grid c at frc + c gstride, rows of P floats).
+constexpr int CT_I = 2, CT_J = 4, CT_SEG = 64;
+constexpr int CT_ROWS = (CT_I + 2) * (CT_J + 2);  // staged rows
+constexpr int CT_Q = CT_SEG + 2;                  // staged voxels per row
+constexpr int kThreadsConv = 32 * CT_I * CT_J;    // one warp per output row
+constexpr size_t kConvSmem = sizeof(bf16) * (NN_WSIZE + (size_t)CT_ROWS * CT_Q * NN_CH);
 
+__device__ __forceinline__ int swz_half(int q, int h) { return h ^ ((q >> 2) & 1); }
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
 }
-
-// ------------------------------------------------- tcgen05 convolution
-// The same convolution on the 5th-generation tensor cores: per output row
-// segment of 128 voxels, D[128 x 16] (FP32, in tensor memory) accumulates 27
-// MMAs (M = 128 voxels, N = 16 output channels, K = 16 input channels), one
-// per tap, whose A operand is the staged input row (i+di, j+dj) shifted by dk
-// voxels and whose B operand is the tap's weights, both read from shared
-// memory through matrix descriptors.  A persistent CTA (one per SM) takes
-// tiles of TC_I x TC_J output rows (8 accumulators, 128 TMEM columns) and
-// stages the (TC_I+2) x (TC_J+2) input rows around a tile once.  Staging
-// buffers and accumulators are double-buffered: while the 216 MMAs of tile t
-// run (warp w issues the 27 of output row w; the eight warps'
-// tcgen05.commit arrivals complete an mbarrier), the
-// CTA's cp.async copies bring in tile t+1 and every warp reads its 32 TMEM
-// lanes of 4 accumulators of tile t-1 (tcgen05.ld) for the epilogue.
-// Shared layout (no swizzle, K-major core matrices of 8 rows x 16 bytes):
-//   staged row r: [half h][voxel q][8 channels], half planes TC_Q*16 bytes
-//     apart (leading byte offset), 8-voxel groups 128 bytes apart (stride
-//     byte offset); a dk shift moves the start address by 16 dk bytes.
-//   weights: [tap][half][out 16][8 in], 512 bytes per tap.
-constexpr int TC_I = 2, TC_J = 4, TC_M = 128;
-constexpr int TC_OUT = TC_I * TC_J;               // accumulators per tile
-constexpr int TC_ROWS = (TC_I + 2) * (TC_J + 2);  // staged rows
-constexpr int TC_Q = TC_M + 2;                    // staged voxels per row
-constexpr uint32_t TC_HALF_BYTES = TC_Q * 16;
-constexpr uint32_t TC_ROW_BYTES = 2 * TC_HALF_BYTES;
-constexpr uint32_t TC_W_BYTES = NN_TAPS * 512;
-constexpr uint32_t TC_BUF_BYTES = TC_ROWS * TC_ROW_BYTES;  // one staging buffer
-constexpr uint32_t TC_TMEM_COLS = 2 * TC_OUT * 16;          // two accumulator sets
-constexpr int kThreadsTc = 32 * TC_OUT;  // warp w issues and owns output row w
-constexpr size_t kTcSmem = TC_W_BYTES + 2 * (size_t)TC_BUF_BYTES + 64;  // + 2 mbarriers, TMEM address
-// kind::f16 instruction descriptor: D f32 (bits 4-5 = 1), A and B bf16
-// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
-constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
-
-__device__ int g_conv_err;  // set when a tensor-core wait gave up
-
-// Shared-memory matrix descriptor: start, leading and stride byte offsets
-// (>> 4), bits 46-48 = 0b001, base offset 0, no swizzle.
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
-}
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(da), "l"(db), "r"(idesc), "r"(acc));
-}
-__device__ __forceinline__ void umma_commit(uint32_t mbar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
-               : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
-__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
-}
-// Wait for the mbarrier phase with the given parity; gives up after about
-// 2e9 SM clocks (1-2 s) and returns false.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-  const long long t0 = clock64();
-  for (;;) {
-    uint32_t done;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(mbar), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (clock64() - t0 > 2000000000LL) return false;
-  }
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      "tcgen05.wait::ld.sync.aligned;\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr)
-      : "memory");
-#pragma unroll
-  for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
-// Stage the input rows of tile t into a buffer (cp.async, not waited for).
-__device__ __forceinline__ void tc_stage(const bf16 *__restrict__ X, int N, long long t, int nseg, int tiles_j,
-                                         unsigned char *buf, int tid) {
-  const int seg = (int)(t % nseg);
-  const long long rest = t / nseg;
-  const int i0 = (int)(rest / tiles_j) * TC_I, j0 = (int)(rest % tiles_j) * TC_J, k0 = seg * TC_M;
-  const int qmax = min(TC_M + 1, N - k0 + 1);  // staged voxels past qmax are zero
-  for (int c = tid; c < TC_ROWS * TC_Q * 2; c += kThreadsTc) {
-    const int r = c / (TC_Q * 2), rem = c - r * (TC_Q * 2), q = rem >> 1, h = rem & 1;
-    unsigned char *dst = buf + r * TC_ROW_BYTES + h * TC_HALF_BYTES + q * 16;
-    if (q > qmax) {
-      *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
-      continue;
-    }
-    int ii = i0 + r / (TC_J + 2) - 1, jj = j0 + r % (TC_J + 2) - 1, kk = k0 - 1 + q;
-    ii += ii < 0 ? N : 0;
-    ii -= ii >= N ? N : 0;
-    jj += jj < 0 ? N : 0;
-    jj -= jj >= N ? N : 0;
-    kk += kk < 0 ? N : 0;
-    kk -= kk >= N ? N : 0;
-    cp_async16(dst, X + (((long long)ii * N + jj) * N + kk) * NN_CH + 8 * h);
-  }
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-
-// Epilogue of tile t from the accumulator set at TMEM column `acc`.
-__device__ __forceinline__ void tc_epilogue(long long t, int nseg, int tiles_j, int N, int mode, uint32_t tmem_acc,
-                                            int warp, int lane, const float (&bb)[16], bf16 *__restrict__ Y16,
-                                            float *__restrict__ Y32, float *__restrict__ frc, long long gstride,
-                                            long long P, float scale) {
-  const int seg = (int)(t % nseg);
-  const long long rest = t / nseg;
-  const int i0 = (int)(rest / tiles_j) * TC_I, j0 = (int)(rest % tiles_j) * TC_J, k0 = seg * TC_M;
-  const int lq = warp & 3, obase = (warp >> 2) * 4;  // TMEM lane quarter and 4 accumulators of this warp
-  const int kk = k0 + 32 * lq + lane;
-  for (int o4 = 0; o4 < 4; o4++) {
-    const int o = obase + o4;
-    float v[16];
-    tmem_ld16(tmem_acc + ((uint32_t)(32 * lq) << 16) + o * 16, v);
-    if (kk >= N) continue;
-    const int i = i0 + o / TC_J, j = j0 + o % TC_J;
-    const long long vx = ((long long)i * N + j) * N + kk;
-#pragma unroll
-    for (int q = 0; q < 16; q++) v[q] += bb[q];
-    if (mode <= 1) {
-      __align__(16) __nv_bfloat162 pk[8];
-#pragma unroll
-      for (int q = 0; q < 8; q++) {
-        float a = v[2 * q], b = v[2 * q + 1];
-        if (mode == 0) {
-          a = fmaxf(a, 0.f);
-          b = fmaxf(b, 0.f);
-        }
-        pk[q] = __floats2bfloat162_rn(a, b);
-      }
-      reinterpret_cast<uint4 *>(Y16 + vx * NN_CH)[0] = reinterpret_cast<uint4 *>(pk)[0];
-      reinterpret_cast<uint4 *>(Y16 + vx * NN_CH)[1] = reinterpret_cast<uint4 *>(pk)[1];
-    } else if (mode == 2) {
-      reinterpret_cast<float4 *>(Y32)[vx] = make_float4(v[0], v[1], v[2], v[3]);
-    } else {
-      const long long gi = ((long long)i * N + j) * P + kk;
-      frc[gi] += scale * v[0];
-      frc[gstride + gi] += scale * v[1];
-      frc[2 * gstride + gi] += scale * v[2];
-    }
-  }
-}
-
-__global__ void __launch_bounds__(kThreadsTc, 1) k_conv_fwd_tc(const bf16 *__restrict__ X, const bf16 *__restrict__ W,
-                                                               const float *__restrict__ bias, int N, int mode,
-                                                               bf16 *__restrict__ Y16, float *__restrict__ Y32,
-                                                               float *__restrict__ frc, long long gstride, long long P,
-                                                               float scale) {
-  extern __shared__ __align__(128) unsigned char tc_smem[];
-  unsigned char *ws = tc_smem;
-  unsigned char *xs = tc_smem + TC_W_BYTES;  // two staging buffers
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(xs + 2 * (size_t)TC_BUF_BYTES);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+__global__ void __launch_bounds__(kThreadsConv, 3) k_conv_fwd(const bf16 *__restrict__ X, const bf16 *__restrict__ W,
+                                                              const float *__restrict__ bias,
+                                                              const bf16 *__restrict__ gate, int N, int mode,
+                                                              bf16 *__restrict__ Y16, float *__restrict__ Y32,
+                                                              float *__restrict__ frc, long long gstride, long long P,
+                                                              float scale) {
+  extern __shared__ __align__(16) unsigned char conv_smem[];
+  bf16(*ws)[NN_CH] = reinterpret_cast<bf16(*)[NN_CH]>(conv_smem);  // [tap * 16 + out][16 in]
+  bf16(*xs)[CT_Q][NN_CH] = reinterpret_cast<bf16(*)[CT_Q][NN_CH]>(conv_smem + sizeof(bf16) * NN_WSIZE);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t ws_a = smem_u32(ws), xs_a = smem_u32(xs);
-  const uint32_t mbar0 = smem_u32(mbar);  // mbarrier of set b at mbar0 + 8 b
-  for (int c = tid; c < NN_WSIZE / 8; c += kThreadsTc) {
-    const int tap = c >> 5, o = (c >> 1) & 15, h = c & 1;
-    cp_async16(ws + tap * 512 + h * 256 + o * 16, W + (size_t)c * 8);
+  for (int c = tid; c < NN_WSIZE / 8; c += kThreadsConv) {
+    const int row = c >> 1, h = c & 1;  // row = tap * 16 + out
+    cp_async16(&ws[row][8 * swz_half(row & 15, h)], W + (size_t)c * 8);
   }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tslot)),
-                 "r"(TC_TMEM_COLS)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
-  }
-  if (tid == 0) {
-    mbar_init(mbar0, TC_OUT);  // one tcgen05.commit per issuing warp
-    mbar_init(mbar0 + 8, TC_OUT);
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tslot;
-  const int nseg = (N + TC_M - 1) / TC_M, tiles_j = N / TC_J;
-  const long long ntiles = (long long)(N / TC_I) * tiles_j * nseg;
-  float bb[16];
-#pragma unroll
-  for (int q = 0; q < 16; q++) bb[q] = (mode != 1 && bias) ? bias[q] : 0.f;
-  uint32_t ph = 0u;  // bit b: phase parity of mbarrier b
-  long long prev = -1;
-  int it = 0;
-  bool ok = true;
-  if ((long long)blockIdx.x < ntiles) tc_stage(X, N, blockIdx.x, nseg, tiles_j, xs, tid);
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
-    const int b = it & 1;
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
-    fence_proxy_async();  // staged rows (and weights) visible to the tensor cores
-    tc_fence_before();    // TMEM reads of earlier epilogues ordered before the barrier
+  const int nseg = (N + CT_SEG - 1) / CT_SEG, tiles_j = N / CT_J;
+  const long long ntiles = (long long)(N / CT_I) * tiles_j * nseg;
+  const int wi = warp / CT_J, wj = warp % CT_J;
+  // ldmatrix lane roles: A (16 voxels x 16 ch), B (16 out x 16 in)
+  const int a_vox = (lane & 7) + 8 * ((lane >> 3) & 1), a_half = lane >> 4;
+  const int b_out = (lane & 7) + 8 * (lane >> 4), b_half = (lane >> 3) & 1;
+  const int vr = lane >> 2, cc = 2 * (lane & 3);
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int seg = (int)(t % nseg);
+    const long long rest = t / nseg;
+    const int i0 = (int)(rest / tiles_j) * CT_I, j0 = (int)(rest % tiles_j) * CT_J, k0 = seg * CT_SEG;
+    const int qmax = min(CT_SEG + 1, N - k0 + 1);  // staged voxels past qmax are zero
+    __syncthreads();  // the previous tile's reads of xs are done
+    for (int c = tid; c < CT_ROWS * CT_Q * 2; c += kThreadsConv) {
+      const int r = c / (CT_Q * 2), rem = c - r * (CT_Q * 2), q = rem >> 1, h = rem & 1;
+      bf16 *dst = &xs[r][q][8 * swz_half(q, h)];
+      if (q > qmax) {
+        *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+        continue;
+      }
+      int ii = i0 + r / (CT_J + 2) - 1, jj = j0 + r % (CT_J + 2) - 1, kk = k0 - 1 + q;
+      ii += ii < 0 ? N : 0;
+      ii -= ii >= N ? N : 0;
+      jj += jj < 0 ? N : 0;
+      jj -= jj >= N ? N : 0;
+      kk += kk < 0 ? N : 0;
+      kk -= kk >= N ? N : 0;
+      cp_async16(dst, X + (((long long)ii * N + jj) * N + kk) * NN_CH + 8 * h);
+    }
+    cp_async_wait_all();
     __syncthreads();
-    if (lane == 0) {  // warp w issues the 27 MMAs of output row w (accumulator w of set b)
-      tc_fence_after();
-      const int wi = warp / TC_J, wj = warp % TC_J;
-      // descriptors of tap 0; a tap adds its byte offset >> 4 to the start-address field
-      const uint64_t da0 = umma_desc(xs_a + b * TC_BUF_BYTES + (wi * (TC_J + 2) + wj) * TC_ROW_BYTES, TC_HALF_BYTES, 128);
-      const uint64_t db0 = umma_desc(ws_a, 256, 128);
-      const uint32_t d = tmem + b * (TC_OUT * 16) + warp * 16;
+    const int ng = min(4, (N - k0) / 16);  // valid 16-voxel groups (N is a multiple of 16)
+    float acc[4][2][4];
 #pragma unroll
-      for (int tap = 0; tap < NN_TAPS; tap++) {
-        const int di = tap / 9, dj = (tap / 3) % 3, dk = tap % 3;
-        const uint32_t offa = ((di * (TC_J + 2) + dj) * TC_ROW_BYTES + dk * 16) >> 4;
-        umma_bf16(d, da0 + offa, db0 + (uint32_t)(tap * 32), kTcIdesc, tap > 0 ? 1u : 0u);
+    for (int g = 0; g < 4; g++)
+#pragma unroll
+      for (int n = 0; n < 2; n++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[g][n][q] = 0.f;
+#pragma unroll 3
+    for (int tap = 0; tap < NN_TAPS; tap++) {
+      const int di = tap / 9, dj = (tap / 3) % 3, dk = tap % 3;
+      const int r = (wi + di) * (CT_J + 2) + (wj + dj);
+      uint32_t b0, b1, b2, b3;
+      ldsm_x4(smem_u32(&ws[tap * NN_CH + b_out][8 * swz_half(b_out, b_half)]), b0, b1, b2, b3);
+#pragma unroll
+      for (int g = 0; g < 4; g++) {
+        if (g < ng) {
+          const int q = 16 * g + a_vox + dk;
+          uint32_t a0, a1, a2, a3;
+          ldsm_x4(smem_u32(&xs[r][q][8 * swz_half(q, a_half)]), a0, a1, a2, a3);
+          mma16816(acc[g][0], a0, a1, a2, a3, b0, b1);
+          mma16816(acc[g][1], a0, a1, a2, a3, b2, b3);
+        }
       }
-      umma_commit(mbar0 + 8 * b);
     }
-    if (prev >= 0) {  // tile prev: its MMAs done -> buffer b^1 free, accumulators b^1 ready
-      ok = mbar_wait(mbar0 + 8 * (b ^ 1), (ph >> (b ^ 1)) & 1u);
-      if (!__syncthreads_and(ok)) break;
-      ph ^= 1u << (b ^ 1);
-      tc_fence_after();
+    // fragment: rows (voxels) lane/4 and lane/4 + 8, columns 2 (lane%4) + {0,1}
+    const int i = i0 + wi, j = j0 + wj;
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+      if (g >= ng) continue;
+      const int kw = k0 + 16 * g;
+      const long long vb = ((long long)i * N + j) * N + kw;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const long long v = vb + vr + 8 * h;
+        float o[4] = {acc[g][0][2 * h], acc[g][0][2 * h + 1], acc[g][1][2 * h], acc[g][1][2 * h + 1]};  // cc, cc+1, cc+8, cc+9
+        if (mode != 1 && bias) {
+          o[0] += bias[cc];
+          o[1] += bias[cc + 1];
+          o[2] += bias[cc + 8];
+          o[3] += bias[cc + 9];
+        }
+        if (mode <= 1) {
+          if (mode == 0) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) o[q] = fmaxf(o[q], 0.f);
+          } else if (gate) {
+            const __nv_bfloat162 g0 = reinterpret_cast<const __nv_bfloat162 *>(gate + v * NN_CH + cc)[0];
+            const __nv_bfloat162 g1 = reinterpret_cast<const __nv_bfloat162 *>(gate + v * NN_CH + cc + 8)[0];
+            if (!(__bfloat162float(g0.x) > 0.f)) o[0] = 0.f;
+            if (!(__bfloat162float(g0.y) > 0.f)) o[1] = 0.f;
+            if (!(__bfloat162float(g1.x) > 0.f)) o[2] = 0.f;
+            if (!(__bfloat162float(g1.y) > 0.f)) o[3] = 0.f;
+          }
+          reinterpret_cast<__nv_bfloat162 *>(Y16 + v * NN_CH + cc)[0] = __floats2bfloat162_rn(o[0], o[1]);
+          reinterpret_cast<__nv_bfloat162 *>(Y16 + v * NN_CH + cc + 8)[0] = __floats2bfloat162_rn(o[2], o[3]);
+        } else if (cc < 4) {
+          if (mode == 2) {
+            Y32[v * 4 + cc] = o[0];
+            Y32[v * 4 + cc + 1] = o[1];
+          } else {
+            const int kk = kw + vr + 8 * h;
+            const long long gi = ((long long)i * N + j) * P + kk;
+            frc[cc * gstride + gi] = o[0];
+            if (cc + 1 < 3) frc[(cc + 1) * gstride + gi] = o[1];
+          }
+        }
+      }
     }
-    const long long next = t + gridDim.x;
-    if (next < ntiles) tc_stage(X, N, next, nseg, tiles_j, xs + (b ^ 1) * TC_BUF_BYTES, tid);
-    if (prev >= 0)
-      tc_epilogue(prev, nseg, tiles_j, N, mode, tmem + (b ^ 1) * (TC_OUT * 16), warp, lane, bb, Y16, Y32, frc, gstride,
-                  P, scale);
-    prev = t;
-  }
-  if (ok && prev >= 0) {
-    const int b = (it - 1) & 1;
-    ok = mbar_wait(mbar0 + 8 * b, (ph >> b) & 1u);
-    if (__syncthreads_and(ok)) {
-      tc_fence_after();
-      tc_epilogue(prev, nseg, tiles_j, N, mode, tmem + b * (TC_OUT * 16), warp, lane, bb, Y16, Y32, frc, gstride, P,
-                  scale);
-    }
-  }
-  if (!ok && tid == 0) atomicExch(&g_conv_err, 1);
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 0) {
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
   }
 }
 
-// Weight and bias gradients: dW[tap][o][c] += sum_v dY[v][o] X[v + d(tap)][c],
-// db[o] += sum_v dY[v][o]; persistent blocks over (row, segment) units.
-__global__ void __launch_bounds__(kThreadsWg) k_conv_wgrad(const bf16 *__restrict__ X, const bf16 *__restrict__ dY,
-                                                           int N, float *__restrict__ dW, float *__restrict__ db) {
-  __shared__ __align__(16) bf16 xs[9][NN_SEG + 2][NN_CH];
-  __shared__ __align__(16) bf16 ys[NN_SEG][NN_CH];
-  const int nseg = (N + NN_SEG - 1) / NN_SEG;
-  const long long units = (long long)N * N * nseg;
+// Weight and bias gradients, dW[tap][o][c] = sum_v dY[v][o] X[v + d(tap)][c]
+// and db[o] = sum_v dY[v][o], over the same tiles as the forward kernel: a
+// persistent block stages the 4 x 6 input rows and the 8 dY rows of a tile
+// (cp.async, swizzled rows), and warp w owns the three taps dk = 0..2 of
+// staged-row offset (di, dj) = (w / 3, w % 3): for each output row it loads
+// the dY^T fragments once (ldmatrix.trans) and runs them against the three
+// dk-shifted X fragments; warp o < 8 also multiplies output row o's dY^T by a
+// ones fragment for the bias.  Sums stay in registers across tiles and are
+// written once per block to `partial` [block][NN_WSIZE + 8 x 16]; a second
+// kernel adds the blocks in a fixed order (deterministic gradients).
+constexpr int kThreadsWg = 32 * 9;
+constexpr int kWgPartial = NN_WSIZE + 8 * NN_CH;
+constexpr size_t kWgSmem = sizeof(bf16) * ((size_t)CT_ROWS * CT_Q * NN_CH + (size_t)CT_I * CT_J * CT_SEG * NN_CH);
+
+__global__ void __launch_bounds__(kThreadsWg, 3) k_conv_wgrad(const bf16 *__restrict__ X, const bf16 *__restrict__ dY,
+                                                              int N, float *__restrict__ partial) {
+  extern __shared__ __align__(16) unsigned char wg_smem[];
+  bf16(*xs)[CT_Q][NN_CH] = reinterpret_cast<bf16(*)[CT_Q][NN_CH]>(wg_smem);
+  bf16(*ys)[CT_SEG][NN_CH] =
+      reinterpret_cast<bf16(*)[CT_SEG][NN_CH]>(wg_smem + sizeof(bf16) * (size_t)CT_ROWS * CT_Q * NN_CH);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  float acc[4][2][4];
+  const int rdi = warp / 3, rdj = warp % 3;
+  float acc[3][2][4], bacc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-  for (int t = 0; t < 4; t++)
+  for (int t = 0; t < 3; t++)
 #pragma unroll
     for (int n = 0; n < 2; n++)
 #pragma unroll
       for (int q = 0; q < 4; q++) acc[t][n][q] = 0.f;
-  float bacc = 0.f;
+  const uint32_t ones = 0x3F803F80u;  // two bf16 1.0
   // ldmatrix.trans lane roles: A = dY^T (16 out x 16 voxels), B = X (16 voxels x 16 in)
   const int a_vox = (lane & 7) + 8 * (lane >> 4), a_half = (lane >> 3) & 1;
   const int b_vox = (lane & 7) + 8 * ((lane >> 3) & 1), b_half = lane >> 4;
-  for (long long u = blockIdx.x; u < units; u += gridDim.x) {
-    const long long row = u / nseg;
-    const int seg = (int)(u - row * nseg);
-    const int i = (int)(row / N), j = (int)(row - (long long)i * N), k0 = seg * NN_SEG;
-    __syncthreads();
-    stage_rows(X, N, i, j, k0, xs, tid, kThreadsWg);
-    for (int c = tid; c < NN_SEG * 2; c += kThreadsWg) {
-      const int q = c >> 1, h = c & 1, kk = k0 + q;
-      uint4 val = make_uint4(0, 0, 0, 0);
-      if (kk < N) val = reinterpret_cast<const uint4 *>(dY + (((long long)i * N + j) * N + kk) * NN_CH)[h];
-      reinterpret_cast<uint4 *>(&ys[q][0])[h] = val;
+  const int nseg = (N + CT_SEG - 1) / CT_SEG, tiles_j = N / CT_J;
+  const long long ntiles = (long long)(N / CT_I) * tiles_j * nseg;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int seg = (int)(t % nseg);
+    const long long rest = t / nseg;
+    const int i0 = (int)(rest / tiles_j) * CT_I, j0 = (int)(rest % tiles_j) * CT_J, k0 = seg * CT_SEG;
+    const int qmax = min(CT_SEG + 1, N - k0 + 1);  // staged voxels past qmax are zero
+    __syncthreads();                              // the previous tile's reads are done
+    for (int c = tid; c < CT_ROWS * CT_Q * 2; c += kThreadsWg) {
+      const int r = c / (CT_Q * 2), rem = c - r * (CT_Q * 2), q = rem >> 1, h = rem & 1;
+      bf16 *dst = &xs[r][q][8 * swz_half(q, h)];
+      if (q > qmax) {
+        *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+        continue;
+      }
+      int ii = i0 + r / (CT_J + 2) - 1, jj = j0 + r % (CT_J + 2) - 1, kk = k0 - 1 + q;
+      ii += ii < 0 ? N : 0;
+      ii -= ii >= N ? N : 0;
+      jj += jj < 0 ? N : 0;
+      jj -= jj >= N ? N : 0;
+      kk += kk < 0 ? N : 0;
+      kk -= kk >= N ? N : 0;
+      cp_async16(dst, X + (((long long)ii * N + jj) * N + kk) * NN_CH + 8 * h);
     }
+    for (int c = tid; c < CT_I * CT_J * CT_SEG * 2; c += kThreadsWg) {
+      const int o = c / (CT_SEG * 2), rem = c - o * (CT_SEG * 2), q = rem >> 1, h = rem & 1;
+      bf16 *dst = &ys[o][q][8 * swz_half(q, h)];
+      const int kk = k0 + q;
+      if (kk >= N) {
+        *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+        continue;
+      }
+      const int i = i0 + o / CT_J, j = j0 + o % CT_J;
+      cp_async16(dst, dY + (((long long)i * N + j) * N + kk) * NN_CH + 8 * h);
+    }
+    cp_async_wait_all();
     __syncthreads();
-    if (tid < NN_CH)
-      for (int q = 0; q < NN_SEG; q++) bacc += __bfloat162float(ys[q][tid]);
+    const int ng = min(CT_SEG / 16, (N - k0) / 16);  // 16-voxel steps holding data
+    for (int o = 0; o < CT_I * CT_J; o++) {
+      const int r = (o / CT_J + rdi) * (CT_J + 2) + (o % CT_J + rdj);
 #pragma unroll
-    for (int t = 0; t < 4; t++) {
-      const int tap = warp + 8 * t;
-      if (tap >= NN_TAPS) break;
-      const int r = tap / 3, dk = tap % 3;
+      for (int ks = 0; ks < CT_SEG / 16; ks++) {
+        if (ks >= ng) break;
+        const int qa = 16 * ks + a_vox;
+        uint32_t a0, a1, a2, a3;
+        ldsm_x4_t(smem_u32(&ys[o][qa][8 * swz_half(qa, a_half)]), a0, a1, a2, a3);
+        if (o == warp) mma16816(bacc, a0, a1, a2, a3, ones, ones);
 #pragma unroll
-      for (int ks = 0; ks < NN_SEG / 16; ks++) {
-        uint32_t a0, a1, a2, a3, b0, b1, b2, b3;
-        ldsm_x4_t(smem_u32(&ys[16 * ks + a_vox][8 * a_half]), a0, a1, a2, a3);
-        ldsm_x4_t(smem_u32(&xs[r][16 * ks + dk + b_vox][8 * b_half]), b0, b1, b2, b3);
-        mma16816(acc[t][0], a0, a1, a2, a3, b0, b1);
-        mma16816(acc[t][1], a0, a1, a2, a3, b2, b3);
+        for (int dk = 0; dk < 3; dk++) {
+          const int qb = 16 * ks + dk + b_vox;
+          uint32_t b0, b1, b2, b3;
+          ldsm_x4_t(smem_u32(&xs[r][qb][8 * swz_half(qb, b_half)]), b0, b1, b2, b3);
+          mma16816(acc[dk][0], a0, a1, a2, a3, b0, b1);
+          mma16816(acc[dk][1], a0, a1, a2, a3, b2, b3);
+        }
       }
     }
   }
   // fragment: rows (out) lane/4, lane/4 + 8; columns (in) 2 (lane%4) + {0,1} (+8 for n-tile 1)
+  float *pb = partial + (size_t)blockIdx.x * kWgPartial;
   const int o0 = lane >> 2, c0 = 2 * (lane & 3);
 #pragma unroll
-  for (int t = 0; t < 4; t++) {
-    const int tap = warp + 8 * t;
-    if (tap >= NN_TAPS) break;
-    float *w = dW + tap * NN_CH * NN_CH;
+  for (int dk = 0; dk < 3; dk++) {
+    float *w = pb + (3 * warp + dk) * NN_CH * NN_CH;
 #pragma unroll
     for (int n = 0; n < 2; n++) {
-      atomicAdd(w + o0 * NN_CH + c0 + 8 * n, acc[t][n][0]);
-      atomicAdd(w + o0 * NN_CH + c0 + 8 * n + 1, acc[t][n][1]);
-      atomicAdd(w + (o0 + 8) * NN_CH + c0 + 8 * n, acc[t][n][2]);
-      atomicAdd(w + (o0 + 8) * NN_CH + c0 + 8 * n + 1, acc[t][n][3]);
+      w[o0 * NN_CH + c0 + 8 * n] = acc[dk][n][0];
+      w[o0 * NN_CH + c0 + 8 * n + 1] = acc[dk][n][1];
+      w[(o0 + 8) * NN_CH + c0 + 8 * n] = acc[dk][n][2];
+      w[(o0 + 8) * NN_CH + c0 + 8 * n + 1] = acc[dk][n][3];
     }
   }
-  if (tid < NN_CH) atomicAdd(db + tid, bacc);
+  if (warp < CT_I * CT_J && (lane & 3) == 0) {  // every column of the ones product holds the row sum
+    pb[NN_WSIZE + warp * NN_CH + o0] = bacc[0];
+    pb[NN_WSIZE + warp * NN_CH + o0 + 8] = bacc[2];
+  }
 }
 
-// dY *= relu'(Y) (Y the layer's bf16 output)
-__global__ void k_relu_grad(bf16 *__restrict__ dY, const bf16 *__restrict__ Y, long long n) {
-  long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride)
-    if (!(__bfloat162float(Y[q]) > 0.f)) dY[q] = __float2bfloat16_rn(0.f);
+// dW and db from the per-block partial sums in a fixed order: thread row ty
+// adds blocks ty, ty + 8, ... in index order, then row 0 adds the 8 row sums
+// in order (deterministic gradients).  blockDim (32, 8), 32 outputs a block.
+__global__ void k_wgrad_reduce(const float *__restrict__ partial, int nblk, float *__restrict__ dW,
+                               float *__restrict__ db) {
+  __shared__ float sh[8][32];
+  const int tx = threadIdx.x, ty = threadIdx.y, e = blockIdx.x * 32 + tx;
+  float s = 0.f;
+  if (e < NN_WSIZE) {
+    for (int b = ty; b < nblk; b += 8) s += partial[(size_t)b * kWgPartial + e];
+  } else if (e < NN_WSIZE + NN_CH) {
+    const int c = e - NN_WSIZE;
+    for (int b = ty; b < nblk; b += 8)
+      for (int w = 0; w < 8; w++) s += partial[(size_t)b * kWgPartial + NN_WSIZE + w * NN_CH + c];
+  }
+  sh[ty][tx] = s;
+  __syncthreads();
+  if (ty == 0) {
+    float t = 0.f;
+    for (int r = 0; r < 8; r++) t += sh[r][tx];
+    if (e < NN_WSIZE) dW[e] = t;
+    else if (e < NN_WSIZE + NN_CH) db[e - NN_WSIZE] = t;
+  }
 }
 
 // Wt[26 - tap][c][o] = W[tap][o][c]
@@ -657,14 +605,15 @@ __global__ void k_particle_target(const float *__restrict__ ff, long long fg, in
 }
 
 // Particle loss = sum over particles and components of (s u_p - r_p)^2 / (3 np),
-// u_p the CIC interpolation of the network output (out [V][4], channels 0-2)
-// at the particle; its gradient d loss / d out is the CIC deposit of
-// 2 s (s u_p - r_p) / (3 np), accumulated into dout [V][4] (float4 atomics).
+// u_p the CIC interpolation at the particle of the (high-passed) network
+// output, held as three padded real grids (grid c at u + c gstride, rows of
+// P floats); its gradient d loss / d u is the CIC deposit of
+// 2 s (s u_p - r_p) / (3 np) into three grids of the same layout (atomics).
 constexpr int kThreadsPl = 256;
-__global__ void __launch_bounds__(kThreadsPl) k_particle_loss(const float *__restrict__ out, int N, long long np,
-                                                              const float *__restrict__ pc,
+__global__ void __launch_bounds__(kThreadsPl) k_particle_loss(const float *__restrict__ u, long long gstride, long long P,
+                                                              int N, long long np, const float *__restrict__ pc,
                                                               const float *__restrict__ pt, float s, float inv,
-                                                              float *__restrict__ dout, double *__restrict__ loss) {
+                                                              float *__restrict__ du, double *__restrict__ loss) {
   __shared__ double sh[kThreadsPl / 32];
   double acc = 0.0;
   long long stride = (long long)gridDim.x * blockDim.x;
@@ -680,30 +629,28 @@ __global__ void __launch_bounds__(kThreadsPl) k_particle_loss(const float *__res
       i0[a] = ic;
       i1[a] = ic + 1 == N ? 0 : ic + 1;
     }
-    long long v[8];
+    long long g[8];
     float wt[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) {
       const int bx = c >> 2, by = (c >> 1) & 1, bz = c & 1;
-      v[c] = ((long long)(bx ? i1[0] : i0[0]) * N + (by ? i1[1] : i0[1])) * N + (bz ? i1[2] : i0[2]);
+      g[c] = ((long long)(bx ? i1[0] : i0[0]) * N + (by ? i1[1] : i0[1])) * P + (bz ? i1[2] : i0[2]);
       wt[c] = (bx ? d[0] : 1.f - d[0]) * (by ? d[1] : 1.f - d[1]) * (bz ? d[2] : 1.f - d[2]);
     }
-    float u0 = 0.f, u1 = 0.f, u2 = 0.f;
+    float e[3];
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-      const float4 o = __ldg(reinterpret_cast<const float4 *>(out) + v[c]);
-      u0 = fmaf(wt[c], o.x, u0);
-      u1 = fmaf(wt[c], o.y, u1);
-      u2 = fmaf(wt[c], o.z, u2);
-    }
-    const float e0 = s * u0 - pt[p], e1 = s * u1 - pt[np + p], e2 = s * u2 - pt[2 * np + p];
-    acc += (double)e0 * e0 + (double)e1 * e1 + (double)e2 * e2;
-    const float g = 2.f * s * inv;
+    for (int q = 0; q < 3; q++) {
+      float uq = 0.f;
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-      const float gw = g * wt[c];
-      atomicAdd(reinterpret_cast<float4 *>(dout) + v[c], make_float4(gw * e0, gw * e1, gw * e2, 0.f));
+      for (int c = 0; c < 8; c++) uq = fmaf(wt[c], __ldg(u + q * gstride + g[c]), uq);
+      e[q] = s * uq - pt[q * np + p];
+      acc += (double)e[q] * e[q];
     }
+    const float gs = 2.f * s * inv;
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+#pragma unroll
+      for (int c = 0; c < 8; c++) atomicAdd(du + q * gstride + g[c], gs * wt[c] * e[q]);
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
@@ -715,19 +662,55 @@ __global__ void __launch_bounds__(kThreadsPl) k_particle_loss(const float *__res
   }
 }
 
-// dout [V][4] f32 -> the BF16 gradient [V][16] of the last layer (channels 0-2)
-__global__ void k_dout_to_bf16(const float *__restrict__ dout, long long V, bf16 *__restrict__ g) {
+// Three padded real grids (channels 0-2) -> the BF16 gradient [V][16] of the
+// last layer.
+__global__ void k_grids_to_bf16(const float *__restrict__ du, long long gstride, long long P, int N,
+                                bf16 *__restrict__ g) {
+  const long long V = (long long)N * N * N;
   long long stride = (long long)gridDim.x * blockDim.x;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += stride) {
-    const float4 d = reinterpret_cast<const float4 *>(dout)[v];
-    __align__(16) bf16 row[NN_CH];
+    const long long row = v / N;
+    const long long gi = row * P + (v - row * N);
+    __align__(16) bf16 r[NN_CH];
 #pragma unroll
-    for (int c = 0; c < NN_CH; c++) row[c] = __float2bfloat16_rn(0.f);
-    row[0] = __float2bfloat16_rn(d.x);
-    row[1] = __float2bfloat16_rn(d.y);
-    row[2] = __float2bfloat16_rn(d.z);
-    reinterpret_cast<uint4 *>(g + v * NN_CH)[0] = reinterpret_cast<uint4 *>(row)[0];
-    reinterpret_cast<uint4 *>(g + v * NN_CH)[1] = reinterpret_cast<uint4 *>(row)[1];
+    for (int c = 0; c < NN_CH; c++) r[c] = __float2bfloat16_rn(0.f);
+    r[0] = __float2bfloat16_rn(du[gi]);
+    r[1] = __float2bfloat16_rn(du[gstride + gi]);
+    r[2] = __float2bfloat16_rn(du[2 * gstride + gi]);
+    reinterpret_cast<uint4 *>(g + v * NN_CH)[0] = reinterpret_cast<uint4 *>(r)[0];
+    reinterpret_cast<uint4 *>(g + v * NN_CH)[1] = reinterpret_cast<uint4 *>(r)[1];
+  }
+}
+
+// Sharp high-pass of three transformed grids (complex [N][N][N/2+1] each,
+// grid c at src + c cstride): modes with wavelength N / |n| >= lambda cells
+// (n the integer wave vector) are zeroed, the others scaled by `factor`;
+// added to dst (the force transforms) when dst is given, else in place.
+__global__ void k_highpass(float2 *__restrict__ src, long long cstride, int N, float lambda, float factor,
+                           float2 *__restrict__ dst) {
+  const int NH = N / 2 + 1;
+  const long long n = (long long)N * N * NH;
+  const float kc2 = lambda > 0.f ? ((float)N / lambda) * ((float)N / lambda) : 0.f;  // |n|^2 kept from here
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+    const int kz = (int)(q % NH);
+    const long long r = q / NH;
+    const int j = (int)(r % N), i = (int)(r / N);
+    const int ki = i <= N / 2 ? i : i - N, kj = j <= N / 2 ? j : j - N;
+    const float k2 = (float)(ki * ki + kj * kj + kz * kz);
+    const float h = (k2 > 0.f && k2 > kc2) ? factor : 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float2 v = src[c * cstride + q];
+      if (dst) {
+        float2 o = dst[c * cstride + q];
+        o.x += h * v.x;
+        o.y += h * v.y;
+        dst[c * cstride + q] = o;
+      } else {
+        src[c * cstride + q] = make_float2(h * v.x, h * v.y);
+      }
+    }
   }
 }
 
@@ -776,48 +759,104 @@ __global__ void k_sumsq_flat(const float *__restrict__ a, long long n, double *_
     if (rc_ != MGP_OK) return rc_; \
   } while (0)
 
-static int conv_fwd(mgp_closure *cl, const bf16 *X, const bf16 *W, const float *bias, int mode, bf16 *Y16, float *Y32,
-                    float *frc, long long gstride, long long P, float scale) {
-  static int grid = 0;  // resident CTAs of the persistent kernel (one device per process)
-  if (!grid) {
-    MGP_CUDA(cudaFuncSetAttribute(k_conv_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
-    int sms = 0;
-    MGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cl->device));
-    grid = sms;  // one CTA per SM: 213 KB of shared memory, 256 TMEM columns
+// Output / gradient grids and the closure's own transforms (lazy).
+static int ensure_hp(mgp_closure *cl) {
+  const long long gf = (long long)cl->N * cl->N * cl->P;
+  if (!cl->ugrid) MGP_CUDA(cudaMalloc(&cl->ugrid, sizeof(float) * 3 * gf));
+  if (!cl->dgrid) MGP_CUDA(cudaMalloc(&cl->dgrid, sizeof(float) * 3 * gf));
+  if (!cl->have_plans) {
+    long long n[3] = {cl->N, cl->N, cl->N};
+    long long rembed[3] = {cl->N, cl->N, cl->P}, cembed[3] = {cl->N, cl->N, cl->P / 2};
+    const long long rdist = gf, cdist = gf / 2;
+    size_t ws = 0;
+    MGP_CUFFT(cufftCreate(&cl->plan_r2c));
+    MGP_CUFFT(cufftCreate(&cl->plan_c2r));
+    cl->have_plans = 1;
+    MGP_CUFFT(cufftMakePlanMany64(cl->plan_r2c, 3, n, rembed, 1, rdist, cembed, 1, cdist, CUFFT_R2C, 1, &ws));
+    MGP_CUFFT(cufftMakePlanMany64(cl->plan_c2r, 3, n, cembed, 1, cdist, rembed, 1, rdist, CUFFT_C2R, 1, &ws));
   }
-  const int N = cl->N;
-  const long long tiles = (long long)(N / TC_I) * (N / TC_J) * ((N + TC_M - 1) / TC_M);
-  const unsigned blocks = (unsigned)(tiles < grid ? tiles : grid);
-  k_conv_fwd_tc<<<blocks, kThreadsTc, kTcSmem, cl->stream>>>(X, W, bias, N, mode, Y16, Y32, frc, gstride, P, scale);
-  MGP_CHECK_LAUNCH();
-  g_kernel_launches++;
   return MGP_OK;
 }
 
-// Error flag of the tensor-core waits (read after a synchronisation).
-static int conv_status() {
-  int e = 0;
-  MGP_CUDA(cudaMemcpyFromSymbol(&e, g_conv_err, sizeof(int)));
-  if (e) return mgp_set_error(MGP_ECUDA, "closure convolution: tensor-core completion wait timed out");
+// In place: the three grids at g become their high-pass (R2C, filter with
+// the 1/N^3 of the round trip, C2R) on stream st.
+static int highpass_grids(mgp_closure *cl, float *g, cudaStream_t st) {
+  const long long gf = (long long)cl->N * cl->N * cl->P;
+  MGP_CUFFT(cufftSetStream(cl->plan_r2c, st));
+  MGP_CUFFT(cufftSetStream(cl->plan_c2r, st));
+  for (int c = 0; c < 3; c++)
+    MGP_CUFFT(cufftExecR2C(cl->plan_r2c, (cufftReal *)(g + c * gf), (cufftComplex *)(g + c * gf)));
+  k_highpass<<<mgp_blocks_for(gf / 2, 4), 256, 0, st>>>((float2 *)g, gf / 2, cl->N, cl->hp_lambda,
+                                                      (float)(1.0 / ((double)cl->V)), NULL);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  for (int c = 0; c < 3; c++)
+    MGP_CUFFT(cufftExecC2R(cl->plan_c2r, (cufftComplex *)(g + c * gf), (cufftReal *)(g + c * gf)));
+  return MGP_OK;
+}
+
+static int conv_fwd(mgp_closure *cl, const bf16 *X, const bf16 *W, const float *bias, const bf16 *gate, int mode,
+                    bf16 *Y16, float *Y32,
+                    float *frc, long long gstride, long long P, float scale) {
+  static int grid = 0;  // resident CTAs of the persistent kernel (one device per process)
+  if (!grid) {
+    MGP_CUDA(cudaFuncSetAttribute(k_conv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kConvSmem));
+    int per_sm = 0, sms = 0;
+    MGP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_fwd, kThreadsConv, kConvSmem));
+    MGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cl->device));
+    grid = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  const int N = cl->N;
+  const long long tiles = (long long)(N / CT_I) * (N / CT_J) * ((N + CT_SEG - 1) / CT_SEG);
+  const unsigned blocks = (unsigned)(tiles < grid ? tiles : grid);
+  k_conv_fwd<<<blocks, kThreadsConv, kConvSmem, cl->stream>>>(X, W, bias, gate, N, mode, Y16, Y32, frc, gstride, P,
+                                                              scale);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
   return MGP_OK;
 }
 
 static int conv_wgrad(mgp_closure *cl, const bf16 *X, const bf16 *dY, float *dW, float *db) {
-  int sms = 152;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cl->device);
-  const int nseg = (cl->N + NN_SEG - 1) / NN_SEG;
-  long long units = (long long)cl->N * cl->N * nseg, blocks = (long long)sms * 4;
-  if (blocks > units) blocks = units;
-  k_conv_wgrad<<<(unsigned)blocks, kThreadsWg, 0, cl->stream>>>(X, dY, cl->N, dW, db);
+  static int grid = 0;  // resident blocks of the persistent kernel (one device per process)
+  if (!grid) {
+    MGP_CUDA(cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWgSmem));
+    MGP_CUDA(cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int per_sm = 0, sms = 0;
+    MGP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_wgrad, kThreadsWg, kWgSmem));
+    MGP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cl->device));
+    grid = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  const int N = cl->N;
+  const long long tiles = (long long)(N / CT_I) * (N / CT_J) * ((N + CT_SEG - 1) / CT_SEG);
+  const int blocks = (int)(tiles < grid ? tiles : grid);
+  if (cl->wg_blocks < blocks) {
+    if (cl->wg_partial) cudaFree(cl->wg_partial);
+    cl->wg_partial = NULL;
+    cl->wg_blocks = 0;
+    MGP_CUDA(cudaMalloc(&cl->wg_partial, sizeof(float) * (size_t)kWgPartial * blocks));
+    cl->wg_blocks = blocks;
+  }
+  k_conv_wgrad<<<blocks, kThreadsWg, kWgSmem, cl->stream>>>(X, dY, N, cl->wg_partial);
   MGP_CHECK_LAUNCH();
-  g_kernel_launches++;
+  k_wgrad_reduce<<<(NN_WSIZE + NN_CH + 31) / 32, dim3(32, 8), 0, cl->stream>>>(cl->wg_partial, blocks, dW, db);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches += 2;
   return MGP_OK;
 }
 
-static int closure_forward(mgp_closure *cl) {
+// Forward pass; grid = 0: raw output into out [V][4]; grid = 1: the
+// high-passed output into ugrid (the particle loss and the in-step path).
+static int closure_forward(mgp_closure *cl, int grid) {
   for (int l = 0; l < NN_LAYERS - 1; l++)
-    NN_RET(conv_fwd(cl, cl->act[l], cl->w16[l], cl->b32[l], 0, cl->act[l + 1], NULL, NULL, 0, 0, 0.f));
-  return conv_fwd(cl, cl->act[NN_LAYERS - 1], cl->w16[NN_LAYERS - 1], cl->b32[NN_LAYERS - 1], 2, NULL, cl->out, NULL,
+    NN_RET(conv_fwd(cl, cl->act[l], cl->w16[l], cl->b32[l], NULL, 0, cl->act[l + 1], NULL, NULL, 0, 0, 0.f));
+  if (grid) {
+    NN_RET(ensure_hp(cl));
+    NN_RET(conv_fwd(cl, cl->act[NN_LAYERS - 1], cl->w16[NN_LAYERS - 1], cl->b32[NN_LAYERS - 1], NULL, 3, NULL, NULL,
+                    cl->ugrid, (long long)cl->N * cl->N * cl->P, cl->P, 0.f));
+    return highpass_grids(cl, cl->ugrid, cl->stream);
+  }
+  return conv_fwd(cl, cl->act[NN_LAYERS - 1], cl->w16[NN_LAYERS - 1], cl->b32[NN_LAYERS - 1], NULL, 2, NULL, cl->out,
+                  NULL,
                   0, 0, 0.f);
 }
 
@@ -826,14 +865,18 @@ static int closure_backward(mgp_closure *cl) {
   const long long V = cl->V;
   MGP_CUDA(cudaMemsetAsync(cl->loss, 0, sizeof(double), cl->stream));
   if (cl->pmode) {
-    MGP_CUDA(cudaMemsetAsync(cl->dout, 0, sizeof(float) * 4 * V, cl->stream));
+    const long long gf = (long long)cl->N * cl->N * cl->P;
+    MGP_CUDA(cudaMemsetAsync(cl->dgrid, 0, sizeof(float) * 3 * gf, cl->stream));
     k_particle_loss<<<mgp_blocks_for(cl->np, 8), kThreadsPl, 0, cl->stream>>>(
-        cl->out, cl->N, cl->np, cl->cur_pc, cl->cur_pt, cl->out_scale, (float)(1.0 / (3.0 * (double)cl->np)), cl->dout,
+        cl->ugrid, gf, cl->P, cl->N, cl->np, cl->cur_pc, cl->cur_pt, cl->pnorm ? cl->pscale : cl->out_scale,
+        (float)(1.0 / (3.0 * (double)cl->np * (cl->pnorm ? (double)cl->pscale * cl->pscale : 1.0))), cl->dgrid,
         cl->loss);
     MGP_CHECK_LAUNCH();
-    k_dout_to_bf16<<<mgp_blocks_for(V, 4), 256, 0, cl->stream>>>(cl->dout, V, cl->g0);
+    g_kernel_launches++;
+    NN_RET(highpass_grids(cl, cl->dgrid, cl->stream));  // the filter is symmetric: its adjoint is itself
+    k_grids_to_bf16<<<mgp_blocks_for(V, 4), 256, 0, cl->stream>>>(cl->dgrid, gf, cl->P, cl->N, cl->g0);
     MGP_CHECK_LAUNCH();
-    g_kernel_launches += 2;
+    g_kernel_launches++;
   } else {
     k_loss_grad<<<mgp_blocks_for(V, 4), 256, 0, cl->stream>>>(cl->out, cl->target, V, cl->out_scale, cl->g0, cl->loss);
     MGP_CHECK_LAUNCH();
@@ -841,17 +884,12 @@ static int closure_backward(mgp_closure *cl) {
   }
   bf16 *g = cl->g0, *gn = cl->g1;
   for (int l = NN_LAYERS - 1; l >= 0; l--) {
-    MGP_CUDA(cudaMemsetAsync(cl->gw[l], 0, sizeof(float) * NN_WSIZE, cl->stream));
-    MGP_CUDA(cudaMemsetAsync(cl->gb[l], 0, sizeof(float) * NN_CH, cl->stream));
     NN_RET(conv_wgrad(cl, cl->act[l], g, cl->gw[l], cl->gb[l]));
     if (l == 0) break;
     k_mirror_transpose<<<(NN_WSIZE + 255) / 256, 256, 0, cl->stream>>>(cl->w16[l], cl->wt16);
     MGP_CHECK_LAUNCH();
     g_kernel_launches++;
-    NN_RET(conv_fwd(cl, g, cl->wt16, NULL, 1, gn, NULL, NULL, 0, 0, 0.f));
-    k_relu_grad<<<mgp_blocks_for(V * NN_CH, 4), 256, 0, cl->stream>>>(gn, cl->act[l], V * NN_CH);
-    MGP_CHECK_LAUNCH();
-    g_kernel_launches++;
+    NN_RET(conv_fwd(cl, g, cl->wt16, NULL, cl->act[l], 1, gn, NULL, NULL, 0, 0, 0.f));
     bf16 *t = g;
     g = gn;
     gn = t;
@@ -878,10 +916,18 @@ extern "C" int mgp_closure_destroy(mgp_closure *cl) {
       if (b[q]) cudaFree(b[q]);
   }
   void *b[] = {cl->wt16, cl->out,  cl->target, cl->g0,   cl->g1,   cl->loss,  cl->grid_a, cl->grid_b,
-               cl->ds_x, cl->ds_t, cl->ds_pc,  cl->ds_pt, cl->pc,   cl->pt,    cl->dout, cl->fscr};
+               cl->ds_x, cl->ds_t, cl->ds_pc,  cl->ds_pt, cl->pc,   cl->pt,    cl->ugrid, cl->dgrid, cl->fscr,
+               cl->wg_partial};
   for (size_t q = 0; q < sizeof(b) / sizeof(b[0]); q++)
     if (b[q]) cudaFree(b[q]);
+  if (cl->have_plans) {
+    cufftDestroy(cl->plan_r2c);
+    cufftDestroy(cl->plan_c2r);
+  }
   if (cl->own_stream && cl->stream) cudaStreamDestroy(cl->stream);
+  free(cl->ds_s);
+  free(cl->scale_a);
+  free(cl->scale_s);
   free(cl);
   return MGP_OK;
 }
@@ -910,6 +956,7 @@ extern "C" int mgp_closure_create(int Nmesh, unsigned seed, int device, mgp_clos
   cl->device = device;
   cl->P = 2LL * (Nmesh / 2 + 1);
   cl->out_scale = 1.0f;
+  cl->hp_lambda = 0.0f;
 #define CL_TRY(x)                        \
   do {                                   \
     cudaError_t e_ = (x);                \
@@ -919,10 +966,6 @@ extern "C" int mgp_closure_create(int Nmesh, unsigned seed, int device, mgp_clos
     }                                    \
   } while (0)
   CL_TRY(cudaStreamCreateWithFlags(&cl->stream, cudaStreamNonBlocking));
-  {
-    const int zero = 0;
-    CL_TRY(cudaMemcpyToSymbol(g_conv_err, &zero, sizeof(int)));
-  }
   cl->own_stream = 1;
   uint64_t st = 0x9E3779B97F4A7C15ULL ^ seed;
   for (int l = 0; l < NN_LAYERS; l++) {
@@ -943,7 +986,7 @@ extern "C" int mgp_closure_create(int Nmesh, unsigned seed, int device, mgp_clos
     // fan-in: 27 taps x (3 live inputs for the first layer, 16 otherwise)
     init_weights(w, NN_TAPS * (l == 0 ? 3 : NN_CH), l == NN_LAYERS - 1 ? 3 : NN_CH, st);
     if (l == NN_LAYERS - 1)
-      for (auto &x : w) x *= 0.1f;  // start near the plain PM force
+      for (auto &x : w) x = 0.f;  // start at the plain PM force (zero residual)
     CL_TRY(cudaMemcpy(cl->w32[l], w.data(), sizeof(float) * NN_WSIZE, cudaMemcpyHostToDevice));
   }
   CL_TRY(cudaMalloc(&cl->wt16, sizeof(bf16) * NN_WSIZE));
@@ -1013,9 +1056,8 @@ extern "C" int mgp_closure_set_sample(mgp_closure *cl, const float *x, const flo
 extern "C" int mgp_closure_forward(mgp_closure *cl, float *out) {
   if (!cl) return mgp_set_error(MGP_EINVAL, "null closure");
   MGP_CUDA(cudaSetDevice(cl->device));
-  NN_RET(closure_forward(cl));
+  NN_RET(closure_forward(cl, 0));
   MGP_CUDA(cudaStreamSynchronize(cl->stream));
-  NN_RET(conv_status());
   if (out) {
     std::vector<float> h((size_t)cl->V * 4);
     MGP_CUDA(cudaMemcpy(h.data(), cl->out, sizeof(float) * h.size(), cudaMemcpyDeviceToHost));
@@ -1029,10 +1071,9 @@ extern "C" int mgp_closure_forward(mgp_closure *cl, float *out) {
 extern "C" int mgp_closure_gradients(mgp_closure *cl, double *loss, float *gw, float *gb) {
   if (!cl) return mgp_set_error(MGP_EINVAL, "null closure");
   MGP_CUDA(cudaSetDevice(cl->device));
-  NN_RET(closure_forward(cl));
+  NN_RET(closure_forward(cl, cl->pmode));
   NN_RET(closure_backward(cl));
   MGP_CUDA(cudaStreamSynchronize(cl->stream));
-  NN_RET(conv_status());
   if (loss) MGP_CUDA(cudaMemcpy(loss, cl->loss, sizeof(double), cudaMemcpyDeviceToHost));
   for (int l = 0; l < NN_LAYERS; l++) {
     if (gw) MGP_CUDA(cudaMemcpy(gw + l * NN_WSIZE, cl->gw[l], sizeof(float) * NN_WSIZE, cudaMemcpyDeviceToHost));
@@ -1045,7 +1086,7 @@ extern "C" int mgp_closure_gradients(mgp_closure *cl, double *loss, float *gw, f
 extern "C" int mgp_closure_train_step(mgp_closure *cl, float lr, double *loss) {
   if (!cl) return mgp_set_error(MGP_EINVAL, "null closure");
   MGP_CUDA(cudaSetDevice(cl->device));
-  NN_RET(closure_forward(cl));
+  NN_RET(closure_forward(cl, cl->pmode));
   NN_RET(closure_backward(cl));
   cl->adam_t++;
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
@@ -1062,7 +1103,6 @@ extern "C" int mgp_closure_train_step(mgp_closure *cl, float lr, double *loss) {
   if (loss) {
     MGP_CUDA(cudaMemcpyAsync(loss, cl->loss, sizeof(double), cudaMemcpyDeviceToHost, cl->stream));
     MGP_CUDA(cudaStreamSynchronize(cl->stream));
-    NN_RET(conv_status());
   }
   return MGP_OK;
 }
@@ -1172,8 +1212,7 @@ static int ensure_particles(mgp_closure *cl, long long np) {
     cl->own_np = np;
   }
   cl->np = np;
-  if (!cl->dout) MGP_CUDA(cudaMalloc(&cl->dout, sizeof(float) * 4 * cl->V));
-  return MGP_OK;
+  return ensure_hp(cl);
 }
 
 // Particle-level training target from a fine and a coarse context holding the
@@ -1231,15 +1270,19 @@ extern "C" int mgp_closure_target_particles(mgp_closure *cl, mgp_ctx *fine, mgp_
   cl->cur_pc = cl->pc;
   cl->cur_pt = cl->pt;
   cl->pmode = 1;
-  if (rms) {
-    MGP_CUDA(cudaMemsetAsync(cl->loss, 0, sizeof(double), cl->stream));
-    k_sumsq_flat<<<mgp_blocks_for(3 * cl->np, 4), 256, 0, cl->stream>>>(cl->pt, 3 * cl->np, cl->loss);
-    MGP_CHECK_LAUNCH();
-    double ss = 0.0;
-    MGP_CUDA(cudaMemcpyAsync(&ss, cl->loss, sizeof(double), cudaMemcpyDeviceToHost, cl->stream));
-    MGP_CUDA(cudaStreamSynchronize(cl->stream));
-    *rms = sqrt(ss / (3.0 * (double)cl->np));
-  }
+  // The sample trains the network to predict its residual in units of its
+  // own rms (the residual grows ~200x over a run, and an unnormalised loss
+  // leaves the early steps, whose errors grow the most, unconstrained).
+  MGP_CUDA(cudaMemsetAsync(cl->loss, 0, sizeof(double), cl->stream));
+  k_sumsq_flat<<<mgp_blocks_for(3 * cl->np, 4), 256, 0, cl->stream>>>(cl->pt, 3 * cl->np, cl->loss);
+  MGP_CHECK_LAUNCH();
+  double ss = 0.0;
+  MGP_CUDA(cudaMemcpyAsync(&ss, cl->loss, sizeof(double), cudaMemcpyDeviceToHost, cl->stream));
+  MGP_CUDA(cudaStreamSynchronize(cl->stream));
+  const double r = sqrt(ss / (3.0 * (double)cl->np));
+  cl->pscale = r > 0.0 ? (float)r : 1.0f;
+  cl->pnorm = 1;
+  if (rms) *rms = r;
   MGP_CUDA(cudaStreamSynchronize(cl->stream));
   return MGP_OK;
 }
@@ -1264,6 +1307,7 @@ extern "C" int mgp_closure_set_particle_sample(mgp_closure *cl, long long np, co
   cl->cur_pc = cl->pc;
   cl->cur_pt = cl->pt;
   cl->pmode = 1;
+  cl->pnorm = 0;  // a host sample uses out_scale and an unnormalised loss
   return MGP_OK;
 }
 
@@ -1297,6 +1341,8 @@ extern "C" int mgp_closure_reserve(mgp_closure *cl, int n, long long np) {
   cl->ds_t = cl->ds_pc = cl->ds_pt = NULL;
   cl->cap_samples = cl->nsamples = 0;
   cl->ds_np = 0;
+  free(cl->ds_s);
+  cl->ds_s = NULL;
   if (cl->pmode && cl->cur_pc != cl->pc) cl->pmode = 0;  // the working sample pointed into the old set
   if (n == 0) return MGP_OK;
   MGP_CUDA(cudaMalloc(&cl->ds_x, sizeof(bf16) * 3 * cl->V * n));
@@ -1306,6 +1352,8 @@ extern "C" int mgp_closure_reserve(mgp_closure *cl, int n, long long np) {
   } else {
     MGP_CUDA(cudaMalloc(&cl->ds_t, sizeof(float) * 3 * cl->V * n));
   }
+  cl->ds_s = (float *)calloc(2 * (size_t)n, sizeof(float));  // scale, normalisation flag
+  if (!cl->ds_s) return mgp_set_error(MGP_ENOMEM, "closure sample scales");
   cl->ds_np = np;
   cl->cap_samples = n;
   return MGP_OK;
@@ -1327,6 +1375,8 @@ extern "C" int mgp_closure_store(mgp_closure *cl, int slot) {
     MGP_CUDA(cudaMemcpyAsync(cl->ds_pt + slot * n3, cl->cur_pt, sizeof(float) * n3, cudaMemcpyDeviceToDevice,
                              cl->stream));
   }
+  cl->ds_s[2 * slot] = cl->pmode && cl->pnorm ? cl->pscale : 0.f;
+  cl->ds_s[2 * slot + 1] = cl->pmode ? (float)cl->pnorm : 0.f;
   if (slot >= cl->nsamples) cl->nsamples = slot + 1;
   MGP_CUDA(cudaStreamSynchronize(cl->stream));
   return MGP_OK;
@@ -1340,38 +1390,112 @@ extern "C" int mgp_closure_load(mgp_closure *cl, int slot) {
       cl->act[0], cl->target);
   MGP_CHECK_LAUNCH();
   if (cl->ds_np) {
-    if (!cl->dout) MGP_CUDA(cudaMalloc(&cl->dout, sizeof(float) * 4 * cl->V));
+    NN_RET(ensure_hp(cl));
     const size_t n3 = (size_t)3 * cl->ds_np;
     cl->np = cl->ds_np;
     cl->cur_pc = cl->ds_pc + slot * n3;
     cl->cur_pt = cl->ds_pt + slot * n3;
     cl->pmode = 1;
+    cl->pscale = cl->ds_s[2 * slot];
+    cl->pnorm = cl->ds_s[2 * slot + 1] != 0.f;
   } else {
     cl->pmode = 0;
   }
   return MGP_OK;
 }
 
-// Inference inside a PM step (called by mgp_get_displacements after the
-// force grids): features, three hidden layers and the last layer added to the
-// force grids, on the context's stream.
+// Output scale at scale factor A: log-log interpolation of the residual-scale
+// table (held at its end values outside it), or out_scale without a table.
+static double closure_scale(const mgp_closure *cl, double A) {
+  const int n = cl->scale_n;
+  if (n <= 0) return cl->out_scale;
+  if (n == 1 || A <= cl->scale_a[0]) return cl->scale_s[0];
+  if (A >= cl->scale_a[n - 1]) return cl->scale_s[n - 1];
+  int q = 0;
+  while (q < n - 2 && A > cl->scale_a[q + 1]) q++;
+  const double t = log(A / cl->scale_a[q]) / log(cl->scale_a[q + 1] / cl->scale_a[q]);
+  return exp((1.0 - t) * log(cl->scale_s[q]) + t * log(cl->scale_s[q + 1]));
+}
+
+// Inference inside a PM step, called by mgp_get_displacements between the
+// force pass and the force C2R: features, four layers (the last into the
+// three output grids), their R2C, and out_scale * H(k) / N^3 times them
+// added to the three force transforms, so the context's C2R yields the PM
+// force plus the high-passed closure force; all on the context's stream.
 int mgp_closure_apply(mgp_closure *cl, mgp_ctx *c, double A) {
   cudaStream_t keep = cl->stream;
   cl->stream = c->stream;
-  int rc = closure_features(cl, c, A);
+  int rc = ensure_hp(cl);
+  if (rc == MGP_OK) rc = closure_features(cl, c, A);
   if (c->timing) cudaEventRecord(c->ev[T_NNCONV][0], c->stream);  // the four convolutions
   for (int l = 0; l < NN_LAYERS - 1 && rc == MGP_OK; l++)
-    rc = conv_fwd(cl, cl->act[l], cl->w16[l], cl->b32[l], 0, cl->act[l + 1], NULL, NULL, 0, 0, 0.f);
+    rc = conv_fwd(cl, cl->act[l], cl->w16[l], cl->b32[l], NULL, 0, cl->act[l + 1], NULL, NULL, 0, 0, 0.f);
+  const long long gf = (long long)cl->N * cl->N * cl->P;
   if (rc == MGP_OK)
-    rc = conv_fwd(cl, cl->act[NN_LAYERS - 1], cl->w16[NN_LAYERS - 1], cl->b32[NN_LAYERS - 1], 3, NULL, NULL, c->frc,
-                  c->g.nreal, c->g.P, cl->out_scale);
+    rc = conv_fwd(cl, cl->act[NN_LAYERS - 1], cl->w16[NN_LAYERS - 1], cl->b32[NN_LAYERS - 1], NULL, 3, NULL, NULL,
+                  cl->ugrid, gf, cl->P, 0.f);
   if (c->timing) {
     cudaEventRecord(c->ev[T_NNCONV][1], c->stream);
     c->timed[T_NNCONV] = 1;
   }
+  if (rc == MGP_OK && cufftSetStream(cl->plan_r2c, c->stream) != CUFFT_SUCCESS)
+    rc = mgp_set_error(MGP_ECUFFT, "closure transform stream");
+  for (int q = 0; q < 3 && rc == MGP_OK; q++)
+    if (cufftExecR2C(cl->plan_r2c, (cufftReal *)(cl->ugrid + q * gf), (cufftComplex *)(cl->ugrid + q * gf)) !=
+        CUFFT_SUCCESS)
+      rc = mgp_set_error(MGP_ECUFFT, "closure output transform");
+  if (rc == MGP_OK) {
+    k_highpass<<<mgp_blocks_for(gf / 2, 4), 256, 0, c->stream>>>((float2 *)cl->ugrid, gf / 2, cl->N, cl->hp_lambda,
+                                                                (float)(closure_scale(cl, A) / (double)cl->V),
+                                                                (float2 *)c->frc);
+    if (cudaGetLastError() != cudaSuccess) rc = mgp_set_error(MGP_ECUDA, "closure force add");
+    g_kernel_launches++;
+  }
+  if (cl->have_plans) cufftSetStream(cl->plan_r2c, keep);
   cl->stream = keep;
   return rc;
 }
+
+// Cutoff wavelength (cells) of the sharp high-pass applied to the closure's
+// output: modes of wavelength >= lambda carry no learned force (default 0:
+// only the mean is removed).  A smooth filter that merely attenuates long
+// waves lets the network keep large-scale output that the particle loss
+// hardly sees but the dynamics integrate; a sharp one removes it, though the
+// correction still reaches large scales through its coupling to the density
+// (measured: lambda = 32 cells cost 0.5-1.5% of P(k) at k < 0.2 h/Mpc on the
+// 256^3 workload, so the default leaves the long waves in).
+extern "C" int mgp_closure_set_highpass(mgp_closure *cl, double lambda_cells) {
+  if (!cl || !(lambda_cells >= 0.0)) return mgp_set_error(MGP_EINVAL, "bad closure high-pass wavelength");
+  MGP_CUDA(cudaStreamSynchronize(cl->stream));
+  cl->hp_lambda = (float)lambda_cells;
+  return MGP_OK;
+}
+
+extern "C" double mgp_closure_get_highpass(mgp_closure *cl) { return cl ? (double)cl->hp_lambda : -1.0; }
+
+// Residual scale s(a) used in the step (n points, a increasing, s > 0;
+// n = 0 clears the table and out_scale is used).
+extern "C" int mgp_closure_set_scale_table(mgp_closure *cl, int n, const double *a, const double *s) {
+  if (!cl || n < 0 || (n > 0 && (!a || !s))) return mgp_set_error(MGP_EINVAL, "bad closure scale table");
+  for (int q = 0; q < n; q++)
+    if (!(a[q] > 0.0 && s[q] > 0.0) || (q > 0 && !(a[q] > a[q - 1])))
+      return mgp_set_error(MGP_EINVAL, "closure scale table needs increasing a > 0 and s > 0");
+  free(cl->scale_a);
+  free(cl->scale_s);
+  cl->scale_a = cl->scale_s = NULL;
+  cl->scale_n = 0;
+  if (n == 0) return MGP_OK;
+  cl->scale_a = (double *)malloc(sizeof(double) * n);
+  cl->scale_s = (double *)malloc(sizeof(double) * n);
+  if (!cl->scale_a || !cl->scale_s) return mgp_set_error(MGP_ENOMEM, "closure scale table");
+  memcpy(cl->scale_a, a, sizeof(double) * n);
+  memcpy(cl->scale_s, s, sizeof(double) * n);
+  cl->scale_n = n;
+  return MGP_OK;
+}
+
+// The scale the step uses at scale factor A.
+extern "C" double mgp_closure_scale_at(mgp_closure *cl, double A) { return cl ? closure_scale(cl, A) : -1.0; }
 
 // Attach (cl != NULL) or detach a closure: every later mgp_get_displacements
 // of the context adds the closure's residual force.

@@ -28,7 +28,8 @@ EXPORTS = [
     "mgp_closure_get_weights", "mgp_closure_set_weights", "mgp_closure_set_sample", "mgp_closure_get_sample",
     "mgp_closure_forward", "mgp_closure_gradients", "mgp_closure_train_step", "mgp_closure_features",
     "mgp_closure_target", "mgp_closure_target_particles", "mgp_closure_set_particle_sample",
-    "mgp_closure_get_particle_sample", "mgp_closure_reserve", "mgp_closure_store", "mgp_closure_load", "mgp_set_closure",
+    "mgp_closure_get_particle_sample", "mgp_closure_set_highpass", "mgp_closure_get_highpass",
+    "mgp_closure_set_scale_table", "mgp_closure_scale_at", "mgp_closure_reserve", "mgp_closure_store", "mgp_closure_load", "mgp_set_closure",
 ]
 
 # field types of mgp_assign_displacement_fields (src/proto.h:155-158)
@@ -125,6 +126,7 @@ def lib():
         L.mgp_batch_graph_nodes.argtypes = [vp]
         L.mgp_batch_graph_kernels.argtypes = [vp]
         fpp = C.POINTER(C.c_float)
+        dpp = C.POINTER(C.c_double)
         L.mgp_closure_create.argtypes = [C.c_int, C.c_uint, C.c_int, C.POINTER(vp)]
         L.mgp_closure_destroy.argtypes = [vp]
         L.mgp_closure_get_weights.argtypes = [vp, fpp, fpp, C.POINTER(C.c_float)]
@@ -140,6 +142,12 @@ def lib():
         L.mgp_closure_set_particle_sample.argtypes = [vp, C.c_longlong, fpp, fpp]
         L.mgp_closure_get_particle_sample.argtypes = [vp, C.POINTER(C.c_longlong), fpp, fpp]
         L.mgp_closure_reserve.argtypes = [vp, C.c_int, C.c_longlong]
+        L.mgp_closure_set_highpass.argtypes = [vp, C.c_double]
+        L.mgp_closure_get_highpass.argtypes = [vp]
+        L.mgp_closure_get_highpass.restype = C.c_double
+        L.mgp_closure_set_scale_table.argtypes = [vp, C.c_int, dpp, dpp]
+        L.mgp_closure_scale_at.argtypes = [vp, C.c_double]
+        L.mgp_closure_scale_at.restype = C.c_double
         L.mgp_closure_store.argtypes = [vp, C.c_int]
         L.mgp_closure_load.argtypes = [vp, C.c_int]
         L.mgp_set_closure.argtypes = [vp, vp]
@@ -496,6 +504,20 @@ class Closure:
         t = np.zeros((n.value, 3), np.float32)
         _check(lib().mgp_closure_get_particle_sample(self.h, C.byref(n), _fptr(cells), _fptr(t)))
         return cells, t
+
+    def set_highpass(self, lambda_cells):
+        _check(lib().mgp_closure_set_highpass(self.h, float(lambda_cells)))
+
+    def highpass(self):
+        return lib().mgp_closure_get_highpass(self.h)
+
+    def set_scale_table(self, a, s):
+        a = np.ascontiguousarray(a, np.float64)
+        s = np.ascontiguousarray(s, np.float64)
+        _check(lib().mgp_closure_set_scale_table(self.h, len(a), _dptr(a), _dptr(s)))
+
+    def scale_at(self, A):
+        return lib().mgp_closure_scale_at(self.h, float(A))
 
     def reserve(self, n, np_particles=0):
         _check(lib().mgp_closure_reserve(self.h, n, np_particles))

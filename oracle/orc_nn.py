@@ -94,22 +94,43 @@ def cic_corners(cells, N):
     return out
 
 
-def loss_and_grads_particles(X, Ws, bs, cells, Tp, scale, bf16=True):
+def highpass(F, lam):
+    """Sharp high-pass of periodic [N, N, N, C] fields: the modes of integer
+    wave vector n with wavelength N / |n| >= lam cells, and the mean, are
+    removed (lam <= 0: only the mean)."""
+    N = F.shape[0]
+    d = np.fft.fftfreq(N, 1.0 / N)
+    dz = np.arange(N // 2 + 1)
+    n2 = d[:, None, None] ** 2 + d[None, :, None] ** 2 + dz[None, None, :] ** 2
+    kc2 = (N / lam) ** 2 if lam > 0 else 0.0
+    H = ((n2 > 0) & (n2 > kc2)).astype(np.float64)
+    out = np.empty_like(F)
+    for c in range(F.shape[-1]):
+        out[..., c] = np.fft.irfftn(np.fft.rfftn(F[..., c]) * H, s=(N,) * 3, axes=(0, 1, 2))
+    return out
+
+
+def loss_and_grads_particles(X, Ws, bs, cells, Tp, scale, bf16=True, hp=None):
     """Particle loss = sum over particles and components of
-    (scale u_p - Tp)^2 / (3 np), u_p the trilinear interpolation of the
-    network output at the particle; d loss / d out is the CIC deposit of the
-    residuals."""
+    (scale u_p - Tp)^2 / (3 np), u_p the trilinear interpolation at the
+    particle of the network output high-passed with cutoff wavelength hp
+    cells (None: no filter);
+    d loss / d out is the high-passed CIC deposit of the residuals (the
+    filter is its own adjoint)."""
     r = to_bf16 if bf16 else (lambda a: a)
     acts, out = forward(X, Ws, bs, bf16)
     N, n = X.shape[0], len(cells)
     corners = cic_corners(np.asarray(cells, np.float64), N)
+    uo = out[..., :3] if hp is None else highpass(out[..., :3], hp)
     u = np.zeros((n, 3))
     for idx, w in corners:
-        u += w[:, None] * out[idx][:, :3]
+        u += w[:, None] * uo[idx]
     e = scale * u - Tp
     loss = float(np.sum(e * e) / (3.0 * n))
-    g = np.zeros(out.shape)
+    g3 = np.zeros(out.shape[:3] + (3,))
     for idx, w in corners:
-        np.add.at(g, idx + (slice(0, 3),), (2.0 * scale / (3.0 * n)) * w[:, None] * e)
+        np.add.at(g3, idx, (2.0 * scale / (3.0 * n)) * w[:, None] * e)
+    g = np.zeros(out.shape)
+    g[..., :3] = g3 if hp is None else highpass(g3, hp)
     gw, gb = backward(acts, r(g), Ws, bf16)
     return loss, out, gw, gb

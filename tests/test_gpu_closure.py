@@ -1,8 +1,8 @@
 """Learned force closure: the CUDA forward and backward passes against the
 FP64 numpy restatement of the network (oracle/orc_nn.py), the training
 inputs and targets against numpy from the context's own grids, the
-in-step application, and a small end-to-end training run that must bring a
-coarse-mesh run's P(k) closer to a 3x finer mesh.
+in-step application, and a small end-to-end training run that must reduce
+the force error against a 3x finer mesh on a held-out seed.
 
 Tolerances: the GPU keeps activations and gradients in BF16 between layers
 (the oracle rounds at the same points), so outputs agree to 1e-2 and
@@ -131,11 +131,15 @@ def test_closure_features_and_target_match_numpy():
     assert abs(rms - np.sqrt(np.mean(tref ** 2))) < 1e-4 * rms
 
 
-def test_closure_applied_in_step_adds_forward_output():
+def test_closure_applied_in_step_adds_highpassed_forward_output():
+    """The in-step closure force is out_scale times the high-passed network
+    output, added through the force transforms (cutoff 12 cells here)."""
     N, A = 32, 0.5
     w, b = rand_net(13, sd=0.05)
     with _lcdm_ctx(N) as c, M.Closure(N) as cl:
         cl.set_weights(w, b, 0.3)
+        cl.set_highpass(12.0)
+        sigma = cl.highpass()
         c.displacement_fields()
         c.get_displacements(A)
         plain = [c.grid(2 + a).reshape(N, N, -1)[:, :, :N].copy() for a in range(3)]
@@ -147,8 +151,10 @@ def test_closure_applied_in_step_adds_forward_output():
         M.Closure.detach(c)
     # the second deposit differs from the first at the 1e-6 level (order of the
     # CIC's float atomics), which moves a few BF16 feature roundings by one ulp
+    hp = NN.highpass(out.astype(np.float64), sigma)
+    assert sigma == 12.0
     for a in range(3):
-        assert rel_rms(withc[a] - plain[a], 0.3 * out[..., a]) < 2e-3
+        assert rel_rms(withc[a] - plain[a], 0.3 * hp[..., a]) < 2e-3
 
 
 def test_closure_particle_loss_gradients_match_oracle():
@@ -160,13 +166,15 @@ def test_closure_particle_loss_gradients_match_oracle():
     tp = rng.normal(0, 1, (n, 3)).astype(np.float32)
     with M.Closure(N) as cl:
         cl.set_weights(w, b, 1.5)
+        cl.set_highpass(5.0)
         cl.set_sample(x, None)
         cl.set_particle_sample(cells, tp)
         c2, t2 = cl.particle_sample()
         loss, gw, gb = cl.gradients()
     assert np.array_equal(c2, cells) and np.array_equal(t2, tp)
     lr, _, gwr, gbr = NN.loss_and_grads_particles(padded(x, N), w.astype(np.float64), b.astype(np.float64),
-                                                  cells.astype(np.float64), tp.astype(np.float64), 1.5)
+                                                  cells.astype(np.float64), tp.astype(np.float64), 1.5,
+                                                  hp=5.0)
     assert abs(loss - lr) / lr < 1e-3
     for l in range(4):
         assert rel_rms(gw[l], gwr[l]) < 3e-2, l
@@ -223,10 +231,12 @@ def test_closure_particle_samples_store_load_and_train():
     x = features(N, 31)
     wt, bt = rand_net(32)
     _, out_t = NN.forward(padded(x, N), wt.astype(np.float64), bt.astype(np.float64))
+    out_t = out_t - out_t.mean(axis=(0, 1, 2))  # the closure output carries no mean
     rng = np.random.default_rng(33)
     cells = rng.uniform(0, N, (n, 3))
     tp = sum(w[:, None] * out_t[idx][:, :3] for idx, w in NN.cic_corners(cells, N)).astype(np.float32)
     with M.Closure(N, seed=34) as cl:
+        cl.set_highpass(0.0)  # only the mean is removed
         cl.reserve(2, n)
         cl.set_sample(x, None)
         cl.set_particle_sample(cells.astype(np.float32), tp)
@@ -242,20 +252,40 @@ def test_closure_particle_samples_store_load_and_train():
     assert last < 0.5 * first
 
 
-def test_trained_closure_brings_coarse_pofk_closer_to_finer_mesh():
-    """End to end at 128^3 particles, Box 128 Mpc/h (the learned-closure
-    workload's resolution of 1 Mpc/h per coarse cell): samples from the 128^3
-    and 384^3 meshes of four seeds, GPU training, then a held-out seed run
-    with and without the closure; the closure must cut the mean
-    |P/P_fine - 1| over 0.4 < k < 1 h/Mpc by at least 10% (measured: 30%)."""
+def test_trained_closure_reduces_held_out_force_error():
+    """End to end at 128^3 particles, Box 128 Mpc/h (1 Mpc/h per coarse cell,
+    the learned-closure workload's resolution): particle samples from the
+    128^3 and 384^3 meshes of four seeds, GPU training, then the force error
+    on a held-out seed.  The untrained closure outputs zero (the plain PM
+    force), so its error relative to the target's mean square is 1; the
+    trained one must explain at least 30% of the band-limited fine-minus-
+    coarse force on the held-out seed (measured: about 70%)."""
     import closure_train as T
 
-    rep = T.run_c5("lcdm", Nc=128, box=128.0, train_seeds=range(7001, 7005), test_seeds=[7017], every=3, epochs=16,
-                   lr=2e-3, log=lambda *a: None)
-    ev = rep["eval"][0]
-    k = np.array(ev["k"])
-    m = (k > 0.4) & (k < 1.0)
-    plain = np.mean(np.abs(np.array(ev["ratio_plain"])[m] - 1))
-    closure = np.mean(np.abs(np.array(ev["ratio_closure"])[m] - 1))
-    assert closure < 0.9 * plain, (plain, closure)
-    assert rep["loss_over_var"][-1] < 0.8 * rep["loss_over_var"][0]
+    Nc, box, r, nsteps = 128, 128.0, 3, 30
+    snaps = set(range(0, nsteps, 3)) | {nsteps - 1}
+    with M.Closure(Nc, seed=5) as cl:
+        cl.reserve(5 * len(snaps), Nc ** 3)
+        cl.set_scale_table([0.1, 1.0], [1.0, 10.0])
+        assert abs(cl.scale_at(np.sqrt(0.1)) - np.sqrt(10.0)) < 1e-9  # log-log interpolation
+        assert cl.scale_at(0.05) == 1.0 and cl.scale_at(2.0) == 10.0  # held at the ends
+        slot = 0
+        for sd in range(7001, 7005):
+            slot, _, _ = T.collect(cl, sd, "lcdm", Nc, r, Nc, box, nsteps, snaps, slot)
+        ntrain = slot
+        slot, _, _ = T.collect(cl, 7017, "lcdm", Nc, r, Nc, box, nsteps, snaps, slot)
+
+        def held_out():  # each sample's loss is relative to its own mean square target
+            out = []
+            for s in range(ntrain, slot):
+                cl.load(s)
+                out.append(cl.gradients()[0])
+            return np.array(out)
+
+        before = held_out()
+        hist = T.train(cl, ntrain, 16, 2e-3)
+        after = held_out()
+    assert np.allclose(before, 1.0, atol=1e-3)
+    assert hist[-1] < hist[0]
+    assert np.mean(after) < 0.7, after
+    assert np.all(after < 1.0), after

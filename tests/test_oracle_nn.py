@@ -52,22 +52,35 @@ def test_particle_loss_gradients_match_finite_differences():
     bs[3, 3:] = 0
     cells = rng.uniform(0, N, (n, 3))
     Tp = rng.normal(0, 1, (n, 3))
-    loss, _, gw, gb = NN.loss_and_grads_particles(X, Ws, bs, cells, Tp, 0.7, bf16=False)
-    eps = 1e-6
-    for (l, t, o, c) in [(0, 7, 1, 2), (1, 13, 4, 9), (3, 22, 0, 5), (3, 1, 2, 14)]:
-        Wp, Wm = Ws.copy(), Ws.copy()
-        Wp[l, t, o, c] += eps
-        Wm[l, t, o, c] -= eps
-        fd = (NN.loss_and_grads_particles(X, Wp, bs, cells, Tp, 0.7, bf16=False)[0] -
-              NN.loss_and_grads_particles(X, Wm, bs, cells, Tp, 0.7, bf16=False)[0]) / (2 * eps)
-        assert abs(fd - gw[l][t, o, c]) < 1e-6 + 1e-4 * abs(fd), (l, t, o, c, fd, gw[l][t, o, c])
-    for (l, o) in [(1, 6), (3, 2)]:
-        bp, bm = bs.copy(), bs.copy()
-        bp[l, o] += eps
-        bm[l, o] -= eps
-        fd = (NN.loss_and_grads_particles(X, Ws, bp, cells, Tp, 0.7, bf16=False)[0] -
-              NN.loss_and_grads_particles(X, Ws, bm, cells, Tp, 0.7, bf16=False)[0]) / (2 * eps)
-        assert abs(fd - gb[l][o]) < 1e-6 + 1e-4 * abs(fd)
+    for hp in (None, 1.5):
+        loss, _, gw, gb = NN.loss_and_grads_particles(X, Ws, bs, cells, Tp, 0.7, bf16=False, hp=hp)
+        eps = 1e-6
+        for (l, t, o, c) in [(0, 7, 1, 2), (1, 13, 4, 9), (3, 22, 0, 5), (3, 1, 2, 14)]:
+            Wp, Wm = Ws.copy(), Ws.copy()
+            Wp[l, t, o, c] += eps
+            Wm[l, t, o, c] -= eps
+            fd = (NN.loss_and_grads_particles(X, Wp, bs, cells, Tp, 0.7, bf16=False, hp=hp)[0] -
+                  NN.loss_and_grads_particles(X, Wm, bs, cells, Tp, 0.7, bf16=False, hp=hp)[0]) / (2 * eps)
+            assert abs(fd - gw[l][t, o, c]) < 1e-6 + 1e-4 * abs(fd), (hp, l, t, o, c, fd, gw[l][t, o, c])
+        for (l, o) in [(1, 6), (3, 2)]:
+            bp, bm = bs.copy(), bs.copy()
+            bp[l, o] += eps
+            bm[l, o] -= eps
+            fd = (NN.loss_and_grads_particles(X, Ws, bp, cells, Tp, 0.7, bf16=False, hp=hp)[0] -
+                  NN.loss_and_grads_particles(X, Ws, bm, cells, Tp, 0.7, bf16=False, hp=hp)[0]) / (2 * eps)
+            assert abs(fd - gb[l][o]) < 1e-6 + 1e-4 * abs(fd)
+
+
+def test_highpass_removes_long_waves_and_keeps_short_ones():
+    N = 16
+    x = np.arange(N)
+    F = np.zeros((N, N, N, 3))
+    F[..., 0] = 3.0  # the mean: removed
+    F[..., 1] = np.cos(2 * np.pi * 2 * x / N)[:, None, None] * np.ones((N, N, N))  # wavelength 8 cells: removed
+    F[..., 2] = np.cos(2 * np.pi * 3 * x / N)[None, :, None] * np.ones((N, N, N))  # 5.3 cells: kept
+    out = NN.highpass(F, 8.0)
+    assert np.max(np.abs(out[..., :2])) < 1e-12
+    assert np.allclose(out[..., 2], F[..., 2])
 
 
 def test_particle_interpolation_weights_are_a_partition_of_unity():
