@@ -265,7 +265,7 @@ def run_gpu(args):
     sync()
     barrier()
     launches0 = ctx.launches()
-    stage_ms = {k: 0.0 for k in ["cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "closure",
+    stage_ms = {k: 0.0 for k in ["fill", "cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "closure",
                                  "closure_conv"]}
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()

@@ -36,7 +36,7 @@ extern "C" const char *mgp_last_error(void) { return g_err; }
 // ----------------------------------------------------------------- timing
 static const char *k_timer_names[MGP_NTIMERS] = {"cic",    "r2c",  "pofk",          "mg",         "forces",
                                                    "c2r",    "interp_kick_drift", "step", "lpt_fields", "closure",
-                                                   "closure_conv"};
+                                                   "closure_conv", "fill"};
 
 static void tstart(mgp_ctx *c, int t) {
   if (c->timing) cudaEventRecord(c->ev[t][0], c->stream);
@@ -651,8 +651,10 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   RET_IF(require_particles(c));
   const int N = c->g.N;
   // PtoMesh, src/auxPM.c:280-432
-  tstart(c, T_CIC);
+  tstart(c, T_FILL);
   RET_IF(mgp_launch_fill(c->rho, c->g.nreal, -1.0f, c->stream));
+  tstop(c, T_FILL);
+  tstart(c, T_CIC);
   double wpar = pow((double)N / (double)c->Ns, 3);
   RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, c->p.Box, (float)wpar, c->rho, c->g.P, c->stream));
   tstop(c, T_CIC);

@@ -34,7 +34,7 @@ typedef struct {
   double mean_v[3];    /* mean of the stored v after the last kick */
 } mgp_dstate;
 
-#define MGP_NTIMERS 11
+#define MGP_NTIMERS 12
 
 typedef struct mgp_grid_geom {
   int N, NH;
@@ -145,7 +145,7 @@ struct mgp_ctx {
   long long launches;
 };
 
-enum { T_CIC = 0, T_R2C, T_POFK, T_MG, T_FORCES, T_C2R, T_IKD, T_MISC, T_SD, T_NN, T_NNCONV };
+enum { T_CIC = 0, T_R2C, T_POFK, T_MG, T_FORCES, T_C2R, T_IKD, T_MISC, T_SD, T_NN, T_NNCONV, T_FILL };
 
 /* error plumbing (C linkage: also called from the C sources) */
 #ifdef __cplusplus

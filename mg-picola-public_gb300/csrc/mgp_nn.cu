@@ -608,12 +608,13 @@ __global__ void k_particle_target(const float *__restrict__ ff, long long fg, in
 // u_p the CIC interpolation at the particle of the (high-passed) network
 // output, held as three padded real grids (grid c at u + c gstride, rows of
 // P floats); its gradient d loss / d u is the CIC deposit of
-// 2 s (s u_p - r_p) / (3 np) into three grids of the same layout (atomics).
+// 2 s (s u_p - r_p) / (3 np), accumulated per voxel into dacc [V][4] with one
+// float4 atomic per corner.
 constexpr int kThreadsPl = 256;
 __global__ void __launch_bounds__(kThreadsPl) k_particle_loss(const float *__restrict__ u, long long gstride, long long P,
                                                               int N, long long np, const float *__restrict__ pc,
                                                               const float *__restrict__ pt, float s, float inv,
-                                                              float *__restrict__ du, double *__restrict__ loss) {
+                                                              float *__restrict__ dacc, double *__restrict__ loss) {
   __shared__ double sh[kThreadsPl / 32];
   double acc = 0.0;
   long long stride = (long long)gridDim.x * blockDim.x;
@@ -629,12 +630,14 @@ __global__ void __launch_bounds__(kThreadsPl) k_particle_loss(const float *__res
       i0[a] = ic;
       i1[a] = ic + 1 == N ? 0 : ic + 1;
     }
-    long long g[8];
+    long long g[8], vx[8];
     float wt[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) {
       const int bx = c >> 2, by = (c >> 1) & 1, bz = c & 1;
-      g[c] = ((long long)(bx ? i1[0] : i0[0]) * N + (by ? i1[1] : i0[1])) * P + (bz ? i1[2] : i0[2]);
+      const long long row = (long long)(bx ? i1[0] : i0[0]) * N + (by ? i1[1] : i0[1]);
+      g[c] = row * P + (bz ? i1[2] : i0[2]);
+      vx[c] = row * N + (bz ? i1[2] : i0[2]);
       wt[c] = (bx ? d[0] : 1.f - d[0]) * (by ? d[1] : 1.f - d[1]) * (bz ? d[2] : 1.f - d[2]);
     }
     float e[3];
@@ -648,9 +651,10 @@ __global__ void __launch_bounds__(kThreadsPl) k_particle_loss(const float *__res
     }
     const float gs = 2.f * s * inv;
 #pragma unroll
-    for (int q = 0; q < 3; q++)
-#pragma unroll
-      for (int c = 0; c < 8; c++) atomicAdd(du + q * gstride + g[c], gs * wt[c] * e[q]);
+    for (int c = 0; c < 8; c++) {
+      const float gw = gs * wt[c];
+      atomicAdd(reinterpret_cast<float4 *>(dacc) + vx[c], make_float4(gw * e[0], gw * e[1], gw * e[2], 0.f));
+    }
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
@@ -659,6 +663,21 @@ __global__ void __launch_bounds__(kThreadsPl) k_particle_loss(const float *__res
     double t = 0.0;
     for (int w = 0; w < kThreadsPl / 32; w++) t += sh[w];
     atomicAdd(loss, t * (double)inv);
+  }
+}
+
+// dacc [V][4] (channels 0-2) -> three padded real grids.
+__global__ void k_acc4_to_grids(const float *__restrict__ dacc, int N, long long P, long long gstride,
+                                float *__restrict__ du) {
+  const long long V = (long long)N * N * N;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += stride) {
+    const long long row = v / N;
+    const long long gi = row * P + (v - row * N);
+    const float4 a = reinterpret_cast<const float4 *>(dacc)[v];
+    du[gi] = a.x;
+    du[gstride + gi] = a.y;
+    du[2 * gstride + gi] = a.z;
   }
 }
 
@@ -866,13 +885,15 @@ static int closure_backward(mgp_closure *cl) {
   MGP_CUDA(cudaMemsetAsync(cl->loss, 0, sizeof(double), cl->stream));
   if (cl->pmode) {
     const long long gf = (long long)cl->N * cl->N * cl->P;
-    MGP_CUDA(cudaMemsetAsync(cl->dgrid, 0, sizeof(float) * 3 * gf, cl->stream));
+    MGP_CUDA(cudaMemsetAsync(cl->out, 0, sizeof(float) * 4 * V, cl->stream));  // the deposit's accumulator
     k_particle_loss<<<mgp_blocks_for(cl->np, 8), kThreadsPl, 0, cl->stream>>>(
         cl->ugrid, gf, cl->P, cl->N, cl->np, cl->cur_pc, cl->cur_pt, cl->pnorm ? cl->pscale : cl->out_scale,
-        (float)(1.0 / (3.0 * (double)cl->np * (cl->pnorm ? (double)cl->pscale * cl->pscale : 1.0))), cl->dgrid,
+        (float)(1.0 / (3.0 * (double)cl->np * (cl->pnorm ? (double)cl->pscale * cl->pscale : 1.0))), cl->out,
         cl->loss);
     MGP_CHECK_LAUNCH();
-    g_kernel_launches++;
+    k_acc4_to_grids<<<mgp_blocks_for(V, 4), 256, 0, cl->stream>>>(cl->out, cl->N, cl->P, gf, cl->dgrid);
+    MGP_CHECK_LAUNCH();
+    g_kernel_launches += 2;
     NN_RET(highpass_grids(cl, cl->dgrid, cl->stream));  // the filter is symmetric: its adjoint is itself
     k_grids_to_bf16<<<mgp_blocks_for(V, 4), 256, 0, cl->stream>>>(cl->dgrid, gf, cl->P, cl->N, cl->g0);
     MGP_CHECK_LAUNCH();
