@@ -92,6 +92,13 @@ def run_batch(args, cfg):
     boxes = batch_boxes(cfg)
     B, Np, nst = len(boxes), cfg["Ns"] ** 3, cfg["nsteps"]
     batch = M.Batch(p, boxes)
+    default_tuning = batch.tuning()
+    batch.run(nst)
+    default_ms = batch.ms(0)
+    tune_t0 = time.perf_counter()
+    tuned_ms = batch.autotune(nst)  # launch budgets picked by timing, before the timed region
+    tune_s = time.perf_counter() - tune_t0
+    tuning = batch.tuning()
     for _ in range(args.warmup):
         batch.run(nst)
     launches = batch.graph_kernels()
@@ -126,6 +133,10 @@ def run_batch(args, cfg):
         "config": {"workload": args.config, "boxes": B, "particles_per_box": Np, "mesh": N, "box_mpc_h": cfg["Box"],
                    "model": "f(R) Hu-Sawicki n=1, screening, |fR0| log-uniform [1e-6, 1e-4] (seed %d)" % BATCH_FR0_SEED,
                    "steps_per_run": nst, "pofk_every_step": True, "pofk_bins": cfg["nbins"],
+                   "launch_budgets": {"tuned": tuning, "default": default_tuning,
+                                      "order": "blocks/SM: CIC deposit, grid passes, kick, P(k) binning",
+                                      "autotune_s": round(tune_s, 2), "graph_ms_default": round(default_ms, 3),
+                                      "graph_ms_tuned": round(tuned_ms, 3)},
                    "l2": "working set %.1f GB > L2" % (B * (6 * 4 * N * N * 2 * (N // 2 + 1) + 48 * Np) / 1e9)},
         "e2e": {"value": round(B * Np * nst / wall / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(B * cfg["nbins"] * 8 / nst), "api": "mgp_batch_run + mgp_batch_pofk",

@@ -281,6 +281,15 @@ double mgp_batch_ms(mgp_ctx *ctx, int what);
 int mgp_batch_graph_nodes(mgp_ctx *ctx);
 /* this library's own kernels among them (the rest are cuFFT's) */
 int mgp_batch_graph_kernels(mgp_ctx *ctx);
+/* Launch budgets in resident blocks per SM: [0] CIC deposit, [1] grid passes
+ * (fill, forces, MG passes), [2] interp+kick+drift, [3] P(k) binning
+ * (defaults 8, 8, 8, 4).  They change launch shapes only; the next run
+ * captures a new graph.  mgp_batch_autotune picks them by coordinate descent,
+ * timing one mgp_batch_run of nsteps per candidate, and leaves the fastest
+ * set (its graph time in *best_ms). */
+int mgp_batch_set_tuning(mgp_ctx *ctx, const int tune[4]);
+int mgp_batch_get_tuning(mgp_ctx *ctx, int tune[4]);
+int mgp_batch_autotune(mgp_ctx *ctx, int nsteps, double z_final, double *best_ms);
 
 /* Learned force closure (no counterpart in the reference): a 3D CNN on the
  * PM mesh -- four periodic 3x3x3 convolutions, 16 channels, ReLU, BF16

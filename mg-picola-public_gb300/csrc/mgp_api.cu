@@ -71,6 +71,18 @@ extern "C" double mgp_kernel_ms(mgp_ctx *c, const char *name) {
 
 extern "C" long long mgp_launch_count(mgp_ctx *c) { return c ? mgp_kernel_launches() : -1; }
 
+
+// P(k) binning blocks per box for a budget of per_sm blocks per SM.
+static int pk_blocks_for(const mgp_ctx *c, int per_sm) {
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  long long nb = ((long long)sms * per_sm + c->nbox - 1) / c->nbox;
+  const long long rows_blocks = ((long long)c->g.N * c->g.N + 7) / 8;
+  if (nb > rows_blocks) nb = rows_blocks;
+  if (nb < 1) nb = 1;
+  return (int)nb;
+}
+
 // ----------------------------------------------------------- P(k) tables
 // adjust_pofk_parameters (src/compute_pofk.c:758-805) in integer k units.
 static void adjust_pofk(int N, int *nbins, int *bintype, int *sub, double *kmin, double *kmax) {
@@ -173,16 +185,12 @@ static int setup_pofk(mgp_ctx *c) {
   }
   MGP_CUDA(cudaMalloc(&c->win1d, sizeof(float) * (h + 1)));
   MGP_CUDA(cudaMemcpy(c->win1d, win.data(), sizeof(float) * (h + 1), cudaMemcpyHostToDevice));
-  // enough warps to cover the SMs; each warp owns whole (i, j) rows
-  int sms = 152;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-  // (a batch shares that budget among its boxes)
-  long long nb = ((long long)sms * 4 + c->nbox - 1) / c->nbox;
-  long long rows_blocks = ((long long)N * N + 7) / 8;
-  if (nb > rows_blocks) nb = rows_blocks;
-  if (nb < 1) nb = 1;
-  c->pk_blocks = (int)nb;
-  MGP_CUDA(cudaMalloc(&c->pk_block, sizeof(double) * (size_t)nb * nbins * c->nbox));
+  // enough warps to cover the SMs (4 blocks per SM; a batch shares that
+  // budget among its boxes); each warp owns whole (i, j) rows.  The partial
+  // buffer holds up to 16 blocks per SM for the batch autotuner.
+  c->pk_blocks = pk_blocks_for(c, 4);
+  c->pk_blocks_cap = pk_blocks_for(c, 16);
+  MGP_CUDA(cudaMalloc(&c->pk_block, sizeof(double) * (size_t)c->pk_blocks_cap * nbins * c->nbox));
   MGP_CUDA(cudaMalloc(&c->pk_sum, sizeof(double) * nbins * c->nbox));
   return MGP_OK;
 }
@@ -405,6 +413,8 @@ static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxe
   if (needs_mg1(p)) TRYCUDA(cudaMalloc(&c->mg1, gbytes));
   TRY(make_plans(c));
   TRY(setup_pofk(c));
+  c->tune[0] = c->tune[1] = c->tune[2] = MGP_BUDGET_DEFAULT;  // deposit, grid passes, kick
+  c->tune[3] = 4;                                             // P(k) binning
   if (p->scaledependent) TRY(mgp_sd_alloc(c));
   if (nbox > 1) {
     TRYCUDA(cudaEventCreate(&c->bev[0]));
@@ -1161,7 +1171,8 @@ static int batch_step_launch(mgp_ctx *c, const batch_step &q, const mgp_box_scal
   RET_IF(mgp_launch_forces(c->dk, c->rho, 0.f, 0.f, mg_kind, N, p->Box, c->frc, gf, c->stream, B, bs));
   for (int g = 0; g < 3; g++)
     MGP_CUFFT(cufftExecC2R(c2r_frc, (cufftComplex *)(c->frc + g * gf), (cufftReal *)(c->frc + g * gf)));
-  const int nblk = mgp_blocks_per_box(c->np, 8, B);
+  int nblk = mgp_blocks_per_box(c->np, c->tune[2], B);
+  if (nblk > c->max_blocks) nblk = c->max_blocks;  // the per-block partials buffer
   RET_IF(mgp_launch_ikd(c->frc, gf, N, c->g.P, c->Ns, c->np, c->s, c->v, c->D1, c->D2, c->dstate, c->partials, nblk,
                         &q.kd, c->stream, B, bs));
   return MGP_OK;
@@ -1186,6 +1197,11 @@ static int batch_build_graph(mgp_ctx *c, int nsteps, double zf) {
   if (c->graph) cudaGraphDestroy(c->graph);
   c->graph_exec = NULL;
   c->graph = NULL;
+  // the batch's launch budgets hold for the captured launches only
+  const int pk_keep = c->pk_blocks;
+  c->pk_blocks = pk_blocks_for(c, c->tune[3]);
+  if (c->pk_blocks > c->pk_blocks_cap) c->pk_blocks = c->pk_blocks_cap;
+  mgp_set_launch_budget(c->tune[0], c->tune[1]);
   MGP_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   const long long k0 = g_kernel_launches;
   int rc = MGP_OK;
@@ -1194,6 +1210,8 @@ static int batch_build_graph(mgp_ctx *c, int nsteps, double zf) {
                            c->pk_hist + (size_t)t * c->nbox * c->pk_nbins);
   cudaGraph_t g = NULL;
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  mgp_set_launch_budget(MGP_BUDGET_DEFAULT, MGP_BUDGET_DEFAULT);
+  c->pk_blocks = pk_keep;
   if (rc != MGP_OK) {
     if (g) cudaGraphDestroy(g);
     return rc;
@@ -1229,6 +1247,61 @@ extern "C" int mgp_batch_run(mgp_ctx *c, int nsteps, double z_final) {
   MGP_CUDA(cudaEventSynchronize(c->bev[1]));
   MGP_CUDA(cudaEventElapsedTime(&c->batch_ms, c->bev[0], c->bev[1]));
   c->have_density = c->have_forces = 0;
+  return MGP_OK;
+}
+
+// Launch budgets of a batch (resident blocks per SM): [0] deposit, [1] grid
+// passes (fill, forces, MG passes), [2] interp+kick+drift, [3] P(k) binning.
+// They change launch shapes only (sums may differ in rounding); the next
+// mgp_batch_run captures a new graph with them.
+extern "C" int mgp_batch_set_tuning(mgp_ctx *c, const int *tune) {
+  if (!c || !tune) return mgp_set_error(MGP_EINVAL, "null argument");
+  for (int q = 0; q < 4; q++)
+    if (tune[q] < 1 || tune[q] > 64) return mgp_set_error(MGP_EINVAL, "launch budget %d out of [1, 64]", tune[q]);
+  for (int q = 0; q < 4; q++) c->tune[q] = tune[q];
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = NULL;
+  c->graph = NULL;
+  return MGP_OK;
+}
+
+extern "C" int mgp_batch_get_tuning(mgp_ctx *c, int *tune) {
+  if (!c || !tune) return mgp_set_error(MGP_EINVAL, "null argument");
+  for (int q = 0; q < 4; q++) tune[q] = c->tune[q];
+  return MGP_OK;
+}
+
+// Autotuner: coordinate descent over the four budgets (grid passes first,
+// then deposit, kick and P(k)), each over {1, 2, 4, 8, 16, 32} blocks per SM
+// (P(k): {1, 2, 4, 8, 16}); every candidate is timed by one mgp_batch_run of
+// nsteps (fresh ICs, a newly captured graph, the graph timed with CUDA events)
+// and the fastest is kept.  *best_ms receives the graph time of the result.
+extern "C" int mgp_batch_autotune(mgp_ctx *c, int nsteps, double z_final, double *best_ms) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  static const int cand[6] = {1, 2, 4, 8, 16, 32};
+  static const int order[4] = {1, 0, 2, 3};
+  int best[4];
+  for (int q = 0; q < 4; q++) best[q] = c->tune[q];
+  RET_IF(mgp_batch_set_tuning(c, best));
+  RET_IF(mgp_batch_run(c, nsteps, z_final));
+  double best_t = c->batch_ms;
+  for (int oi = 0; oi < 4; oi++) {
+    const int q = order[oi];
+    for (int ci = 0; ci < (q == 3 ? 5 : 6); ci++) {
+      if (cand[ci] == best[q]) continue;
+      int trial[4] = {best[0], best[1], best[2], best[3]};
+      trial[q] = cand[ci];
+      RET_IF(mgp_batch_set_tuning(c, trial));
+      RET_IF(mgp_batch_run(c, nsteps, z_final));
+      if (c->batch_ms < best_t) {
+        best_t = c->batch_ms;
+        best[q] = cand[ci];
+      }
+    }
+  }
+  RET_IF(mgp_batch_set_tuning(c, best));
+  if (best_ms) *best_ms = best_t;
   return MGP_OK;
 }
 

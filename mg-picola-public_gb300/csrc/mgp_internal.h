@@ -91,6 +91,8 @@ struct mgp_ctx {
   double *pk_n, *pk_k;      /* host: mode counts and k sums per bin */
   double *pk_host;          /* host: last P(k) sums */
   int pk_blocks;
+  int pk_blocks_cap;        /* blocks the P(k) partial buffer holds (per box) */
+  int tune[4];              /* batch launch budgets, blocks per SM: deposit, grid passes, kick, P(k) */
   int have_density, have_forces;
   double last_density_a;
 
@@ -184,6 +186,8 @@ int mgp_set_error(int code, const char *fmt, ...);
  * being blockIdx.y; `bs` (device, nbox entries) replaces the by-value
  * scalars when non-NULL. */
 int mgp_blocks_per_box(long long n_per_box, int per_sm, int nbox);
+#define MGP_BUDGET_DEFAULT 8
+void mgp_set_launch_budget(int cic, int grid);
 /* Per-launch scalars of the fused MtoParticles + Kick + Drift kernel. */
 typedef struct {
   float scale;        /* N / Box */

@@ -51,6 +51,15 @@ static dim3 grid_boxes(long long n_per_box, int per_sm, int nbox) {
 }
 int mgp_blocks_per_box(long long n_per_box, int per_sm, int nbox) { return (int)grid_boxes(n_per_box, per_sm, nbox).x; }
 
+// Launch budgets (resident blocks per SM) of the deposit and of the grid
+// passes.  A batch sets its tuned values while its graph is captured and
+// restores these defaults afterwards.
+static int g_budget_cic = MGP_BUDGET_DEFAULT, g_budget_grid = MGP_BUDGET_DEFAULT;
+void mgp_set_launch_budget(int cic, int grid) {
+  g_budget_cic = cic > 0 ? cic : MGP_BUDGET_DEFAULT;
+  g_budget_grid = grid > 0 ? grid : MGP_BUDGET_DEFAULT;
+}
+
 // -------------------------------------------------------------- helpers
 __global__ void k_fill(float *__restrict__ p, long long n, float v) {
   long long stride = (long long)gridDim.x * blockDim.x;
@@ -62,7 +71,7 @@ __global__ void k_fill(float *__restrict__ p, long long n, float v) {
 }
 
 int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st) {
-  k_fill<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>(p, n, value);
+  k_fill<<<blocks_for(n, g_budget_grid), MGP_THREADS, 0, st>>>(p, n, value);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -109,7 +118,7 @@ __global__ void __launch_bounds__(MGP_THREADS) k_cic(const float *__restrict__ s
 
 int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box, float wpar,
                    float *rho, long long P, cudaStream_t stream, int nbox, long long g_bs) {
-  k_cic<<<grid_boxes(np, 8, nbox), MGP_THREADS, 0, stream>>>(s, st, np, Ns, N, (float)(N / box), wpar, rho, P, g_bs);
+  k_cic<<<grid_boxes(np, g_budget_cic, nbox), MGP_THREADS, 0, stream>>>(s, st, np, Ns, N, (float)(N / box), wpar, rho, P, g_bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -423,7 +432,7 @@ int mgp_launch_forces(const float *dk, const float *mgk, float mg_coupling, floa
   double scale = 2.0 * M_PI / box;
   float cfac = (float)(-1.0 / ((double)N * N * N * scale));
   float2 *fx = (float2 *)frc, *fy = (float2 *)(frc + grid_floats), *fz = (float2 *)(frc + 2 * grid_floats);
-  k_forces<<<grid_boxes(total, 8, nbox), MGP_THREADS, 0, st>>>((const float2 *)dk, (const float2 *)mgk, mg_coupling,
+  k_forces<<<grid_boxes(total, g_budget_grid, nbox), MGP_THREADS, 0, st>>>((const float2 *)dk, (const float2 *)mgk, mg_coupling,
                                                                mg_mass2, mg_kind, N, cfac, fx, fy, fz, grid_floats, bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
@@ -619,7 +628,7 @@ __global__ void k_div_laplacian(const float2 *__restrict__ dk, float2 *__restric
 int mgp_launch_div_laplacian(const float *dk, float *out, int N, float norm, cudaStream_t st, int nbox,
                              long long g_bs) {
   const long long total = (long long)N * N * (N / 2 + 1);
-  k_div_laplacian<<<grid_boxes(total, 8, nbox), MGP_THREADS, 0, st>>>((const float2 *)dk, (float2 *)out, N, norm, g_bs);
+  k_div_laplacian<<<grid_boxes(total, g_budget_grid, nbox), MGP_THREADS, 0, st>>>((const float2 *)dk, (float2 *)out, N, norm, g_bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -658,7 +667,7 @@ __global__ void k_smooth(const float2 *__restrict__ dk, float2 *__restrict__ out
 int mgp_launch_smooth(const float *dk, float *out, int N, int filter, float kR1, float norm, cudaStream_t st,
                       int nbox, long long g_bs) {
   const long long total = (long long)N * N * (N / 2 + 1);
-  k_smooth<<<grid_boxes(total, 8, nbox), MGP_THREADS, 0, st>>>((const float2 *)dk, (float2 *)out, N, filter, kR1, norm,
+  k_smooth<<<grid_boxes(total, g_budget_grid, nbox), MGP_THREADS, 0, st>>>((const float2 *)dk, (float2 *)out, N, filter, kR1, norm,
                                                                g_bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
@@ -698,7 +707,7 @@ __global__ void k_screen_potential(float *__restrict__ rho, const float *__restr
 
 int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float phicrit, cudaStream_t st, int nbox,
                                 const mgp_box_scalars *bs) {
-  k_screen_potential<<<grid_boxes(n, 8, nbox), MGP_THREADS, 0, st>>>(rho, phi, n, phicrit, bs);
+  k_screen_potential<<<grid_boxes(n, g_budget_grid, nbox), MGP_THREADS, 0, st>>>(rho, phi, n, phicrit, bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -736,7 +745,7 @@ __global__ void k_screen_density(float *__restrict__ rho, const float *__restric
 
 int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float coupling, float pref, cudaStream_t st,
                               int nbox, const mgp_box_scalars *bs) {
-  k_screen_density<<<grid_boxes(n, 8, nbox), MGP_THREADS, 0, st>>>(rho, dsm, n, coupling, pref, bs);
+  k_screen_density<<<grid_boxes(n, g_budget_grid, nbox), MGP_THREADS, 0, st>>>(rho, dsm, n, coupling, pref, bs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;

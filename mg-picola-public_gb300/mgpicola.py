@@ -24,7 +24,8 @@ EXPORTS = [
     "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_launch_count",
     "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
-    "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_closure_create", "mgp_closure_destroy",
+    "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_batch_set_tuning",
+    "mgp_batch_get_tuning", "mgp_batch_autotune", "mgp_closure_create", "mgp_closure_destroy",
     "mgp_closure_get_weights", "mgp_closure_set_weights", "mgp_closure_set_sample", "mgp_closure_get_sample",
     "mgp_closure_forward", "mgp_closure_gradients", "mgp_closure_train_step", "mgp_closure_features",
     "mgp_closure_target", "mgp_closure_target_particles", "mgp_closure_set_particle_sample",
@@ -125,6 +126,9 @@ def lib():
         L.mgp_batch_ms.restype = C.c_double
         L.mgp_batch_graph_nodes.argtypes = [vp]
         L.mgp_batch_graph_kernels.argtypes = [vp]
+        L.mgp_batch_set_tuning.argtypes = [vp, C.POINTER(C.c_int)]
+        L.mgp_batch_get_tuning.argtypes = [vp, C.POINTER(C.c_int)]
+        L.mgp_batch_autotune.argtypes = [vp, C.c_int, C.c_double, C.POINTER(C.c_double)]
         fpp = C.POINTER(C.c_float)
         dpp = C.POINTER(C.c_double)
         L.mgp_closure_create.argtypes = [C.c_int, C.c_uint, C.c_int, C.POINTER(vp)]
@@ -406,6 +410,21 @@ class Batch:
 
     def graph_kernels(self):
         return lib().mgp_batch_graph_kernels(self.h)
+
+    def tuning(self):
+        t = (C.c_int * 4)()
+        _check(lib().mgp_batch_get_tuning(self.h, t))
+        return list(t)
+
+    def set_tuning(self, tune):
+        t = (C.c_int * 4)(*tune)
+        _check(lib().mgp_batch_set_tuning(self.h, t))
+
+    def autotune(self, nsteps, z_final=0.0):
+        """Pick the launch budgets by timing runs; returns the best graph ms."""
+        ms = C.c_double(0)
+        _check(lib().mgp_batch_autotune(self.h, nsteps, z_final, C.byref(ms)))
+        return ms.value
 
 
 def _fptr(a):

@@ -108,3 +108,26 @@ def test_batch_rejects_single_box_calls():
         with pytest.raises(M.MGPError):
             ctx.get_displacements(0.1)
         ctx.h = None
+
+
+def test_batch_autotune_keeps_parity():
+    """The autotuner changes launch shapes only: after it picks the budgets
+    (each a candidate of its set), every box still matches its oracle run, and
+    a hand-set extreme budget (1 block per SM everywhere) too."""
+    nsteps = 4
+    p = params(model=M.MODEL_FOFR, modified_gravity_active=1, include_screening=1, fofr0=1e-5, nfofr=1.0)
+    boxes = [dict(Seed=6011, inverted=0, fofr0=1e-5), dict(Seed=6012, inverted=1, fofr0=3e-6)]
+    with M.Batch(p, boxes) as batch:
+        assert batch.tuning() == [8, 8, 8, 4]
+        ms = batch.autotune(nsteps)
+        t = batch.tuning()
+        assert ms > 0 and all(x in (1, 2, 4, 8, 16, 32) for x in t) and t[3] <= 16
+        batch.run(nsteps)
+        for b, box in enumerate(boxes):
+            check_box(batch, b, p, O.make_mg(O.FOFR, 0.267, fofr0=box["fofr0"], nfofr=1.0), box, nsteps)
+        batch.set_tuning([1, 1, 1, 1])
+        batch.run(nsteps)
+        for b, box in enumerate(boxes):
+            check_box(batch, b, p, O.make_mg(O.FOFR, 0.267, fofr0=box["fofr0"], nfofr=1.0), box, nsteps)
+        with pytest.raises(M.MGPError):
+            batch.set_tuning([0, 8, 8, 4])
