@@ -202,6 +202,13 @@ int mgp_assign_displacement_fields(mgp_ctx *ctx, double A, double AFF, int n, co
 /* Full time loop with outputs (main.c:394-611).  Writes snapshot files
  * (GADGET-1 when gadget != 0, else ASCII) and pofk_* files to OutputDir. */
 int mgp_run(mgp_ctx *ctx, int gadget);
+/* mgp_run writes each snapshot from pinned host memory (two slots) on a host
+ * thread while the next steps run; the files are complete when mgp_run
+ * returns.  Statistics since the context was created, host milliseconds:
+ * snapshots, writers waiting for the GPU to reach the snapshot and download
+ * it, writers writing files, and the caller's thread held by output launches
+ * and waits for a free slot. */
+int mgp_output_stats(mgp_ctx *ctx, int *count, double *wait_ms, double *file_ms, double *blocked_ms);
 
 /* P(k) of the most recent density (compute_power_spectrum).  Arrays of
  * capacity `cap`; *nbins receives the bin count after the reference's

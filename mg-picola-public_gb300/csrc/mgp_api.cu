@@ -273,6 +273,7 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   if (!c) return MGP_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  mgp_run_release(c);  // a snapshot write still in flight
   cufftHandle plans[7] = {c->plan_r2c_oop, c->plan_r2c_ip, c->plan_c2r_1, c->plan_r2c_oop_b, c->plan_r2c_ip_b,
                           c->plan_c2r_b, c->plan_c2r_frc_b};
   for (int i = 0; i < 7; i++)

@@ -136,6 +136,14 @@ struct mgp_ctx {
   cudaEvent_t bev[2];
   float batch_ms, batch_ic_ms;
 
+  /* snapshot output overlapped with the following steps (mgp_run): the
+   * output kernel writes a device staging buffer, a copy stream downloads it
+   * into pinned host memory and a host thread writes the files */
+  float *out_dev, *out_host;   /* two slots of 2 x 3 np floats each (lazy) */
+  cudaStream_t out_stream;
+  cudaEvent_t out_ev[2];
+  void *out_writer;            /* host writer thread state (mgp_run.cu) */
+
   /* learned force closure added to the force grids (mgp_set_closure) */
   struct mgp_closure *closure;
 
@@ -213,6 +221,8 @@ int mgp_blocks_for(long long n, int per_sm);
 
 /* learned force closure (mgp_nn.cu): adds its residual to the force grids */
 int mgp_closure_apply(struct mgp_closure *cl, mgp_ctx *c, double A);
+/* waits for a pending snapshot write and frees the output buffers (mgp_destroy) */
+int mgp_run_release(mgp_ctx *c);
 
 /* scale-dependent growth (mgp_sd.cu) */
 int mgp_sd_alloc(mgp_ctx *c);

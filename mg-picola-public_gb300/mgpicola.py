@@ -25,7 +25,7 @@ EXPORTS = [
     "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
     "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_batch_set_tuning",
-    "mgp_batch_get_tuning", "mgp_batch_autotune", "mgp_closure_create", "mgp_closure_destroy",
+    "mgp_batch_get_tuning", "mgp_batch_autotune", "mgp_output_stats", "mgp_closure_create", "mgp_closure_destroy",
     "mgp_closure_get_weights", "mgp_closure_set_weights", "mgp_closure_set_sample", "mgp_closure_get_sample",
     "mgp_closure_forward", "mgp_closure_gradients", "mgp_closure_train_step", "mgp_closure_features",
     "mgp_closure_target", "mgp_closure_target_particles", "mgp_closure_set_particle_sample",
@@ -129,6 +129,7 @@ def lib():
         L.mgp_batch_set_tuning.argtypes = [vp, C.POINTER(C.c_int)]
         L.mgp_batch_get_tuning.argtypes = [vp, C.POINTER(C.c_int)]
         L.mgp_batch_autotune.argtypes = [vp, C.c_int, C.c_double, C.POINTER(C.c_double)]
+        L.mgp_output_stats.argtypes = [vp, C.POINTER(C.c_int)] + [C.POINTER(C.c_double)] * 3
         fpp = C.POINTER(C.c_float)
         dpp = C.POINTER(C.c_double)
         L.mgp_closure_create.argtypes = [C.c_int, C.c_uint, C.c_int, C.POINTER(vp)]
@@ -292,6 +293,13 @@ class Context:
 
     def run(self, gadget=True):
         _check(lib().mgp_run(self.h, 1 if gadget else 0))
+
+    def output_stats(self):
+        """(snapshots, writer ms waiting for the GPU, writer ms on files, ms the
+        calling thread was held) of mgp_run."""
+        n, w, f, b = C.c_int(0), C.c_double(0), C.c_double(0), C.c_double(0)
+        _check(lib().mgp_output_stats(self.h, C.byref(n), C.byref(w), C.byref(f), C.byref(b)))
+        return n.value, w.value, f.value, b.value
 
     def pofk(self):
         cap = max(self.params.pofk_nbins, self.N, 1)
