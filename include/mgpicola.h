@@ -142,6 +142,18 @@ typedef struct mgp_params {
    * [pi/Box, 4 pi sqrt(3) Nmesh/Box]. */
   int sd_nk;
   double sd_kmin, sd_kmax;
+  /* initial conditions from particle files (src/readICfromfile.c, the
+   * READICFROMFILE build): when ReadParticlesFromFile is set,
+   * mgp_displacement_fields deposits the particles of NumInputParticleFiles
+   * files, takes their density as the LCDM linear field at Init_Redshift and
+   * runs the 2LPT IC from it.  TypeInputParticleFiles: 1 RAMSES
+   * (<dir>/part_<RamsesOutputNumber %05d>.out<n %05d>, n = 1..), 2 ASCII
+   * (<dir>/<prefix>.<n>, n = 1.., "npart" then "x y z mass" in [0,1)),
+   * 3 GADGET-1 (<dir>/<prefix>.<n>, n = 0.., type-1 positions in Box units).
+   * Setting ReadParticlesFromFile before mgp_read_parameterfile makes the six
+   * keys required, as the READICFROMFILE build does. */
+  int ReadParticlesFromFile, NumInputParticleFiles, RamsesOutputNumber, TypeInputParticleFiles;
+  char InputParticleFileDir[500], InputParticleFilePrefix[500];
 } mgp_params;
 
 typedef struct mgp_ctx mgp_ctx;
@@ -168,6 +180,19 @@ const char *mgp_last_error(void);
  * a_init = 1/(1+Init_Redshift), zero COLA velocities and the Lagrangian
  * displacements D1 (ZA) and D2 (2LPT, times -3/7). */
 int mgp_displacement_fields(mgp_ctx *ctx);
+/* displacement_fields from particles held by the caller instead of files
+ * (the ReadParticlesFromFile path, src/readICfromfile.c:533-777): n
+ * positions in Mpc/h, [n][3]; their CIC density at Init_Redshift is taken as
+ * the LCDM linear field.  For Nmesh <= Nsample the three Nyquist planes of
+ * that field are zeroed (the reference uses +N/2 there in its displacement
+ * and -N/2 in its gradient pass); for Nmesh > Nsample its |k| > Nsample/2 cut
+ * removes them anyway. */
+int mgp_displacement_fields_from_positions(mgp_ctx *ctx, const double *pos, size_t n);
+/* The IC particle files of p read on the host (readICfromfile.c:221-531):
+ * *pos receives n positions in [0,1) of the box, [n][3], allocated by the
+ * library; release it with mgp_free_particles. */
+int mgp_read_particle_files(const mgp_params *p, double **pos, size_t *n);
+void mgp_free_particles(double *pos);
 
 /* GetDisplacements at scale factor A: CIC density, forward FFT, optional
  * P(k) (pofk_compute_every_step), fifth force, and the force grids. */

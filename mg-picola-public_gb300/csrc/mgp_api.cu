@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "mgp_internal.h"
+#include "mgp_io.h"
 #include "mgp_rng.h"
 
 static thread_local char g_err[1024] = "";
@@ -440,7 +441,12 @@ extern "C" int mgp_batch_create(const mgp_params *p, int nbox, const mgp_box_par
 // ---------------------------------------------------------------- IC
 // displacement_fields + the particle assignment of main.c:231-309 for box b
 // (single-grid transforms; box b's particle arrays and state).
-static int ic_box(mgp_ctx *c, int bx) {
+// 2LPT initial conditions of box bx (displacement_fields, src/2LPT.c:185-495,
+// 1209-1519): delta(k) from the Gaussian draw, or, given pos01 (particles in
+// [0,1) of the box, the ReadParticlesFromFile path of
+// src/readICfromfile.c:533-777), from the particles' density; then the 2LPT
+// fields, the lattice read-out and the particle state.
+static int ic_box(mgp_ctx *c, int bx, const double *pos01 = NULL, size_t npos = 0) {
   const mgp_params *pb = &c->box_p[bx];
   const mgp_cosmo *cb = cosmo_of(c, bx);
   float *dkb = c->dk + (size_t)bx * c->g.nreal;
@@ -527,9 +533,47 @@ static int ic_box(mgp_ctx *c, int bx) {
   CKC(cudaMemcpyAsync(d_seeds, seeds.data(), sizeof(uint32_t) * seeds.size(), cudaMemcpyHostToDevice, c->stream));
   CKC(cudaMemcpyAsync(d_amp, amp.data(), sizeof(double) * amp.size(), cudaMemcpyHostToDevice, c->stream));
   CKC(cudaMemcpyAsync(d_cut, cut.data(), cut.size(), cudaMemcpyHostToDevice, c->stream));
-  CKC(cudaMemsetAsync(dkb, 0, sizeof(float) * (size_t)gf, c->stream));
-  CK(mgp_launch_ic_delta(d_seeds, d_amp, d_cut, N, Ns, box, pb->amplitude_fixed_initial_condition,
-                         pb->inverted_initial_condition, pb->SphereMode == 1, dkb, c->stream));
+  if (pos01) {
+    // the particles' CIC density at a_i as the LCDM linear field, brought to
+    // a = 1 (readICfromfile.c:640-676), deconvolved and rescaled (701-777)
+    std::vector<double> gcw(h + 1), resc(rkmax + 1);
+    for (int d = 0; d <= h; d++) {
+      const double x = M_PI * d / (double)N, sc = d == 0 ? 1.0 : sin(x) / x;
+      gcw[d] = 1.0 / (sc * sc);
+    }
+    {
+      std::vector<double> r2(rkmax + 1, 1.0);
+      mgp_cosmo_pofk_ratio_many(cb, 1.0, rkmax, kk.data() + 1, r2.data() + 1);
+      const double s8 = pb->input_sigma8_is_for_lcdm ? 1.0 : mgp_cosmo_sigma8_enh(cb, 1.0);
+      for (int rk = 0; rk <= rkmax; rk++) resc[rk] = sqrt(r2[rk]) / s8;
+    }
+    const double normfac = 1.0 / ((double)N * N * N) / mgp_cosmo_growth(cb, 6, 1.0 / (1.0 + pb->Init_Redshift));
+    struct dbuf {  // freed on every exit from this block
+      double *p = NULL;
+      ~dbuf() {
+        if (p) cudaFree(p);
+      }
+    } b_pos, b_gc, b_resc;
+    CKC(cudaMalloc(&b_pos.p, sizeof(double) * 3 * npos));
+    CKC(cudaMalloc(&b_gc.p, sizeof(double) * gcw.size()));
+    CKC(cudaMalloc(&b_resc.p, sizeof(double) * resc.size()));
+    double *d_pos = b_pos.p, *d_gc = b_gc.p, *d_resc = b_resc.p;
+    CKC(cudaMemcpyAsync(d_pos, pos01, sizeof(double) * 3 * npos, cudaMemcpyHostToDevice, c->stream));
+    CKC(cudaMemcpyAsync(d_gc, gcw.data(), sizeof(double) * gcw.size(), cudaMemcpyHostToDevice, c->stream));
+    CKC(cudaMemcpyAsync(d_resc, resc.data(), sizeof(double) * resc.size(), cudaMemcpyHostToDevice, c->stream));
+    rc = mgp_launch_fill(c->rho, gf, -1.0f, c->stream);
+    if (rc == MGP_OK)
+      rc = mgp_launch_cic_unit(d_pos, (long long)npos, N, c->g.P, (float)pow((double)N / Ns, 3), c->rho, c->stream);
+    if (rc == MGP_OK && cufftExecR2C(c->plan_r2c_oop, (cufftReal *)c->rho, (cufftComplex *)dkb) != CUFFT_SUCCESS)
+      rc = mgp_set_error(MGP_ECUFFT, "IC density transform");
+    if (rc == MGP_OK) rc = mgp_launch_ic_from_density(dkb, N, Ns, normfac, d_gc, d_resc, c->stream);
+    cudaStreamSynchronize(c->stream);
+    if (rc != MGP_OK) goto cleanup;
+  } else {
+    CKC(cudaMemsetAsync(dkb, 0, sizeof(float) * (size_t)gf, c->stream));
+    CK(mgp_launch_ic_delta(d_seeds, d_amp, d_cut, N, Ns, box, pb->amplitude_fixed_initial_condition,
+                           pb->inverted_initial_condition, pb->SphereMode == 1, dkb, c->stream));
+  }
   CK(mgp_launch_ic_grad6(dkb, g6, gf, N, c->stream));
   for (int g = 0; g < 3; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
   for (int g = 3; g < 6; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
@@ -572,7 +616,33 @@ extern "C" int mgp_displacement_fields(mgp_ctx *c) {
   if (!c) return mgp_set_error(MGP_EINVAL, "null context");
   if (c->nbox != 1) return mgp_set_error(MGP_ESTATE, "single-box call on a batch of %d boxes", c->nbox);
   MGP_CUDA(cudaSetDevice(c->device));
+  if (c->p.ReadParticlesFromFile) {
+    // ReadFilesMakeDisplacementField (src/readICfromfile.c:533-699)
+    double *pos = NULL;
+    size_t n = 0;
+    RET_IF(mgp_read_particle_files(&c->p, &pos, &n));
+    const int rc = ic_box(c, 0, pos, n);
+    free(pos);
+    return rc;
+  }
   return ic_box(c, 0);
+}
+
+// The same from particles held by the caller: positions in Mpc/h, [n][3],
+// wrapped into [0, Box).
+extern "C" int mgp_displacement_fields_from_positions(mgp_ctx *c, const double *pos, size_t n) {
+  if (!c || (!pos && n)) return mgp_set_error(MGP_EINVAL, "null argument");
+  if (c->nbox != 1) return mgp_set_error(MGP_ESTATE, "single-box call on a batch of %d boxes", c->nbox);
+  MGP_CUDA(cudaSetDevice(c->device));
+  std::vector<double> u(3 * n);
+  const double inv = 1.0 / c->p.Box;
+  for (size_t q = 0; q < 3 * n; q++) {
+    double x = pos[q] * inv;
+    x -= floor(x);
+    if (x >= 1.0) x = 0.0;
+    u[q] = x;
+  }
+  return ic_box(c, 0, u.data(), n);
 }
 
 // ------------------------------------------------------------ PM step

@@ -252,6 +252,9 @@ int mgp_launch_ikd(const float *frc, long long grid_floats, int N, long long P, 
                    double *partials, int nblocks, const mgp_kd_args *a, cudaStream_t st, int nbox = 1,
                    const mgp_box_scalars *bs = NULL);
 int mgp_ikd_blocks(long long np);
+int mgp_launch_cic_unit(const double *pos, long long n, int N, long long P, float wpar, float *rho, cudaStream_t st);
+int mgp_launch_ic_from_density(float *dk, int N, int Ns, double normfac, const double *gc, const double *rescale,
+                               cudaStream_t st);
 long long mgp_kernel_launches(void);
 
 /* MG real-space and k-space passes */

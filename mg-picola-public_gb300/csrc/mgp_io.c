@@ -5,6 +5,7 @@
 
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 int mgp_set_error(int code, const char *fmt, ...);
@@ -141,3 +142,117 @@ int mgp_write_pofk_rsd(const mgp_params *p, double a, int nbins, const double *k
   fclose(fp);
   return MGP_OK;
 }
+
+/* ------------------------------------------------ IC particle files
+ * The readers of src/readICfromfile.c:221-531.  Fortran-style records
+ * (int byte count, payload, int byte count); the counts are checked. */
+static int rec_read(FILE *fp, void *buf, size_t bytes, const char *path) {
+  int m0 = 0, m1 = 0;
+  if (fread(&m0, sizeof(int), 1, fp) != 1 || fread(buf, 1, bytes, fp) != bytes || fread(&m1, sizeof(int), 1, fp) != 1)
+    return mgp_set_error(MGP_EIO, "short read in '%s'", path);
+  if ((size_t)m0 != bytes || m1 != m0)
+    return mgp_set_error(MGP_EIO, "record of %d bytes where %zu expected in '%s'", m0, bytes, path);
+  return MGP_OK;
+}
+
+static int grow(double **pos, size_t *cap, size_t need) {
+  if (need <= *cap) return MGP_OK;
+  size_t c = *cap ? *cap : 1024;
+  while (c < need) c *= 2;
+  double *q = (double *)realloc(*pos, sizeof(double) * 3 * c);
+  if (!q) return mgp_set_error(MGP_ENOMEM, "particle buffer of %zu particles", c);
+  *pos = q;
+  *cap = c;
+  return MGP_OK;
+}
+
+int mgp_read_particle_files(const mgp_params *p, double **pos_out, size_t *n_out) {
+  *pos_out = NULL;
+  *n_out = 0;
+  const int type = p->TypeInputParticleFiles, nf = p->NumInputParticleFiles;
+  if (type < 1 || type > 3) return mgp_set_error(MGP_EPARAM, "Error: unknown file-format [%d]", type);
+  if (nf < 1) return mgp_set_error(MGP_EPARAM, "NumInputParticleFiles = %d", nf);
+  double *pos = NULL;
+  size_t n = 0, cap = 0;
+  int rc = MGP_OK;
+  for (int f = 0; f < nf && rc == MGP_OK; f++) {
+    char path[1100];
+    if (type == 1)
+      snprintf(path, sizeof(path), "%s/part_%05d.out%05d", p->InputParticleFileDir, p->RamsesOutputNumber, f + 1);
+    else
+      snprintf(path, sizeof(path), "%s/%s.%d", p->InputParticleFileDir, p->InputParticleFilePrefix,
+               type == 3 ? f : f + 1);
+    FILE *fp = fopen(path, type == 2 ? "r" : "rb");
+    if (!fp) {
+      rc = mgp_set_error(MGP_EIO, "Error: cannot open file [%s]", path);
+      break;
+    }
+    if (type == 3) {
+      /* GADGET-1: header, then the type-1 positions in Box units (float) */
+      mgp_gadget_header h;
+      rc = rec_read(fp, &h, sizeof(h), path);
+      const size_t np = rc == MGP_OK ? h.npart[1] : 0;
+      float *buf = np ? (float *)malloc(sizeof(float) * 3 * np) : NULL;
+      if (rc == MGP_OK && np && !buf) rc = mgp_set_error(MGP_ENOMEM, "GADGET read buffer");
+      if (rc == MGP_OK && np) rc = rec_read(fp, buf, sizeof(float) * 3 * np, path);
+      if (rc == MGP_OK) rc = grow(&pos, &cap, n + np);
+      if (rc == MGP_OK) {
+        const double normfac = 1.0 / h.BoxSize;
+        for (size_t q = 0; q < 3 * np; q++) {
+          float x = (float)(buf[q] * normfac); /* the reference keeps the float buffer */
+          if (x >= 1.0f) x = (float)(x - 1.0);
+          pos[3 * n + q] = x;
+        }
+        n += np;
+      }
+      free(buf);
+    } else if (type == 2) {
+      /* ASCII: npart, then "x y z mass" per line, x in [0,1) */
+      int np = 0;
+      if (fscanf(fp, "%d", &np) != 1 || np < 0) rc = mgp_set_error(MGP_EIO, "bad particle count in '%s'", path);
+      if (rc == MGP_OK) rc = grow(&pos, &cap, n + (size_t)np);
+      for (int q = 0; q < np && rc == MGP_OK; q++) {
+        double x, y, z, m;
+        if (fscanf(fp, "%lf %lf %lf %lf", &x, &y, &z, &m) != 4) {
+          rc = mgp_set_error(MGP_EIO, "short particle list in '%s'", path);
+          break;
+        }
+        double v[3] = {x, y, z};
+        for (int a = 0; a < 3; a++) pos[3 * (n + q) + a] = v[a] >= 1.0 ? v[a] - 1.0 : v[a];
+      }
+      if (rc == MGP_OK) n += (size_t)np;
+    } else {
+      /* RAMSES part file: ncpu, ndim, npart, localseed[4], nstar_tot,
+       * mstar_tot[2], mstar_lost[2], nsink, then x, y, z (double, in [0,1)) */
+      int hdr[3], seed4[4], nstar, m2[2], l2[2], nsink;
+      rc = rec_read(fp, &hdr[0], sizeof(int), path);
+      if (rc == MGP_OK) rc = rec_read(fp, &hdr[1], sizeof(int), path);
+      if (rc == MGP_OK) rc = rec_read(fp, &hdr[2], sizeof(int), path);
+      if (rc == MGP_OK) rc = rec_read(fp, seed4, sizeof(seed4), path);
+      if (rc == MGP_OK) rc = rec_read(fp, &nstar, sizeof(int), path);
+      if (rc == MGP_OK) rc = rec_read(fp, m2, sizeof(m2), path);
+      if (rc == MGP_OK) rc = rec_read(fp, l2, sizeof(l2), path);
+      if (rc == MGP_OK) rc = rec_read(fp, &nsink, sizeof(int), path);
+      const size_t np = rc == MGP_OK && hdr[2] > 0 ? (size_t)hdr[2] : 0;
+      double *buf = np ? (double *)malloc(sizeof(double) * np) : NULL;
+      if (rc == MGP_OK && np && !buf) rc = mgp_set_error(MGP_ENOMEM, "RAMSES read buffer");
+      if (rc == MGP_OK) rc = grow(&pos, &cap, n + np);
+      for (int a = 0; a < 3 && rc == MGP_OK && np; a++) {
+        rc = rec_read(fp, buf, sizeof(double) * np, path);
+        for (size_t q = 0; q < np && rc == MGP_OK; q++) pos[3 * (n + q) + a] = buf[q] >= 1.0 ? buf[q] - 1.0 : buf[q];
+      }
+      free(buf);
+      if (rc == MGP_OK) n += np;
+    }
+    fclose(fp);
+  }
+  if (rc != MGP_OK) {
+    free(pos);
+    return rc;
+  }
+  *pos_out = pos;
+  *n_out = n;
+  return MGP_OK;
+}
+
+void mgp_free_particles(double *pos) { free(pos); }

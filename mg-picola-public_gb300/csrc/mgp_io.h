@@ -47,6 +47,10 @@ typedef struct {
 void mgp_snapshot_name(const mgp_params *p, double z, char *buf, size_t len);
 /* pos/vel already in output units (Mpc/h, km/s), AoS float [np][3]. */
 int mgp_write_gadget(const char *path, const mgp_params *p, double A, const float *pos, const float *vel, size_t np);
+/* Positions of the IC particle files of p (TypeInputParticleFiles,
+ * NumInputParticleFiles, InputParticleFileDir/Prefix, RamsesOutputNumber),
+ * in [0,1) of the box, [n][3]; *pos is malloc'ed (free it). */
+int mgp_read_particle_files(const mgp_params *p, double **pos, size_t *n);
 int mgp_write_ascii(const char *path, const float *pos, const float *vel, size_t np);
 int mgp_write_info(const mgp_params *p, double A, size_t np);
 /* P(k) file "pofk_<FileBase>_z%d.%03d_<label>.txt" (bins from 1, n > 0). */

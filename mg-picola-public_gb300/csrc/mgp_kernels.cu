@@ -837,6 +837,82 @@ int mgp_launch_ic_delta(const uint32_t *seedtable, const double *amp_rk, const u
   return MGP_OK;
 }
 
+// ProcessParticlesSingleFile (src/readICfromfile.c:133-219): CIC of particles
+// at positions in [0,1) of the box (FP64, [n][3]) onto a density grid pre-set
+// to -1, with WPAR = (N/Ns)^3 folded into the y factors; a cell index that
+// reaches N (position rounded up to the box edge) wraps to 0, as the
+// reference's ghost slice does for x.
+__global__ void k_cic_unit(const double *__restrict__ pos, long long n, int N, long long P, float wpar,
+                           float *__restrict__ rho) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+    const double X = pos[3 * q] * N, Y = pos[3 * q + 1] * N, Z = pos[3 * q + 2] * N;
+    unsigned IX = (unsigned)X, IY = (unsigned)Y, IZ = (unsigned)Z;
+    const float DX = (float)(X - (double)IX), DZ = (float)(Z - (double)IZ);
+    const float DYr = (float)(Y - (double)IY);
+    const float TX = 1.f - DX, TZ = 1.f - DZ, TY = (1.f - DYr) * wpar, DY = DYr * wpar;
+    if (IX >= (unsigned)N) IX = 0;
+    if (IY >= (unsigned)N) IY = 0;
+    if (IZ >= (unsigned)N) IZ = 0;
+    const unsigned IXn = IX + 1 >= (unsigned)N ? 0 : IX + 1, IYn = IY + 1 >= (unsigned)N ? 0 : IY + 1,
+                   IZn = IZ + 1 >= (unsigned)N ? 0 : IZ + 1;
+    const long long x0 = (long long)IX * N, x1 = (long long)IXn * N;
+    atomicAdd(rho + (x0 + IY) * P + IZ, TX * TY * TZ);
+    atomicAdd(rho + (x0 + IY) * P + IZn, TX * TY * DZ);
+    atomicAdd(rho + (x0 + IYn) * P + IZ, TX * DY * TZ);
+    atomicAdd(rho + (x0 + IYn) * P + IZn, TX * DY * DZ);
+    atomicAdd(rho + (x1 + IY) * P + IZ, DX * TY * TZ);
+    atomicAdd(rho + (x1 + IY) * P + IZn, DX * TY * DZ);
+    atomicAdd(rho + (x1 + IYn) * P + IZ, DX * DY * TZ);
+    atomicAdd(rho + (x1 + IYn) * P + IZn, DX * DY * DZ);
+  }
+}
+
+int mgp_launch_cic_unit(const double *pos, long long n, int N, long long P, float wpar, float *rho, cudaStream_t st) {
+  k_cic_unit<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>(pos, n, N, P, wpar, rho);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// delta(k) of a particle density as the linear field at z = 0
+// (src/readICfromfile.c:640-676, 701-777): times normfac = D_LCDM(1) /
+// D_LCDM(a_i) / N^3; modes with |d| > Ns/2 zeroed when N > Ns (for N <= Ns the
+// three Nyquist planes, whose sign conventions differ between the
+// reference's displacement and gradient passes); the CIC window divided out
+// (gc[|d|] = 1/sinc^2(pi d/N) per axis) and the P(k) rescaling per integer
+// |k|^2; the k = 0 mode zeroed.  In place on [N][N][N/2+1].
+__global__ void k_ic_from_density(float2 *__restrict__ dk, int N, int Ns, double normfac,
+                                  const double *__restrict__ gc, const double *__restrict__ rescale) {
+  const int NH = N / 2 + 1;
+  const long long n = (long long)N * N * NH;
+  const long long cut2 = (long long)(Ns / 2) * (Ns / 2);
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+    const int kz = (int)(q % NH);
+    const long long r = q / NH;
+    const int j = (int)(r % N), i = (int)(r / N);
+    const int di = i > N / 2 ? N - i : i, dj = j > N / 2 ? N - j : j;  // |d| per axis
+    const long long d2 = (long long)di * di + (long long)dj * dj + (long long)kz * kz;
+    const bool zero = d2 == 0 || (N > Ns && d2 > cut2) ||
+                      (N <= Ns && (2 * i == N || 2 * j == N || 2 * kz == N));
+    const double f = zero ? 0.0 : normfac * gc[di] * gc[dj] * gc[kz] * rescale[d2];
+    float2 v = dk[q];
+    v.x = (float)(f * v.x);
+    v.y = (float)(f * v.y);
+    dk[q] = v;
+  }
+}
+
+int mgp_launch_ic_from_density(float *dk, int N, int Ns, double normfac, const double *gc, const double *rescale,
+                               cudaStream_t st) {
+  const long long n = (long long)N * N * (N / 2 + 1);
+  k_ic_from_density<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>((float2 *)dk, N, Ns, normfac, gc, rescale);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
 // Integer wave number of index idx in the IC convention (2LPT.c:359-375):
 // idx < N/2 -> idx, else idx - N (so N/2 maps to -N/2).
 __device__ __forceinline__ int ic_d(int idx, int N) { return idx < N / 2 ? idx : idx - N; }

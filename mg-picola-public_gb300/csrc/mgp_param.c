@@ -148,10 +148,19 @@ int mgp_read_parameterfile(const char *fname, int model, int pofk_keys, int read
   int nt = 0;
   g_perr[0] = 0;
   if (!fname || !p) return MGP_EINVAL;
-  int use_w0wa = p->use_w0wa;
+  int use_w0wa = p->use_w0wa, readic = p->ReadParticlesFromFile;
   mgp_params_default(p);
   p->model = model;
   p->use_w0wa = use_w0wa;
+  if (readic) {
+    /* src/read_param.c:129-151 (READICFROMFILE) */
+    ADD("ReadParticlesFromFile", ReadParticlesFromFile, T_INT);
+    ADD("InputParticleFileDir", InputParticleFileDir, T_STRING);
+    ADD("InputParticleFilePrefix", InputParticleFilePrefix, T_STRING);
+    ADD("TypeInputParticleFiles", TypeInputParticleFiles, T_INT);
+    ADD("NumInputParticleFiles", NumInputParticleFiles, T_INT);
+    ADD("RamsesOutputNumber", RamsesOutputNumber, T_INT);
+  }
   if (model == MGP_MODEL_DGP) p->smoothing_filter = MGP_FILTER_GAUSSIAN;
   /* read_mg_parameters, user_defined_functions.h:233-405 */
   ADD("modified_gravity_active", modified_gravity_active, T_INT);

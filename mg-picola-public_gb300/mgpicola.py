@@ -25,7 +25,8 @@ EXPORTS = [
     "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
     "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_batch_set_tuning",
-    "mgp_batch_get_tuning", "mgp_batch_autotune", "mgp_output_stats", "mgp_closure_create", "mgp_closure_destroy",
+    "mgp_batch_get_tuning", "mgp_batch_autotune", "mgp_output_stats", "mgp_displacement_fields_from_positions",
+    "mgp_read_particle_files", "mgp_free_particles", "mgp_closure_create", "mgp_closure_destroy",
     "mgp_closure_get_weights", "mgp_closure_set_weights", "mgp_closure_set_sample", "mgp_closure_get_sample",
     "mgp_closure_forward", "mgp_closure_gradients", "mgp_closure_train_step", "mgp_closure_features",
     "mgp_closure_target", "mgp_closure_target_particles", "mgp_closure_set_particle_sample",
@@ -65,6 +66,9 @@ class Params(C.Structure):
         ("InputSpectrum_UnitLength_in_cm", C.c_double),
         ("Noutputs", C.c_int), ("output_redshift", C.c_double * 64), ("output_nsteps", C.c_int * 64),
         ("sd_nk", C.c_int), ("sd_kmin", C.c_double), ("sd_kmax", C.c_double),
+        ("ReadParticlesFromFile", C.c_int), ("NumInputParticleFiles", C.c_int), ("RamsesOutputNumber", C.c_int),
+        ("TypeInputParticleFiles", C.c_int), ("InputParticleFileDir", C.c_char * 500),
+        ("InputParticleFilePrefix", C.c_char * 500),
     ]
 
 
@@ -130,6 +134,9 @@ def lib():
         L.mgp_batch_get_tuning.argtypes = [vp, C.POINTER(C.c_int)]
         L.mgp_batch_autotune.argtypes = [vp, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.mgp_output_stats.argtypes = [vp, C.POINTER(C.c_int)] + [C.POINTER(C.c_double)] * 3
+        L.mgp_displacement_fields_from_positions.argtypes = [vp, C.POINTER(C.c_double), C.c_size_t]
+        L.mgp_read_particle_files.argtypes = [C.c_void_p, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_size_t)]
+        L.mgp_free_particles.argtypes = [C.POINTER(C.c_double)]
         fpp = C.POINTER(C.c_float)
         dpp = C.POINTER(C.c_double)
         L.mgp_closure_create.argtypes = [C.c_int, C.c_uint, C.c_int, C.POINTER(vp)]
@@ -187,10 +194,13 @@ def default_params(**kw):
     return p
 
 
-def read_parameterfile(fname, model=MODEL_LCDM, pofk_keys=True, read_outputs=True, use_w0wa=False):
-    """read_parameterfile + read_outputs of the reference."""
+def read_parameterfile(fname, model=MODEL_LCDM, pofk_keys=True, read_outputs=True, use_w0wa=False,
+                       read_ic_from_file=False):
+    """read_parameterfile + read_outputs of the reference (read_ic_from_file:
+    the READICFROMFILE build's six keys are required)."""
     p = Params()
     p.use_w0wa = 1 if use_w0wa else 0
+    p.ReadParticlesFromFile = 1 if read_ic_from_file else 0
     _check(lib().mgp_read_parameterfile(fname.encode(), model, 1 if pofk_keys else 0, 1 if read_outputs else 0,
                                         C.byref(p)))
     return p
@@ -198,6 +208,18 @@ def read_parameterfile(fname, model=MODEL_LCDM, pofk_keys=True, read_outputs=Tru
 
 def _dptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def read_particle_files(params):
+    """Positions in [0,1) of the box ([n][3]) from the IC particle files of
+    params (TypeInputParticleFiles 1 RAMSES, 2 ASCII, 3 GADGET-1)."""
+    ptr = C.POINTER(C.c_double)()
+    n = C.c_size_t(0)
+    _check(lib().mgp_read_particle_files(C.byref(params), C.byref(ptr), C.byref(n)))
+    try:
+        return np.ctypeslib.as_array(ptr, shape=(n.value, 3)).copy() if n.value else np.zeros((0, 3))
+    finally:
+        lib().mgp_free_particles(ptr)
 
 
 def cosmo_eval(params, which, x):
@@ -277,6 +299,11 @@ class Context:
     # reference entry points
     def displacement_fields(self):
         _check(lib().mgp_displacement_fields(self.h))
+
+    def displacement_fields_from_positions(self, pos):
+        """2LPT IC from the density of the given particles (Mpc/h, [n][3])."""
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        _check(lib().mgp_displacement_fields_from_positions(self.h, _dptr(pos), len(pos)))
 
     def get_displacements(self, A):
         _check(lib().mgp_get_displacements(self.h, A))

@@ -125,6 +125,8 @@ def lib():
         L.orc_tophat_sigma2.restype = C.c_double
         L.orc_seedtable.argtypes = [C.c_int, C.c_uint32, u32ptr]
         L.orc_ic_2lpt.argtypes = [C.POINTER(ICParams), C.POINTER(Power), dptr, dptr, C.c_void_p, C.c_void_p]
+        L.orc_ic_2lpt_from_particles.argtypes = [C.POINTER(ICParams), dptr, C.c_long, C.c_double, dptr, dptr, dptr,
+                                                 C.c_void_p, C.c_void_p]
         L.orc_jbd_solve.argtypes = [C.POINTER(MG)]
         L.orc_jbd_solve.restype = C.c_double
         L.orc_phia_solve.argtypes = [C.POINTER(MG), C.c_double]
@@ -260,6 +262,23 @@ def ic_2lpt(N, Ns, box, seed, pw, fixed=0, inverted=0, sphere=0, rescale=1.0, wa
     s2 = np.zeros(padded_shape(N)) if want_k else None
     lib().orc_ic_2lpt(C.byref(ip), C.byref(pw), D1, D2, None if dk is None else dk.ctypes.data,
                       None if s2 is None else s2.ctypes.data)
+    return (D1, D2, dk, s2) if want_k else (D1, D2)
+
+
+def ic_2lpt_from_particles(N, Ns, box, pos01, normfac, rescale_rk, want_k=False):
+    """ReadParticlesFromFile IC: pos01 [n][3] in [0,1); rescale_rk per integer
+    |k|^2 (length >= 3 (N/2)^2 + 1)."""
+    ip = ICParams(N, Ns, box, 0, 0, 0, 0, 1.0)
+    pos01 = np.ascontiguousarray(pos01, np.float64)
+    rescale_rk = np.ascontiguousarray(rescale_rk, np.float64)
+    assert len(rescale_rk) >= 3 * (N // 2) ** 2 + 1
+    npart = Ns ** 3
+    D1 = np.zeros((npart, 3))
+    D2 = np.zeros((npart, 3))
+    dk = np.zeros(padded_shape(N)) if want_k else None
+    s2 = np.zeros(padded_shape(N)) if want_k else None
+    lib().orc_ic_2lpt_from_particles(C.byref(ip), pos01, len(pos01), float(normfac), rescale_rk, D1, D2,
+                                     None if dk is None else dk.ctypes.data, None if s2 is None else s2.ctypes.data)
     return (D1, D2, dk, s2) if want_k else (D1, D2)
 
 

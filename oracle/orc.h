@@ -207,6 +207,13 @@ void orc_seedtable(int N, uint32_t seed, uint32_t *table);
  * pointers are non-NULL. */
 void orc_ic_2lpt(const orc_ic_params *ip, const orc_power *pw, double *D1, double *D2,
                  double *deltak_out, double *source2k_out);
+/* The same from particles read from files (ReadParticlesFromFile,
+ * src/readICfromfile.c:133-777): pos01 [n][3] in [0,1), normfac =
+ * D_LCDM(1)/D_LCDM(a_i)/N^3, rescale_rk[|d|^2] the P(k) rescaling per integer
+ * |k|^2 (sqrt(mg_pofk_ratio(k, 1)) / sigma8 enhancement as applicable). */
+void orc_ic_2lpt_from_particles(const orc_ic_params *ip, const double *pos01, long n, double normfac,
+                                const double *rescale_rk, double *D1, double *D2, double *deltak_out,
+                                double *source2k_out);
 
 /* Scale-dependent displacement fields (SCALEDEPENDENT build).  Field types
  * as src/proto.h:153-158. */

@@ -35,6 +35,9 @@ static double kcomp(int i, int N, double box) {
 
 static void cset(double *c, size_t idx, double re, double im) { c[2 * idx] = re; c[2 * idx + 1] = im; }
 
+static void lpt_from_cdisp(const orc_ic_params *ip, double *cdisp[3], double *D1, double *D2,
+                           double *source2k_out);
+
 void orc_ic_2lpt(const orc_ic_params *ip, const orc_power *pw, double *D1, double *D2,
                  double *deltak_out, double *source2k_out) {
   const int N = ip->N, Ns = ip->Ns, NH = N / 2 + 1;
@@ -105,7 +108,17 @@ void orc_ic_2lpt(const orc_ic_params *ip, const orc_power *pw, double *D1, doubl
   free(seedtable);
   if (deltak_out) memcpy(deltak_out, cdelta, sizeof(double) * 2 * tot);
   free(cdelta);
+  lpt_from_cdisp(ip, cdisp, D1, D2, source2k_out);
+}
 
+/* The 2LPT part shared by both IC sources (2LPT.c:1209-1519): gradients of
+ * the ZA displacements, second-order source, both displacement fields and
+ * the read-out to the lattice.  Frees cdisp. */
+static void lpt_from_cdisp(const orc_ic_params *ip, double *cdisp[3], double *D1, double *D2,
+                           double *source2k_out) {
+  const int N = ip->N, Ns = ip->Ns, NH = N / 2 + 1;
+  const double Box = ip->box;
+  const size_t tot = (size_t)N * N * NH;
   /* displacement gradients, 2LPT.c:1224-1270 */
   double *dg[6];
   for (int g = 0; g < 6; g++) dg[g] = malloc(sizeof(double) * 2 * tot);
@@ -194,4 +207,77 @@ void orc_ic_2lpt(const orc_ic_params *ip, const orc_power *pw, double *D1, doubl
   for (long q = 0; q < np; q++)
     for (int a = 0; a < 3; a++) { D1[3 * q + a] -= sum1[a]; D2[3 * q + a] -= sum2[a]; }
   for (int a = 0; a < 3; a++) { free(cdisp[a]); free(cdisp2[a]); }
+}
+
+/* ReadFilesMakeDisplacementField + AssignDisplacementField
+ * (src/readICfromfile.c:133-219, 533-777): particles (positions in [0,1) of
+ * the box, [n][3]) CIC-deposited as ProcessParticlesSingleFile does (density
+ * starts at -1, weight (N/Ns)^3 folded into the y factors), R2C, times
+ * normfac = D_LCDM(1) / D_LCDM(a_i) / N^3, modes with |d| > Ns/2 zeroed when
+ * N > Ns; then cdisp = i k / k^2 delta(k) * grid_corr * rescale with
+ * grid_corr = 1 / prod_{d != 0} sinc(pi d / N)^2 and rescale[|d|^2] given by
+ * the caller (sqrt(mg_pofk_ratio(k, 1)), divided by the sigma8 enhancement
+ * when the input sigma8 is not for LCDM).  With N <= Ns the three Nyquist
+ * planes of delta(k) are zeroed (the reference uses +N/2 there for the
+ * displacement and -N/2 for its gradients).  Then the shared 2LPT part. */
+void orc_ic_2lpt_from_particles(const orc_ic_params *ip, const double *pos01, long n, double normfac,
+                                const double *rescale_rk, double *D1, double *D2, double *deltak_out,
+                                double *source2k_out) {
+  const int N = ip->N, Ns = ip->Ns, NH = N / 2 + 1;
+  const size_t P = 2 * (size_t)NH, tot = (size_t)N * N * NH;
+  const double Box = ip->box;
+  double *rho = malloc(sizeof(double) * (size_t)N * N * P);
+  for (size_t q = 0; q < (size_t)N * N * P; q++) rho[q] = -1.0;
+  const double wpar = pow((double)N / (double)Ns, 3);
+  for (long q = 0; q < n; q++) {
+    double X = pos01[3 * q] * N, Y = pos01[3 * q + 1] * N, Z = pos01[3 * q + 2] * N;
+    unsigned IX = (unsigned)X, IY = (unsigned)Y, IZ = (unsigned)Z;
+    double DX = X - IX, DY = Y - IY, DZ = Z - IZ, TX = 1 - DX, TY = 1 - DY, TZ = 1 - DZ;
+    DY *= wpar;
+    TY *= wpar;
+    if (IX >= (unsigned)N) IX = 0;
+    if (IY >= (unsigned)N) IY = 0;
+    if (IZ >= (unsigned)N) IZ = 0;
+    unsigned IXn = IX + 1 >= (unsigned)N ? 0 : IX + 1, IYn = IY + 1 >= (unsigned)N ? 0 : IY + 1,
+             IZn = IZ + 1 >= (unsigned)N ? 0 : IZ + 1; /* the ghost x-slice is slice 0 for one task */
+    rho[((size_t)IX * N + IY) * P + IZ] += TX * TY * TZ;
+    rho[((size_t)IX * N + IY) * P + IZn] += TX * TY * DZ;
+    rho[((size_t)IX * N + IYn) * P + IZ] += TX * DY * TZ;
+    rho[((size_t)IX * N + IYn) * P + IZn] += TX * DY * DZ;
+    rho[((size_t)IXn * N + IY) * P + IZ] += DX * TY * TZ;
+    rho[((size_t)IXn * N + IY) * P + IZn] += DX * TY * DZ;
+    rho[((size_t)IXn * N + IYn) * P + IZ] += DX * DY * TZ;
+    rho[((size_t)IXn * N + IYn) * P + IZn] += DX * DY * DZ;
+  }
+  orc_fft_r2c(N, rho);
+  double *dk = rho; /* complex [N][N][NH] in place */
+  for (size_t c = 0; c < 2 * tot; c++) dk[c] *= normfac;
+  double *cdisp[3], *cdelta = calloc(2 * tot, 8);
+  for (int a = 0; a < 3; a++) cdisp[a] = calloc(2 * tot, 8);
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++)
+      for (int k = 0; k < NH; k++) {
+        const size_t c = ((size_t)i * N + j) * NH + k;
+        const int d[3] = {i > N / 2 ? i - N : i, j > N / 2 ? j - N : j, k};
+        const long d2 = (long)d[0] * d[0] + (long)d[1] * d[1] + (long)d[2] * d[2];
+        if (d2 == 0) continue;
+        if (N > Ns && sqrt((double)d2) > Ns / 2) continue;
+        if (N <= Ns && (i == N / 2 || j == N / 2 || k == N / 2)) continue;
+        double gc = 1.0;
+        for (int a = 0; a < 3; a++)
+          if (d[a] != 0) gc *= sin(PI * d[a] / (double)N) / (PI * d[a] / (double)N);
+        const double f = 1.0 / (gc * gc) * rescale_rk[d2];
+        const double re = dk[2 * c] * f, im = dk[2 * c + 1] * f;
+        double kvec[3], kmag2 = 0.0;
+        for (int a = 0; a < 3; a++) {
+          kvec[a] = d[a] * 2 * PI / Box;
+          kmag2 += kvec[a] * kvec[a];
+        }
+        for (int a = 0; a < 3; a++) cset(cdisp[a], c, -kvec[a] / kmag2 * im, kvec[a] / kmag2 * re);
+        cset(cdelta, c, re, im);
+      }
+  free(rho);
+  if (deltak_out) memcpy(deltak_out, cdelta, sizeof(double) * 2 * tot);
+  free(cdelta);
+  lpt_from_cdisp(ip, cdisp, D1, D2, source2k_out);
 }
