@@ -154,6 +154,19 @@ typedef struct mgp_params {
    * keys required, as the READICFROMFILE build does. */
   int ReadParticlesFromFile, NumInputParticleFiles, RamsesOutputNumber, TypeInputParticleFiles;
   char InputParticleFileDir[500], InputParticleFilePrefix[500];
+  /* massive neutrinos (the MASSIVE_NEUTRINOS build, which needs
+   * scaledependent = 1): massive_neutrinos plays the build flag (the three
+   * nu_ keys are read from a parameter file when it is set before
+   * mgp_read_parameterfile); nu_include_massive_neutrinos switches them on,
+   * Omega_nu = nu_SumMassNuEV / (93.14 h^2), and nu_FilenameTransferInfofile
+   * names "<dir> <n>" followed by n lines "<file> <z>" of CAMB transfer
+   * files (one header line, 13 columns: k/h, T_cdm, T_b, T_g, T_nu,
+   * T_massive_nu, T_tot, ...), z increasing.  The linear P(k) is then the
+   * CDM+baryon spectrum of those files and every step adds the neutrino
+   * density to delta(k) (src/auxPM.c:383-428). */
+  int massive_neutrinos, nu_include_massive_neutrinos;
+  double nu_SumMassNuEV;
+  char nu_FilenameTransferInfofile[500];
 } mgp_params;
 
 typedef struct mgp_ctx mgp_ctx;
@@ -241,6 +254,11 @@ int mgp_output_stats(mgp_ctx *ctx, int *count, double *wait_ms, double *file_ms,
  * kmean = mean |k| of the modes, n = mode count (weights as the reference). */
 int mgp_pofk(mgp_ctx *ctx, int cap, int *nbins, double *k, double *pk, double *kmean, double *n);
 
+/* Total matter P(k) of a run with massive neutrinos (the "total" spectrum
+ * of src/auxPM.c:423-426: delta(k) after the neutrino density was added in
+ * the last mgp_get_displacements); without neutrinos the same as mgp_pofk. */
+int mgp_pofk_total(mgp_ctx *ctx, int cap, int *nbins, double *k, double *pk, double *kmean, double *n);
+
 /* RSD multipoles P0/P2/P4 for LOS y and z (compute_RSD_powerspectrum,
  * src/compute_pofk.c:403-512) at the current particle state.  The seven
  * output arrays (k, P0, P2, P4 averaged over y and z, and the sigma
@@ -270,8 +288,10 @@ double mgp_Sphi(mgp_ctx *ctx, double ai, double af, double aref);
 double mgp_power_spectrum(mgp_ctx *ctx, double k);
 
 /* Host-only cosmology of a parameter set (no device needed): which 0-6 as
- * mgp_growth, 7 the linear P(k) at x = k (h/Mpc); mgp_cosmo_coeff gives Sq
- * (kind 0) or Sphi (kind 1) for n triples (ai, af, aref). */
+ * mgp_growth, 7 the linear P(k) at x = k (h/Mpc), 8 mg_pofk_ratio(k = x,
+ * a = 1), 9 mg_sigma8_enhancement(a = x) (src/cosmo.c:688-756);
+ * mgp_cosmo_coeff gives Sq (kind 0) or Sphi (kind 1) for n triples
+ * (ai, af, aref). */
 int mgp_cosmo_eval(const mgp_params *p, int which, const double *x, int n, double *out);
 /* growth_*_scaledependent(k, a) (src/cosmo.c:987-1010) of a parameter set
  * with scaledependent = 1, host only: which 0 D, 1 dD/dy, 2 d2D/dy2, 3 D2,
@@ -390,9 +410,12 @@ double mgp_closure_scale_at(mgp_closure *cl, double A);
 double mgp_closure_get_highpass(mgp_closure *cl);
 
 /* Copy an internal grid to a host buffer (diagnostics and parity tests).
- * which: 0 density (real padded [N][N][2(N/2+1)] float), 1 delta(k)
- * (complex [N][N][N/2+1] float pairs), 2..4 force grids x,y,z (real
- * padded), 5 MG source (complex).  `count` is the number of floats. */
+ * which: 0 density (real padded [N][N][2(N/2+1)] float; after the fifth
+ * force the MG source, which reuses it), 1 delta(k) (complex [N][N][N/2+1]
+ * float pairs; the total matter field once massive neutrinos were added),
+ * 2..4 force grids x,y,z (real padded), 5 as 0, 6 the filtered density of
+ * the MG solver, 7 the stored IC delta(k) of the scale-dependent build
+ * (cdelta_cdm).  `count` is the number of floats. */
 int mgp_copy_grid(mgp_ctx *ctx, int which, float *host, size_t count);
 
 /* Kernel timing: CUDA-event milliseconds of the named kernels launched by

@@ -292,9 +292,14 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   }
   free(c->box_p);
   void *bufs[] = {c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
-                  c->fft_work, c->rk_bin, c->pk_thr, c->win1d, c->pk_block, c->pk_sum, c->rsd_block, c->rsd_sum};
+                  c->fft_work, c->rk_bin, c->pk_thr, c->win1d, c->pk_block, c->pk_sum, c->rsd_block, c->rsd_sum,
+                  c->pk_sum_tot, c->nu_tab_d};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
     if (bufs[i]) cudaFree(bufs[i]);
+  if (c->nu_tab_h) cudaFreeHost(c->nu_tab_h);
+  for (int q = 0; q < 2; q++)
+    if (c->nu_ev[q]) cudaEventDestroy(c->nu_ev[q]);
+  free(c->nu_den);
   for (int t = 0; t < MGP_NTIMERS; t++) {
     if (c->ev[t][0]) cudaEventDestroy(c->ev[t][0]);
     if (c->ev[t][1]) cudaEventDestroy(c->ev[t][1]);
@@ -712,7 +717,8 @@ static int mg_filter_kind(const mgp_params *p) {
   return 0;
 }
 
-static int pofk_now(mgp_ctx *c, int fuse_kind, double A) {
+// P(k) sums of the current delta(k) into `sums` (c->pk_sum by default).
+static int pofk_now(mgp_ctx *c, int fuse_kind, double A, double *sums = NULL) {
   const mgp_params *p = &c->p;
   const int N = c->g.N;
   float fa = 0.f, fb = 0.f;
@@ -723,14 +729,51 @@ static int pofk_now(mgp_ctx *c, int fuse_kind, double A) {
     fb = (float)(1.0 / pow((double)N, 3) * 1.5 * p->Omega / A * pow(p->Box / 2997.92458 / (2.0 * M_PI), 2));
   }
   RET_IF(mgp_launch_pofk_thr(c->dk, N, c->pk_thr, c->win1d, c->pk_nbins, c->pk_bintype, c->pk_kmin, c->pk_kmax,
-                             c->pk_block, c->pk_blocks, c->pk_sum, fuse_kind, p->smoothing_filter,
+                             c->pk_block, c->pk_blocks, sums ? sums : c->pk_sum, fuse_kind, p->smoothing_filter,
                              fuse_kind ? c->mg1 : NULL, fa, fb, c->stream));
+  return MGP_OK;
+}
+
+// Massive neutrinos (src/auxPM.c:383-428).  The factor table of this step
+// is computed on the host and uploaded before the step's first launch, so
+// the host works while the GPU finishes the previous step's kick and drift.
+static int nu_prepare(mgp_ctx *c, double A) {
+  const int N = c->g.N, h = N / 2;
+  const int nrk = 3 * h * h + 1;
+  if (!c->nu_tab_h) {
+    MGP_CUDA(cudaMallocHost(&c->nu_tab_h, sizeof(double) * 2 * nrk));
+    MGP_CUDA(cudaMalloc(&c->nu_tab_d, sizeof(double) * nrk));
+    for (int q = 0; q < 2; q++) MGP_CUDA(cudaEventCreateWithFlags(&c->nu_ev[q], cudaEventDisableTiming));
+    c->nu_den = (double *)malloc(sizeof(double) * nrk);
+    if (!c->nu_den) return mgp_set_error(MGP_ENOMEM, "neutrino table");
+    mgp_cosmo_nu_den(&c->cosmo, N, nrk, c->nu_den);
+  }
+  c->nu_slot ^= 1;
+  double *slot = c->nu_tab_h + (size_t)c->nu_slot * nrk;
+  MGP_CUDA(cudaEventSynchronize(c->nu_ev[c->nu_slot]));  // its upload two steps ago is done
+  c->nu_cdmfac = mgp_cosmo_nu_table(&c->cosmo, A, N, nrk, c->nu_den, slot);
+  MGP_CUDA(cudaMemcpyAsync(c->nu_tab_d, slot, sizeof(double) * nrk, cudaMemcpyHostToDevice, c->stream));
+  MGP_CUDA(cudaEventRecord(c->nu_ev[c->nu_slot], c->stream));
+  return MGP_OK;
+}
+
+// delta(k) becomes the total matter density, cdmfac delta_cdm(k) + the
+// neutrino term grown from the stored IC field, and its P(k) ("total") is
+// binned.
+static int add_neutrinos(mgp_ctx *c, double A) {
+  if (!c->sd_dk[0]) return mgp_set_error(MGP_ESTATE, "massive neutrinos need the scale-dependent IC field");
+  RET_IF(mgp_launch_nu_add(c->dk, c->sd_dk[0], c->g.N, c->nu_cdmfac, c->nu_tab_d, c->stream));
+  if (c->p.pofk_compute_every_step) {
+    if (!c->pk_sum_tot) MGP_CUDA(cudaMalloc(&c->pk_sum_tot, sizeof(double) * c->pk_nbins));
+    RET_IF(pofk_now(c, 0, A, c->pk_sum_tot));
+  }
   return MGP_OK;
 }
 
 extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   RET_IF(require_particles(c));
   const int N = c->g.N;
+  if (c->cosmo.nu) RET_IF(nu_prepare(c, A));
   // PtoMesh, src/auxPM.c:280-432
   tstart(c, T_FILL);
   RET_IF(mgp_launch_fill(c->rho, c->g.nreal, -1.0f, c->stream));
@@ -746,11 +789,14 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   c->last_density_a = A;
   int fused = 0;
   if (c->p.pofk_compute_every_step) {
-    fused = mg_filter_kind(&c->p);
+    // with massive neutrinos the fifth-force filter reads the total field,
+    // so it is not fused into the CDM P(k) pass
+    fused = c->cosmo.nu ? 0 : mg_filter_kind(&c->p);
     tstart(c, T_POFK);
     RET_IF(pofk_now(c, fused, A));
     tstop(c, T_POFK);
   }
+  if (c->cosmo.nu) RET_IF(add_neutrinos(c, A));
   int mg_kind = 0;
   float coupling = 0.f, mass2 = 0.f;
   tstart(c, T_MG);
@@ -854,14 +900,17 @@ extern "C" int mgp_step(mgp_ctx *c, double A, double AI, double AF, double AFF) 
   return MGP_OK;
 }
 
-extern "C" int mgp_pofk(mgp_ctx *c, int cap, int *nbins, double *k, double *pk, double *kmean, double *n) {
+static int pofk_out(mgp_ctx *c, int total, int cap, int *nbins, double *k, double *pk, double *kmean, double *n) {
   RET_IF(require_particles(c));
   if (!c->have_density) return mgp_set_error(MGP_ESTATE, "no density: call mgp_get_displacements first");
+  // without P(k) every step the sums are taken now from delta(k), which is
+  // the total matter field once massive neutrinos were added
   if (!c->p.pofk_compute_every_step) RET_IF(pofk_now(c, 0, c->last_density_a));
+  const double *sums = total && c->cosmo.nu && c->p.pofk_compute_every_step ? c->pk_sum_tot : c->pk_sum;
   const int nb = c->pk_nbins;
   if (nbins) *nbins = nb;
   if (cap < nb) return mgp_set_error(MGP_EINVAL, "P(k) capacity %d < %d bins", cap, nb);
-  MGP_CUDA(cudaMemcpyAsync(c->pk_host, c->pk_sum, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
+  MGP_CUDA(cudaMemcpyAsync(c->pk_host, sums, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
   MGP_CUDA(cudaStreamSynchronize(c->stream));
   const double N = c->g.N, box = c->p.Box;
   const double norm = pow(box, 3) / pow(N, 6), shot = pow(box / (double)c->Ns, 3);
@@ -878,6 +927,15 @@ extern "C" int mgp_pofk(mgp_ctx *c, int cap, int *nbins, double *k, double *pk, 
     if (n) n[b] = c->pk_n[b];
   }
   return MGP_OK;
+}
+
+// P(k) of the last density (compute_power_spectrum "CDM"), and the total
+// matter P(k) of a run with massive neutrinos ("total"; the CDM one without)
+extern "C" int mgp_pofk(mgp_ctx *c, int cap, int *nbins, double *k, double *pk, double *kmean, double *n) {
+  return pofk_out(c, 0, cap, nbins, k, pk, kmean, n);
+}
+extern "C" int mgp_pofk_total(mgp_ctx *c, int cap, int *nbins, double *k, double *pk, double *kmean, double *n) {
+  return pofk_out(c, 1, cap, nbins, k, pk, kmean, n);
 }
 
 // compute_RSD_powerspectrum (src/compute_pofk.c:403-512): redshift-space
@@ -1097,6 +1155,7 @@ extern "C" int mgp_copy_grid(mgp_ctx *c, int which, float *host, size_t count) {
     case 2: case 3: case 4: src = c->frc + (which - 2) * c->g.nreal; break;
     case 5: src = c->rho; break;
     case 6: src = c->mg1; break;
+    case 7: src = c->sd_dk[0]; break;
     default: return mgp_set_error(MGP_EINVAL, "unknown grid %d", which);
   }
   if (!src) return mgp_set_error(MGP_ESTATE, "grid %d is not allocated", which);

@@ -306,6 +306,15 @@ static double quad(qfn f, const void *par, double a, double b, int panels) {
   return s;
 }
 
+/* massive-neutrino factors of the growth equations (defined below) */
+typedef struct {
+  int nx;
+  double *rows; /* 8 nx: value and d/d ln k of the four transfer functions */
+} nu_rows;
+static void nu_rows_at(const mgp_cosmo *c, double a, nu_rows *o);
+static double nu_mu1(const mgp_cosmo *c, const nu_rows *o, double k);
+static double nu_mu2(const mgp_cosmo *c);
+
 /* ------------------------------------------------------------ growth ODE */
 typedef struct { const mgp_cosmo *c; int lcdm; } ode_par;
 
@@ -325,10 +334,20 @@ static void growth_rhs(const ode_par *op, double x, const double *y, double *f) 
       mod = mgp_factor_2lpt(c, a);
     }
   }
+  double mu1 = 1.0;
+  if (c->nu_growth) {
+    /* ode_growth_D / ode_growth_DLCDM at k_value = 1e-3 (cosmo.c:227-236,
+     * 256-265, 459) */
+    double *buf = (double *)malloc(sizeof(double) * 8 * c->nuT[0].nx);
+    nu_rows nr = {0, buf};
+    nu_rows_at(c, a, &nr);
+    mu1 = nu_mu1(c, &nr, 1e-3);
+    free(buf);
+  }
   f[0] = y[1];
-  f[1] = -alpha * y[1] + beta * y[0];
+  f[1] = -alpha * y[1] + beta * mu1 * y[0];
   f[2] = y[3];
-  f[3] = -alpha * y[3] + beta * (y[2] - mod * y[0] * y[0]);
+  f[3] = -alpha * y[3] + beta * nu_mu2(c) * (y[2] - mod * y[0] * y[0]);
 }
 
 /* Dormand-Prince 5(4) coefficients (Dormand & Prince 1980, Table 2). */
@@ -510,27 +529,178 @@ static double column_eval(const mgp_bicubic *b, const double *val, const double 
          u * (1 - u) * (1 - u) * dy * dval[j] + u * u * (u - 1) * dy * dval[j + 1];
 }
 
+/* value and d/dx of the bicubic along y = yv (clamped) at every x node: the
+ * cubic Hermite in y of z and z_x */
+static void bicubic_row(const mgp_bicubic *b, double yv, double *val, double *dval) {
+  if (yv < b->y[0]) yv = b->y[0];
+  if (yv > b->y[b->ny - 1]) yv = b->y[b->ny - 1];
+  int j = grid_cell(b->y, b->ny, yv);
+  double dy = b->y[j + 1] - b->y[j], u = (yv - b->y[j]) / dy;
+  double h0 = (1 + 2 * u) * (1 - u) * (1 - u), h1 = u * u * (3 - 2 * u), g0 = u * (1 - u) * (1 - u) * dy,
+         g1 = u * u * (u - 1) * dy;
+  for (int i = 0; i < b->nx; i++) {
+    size_t c0 = (size_t)j * b->nx + i, c1 = c0 + b->nx;
+    val[i] = h0 * b->z[c0] + h1 * b->z[c1] + g0 * b->zy[c0] + g1 * b->zy[c1];
+    dval[i] = h0 * b->zx[c0] + h1 * b->zx[c1] + g0 * b->zxy[c0] + g1 * b->zxy[c1];
+  }
+}
+
+/* cubic Hermite in x of a row (val, dval on the x nodes), x clamped */
+static double row_eval(const mgp_bicubic *b, const double *val, const double *dval, double xv) {
+  if (xv < b->x[0]) xv = b->x[0];
+  if (xv > b->x[b->nx - 1]) xv = b->x[b->nx - 1];
+  int i = grid_cell(b->x, b->nx, xv);
+  double dx = b->x[i + 1] - b->x[i], t = (xv - b->x[i]) / dx;
+  return (1 + 2 * t) * (1 - t) * (1 - t) * val[i] + t * t * (3 - 2 * t) * val[i + 1] +
+         t * (1 - t) * (1 - t) * dx * dval[i] + t * t * (t - 1) * dx * dval[i + 1];
+}
+
+/* ------------------------------------------------------ massive neutrinos */
+/* The CAMB transfer functions at one redshift z = 1/a - 1 as rows over ln k
+ * (Lookup_GSL_2D_Spline(spline, ln k, z), clamped, src/wrappers.c:132-139):
+ * rows[2 q], rows[2 q + 1] value and d/d ln k of table q (nu, cdm, baryon,
+ * total).  Every file shares the same k nodes. */
+static void nu_rows_at(const mgp_cosmo *c, double a, nu_rows *o) {
+  o->nx = c->nuT[0].nx;
+  for (int q = 0; q < 4; q++)
+    bicubic_row(&c->nuT[q], 1.0 / a - 1.0, o->rows + 2 * q * o->nx, o->rows + (2 * q + 1) * o->nx);
+}
+static double nu_T(const mgp_cosmo *c, const nu_rows *o, int q, double k) {
+  return row_eval(&c->nuT[q], o->rows + 2 * q * o->nx, o->rows + (2 * q + 1) * o->nx, log(k));
+}
+/* get_cdm_baryon_transfer_function (read_CAMB_data.h:198-201) */
+static double nu_Tcb(const mgp_cosmo *c, const nu_rows *o, double k, double ocdm) {
+  const double ob = c->p.OmegaBaryon;
+  return (ob * nu_T(c, o, 2, k) + ocdm * nu_T(c, o, 1, k)) / (ob + ocdm);
+}
+/* GeffoverG_neutrino_1LPT / _2LPT (user_defined_functions.h:664-684) */
+static double nu_mu1(const mgp_cosmo *c, const nu_rows *o, double k) {
+  if (!c->nu_growth) return 1.0;
+  const double om = c->p.Omega;
+  return (om - c->OmegaNu) / om + c->OmegaNu / om * nu_T(c, o, 0, k) / nu_Tcb(c, o, k, c->OmegaCDM);
+}
+static double nu_mu2(const mgp_cosmo *c) { return c->nu_growth ? (c->p.Omega - c->OmegaNu) / c->p.Omega : 1.0; }
+
+/* read_and_spline_transfer_functions + read_single_transfer_function_file
+ * (src/read_CAMB_data.h:41-170, 238-278) */
+static int read_camb(mgp_cosmo *c, char *err, size_t errlen) {
+  FILE *fp = fopen(c->p.nu_FilenameTransferInfofile, "r");
+  if (!fp) {
+    snprintf(err, errlen, "Error read_and_spline_transfer_functions: cannot read [%s]", c->p.nu_FilenameTransferInfofile);
+    return MGP_EIO;
+  }
+  char dir[500];
+  int nz = 0;
+  if (fscanf(fp, "%499s %d", dir, &nz) != 2 || nz < 2) {
+    fclose(fp);
+    snprintf(err, errlen, "transfer info file '%s': need '<dir> <n>' with n >= 2", c->p.nu_FilenameTransferInfofile);
+    return MGP_EPARAM;
+  }
+  double *zs = (double *)malloc(sizeof(double) * nz), *logk = NULL, *T[4] = {NULL, NULL, NULL, NULL};
+  int nk = 0, rc = MGP_OK;
+  const int col[4] = {5, 1, 2, 6}; /* T_massive_nu, T_cdm, T_b, T_tot */
+  for (int i = 0; i < nz && rc == MGP_OK; i++) {
+    char fn[500], path[1100];
+    if (fscanf(fp, "%499s %lf", fn, &zs[i]) != 2) {
+      snprintf(err, errlen, "transfer info file: short list (%d of %d files)", i, nz);
+      rc = MGP_EPARAM;
+      break;
+    }
+    if (i > 0 && !(zs[i] > zs[i - 1])) {
+      snprintf(err, errlen, "transfer files must be listed with increasing redshift");
+      rc = MGP_EPARAM;
+      break;
+    }
+    snprintf(path, sizeof(path), "%s/%s", dir, fn);
+    FILE *tf = fopen(path, "r");
+    if (!tf) {
+      snprintf(err, errlen, "Error ed_camb_transfer_function_file: cannot open [%s]", path);
+      rc = MGP_EIO;
+      break;
+    }
+    int ch;
+    while ((ch = fgetc(tf)) != EOF && ch != '\n') {
+    } /* one header line */
+    int cap = 256, n = 0;
+    double *rows = (double *)malloc(sizeof(double) * 13 * cap), v[13];
+    for (;;) {
+      int got = 0;
+      while (got < 13 && fscanf(tf, "%lf", &v[got]) == 1) got++;
+      if (got == 0) break;
+      if (got < 13) {
+        snprintf(err, errlen, "transfer file '%s': a row with %d of 13 columns", path, got);
+        rc = MGP_EIO;
+        break;
+      }
+      if (n == cap) {
+        cap *= 2;
+        rows = (double *)realloc(rows, sizeof(double) * 13 * cap);
+      }
+      memcpy(rows + 13 * n, v, sizeof(v));
+      n++;
+    }
+    fclose(tf);
+    if (rc == MGP_OK && i == 0) {
+      nk = n;
+      logk = (double *)malloc(sizeof(double) * nk);
+      for (int q = 0; q < 4; q++) T[q] = (double *)malloc(sizeof(double) * (size_t)nz * nk);
+      for (int j = 0; j < nk; j++) logk[j] = log(rows[13 * j]);
+    }
+    if (rc == MGP_OK && (n != nk || nk < 4)) {
+      snprintf(err, errlen, "transfer file '%s' has %d rows where %d expected (same k nodes in every file)", path, n, nk);
+      rc = MGP_EIO;
+    }
+    for (int j = 0; j < nk && rc == MGP_OK; j++)
+      for (int q = 0; q < 4; q++) T[q][(size_t)i * nk + j] = rows[13 * j + col[q]];
+    free(rows);
+  }
+  fclose(fp);
+  if (rc == MGP_OK)
+    for (int q = 0; q < 4; q++) bicubic_init(&c->nuT[q], logk, zs, T[q], nk, nz);
+  else
+    for (int q = 0; q < 4; q++) free(T[q]);
+  free(logk);
+  free(zs);
+  return rc;
+}
+
+/* get_total_power_spectrum / get_cdm_baryon_power_spectrum at z = 0
+ * (read_CAMB_data.h:215-228), before the normalisation */
+static double nu_pofk_cb(const mgp_cosmo *c, double k, double ocdm) {
+  const double h = c->p.HubbleParam;
+  const nu_rows o = {c->nuT[0].nx, c->nu_rows0};
+  const double Ttot = nu_T(c, &o, 3, k), Tcb = nu_Tcb(c, &o, k, ocdm);
+  const double ptot = 2.0 * M_PI * M_PI * Ttot * Ttot * (k * h) * pow(k * h / 0.05, c->p.PrimordialIndex - 1.0) * h * h * h;
+  return ptot * (Tcb / Ttot) * (Tcb / Ttot);
+}
+
 /* Dormand-Prince 5(4) over all k at once with one shared step size (the
  * a-dependent parts of the right-hand side are evaluated once per stage). */
 typedef struct {
   const mgp_cosmo *c;
   int nk;
   const double *k;
+  int lcdm;      /* mu = 1 and modfac = 1 (the LCDM growth of the neutrino build) */
+  double *nubuf; /* 8 nx scratch for the neutrino rows */
 } sd_ode;
 
 static void sd_rhs(const sd_ode *o, double x, const double *y, double *f) {
   double a = exp(x), om = o->c->p.Omega;
   mgp_sd_apart ap;
   sd_apart(o->c, a, &ap);
+  nu_rows nr = {0, o->nubuf};
+  if (o->c->nu_growth) nu_rows_at(o->c, a, &nr);
+  const double mu2 = nu_mu2(o->c);
   for (int q = 0; q < o->nk; q++) {
     const double *Y = y + 4 * q;
     double *F = f + 4 * q;
-    double mu = sd_mu(&ap, o->k[q]);
-    double beta = ap.beta0 * mu, mod = sd_modfac(&ap, a, o->k[q], mu, om);
+    double mu = o->lcdm ? 1.0 : sd_mu(&ap, o->k[q]);
+    double beta = ap.beta0 * mu, mod = o->lcdm ? 1.0 : sd_modfac(&ap, a, o->k[q], mu, om);
+    double mu1 = o->c->nu_growth ? nu_mu1(o->c, &nr, o->k[q]) : 1.0;
     F[0] = Y[1];
-    F[1] = -ap.alpha * Y[1] + beta * Y[0];
+    F[1] = -ap.alpha * Y[1] + beta * mu1 * Y[0];
     F[2] = Y[3];
-    F[3] = -ap.alpha * Y[3] + beta * (Y[2] - mod * Y[0] * Y[0]);
+    F[3] = -ap.alpha * Y[3] + beta * mu2 * (Y[2] - mod * Y[0] * Y[0]);
   }
 }
 
@@ -576,8 +746,10 @@ static int sd_dp45(const sd_ode *o, double x0, double x1, double *y, double *hgu
   return 0;
 }
 
-/* calculate_scale_dependent_growth_factor (src/cosmo.c:798-981) */
-static int solve_growth_sd(mgp_cosmo *c, char *err, size_t errlen) {
+/* calculate_scale_dependent_growth_factor (src/cosmo.c:798-981); lcdm = 1
+ * solves the LCDM growth of the neutrino build (cosmo.c:829-884: mu = 1,
+ * modfac = 1, the neutrino factor kept) and keeps only D(k, a). */
+static int solve_growth_sd(mgp_cosmo *c, int lcdm, char *err, size_t errlen) {
   const int npts = 1000;
   const int nk = c->p.sd_nk > 0 ? c->p.sd_nk : 1000;
   const double kmin = c->p.sd_kmin > 0 ? c->p.sd_kmin : 2.0 * M_PI / c->p.Box * 0.5;
@@ -602,7 +774,8 @@ static int solve_growth_sd(mgp_cosmo *c, char *err, size_t errlen) {
     y[4 * q + 2] = -3.0 / 7.0;
     y[4 * q + 3] = -6.0 / 7.0;
   }
-  sd_ode o = {c, nk, kk};
+  double *nubuf = c->nu_growth ? (double *)malloc(sizeof(double) * 8 * c->nuT[0].nx) : NULL;
+  sd_ode o = {c, nk, kk, lcdm, nubuf};
   double h = 1e-4;
   int rc = MGP_OK;
   for (int i = 0; i < npts && rc == MGP_OK; i++) {
@@ -614,25 +787,31 @@ static int solve_growth_sd(mgp_cosmo *c, char *err, size_t errlen) {
     double a = exp(x[i]), qa = Qfactor(c, a) / a, om = c->p.Omega;
     mgp_sd_apart ap;
     sd_apart(c, a, &ap);
+    nu_rows nr = {0, nubuf};
+    if (c->nu_growth) nu_rows_at(c, a, &nr);
+    const double mu2 = nu_mu2(c);
     for (int q = 0; q < nk; q++) {
       const double *Y = y + 4 * q;
-      double mu = sd_mu(&ap, kk[q]);
+      double mu = lcdm ? 1.0 : sd_mu(&ap, kk[q]), mu1 = c->nu_growth ? nu_mu1(c, &nr, kk[q]) : 1.0;
       size_t cc = (size_t)q * npts + i;
       T[0][cc] = Y[0];
       T[1][cc] = Y[1] * qa;
-      T[2][cc] = 1.5 * mu * om * a * Y[0];
+      T[2][cc] = 1.5 * mu * mu1 * om * a * Y[0];
       T[3][cc] = Y[2];
       T[4][cc] = Y[3] * qa;
-      T[5][cc] = 1.5 * mu * om * a * (Y[2] - Y[0] * Y[0]);
+      T[5][cc] = 1.5 * mu * mu2 * om * a * (Y[2] - Y[0] * Y[0]);
     }
   }
-  if (rc == MGP_OK) {
+  if (rc == MGP_OK && lcdm) {
+    bicubic_init(&c->sd_lcdm, x, logk, T[0], npts, nk);
+    for (int f = 1; f < 6; f++) free(T[f]);
+  } else if (rc == MGP_OK) {
     for (int f = 0; f < 6; f++) bicubic_init(&c->sd_tab[f], x, logk, T[f], npts, nk);
     c->sd = 1;
   } else {
     for (int f = 0; f < 6; f++) free(T[f]);
   }
-  free(x); free(logk); free(kk); free(y); free(work);
+  free(x); free(logk); free(kk); free(y); free(work); free(nubuf);
   return rc;
 }
 
@@ -712,6 +891,9 @@ static double table_interp(const mgp_cosmo *c, double k) {
 }
 
 double mgp_cosmo_power(const mgp_cosmo *c, double k) {
+  /* PowerSpec with MASSIVE_NEUTRINOS (src/power.c:376-379): the CDM+baryon
+   * spectrum of the CAMB files */
+  if (c->p.massive_neutrinos) return c->norm * nu_pofk_cb(c, k, c->OmegaCDM);
   switch (c->p.WhichSpectrum) {
     case 0: {
       double T = c->p.WhichTransfer == 1 ? table_interp(c, k) : transfer_eh(c, k);
@@ -777,6 +959,17 @@ static int read_table(mgp_cosmo *c, const char *fname, int transfer, char *err, 
   return MGP_OK;
 }
 
+/* The raw LCDM growth factor: D_LCDM(k, a) of the neutrino build, else
+ * D_LCDM(a) (cosmo.c:692-698, 741-745). */
+static double lcdm_D(const mgp_cosmo *c, double k, double a) {
+  if (!c->sd_lcdm.nx) return spline_eval(&c->DL, log(a));
+  double *col = (double *)malloc(sizeof(double) * 2 * c->sd_lcdm.ny);
+  bicubic_column(&c->sd_lcdm, log(a), col, col + c->sd_lcdm.ny);
+  double d = column_eval(&c->sd_lcdm, col, col + c->sd_lcdm.ny, log(k));
+  free(col);
+  return d;
+}
+
 /* mg_pofk_ratio(k, a) (src/cosmo.c:688-706): (D/D_LCDM)^2 with the raw
  * (unnormalised) tables; D(k, a) in the scale-dependent build. */
 double mgp_cosmo_pofk_ratio(const mgp_cosmo *c, double k, double a) {
@@ -791,7 +984,7 @@ double mgp_cosmo_pofk_ratio(const mgp_cosmo *c, double k, double a) {
   } else {
     D = spline_eval(&c->D, log(a));
   }
-  double r = D / spline_eval(&c->DL, log(a));
+  double r = D / lcdm_D(c, k, a);
   return r * r;
 }
 void mgp_cosmo_pofk_ratio_many(const mgp_cosmo *c, double a, int n, const double *k, double *out) {
@@ -805,11 +998,14 @@ void mgp_cosmo_pofk_ratio_many(const mgp_cosmo *c, double a, int n, const double
     for (int i = 0; i < n; i++) out[i] = r * r;
     return;
   }
-  const mgp_bicubic *b = &c->sd_tab[0];
-  double *col = (double *)malloc(sizeof(double) * 2 * b->ny);
+  const mgp_bicubic *b = &c->sd_tab[0], *bl = &c->sd_lcdm;
+  double *col = (double *)malloc(sizeof(double) * 2 * (b->ny + bl->ny));
+  double *coll = col + 2 * b->ny;
   bicubic_column(b, log(a), col, col + b->ny);
+  if (bl->nx) bicubic_column(bl, log(a), coll, coll + bl->ny);
   for (int i = 0; i < n; i++) {
-    double r = column_eval(b, col, col + b->ny, log(k[i])) / DL;
+    double r = column_eval(b, col, col + b->ny, log(k[i])) /
+               (bl->nx ? column_eval(bl, coll, coll + bl->ny, log(k[i])) : DL);
     out[i] = r * r;
   }
   free(col);
@@ -831,8 +1027,9 @@ double mgp_cosmo_sigma8_enh(const mgp_cosmo *c, double a) {
     double k = exp(log(kmin) + log(kmax / kmin) * i / (double)(npts - 1)), kR8 = k * 8.0;
     double w = 3.0 / (kR8 * kR8 * kR8) * (sin(kR8) - kR8 * cos(kR8));
     double D = column_eval(b, col, col + b->ny, log(k)), pk = mgp_cosmo_power(c, k);
+    double DLk = c->sd_lcdm.nx ? lcdm_D(c, k, a) : DL;
     s += pk * w * w * D * D * k * k * k * dlogk / (2.0 * M_PI * M_PI);
-    sl += pk * w * w * DL * DL * k * k * k * dlogk / (2.0 * M_PI * M_PI);
+    sl += pk * w * w * DLk * DLk * k * k * k * dlogk / (2.0 * M_PI * M_PI);
   }
   free(col);
   return sqrt(s) / sqrt(sl);
@@ -980,7 +1177,16 @@ int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen) 
   memset(c, 0, sizeof(*c));
   c->p = *p;
   int rc;
-  if (p->WhichSpectrum == 1) {
+  if (p->massive_neutrinos) {
+    if (!p->scaledependent) {
+      snprintf(err, errlen, "Massive neutrinos must be compiled with SCALEDEPENDENT");
+      return MGP_EPARAM;
+    }
+    if ((rc = read_camb(c, err, errlen))) return rc;
+    c->nu_rows0 = (double *)malloc(sizeof(double) * 8 * c->nuT[0].nx);
+    nu_rows r0 = {0, c->nu_rows0};
+    nu_rows_at(c, 1.0, &r0);
+  } else if (p->WhichSpectrum == 1) {
     if ((rc = read_table(c, p->FileWithInputSpectrum, 0, err, errlen))) return rc;
   } else if (p->WhichSpectrum == 0 && p->WhichTransfer == 1) {
     if ((rc = read_table(c, p->FileWithInputTransfer, 1, err, errlen))) return rc;
@@ -995,11 +1201,28 @@ int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen) 
   }
   c->norm = p->Sigma8 * p->Sigma8 / s2;
   /* init_modified_version runs after initialize_powerspectrum in main.c
-   * (main.c:186-196), so the normalisation above uses the file's Omega/h */
+   * (main.c:153-162), so the normalisation above uses the file's Omega/h;
+   * with massive neutrinos it also ran with Omega_cdm still 0, i.e. with
+   * the baryon transfer function in place of the CDM+baryon one (kept) */
+  if (p->massive_neutrinos) {
+    /* init_modified_version (user_defined_functions.h:59-66) */
+    c->OmegaNu = p->nu_SumMassNuEV / (93.14 * p->HubbleParam * p->HubbleParam);
+    c->OmegaCDM = p->Omega - p->OmegaBaryon - c->OmegaNu;
+    if (c->OmegaNu < 1e-6) {
+      c->OmegaNu = 0.0;
+      c->OmegaCDM = p->Omega - p->OmegaBaryon;
+    }
+    /* the growth equations see the neutrinos whenever OmegaNu survived the
+     * cut (GeffoverG_neutrino_*, user_defined_functions.h:662-684); the
+     * density is added only with nu_include_massive_neutrinos */
+    c->nu_growth = c->OmegaNu > 0.0;
+    c->nu = p->nu_include_massive_neutrinos && c->nu_growth;
+  }
   if (p->model == MGP_MODEL_BRANSDICKE && (rc = jbd_solve(c, err, errlen))) return rc;
   if (p->model == MGP_MODEL_MBETA && p->modified_gravity_active) phia_solve(c);
   if ((rc = solve_growth(c, err, errlen))) return rc;
-  if (p->scaledependent) return solve_growth_sd(c, err, errlen);
+  if (p->massive_neutrinos && (rc = solve_growth_sd(c, 1, err, errlen))) return rc;
+  if (p->scaledependent) return solve_growth_sd(c, 0, err, errlen);
   return MGP_OK;
 }
 
@@ -1014,6 +1237,11 @@ void mgp_cosmo_free(mgp_cosmo *c) {
   if (c->sd)
     for (int f = 0; f < 6; f++) bicubic_free(&c->sd_tab[f]);
   c->sd = 0;
+  if (c->sd_lcdm.nx) bicubic_free(&c->sd_lcdm);
+  for (int q = 0; q < 4; q++)
+    if (c->nuT[q].nx) bicubic_free(&c->nuT[q]);
+  free(c->nu_rows0);
+  c->nu_rows0 = NULL;
   free(c->tab_logk);
   free(c->tab_logv);
   c->tab_logk = c->tab_logv = NULL;
@@ -1023,6 +1251,7 @@ void mgp_cosmo_free(mgp_cosmo *c) {
  * which 0-6 as mgp_growth, 7 the linear power spectrum P(x) (x = k in h/Mpc).
  * Sq/Sphi are available through mgp_cosmo_coeff. */
 int mgp_cosmo_eval(const mgp_params *p, int which, const double *x, int n, double *out) {
+  if (which < 0 || which > 9) return mgp_set_error(MGP_EINVAL, "which = %d out of range", which);
   char err[512] = "";
   mgp_cosmo c;
   int rc = mgp_cosmo_init(&c, p, err, sizeof(err));
@@ -1030,7 +1259,14 @@ int mgp_cosmo_eval(const mgp_params *p, int which, const double *x, int n, doubl
     mgp_cosmo_free(&c);
     return mgp_set_error(rc, "%s", err);
   }
-  for (int i = 0; i < n; i++) out[i] = which == 7 ? mgp_cosmo_power(&c, x[i]) : mgp_cosmo_growth(&c, which, x[i]);
+  for (int i = 0; i < n; i++) {
+    switch (which) {
+      case 7: out[i] = mgp_cosmo_power(&c, x[i]); break;
+      case 8: out[i] = mgp_cosmo_pofk_ratio(&c, x[i], 1.0); break;
+      case 9: out[i] = mgp_cosmo_sigma8_enh(&c, x[i]); break;
+      default: out[i] = mgp_cosmo_growth(&c, which, x[i]);
+    }
+  }
   mgp_cosmo_free(&c);
   return MGP_OK;
 }
@@ -1064,4 +1300,27 @@ int mgp_cosmo_coeff(const mgp_params *p, int kind, const double *ai, const doubl
     out[i] = kind == 0 ? mgp_cosmo_Sq(&c, ai[i], af[i], aref[i]) : mgp_cosmo_Sphi(&c, ai[i], af[i], aref[i]);
   mgp_cosmo_free(&c);
   return MGP_OK;
+}
+
+/* The neutrino term of the density at scale factor a (src/auxPM.c:383-428)
+ * per integer |k|^2 (k = 2 pi/Box sqrt(rk)): Omega_nu/Omega N^3
+ * T_nu(k, a) / T_cb(k, 1); out[0] unused.  Returns (Omega - Omega_nu)/Omega,
+ * the factor of the CDM density, or 1 without neutrinos. */
+void mgp_cosmo_nu_den(const mgp_cosmo *c, int N, int nrk, double *den) {
+  (void)N;
+  const nu_rows o1 = {c->nuT[0].nx, c->nu_rows0};
+  den[0] = 1.0;
+  for (int rk = 1; rk < nrk; rk++) den[rk] = nu_Tcb(c, &o1, 2.0 * M_PI / c->p.Box * sqrt((double)rk), c->OmegaCDM);
+}
+
+double mgp_cosmo_nu_table(const mgp_cosmo *c, double a, int N, int nrk, const double *den, double *out) {
+  if (!c->nu) return 1.0;
+  double *buf = (double *)malloc(sizeof(double) * 8 * c->nuT[0].nx);
+  nu_rows o = {0, buf};
+  nu_rows_at(c, a, &o);
+  const double fac = c->OmegaNu / c->p.Omega * (double)N * (double)N * (double)N;
+  out[0] = 0.0;
+  for (int rk = 1; rk < nrk; rk++) out[rk] = fac * nu_T(c, &o, 0, 2.0 * M_PI / c->p.Box * sqrt((double)rk)) / den[rk];
+  free(buf);
+  return (c->p.Omega - c->OmegaNu) / c->p.Omega;
 }

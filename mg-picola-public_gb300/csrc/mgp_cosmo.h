@@ -37,6 +37,16 @@ typedef struct mgp_cosmo {
    * dD2dy, ddD2ddy over (ln a, ln k) */
   int sd;
   mgp_bicubic sd_tab[6];
+  /* massive neutrinos (MASSIVE_NEUTRINOS build): Omega_nu, Omega_cdm
+   * (user_defined_functions.h:59-66); CAMB transfer functions over
+   * (ln k, z) for nu, cdm, baryon, total (read_CAMB_data.h:41-170); the
+   * LCDM growth D(k, a) with the neutrino factor (cosmo.c:829-884) */
+  int nu;          /* neutrino density added to delta(k) every step */
+  int nu_growth;   /* neutrino factors in the growth equations */
+  double OmegaNu, OmegaCDM;
+  mgp_bicubic nuT[4];
+  double *nu_rows0;   /* the four transfer functions at z = 0 as rows over ln k */
+  mgp_bicubic sd_lcdm;
   /* power spectrum */
   double norm;
   int ntab;
@@ -44,6 +54,13 @@ typedef struct mgp_cosmo {
 } mgp_cosmo;
 
 int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen);
+/* Massive-neutrino density factors per integer |k|^2 = rk of an N^3 mesh
+ * (src/auxPM.c:383-421): mgp_cosmo_nu_den fills den[rk] = T_cb(k, 1), the
+ * step-independent denominators; mgp_cosmo_nu_table fills out[rk] =
+ * OmegaNu/Omega N^3 T_nu(k, a) / den[rk] (out[0] = 0) and returns cdmfac =
+ * (Omega - OmegaNu) / Omega. */
+void mgp_cosmo_nu_den(const mgp_cosmo *c, int N, int nrk, double *den);
+double mgp_cosmo_nu_table(const mgp_cosmo *c, double a, int N, int nrk, const double *den, double *out);
 void mgp_cosmo_free(mgp_cosmo *c);
 
 /* hooks, src/user_defined_functions.h:413-904 */

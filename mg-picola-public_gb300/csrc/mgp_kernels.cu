@@ -837,6 +837,34 @@ int mgp_launch_ic_delta(const uint32_t *seedtable, const double *amp_rk, const u
   return MGP_OK;
 }
 
+// Massive neutrinos in the density (src/auxPM.c:383-428): delta(k) <-
+// cdmfac delta(k) + nufac[|k|^2] delta_IC(k) with delta_IC the stored linear
+// CDM+baryon field of the IC (cdelta_cdm); the k = 0 mode is left as it is.
+__global__ void k_nu_add(float2 *__restrict__ dk, const float2 *__restrict__ dk0, int N, double cdmfac,
+                         const double *__restrict__ nufac) {
+  const int NH = N / 2 + 1;
+  const long long n = (long long)N * N * NH;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+    if (q == 0) continue;
+    const int kz = (int)(q % NH);
+    const long long r = q / NH;
+    const int j = (int)(r % N), i = (int)(r / N);
+    const int di = i > N / 2 ? N - i : i, dj = j > N / 2 ? N - j : j;
+    const double f = nufac[(long long)di * di + (long long)dj * dj + (long long)kz * kz];
+    const float2 a = dk[q], b = dk0[q];
+    dk[q] = make_float2((float)(cdmfac * a.x + f * b.x), (float)(cdmfac * a.y + f * b.y));
+  }
+}
+
+int mgp_launch_nu_add(float *dk, const float *dk0, int N, double cdmfac, const double *nufac, cudaStream_t st) {
+  const long long n = (long long)N * N * (N / 2 + 1);
+  k_nu_add<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>((float2 *)dk, (const float2 *)dk0, N, cdmfac, nufac);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
 // ProcessParticlesSingleFile (src/readICfromfile.c:133-219): CIC of particles
 // at positions in [0,1) of the box (FP64, [n][3]) onto a density grid pre-set
 // to -1, with WPAR = (N/Ns)^3 folded into the y factors; a cell index that

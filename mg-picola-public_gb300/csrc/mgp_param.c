@@ -148,10 +148,13 @@ int mgp_read_parameterfile(const char *fname, int model, int pofk_keys, int read
   int nt = 0;
   g_perr[0] = 0;
   if (!fname || !p) return MGP_EINVAL;
-  int use_w0wa = p->use_w0wa, readic = p->ReadParticlesFromFile;
+  int use_w0wa = p->use_w0wa, readic = p->ReadParticlesFromFile, mnu = p->massive_neutrinos;
+  int sdep = p->scaledependent;
   mgp_params_default(p);
   p->model = model;
   p->use_w0wa = use_w0wa;
+  p->massive_neutrinos = mnu;
+  p->scaledependent = sdep;
   if (readic) {
     /* src/read_param.c:129-151 (READICFROMFILE) */
     ADD("ReadParticlesFromFile", ReadParticlesFromFile, T_INT);
@@ -170,6 +173,12 @@ int mgp_read_parameterfile(const char *fname, int model, int pofk_keys, int read
   ADD("inverted_initial_condition", inverted_initial_condition, T_INT);
   ADD("amplitude_fixed_initial_condition", amplitude_fixed_initial_condition, T_INT);
   ADD("include_screening", include_screening, T_INT);
+  if (mnu) {
+    /* read_mg_parameters, user_defined_functions.h:261-273 (MASSIVE_NEUTRINOS) */
+    ADD("nu_include_massive_neutrinos", nu_include_massive_neutrinos, T_INT);
+    ADD("nu_SumMassNuEV", nu_SumMassNuEV, T_FLOAT);
+    ADD("nu_FilenameTransferInfofile", nu_FilenameTransferInfofile, T_STRING);
+  }
   if (pofk_keys) {
     ADD("pofk_compute_every_step", pofk_compute_every_step, T_INT);
     ADD("pofk_compute_rsd_pofk", pofk_compute_rsd_pofk, T_INT);

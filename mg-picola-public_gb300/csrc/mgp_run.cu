@@ -184,7 +184,7 @@ static int write_rsd_now(mgp_ctx *c, double A) {
 static int write_pofk_now(mgp_ctx *c, double A, const char *label) {
   int nb = c->pk_nbins;
   std::vector<double> k(nb), pk(nb), km(nb), n(nb);
-  RET_IF(mgp_pofk(c, nb, &nb, k.data(), pk.data(), km.data(), n.data()));
+  RET_IF((strcmp(label, "total") ? mgp_pofk : mgp_pofk_total)(c, nb, &nb, k.data(), pk.data(), km.data(), n.data()));
   return mgp_write_pofk(&c->p, A, label, nb, k.data(), pk.data(), km.data(), n.data());
 }
 
@@ -225,7 +225,10 @@ static int run_loop(mgp_ctx *c, int gadget) {
       // RSD every step except at outputs (src/compute_pofk.c call in auxPM.c:376-381)
       if (c->p.pofk_compute_rsd_pofk == 1 && !output_step) RET_IF(write_rsd_now(c, A));
       RET_IF(mgp_get_displacements(c, A));
-      if (p->pofk_compute_every_step) RET_IF(write_pofk_now(c, A, "CDM"));
+      if (p->pofk_compute_every_step) {
+        RET_IF(write_pofk_now(c, A, "CDM"));
+        if (c->cosmo.nu) RET_IF(write_pofk_now(c, A, "total"));  // src/auxPM.c:423-426
+      }
       if (c->sd) {
         // scale-dependent fields of this step (main.c:487-503)
         const int types[2] = {MGP_FIELD_ddDddy, MGP_FIELD_deltaD};

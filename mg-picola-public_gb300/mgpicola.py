@@ -20,7 +20,7 @@ FILTER_NONE, FILTER_GAUSSIAN, FILTER_TOPHAT, FILTER_SHARPK = 0, 1, 2, 3
 EXPORTS = [
     "mgp_params_default", "mgp_read_parameterfile", "mgp_create", "mgp_destroy", "mgp_last_error",
     "mgp_displacement_fields", "mgp_get_displacements", "mgp_kick_drift", "mgp_step", "mgp_run", "mgp_pofk",
-    "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
+    "mgp_pofk_total", "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
     "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_launch_count",
     "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
@@ -69,6 +69,8 @@ class Params(C.Structure):
         ("ReadParticlesFromFile", C.c_int), ("NumInputParticleFiles", C.c_int), ("RamsesOutputNumber", C.c_int),
         ("TypeInputParticleFiles", C.c_int), ("InputParticleFileDir", C.c_char * 500),
         ("InputParticleFilePrefix", C.c_char * 500),
+        ("massive_neutrinos", C.c_int), ("nu_include_massive_neutrinos", C.c_int), ("nu_SumMassNuEV", C.c_double),
+        ("nu_FilenameTransferInfofile", C.c_char * 500),
     ]
 
 
@@ -108,6 +110,7 @@ def lib():
         L.mgp_run.argtypes = [vp, C.c_int]
         dp = C.POINTER(C.c_double)
         L.mgp_pofk.argtypes = [vp, C.c_int, C.POINTER(C.c_int), dp, dp, dp, dp]
+        L.mgp_pofk_total.argtypes = [vp, C.c_int, C.POINTER(C.c_int), dp, dp, dp, dp]
         L.mgp_pofk_rsd.argtypes = [vp, C.c_double, C.c_int, C.POINTER(C.c_int)] + [dp] * 8
         L.mgp_get_particles.argtypes = [vp, vp, vp, vp, vp, C.c_size_t]
         L.mgp_set_particles.argtypes = [vp, vp, vp, vp, vp, C.c_size_t]
@@ -195,12 +198,16 @@ def default_params(**kw):
 
 
 def read_parameterfile(fname, model=MODEL_LCDM, pofk_keys=True, read_outputs=True, use_w0wa=False,
-                       read_ic_from_file=False):
+                       read_ic_from_file=False, massive_neutrinos=False):
     """read_parameterfile + read_outputs of the reference (read_ic_from_file:
-    the READICFROMFILE build's six keys are required)."""
+    the READICFROMFILE build's six keys are required; massive_neutrinos: the
+    MASSIVE_NEUTRINOS build, which is also scale dependent, with its three
+    nu_* keys)."""
     p = Params()
     p.use_w0wa = 1 if use_w0wa else 0
     p.ReadParticlesFromFile = 1 if read_ic_from_file else 0
+    if massive_neutrinos:
+        p.massive_neutrinos = p.scaledependent = 1
     _check(lib().mgp_read_parameterfile(fname.encode(), model, 1 if pofk_keys else 0, 1 if read_outputs else 0,
                                         C.byref(p)))
     return p
@@ -223,7 +230,8 @@ def read_particle_files(params):
 
 
 def cosmo_eval(params, which, x):
-    """Host-only growth factors (which 0-6) or P(k) (which 7)."""
+    """Host-only growth factors (which 0-6), P(k) (which 7), mg_pofk_ratio(k,
+    a = 1) (which 8) or the sigma8 enhancement at a (which 9)."""
     x = np.ascontiguousarray(x, dtype=np.float64)
     out = np.zeros_like(x)
     _check(lib().mgp_cosmo_eval(C.byref(params), which, _dptr(x), x.size, _dptr(out)))
@@ -328,11 +336,14 @@ class Context:
         _check(lib().mgp_output_stats(self.h, C.byref(n), C.byref(w), C.byref(f), C.byref(b)))
         return n.value, w.value, f.value, b.value
 
-    def pofk(self):
+    def pofk(self, total=False):
+        """P(k) of the last density: k, P, mean |k|, mode count.  total=True
+        gives the total matter spectrum of a run with massive neutrinos."""
         cap = max(self.params.pofk_nbins, self.N, 1)
         k, pk, km, n = (np.zeros(cap) for _ in range(4))
         nb = C.c_int(0)
-        _check(lib().mgp_pofk(self.h, cap, C.byref(nb), _dptr(k), _dptr(pk), _dptr(km), _dptr(n)))
+        fn = lib().mgp_pofk_total if total else lib().mgp_pofk
+        _check(fn(self.h, cap, C.byref(nb), _dptr(k), _dptr(pk), _dptr(km), _dptr(n)))
         m = nb.value
         return k[:m], pk[:m], km[:m], n[:m]
 

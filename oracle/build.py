@@ -10,7 +10,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SOURCES = ["orc_fft.c", "orc_pm.c", "orc_cosmo.c", "orc_rng.c", "orc_mg.c", "orc_ic.c", "orc_run.c", "orc_interp2d.c",
-           "orc_sd.c"]
+           "orc_sd.c", "orc_nu.c"]
 OUT_DIR = os.path.join(HERE, "build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 

@@ -26,14 +26,14 @@ class MG(C.Structure):
                 ("beta_symm", C.c_double), ("assb_symm", C.c_double), ("range_symm", C.c_double),
                 ("smoothing_filter", C.c_int), ("wBD", C.c_double), ("Omegah2", C.c_double),
                 ("Omegarh2", C.c_double), ("Omegavh2", C.c_double), ("scaledependent", C.c_int),
-                ("sd_nk", C.c_int), ("sd_kmin", C.c_double), ("sd_kmax", C.c_double)]
+                ("sd_nk", C.c_int), ("sd_kmin", C.c_double), ("sd_kmax", C.c_double), ("nu", C.c_void_p)]
 
 
 class Power(C.Structure):
     _fields_ = [("which_spectrum", C.c_int), ("omega", C.c_double), ("omega_b", C.c_double),
                 ("h", C.c_double), ("ns", C.c_double), ("sigma8", C.c_double), ("ntab", C.c_int),
                 ("tab_logk", C.POINTER(C.c_double)), ("tab_logP", C.POINTER(C.c_double)),
-                ("norm", C.c_double)]
+                ("norm", C.c_double), ("nu", C.c_void_p), ("nu_ocdm", C.c_double)]
 
 
 class ICParams(C.Structure):
@@ -136,6 +136,21 @@ def lib():
         L.orc_run.restype = C.c_int
         L.orc_time_steps.argtypes = [C.POINTER(RunParams), C.c_int]
         L.orc_time_steps.restype = C.c_double
+        L.orc_nu_create.argtypes = [C.c_char_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+        L.orc_nu_create.restype = C.c_void_p
+        L.orc_nu_free.argtypes = [C.c_void_p]
+        for name in ["orc_nu_omega_nu", "orc_nu_omega_cdm", "orc_nu_mu2"]:
+            getattr(L, name).argtypes = [C.c_void_p]
+            getattr(L, name).restype = C.c_double
+        L.orc_nu_transfer.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double]
+        L.orc_nu_transfer.restype = C.c_double
+        L.orc_nu_Tcb.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
+        L.orc_nu_Tcb.restype = C.c_double
+        L.orc_nu_mu1.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        L.orc_nu_mu1.restype = C.c_double
+        L.orc_nu_pofk_cb.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        L.orc_nu_pofk_cb.restype = C.c_double
+        L.orc_nu_add_density.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_double, dptr, dptr]
         _lib = L
     return _lib
 
@@ -237,6 +252,9 @@ def make_mg(model=LCDM, omega=0.267, **kw):
     m.sd_nk = kw.get("sd_nk", 0)
     m.sd_kmin = kw.get("sd_kmin", 0.0)
     m.sd_kmax = kw.get("sd_kmax", 0.0)
+    if kw.get("nu") is not None:
+        m.nu = kw["nu"].h
+        m._nu_keep = kw["nu"]
     if model == JBD_GEFF:
         lib().orc_jbd_solve(C.byref(m))
     if model == MBETA and m.mg_active:
@@ -244,13 +262,54 @@ def make_mg(model=LCDM, omega=0.267, **kw):
     return m
 
 
-def make_power(omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sigma8=0.8, which=2):
+def make_power(omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sigma8=0.8, which=2, nu=None):
+    """nu: a Neutrinos object (the CDM+baryon spectrum of its CAMB tables)."""
     p = Power()
     p.which_spectrum = which
     p.omega, p.omega_b, p.h, p.ns, p.sigma8 = omega, omega_b, h, ns, sigma8
     p.ntab = 0
+    if nu is not None:
+        p.nu = nu.h
+        p._nu_keep = nu
     lib().orc_power_init(C.byref(p))
     return p
+
+
+class Neutrinos:
+    """CAMB transfer tables and Omega's of the massive-neutrino build
+    (orc_nu.c).  Attach to make_mg(nu=...) / make_power(nu=...)."""
+
+    TNU, TCDM, TB, TTOT = 0, 1, 2, 3
+
+    def __init__(self, infofile, omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sum_mnu_ev=0.3, include=1):
+        self.h = lib().orc_nu_create(str(infofile).encode(), omega, omega_b, h, ns, sum_mnu_ev, include)
+        if not self.h:
+            raise OSError("cannot read the transfer tables of %s" % infofile)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_nu_free(self.h)
+            self.h = None
+
+    @property
+    def omega_nu(self):
+        return lib().orc_nu_omega_nu(self.h)
+
+    @property
+    def omega_cdm(self):
+        return lib().orc_nu_omega_cdm(self.h)
+
+    def transfer(self, which, k, a):
+        return lib().orc_nu_transfer(self.h, which, k, a)
+
+    def mu1(self, a, k):
+        return lib().orc_nu_mu1(self.h, a, k)
+
+    def mu2(self):
+        return lib().orc_nu_mu2(self.h)
+
+    def add_density(self, a, N, box, grid, cdelta):
+        lib().orc_nu_add_density(self.h, a, N, box, grid, np.ascontiguousarray(cdelta))
 
 
 def ic_2lpt(N, Ns, box, seed, pw, fixed=0, inverted=0, sphere=0, rescale=1.0, want_k=False):

@@ -108,6 +108,8 @@ typedef struct {
   int scaledependent;
   int sd_nk;
   double sd_kmin, sd_kmax;
+  /* MASSIVE_NEUTRINOS build: transfer tables and Omega's (orc_nu.c), or NULL */
+  const struct orc_nu_s *nu;
 } orc_mg;
 
 /* Brans-Dicke background (src/jbd.c) and the m(a), beta(a) phi_crit(a)
@@ -149,6 +151,25 @@ void orc_bicubic_init(orc_bicubic *b, const double *x, const double *y, const do
 double orc_bicubic_eval(const orc_bicubic *b, double x, double y);
 void orc_bicubic_free(orc_bicubic *b);
 
+/* ------------------------------------------------- massive neutrinos */
+/* orc_nu.c: CAMB transfer tables over (ln k, z) read from the info file
+ * (src/read_CAMB_data.h), OmegaNu = sum m_nu / (93.14 h^2) and OmegaCDM as
+ * init_modified_version sets them, the growth-equation factors, the CDM+
+ * baryon P(k) and the per-step k-space density add.  which: 0 massive nu,
+ * 1 CDM, 2 baryon, 3 total. */
+typedef struct orc_nu_s orc_nu;
+orc_nu *orc_nu_create(const char *infofile, double omega, double omega_b, double h, double ns, double sum_mnu_ev,
+                      int include);
+void orc_nu_free(orc_nu *nu);
+double orc_nu_omega_nu(const orc_nu *nu);
+double orc_nu_omega_cdm(const orc_nu *nu);
+double orc_nu_transfer(const orc_nu *nu, int which, double k, double a);
+double orc_nu_Tcb(const orc_nu *nu, double k, double a, double omega_cdm);
+double orc_nu_mu1(const orc_nu *nu, double a, double k);
+double orc_nu_mu2(const orc_nu *nu);
+double orc_nu_pofk_cb(const orc_nu *nu, double k, double omega_cdm);
+void orc_nu_add_density(const orc_nu *nu, double a, int N, double box, double *grid, const double *cdelta);
+
 /* ----------------------------------------------------------- cosmology */
 struct orc_power_s;
 typedef struct orc_cosmo orc_cosmo;
@@ -186,6 +207,10 @@ typedef struct orc_power_s {
   double omega, omega_b, h, ns, sigma8;
   int ntab; const double *tab_logk, *tab_logP;   /* log10 table for type 1 */
   double norm;              /* filled by orc_power_init */
+  /* MASSIVE_NEUTRINOS build: the CDM+baryon spectrum of the CAMB tables,
+   * with the OmegaCDM it is evaluated at (orc_power_init sets it) */
+  const struct orc_nu_s *nu;
+  double nu_ocdm;
 } orc_power;
 void orc_power_init(orc_power *p);
 double orc_power_spec(const orc_power *p, double k);

@@ -271,6 +271,9 @@ struct orc_cosmo {
   /* SCALEDEPENDENT: D, dDdy, ddDddy, D2, dD2dy, ddD2ddy over (ln a, ln k) */
   int sd;
   orc_bicubic tab[6];
+  /* massive neutrinos: the LCDM D(k, a) of the same build (cosmo.c:829-884) */
+  int sd_lcdm;
+  orc_bicubic tab_lcdm;
 };
 
 /* ode_growth_D (cosmo.c:206-239); lcdm = 1 gives ode_growth_DLCDM
@@ -292,10 +295,13 @@ static void growth_rhs(const orc_mg *m, int lcdm, double k, double x, const doub
     else
       modfac = orc_factor_2lpt(m, a);
   }
+  /* massive neutrinos (cosmo.c:224-236, 253-265): mu_nu multiplies the
+   * source terms */
+  double mu1 = orc_nu_mu1(m->nu, a, k), mu2 = orc_nu_mu2(m->nu);
   dD[0] = D[1];
-  dD[1] = -alphafac * D[1] + betafac * D[0];
+  dD[1] = -alphafac * D[1] + betafac * mu1 * D[0];
   dD[2] = D[3];
-  dD[3] = -alphafac * D[3] + betafac * (D[2] - modfac * D[0] * D[0]);
+  dD[3] = -alphafac * D[3] + betafac * mu2 * (D[2] - modfac * D[0] * D[0]);
 }
 
 static void rk4(const orc_mg *m, int lcdm, double k, double x0, double x1, int nsub, double *y) {
@@ -337,11 +343,29 @@ static void solve_sd(orc_cosmo *c, double xini, double xend, int npts, double bo
       size_t c0 = (size_t)ik * npts + i;
       T[0][c0] = y[0];
       T[1][c0] = y[1] * Qfactor(m, anow) / anow;
-      T[2][c0] = 1.5 * mu * m->omega * anow * y[0];
+      const double mu1 = orc_nu_mu1(m->nu, anow, know), mu2 = orc_nu_mu2(m->nu);
+      T[2][c0] = 1.5 * mu * mu1 * m->omega * anow * y[0];
       T[3][c0] = y[2];
       T[4][c0] = y[3] * Qfactor(m, anow) / anow;
-      T[5][c0] = 1.5 * mu * m->omega * anow * (y[2] - y[0] * y[0]);
+      T[5][c0] = 1.5 * mu * mu2 * m->omega * anow * (y[2] - y[0] * y[0]);
     }
+  }
+  if (m->nu) {
+    /* the LCDM growth per k with the neutrino factors (gravity switched off:
+     * mu = 1 and no second-order kernel); only D is looked up later */
+    double *L = malloc(sizeof(double) * npts * nk);
+#pragma omp parallel for schedule(dynamic)
+    for (int ik = 0; ik < nk; ik++) {
+      double know = exp(log(kmin) + log(kmax / kmin) * ik / (double)(nk - 1));
+      double y[4] = {1.0, 1.0, -3.0 / 7.0, -6.0 / 7.0};
+      for (int i = 0; i < npts; i++) {
+        if (i > 0) rk4(m, 1, know, x[i - 1], x[i], 16, y);
+        L[(size_t)ik * npts + i] = y[0];
+      }
+    }
+    orc_bicubic_init(&c->tab_lcdm, x, logk, L, npts, nk);
+    free(L);
+    c->sd_lcdm = 1;
   }
   for (int f = 0; f < 6; f++) {
     orc_bicubic_init(&c->tab[f], x, logk, T[f], npts, nk);
@@ -405,6 +429,7 @@ void orc_cosmo_free(orc_cosmo *c) {
   spline_free(&c->D2); spline_free(&c->dD2dy); spline_free(&c->ddD2ddy); spline_free(&c->DLCDM);
   if (c->sd)
     for (int f = 0; f < 6; f++) orc_bicubic_free(&c->tab[f]);
+  if (c->sd_lcdm) orc_bicubic_free(&c->tab_lcdm);
   free(c);
 }
 /* growth_*_scaledependent (cosmo.c:987-1010) */
@@ -415,6 +440,10 @@ double orc_growth_sd(orc_cosmo *c, int which, double k, double a) {
 /* mg_pofk_ratio (cosmo.c:688-706), no massive neutrinos */
 double orc_mg_pofk_ratio(orc_cosmo *c, double k, double a) {
   if (!c->m.mg_active) return 1.0;
+  if (c->sd_lcdm) {  /* cosmo.c:692-695 */
+    double q = lookup2d(&c->tab[0], log(a), log(k)) / lookup2d(&c->tab_lcdm, log(a), log(k));
+    return q * q;
+  }
   double r = c->sd ? lookup2d(&c->tab[0], log(a), log(k)) / spline_eval(&c->DLCDM, log(a))
                    : spline_eval(&c->D, log(a)) / spline_eval(&c->DLCDM, log(a));
   return r * r;
@@ -431,7 +460,7 @@ double orc_mg_sigma8_enh(orc_cosmo *c, const struct orc_power_s *pw, double a) {
     double kR8 = know * 8.0;
     double w = 3.0 / (kR8 * kR8 * kR8) * (sin(kR8) - kR8 * cos(kR8));
     double D = lookup2d(&c->tab[0], log(a), log(know));
-    double DL = spline_eval(&c->DLCDM, log(a));
+    double DL = c->sd_lcdm ? lookup2d(&c->tab_lcdm, log(a), log(know)) : spline_eval(&c->DLCDM, log(a));
     double power = orc_power_spec((const orc_power *)pw, know);
     s += power * w * w * D * D * know * know * know * dlogk / (2.0 * M_PI * M_PI);
     sl += power * w * w * DL * DL * know * know * know * dlogk / (2.0 * M_PI * M_PI);
@@ -554,6 +583,7 @@ static double pk_tab(const orc_power *p, double k) {
 }
 /* PowerSpec, src/power.c:373-394 */
 double orc_power_spec(const orc_power *p, double k) {
+  if (p->nu) return p->norm * orc_nu_pofk_cb(p->nu, k, p->nu_ocdm);  /* power.c:376-380 */
   if (p->which_spectrum == 1) return pk_tab(p, k);
   double T = orc_transfer_eh(p, k);
   return p->norm * pow(k, p->ns) * T * T;
@@ -579,8 +609,13 @@ double orc_tophat_sigma2(const orc_power *p, double R) {
 /* initialize_powerspectrum, src/power.c:226-257 */
 void orc_power_init(orc_power *p) {
   p->norm = 1.0;
+  /* with massive neutrinos the normalisation runs before
+   * init_modified_version has set OmegaCDM (main.c:153-162), so the
+   * CDM+baryon transfer function is the baryon one there */
+  p->nu_ocdm = 0.0;
   double res = orc_tophat_sigma2(p, 8.0);
   p->norm = p->sigma8 * p->sigma8 / res;
+  if (p->nu) p->nu_ocdm = orc_nu_omega_cdm(p->nu);
 }
 
 /* ------------------------------------------------------------ splines */

@@ -79,6 +79,14 @@ int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
       nb = rp->pofk_nbins;
       orc_pofk(grid, N, Ns, Box, &nb, rp->pofk_bintype, rp->pofk_subtract_shotnoise, rp->pofk_kmin,
                rp->pofk_kmax, kbin, pk, kmean, nmodes);
+      if (sd && rp->mg.nu) {
+        /* massive neutrinos (auxPM.c:383-426): the outputs then hold the
+         * total matter P(k) */
+        orc_nu_add_density(rp->mg.nu, A, N, Box, grid, cdelta);
+        nb = rp->pofk_nbins;
+        orc_pofk(grid, N, Ns, Box, &nb, rp->pofk_bintype, rp->pofk_subtract_shotnoise, rp->pofk_kmin,
+                 rp->pofk_kmax, kbin, pk, kmean, nmodes);
+      }
       if (rp->mg.mg_active) orc_fifth_force(&rp->mg, A, N, Box, dens_x, grid, mgk);
       orc_forces_kspace(grid, uses_mgk ? mgk : NULL, N, Box, f[0], f[1], f[2]);
       for (int a = 0; a < 3; a++) orc_fft_c2r(N, f[a]);

@@ -29,6 +29,7 @@ MODELS = {
     "MBETA_LCDM": ["-DMBETAMODEL"],
     "FOFR": ["-DFOFRGRAVITY", "-DSCALEDEPENDENT"],
     "MBETA": ["-DMBETAMODEL", "-DSCALEDEPENDENT"],
+    "FOFRNU": ["-DFOFRGRAVITY", "-DMASSIVE_NEUTRINOS", "-DSCALEDEPENDENT"],
 }
 
 

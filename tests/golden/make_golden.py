@@ -20,6 +20,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 from oracle import ref_build  # noqa: E402
+from tests.golden import camb_tables  # noqa: E402
 
 BASE = dict(Nmesh=32, Nsample=16, Box=128.0, Init_Redshift=19.0, Seed=4242, nsteps=5)
 
@@ -39,6 +40,12 @@ CASES = {
     "fofr_sd": ("FOFR", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1)),
     "mbeta_sd": ("MBETA", dict(modified_gravity_active=1, range_symm=1.0, assb_symm=0.5, beta_symm=1.0,
                                include_screening=1)),
+    # MASSIVE_NEUTRINOS build (scale dependent) on the synthetic CAMB tables
+    # of camb_tables.py: P(k) of CDM+baryons and of the total matter field
+    "lcdm_nu": ("FOFRNU", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1,
+                               nu_include_massive_neutrinos=1, nu_SumMassNuEV=camb_tables.SUM_MNU_EV)),
+    "fofr_nu": ("FOFRNU", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1,
+                               nu_include_massive_neutrinos=1, nu_SumMassNuEV=camb_tables.SUM_MNU_EV)),
 }
 
 STD = """use_lcdm_growth_factors  0
@@ -86,6 +93,8 @@ def run_case(name, model, mg):
         mgd = dict(inverted_initial_condition=0, amplitude_fixed_initial_condition=0)
         mgd.update(mg)
         txt = STD.format(out=d, **BASE) + "".join("%s %s\n" % kv for kv in mgd.items())
+        if "nu_SumMassNuEV" in mg:
+            txt += "nu_FilenameTransferInfofile %s\n" % camb_tables.write_tables(os.path.join(d, "camb"))
         pf = os.path.join(d, "params.txt")
         with open(pf, "w") as f:
             f.write(txt)
@@ -98,8 +107,11 @@ def run_case(name, model, mg):
         pos = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3)
         vel = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3)
         idx = np.arange(0, n, 8)
+        extra = {}
+        if "nu_SumMassNuEV" in mg:
+            extra["pk_total"] = np.loadtxt(os.path.join(d, "pofk_run_z0.000_total.txt"))
         np.savez(os.path.join(ROOT, "tests", "golden", "ref_%s.npz" % name), pk=pk, idx=idx, pos=pos[idx],
-                 vel=vel[idx], model=model, **{k: float(v) for k, v in mgd.items()}, **BASE)
+                 vel=vel[idx], model=model, **{k: float(v) for k, v in mgd.items()}, **BASE, **extra)
         print(name, "bins", pk.shape[0])
 
 

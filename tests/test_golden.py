@@ -12,12 +12,19 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from golden import camb_tables
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_*.npz")))
 
 
-def oracle_run(g):
+def oracle_run(g, tmpdir=None):
     model = str(g["model"])
+    nu = None
+    if model == "FOFRNU":
+        # the synthetic CAMB tables the fixture was made with
+        info = camb_tables.write_tables(os.path.join(str(tmpdir), "camb"))
+        nu = O.Neutrinos(info, 0.267, 0.049, 0.71, 0.96, float(g["nu_SumMassNuEV"]),
+                         int(g["nu_include_massive_neutrinos"]))
     active = int(g["modified_gravity_active"])
     scr = int(g["include_screening"])
     if model == "DGP":
@@ -32,11 +39,11 @@ def oracle_run(g):
                        scaledependent=int(model == "MBETA"))
     else:
         mg = O.make_mg(O.FOFR, 0.267, mg_active=active, include_screening=scr, fofr0=float(g["fofr0"]),
-                       nfofr=float(g["nfofr"]), scaledependent=int(model == "FOFR"))
+                       nfofr=float(g["nfofr"]), scaledependent=int(model in ("FOFR", "FOFRNU")), nu=nu)
     N, Ns, box = int(g["Nmesh"]), int(g["Nsample"]), float(g["Box"])
     rp = O.RunParams()
     rp.mg = mg
-    rp.pw = O.make_power(omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sigma8=0.8)
+    rp.pw = O.make_power(omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sigma8=0.8, nu=nu)
     if model == "BRANSDICKE":
         # normalised with the file's Omega/h, evaluated with the background's
         rp.pw.omega, rp.pw.h = mg.omega, float(np.sqrt(mg.Omegah2 / mg.omega))
@@ -52,17 +59,18 @@ def oracle_run(g):
     pos, vel = np.zeros((n, 3)), np.zeros((n, 3))
     kb, pk, km, nm = (np.zeros(N) for _ in range(4))
     nb = O.lib().orc_run(rp, pos, vel, kb, pk, km, nm)
-    h = 0.71 if model != "BRANSDICKE" else float(np.sqrt(mg.Omegah2 / mg.omega))
+    del nu  # the tables stay alive through rp.mg / rp.pw until here
     return (kb[:nb], pk[:nb], km[:nb], nm[:nb]), pos, vel, box
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[4:-4] for p in GOLDEN])
-def test_oracle_matches_reference_run(path):
+def test_oracle_matches_reference_run(path, tmp_path):
     g = np.load(path)
-    (kb, pk, km, nm), pos, vel, box = oracle_run(g)
+    (kb, pk, km, nm), pos, vel, box = oracle_run(g, tmp_path)
     m = nm > 0
     m[0] = False  # the reference writes bins from 1 (compute_pofk.c:251)
-    ref = g["pk"]
+    # with massive neutrinos the oracle's P(k) is the total matter one
+    ref = g["pk_total"] if "pk_total" in g else g["pk"]
     assert ref.shape[0] == m.sum()
     np.testing.assert_allclose(kb[m], ref[:, 0], atol=6e-6)
     np.testing.assert_allclose(pk[m], ref[:, 1], rtol=1e-6, atol=6e-6)
