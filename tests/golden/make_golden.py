@@ -23,6 +23,7 @@ from oracle import ref_build  # noqa: E402
 from tests.golden import camb_tables  # noqa: E402
 
 BASE = dict(Nmesh=32, Nsample=16, Box=128.0, Init_Redshift=19.0, Seed=4242, nsteps=5)
+COSMO = dict(Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96)
 
 CASES = {
     # case: (binary model, MG keys)
@@ -74,11 +75,11 @@ WhichSpectrum    2
 WhichTransfer    0
 FileWithInputSpectrum  none
 FileWithInputTransfer  none
-Omega            0.267
-OmegaBaryon      0.049
-HubbleParam      0.71
-Sigma8           0.8
-PrimordialIndex  0.96
+Omega            {Omega}
+OmegaBaryon      {OmegaBaryon}
+HubbleParam      {HubbleParam}
+Sigma8           {Sigma8}
+PrimordialIndex  {PrimordialIndex}
 UnitLength_in_cm                3.085678e24
 UnitMass_in_g                   1.989e43
 UnitVelocity_in_cm_per_s        1e5
@@ -86,34 +87,46 @@ InputSpectrum_UnitLength_in_cm  3.085678e24
 """
 
 
-def run_case(name, model, mg):
+def run_reference(model, mg, base=None, cosmo=None, nu_info=None):
+    """Run the reference binary of `model` on one small case; returns the
+    final CDM P(k) table, the total one (neutrino builds) and the snapshot's
+    positions and velocities.  nu_info: the CAMB info file of a neutrino
+    build (default: the synthetic tables of camb_tables.py)."""
+    base = dict(BASE, **(base or {}))
+    cosmo = dict(COSMO, **(cosmo or {}))
     with tempfile.TemporaryDirectory() as d:
         with open(os.path.join(d, "outputs.txt"), "w") as f:
-            f.write("0, %d\n" % BASE["nsteps"])
-        mgd = dict(inverted_initial_condition=0, amplitude_fixed_initial_condition=0)
-        mgd.update(mg)
-        txt = STD.format(out=d, **BASE) + "".join("%s %s\n" % kv for kv in mgd.items())
+            f.write("0, %d\n" % base["nsteps"])
+        txt = STD.format(out=d, **base, **cosmo) + "".join("%s %s\n" % kv for kv in mg.items())
         if "nu_SumMassNuEV" in mg:
-            txt += "nu_FilenameTransferInfofile %s\n" % camb_tables.write_tables(os.path.join(d, "camb"))
+            info = nu_info or camb_tables.write_tables(os.path.join(d, "camb"))
+            txt += "nu_FilenameTransferInfofile %s\n" % info
         pf = os.path.join(d, "params.txt")
         with open(pf, "w") as f:
             f.write(txt)
         log = subprocess.run([ref_build.binary(model), pf], capture_output=True, text=True)
         if log.returncode != 0:
-            raise RuntimeError(name + ": " + log.stdout[-2000:] + log.stderr[-2000:])
-        pk = np.loadtxt(os.path.join(d, "pofk_run_z0.000_CDM.txt"))
-        raw = open(os.path.join(d, "run_z0p000.0"), "rb").read()
-        n = BASE["Nsample"] ** 3
-        pos = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3)
-        vel = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3)
-        idx = np.arange(0, n, 8)
-        extra = {}
+            raise RuntimeError(model + ": " + log.stdout[-2000:] + log.stderr[-2000:])
+        out = dict(pk=np.loadtxt(os.path.join(d, "pofk_run_z0.000_CDM.txt")))
         if "nu_SumMassNuEV" in mg:
-            extra["pk_total"] = np.loadtxt(os.path.join(d, "pofk_run_z0.000_total.txt"))
-        np.savez(os.path.join(ROOT, "tests", "golden", "ref_%s.npz" % name), pk=pk, idx=idx, pos=pos[idx],
-                 vel=vel[idx], model=model, **{k: float(v) for k, v in mgd.items()}, **BASE, **extra)
-        print(name, "bins", pk.shape[0])
+            out["pk_total"] = np.loadtxt(os.path.join(d, "pofk_run_z0.000_total.txt"))
+        raw = open(os.path.join(d, "run_z0p000.0"), "rb").read()
+        n = base["Nsample"] ** 3
+        out["pos"] = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3).copy()
+        out["vel"] = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3).copy()
+    return out
 
+
+def run_case(name, model, mg):
+    mgd = dict(inverted_initial_condition=0, amplitude_fixed_initial_condition=0)
+    mgd.update(mg)
+    r = run_reference(model, mgd)
+    n = BASE["Nsample"] ** 3
+    idx = np.arange(0, n, 8)
+    extra = {"pk_total": r["pk_total"]} if "pk_total" in r else {}
+    np.savez(os.path.join(ROOT, "tests", "golden", "ref_%s.npz" % name), pk=r["pk"], idx=idx, pos=r["pos"][idx],
+             vel=r["vel"][idx], model=model, **{k: float(v) for k, v in mgd.items()}, **BASE, **extra)
+    print(name, "bins", r["pk"].shape[0])
 
 if __name__ == "__main__":
     ref_build.build()

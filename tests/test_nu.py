@@ -15,6 +15,7 @@ dependent): the host side against the FP64 oracle on synthetic CAMB tables
   - the parameter keys of that build and the reader's errors.
 """
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -44,8 +45,8 @@ def oracle_cosmo(info, p, model="lcdm"):
     nu = O.Neutrinos(info, p.Omega, p.OmegaBaryon, p.HubbleParam, p.PrimordialIndex, p.nu_SumMassNuEV,
                      p.nu_include_massive_neutrinos)
     if model == "fofr":
-        mg = O.make_mg(O.FOFR, p.Omega, mg_active=1, include_screening=1, fofr0=1e-5, nfofr=1.0, scaledependent=1,
-                       nu=nu, sd_nk=p.sd_nk)
+        mg = O.make_mg(O.FOFR, p.Omega, mg_active=1, include_screening=1, fofr0=p.fofr0, nfofr=p.nfofr,
+                       scaledependent=1, nu=nu, sd_nk=p.sd_nk)
     else:
         mg = O.make_mg(O.LCDM, p.Omega, scaledependent=1, nu=nu, sd_nk=p.sd_nk)
     return nu, O.Cosmo(mg, p.Init_Redshift, p.Box, p.Nmesh)
@@ -153,3 +154,77 @@ def test_neutrino_reader_errors(tmp_path, info):
         M.cosmo_eval(nu_params(str(tmp_path / "missing.txt")), 0, np.array([1.0]))
     with pytest.raises(M.MGPError, match="SCALEDEPENDENT"):
         M.cosmo_eval(nu_params(info, scaledependent=0), 0, np.array([1.0]))
+
+
+# --------------------------------------------------------------------------
+# The reference's own CAMB example tables (camb_data/example_data_nu0.4, the
+# inputs of its f(R)+neutrino test runs) and its own neutrino build, where
+# the reference tree is present.
+REAL_COSMO = dict(Omega=0.3175, OmegaBaryon=0.049, HubbleParam=0.671, Sigma8=0.7656, PrimordialIndex=0.966)
+
+
+@pytest.fixture(scope="module")
+def real_info(tmp_path_factory):
+    from oracle import ref_build
+    d = os.path.join(os.path.dirname(ref_build.REF_SRC), "camb_data", "example_data_nu0.4")
+    if not os.path.isdir(d):
+        pytest.skip("reference CAMB example data not present")
+    lines = open(os.path.join(d, "picola_transfer_info_nu0.4.txt")).read().split("\n")
+    # the info file names its author's directory: point it at this copy
+    info = os.path.join(str(tmp_path_factory.mktemp("realcamb")), "info.txt")
+    with open(info, "w") as f:
+        f.write("%s %s\n" % (d, lines[0].split()[1]) + "\n".join(lines[1:]) + "\n")
+    return info
+
+
+@pytest.mark.parametrize("model", ["lcdm", "fofr"])
+def test_host_cosmology_on_reference_camb_tables(real_info, model):
+    p = nu_params(real_info, model, nu_SumMassNuEV=0.4, fofr0=1e-4, **REAL_COSMO)
+    nu, cos = oracle_cosmo(real_info, p, model)
+    assert nu.omega_nu == pytest.approx(0.4 / (93.14 * 0.671 ** 2), rel=1e-14)
+    kk, aa = (g.ravel() for g in np.meshgrid(np.array([0.01, 0.1, 0.5, 2.0]), np.array([0.05, 0.5]), indexing="ij"))
+    for which in (0, 2, 3):
+        np.testing.assert_allclose(M.growth_scaledependent(p, which, kk, aa),
+                                   [cos.growth_sd(which, x, y) for x, y in zip(kk, aa)], rtol=2e-5)
+    pw = O.make_power(omega=p.Omega, omega_b=p.OmegaBaryon, h=p.HubbleParam, ns=p.PrimordialIndex, sigma8=p.Sigma8,
+                      nu=nu)
+    k = np.array([1e-3, 0.05, 0.3, 2.0])
+    np.testing.assert_allclose(M.cosmo_eval(p, 7, k), [O.lib().orc_power_spec(C.byref(pw), x) for x in k], rtol=1e-9)
+
+
+def test_oracle_matches_reference_run_on_its_camb_tables(real_info, tmp_path):
+    """The reference's f(R)+neutrino build (f_R0 = 1e-4, 0.4 eV, its example
+    cosmology) run here on its own CAMB tables, against the oracle's loop."""
+    from oracle import ref_build
+    from golden import make_golden
+    ref_build.build(models=["FOFRNU"])
+    mg = dict(modified_gravity_active=1, fofr0=1e-4, nfofr=1.0, include_screening=1, inverted_initial_condition=0,
+              amplitude_fixed_initial_condition=0, nu_include_massive_neutrinos=1, nu_SumMassNuEV=0.4)
+    base = dict(Box=256.0)
+    r = make_golden.run_reference("FOFRNU", mg, base=base, cosmo=REAL_COSMO, nu_info=real_info)
+    nu = O.Neutrinos(real_info, 0.3175, 0.049, 0.671, 0.966, 0.4, 1)
+    rp = O.RunParams()
+    rp.mg = O.make_mg(O.FOFR, 0.3175, mg_active=1, include_screening=1, fofr0=1e-4, nfofr=1.0, scaledependent=1,
+                      nu=nu)
+    rp.pw = O.make_power(omega=0.3175, omega_b=0.049, h=0.671, ns=0.966, sigma8=0.7656, nu=nu)
+    b = dict(make_golden.BASE, **base)
+    rp.ic = O.ICParams(b["Nmesh"], b["Nsample"], b["Box"], b["Seed"], 0, 0, 0, 1.0)
+    rp.init_redshift, rp.nsteps, rp.final_redshift = b["Init_Redshift"], b["nsteps"], 0.0
+    rp.pofk_nbins, rp.pofk_bintype, rp.pofk_subtract_shotnoise = 16, 0, 0
+    rp.pofk_kmin, rp.pofk_kmax, rp.usecola = 0.0, 0.0, 1
+    n = b["Nsample"] ** 3
+    pos, vel = np.zeros((n, 3)), np.zeros((n, 3))
+    kb, pk, km, nm = (np.zeros(b["Nmesh"]) for _ in range(4))
+    nb = O.lib().orc_run(rp, pos, vel, kb, pk, km, nm)
+    m = nm[:nb] > 0
+    m[0] = False
+    ref = r["pk_total"]
+    assert ref.shape[0] == m.sum()
+    np.testing.assert_allclose(pk[:nb][m], ref[:, 1], rtol=1e-6, atol=6e-6)
+    dx = np.abs(pos - r["pos"])
+    dx = np.minimum(dx, b["Box"] - dx)
+    assert dx.max() < 2e-5 * b["Box"]
+    v = 100.0 * vel
+    assert np.abs(r["vel"] - v).max() < 1e-6 * np.abs(v).max() + 1e-5
+    # the neutrinos are visible: total below CDM on every bin
+    assert np.all(r["pk_total"][:, 1] < r["pk"][:, 1])
