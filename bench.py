@@ -47,7 +47,41 @@ CONFIGS = {
     # particles on the 256^3 mesh, Box 256 Mpc/h, 30 steps)
     "closure_lcdm_256": dict(Ns=256, N=256, Box=256.0, model="lcdm", nsteps=30, seed=7017, fixed=0, nbins=128,
                              closure=True),
+    # f(R) Hu-Sawicki n=1, |fR0|=1e-5, screening, scale-dependent growth on
+    # 512 log-spaced k in [1e-4, 10] h/Mpc (256^3 particles, 512^3 mesh)
+    "fofr_sd_256_512": dict(Ns=256, N=512, Box=512.0, model="fofr", nsteps=30, seed=5002, fixed=0, nbins=256,
+                            sd=True),
+    # the same with massive neutrinos (0.4 eV, synthetic CAMB tables)
+    "fofr_nu_256_512": dict(Ns=256, N=512, Box=512.0, model="fofr", nsteps=30, seed=5002, fixed=0, nbins=256,
+                            sd=True, nu=True),
 }
+
+SD_GRID = dict(sd_nk=512, sd_kmin=1e-4, sd_kmax=10.0)
+_NU_INFO = []
+
+
+def nu_info():
+    """Synthetic CAMB transfer tables (0.4 eV) in a temporary directory,
+    written once per process."""
+    if not _NU_INFO:
+        import tempfile
+        from tests.golden import camb_tables
+        _NU_INFO.append(camb_tables.write_tables(tempfile.mkdtemp(prefix="mgp_camb_")))
+    return _NU_INFO[0]
+
+
+def model_name(cfg):
+    if cfg["model"] == "dgp":
+        name = "nDGP rcH0=1 screening (Gaussian, Rsmooth=1)"
+    elif cfg["model"] == "fofr":
+        name = "f(R) HS n=1 |fR0|=1e-5 screening"
+    else:
+        name = "LCDM"
+    if cfg.get("sd"):
+        name += ", scale-dependent growth (512 log k in [1e-4, 10] h/Mpc)"
+    if cfg.get("nu"):
+        name += " + massive neutrinos 0.4 eV (synthetic CAMB tables)"
+    return name
 
 
 def closure_flops(N):
@@ -79,6 +113,11 @@ def make_params(M, cfg):
     elif cfg["model"] == "fofr":
         kw.update(model=M.MODEL_FOFR, modified_gravity_active=1, include_screening=1, fofr0=1e-5, nfofr=1.0,
                   input_pofk_is_for_lcdm=1, input_sigma8_is_for_lcdm=1)
+    if cfg.get("sd"):
+        kw.update(scaledependent=1, **SD_GRID)
+    if cfg.get("nu"):
+        kw.update(massive_neutrinos=1, nu_include_massive_neutrinos=1, nu_SumMassNuEV=0.4,
+                  nu_FilenameTransferInfofile=nu_info())
     return M.default_params(**kw)
 
 
@@ -276,8 +315,8 @@ def run_gpu(args):
     sync()
     barrier()
     launches0 = ctx.launches()
-    stage_ms = {k: 0.0 for k in ["fill", "cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "closure",
-                                 "closure_conv"]}
+    stage_ms = {k: 0.0 for k in ["fill", "cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "lpt_fields",
+                                 "closure", "closure_conv"]}
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         dev_ms = 0.0
@@ -355,7 +394,7 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (2LPT IC generated on the device, seed 5003)",
         "config": {"workload": args.config, "particles": Np, "mesh": N, "box_mpc_h": cfg["Box"],
-                   "model": ("nDGP rcH0=1 screening (Gaussian, Rsmooth=1)" if cfg["model"] == "dgp" else "LCDM")
+                   "model": model_name(cfg)
                    + (" + learned force closure (4x 3^3 conv, 16 ch, BF16/FP32 acc)" if closure is not None else ""),
                    "pofk_every_step": True, "pofk_bins": cfg["nbins"], "l2": "inputs larger than L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -375,15 +414,24 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+_KEEP = []
+
+
 def oracle_params(O, cfg):
     rp = O.RunParams()
+    sdkw = dict(scaledependent=1, **SD_GRID) if cfg.get("sd") else {}
+    nu = None
+    if cfg.get("nu"):
+        nu = O.Neutrinos(nu_info(), 0.267, 0.049, 0.71, 0.96, 0.4, 1)
+        _KEEP.append(nu)  # the oracle structs point at its tables
+        sdkw["nu"] = nu
     if cfg["model"] == "dgp":
         rp.mg = O.make_mg(O.DGP, 0.267, rcH0=1.0, rsmooth=1.0)
     elif cfg["model"] == "fofr":
-        rp.mg = O.make_mg(O.FOFR, 0.267, fofr0=1e-5, nfofr=1.0)
+        rp.mg = O.make_mg(O.FOFR, 0.267, fofr0=1e-5, nfofr=1.0, **sdkw)
     else:
-        rp.mg = O.make_mg(O.LCDM, 0.267)
-    rp.pw = O.make_power(omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sigma8=0.8)
+        rp.mg = O.make_mg(O.LCDM, 0.267, **sdkw)
+    rp.pw = O.make_power(omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sigma8=0.8, nu=nu)
     rp.ic = O.ICParams(cfg["N"], cfg["Ns"], cfg["Box"], cfg["seed"], 0, cfg["fixed"], 0, 1.0)
     rp.init_redshift = 19.0
     rp.nsteps = cfg["nsteps"]
@@ -395,7 +443,12 @@ def oracle_params(O, cfg):
 
 
 SAMPLE = {"ndgp_512_1024": "ndgp_128_256", "ndgp_256_512": "ndgp_128_256", "lcdm_64_128": "lcdm_64_128",
-          "fofr_batch_64x64_128": "fofr_64_128", "closure_lcdm_256": "lcdm_128_128"}
+          "fofr_batch_64x64_128": "fofr_64_128", "closure_lcdm_256": "lcdm_128_128",
+          "fofr_sd_256_512": "fofr_sd_64_128", "fofr_nu_256_512": "fofr_nu_64_128"}
+CONFIGS["fofr_sd_64_128"] = dict(Ns=64, N=128, Box=128.0, model="fofr", nsteps=30, seed=5002, fixed=0, nbins=64,
+                                 sd=True)
+CONFIGS["fofr_nu_64_128"] = dict(Ns=64, N=128, Box=128.0, model="fofr", nsteps=30, seed=5002, fixed=0, nbins=64,
+                                 sd=True, nu=True)
 CONFIGS["fofr_64_128"] = dict(Ns=64, N=128, Box=256.0, model="fofr", nsteps=20, seed=6001, fixed=0, nbins=64)
 CONFIGS["lcdm_128_128"] = dict(Ns=128, N=128, Box=128.0, model="lcdm", nsteps=30, seed=7017, fixed=0, nbins=64)
 CONFIGS["ndgp_128_256"] = dict(Ns=128, N=256, Box=256.0, model="dgp", nsteps=50, seed=5003, fixed=1, nbins=128)

@@ -293,13 +293,12 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   free(c->box_p);
   void *bufs[] = {c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
                   c->fft_work, c->rk_bin, c->pk_thr, c->win1d, c->pk_block, c->pk_sum, c->rsd_block, c->rsd_sum,
-                  c->pk_sum_tot, c->nu_tab_d};
+                  c->pk_sum_tot, c->nu_tab_d, c->nu_row_d, c->nu_x_d, c->nu_den_d};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
     if (bufs[i]) cudaFree(bufs[i]);
-  if (c->nu_tab_h) cudaFreeHost(c->nu_tab_h);
+  if (c->nu_row_h) cudaFreeHost(c->nu_row_h);
   for (int q = 0; q < 2; q++)
     if (c->nu_ev[q]) cudaEventDestroy(c->nu_ev[q]);
-  free(c->nu_den);
   for (int t = 0; t < MGP_NTIMERS; t++) {
     if (c->ev[t][0]) cudaEventDestroy(c->ev[t][0]);
     if (c->ev[t][1]) cudaEventDestroy(c->ev[t][1]);
@@ -734,27 +733,40 @@ static int pofk_now(mgp_ctx *c, int fuse_kind, double A, double *sums = NULL) {
   return MGP_OK;
 }
 
-// Massive neutrinos (src/auxPM.c:383-428).  The factor table of this step
-// is computed on the host and uploaded before the step's first launch, so
-// the host works while the GPU finishes the previous step's kick and drift.
+// Massive neutrinos (src/auxPM.c:383-428).  The factor depends on |k|^2
+// only: the host restricts the transfer table to this step's redshift (one
+// row over the ln k nodes), uploads it before the step's first launch, and
+// k_nu_table evaluates the factor for every integer |k|^2 on the device.
 static int nu_prepare(mgp_ctx *c, double A) {
   const int N = c->g.N, h = N / 2;
   const int nrk = 3 * h * h + 1;
-  if (!c->nu_tab_h) {
-    MGP_CUDA(cudaMallocHost(&c->nu_tab_h, sizeof(double) * 2 * nrk));
+  if (!c->nu_row_h) {
+    int nx = 0;
+    const double *lnk = mgp_cosmo_nu_lnk(&c->cosmo, &nx);
+    c->nu_nx = nx;
+    MGP_CUDA(cudaMallocHost(&c->nu_row_h, sizeof(double) * 4 * nx));
+    MGP_CUDA(cudaMalloc(&c->nu_row_d, sizeof(double) * 2 * nx));
+    MGP_CUDA(cudaMalloc(&c->nu_x_d, sizeof(double) * nx));
+    MGP_CUDA(cudaMalloc(&c->nu_den_d, sizeof(double) * nrk));
     MGP_CUDA(cudaMalloc(&c->nu_tab_d, sizeof(double) * nrk));
     for (int q = 0; q < 2; q++) MGP_CUDA(cudaEventCreateWithFlags(&c->nu_ev[q], cudaEventDisableTiming));
-    c->nu_den = (double *)malloc(sizeof(double) * nrk);
-    if (!c->nu_den) return mgp_set_error(MGP_ENOMEM, "neutrino table");
-    mgp_cosmo_nu_den(&c->cosmo, N, nrk, c->nu_den);
+    std::vector<double> den(nrk);
+    mgp_cosmo_nu_den(&c->cosmo, N, nrk, den.data());
+    MGP_CUDA(cudaMemcpy(c->nu_den_d, den.data(), sizeof(double) * nrk, cudaMemcpyHostToDevice));
+    MGP_CUDA(cudaMemcpy(c->nu_x_d, lnk, sizeof(double) * nx, cudaMemcpyHostToDevice));
   }
+  const int nx = c->nu_nx;
   c->nu_slot ^= 1;
-  double *slot = c->nu_tab_h + (size_t)c->nu_slot * nrk;
+  double *row = c->nu_row_h + (size_t)c->nu_slot * 2 * nx;
   MGP_CUDA(cudaEventSynchronize(c->nu_ev[c->nu_slot]));  // its upload two steps ago is done
-  c->nu_cdmfac = mgp_cosmo_nu_table(&c->cosmo, A, N, nrk, c->nu_den, slot);
-  MGP_CUDA(cudaMemcpyAsync(c->nu_tab_d, slot, sizeof(double) * nrk, cudaMemcpyHostToDevice, c->stream));
+  mgp_cosmo_nu_row(&c->cosmo, A, row, row + nx);
+  MGP_CUDA(cudaMemcpyAsync(c->nu_row_d, row, sizeof(double) * 2 * nx, cudaMemcpyHostToDevice, c->stream));
   MGP_CUDA(cudaEventRecord(c->nu_ev[c->nu_slot], c->stream));
-  return MGP_OK;
+  const mgp_cosmo *cs = &c->cosmo;
+  const double fac = cs->OmegaNu / cs->p.Omega * (double)N * (double)N * (double)N;
+  c->nu_cdmfac = (cs->p.Omega - cs->OmegaNu) / cs->p.Omega;
+  return mgp_launch_nu_table(c->nu_tab_d, nrk, 2.0 * M_PI / cs->p.Box, fac, c->nu_x_d, c->nu_row_d, c->nu_row_d + nx, nx,
+                             c->nu_den_d, c->stream);
 }
 
 // delta(k) becomes the total matter density, cdmfac delta_cdm(k) + the

@@ -1313,14 +1313,13 @@ void mgp_cosmo_nu_den(const mgp_cosmo *c, int N, int nrk, double *den) {
   for (int rk = 1; rk < nrk; rk++) den[rk] = nu_Tcb(c, &o1, 2.0 * M_PI / c->p.Box * sqrt((double)rk), c->OmegaCDM);
 }
 
-double mgp_cosmo_nu_table(const mgp_cosmo *c, double a, int N, int nrk, const double *den, double *out) {
-  if (!c->nu) return 1.0;
-  double *buf = (double *)malloc(sizeof(double) * 8 * c->nuT[0].nx);
-  nu_rows o = {0, buf};
-  nu_rows_at(c, a, &o);
-  const double fac = c->OmegaNu / c->p.Omega * (double)N * (double)N * (double)N;
-  out[0] = 0.0;
-  for (int rk = 1; rk < nrk; rk++) out[rk] = fac * nu_T(c, &o, 0, 2.0 * M_PI / c->p.Box * sqrt((double)rk)) / den[rk];
-  free(buf);
-  return (c->p.Omega - c->OmegaNu) / c->p.Omega;
+int mgp_cosmo_nu_row(const mgp_cosmo *c, double a, double *val, double *dval) {
+  if (!c->nu) return 0;
+  bicubic_row(&c->nuT[0], 1.0 / a - 1.0, val, dval);
+  return c->nuT[0].nx;
+}
+
+const double *mgp_cosmo_nu_lnk(const mgp_cosmo *c, int *nx) {
+  *nx = c->nu ? c->nuT[0].nx : 0;
+  return c->nu ? c->nuT[0].x : NULL;
 }

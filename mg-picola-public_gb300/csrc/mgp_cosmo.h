@@ -55,12 +55,15 @@ typedef struct mgp_cosmo {
 
 int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen);
 /* Massive-neutrino density factors per integer |k|^2 = rk of an N^3 mesh
- * (src/auxPM.c:383-421): mgp_cosmo_nu_den fills den[rk] = T_cb(k, 1), the
- * step-independent denominators; mgp_cosmo_nu_table fills out[rk] =
- * OmegaNu/Omega N^3 T_nu(k, a) / den[rk] (out[0] = 0) and returns cdmfac =
- * (Omega - OmegaNu) / Omega. */
+ * (src/auxPM.c:383-421), OmegaNu/Omega N^3 T_nu(k, a) / T_cb(k, 1):
+ * mgp_cosmo_nu_den fills den[rk] = T_cb(k, 1), the step-independent
+ * denominators; mgp_cosmo_nu_row gives the massive-nu transfer function at
+ * z = 1/a - 1 as value and d/d ln k on the table's ln k nodes
+ * (mgp_cosmo_nu_lnk; clamped lookups use the cubic Hermite between nodes)
+ * and returns the node count. */
 void mgp_cosmo_nu_den(const mgp_cosmo *c, int N, int nrk, double *den);
-double mgp_cosmo_nu_table(const mgp_cosmo *c, double a, int N, int nrk, const double *den, double *out);
+int mgp_cosmo_nu_row(const mgp_cosmo *c, double a, double *val, double *dval);
+const double *mgp_cosmo_nu_lnk(const mgp_cosmo *c, int *nx);
 void mgp_cosmo_free(mgp_cosmo *c);
 
 /* hooks, src/user_defined_functions.h:413-904 */

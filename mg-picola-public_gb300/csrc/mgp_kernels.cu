@@ -857,6 +857,41 @@ __global__ void k_nu_add(float2 *__restrict__ dk, const float2 *__restrict__ dk0
   }
 }
 
+// The neutrino factor per integer |k|^2 (rk = 1 .. nrk-1; rk = 0 is 0):
+// fac T_nu(k, a) / den[rk] at k = kfac sqrt(rk), T_nu the cubic Hermite in
+// ln k of the transfer row (val, dval on the nodes x), clamped to the table
+// as Lookup_GSL_2D_Spline does (src/wrappers.c:129-136).
+__global__ void k_nu_table(double *__restrict__ tab, int nrk, double kfac, double fac, const double *__restrict__ x,
+                           const double *__restrict__ val, const double *__restrict__ dval, int nx,
+                           const double *__restrict__ den) {
+  for (int rk = blockIdx.x * blockDim.x + threadIdx.x; rk < nrk; rk += gridDim.x * blockDim.x) {
+    if (rk == 0) {
+      tab[0] = 0.0;
+      continue;
+    }
+    double xv = log(kfac * sqrt((double)rk));
+    xv = fmin(fmax(xv, x[0]), x[nx - 1]);
+    int lo = 0, hi = nx - 1;
+    while (hi - lo > 1) {
+      const int m = (lo + hi) / 2;
+      if (x[m] > xv) hi = m;
+      else lo = m;
+    }
+    const double dx = x[lo + 1] - x[lo], t = (xv - x[lo]) / dx;
+    const double T = (1 + 2 * t) * (1 - t) * (1 - t) * val[lo] + t * t * (3 - 2 * t) * val[lo + 1] +
+                     t * (1 - t) * (1 - t) * dx * dval[lo] + t * t * (t - 1) * dx * dval[lo + 1];
+    tab[rk] = fac * T / den[rk];
+  }
+}
+
+int mgp_launch_nu_table(double *tab, int nrk, double kfac, double fac, const double *x, const double *val,
+                        const double *dval, int nx, const double *den, cudaStream_t st) {
+  k_nu_table<<<blocks_for(nrk, 4), MGP_THREADS, 0, st>>>(tab, nrk, kfac, fac, x, val, dval, nx, den);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
 int mgp_launch_nu_add(float *dk, const float *dk0, int N, double cdmfac, const double *nufac, cudaStream_t st) {
   const long long n = (long long)N * N * (N / 2 + 1);
   k_nu_add<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>((float2 *)dk, (const float2 *)dk0, N, cdmfac, nufac);

@@ -157,16 +157,31 @@ double orc_time_steps(const orc_run_params *rp, int nsteps) {
   const double Box = rp->ic.box;
   const long np = (long)Ns * Ns * Ns;
   const size_t tot = (size_t)N * N * NH;
-  orc_cosmo *c = orc_cosmo_create(&rp->mg, rp->init_redshift);
+  const int sd = rp->mg.scaledependent;
+  orc_cosmo *c = orc_cosmo_create_sd(&rp->mg, rp->init_redshift, Box, N);
   double *D1 = malloc(8 * 3 * np), *D2 = malloc(8 * 3 * np), *pos = malloc(8 * 3 * np), *vel = calloc(3 * np, 8);
   double *disp = malloc(8 * 3 * np);
-  orc_ic_2lpt(&rp->ic, &rp->pw, D1, D2, NULL, NULL);
+  /* scale-dependent build: stored delta(k), -source(k) and the per-step
+   * fields, as orc_run */
+  double *cdelta = NULL, *cdelta2 = NULL, *V1 = NULL, *V2 = NULL;
+  if (sd) {
+    cdelta = malloc(sizeof(double) * 2 * tot);
+    cdelta2 = malloc(sizeof(double) * 2 * tot);
+    V1 = malloc(8 * 3 * np);
+    V2 = malloc(8 * 3 * np);
+  }
+  orc_ic_2lpt(&rp->ic, &rp->pw, D1, D2, cdelta, cdelta2);
   double A = 1.0 / (1.0 + rp->init_redshift);
   double Di = orc_growth_D(c, A), Di2 = orc_growth_D2(c, A);
+  if (sd) {
+    orc_sd_field(c, cdelta, N, Ns, Box, A, A, ORC_FIELD_D, 1, D1);
+    orc_sd_field(c, cdelta2, N, Ns, Box, A, A, ORC_FIELD_D, 2, D2);
+  }
+  const double fD = sd ? 1.0 : Di, fD2 = sd ? 1.0 : Di2;
   for (long p = 0; p < np; p++) {
     long q[3] = {p / ((long)Ns * Ns), (p / Ns) % Ns, p % Ns};
     for (int a = 0; a < 3; a++)
-      pos[3 * p + a] = orc_periodic_wrap(q[a] * (Box / (double)Ns) + D1[3 * p + a] * Di + D2[3 * p + a] * Di2, Box);
+      pos[3 * p + a] = orc_periodic_wrap(q[a] * (Box / (double)Ns) + D1[3 * p + a] * fD + D2[3 * p + a] * fD2, Box);
   }
   double *grid = malloc(sizeof(double) * 2 * tot), *dens_x = malloc(sizeof(double) * 2 * tot);
   double *mgk = malloc(sizeof(double) * 2 * tot), *f[3];
@@ -184,15 +199,30 @@ double orc_time_steps(const orc_run_params *rp, int nsteps) {
     int nb = rp->pofk_nbins;
     orc_pofk(grid, N, Ns, Box, &nb, rp->pofk_bintype, rp->pofk_subtract_shotnoise, rp->pofk_kmin, rp->pofk_kmax, kb, pk,
              km, nm);
+    if (sd && rp->mg.nu) {
+      orc_nu_add_density(rp->mg.nu, A, N, Box, grid, cdelta);
+      nb = rp->pofk_nbins;
+      orc_pofk(grid, N, Ns, Box, &nb, rp->pofk_bintype, rp->pofk_subtract_shotnoise, rp->pofk_kmin, rp->pofk_kmax, kb,
+               pk, km, nm);
+    }
     if (rp->mg.mg_active) orc_fifth_force(&rp->mg, A, N, Box, dens_x, grid, mgk);
     orc_forces_kspace(grid, uses_mgk ? mgk : NULL, N, Box, f[0], f[1], f[2]);
     for (int a = 0; a < 3; a++) orc_fft_c2r(N, f[a]);
     double sumD[3];
     orc_interp(f[0], f[1], f[2], N, Box, pos, np, disp, sumD);
-    orc_kick(np, vel, disp, D1, D2, sumD, rp->mg.omega, orc_Sphi(c, AI, AF, A), orc_growth_ddDddy(c, A),
-             orc_growth_ddD2ddy(c, A), A, rp->usecola, sumv);
-    orc_drift(np, pos, vel, D1, D2, sumv, orc_Sq(c, A, AFF, AF), orc_growth_D(c, AFF) - Di, orc_growth_D2(c, AFF) - Di2,
-              rp->usecola, Box);
+    if (sd) {
+      orc_sd_field(c, cdelta, N, Ns, Box, A, AFF, ORC_FIELD_deltaD, 1, V1);
+      orc_sd_field(c, cdelta2, N, Ns, Box, A, AFF, ORC_FIELD_deltaD, 2, V2);
+      orc_sd_field(c, cdelta, N, Ns, Box, A, AFF, ORC_FIELD_ddDddy, 1, D1);
+      orc_sd_field(c, cdelta2, N, Ns, Box, A, AFF, ORC_FIELD_ddDddy, 2, D2);
+    }
+    orc_kick(np, vel, disp, D1, D2, sumD, rp->mg.omega, orc_Sphi(c, AI, AF, A), sd ? 1.0 : orc_growth_ddDddy(c, A),
+             sd ? 1.0 : orc_growth_ddD2ddy(c, A), A, rp->usecola, sumv);
+    if (sd)
+      orc_drift(np, pos, vel, V1, V2, sumv, orc_Sq(c, A, AFF, AF), 1.0, 1.0, rp->usecola, Box);
+    else
+      orc_drift(np, pos, vel, D1, D2, sumv, orc_Sq(c, A, AFF, AF), orc_growth_D(c, AFF) - Di,
+                orc_growth_D2(c, AFF) - Di2, rp->usecola, Box);
     A = AFF;
     AI = AF;
     Di = orc_growth_D(c, A);
@@ -202,6 +232,7 @@ double orc_time_steps(const orc_run_params *rp, int nsteps) {
   for (int a = 0; a < 3; a++) free(f[a]);
   free(grid); free(dens_x); free(mgk); free(D1); free(D2); free(pos); free(vel); free(disp);
   free(kb); free(pk); free(km); free(nm);
+  free(cdelta); free(cdelta2); free(V1); free(V2);
   orc_cosmo_free(c);
   return dt;
 }
