@@ -299,6 +299,8 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   if (c->nu_row_h) cudaFreeHost(c->nu_row_h);
   for (int q = 0; q < 2; q++)
     if (c->nu_ev[q]) cudaEventDestroy(c->nu_ev[q]);
+  for (int k = 0; k < MGP_POS_CHUNKS; k++)
+    if (c->ev_chunk[k]) cudaEventDestroy(c->ev_chunk[k]);
   for (int t = 0; t < MGP_NTIMERS; t++) {
     if (c->ev[t][0]) cudaEventDestroy(c->ev[t][0]);
     if (c->ev[t][1]) cudaEventDestroy(c->ev[t][1]);
@@ -782,6 +784,8 @@ static int add_neutrinos(mgp_ctx *c, double A) {
   return MGP_OK;
 }
 
+static int fields_from_density(mgp_ctx *c, double A);
+
 extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   RET_IF(require_particles(c));
   const int N = c->g.N;
@@ -794,6 +798,13 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   double wpar = pow((double)N / (double)c->Ns, 3);
   RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, c->p.Box, (float)wpar, c->rho, c->g.P, c->stream));
   tstop(c, T_CIC);
+  return fields_from_density(c, A);
+}
+
+// The rest of GetDisplacements once the density is on the mesh: R2C, P(k),
+// neutrinos, fifth force, forces and the three C2R.
+static int fields_from_density(mgp_ctx *c, double A) {
+  const int N = c->g.N;
   tstart(c, T_R2C);
   MGP_CUFFT(cufftExecR2C(c->plan_r2c_oop, (cufftReal *)c->rho, (cufftComplex *)c->dk));
   tstop(c, T_R2C);
@@ -1133,15 +1144,35 @@ extern "C" int mgp_step_host(mgp_ctx *c, double A, double AI, double AF, double 
     RET_IF(ensure_stage(c, 4));
     const size_t bytes = sizeof(float) * 3 * np;
     float *st[4] = {c->stage, c->stage + 3 * np, c->stage + 6 * np, c->stage + 9 * np};
-    if (pos) {
-      MGP_CUDA(cudaMemcpyAsync(st[0], pos, bytes, cudaMemcpyHostToDevice, c->stream));
-      RET_IF(mgp_launch_set_state(c->s, c->v, st[0], NULL, c->np, c->Ns, c->p.Box, c->stream));
-    }
     MGP_CUDA(cudaMemsetAsync(c->dstate, 0, sizeof(mgp_dstate), c->stream));
     // the side stream starts after everything queued so far (earlier readers
-    // of v, D1, D2 included)
+    // of the staging slots, s, v, D1 and D2 included)
     MGP_CUDA(cudaEventRecord(c->ev_side[0], c->stream));
     MGP_CUDA(cudaStreamWaitEvent(c->side, c->ev_side[0], 0));
+    if (pos) {
+      // positions first, in chunks: each is converted and deposited while
+      // the next one is still on the link (PtoMesh, src/auxPM.c:280-343)
+      if (!c->ev_chunk[0])
+        for (int k = 0; k < MGP_POS_CHUNKS; k++) MGP_CUDA(cudaEventCreateWithFlags(&c->ev_chunk[k], cudaEventDisableTiming));
+      const int N = c->g.N;
+      const double wpar = pow((double)N / (double)c->Ns, 3);
+      tstart(c, T_FILL);
+      RET_IF(mgp_launch_fill(c->rho, c->g.nreal, -1.0f, c->stream));
+      tstop(c, T_FILL);
+      tstart(c, T_CIC);
+      for (int k = 0; k < MGP_POS_CHUNKS; k++) {
+        const long long p0 = c->np * k / MGP_POS_CHUNKS, p1 = c->np * (k + 1) / MGP_POS_CHUNKS;
+        if (p1 <= p0) continue;
+        MGP_CUDA(cudaMemcpyAsync(st[0] + 3 * p0, pos + 3 * p0, sizeof(float) * 3 * (p1 - p0), cudaMemcpyHostToDevice,
+                                 c->side));
+        MGP_CUDA(cudaEventRecord(c->ev_chunk[k], c->side));
+        MGP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_chunk[k], 0));
+        RET_IF(mgp_launch_set_state_range(c->s, c->v, st[0], NULL, c->np, c->Ns, c->p.Box, p0, p1, c->stream));
+        RET_IF(mgp_launch_cic_range(c->s, c->dstate, c->np, p0, p1, c->Ns, N, c->p.Box, (float)wpar, c->rho, c->g.P,
+                                    c->stream));
+      }
+      tstop(c, T_CIC);
+    }
     const float *src[3] = {vel, D1, D2};
     float *dst[3] = {c->v, c->D1, c->D2};
     for (int q = 0; q < 3; q++) {
@@ -1152,6 +1183,15 @@ extern "C" int mgp_step_host(mgp_ctx *c, double A, double AI, double AF, double 
     MGP_CUDA(cudaEventRecord(c->ev_side[1], c->side));
     c->side_pending = 1;
     c->have_density = c->have_forces = 0;
+    if (pos) {
+      // the density is on the mesh: the rest of the step as mgp_step
+      tstart(c, T_MISC);
+      RET_IF(fields_from_density(c, A));
+      RET_IF(mgp_kick_drift(c, AI, AF, A, AFF, 1));
+      tstop(c, T_MISC);
+      RET_IF(mgp_get_particles(c, pos, vel, NULL, NULL, np));
+      return MGP_OK;
+    }
   }
   RET_IF(mgp_step(c, A, AI, AF, AFF));
   RET_IF(mgp_get_particles(c, pos, vel, NULL, NULL, np));

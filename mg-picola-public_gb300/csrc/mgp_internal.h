@@ -70,6 +70,9 @@ struct mgp_ctx {
   int stage_arrays;
   cudaStream_t side;       /* host-buffer step: copies that only the kick waits for */
   cudaEvent_t ev_side[2];
+  /* host-buffer step: the position upload in MGP_POS_CHUNKS pieces, each
+   * converted and deposited as soon as it has arrived */
+  cudaEvent_t ev_chunk[8];
   int side_pending;
   int max_blocks;
 
@@ -204,6 +207,7 @@ int mgp_set_error(int code, const char *fmt, ...);
  * being blockIdx.y; `bs` (device, nbox entries) replaces the by-value
  * scalars when non-NULL. */
 int mgp_blocks_per_box(long long n_per_box, int per_sm, int nbox);
+#define MGP_POS_CHUNKS 8  /* pieces of the position upload of mgp_step_host */
 #define MGP_BUDGET_DEFAULT 8
 void mgp_set_launch_budget(int cic, int grid);
 /* Per-launch scalars of the fused MtoParticles + Kick + Drift kernel. */
@@ -248,6 +252,8 @@ int mgp_sd_init_particles(mgp_ctx *c);
 int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st);
 int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box,
                    float wpar, float *rho, long long P, cudaStream_t stream, int nbox = 1, long long g_bs = 0);
+int mgp_launch_cic_range(const float *s, const mgp_dstate *st, long long np, long long p0, long long p1, int Ns, int N,
+                         double box, float wpar, float *rho, long long P, cudaStream_t stream);
 int mgp_launch_pofk(const float *dk, int N, const int *rk_bin, const float *win, int nbins,
                     double *block_part, int nblocks, double *sums, cudaStream_t st);
 int mgp_launch_pofk_thr(const float *dk, int N, const int *thr, const float *win, int nbins, int bintype, double kmin,
@@ -308,5 +314,7 @@ int mgp_launch_positions(const float *s, const mgp_dstate *dst, long long np, in
                          float *out_pos, float *out_vel, const float *v, cudaStream_t st);
 int mgp_launch_set_state(float *s, float *v, const float *pos, const float *vel, long long np, int Ns,
                          double box, cudaStream_t st);
+int mgp_launch_set_state_range(float *s, float *v, const float *pos, const float *vel, long long np, int Ns,
+                               double box, long long p0, long long p1, cudaStream_t st);
 
 #endif

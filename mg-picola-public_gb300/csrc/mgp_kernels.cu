@@ -84,7 +84,8 @@ int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st) {
 // x-slice exchange of auxPM.c:350-356 is the x wrap).
 __global__ void __launch_bounds__(MGP_THREADS) k_cic(const float *__restrict__ s, const mgp_dstate *__restrict__ st,
                                                      long long np, int Ns, int N, float scale, float wpar,
-                                                     float *__restrict__ rho, long long P, long long g_bs) {
+                                                     float *__restrict__ rho, long long P, long long g_bs,
+                                                     long long p0, long long p1) {
   // box blockIdx.y of a batch: particles 3 np apart, grids g_bs floats apart
   s += blockIdx.y * 3 * np;
   st += blockIdx.y;
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(MGP_THREADS) k_cic(const float *__restrict__ s
   const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
   const float *sx = s, *sy = s + np, *sz = s + 2 * np;
   long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+  for (long long p = p0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += stride) {
     int i, j, k;
     lattice_ijk(p, Ns, i, j, k);
     int ix, iy, iz;
@@ -118,7 +119,19 @@ __global__ void __launch_bounds__(MGP_THREADS) k_cic(const float *__restrict__ s
 
 int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box, float wpar,
                    float *rho, long long P, cudaStream_t stream, int nbox, long long g_bs) {
-  k_cic<<<grid_boxes(np, g_budget_cic, nbox), MGP_THREADS, 0, stream>>>(s, st, np, Ns, N, (float)(N / box), wpar, rho, P, g_bs);
+  k_cic<<<grid_boxes(np, g_budget_cic, nbox), MGP_THREADS, 0, stream>>>(s, st, np, Ns, N, (float)(N / box), wpar, rho, P, g_bs,
+                                                                      0, np);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
+// one box, particles p0 .. p1-1 (deposits of the chunks of a host upload)
+int mgp_launch_cic_range(const float *s, const mgp_dstate *st, long long np, long long p0, long long p1, int Ns, int N,
+                         double box, float wpar, float *rho, long long P, cudaStream_t stream) {
+  if (p1 <= p0) return MGP_OK;
+  k_cic<<<grid_boxes(p1 - p0, g_budget_cic, 1), MGP_THREADS, 0, stream>>>(s, st, np, Ns, N, (float)(N / box), wpar, rho, P,
+                                                                        0, p0, p1);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -1209,10 +1222,11 @@ int mgp_launch_positions(const float *s, const mgp_dstate *dst, long long np, in
 
 // Import absolute AoS positions/velocities: s = nearest-image (pos - q).
 __global__ void k_set_state(float *__restrict__ s, float *__restrict__ v, const float *__restrict__ pos,
-                            const float *__restrict__ vel, long long np, int Ns, double box) {
+                            const float *__restrict__ vel, long long np, int Ns, double box, long long p0,
+                            long long p1) {
   long long stride = (long long)gridDim.x * blockDim.x;
   const float dq = (float)(box / (double)Ns), fbox = (float)box, half = 0.5f * (float)box;
-  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+  for (long long p = p0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += stride) {
     int li[3];
     lattice_ijk(p, Ns, li[0], li[1], li[2]);
     for (int a = 0; a < 3; a++) {
@@ -1229,7 +1243,14 @@ __global__ void k_set_state(float *__restrict__ s, float *__restrict__ v, const 
 
 int mgp_launch_set_state(float *s, float *v, const float *pos, const float *vel, long long np, int Ns, double box,
                          cudaStream_t st) {
-  k_set_state<<<blocks_for(np, 4), MGP_THREADS, 0, st>>>(s, v, pos, vel, np, Ns, box);
+  return mgp_launch_set_state_range(s, v, pos, vel, np, Ns, box, 0, np, st);
+}
+
+// particles p0 .. p1-1 only (the host-buffer step converts each uploaded chunk)
+int mgp_launch_set_state_range(float *s, float *v, const float *pos, const float *vel, long long np, int Ns,
+                               double box, long long p0, long long p1, cudaStream_t st) {
+  if (p1 <= p0) return MGP_OK;
+  k_set_state<<<blocks_for(p1 - p0, 4), MGP_THREADS, 0, st>>>(s, v, pos, vel, np, Ns, box, p0, p1);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
