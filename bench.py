@@ -398,7 +398,9 @@ def run_gpu(args):
                    + (" + learned force closure (4x 3^3 conv, 16 ch, BF16/FP32 acc)" if closure is not None else ""),
                    "pofk_every_step": True, "pofk_bins": cfg["nbins"], "l2": "inputs larger than L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "e2e": {"value": round(e2e_val, 3), "unit": UNIT, "h2d_bytes_per_step": 4 * 12 * Np,
+        "e2e": {"value": round(e2e_val, 3), "unit": UNIT,
+                # scale-dependent growth: the step assigns its own D1/D2, only pos/vel go up
+                "h2d_bytes_per_step": (2 if cfg.get("sd") else 4) * 12 * Np,
                 "d2h_bytes_per_step": 2 * 12 * Np, "api": "mgp_step_host",
                 "step_ms": [round(x, 2) for x in e2e_ms]},
         "gpu_launches": int(launches),

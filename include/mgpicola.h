@@ -269,13 +269,18 @@ int mgp_pofk_rsd(mgp_ctx *ctx, double A, int cap, int *nbins, double *k, double 
 /* Particle state, host buffers of [np][3] floats (AoS, the order of
  * struct part_data's Pos/Vel/D/D2, src/vars.h:292-321).  Positions are
  * wrapped to [0, Box); velocities are the internal COLA velocities
- * (Vel - <Vel> is what Drift uses).  Any pointer may be NULL. */
+ * (Vel - <Vel> is what Drift uses).  Any pointer may be NULL; setting only
+ * positions (velocities) leaves the velocities (positions) as they were. */
 int mgp_get_particles(mgp_ctx *ctx, float *pos, float *vel, float *D1, float *D2, size_t np);
 int mgp_set_particles(mgp_ctx *ctx, const float *pos, const float *vel, const float *D1,
                       const float *D2, size_t np);
 
 /* Host-buffer step for drop-in callers that keep particles in host memory:
- * copies pos/vel/D1/D2 in, runs mgp_step, copies pos/vel back. */
+ * copies pos/vel/D1/D2 in, runs mgp_step, copies pos/vel back.  The
+ * positions are uploaded in chunks that are deposited as they arrive; the
+ * other arrays travel on a second stream while the step runs.  With
+ * scale-dependent growth the step assigns its own LPT fields, so D1/D2 are
+ * not read (as mgp_set_particles). */
 int mgp_step_host(mgp_ctx *ctx, double A, double AI, double AF, double AFF, float *pos, float *vel,
                   const float *D1, const float *D2, size_t np);
 

@@ -10,6 +10,7 @@
 #include <string.h>
 
 #include <string>
+#include <cstddef>
 #include <vector>
 
 #include "mgp_internal.h"
@@ -1086,6 +1087,14 @@ extern "C" int mgp_get_particles(mgp_ctx *c, float *pos, float *vel, float *D1, 
   return MGP_OK;
 }
 
+// New absolute positions (velocities) restart the position (velocity) offset
+// from zero; the other offset stays, or the particles would move.
+static int reset_offsets(mgp_ctx *c, int pos_set, int vel_set, cudaStream_t st) {
+  if (pos_set) MGP_CUDA(cudaMemsetAsync((char *)c->dstate + offsetof(mgp_dstate, cx), 0, sizeof(double) * 3, st));
+  if (vel_set) MGP_CUDA(cudaMemsetAsync((char *)c->dstate + offsetof(mgp_dstate, cv), 0, sizeof(double) * 3, st));
+  return MGP_OK;
+}
+
 extern "C" int mgp_set_particles(mgp_ctx *c, const float *pos, const float *vel, const float *D1, const float *D2,
                                  size_t np) {
   RET_IF(require_particles(c));
@@ -1097,8 +1106,7 @@ extern "C" int mgp_set_particles(mgp_ctx *c, const float *pos, const float *vel,
   if (vel) MGP_CUDA(cudaMemcpyAsync(b, vel, bytes, cudaMemcpyHostToDevice, c->stream));
   if (pos || vel) {
     RET_IF(mgp_launch_set_state(c->s, c->v, pos ? a : NULL, vel ? b : NULL, c->np, c->Ns, c->p.Box, c->stream));
-    // absolute state: offsets restart from zero
-    MGP_CUDA(cudaMemsetAsync(c->dstate, 0, sizeof(mgp_dstate), c->stream));
+    RET_IF(reset_offsets(c, pos != NULL, vel != NULL, c->stream));
   }
   // with scale-dependent growth the LPT fields are recomputed from the stored
   // delta(k) before every use, so D1/D2 are not read
@@ -1125,17 +1133,16 @@ extern "C" int mgp_host_unregister(void *ptr) {
   return MGP_OK;
 }
 
-// The positions go first (the deposit needs them); the velocities and the
-// LPT displacements, which only the kick reads, are copied and converted on
-// a second stream while the deposit, the FFTs and the force pass run, and the
-// kick waits for them.
+// The positions go first, in chunks that are deposited as they arrive; the
+// velocities and the LPT displacements, which only the kick reads, are
+// copied and converted on a second stream while the deposit, the FFTs and
+// the force pass run, and the kick waits for them.  With scale-dependent
+// growth the step assigns its own LPT fields and D1/D2 are not read.
 extern "C" int mgp_step_host(mgp_ctx *c, double A, double AI, double AF, double AFF, float *pos, float *vel,
                              const float *D1, const float *D2, size_t np) {
   RET_IF(require_particles(c));
   if ((long long)np != c->np) return mgp_set_error(MGP_EINVAL, "np = %zu, context holds %lld", np, c->np);
-  if (c->sd) {
-    RET_IF(mgp_set_particles(c, pos, vel, D1, D2, np));
-  } else {
+  {
     if (!c->side) {
       MGP_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
       MGP_CUDA(cudaEventCreateWithFlags(&c->ev_side[0], cudaEventDisableTiming));
@@ -1144,7 +1151,7 @@ extern "C" int mgp_step_host(mgp_ctx *c, double A, double AI, double AF, double 
     RET_IF(ensure_stage(c, 4));
     const size_t bytes = sizeof(float) * 3 * np;
     float *st[4] = {c->stage, c->stage + 3 * np, c->stage + 6 * np, c->stage + 9 * np};
-    MGP_CUDA(cudaMemsetAsync(c->dstate, 0, sizeof(mgp_dstate), c->stream));
+    RET_IF(reset_offsets(c, pos != NULL, vel != NULL, c->stream));
     // the side stream starts after everything queued so far (earlier readers
     // of the staging slots, s, v, D1 and D2 included)
     MGP_CUDA(cudaEventRecord(c->ev_side[0], c->stream));
@@ -1173,7 +1180,8 @@ extern "C" int mgp_step_host(mgp_ctx *c, double A, double AI, double AF, double 
       }
       tstop(c, T_CIC);
     }
-    const float *src[3] = {vel, D1, D2};
+    // with scale-dependent growth the step assigns the LPT fields itself
+    const float *src[3] = {vel, c->sd ? NULL : D1, c->sd ? NULL : D2};
     float *dst[3] = {c->v, c->D1, c->D2};
     for (int q = 0; q < 3; q++) {
       if (!src[q]) continue;
@@ -1187,6 +1195,12 @@ extern "C" int mgp_step_host(mgp_ctx *c, double A, double AI, double AF, double 
       // the density is on the mesh: the rest of the step as mgp_step
       tstart(c, T_MISC);
       RET_IF(fields_from_density(c, A));
+      if (c->sd) {
+        const int types[2] = {MGP_FIELD_ddDddy, MGP_FIELD_deltaD};
+        tstart(c, T_SD);
+        RET_IF(mgp_sd_fields(c, A, AFF, 2, types));
+        tstop(c, T_SD);
+      }
       RET_IF(mgp_kick_drift(c, AI, AF, A, AFF, 1));
       tstop(c, T_MISC);
       RET_IF(mgp_get_particles(c, pos, vel, NULL, NULL, np));

@@ -294,6 +294,31 @@ def test_rsd_multipoles_match_oracle():
     np.testing.assert_allclose(s0[m], np.abs(y0 - z0)[m] / np.sqrt(2), atol=1e-5 * np.abs(y0 + shot).max())
 
 
+def test_set_one_of_positions_or_velocities_keeps_the_other():
+    """After steps the positions and velocities carry global offsets; setting
+    only velocities (positions) must not move the particles (change the
+    velocities)."""
+    p = params(32, 16, 128.0, Seed=4242)
+    A0 = 1.0 / 20.0
+    da = (1.0 - A0) / 5
+    with M.Context(p) as c:
+        c.displacement_fields()
+        A, AI = A0, A0
+        for _ in range(2):
+            c.step(A, AI, A + 0.5 * da, A + da)
+            A, AI = A + da, A + 0.5 * da
+        pos, vel, _, _ = c.get_particles()
+        c.set_particles(vel=vel * 0.5)
+        pos2, vel2, _, _ = c.get_particles()
+        assert np.abs(pos2 - pos).max() < 1e-6 * 128.0
+        np.testing.assert_allclose(vel2, vel * 0.5, rtol=1e-5, atol=1e-5 * np.abs(vel).max())
+        c.set_particles(pos=pos)
+        pos3, vel3, _, _ = c.get_particles()
+        np.testing.assert_allclose(vel3, vel2, rtol=1e-6, atol=1e-6 * np.abs(vel).max())
+        dx = np.abs(pos3 - pos)
+        assert np.minimum(dx, 128.0 - dx).max() < 1e-5 * 128.0
+
+
 def test_run_writes_reference_formats(tmp_path):
     """mgp_run: GADGET-1 snapshot, info file and pofk files (src/main.c:792-1149,
     src/compute_pofk.c:238-478) with the reference's names and layouts."""
