@@ -121,6 +121,29 @@ def make_params(M, cfg):
     return M.default_params(**kw)
 
 
+def rank_seed(cfg, rank):
+    """Replicas are independent boxes: rank r runs seed + r."""
+    return cfg["seed"] + rank
+
+
+def reduce_max(value, dist):
+    """The job's time is the slowest rank's (max over ranks); identity on one
+    process."""
+    if dist is None:
+        return value
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, Np, steps, elapsed):
+    """Whole-job throughput: the particle-steps of all ranks over the slowest
+    rank's time (Mparticle-steps/s)."""
+    return world * Np * steps / elapsed / 1e6
+
+
 def run_batch(args, cfg):
     """A batch of independent boxes: each timed step is one graph launch that
     runs the whole KDK loop of every box; value counts particle-steps of all
@@ -283,6 +306,7 @@ def run_gpu(args):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     p = make_params(M, cfg)
+    p.Seed = rank_seed(cfg, rank)
     Np = cfg["Ns"] ** 3
     N = cfg["N"]
     ctx = M.Context(p, device=local if world > 1 else 0)
@@ -331,13 +355,9 @@ def run_gpu(args):
     elapsed = dev_ms * 1e-3
     launches = ctx.launches() - launches0
     barrier()
-    if dist is not None:
-        import torch
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = reduce_max(elapsed, dist)
     ms_per_step = elapsed / args.steps * 1e3
-    value = world * Np * args.steps / elapsed / 1e6
+    value = job_value(world, Np, args.steps, elapsed)
 
     # e2e through the host-buffer C-ABI entry point, pinned host memory
     ctx.set_timing(False)
@@ -357,10 +377,10 @@ def run_gpu(args):
     host_step()  # untimed: allocates the staging buffers and the copy stream
     barrier()
     e2e_ms = [host_step() * 1e3 for _ in range(e2e_steps)]
-    e2e_t = sum(e2e_ms) * 1e-3
+    e2e_t = reduce_max(sum(e2e_ms) * 1e-3, dist)
     for a in (pos, vel, d1, d2):
         M.unpin(a)
-    e2e_val = world * Np * e2e_steps / e2e_t / 1e6
+    e2e_val = job_value(world, Np, e2e_steps, e2e_t)
     ctx.close()
     if closure is not None:
         closure.close()
