@@ -751,7 +751,7 @@ static int nu_prepare(mgp_ctx *c, double A) {
     MGP_CUDA(cudaMalloc(&c->nu_row_d, sizeof(double) * 2 * nx));
     MGP_CUDA(cudaMalloc(&c->nu_x_d, sizeof(double) * nx));
     MGP_CUDA(cudaMalloc(&c->nu_den_d, sizeof(double) * nrk));
-    MGP_CUDA(cudaMalloc(&c->nu_tab_d, sizeof(double) * nrk));
+    MGP_CUDA(cudaMalloc(&c->nu_tab_d, sizeof(float) * nrk));
     for (int q = 0; q < 2; q++) MGP_CUDA(cudaEventCreateWithFlags(&c->nu_ev[q], cudaEventDisableTiming));
     std::vector<double> den(nrk);
     mgp_cosmo_nu_den(&c->cosmo, N, nrk, den.data());

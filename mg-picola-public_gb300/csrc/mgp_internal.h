@@ -98,7 +98,8 @@ struct mgp_ctx {
    * of value + d/d ln k, alternating per step, each reusable once its upload
    * event has passed), its device copy and ln k nodes, the T_cb(k, 1)
    * denominators and the factor table per integer |k|^2 on the device */
-  double *nu_row_h, *nu_row_d, *nu_x_d, *nu_den_d, *nu_tab_d;
+  double *nu_row_h, *nu_row_d, *nu_x_d, *nu_den_d;
+  float *nu_tab_d;
   int nu_nx;
   cudaEvent_t nu_ev[2];
   int nu_slot;
@@ -268,9 +269,9 @@ int mgp_launch_ikd(const float *frc, long long grid_floats, int N, long long P, 
                    double *partials, int nblocks, const mgp_kd_args *a, cudaStream_t st, int nbox = 1,
                    const mgp_box_scalars *bs = NULL);
 int mgp_ikd_blocks(long long np);
-int mgp_launch_nu_table(double *tab, int nrk, double kfac, double fac, const double *x, const double *val,
+int mgp_launch_nu_table(float *tab, int nrk, double kfac, double fac, const double *x, const double *val,
                         const double *dval, int nx, const double *den, cudaStream_t st);
-int mgp_launch_nu_add(float *dk, const float *dk0, int N, double cdmfac, const double *nufac, cudaStream_t st);
+int mgp_launch_nu_add(float *dk, const float *dk0, int N, double cdmfac, const float *nufac, cudaStream_t st);
 int mgp_launch_cic_unit(const double *pos, long long n, int N, long long P, float wpar, float *rho, cudaStream_t st);
 int mgp_launch_ic_from_density(float *dk, int N, int Ns, double normfac, const double *gc, const double *rescale,
                                cudaStream_t st);

@@ -853,20 +853,26 @@ int mgp_launch_ic_delta(const uint32_t *seedtable, const double *amp_rk, const u
 // Massive neutrinos in the density (src/auxPM.c:383-428): delta(k) <-
 // cdmfac delta(k) + nufac[|k|^2] delta_IC(k) with delta_IC the stored linear
 // CDM+baryon field of the IC (cdelta_cdm); the k = 0 mode is left as it is.
-__global__ void k_nu_add(float2 *__restrict__ dk, const float2 *__restrict__ dk0, int N, double cdmfac,
-                         const double *__restrict__ nufac) {
+// One warp per (i, j) row of the half-complex grid, lanes along kz; FP32
+// arithmetic (the grids are FP32, and FP64 runs at a small fraction of the
+// FP32 rate on this part).
+__global__ void k_nu_add(float2 *__restrict__ dk, const float2 *__restrict__ dk0, int N, float cdmfac,
+                         const float *__restrict__ nufac) {
   const int NH = N / 2 + 1;
-  const long long n = (long long)N * N * NH;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
-    if (q == 0) continue;
-    const int kz = (int)(q % NH);
-    const long long r = q / NH;
-    const int j = (int)(r % N), i = (int)(r / N);
+  const int lane = threadIdx.x & 31;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = wid; r < (long long)N * N; r += nw) {
+    const int i = (int)(r / N), j = (int)(r - (long long)i * N);
     const int di = i > N / 2 ? N - i : i, dj = j > N / 2 ? N - j : j;
-    const double f = nufac[(long long)di * di + (long long)dj * dj + (long long)kz * kz];
-    const float2 a = dk[q], b = dk0[q];
-    dk[q] = make_float2((float)(cdmfac * a.x + f * b.x), (float)(cdmfac * a.y + f * b.y));
+    const int r2 = di * di + dj * dj;
+    for (int kz = lane; kz < NH; kz += 32) {
+      if (r == 0 && kz == 0) continue;
+      const long long c = r * NH + kz;
+      const float f = nufac[r2 + kz * kz];
+      const float2 a = dk[c], b = dk0[c];
+      dk[c] = make_float2(fmaf(f, b.x, cdmfac * a.x), fmaf(f, b.y, cdmfac * a.y));
+    }
   }
 }
 
@@ -874,12 +880,12 @@ __global__ void k_nu_add(float2 *__restrict__ dk, const float2 *__restrict__ dk0
 // fac T_nu(k, a) / den[rk] at k = kfac sqrt(rk), T_nu the cubic Hermite in
 // ln k of the transfer row (val, dval on the nodes x), clamped to the table
 // as Lookup_GSL_2D_Spline does (src/wrappers.c:129-136).
-__global__ void k_nu_table(double *__restrict__ tab, int nrk, double kfac, double fac, const double *__restrict__ x,
+__global__ void k_nu_table(float *__restrict__ tab, int nrk, double kfac, double fac, const double *__restrict__ x,
                            const double *__restrict__ val, const double *__restrict__ dval, int nx,
                            const double *__restrict__ den) {
   for (int rk = blockIdx.x * blockDim.x + threadIdx.x; rk < nrk; rk += gridDim.x * blockDim.x) {
     if (rk == 0) {
-      tab[0] = 0.0;
+      tab[0] = 0.0f;
       continue;
     }
     double xv = log(kfac * sqrt((double)rk));
@@ -893,11 +899,11 @@ __global__ void k_nu_table(double *__restrict__ tab, int nrk, double kfac, doubl
     const double dx = x[lo + 1] - x[lo], t = (xv - x[lo]) / dx;
     const double T = (1 + 2 * t) * (1 - t) * (1 - t) * val[lo] + t * t * (3 - 2 * t) * val[lo + 1] +
                      t * (1 - t) * (1 - t) * dx * dval[lo] + t * t * (t - 1) * dx * dval[lo + 1];
-    tab[rk] = fac * T / den[rk];
+    tab[rk] = (float)(fac * T / den[rk]);
   }
 }
 
-int mgp_launch_nu_table(double *tab, int nrk, double kfac, double fac, const double *x, const double *val,
+int mgp_launch_nu_table(float *tab, int nrk, double kfac, double fac, const double *x, const double *val,
                         const double *dval, int nx, const double *den, cudaStream_t st) {
   k_nu_table<<<blocks_for(nrk, 4), MGP_THREADS, 0, st>>>(tab, nrk, kfac, fac, x, val, dval, nx, den);
   MGP_CHECK_LAUNCH();
@@ -905,9 +911,10 @@ int mgp_launch_nu_table(double *tab, int nrk, double kfac, double fac, const dou
   return MGP_OK;
 }
 
-int mgp_launch_nu_add(float *dk, const float *dk0, int N, double cdmfac, const double *nufac, cudaStream_t st) {
-  const long long n = (long long)N * N * (N / 2 + 1);
-  k_nu_add<<<blocks_for(n, 8), MGP_THREADS, 0, st>>>((float2 *)dk, (const float2 *)dk0, N, cdmfac, nufac);
+int mgp_launch_nu_add(float *dk, const float *dk0, int N, double cdmfac, const float *nufac, cudaStream_t st) {
+  const long long rows = (long long)N * N;
+  k_nu_add<<<blocks_for(rows * 32, 8), MGP_THREADS, 0, st>>>((float2 *)dk, (const float2 *)dk0, N, (float)cdmfac,
+                                                             nufac);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
