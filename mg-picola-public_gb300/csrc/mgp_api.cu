@@ -774,13 +774,14 @@ static int nu_prepare(mgp_ctx *c, double A) {
 
 // delta(k) becomes the total matter density, cdmfac delta_cdm(k) + the
 // neutrino term grown from the stored IC field, and its P(k) ("total") is
-// binned.
-static int add_neutrinos(mgp_ctx *c, double A) {
+// binned; that pass also writes the fifth-force filter output (fuse_kind),
+// which the MG solver reads from the total field.
+static int add_neutrinos(mgp_ctx *c, double A, int fuse_kind) {
   if (!c->sd_dk[0]) return mgp_set_error(MGP_ESTATE, "massive neutrinos need the scale-dependent IC field");
   RET_IF(mgp_launch_nu_add(c->dk, c->sd_dk[0], c->g.N, c->nu_cdmfac, c->nu_tab_d, c->stream));
   if (c->p.pofk_compute_every_step) {
     if (!c->pk_sum_tot) MGP_CUDA(cudaMalloc(&c->pk_sum_tot, sizeof(double) * c->pk_nbins));
-    RET_IF(pofk_now(c, 0, A, c->pk_sum_tot));
+    RET_IF(pofk_now(c, fuse_kind, A, c->pk_sum_tot));
   }
   return MGP_OK;
 }
@@ -813,14 +814,14 @@ static int fields_from_density(mgp_ctx *c, double A) {
   c->last_density_a = A;
   int fused = 0;
   if (c->p.pofk_compute_every_step) {
-    // with massive neutrinos the fifth-force filter reads the total field,
-    // so it is not fused into the CDM P(k) pass
-    fused = c->cosmo.nu ? 0 : mg_filter_kind(&c->p);
+    // with massive neutrinos the fifth-force filter reads the total field:
+    // it is fused into the total P(k) pass instead of the CDM one
+    fused = mg_filter_kind(&c->p);
     tstart(c, T_POFK);
-    RET_IF(pofk_now(c, fused, A));
+    RET_IF(pofk_now(c, c->cosmo.nu ? 0 : fused, A));
     tstop(c, T_POFK);
   }
-  if (c->cosmo.nu) RET_IF(add_neutrinos(c, A));
+  if (c->cosmo.nu) RET_IF(add_neutrinos(c, A, fused));
   int mg_kind = 0;
   float coupling = 0.f, mass2 = 0.f;
   tstart(c, T_MG);
