@@ -22,7 +22,7 @@ sys.path.insert(0, ROOT)
 from oracle import ref_build  # noqa: E402
 from tests.golden import camb_tables  # noqa: E402
 
-BASE = dict(Nmesh=32, Nsample=16, Box=128.0, Init_Redshift=19.0, Seed=4242, nsteps=5)
+BASE = dict(Nmesh=32, Nsample=16, Box=128.0, Init_Redshift=19.0, Seed=4242, nsteps=5, rsd=0)
 COSMO = dict(Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96)
 
 CASES = {
@@ -47,13 +47,17 @@ CASES = {
                                nu_include_massive_neutrinos=1, nu_SumMassNuEV=camb_tables.SUM_MNU_EV)),
     "fofr_nu": ("FOFRNU", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1,
                                nu_include_massive_neutrinos=1, nu_SumMassNuEV=camb_tables.SUM_MNU_EV)),
+    # redshift-space multipoles (compute_RSD_powerspectrum): at the output
+    # (pofk_compute_rsd_pofk 2), and every step plus the output (1)
+    "lcdm_rsd": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1), dict(rsd=2)),
+    "fofr_rsd": ("FOFR_LCDM", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1), dict(rsd=1)),
 }
 
 STD = """use_lcdm_growth_factors  0
 input_pofk_is_for_lcdm   0
 input_sigma8_is_for_lcdm 1
 pofk_compute_every_step   1
-pofk_compute_rsd_pofk     0
+pofk_compute_rsd_pofk     {rsd}
 pofk_nbins                16
 pofk_bintype              0
 pofk_subtract_shotnoise   0
@@ -108,6 +112,9 @@ def run_reference(model, mg, base=None, cosmo=None, nu_info=None):
         if log.returncode != 0:
             raise RuntimeError(model + ": " + log.stdout[-2000:] + log.stderr[-2000:])
         out = dict(pk=np.loadtxt(os.path.join(d, "pofk_run_z0.000_CDM.txt")))
+        for f in sorted(os.listdir(d)):
+            if f.startswith("pofk_RSD_run_z"):
+                out["rsd_" + f[len("pofk_RSD_run_z"):-4]] = np.loadtxt(os.path.join(d, f))
         if "nu_SumMassNuEV" in mg:
             out["pk_total"] = np.loadtxt(os.path.join(d, "pofk_run_z0.000_total.txt"))
         raw = open(os.path.join(d, "run_z0p000.0"), "rb").read()
@@ -117,21 +124,22 @@ def run_reference(model, mg, base=None, cosmo=None, nu_info=None):
     return out
 
 
-def run_case(name, model, mg):
+def run_case(name, model, mg, base=None):
     mgd = dict(inverted_initial_condition=0, amplitude_fixed_initial_condition=0)
     mgd.update(mg)
-    r = run_reference(model, mgd)
+    r = run_reference(model, mgd, base=base)
     n = BASE["Nsample"] ** 3
     idx = np.arange(0, n, 8)
-    extra = {"pk_total": r["pk_total"]} if "pk_total" in r else {}
+    extra = {k: v for k, v in r.items() if k == "pk_total" or k.startswith("rsd_")}
     np.savez(os.path.join(ROOT, "tests", "golden", "ref_%s.npz" % name), pk=r["pk"], idx=idx, pos=r["pos"][idx],
-             vel=r["vel"][idx], model=model, **{k: float(v) for k, v in mgd.items()}, **BASE, **extra)
+             vel=r["vel"][idx], model=model, **{k: float(v) for k, v in mgd.items()}, **dict(BASE, **(base or {})),
+             **extra)
     print(name, "bins", r["pk"].shape[0])
 
 if __name__ == "__main__":
     ref_build.build()
     # optional case names on the command line regenerate only those
-    for name, (model, mg) in CASES.items():
+    for name, case in CASES.items():
         if len(sys.argv) > 1 and name not in sys.argv[1:]:
             continue
-        run_case(name, model, mg)
+        run_case(name, *case)

@@ -1,0 +1,114 @@
+"""The CUDA path's mgp_run against the reference's own runs.
+
+tests/golden/ref_*.npz hold the output of MG-PICOLA's unmodified sources
+compiled against single-rank shims and run here (tests/golden/make_golden.py):
+the final CDM P(k) file (and the total one of the neutrino build), the
+redshift-space multipole files (compute_RSD_powerspectrum,
+src/compute_pofk.c:403-512) where the case asked for them, and a subsample of
+the final GADGET snapshot.  Every case is rerun here through mgp_run with the
+same parameters and white-noise stream.  FP32 path vs FP64 reference over 5
+steps: P(k) within 1e-3 relative; multipoles within 1e-3 of max |P0| (P2 and
+P4 cross zero); positions rms < 1e-3 of the particle spacing; velocities 1e-3
+relative rms.
+"""
+import glob
+import os
+import struct
+
+import numpy as np
+import pytest
+
+import mgpicola as M
+from golden import camb_tables
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_*.npz")))
+
+
+def _f(g, k, default=0.0):
+    return float(g[k]) if k in g.files else default
+
+
+def params_for(g, out, tmp):
+    model = str(g["model"])
+    d = dict(Nmesh=int(g["Nmesh"]), Nsample=int(g["Nsample"]), Box=float(g["Box"]), Seed=int(g["Seed"]),
+             Init_Redshift=float(g["Init_Redshift"]), pofk_nbins=16, pofk_bintype=0, pofk_kmin=0.0, pofk_kmax=0.0,
+             pofk_compute_every_step=1, pofk_subtract_shotnoise=0, pofk_compute_rsd_pofk=int(_f(g, "rsd")),
+             input_pofk_is_for_lcdm=0, input_sigma8_is_for_lcdm=1, use_lcdm_growth_factors=0,
+             amplitude_fixed_initial_condition=int(_f(g, "amplitude_fixed_initial_condition")),
+             inverted_initial_condition=int(_f(g, "inverted_initial_condition")),
+             Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96, WhichSpectrum=2,
+             UseCOLA=1, OutputDir=out, FileBase="run", Noutputs=1,
+             modified_gravity_active=int(_f(g, "modified_gravity_active")),
+             include_screening=int(_f(g, "include_screening", 1)))
+    if model.startswith("FOFR"):
+        d.update(model=M.MODEL_FOFR, fofr0=_f(g, "fofr0"), nfofr=_f(g, "nfofr"))
+    elif model == "DGP":
+        d.update(model=M.MODEL_DGP, rcH0_DGP=_f(g, "rcH0_DGP"), Rsmooth=_f(g, "Rsmooth"),
+                 smoothing_filter=M.FILTER_GAUSSIAN)
+    elif model == "BRANSDICKE":
+        d.update(model=M.MODEL_BRANSDICKE, wBD=_f(g, "wBD"), Omegah2=_f(g, "Omegah2"), Omegarh2=_f(g, "Omegar2"),
+                 Omegavh2=_f(g, "Omegav2"))
+    elif model.startswith("MBETA"):
+        d.update(model=M.MODEL_MBETA, range_symm=_f(g, "range_symm"), assb_symm=_f(g, "assb_symm"),
+                 beta_symm=_f(g, "beta_symm"))
+    if model in ("FOFR", "MBETA", "FOFRNU"):
+        d.update(scaledependent=1)
+    if model == "FOFRNU":
+        d.update(massive_neutrinos=1, nu_include_massive_neutrinos=int(_f(g, "nu_include_massive_neutrinos")),
+                 nu_SumMassNuEV=_f(g, "nu_SumMassNuEV"),
+                 nu_FilenameTransferInfofile=camb_tables.write_tables(os.path.join(tmp, "camb")))
+    p = M.default_params(**d)
+    p.output_redshift[0], p.output_nsteps[0] = 0.0, int(g["nsteps"])
+    return p
+
+
+def rel_rms(a, b):
+    return float(np.sqrt(np.mean((np.asarray(a, np.float64) - b) ** 2) / np.mean(np.asarray(b, np.float64) ** 2)))
+
+
+def max_rel(a, b):
+    return float(np.max(np.abs(a - b) / np.abs(b)))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[4:-4] for p in GOLDEN])
+def test_run_matches_reference_run(path, tmp_path):
+    g = np.load(path)
+    out = str(tmp_path / "out")
+    os.makedirs(out)
+    p = params_for(g, out, str(tmp_path))
+    with M.Context(p) as ctx:
+        ctx.run(gadget=True)
+    pk = np.loadtxt(os.path.join(out, "pofk_run_z0.000_CDM.txt"))
+    assert pk.shape == g["pk"].shape
+    np.testing.assert_allclose(pk[:, 0], g["pk"][:, 0], atol=6e-6)
+    assert max_rel(pk[:, 1], g["pk"][:, 1]) < 1e-3
+    if "pk_total" in g.files:
+        tot = np.loadtxt(os.path.join(out, "pofk_run_z0.000_total.txt"))
+        assert max_rel(tot[:, 1], g["pk_total"][:, 1]) < 1e-3
+    rsd = [k for k in g.files if k.startswith("rsd_")]
+    for key in rsd:
+        ref = g[key]
+        got = np.loadtxt(os.path.join(out, "pofk_RSD_run_z%s.txt" % key[4:]))
+        assert got.shape == ref.shape, key
+        np.testing.assert_allclose(got[:, 0], ref[:, 0], atol=6e-6)
+        scale = np.abs(ref[:, 1]).max()
+        # P0, P2, P4 and the y/z-LOS differences (sigma columns)
+        assert np.abs(got[:, 1:] - ref[:, 1:]).max() < 1e-3 * scale, key
+    n = p.Nsample ** 3
+    raw = open(os.path.join(out, "run_z0p000.0"), "rb").read()
+    pos = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3)
+    vel = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3)
+    idx = g["idx"]
+    dx = np.abs(pos[idx] - g["pos"])
+    dx = np.minimum(dx, p.Box - dx)
+    assert np.sqrt(np.mean(dx ** 2)) < 1e-3 * p.Box / p.Nsample
+    assert rel_rms(vel[idx], g["vel"]) < 1e-3
+
+
+def test_golden_rsd_cases_present():
+    names = [os.path.basename(p) for p in GOLDEN]
+    assert "ref_lcdm_rsd.npz" in names and "ref_fofr_rsd.npz" in names
+    g = np.load(os.path.join(os.path.dirname(GOLDEN[0]), "ref_fofr_rsd.npz"))
+    assert len([k for k in g.files if k.startswith("rsd_")]) == 5  # four steps and the output
