@@ -258,6 +258,12 @@ typedef struct {
   int pofk_nbins, pofk_bintype, pofk_subtract_shotnoise;
   double pofk_kmin, pofk_kmax;
   int usecola;
+  /* ReadParticlesFromFile: the IC from these particles (positions in [0,1),
+   * [n][3]) and the P(k) rescaling per integer |k|^2, instead of the
+   * Gaussian field; NULL for the Gaussian IC */
+  const double *ic_pos01;
+  long ic_n;
+  const double *ic_rescale_rk;
 } orc_run_params;
 /* Runs IC + the KDK loop of src/main.c:394-611 for one output redshift.
  * pos/vel out [Ns^3][3] at the final time (vel incl. LPT part as written by

@@ -27,9 +27,15 @@ int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
     V1 = malloc(8 * 3 * np);
     V2 = malloc(8 * 3 * np);
   }
-  orc_ic_2lpt(&rp->ic, &rp->pw, D1, D2, cdelta, cdelta2);
-
   double A = 1.0 / (1.0 + rp->init_redshift);
+  if (rp->ic_pos01) {
+    /* ReadFilesMakeDisplacementField (src/readICfromfile.c:533-700):
+     * delta(k) of the particles x D_LCDM(1)/D_LCDM(a_i)/N^3 */
+    const double normfac = 1.0 / ((double)N * N * N) / orc_growth_DLCDM(c, A);
+    orc_ic_2lpt_from_particles(&rp->ic, rp->ic_pos01, rp->ic_n, normfac, rp->ic_rescale_rk, D1, D2, cdelta, cdelta2);
+  } else {
+    orc_ic_2lpt(&rp->ic, &rp->pw, D1, D2, cdelta, cdelta2);
+  }
   double Di = orc_growth_D(c, A), Di2 = orc_growth_D2(c, A);
   if (sd) {
     /* main.c:244-251 */

@@ -30,7 +30,11 @@ MODELS = {
     "FOFR": ["-DFOFRGRAVITY", "-DSCALEDEPENDENT"],
     "MBETA": ["-DMBETAMODEL", "-DSCALEDEPENDENT"],
     "FOFRNU": ["-DFOFRGRAVITY", "-DMASSIVE_NEUTRINOS", "-DSCALEDEPENDENT"],
+    # initial conditions read from particle files (src/readICfromfile.c)
+    "FOFR_LCDM_IC": ["-DFOFRGRAVITY", "-DREADICFROMFILE"],
 }
+# sources a build adds to SOURCES
+EXTRA_SOURCES = {"FOFR_LCDM_IC": ["readICfromfile.c"]}
 
 
 def available():
@@ -54,8 +58,9 @@ def build(models=None, verbose=False):
         out = binary(model)
         if os.path.exists(out) and os.path.getmtime(out) >= newest:
             continue
+        extra = [os.path.join(REF_SRC, f) for f in EXTRA_SOURCES.get(model, [])]
         cmd = (["gcc", "-O2", "-std=gnu99", "-fopenmp", "-w", "-o", out] + COMMON + MODELS[model] + inc + srcs +
-               ["-lm"])
+               extra + ["-lm"])
         if verbose:
             print(" ".join(cmd))
         subprocess.check_call(cmd)

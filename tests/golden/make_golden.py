@@ -20,7 +20,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 from oracle import ref_build  # noqa: E402
-from tests.golden import camb_tables  # noqa: E402
+from tests.golden import camb_tables, particle_files  # noqa: E402
 
 BASE = dict(Nmesh=32, Nsample=16, Box=128.0, Init_Redshift=19.0, Seed=4242, nsteps=5, rsd=0)
 COSMO = dict(Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96)
@@ -49,6 +49,11 @@ CASES = {
                                nu_include_massive_neutrinos=1, nu_SumMassNuEV=camb_tables.SUM_MNU_EV)),
     # redshift-space multipoles (compute_RSD_powerspectrum): at the output
     # (pofk_compute_rsd_pofk 2), and every step plus the output (1)
+    # initial conditions from two GADGET-1 files of a displaced 20^3 lattice
+    # (particle_files.py), READICFROMFILE build
+    "lcdm_icfile": ("FOFR_LCDM_IC", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1,
+                                         ReadParticlesFromFile=1, TypeInputParticleFiles=3, NumInputParticleFiles=2,
+                                         RamsesOutputNumber=0)),
     "lcdm_rsd": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1), dict(rsd=2)),
     "fofr_rsd": ("FOFR_LCDM", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1), dict(rsd=1)),
 }
@@ -105,6 +110,9 @@ def run_reference(model, mg, base=None, cosmo=None, nu_info=None):
         if "nu_SumMassNuEV" in mg:
             info = nu_info or camb_tables.write_tables(os.path.join(d, "camb"))
             txt += "nu_FilenameTransferInfofile %s\n" % info
+        if mg.get("ReadParticlesFromFile"):
+            icdir = particle_files.write_ic_files(os.path.join(d, "ic"), base["Box"])
+            txt += "InputParticleFileDir %s\nInputParticleFilePrefix ics\n" % icdir
         pf = os.path.join(d, "params.txt")
         with open(pf, "w") as f:
             f.write(txt)

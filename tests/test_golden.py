@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from golden import camb_tables
+from golden import camb_tables, particle_files
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_*.npz")))
 
@@ -55,6 +55,16 @@ def oracle_run(g, tmpdir=None):
     rp.pofk_nbins, rp.pofk_bintype, rp.pofk_subtract_shotnoise = 16, 0, 0
     rp.pofk_kmin, rp.pofk_kmax = 0.0, 0.0
     rp.usecola = 1
+    keep = []
+    if "ReadParticlesFromFile" in g.files and int(g["ReadParticlesFromFile"]):
+        # the particle files the fixture was made from, read as the reference
+        # reads them (float positions / BoxSize, wrapped)
+        pos = particle_files.displaced_lattice(20, box)
+        u = (pos.astype(np.float64) * (1.0 / box)).astype(np.float32)
+        u = np.where(u >= 1.0, (u - np.float32(1.0)).astype(np.float32), u).astype(np.float64)
+        resc = np.ones(3 * (N // 2) ** 2 + 1)
+        keep += [np.ascontiguousarray(u), resc]
+        rp.ic_pos01, rp.ic_n, rp.ic_rescale_rk = keep[0].ctypes.data, len(u), resc.ctypes.data
     n = Ns ** 3
     pos, vel = np.zeros((n, 3)), np.zeros((n, 3))
     kb, pk, km, nm = (np.zeros(N) for _ in range(4))

@@ -2,7 +2,8 @@
 
 tests/golden/ref_*.npz hold the output of MG-PICOLA's unmodified sources
 compiled against single-rank shims and run here (tests/golden/make_golden.py):
-the final CDM P(k) file (and the total one of the neutrino build), the
+the final CDM P(k) file (and the total one of the neutrino build; the
+READICFROMFILE build starts from two GADGET-1 particle files), the
 redshift-space multipole files (compute_RSD_powerspectrum,
 src/compute_pofk.c:403-512) where the case asked for them, and a subsample of
 the final GADGET snapshot.  Every case is rerun here through mgp_run with the
@@ -13,13 +14,12 @@ relative rms.
 """
 import glob
 import os
-import struct
 
 import numpy as np
 import pytest
 
 import mgpicola as M
-from golden import camb_tables
+from golden import camb_tables, particle_files
 
 pytestmark = pytest.mark.gpu
 
@@ -42,6 +42,11 @@ def params_for(g, out, tmp):
              UseCOLA=1, OutputDir=out, FileBase="run", Noutputs=1,
              modified_gravity_active=int(_f(g, "modified_gravity_active")),
              include_screening=int(_f(g, "include_screening", 1)))
+    if model == "FOFR_LCDM_IC":
+        # two GADGET-1 files of the displaced lattice the fixture was made from
+        d.update(ReadParticlesFromFile=1, TypeInputParticleFiles=3, NumInputParticleFiles=2, RamsesOutputNumber=0,
+                 InputParticleFileDir=particle_files.write_ic_files(os.path.join(tmp, "ic"), d["Box"]),
+                 InputParticleFilePrefix="ics")
     if model.startswith("FOFR"):
         d.update(model=M.MODEL_FOFR, fofr0=_f(g, "fofr0"), nfofr=_f(g, "nfofr"))
     elif model == "DGP":

@@ -8,20 +8,8 @@ import numpy as np
 import pytest
 
 import mgpicola as M
+from golden.particle_files import gadget_file  # noqa: F401  (also imported by test_gpu_icfile)
 from test_host import write_param
-
-
-def gadget_file(path, pos_box, box):
-    """GADGET-1 file with type-1 positions (Box units) and zero velocities."""
-    n = len(pos_box)
-    hdr = struct.pack("<6I6dddii6Iiiddddii6Ii", 0, n, 0, 0, 0, 0, *([0.0] * 6), 0.1, 9.0, 0, 0, 0, n, 0, 0, 0, 0, 0, 1,
-                      box, 0.267, 0.733, 0.71, 0, 0, 0, 0, 0, 0, 0, 0, 0)
-    hdr += b"\0" * (256 - len(hdr))
-    blk = np.ascontiguousarray(pos_box, "<f4").tobytes()
-    with open(path, "wb") as f:
-        f.write(struct.pack("<i", 256) + hdr + struct.pack("<i", 256))
-        f.write(struct.pack("<i", len(blk)) + blk + struct.pack("<i", len(blk)))
-        f.write(struct.pack("<i", len(blk)) + bytes(len(blk)) + struct.pack("<i", len(blk)))
 
 
 def ascii_file(path, pos01):
