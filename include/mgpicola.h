@@ -296,7 +296,8 @@ double mgp_power_spectrum(mgp_ctx *ctx, double k);
  * mgp_growth, 7 the linear P(k) at x = k (h/Mpc), 8 mg_pofk_ratio(k = x,
  * a = 1), 9 mg_sigma8_enhancement(a = x) (src/cosmo.c:688-756);
  * mgp_cosmo_coeff gives Sq (kind 0) or Sphi (kind 1) for n triples
- * (ai, af, aref). */
+ * (ai, af, aref), or SqStd (2) / SphiStd (3) of (ai, af), the coefficients
+ * of a run with UseCOLA = 0 (src/cosmo.c:1165-1200). */
 int mgp_cosmo_eval(const mgp_params *p, int which, const double *x, int n, double *out);
 /* growth_*_scaledependent(k, a) (src/cosmo.c:987-1010) of a parameter set
  * with scaledependent = 1, host only: which 0 D, 1 dD/dy, 2 d2D/dy2, 3 D2,

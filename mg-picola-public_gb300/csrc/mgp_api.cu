@@ -509,6 +509,9 @@ static int ic_box(mgp_ctx *c, int bx, const double *pos01 = NULL, size_t npos = 
   const long long gf = c->g.nreal;
   const double Di = mgp_cosmo_growth(cb, 0, 1.0 / (1.0 + pb->Init_Redshift));
   const double Di2 = mgp_cosmo_growth(cb, 3, 1.0 / (1.0 + pb->Init_Redshift));
+  // without COLA the particles start with the 2LPT velocity (main.c:276-283)
+  const double vD = pb->UseCOLA ? 0.0 : mgp_cosmo_growth(cb, 1, 1.0 / (1.0 + pb->Init_Redshift));
+  const double vD2 = pb->UseCOLA ? 0.0 : mgp_cosmo_growth(cb, 4, 1.0 / (1.0 + pb->Init_Redshift));
   const int nblk = mgp_ikd_blocks(c->np);
 #define CK(x)                      \
   do {                             \
@@ -604,7 +607,7 @@ static int ic_box(mgp_ctx *c, int bx, const double *pos01 = NULL, size_t npos = 
   for (int g = 3; g < 6; g++) CKF(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(g6 + g * gf), (cufftReal *)(g6 + g * gf)));
   CK(mgp_launch_ic_readout(g6, gf, N, c->g.P, Ns, c->D1 + po, c->D2 + po, c->partials, nblk, c->stream));
   CK(mgp_launch_ic_finish(c->D1 + po, c->D2 + po, c->s + po, c->v + po, c->np, c->partials, nblk, (float)Di,
-                          (float)Di2, 0.0, c->stream));
+                          (float)Di2, (float)vD, (float)vD2, c->stream));
   CKC(cudaMemsetAsync(c->dstate + bx, 0, sizeof(mgp_dstate), c->stream));
   CKC(cudaStreamSynchronize(c->stream));
   c->have_density = c->have_forces = 0;
@@ -847,7 +850,7 @@ static int fields_from_density(mgp_ctx *c, double A) {
 static void kd_args(mgp_ctx *c, double AI, double AF, double A, double AFF, int do_drift, mgp_kd_args *a) {
   const mgp_cosmo *cs = &c->cosmo;
   const double om = c->p.Omega, cola = c->p.UseCOLA ? 1.0 : 0.0;
-  double dda = mgp_cosmo_Sphi(cs, AI, AF, A);  // StdDA = 0 (main.c:696-697)
+  double dda = mgp_cosmo_kick_dda(cs, AI, AF, A);  // StdDA 0 (COLA) or 2 (main.c:696-701)
   memset(a, 0, sizeof(*a));
   a->scale = (float)(c->g.N / c->p.Box);
   a->inv_scale = (float)(c->p.Box / c->g.N);
@@ -869,7 +872,7 @@ static void kd_args(mgp_ctx *c, double AI, double AF, double A, double AFF, int 
     a->lpt_pitch = c->Ns;
   }
   if (do_drift) {
-    double dyyy = mgp_cosmo_Sq(cs, A, AFF, AF);
+    double dyyy = mgp_cosmo_drift_dyyy(cs, A, AFF, AF);
     a->dyyy = (float)dyyy;
     a->dyyy_d = dyyy;
     if (c->sd) {
@@ -1256,7 +1259,7 @@ static void batch_schedule(const mgp_ctx *c, int nsteps, double zf, std::vector<
                            std::vector<mgp_box_scalars> &bs) {
   const mgp_params *p = &c->p;
   const double A0 = 1.0 / (1.0 + p->Init_Redshift), ao = 1.0 / (1.0 + zf);
-  const double da = (ao - A0) / (double)nsteps, cola = p->UseCOLA ? 1.0 : 0.0, om = p->Omega;
+  const double da = mgp_cosmo_step_da(p, A0, ao, nsteps), cola = p->UseCOLA ? 1.0 : 0.0, om = p->Omega;
   st.assign(nsteps + 1, batch_step());
   bs.assign((size_t)(nsteps + 1) * c->nbox, mgp_box_scalars());
   double A = A0, AI = A0;
@@ -1265,10 +1268,10 @@ static void batch_schedule(const mgp_ctx *c, int nsteps, double zf, std::vector<
     q.drift = t < nsteps;
     q.A = A;
     q.AI = AI;
-    q.AF = q.drift ? A + 0.5 * da : A;
-    q.AFF = A + da;
+    q.AF = q.drift ? mgp_cosmo_step_mid(p, A, da) : A;
+    q.AFF = mgp_cosmo_step_end(p, A, da);
     const mgp_cosmo *c0 = &c->cosmo;
-    double dda = mgp_cosmo_Sphi(c0, q.AI, q.AF, A);
+    double dda = mgp_cosmo_kick_dda(c0, q.AI, q.AF, A);
     memset(&q.kd, 0, sizeof(q.kd));
     q.kd.scale = (float)(c->g.N / p->Box);
     q.kd.inv_scale = (float)(p->Box / c->g.N);
@@ -1278,7 +1281,7 @@ static void batch_schedule(const mgp_ctx *c, int nsteps, double zf, std::vector<
     q.kd.lpt_stride = c->np;
     q.kd.lpt_pitch = c->Ns;
     if (q.drift) {
-      double dyyy = mgp_cosmo_Sq(c0, A, q.AFF, q.AF);
+      double dyyy = mgp_cosmo_drift_dyyy(c0, A, q.AFF, q.AF);
       q.kd.dyyy = (float)dyyy;
       q.kd.dyyy_d = dyyy;
     }

@@ -860,6 +860,28 @@ double mgp_cosmo_Sq(const mgp_cosmo *c, double ai, double af, double aref) {
 double mgp_cosmo_Sphi(const mgp_cosmo *c, double ai, double af, double aref) {
   return (pow(af, -2.5) - pow(ai, -2.5)) * aref / Qfactor(c, aref) / (-2.5 * pow(aref, -3.5));
 }
+/* Quinn et al. time stepping of the non-COLA run (StdDA = 2, main.c:75-81):
+ * SqStd = int_ai^af da / Q(a), SphiStd = int_ai^af a da / Q(a)
+ * (src/cosmo.c:1165-1200) */
+static double sqstd_integrand(double a, const void *par) { return 1.0 / Qfactor((const mgp_cosmo *)par, a); }
+static double sphistd_integrand(double a, const void *par) { return a / Qfactor((const mgp_cosmo *)par, a); }
+double mgp_cosmo_SqStd(const mgp_cosmo *c, double ai, double af) { return quad(sqstd_integrand, c, ai, af, 4); }
+double mgp_cosmo_SphiStd(const mgp_cosmo *c, double ai, double af) { return quad(sphistd_integrand, c, ai, af, 4); }
+/* main.c:400-455: the step in a (UseCOLA, stepDistr = 0) or in ln a
+ * (stepDistr = 1 otherwise): da from A to a_out in nsteps, and AF (mid
+ * point) / AFF (end) of the step starting at A */
+double mgp_cosmo_step_da(const mgp_params *p, double A, double aout, int nsteps) {
+  return p->UseCOLA ? (aout - A) / (double)nsteps : (log(aout) - log(A)) / (double)nsteps;
+}
+double mgp_cosmo_step_mid(const mgp_params *p, double A, double da) { return p->UseCOLA ? A + 0.5 * da : A * exp(0.5 * da); }
+double mgp_cosmo_step_end(const mgp_params *p, double A, double da) { return p->UseCOLA ? A + da : A * exp(da); }
+/* Kick and Drift coefficients of the run's StdDA (main.c:696-701, 751-757) */
+double mgp_cosmo_kick_dda(const mgp_cosmo *c, double ai, double af, double a) {
+  return c->p.UseCOLA ? mgp_cosmo_Sphi(c, ai, af, a) : mgp_cosmo_SphiStd(c, ai, af);
+}
+double mgp_cosmo_drift_dyyy(const mgp_cosmo *c, double a, double aff, double af) {
+  return c->p.UseCOLA ? mgp_cosmo_Sq(c, a, aff, af) : mgp_cosmo_SqStd(c, a, aff);
+}
 
 /* -------------------------------------------------------- power spectrum */
 /* Eisenstein & Hu no-wiggle transfer function (src/power.c:447-476). */
@@ -1289,6 +1311,7 @@ int mgp_growth_scaledependent(const mgp_params *p, int which, const double *k, c
 /* COLA coefficients for triples (ai, af, aref): kind 0 Sq, 1 Sphi. */
 int mgp_cosmo_coeff(const mgp_params *p, int kind, const double *ai, const double *af, const double *aref, int n,
                     double *out) {
+  if (kind < 0 || kind > 3) return mgp_set_error(MGP_EINVAL, "kind = %d out of range", kind);
   char err[512] = "";
   mgp_cosmo c;
   int rc = mgp_cosmo_init(&c, p, err, sizeof(err));
@@ -1296,8 +1319,14 @@ int mgp_cosmo_coeff(const mgp_params *p, int kind, const double *ai, const doubl
     mgp_cosmo_free(&c);
     return mgp_set_error(rc, "%s", err);
   }
-  for (int i = 0; i < n; i++)
-    out[i] = kind == 0 ? mgp_cosmo_Sq(&c, ai[i], af[i], aref[i]) : mgp_cosmo_Sphi(&c, ai[i], af[i], aref[i]);
+  for (int i = 0; i < n; i++) {
+    switch (kind) {
+      case 0: out[i] = mgp_cosmo_Sq(&c, ai[i], af[i], aref[i]); break;
+      case 1: out[i] = mgp_cosmo_Sphi(&c, ai[i], af[i], aref[i]); break;
+      case 2: out[i] = mgp_cosmo_SqStd(&c, ai[i], af[i]); break;
+      default: out[i] = mgp_cosmo_SphiStd(&c, ai[i], af[i]);
+    }
+  }
   mgp_cosmo_free(&c);
   return MGP_OK;
 }

@@ -85,6 +85,13 @@ double mgp_dgp_screen_prefactor(const mgp_cosmo *c, double a);
 double mgp_cosmo_growth(const mgp_cosmo *c, int which, double a);
 double mgp_cosmo_Sq(const mgp_cosmo *c, double ai, double af, double aref);
 double mgp_cosmo_Sphi(const mgp_cosmo *c, double ai, double af, double aref);
+double mgp_cosmo_SqStd(const mgp_cosmo *c, double ai, double af);
+double mgp_cosmo_SphiStd(const mgp_cosmo *c, double ai, double af);
+double mgp_cosmo_step_da(const mgp_params *p, double A, double aout, int nsteps);
+double mgp_cosmo_step_mid(const mgp_params *p, double A, double da);
+double mgp_cosmo_step_end(const mgp_params *p, double A, double da);
+double mgp_cosmo_kick_dda(const mgp_cosmo *c, double ai, double af, double a);
+double mgp_cosmo_drift_dyyy(const mgp_cosmo *c, double a, double aff, double af);
 
 /* PowerSpec (src/power.c:373-394) in (Mpc/h)^3, k in h/Mpc */
 double mgp_cosmo_power(const mgp_cosmo *c, double k);

@@ -308,7 +308,7 @@ int mgp_launch_output(const float *s, const float *v, const float *D1, const flo
 int mgp_launch_ic_readout(const float *g6, long long grid_floats, int N, long long P, int Ns,
                           float *D1, float *D2, double *partials, int nblocks, cudaStream_t st);
 int mgp_launch_ic_finish(float *D1, float *D2, float *s, float *v, long long np, const double *partials,
-                         int nblocks, float Di, float Di2, double inv_n3, cudaStream_t st);
+                         int nblocks, float Di, float Di2, float vD, float vD2, cudaStream_t st);
 int mgp_launch_finalize_kd(mgp_dstate *dst, const double *partials, int nblocks, long long np,
                            double dda_omega, double dyyy, int do_drift, cudaStream_t st);
 int mgp_launch_positions(const float *s, const mgp_dstate *dst, long long np, int Ns, double box,

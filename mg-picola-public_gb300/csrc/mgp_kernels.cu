@@ -1160,10 +1160,13 @@ int mgp_launch_ic_readout(const float *g6, long long gf, int N, long long P, int
   return MGP_OK;
 }
 
-// Mean removal (2LPT.c:1493-1508) and initial COLA state (main.c:257-309):
-// s = D1 Di + D2 Di2 (displacement from q), v = 0.
+// Mean removal (2LPT.c:1493-1508) and initial state (main.c:257-309):
+// s = D1 Di + D2 Di2 (displacement from q); v = D1 vD + D2 vD2, with
+// vD = vD2 = 0 for COLA and dD/dy, dD2/dy at a_i without it (the 2LPT
+// velocity, main.c:276-283).
 __global__ void k_ic_finish(float *__restrict__ D1, float *__restrict__ D2, float *__restrict__ s, float *__restrict__ v,
-                            long long np, const double *__restrict__ partials, int nblocks, float Di, float Di2) {
+                            long long np, const double *__restrict__ partials, int nblocks, float Di, float Di2,
+                            float vD, float vD2) {
   __shared__ float mean[6];
   if (threadIdx.x < 6) {
     double t = 0.0;
@@ -1179,15 +1182,14 @@ __global__ void k_ic_finish(float *__restrict__ D1, float *__restrict__ D2, floa
       D1[o] = d1;
       D2[o] = d2;
       s[o] = d1 * Di + d2 * Di2;
-      v[o] = 0.0f;
+      v[o] = d1 * vD + d2 * vD2;
     }
   }
 }
 
 int mgp_launch_ic_finish(float *D1, float *D2, float *s, float *v, long long np, const double *partials, int nblocks,
-                         float Di, float Di2, double inv_n3, cudaStream_t st) {
-  (void)inv_n3;
-  k_ic_finish<<<blocks_for(np, 8), MGP_THREADS, 0, st>>>(D1, D2, s, v, np, partials, nblocks, Di, Di2);
+                         float Di, float Di2, float vD, float vD2, cudaStream_t st) {
+  k_ic_finish<<<blocks_for(np, 8), MGP_THREADS, 0, st>>>(D1, D2, s, v, np, partials, nblocks, Di, Di2, vD, vD2);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;

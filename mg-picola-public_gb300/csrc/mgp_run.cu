@@ -216,12 +216,13 @@ static int run_loop(mgp_ctx *c, int gadget) {
     if (i != Noutputs) {
       nsteps = p->output_nsteps[i];
       double ao = 1.0 / (1.0 + p->output_redshift[i]);
-      da = (ao - A) / (double)nsteps;  // stepDistr = 0 for COLA (main.c:75-81)
+      // steps in a for COLA, in ln a otherwise (stepDistr, main.c:75-81, 400-404)
+      da = mgp_cosmo_step_da(p, A, ao, nsteps);
     }
     for (int ts = 0; ts < nsteps; ts++) {
       int output_step = (ts == 0) && (i != NoutputStart);
-      AF = output_step ? A : A + da * 0.5;
-      AFF = A + da;
+      AF = output_step ? A : mgp_cosmo_step_mid(p, A, da);
+      AFF = mgp_cosmo_step_end(p, A, da);
       // RSD every step except at outputs (src/compute_pofk.c call in auxPM.c:376-381)
       if (c->p.pofk_compute_rsd_pofk == 1 && !output_step) RET_IF(write_rsd_now(c, A));
       RET_IF(mgp_get_displacements(c, A));
@@ -241,7 +242,7 @@ static int run_loop(mgp_ctx *c, int gadget) {
         // the RSD deposits used the force grids as scratch: rebuild them at A
         if (!c->have_forces) RET_IF(mgp_get_displacements(c, A));
         AI = A;
-        AF = A + da * 0.5;
+        AF = mgp_cosmo_step_mid(p, A, da);
         RET_IF(mgp_kick_drift(c, AI, AF, A, AFF, 1));
       } else {
         RET_IF(mgp_kick_drift(c, AI, AF, A, AFF, 1));

@@ -248,7 +248,8 @@ def growth_scaledependent(params, which, k, a):
 
 
 def cosmo_coeff(params, kind, ai, af, aref):
-    """COLA Sq (kind 0) / Sphi (kind 1) on the host."""
+    """Kick/drift coefficients on the host: COLA Sq (kind 0) / Sphi (kind 1)
+    at aref, or the non-COLA SqStd (kind 2) / SphiStd (kind 3)."""
     ai, af, aref = (np.ascontiguousarray(v, dtype=np.float64) for v in (ai, af, aref))
     out = np.zeros_like(ai)
     _check(lib().mgp_cosmo_coeff(C.byref(params), kind, _dptr(ai), _dptr(af), _dptr(aref), ai.size, _dptr(out)))

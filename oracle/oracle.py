@@ -113,6 +113,10 @@ def lib():
             f = getattr(L, name)
             f.argtypes = [C.c_void_p, C.c_double]
             f.restype = C.c_double
+        for name in ["orc_SqStd", "orc_SphiStd"]:
+            f = getattr(L, name)
+            f.argtypes = [C.c_void_p, C.c_double, C.c_double]
+            f.restype = C.c_double
         for name in ["orc_Sq", "orc_Sphi"]:
             f = getattr(L, name)
             f.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]

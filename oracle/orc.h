@@ -198,6 +198,9 @@ double orc_mg_sigma8_enh(orc_cosmo *c, const struct orc_power_s *pw, double a);
 /* COLA coefficients (src/cosmo.c:1114-1160), nLPT = -2.5, fullT = 1. */
 double orc_Sq(orc_cosmo *c, double ai, double af, double aref);
 double orc_Sphi(orc_cosmo *c, double ai, double af, double aref);
+/* non-COLA (UseCOLA = 0): SqStd, SphiStd (src/cosmo.c:1165-1200) */
+double orc_SqStd(orc_cosmo *c, double ai, double af);
+double orc_SphiStd(orc_cosmo *c, double ai, double af);
 /* LCDM fitting functions (src/cosmo.c:1291-1398) -- known-answer checks. */
 double orc_growthD_fit(double omega, double a);
 

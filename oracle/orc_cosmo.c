@@ -487,6 +487,12 @@ double orc_Sq(orc_cosmo *c, double ai, double af, double aref) {
 double orc_Sphi(orc_cosmo *c, double ai, double af, double aref) {
   return (gpQ(af) - gpQ(ai)) * aref / Qfactor(&c->m, aref) / DERgpQ(aref);
 }
+/* SqStd / SphiStd (src/cosmo.c:1165-1200): the Quinn et al. coefficients of
+ * the non-COLA run (StdDA = 2, main.c:75-81) */
+static double sqstd_integrand(double a, void *m) { return 1.0 / Qfactor((const orc_mg *)m, a); }
+static double sphistd_integrand(double a, void *m) { return a / Qfactor((const orc_mg *)m, a); }
+double orc_SqStd(orc_cosmo *c, double ai, double af) { return integrate(sqstd_integrand, &c->m, ai, af); }
+double orc_SphiStd(orc_cosmo *c, double ai, double af) { return integrate(sphistd_integrand, &c->m, ai, af); }
 
 /* Gauss hypergeometric series 2F1(a,b;c;z), |z| < 1. */
 static double hyp2f1(double a, double b, double c, double z) {

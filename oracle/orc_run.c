@@ -7,6 +7,20 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* main.c:75-81, 400-455: COLA steps linearly in a with Sq/Sphi (StdDA 0);
+ * the non-COLA run steps in ln a (stepDistr 1) with SqStd/SphiStd (StdDA 2) */
+static double step_da(const orc_run_params *rp, double A, double ao, int n) {
+  return rp->usecola ? (ao - A) / (double)n : (log(ao) - log(A)) / (double)n;
+}
+static double step_mid(const orc_run_params *rp, double A, double da) { return rp->usecola ? A + 0.5 * da : A * exp(0.5 * da); }
+static double step_end(const orc_run_params *rp, double A, double da) { return rp->usecola ? A + da : A * exp(da); }
+static double kick_dda(const orc_run_params *rp, orc_cosmo *c, double AI, double AF, double A) {
+  return rp->usecola ? orc_Sphi(c, AI, AF, A) : orc_SphiStd(c, AI, AF);
+}
+static double drift_dyyy(const orc_run_params *rp, orc_cosmo *c, double A, double AFF, double AF) {
+  return rp->usecola ? orc_Sq(c, A, AFF, AF) : orc_SqStd(c, A, AFF);
+}
+
 int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
             double *kbin, double *pk, double *kmean, double *nmodes) {
   const int N = rp->ic.N, Ns = rp->ic.Ns, NH = N / 2 + 1;
@@ -72,12 +86,12 @@ int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
     else {
       nsteps = rp->nsteps;
       double ao = 1.0 / (1.0 + rp->final_redshift);
-      da = (ao - A) / (double)nsteps;
+      da = step_da(rp, A, ao, nsteps);
     }
     for (int ts = 0; ts < nsteps; ts++) {
       if (ts == 0 && io != 0) AF = A;
-      else AF = A + da * 0.5;
-      AFF = A + da;
+      else AF = step_mid(rp, A, da);
+      AFF = step_end(rp, A, da);
       /* GetDisplacements (auxPM.c:37-103) */
       orc_cic(pos, np, N, Ns, Box, grid);
       memcpy(dens_x, grid, sizeof(double) * 2 * tot);
@@ -106,7 +120,7 @@ int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
         orc_sd_field(c, cdelta2, N, Ns, Box, A, AFF, ORC_FIELD_ddDddy, 2, D2);
       }
       /* Kick (main.c:688-742); the scale-dependent Kick uses D + D2 */
-      double dda = orc_Sphi(c, AI, AF, A);
+      double dda = kick_dda(rp, c, AI, AF, A);
       orc_kick(np, vel, disp, D1, D2, sumD, rp->mg.omega, dda, sd ? 1.0 : orc_growth_ddDddy(c, A),
                sd ? 1.0 : orc_growth_ddD2ddy(c, A), A, rp->usecola, sumv);
       if (ts == 0 && io != 0) {
@@ -128,7 +142,7 @@ int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
       }
       /* Drift (main.c:747-787); the scale-dependent Drift adds dDdy + dD2dy,
        * which hold [deltaD] here */
-      double dyyy = orc_Sq(c, A, AFF, AF);
+      double dyyy = drift_dyyy(rp, c, A, AFF, AF);
       if (sd) {
         orc_drift(np, pos, vel, V1, V2, sumv, dyyy, 1.0, 1.0, rp->usecola, Box);
       } else {
@@ -195,10 +209,10 @@ double orc_time_steps(const orc_run_params *rp, int nsteps) {
   int cap = rp->pofk_nbins > N ? rp->pofk_nbins : N;
   double *kb = malloc(8 * cap), *pk = malloc(8 * cap), *km = malloc(8 * cap), *nm = malloc(8 * cap);
   int uses_mgk = rp->mg.mg_active && (rp->mg.model == ORC_FOFR || rp->mg.model == ORC_MBETA || rp->mg.model == ORC_DGP);
-  double da = (1.0 / (1.0 + rp->final_redshift) - A) / (double)rp->nsteps, AI = A, sumv[3];
+  double da = step_da(rp, A, 1.0 / (1.0 + rp->final_redshift), rp->nsteps), AI = A, sumv[3];
   double t0 = now_s();
   for (int ts = 0; ts < nsteps; ts++) {
-    double AF = A + 0.5 * da, AFF = A + da;
+    double AF = step_mid(rp, A, da), AFF = step_end(rp, A, da);
     orc_cic(pos, np, N, Ns, Box, grid);
     memcpy(dens_x, grid, sizeof(double) * 2 * tot);
     orc_fft_r2c(N, grid);
@@ -222,12 +236,12 @@ double orc_time_steps(const orc_run_params *rp, int nsteps) {
       orc_sd_field(c, cdelta, N, Ns, Box, A, AFF, ORC_FIELD_ddDddy, 1, D1);
       orc_sd_field(c, cdelta2, N, Ns, Box, A, AFF, ORC_FIELD_ddDddy, 2, D2);
     }
-    orc_kick(np, vel, disp, D1, D2, sumD, rp->mg.omega, orc_Sphi(c, AI, AF, A), sd ? 1.0 : orc_growth_ddDddy(c, A),
+    orc_kick(np, vel, disp, D1, D2, sumD, rp->mg.omega, kick_dda(rp, c, AI, AF, A), sd ? 1.0 : orc_growth_ddDddy(c, A),
              sd ? 1.0 : orc_growth_ddD2ddy(c, A), A, rp->usecola, sumv);
     if (sd)
-      orc_drift(np, pos, vel, V1, V2, sumv, orc_Sq(c, A, AFF, AF), 1.0, 1.0, rp->usecola, Box);
+      orc_drift(np, pos, vel, V1, V2, sumv, drift_dyyy(rp, c, A, AFF, AF), 1.0, 1.0, rp->usecola, Box);
     else
-      orc_drift(np, pos, vel, D1, D2, sumv, orc_Sq(c, A, AFF, AF), orc_growth_D(c, AFF) - Di,
+      orc_drift(np, pos, vel, D1, D2, sumv, drift_dyyy(rp, c, A, AFF, AF), orc_growth_D(c, AFF) - Di,
                 orc_growth_D2(c, AFF) - Di2, rp->usecola, Box);
     A = AFF;
     AI = AF;

@@ -22,7 +22,8 @@ sys.path.insert(0, ROOT)
 from oracle import ref_build  # noqa: E402
 from tests.golden import camb_tables, particle_files  # noqa: E402
 
-BASE = dict(Nmesh=32, Nsample=16, Box=128.0, Init_Redshift=19.0, Seed=4242, nsteps=5, rsd=0)
+BASE = dict(Nmesh=32, Nsample=16, Box=128.0, Init_Redshift=19.0, Seed=4242, nsteps=5, rsd=0, nbins=16, bintype=0,
+            shotnoise=0, kmin=0.0, kmax=0.0, cola=1, z1steps=0)
 COSMO = dict(Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96)
 
 CASES = {
@@ -55,6 +56,16 @@ CASES = {
                                          ReadParticlesFromFile=1, TypeInputParticleFiles=3, NumInputParticleFiles=2,
                                          RamsesOutputNumber=0)),
     "lcdm_rsd": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1), dict(rsd=2)),
+    # standard PM instead of COLA (UseCOLA 0): 2LPT velocities at the IC
+    "lcdm_pm": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1),
+                dict(cola=0)),
+    # logarithmic bins in [0.1, 1] h/Mpc, shot noise subtracted
+    "fofr_logbins": ("FOFR_LCDM", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1),
+                     dict(nbins=10, bintype=1, shotnoise=1, kmin=0.1, kmax=1.0)),
+    # two outputs: z = 1 after 3 steps, z = 0 after 4 more (the output steps'
+    # half kicks, src/main.c:394-611)
+    "dgp_2out": ("DGP", dict(modified_gravity_active=1, rcH0_DGP=1.0, Rsmooth=1.0, include_screening=1),
+                 dict(z1steps=3, nsteps=4)),
     "fofr_rsd": ("FOFR_LCDM", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1), dict(rsd=1)),
 }
 
@@ -63,16 +74,16 @@ input_pofk_is_for_lcdm   0
 input_sigma8_is_for_lcdm 1
 pofk_compute_every_step   1
 pofk_compute_rsd_pofk     {rsd}
-pofk_nbins                16
-pofk_bintype              0
-pofk_subtract_shotnoise   0
-pofk_kmin                 0.0
-pofk_kmax                 0.0
+pofk_nbins                {nbins}
+pofk_bintype              {bintype}
+pofk_subtract_shotnoise   {shotnoise}
+pofk_kmin                 {kmin}
+pofk_kmax                 {kmax}
 OutputDir                   {out}
 FileBase                    run
 OutputRedshiftFile          {out}/outputs.txt
 NumFilesWrittenInParallel   1
-UseCOLA          1
+UseCOLA          {cola}
 Buffer           1.5
 Nmesh            {Nmesh}
 Nsample          {Nsample}
@@ -105,6 +116,8 @@ def run_reference(model, mg, base=None, cosmo=None, nu_info=None):
     cosmo = dict(COSMO, **(cosmo or {}))
     with tempfile.TemporaryDirectory() as d:
         with open(os.path.join(d, "outputs.txt"), "w") as f:
+            if base["z1steps"]:
+                f.write("1, %d\n" % base["z1steps"])
             f.write("0, %d\n" % base["nsteps"])
         txt = STD.format(out=d, **base, **cosmo) + "".join("%s %s\n" % kv for kv in mg.items())
         if "nu_SumMassNuEV" in mg:
@@ -129,6 +142,11 @@ def run_reference(model, mg, base=None, cosmo=None, nu_info=None):
         n = base["Nsample"] ** 3
         out["pos"] = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3).copy()
         out["vel"] = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3).copy()
+        if base["z1steps"]:
+            raw = open(os.path.join(d, "run_z1p000.0"), "rb").read()
+            out["pos_z1"] = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3).copy()
+            out["vel_z1"] = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3).copy()
+            out["pk_z1"] = np.loadtxt(os.path.join(d, "pofk_run_z1.000_CDM.txt"))
     return out
 
 
@@ -138,7 +156,8 @@ def run_case(name, model, mg, base=None):
     r = run_reference(model, mgd, base=base)
     n = BASE["Nsample"] ** 3
     idx = np.arange(0, n, 8)
-    extra = {k: v for k, v in r.items() if k == "pk_total" or k.startswith("rsd_")}
+    extra = {k: v for k, v in r.items() if k in ("pk_total", "pk_z1") or k.startswith("rsd_")}
+    extra.update({k: r[k][idx] for k in ("pos_z1", "vel_z1") if k in r})
     np.savez(os.path.join(ROOT, "tests", "golden", "ref_%s.npz" % name), pk=r["pk"], idx=idx, pos=r["pos"][idx],
              vel=r["vel"][idx], model=model, **{k: float(v) for k, v in mgd.items()}, **dict(BASE, **(base or {})),
              **extra)

@@ -7,7 +7,8 @@ READICFROMFILE build starts from two GADGET-1 particle files), the
 redshift-space multipole files (compute_RSD_powerspectrum,
 src/compute_pofk.c:403-512) where the case asked for them, and a subsample of
 the final GADGET snapshot.  Every case is rerun here through mgp_run with the
-same parameters and white-noise stream.  FP32 path vs FP64 reference over 5
+same parameters and white-noise stream (COLA or standard PM, linear or
+logarithmic bins, one or two outputs).  FP32 path vs FP64 reference over 5-7
 steps: P(k) within 1e-3 relative; multipoles within 1e-3 of max |P0| (P2 and
 P4 cross zero); positions rms < 1e-3 of the particle spacing; velocities 1e-3
 relative rms.
@@ -33,13 +34,15 @@ def _f(g, k, default=0.0):
 def params_for(g, out, tmp):
     model = str(g["model"])
     d = dict(Nmesh=int(g["Nmesh"]), Nsample=int(g["Nsample"]), Box=float(g["Box"]), Seed=int(g["Seed"]),
-             Init_Redshift=float(g["Init_Redshift"]), pofk_nbins=16, pofk_bintype=0, pofk_kmin=0.0, pofk_kmax=0.0,
-             pofk_compute_every_step=1, pofk_subtract_shotnoise=0, pofk_compute_rsd_pofk=int(_f(g, "rsd")),
+             Init_Redshift=float(g["Init_Redshift"]), pofk_nbins=int(_f(g, "nbins", 16)),
+             pofk_bintype=int(_f(g, "bintype")), pofk_kmin=_f(g, "kmin"), pofk_kmax=_f(g, "kmax"),
+             pofk_compute_every_step=1, pofk_subtract_shotnoise=int(_f(g, "shotnoise")),
+             pofk_compute_rsd_pofk=int(_f(g, "rsd")),
              input_pofk_is_for_lcdm=0, input_sigma8_is_for_lcdm=1, use_lcdm_growth_factors=0,
              amplitude_fixed_initial_condition=int(_f(g, "amplitude_fixed_initial_condition")),
              inverted_initial_condition=int(_f(g, "inverted_initial_condition")),
              Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96, WhichSpectrum=2,
-             UseCOLA=1, OutputDir=out, FileBase="run", Noutputs=1,
+             UseCOLA=int(_f(g, "cola", 1)), OutputDir=out, FileBase="run",
              modified_gravity_active=int(_f(g, "modified_gravity_active")),
              include_screening=int(_f(g, "include_screening", 1)))
     if model == "FOFR_LCDM_IC":
@@ -65,7 +68,14 @@ def params_for(g, out, tmp):
                  nu_SumMassNuEV=_f(g, "nu_SumMassNuEV"),
                  nu_FilenameTransferInfofile=camb_tables.write_tables(os.path.join(tmp, "camb")))
     p = M.default_params(**d)
-    p.output_redshift[0], p.output_nsteps[0] = 0.0, int(g["nsteps"])
+    if int(_f(g, "z1steps")):
+        # two outputs: z = 1, then z = 0
+        p.Noutputs = 2
+        p.output_redshift[0], p.output_nsteps[0] = 1.0, int(g["z1steps"])
+        p.output_redshift[1], p.output_nsteps[1] = 0.0, int(g["nsteps"])
+    else:
+        p.Noutputs = 1
+        p.output_redshift[0], p.output_nsteps[0] = 0.0, int(g["nsteps"])
     return p
 
 
@@ -101,15 +111,21 @@ def test_run_matches_reference_run(path, tmp_path):
         scale = np.abs(ref[:, 1]).max()
         # P0, P2, P4 and the y/z-LOS differences (sigma columns)
         assert np.abs(got[:, 1:] - ref[:, 1:]).max() < 1e-3 * scale, key
+    snaps = [("z0p000", "pos", "vel")]
+    if "pk_z1" in g.files:
+        pk1 = np.loadtxt(os.path.join(out, "pofk_run_z1.000_CDM.txt"))
+        assert max_rel(pk1[:, 1], g["pk_z1"][:, 1]) < 1e-3
+        snaps.append(("z1p000", "pos_z1", "vel_z1"))
     n = p.Nsample ** 3
-    raw = open(os.path.join(out, "run_z0p000.0"), "rb").read()
-    pos = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3)
-    vel = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3)
     idx = g["idx"]
-    dx = np.abs(pos[idx] - g["pos"])
-    dx = np.minimum(dx, p.Box - dx)
-    assert np.sqrt(np.mean(dx ** 2)) < 1e-3 * p.Box / p.Nsample
-    assert rel_rms(vel[idx], g["vel"]) < 1e-3
+    for tag, kp, kv in snaps:
+        raw = open(os.path.join(out, "run_%s.0" % tag), "rb").read()
+        pos = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3)
+        vel = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3)
+        dx = np.abs(pos[idx] - g[kp])
+        dx = np.minimum(dx, p.Box - dx)
+        assert np.sqrt(np.mean(dx ** 2)) < 1e-3 * p.Box / p.Nsample, tag
+        assert rel_rms(vel[idx], g[kv]) < 1e-3, tag
 
 
 def test_golden_rsd_cases_present():

@@ -146,6 +146,18 @@ def test_host_cosmology_matches_oracle():
                                rtol=1e-10)
 
 
+def test_host_standard_pm_coefficients_match_oracle():
+    """Quinn et al. kick/drift coefficients of the non-COLA run (UseCOLA 0:
+    StdDA 2, steps in ln a; src/cosmo.c:1165-1200, main.c:75-81)."""
+    p = M.default_params(Init_Redshift=19.0, UseCOLA=0)
+    cos = O.Cosmo(O.make_mg(O.LCDM, p.Omega), 19.0)
+    ai, af = np.array([0.05, 0.3, 0.7]), np.array([0.08, 0.35, 0.9])
+    np.testing.assert_allclose(M.cosmo_coeff(p, 2, ai, af, af), [cos.SqStd(*t) for t in zip(ai, af)], rtol=1e-11)
+    np.testing.assert_allclose(M.cosmo_coeff(p, 3, ai, af, af), [cos.SphiStd(*t) for t in zip(ai, af)], rtol=1e-11)
+    with pytest.raises(M.MGPError):
+        M.cosmo_coeff(p, 4, ai, af, af)
+
+
 def test_host_cosmology_mg_models():
     for model, kw, omk in [(M.MODEL_FOFR, dict(fofr0=1e-5, nfofr=1.0), dict(model=O.FOFR)),
                            (M.MODEL_DGP, dict(rcH0_DGP=1.0), dict(model=O.DGP))]:
