@@ -20,10 +20,11 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 from oracle import ref_build  # noqa: E402
-from tests.golden import camb_tables, particle_files  # noqa: E402
+from tests.golden import camb_tables, particle_files, spectrum_table  # noqa: E402
 
 BASE = dict(Nmesh=32, Nsample=16, Box=128.0, Init_Redshift=19.0, Seed=4242, nsteps=5, rsd=0, nbins=16, bintype=0,
-            shotnoise=0, kmin=0.0, kmax=0.0, cola=1, z1steps=0)
+            shotnoise=0, kmin=0.0, kmax=0.0, cola=1, z1steps=0, sphere=0, pofk_lcdm=0, s8_lcdm=1, lcdm_growth=0,
+            which_spectrum=2)
 COSMO = dict(Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96)
 
 CASES = {
@@ -66,12 +67,25 @@ CASES = {
     # half kicks, src/main.c:394-611)
     "dgp_2out": ("DGP", dict(modified_gravity_active=1, rcH0_DGP=1.0, Rsmooth=1.0, include_screening=1),
                  dict(z1steps=3, nsteps=4)),
+    # spherical mode cut of the IC (SphereMode 1)
+    "lcdm_sphere": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1),
+                    dict(sphere=1)),
+    # the input P(k) and sigma8 quoted for LCDM: the IC rescaled by
+    # mg_pofk_ratio and the sigma8 enhancement (2LPT.c:392-407)
+    "fofr_lcdmic": ("FOFR_LCDM", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1),
+                    dict(pofk_lcdm=1, s8_lcdm=0)),
+    # LCDM growth factors in an f(R) run (use_lcdm_growth_factors 1)
+    "fofr_lcdmgrowth": ("FOFR_LCDM", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1),
+                        dict(lcdm_growth=1)),
+    # tabulated input spectrum (WhichSpectrum 1, spectrum_table.py)
+    "lcdm_table": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1),
+                   dict(which_spectrum=1)),
     "fofr_rsd": ("FOFR_LCDM", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1), dict(rsd=1)),
 }
 
-STD = """use_lcdm_growth_factors  0
-input_pofk_is_for_lcdm   0
-input_sigma8_is_for_lcdm 1
+STD = """use_lcdm_growth_factors  {lcdm_growth}
+input_pofk_is_for_lcdm   {pofk_lcdm}
+input_sigma8_is_for_lcdm {s8_lcdm}
 pofk_compute_every_step   1
 pofk_compute_rsd_pofk     {rsd}
 pofk_nbins                {nbins}
@@ -90,10 +104,10 @@ Nsample          {Nsample}
 Box              {Box}
 Init_Redshift    {Init_Redshift}
 Seed             {Seed}
-SphereMode       0
-WhichSpectrum    2
+SphereMode       {sphere}
+WhichSpectrum    {which_spectrum}
 WhichTransfer    0
-FileWithInputSpectrum  none
+FileWithInputSpectrum  {spectrum_file}
 FileWithInputTransfer  none
 Omega            {Omega}
 OmegaBaryon      {OmegaBaryon}
@@ -119,7 +133,8 @@ def run_reference(model, mg, base=None, cosmo=None, nu_info=None):
             if base["z1steps"]:
                 f.write("1, %d\n" % base["z1steps"])
             f.write("0, %d\n" % base["nsteps"])
-        txt = STD.format(out=d, **base, **cosmo) + "".join("%s %s\n" % kv for kv in mg.items())
+        spectrum = spectrum_table.write_pk_table(os.path.join(d, "pk_table.dat")) if base["which_spectrum"] == 1 else "none"
+        txt = STD.format(out=d, spectrum_file=spectrum, **base, **cosmo) + "".join("%s %s\n" % kv for kv in mg.items())
         if "nu_SumMassNuEV" in mg:
             info = nu_info or camb_tables.write_tables(os.path.join(d, "camb"))
             txt += "nu_FilenameTransferInfofile %s\n" % info

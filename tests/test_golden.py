@@ -5,6 +5,7 @@ compiles the reference's unmodified sources against single-rank shims and
 runs them.  Tolerances reflect the reference's output formats: P(k) is
 written with %10.5f (absolute 5e-6) and snapshots in float32.
 """
+import ctypes as C
 import glob
 import os
 
@@ -12,7 +13,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from golden import camb_tables, particle_files
+from golden import camb_tables, particle_files, spectrum_table
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_*.npz")))
 
@@ -39,16 +40,40 @@ def oracle_run(g, tmpdir=None):
                        scaledependent=int(model == "MBETA"))
     else:
         mg = O.make_mg(O.FOFR, 0.267, mg_active=active, include_screening=scr, fofr0=float(g["fofr0"]),
-                       nfofr=float(g["nfofr"]), scaledependent=int(model in ("FOFR", "FOFRNU")), nu=nu)
+                       nfofr=float(g["nfofr"]), scaledependent=int(model in ("FOFR", "FOFRNU")), nu=nu,
+                       use_lcdm_growth=int(g["lcdm_growth"]) if "lcdm_growth" in g.files else 0)
     N, Ns, box = int(g["Nmesh"]), int(g["Nsample"]), float(g["Box"])
     rp = O.RunParams()
     rp.mg = mg
-    rp.pw = O.make_power(omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sigma8=0.8, nu=nu)
+    table = None
+    if "which_spectrum" in g.files and int(g["which_spectrum"]) == 1:
+        # the tabulated spectrum the fixture was made with, as log10 pairs
+        path = spectrum_table.write_pk_table(os.path.join(str(tmpdir), "pk_table.dat"))
+        kp = np.loadtxt(path)
+        table = (np.ascontiguousarray(np.log10(kp[:, 0])), np.ascontiguousarray(np.log10(kp[:, 1])))
+        pw = O.Power()
+        pw.which_spectrum, pw.omega, pw.omega_b, pw.h, pw.ns, pw.sigma8 = 1, 0.267, 0.049, 0.71, 0.96, 0.8
+        pw.ntab = len(kp)
+        pw.tab_logk = table[0].ctypes.data_as(C.POINTER(C.c_double))
+        pw.tab_logP = table[1].ctypes.data_as(C.POINTER(C.c_double))
+        O.lib().orc_power_init(C.byref(pw))
+        rp.pw = pw
+    else:
+        rp.pw = O.make_power(omega=0.267, omega_b=0.049, h=0.71, ns=0.96, sigma8=0.8, nu=nu)
     if model == "BRANSDICKE":
         # normalised with the file's Omega/h, evaluated with the background's
         rp.pw.omega, rp.pw.h = mg.omega, float(np.sqrt(mg.Omegah2 / mg.omega))
-    rp.ic = O.ICParams(N, Ns, box, int(g["Seed"]), 0, int(g["amplitude_fixed_initial_condition"]),
-                       int(g["inverted_initial_condition"]), 1.0)
+    rescale = 1.0
+    if "pofk_lcdm" in g.files and int(g["pofk_lcdm"]) and active:
+        # 2LPT.c:392-407: P(k) x mg_pofk_ratio(k, 1) (k-independent without
+        # scale-dependent growth), / (sigma8_MG / sigma8_LCDM)^2
+        cos = O.Cosmo(mg, float(g["Init_Redshift"]))
+        rescale = cos.mg_pofk_ratio(0.1, 1.0)
+        if not int(g["s8_lcdm"]):
+            rescale /= O.lib().orc_mg_sigma8_enh(cos.h, C.byref(rp.pw), 1.0) ** 2
+    sphere = int(g["sphere"]) if "sphere" in g.files else 0
+    rp.ic = O.ICParams(N, Ns, box, int(g["Seed"]), sphere, int(g["amplitude_fixed_initial_condition"]),
+                       int(g["inverted_initial_condition"]), rescale)
     rp.init_redshift = float(g["Init_Redshift"])
     rp.nsteps = int(g["nsteps"])
     rp.final_redshift = 0.0
@@ -72,7 +97,7 @@ def oracle_run(g, tmpdir=None):
     pos, vel = np.zeros((n, 3)), np.zeros((n, 3))
     kb, pk, km, nm = (np.zeros(N) for _ in range(4))
     nb = O.lib().orc_run(rp, pos, vel, kb, pk, km, nm)
-    del nu  # the tables stay alive through rp.mg / rp.pw until here
+    del nu, table  # the tables stay alive through rp.mg / rp.pw until here
     return (kb[:nb], pk[:nb], km[:nb], nm[:nb]), pos, vel, box
 
 

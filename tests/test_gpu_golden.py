@@ -8,7 +8,9 @@ redshift-space multipole files (compute_RSD_powerspectrum,
 src/compute_pofk.c:403-512) where the case asked for them, and a subsample of
 the final GADGET snapshot.  Every case is rerun here through mgp_run with the
 same parameters and white-noise stream (COLA or standard PM, linear or
-logarithmic bins, one or two outputs).  FP32 path vs FP64 reference over 5-7
+logarithmic bins, one or two outputs, cube or sphere mode cut, P(k) and
+sigma8 quoted for LCDM or for the model, LCDM growth factors, Eisenstein-Hu
+or tabulated spectrum).  FP32 path vs FP64 reference over 5-7
 steps: P(k) within 1e-3 relative; multipoles within 1e-3 of max |P0| (P2 and
 P4 cross zero); positions rms < 1e-3 of the particle spacing; velocities 1e-3
 relative rms.
@@ -20,7 +22,7 @@ import numpy as np
 import pytest
 
 import mgpicola as M
-from golden import camb_tables, particle_files
+from golden import camb_tables, particle_files, spectrum_table
 
 pytestmark = pytest.mark.gpu
 
@@ -38,13 +40,17 @@ def params_for(g, out, tmp):
              pofk_bintype=int(_f(g, "bintype")), pofk_kmin=_f(g, "kmin"), pofk_kmax=_f(g, "kmax"),
              pofk_compute_every_step=1, pofk_subtract_shotnoise=int(_f(g, "shotnoise")),
              pofk_compute_rsd_pofk=int(_f(g, "rsd")),
-             input_pofk_is_for_lcdm=0, input_sigma8_is_for_lcdm=1, use_lcdm_growth_factors=0,
+             input_pofk_is_for_lcdm=int(_f(g, "pofk_lcdm")), input_sigma8_is_for_lcdm=int(_f(g, "s8_lcdm", 1)),
+             use_lcdm_growth_factors=int(_f(g, "lcdm_growth")), SphereMode=int(_f(g, "sphere")),
              amplitude_fixed_initial_condition=int(_f(g, "amplitude_fixed_initial_condition")),
              inverted_initial_condition=int(_f(g, "inverted_initial_condition")),
-             Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96, WhichSpectrum=2,
+             Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96,
+             WhichSpectrum=int(_f(g, "which_spectrum", 2)),
              UseCOLA=int(_f(g, "cola", 1)), OutputDir=out, FileBase="run",
              modified_gravity_active=int(_f(g, "modified_gravity_active")),
              include_screening=int(_f(g, "include_screening", 1)))
+    if d["WhichSpectrum"] == 1:
+        d["FileWithInputSpectrum"] = spectrum_table.write_pk_table(os.path.join(tmp, "pk_table.dat"))
     if model == "FOFR_LCDM_IC":
         # two GADGET-1 files of the displaced lattice the fixture was made from
         d.update(ReadParticlesFromFile=1, TypeInputParticleFiles=3, NumInputParticleFiles=2, RamsesOutputNumber=0,
