@@ -32,7 +32,10 @@ MODELS = {
     "FOFRNU": ["-DFOFRGRAVITY", "-DMASSIVE_NEUTRINOS", "-DSCALEDEPENDENT"],
     # initial conditions read from particle files (src/readICfromfile.c)
     "FOFR_LCDM_IC": ["-DFOFRGRAVITY", "-DREADICFROMFILE"],
+    # ASCII snapshots instead of GADGET-1 (GADGET_STYLE off)
+    "FOFR_LCDM_ASCII": ["-DFOFRGRAVITY"],
 }
+NO_GADGET_STYLE = {"FOFR_LCDM_ASCII"}
 # sources a build adds to SOURCES
 EXTRA_SOURCES = {"FOFR_LCDM_IC": ["readICfromfile.c"]}
 
@@ -59,7 +62,8 @@ def build(models=None, verbose=False):
         if os.path.exists(out) and os.path.getmtime(out) >= newest:
             continue
         extra = [os.path.join(REF_SRC, f) for f in EXTRA_SOURCES.get(model, [])]
-        cmd = (["gcc", "-O2", "-std=gnu99", "-fopenmp", "-w", "-o", out] + COMMON + MODELS[model] + inc + srcs +
+        common = [f for f in COMMON if not (model in NO_GADGET_STYLE and f == "-DGADGET_STYLE")]
+        cmd = (["gcc", "-O2", "-std=gnu99", "-fopenmp", "-w", "-o", out] + common + MODELS[model] + inc + srcs +
                extra + ["-lm"])
         if verbose:
             print(" ".join(cmd))

@@ -67,6 +67,8 @@ CASES = {
     # half kicks, src/main.c:394-611)
     "dgp_2out": ("DGP", dict(modified_gravity_active=1, rcH0_DGP=1.0, Rsmooth=1.0, include_screening=1),
                  dict(z1steps=3, nsteps=4)),
+    # ASCII snapshot output (a build without GADGET_STYLE)
+    "lcdm_ascii": ("FOFR_LCDM_ASCII", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1)),
     # spherical mode cut of the IC (SphereMode 1)
     "lcdm_sphere": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1),
                     dict(sphere=1)),
@@ -153,10 +155,19 @@ def run_reference(model, mg, base=None, cosmo=None, nu_info=None):
                 out["rsd_" + f[len("pofk_RSD_run_z"):-4]] = np.loadtxt(os.path.join(d, f))
         if "nu_SumMassNuEV" in mg:
             out["pk_total"] = np.loadtxt(os.path.join(d, "pofk_run_z0.000_total.txt"))
-        raw = open(os.path.join(d, "run_z0p000.0"), "rb").read()
         n = base["Nsample"] ** 3
-        out["pos"] = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3).copy()
-        out["vel"] = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3).copy()
+        out["info_txt"] = np.array(open(os.path.join(d, "info_run_z0p000.txt")).read())
+        if model in ref_build.NO_GADGET_STYLE:
+            # ASCII: the particle count, then x y z vx vy vz per line (%12.6f)
+            lines = open(os.path.join(d, "run_z0p000.0")).read().splitlines()
+            out["ascii_first_line"] = np.array(lines[0])
+            rows = np.array([[float(v) for v in l.split()] for l in lines[1:]])
+            out["pos"], out["vel"] = rows[:, :3].copy(), rows[:, 3:].copy()
+        else:
+            raw = open(os.path.join(d, "run_z0p000.0"), "rb").read()
+            out["gadget_header"] = np.frombuffer(raw[:264], dtype=np.uint8).copy()
+            out["pos"] = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3).copy()
+            out["vel"] = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3).copy()
         if base["z1steps"]:
             raw = open(os.path.join(d, "run_z1p000.0"), "rb").read()
             out["pos_z1"] = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3).copy()
@@ -171,7 +182,8 @@ def run_case(name, model, mg, base=None):
     r = run_reference(model, mgd, base=base)
     n = BASE["Nsample"] ** 3
     idx = np.arange(0, n, 8)
-    extra = {k: v for k, v in r.items() if k in ("pk_total", "pk_z1") or k.startswith("rsd_")}
+    extra = {k: v for k, v in r.items()
+             if k in ("pk_total", "pk_z1", "info_txt", "ascii_first_line", "gadget_header") or k.startswith("rsd_")}
     extra.update({k: r[k][idx] for k in ("pos_z1", "vel_z1") if k in r})
     np.savez(os.path.join(ROOT, "tests", "golden", "ref_%s.npz" % name), pk=r["pk"], idx=idx, pos=r["pos"][idx],
              vel=r["vel"][idx], model=model, **{k: float(v) for k, v in mgd.items()}, **dict(BASE, **(base or {})),

@@ -56,7 +56,7 @@ def params_for(g, out, tmp):
         d.update(ReadParticlesFromFile=1, TypeInputParticleFiles=3, NumInputParticleFiles=2, RamsesOutputNumber=0,
                  InputParticleFileDir=particle_files.write_ic_files(os.path.join(tmp, "ic"), d["Box"]),
                  InputParticleFilePrefix="ics")
-    if model.startswith("FOFR"):
+    if model.startswith("FOFR"):  # FOFR, FOFR_LCDM, FOFRNU, FOFR_LCDM_IC, FOFR_LCDM_ASCII
         d.update(model=M.MODEL_FOFR, fofr0=_f(g, "fofr0"), nfofr=_f(g, "nfofr"))
     elif model == "DGP":
         d.update(model=M.MODEL_DGP, rcH0_DGP=_f(g, "rcH0_DGP"), Rsmooth=_f(g, "Rsmooth"),
@@ -99,8 +99,12 @@ def test_run_matches_reference_run(path, tmp_path):
     out = str(tmp_path / "out")
     os.makedirs(out)
     p = params_for(g, out, str(tmp_path))
+    ascii_out = str(g["model"]).endswith("_ASCII")
     with M.Context(p) as ctx:
-        ctx.run(gadget=True)
+        ctx.run(gadget=not ascii_out)
+    # the info file (Output_Info, src/main.c:1067-1099) as text
+    if "info_txt" in g.files:
+        assert open(os.path.join(out, "info_run_z0p000.txt")).read() == str(g["info_txt"])
     pk = np.loadtxt(os.path.join(out, "pofk_run_z0.000_CDM.txt"))
     assert pk.shape == g["pk"].shape
     np.testing.assert_allclose(pk[:, 0], g["pk"][:, 0], atol=6e-6)
@@ -125,9 +129,19 @@ def test_run_matches_reference_run(path, tmp_path):
     n = p.Nsample ** 3
     idx = g["idx"]
     for tag, kp, kv in snaps:
-        raw = open(os.path.join(out, "run_%s.0" % tag), "rb").read()
-        pos = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3)
-        vel = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3)
+        if ascii_out:
+            # ASCII snapshot (src/main.c:1000-1025): the count, then %12.6f columns
+            lines = open(os.path.join(out, "run_%s.0" % tag)).read().splitlines()
+            assert lines[0] == str(g["ascii_first_line"])
+            rows = np.array([[float(v) for v in l.split()] for l in lines[1:]])
+            pos, vel = rows[:, :3], rows[:, 3:]
+        else:
+            raw = open(os.path.join(out, "run_%s.0" % tag), "rb").read()
+            if tag == "z0p000" and "gadget_header" in g.files:
+                # the GADGET-1 header block byte for byte (src/main.c:1106-1149)
+                np.testing.assert_array_equal(np.frombuffer(raw[:264], dtype=np.uint8), g["gadget_header"])
+            pos = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3)
+            vel = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3)
         dx = np.abs(pos[idx] - g[kp])
         dx = np.minimum(dx, p.Box - dx)
         assert np.sqrt(np.mean(dx ** 2)) < 1e-3 * p.Box / p.Nsample, tag
