@@ -34,6 +34,11 @@ MODELS = {
     "FOFR_LCDM_IC": ["-DFOFRGRAVITY", "-DREADICFROMFILE"],
     # ASCII snapshots instead of GADGET-1 (GADGET_STYLE off)
     "FOFR_LCDM_ASCII": ["-DFOFRGRAVITY"],
+    # w(a) = w0 + wa (1 - a) background
+    "FOFR_LCDM_W0WA": ["-DFOFRGRAVITY", "-DEQUATIONOFSTATE_PARAMETRIZATION"],
+    # nDGP with the top-hat / sharp-k smoothing filter (src/mg.h:318-338)
+    "DGP_TOPHAT": ["-DDGPGRAVITY", "-DTOPHATFILTER"],
+    "DGP_SHARPK": ["-DDGPGRAVITY", "-DSHARPKFILTER"],
 }
 NO_GADGET_STYLE = {"FOFR_LCDM_ASCII"}
 # sources a build adds to SOURCES

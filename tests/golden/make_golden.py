@@ -67,6 +67,13 @@ CASES = {
     # half kicks, src/main.c:394-611)
     "dgp_2out": ("DGP", dict(modified_gravity_active=1, rcH0_DGP=1.0, Rsmooth=1.0, include_screening=1),
                  dict(z1steps=3, nsteps=4)),
+    # w(a) = w0 + wa (1 - a) background (EQUATIONOFSTATE_PARAMETRIZATION)
+    "lcdm_w0wa": ("FOFR_LCDM_W0WA", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1,
+                                         w_0=-0.9, w_a=0.2)),
+    # nDGP: top-hat and sharp-k smoothing, and no screening
+    "dgp_tophat": ("DGP_TOPHAT", dict(modified_gravity_active=1, rcH0_DGP=1.0, Rsmooth=1.0, include_screening=1)),
+    "dgp_sharpk": ("DGP_SHARPK", dict(modified_gravity_active=1, rcH0_DGP=1.0, Rsmooth=1.0, include_screening=1)),
+    "dgp_nosc": ("DGP", dict(modified_gravity_active=1, rcH0_DGP=1.0, Rsmooth=1.0, include_screening=0)),
     # ASCII snapshot output (a build without GADGET_STYLE)
     "lcdm_ascii": ("FOFR_LCDM_ASCII", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1)),
     # spherical mode cut of the IC (SphereMode 1)

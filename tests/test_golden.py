@@ -28,9 +28,11 @@ def oracle_run(g, tmpdir=None):
                          int(g["nu_include_massive_neutrinos"]))
     active = int(g["modified_gravity_active"])
     scr = int(g["include_screening"])
-    if model == "DGP":
+    if model.startswith("DGP"):
+        # GAUSSIANFILTER (the DGP build), TOPHATFILTER or SHARPKFILTER
+        filt = {"DGP": 1, "DGP_TOPHAT": 2, "DGP_SHARPK": 3}[model]
         mg = O.make_mg(O.DGP, 0.267, mg_active=active, include_screening=scr, rcH0=float(g["rcH0_DGP"]),
-                       rsmooth=float(g["Rsmooth"]))
+                       rsmooth=float(g["Rsmooth"]), smoothing_filter=filt)
     elif model == "BRANSDICKE":
         mg = O.make_mg(O.JBD_GEFF, 0.267, mg_active=active, wBD=float(g["wBD"]), Omegah2=float(g["Omegah2"]),
                        Omegarh2=float(g["Omegar2"]), Omegavh2=float(g["Omegav2"]))
@@ -39,9 +41,10 @@ def oracle_run(g, tmpdir=None):
                        beta_symm=float(g["beta_symm"]), range_symm=float(g["range_symm"]),
                        scaledependent=int(model == "MBETA"))
     else:
+        w0wa = dict(use_w0wa=1, w0=float(g["w_0"]), wa=float(g["w_a"])) if model == "FOFR_LCDM_W0WA" else {}
         mg = O.make_mg(O.FOFR, 0.267, mg_active=active, include_screening=scr, fofr0=float(g["fofr0"]),
                        nfofr=float(g["nfofr"]), scaledependent=int(model in ("FOFR", "FOFRNU")), nu=nu,
-                       use_lcdm_growth=int(g["lcdm_growth"]) if "lcdm_growth" in g.files else 0)
+                       use_lcdm_growth=int(g["lcdm_growth"]) if "lcdm_growth" in g.files else 0, **w0wa)
     N, Ns, box = int(g["Nmesh"]), int(g["Nsample"]), float(g["Box"])
     rp = O.RunParams()
     rp.mg = mg

@@ -56,11 +56,13 @@ def params_for(g, out, tmp):
         d.update(ReadParticlesFromFile=1, TypeInputParticleFiles=3, NumInputParticleFiles=2, RamsesOutputNumber=0,
                  InputParticleFileDir=particle_files.write_ic_files(os.path.join(tmp, "ic"), d["Box"]),
                  InputParticleFilePrefix="ics")
-    if model.startswith("FOFR"):  # FOFR, FOFR_LCDM, FOFRNU, FOFR_LCDM_IC, FOFR_LCDM_ASCII
+    if model.startswith("FOFR"):  # FOFR, FOFR_LCDM, FOFRNU, FOFR_LCDM_IC, FOFR_LCDM_ASCII, FOFR_LCDM_W0WA
         d.update(model=M.MODEL_FOFR, fofr0=_f(g, "fofr0"), nfofr=_f(g, "nfofr"))
-    elif model == "DGP":
-        d.update(model=M.MODEL_DGP, rcH0_DGP=_f(g, "rcH0_DGP"), Rsmooth=_f(g, "Rsmooth"),
-                 smoothing_filter=M.FILTER_GAUSSIAN)
+        if model == "FOFR_LCDM_W0WA":
+            d.update(use_w0wa=1, w_0=_f(g, "w_0"), w_a=_f(g, "w_a"))
+    elif model.startswith("DGP"):
+        filt = {"DGP": M.FILTER_GAUSSIAN, "DGP_TOPHAT": M.FILTER_TOPHAT, "DGP_SHARPK": M.FILTER_SHARPK}[model]
+        d.update(model=M.MODEL_DGP, rcH0_DGP=_f(g, "rcH0_DGP"), Rsmooth=_f(g, "Rsmooth"), smoothing_filter=filt)
     elif model == "BRANSDICKE":
         d.update(model=M.MODEL_BRANSDICKE, wBD=_f(g, "wBD"), Omegah2=_f(g, "Omegah2"), Omegarh2=_f(g, "Omegar2"),
                  Omegavh2=_f(g, "Omegav2"))
