@@ -24,7 +24,7 @@ from tests.golden import camb_tables, particle_files, spectrum_table  # noqa: E4
 
 BASE = dict(Nmesh=32, Nsample=16, Box=128.0, Init_Redshift=19.0, Seed=4242, nsteps=5, rsd=0, nbins=16, bintype=0,
             shotnoise=0, kmin=0.0, kmax=0.0, cola=1, z1steps=0, sphere=0, pofk_lcdm=0, s8_lcdm=1, lcdm_growth=0,
-            which_spectrum=2)
+            which_spectrum=2, which_transfer=0, unit_length=3.085678e24, input_unit_length=3.085678e24)
 COSMO = dict(Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96)
 
 CASES = {
@@ -86,6 +86,12 @@ CASES = {
     # LCDM growth factors in an f(R) run (use_lcdm_growth_factors 1)
     "fofr_lcdmgrowth": ("FOFR_LCDM", dict(modified_gravity_active=1, fofr0=1e-5, nfofr=1.0, include_screening=1),
                         dict(lcdm_growth=1)),
+    # tabulated transfer function (WhichSpectrum 0, WhichTransfer 1)
+    "lcdm_transfer": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1),
+                      dict(which_spectrum=0, which_transfer=1)),
+    # lengths in kpc/h (UnitLength_in_cm 3.085678e21, Box 128000 kpc/h)
+    "lcdm_kpc": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1),
+                 dict(unit_length=3.085678e21, Box=128000.0)),
     # tabulated input spectrum (WhichSpectrum 1, spectrum_table.py)
     "lcdm_table": ("FOFR_LCDM", dict(modified_gravity_active=0, fofr0=1e-5, nfofr=1.0, include_screening=1),
                    dict(which_spectrum=1)),
@@ -115,18 +121,18 @@ Init_Redshift    {Init_Redshift}
 Seed             {Seed}
 SphereMode       {sphere}
 WhichSpectrum    {which_spectrum}
-WhichTransfer    0
+WhichTransfer    {which_transfer}
 FileWithInputSpectrum  {spectrum_file}
-FileWithInputTransfer  none
+FileWithInputTransfer  {transfer_file}
 Omega            {Omega}
 OmegaBaryon      {OmegaBaryon}
 HubbleParam      {HubbleParam}
 Sigma8           {Sigma8}
 PrimordialIndex  {PrimordialIndex}
-UnitLength_in_cm                3.085678e24
+UnitLength_in_cm                {unit_length}
 UnitMass_in_g                   1.989e43
 UnitVelocity_in_cm_per_s        1e5
-InputSpectrum_UnitLength_in_cm  3.085678e24
+InputSpectrum_UnitLength_in_cm  {input_unit_length}
 """
 
 
@@ -143,7 +149,10 @@ def run_reference(model, mg, base=None, cosmo=None, nu_info=None):
                 f.write("1, %d\n" % base["z1steps"])
             f.write("0, %d\n" % base["nsteps"])
         spectrum = spectrum_table.write_pk_table(os.path.join(d, "pk_table.dat")) if base["which_spectrum"] == 1 else "none"
-        txt = STD.format(out=d, spectrum_file=spectrum, **base, **cosmo) + "".join("%s %s\n" % kv for kv in mg.items())
+        transfer = (spectrum_table.write_transfer_table(os.path.join(d, "t_table.dat")) if base["which_transfer"] == 1
+                    else "none")
+        txt = STD.format(out=d, spectrum_file=spectrum, transfer_file=transfer, **base, **cosmo) + "".join(
+            "%s %s\n" % kv for kv in mg.items())
         if "nu_SumMassNuEV" in mg:
             info = nu_info or camb_tables.write_tables(os.path.join(d, "camb"))
             txt += "nu_FilenameTransferInfofile %s\n" % info

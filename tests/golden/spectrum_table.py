@@ -16,3 +16,16 @@ def write_pk_table(path, omega=0.267, h=0.71, ns=0.96, n=300):
         for a, b in zip(k, p):
             f.write("%.8e %.8e\n" % (a, b))
     return path
+
+
+def write_transfer_table(path, omega=0.267, h=0.71, n=300):
+    """A tabulated transfer function for WhichSpectrum = 0, WhichTransfer = 1
+    (read_transfer_table, src/power.c): k (h/Mpc) and T(k), BBKS-shaped."""
+    k = np.exp(np.linspace(np.log(1e-4), np.log(100.0), n))
+    q = k / (omega * h)
+    t = np.log(1.0 + 2.34 * q) / (2.34 * q) * (1.0 + 3.89 * q + (16.1 * q) ** 2 + (5.46 * q) ** 3 +
+                                               (6.71 * q) ** 4) ** -0.25
+    with open(path, "w") as f:
+        for a, b in zip(k, t):
+            f.write("%.8e %.8e\n" % (a, b))
+    return path

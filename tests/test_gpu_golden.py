@@ -10,7 +10,7 @@ the final GADGET snapshot.  Every case is rerun here through mgp_run with the
 same parameters and white-noise stream (COLA or standard PM, linear or
 logarithmic bins, one or two outputs, cube or sphere mode cut, P(k) and
 sigma8 quoted for LCDM or for the model, LCDM growth factors, Eisenstein-Hu
-or tabulated spectrum).  FP32 path vs FP64 reference over 5-7
+or tabulated spectrum or transfer function, Mpc/h or kpc/h units).  FP32 path vs FP64 reference over 5-7
 steps: P(k) within 1e-3 relative; multipoles within 1e-3 of max |P0| (P2 and
 P4 cross zero); positions rms < 1e-3 of the particle spacing; velocities 1e-3
 relative rms.
@@ -45,12 +45,16 @@ def params_for(g, out, tmp):
              amplitude_fixed_initial_condition=int(_f(g, "amplitude_fixed_initial_condition")),
              inverted_initial_condition=int(_f(g, "inverted_initial_condition")),
              Omega=0.267, OmegaBaryon=0.049, HubbleParam=0.71, Sigma8=0.8, PrimordialIndex=0.96,
-             WhichSpectrum=int(_f(g, "which_spectrum", 2)),
+             WhichSpectrum=int(_f(g, "which_spectrum", 2)), WhichTransfer=int(_f(g, "which_transfer")),
+             UnitLength_in_cm=_f(g, "unit_length", 3.085678e24),
+             InputSpectrum_UnitLength_in_cm=_f(g, "input_unit_length", 3.085678e24),
              UseCOLA=int(_f(g, "cola", 1)), OutputDir=out, FileBase="run",
              modified_gravity_active=int(_f(g, "modified_gravity_active")),
              include_screening=int(_f(g, "include_screening", 1)))
     if d["WhichSpectrum"] == 1:
         d["FileWithInputSpectrum"] = spectrum_table.write_pk_table(os.path.join(tmp, "pk_table.dat"))
+    if d["WhichTransfer"] == 1:
+        d["FileWithInputTransfer"] = spectrum_table.write_transfer_table(os.path.join(tmp, "t_table.dat"))
     if model == "FOFR_LCDM_IC":
         # two GADGET-1 files of the displaced lattice the fixture was made from
         d.update(ReadParticlesFromFile=1, TypeInputParticleFiles=3, NumInputParticleFiles=2, RamsesOutputNumber=0,
@@ -130,6 +134,8 @@ def test_run_matches_reference_run(path, tmp_path):
         snaps.append(("z1p000", "pos_z1", "vel_z1"))
     n = p.Nsample ** 3
     idx = g["idx"]
+    # snapshots are written in Mpc/h (lengthfac, src/main.c:913-977)
+    box_out = p.Box * p.UnitLength_in_cm / 3.085678e24
     for tag, kp, kv in snaps:
         if ascii_out:
             # ASCII snapshot (src/main.c:1000-1025): the count, then %12.6f columns
@@ -145,8 +151,8 @@ def test_run_matches_reference_run(path, tmp_path):
             pos = np.frombuffer(raw[268:268 + 12 * n], dtype="<f4").reshape(n, 3)
             vel = np.frombuffer(raw[268 + 12 * n + 8:268 + 24 * n + 8], dtype="<f4").reshape(n, 3)
         dx = np.abs(pos[idx] - g[kp])
-        dx = np.minimum(dx, p.Box - dx)
-        assert np.sqrt(np.mean(dx ** 2)) < 1e-3 * p.Box / p.Nsample, tag
+        dx = np.minimum(dx, box_out - dx)
+        assert np.sqrt(np.mean(dx ** 2)) < 1e-3 * box_out / p.Nsample, tag
         assert rel_rms(vel[idx], g[kv]) < 1e-3, tag
 
 
