@@ -214,6 +214,7 @@ def run_batch(args, cfg):
     }
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args)
+        out["pofk_check"] = pofk_check(args.config)
     print(json.dumps(out))
 
 
@@ -435,6 +436,7 @@ def run_gpu(args):
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args)
+        out["pofk_check"] = pofk_check(args.config)
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:
@@ -479,6 +481,50 @@ CONFIGS["fofr_nu_64_128"] = dict(Ns=64, N=128, Box=128.0, model="fofr", nsteps=3
 CONFIGS["fofr_64_128"] = dict(Ns=64, N=128, Box=256.0, model="fofr", nsteps=20, seed=6001, fixed=0, nbins=64)
 CONFIGS["lcdm_128_128"] = dict(Ns=128, N=128, Box=128.0, model="lcdm", nsteps=30, seed=7017, fixed=0, nbins=64)
 CONFIGS["ndgp_128_256"] = dict(Ns=128, N=256, Box=256.0, model="dgp", nsteps=50, seed=5003, fixed=1, nbins=128)
+
+
+def pofk_check(config):
+    """P(k) relative error against the FP64 oracle, stated with the throughput:
+    the same model, seed and IC type at 64^3 particles / 128^3 mesh (the
+    512^3/1024^3 run is far beyond what the FP64 oracle can redo on the host),
+    run to z = 0 on the GPU and through the oracle's KDK loop; the maximum
+    |P_gpu / P_oracle - 1| over the bins with k <= 0.5 h/Mpc."""
+    import mgpicola as M
+    from oracle import oracle as O
+
+    cfg = dict(CONFIGS[config], Ns=64, N=128, Box=256.0, nsteps=10, nbins=64)
+    cfg.pop("closure", None)
+    cfg.pop("batch", None)
+    p = make_params(M, cfg)
+    note = ""
+    if cfg.get("sd"):
+        # the oracle's IC rescaling is one number; with scale-dependent growth
+        # mg_pofk_ratio depends on k, so both sides take P(k) as quoted
+        p.input_pofk_is_for_lcdm = 0
+        note = ", input P(k) quoted for the model"
+    A0 = 1.0 / (1.0 + p.Init_Redshift)
+    da = (1.0 - A0) / cfg["nsteps"]
+    with M.Context(p) as ctx:
+        ctx.displacement_fields()
+        A, AI = A0, A0
+        for _ in range(cfg["nsteps"]):
+            ctx.step(A, AI, A + 0.5 * da, A + da)  # assigns the scale-dependent fields where needed
+            A, AI = A + da, A + 0.5 * da
+        ctx.get_displacements(A)
+        k, pk, _, n = ctx.pofk(total=bool(cfg.get("nu")))
+    rp = oracle_params(O, cfg)
+    if p.modified_gravity_active and p.input_pofk_is_for_lcdm and not cfg.get("sd"):
+        # the IC is rescaled by mg_pofk_ratio(k, 1), k-independent without
+        # scale-dependent growth (2LPT.c:392-407)
+        rp.ic.pofk_rescale = O.Cosmo(rp.mg, p.Init_Redshift).mg_pofk_ratio(0.1, 1.0)
+    nb = p.pofk_nbins
+    kb, po, km, nm = (np.zeros(max(nb, p.Nmesh)) for _ in range(4))
+    n_o = O.lib().orc_run(rp, np.zeros((p.Nsample ** 3, 3)), np.zeros((p.Nsample ** 3, 3)), kb, po, km, nm)
+    m = (nm[:n_o] > 0) & (kb[:n_o] <= 0.5) & (kb[:n_o] > 0)
+    err = float(np.max(np.abs(pk[:n_o][m] / po[:n_o][m] - 1.0)))
+    return {"max_rel_err": float("%.3g" % err), "k_max_h_mpc": 0.5, "bins": int(m.sum()),
+            "case": "%s at 64^3 particles / 128^3 mesh, Box 256, 10 steps to z = 0, seed %d%s, vs the FP64 oracle"
+                    % (model_name(cfg), cfg["seed"], note)}
 
 
 def cpu_baseline(args, nsteps=1):
