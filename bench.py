@@ -387,6 +387,13 @@ def run_gpu(args):
     for a in (pos, vel, d1, d2):
         M.unpin(a)
     e2e_val = job_value(world, Np, e2e_steps, e2e_t)
+    # RSD multipoles P0/P2/P4 of the final state (compute_RSD_powerspectrum,
+    # src/compute_pofk.c:403-512: y and z lines of sight, averaged), timed
+    # end to end on the host (two redshift-space deposits, two R2C, binning)
+    ctx.kernel_ms("interp_kick_drift")  # synchronise before timing
+    t0 = time.perf_counter()
+    rsd = ctx.pofk_rsd(state["A"])
+    rsd_ms = (time.perf_counter() - t0) * 1e3
     ctx.close()
     if closure is not None:
         closure.close()
@@ -431,6 +438,8 @@ def run_gpu(args):
                 "step_ms": [round(x, 2) for x in e2e_ms]},
         "gpu_launches": int(launches),
         "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stage_ms.items()},
+        "rsd_multipoles": {"ms": round(rsd_ms, 3), "bins": int(len(rsd[0])), "a": round(state["A"], 5),
+                           "los": "y and z, averaged (compute_RSD_powerspectrum)"},
         "roofline": roof,
         "clocks": clk.summary(),
     }
