@@ -88,12 +88,13 @@ __global__ void __launch_bounds__(kThreads) k_sd_fold(const float2 *__restrict__
                                                        int nfields, float2 *__restrict__ out0,
                                                        float2 *__restrict__ out1, long long ostride) {
   const int NH = N / 2 + 1, NHs = Ns / 2 + 1;
-  const long long total = (long long)Ns * Ns * NHs;
-  long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x; o < total; o += stride) {
-    const int kzp = (int)(o % NHs);
-    const long long row = o / NHs;
-    const int kyp = (int)(row % Ns), kxp = (int)(row / Ns);
+  // one warp per folded (kx, ky) row, lanes along kz: no division per mode
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < (long long)Ns * Ns; row += nw)
+  for (int kzp = lane; kzp < NHs; kzp += 32) {
+    const long long o = row * NHs + kzp;
+    const int kxp = (int)(row / Ns), kyp = (int)(row - (long long)kxp * Ns);
     float2 G[2][3];
 #pragma unroll
     for (int f = 0; f < 2; f++)
@@ -108,7 +109,7 @@ __global__ void __launch_bounds__(kThreads) k_sd_fold(const float2 *__restrict__
             const int kz = kzp + Ns * az;
             // stored half space, or the conjugate of the mirrored mode
             const bool cj = 2 * kz > N;
-            const int sx = cj ? (N - kx) % N : kx, sy = cj ? (N - ky) % N : ky, sz = cj ? N - kz : kz;
+            const int sx = cj ? (kx == 0 ? 0 : N - kx) : kx, sy = cj ? (ky == 0 ? 0 : N - ky) : ky, sz = cj ? N - kz : kz;
             const long long c = ((long long)sx * N + sy) * NH + sz;
             const int dx = sd_d(sx, N), dy = sd_d(sy, N), dz = sd_d(sz, N);
             const float4 t = __ldg(tab + ((long long)dx * dx + (long long)dy * dy + (long long)dz * dz));
@@ -297,9 +298,8 @@ static int fields_pass(mgp_ctx *c, double A, double AFF, int n, const int *types
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   const int Ns = c->Ns;
-  const long long total = (long long)Ns * Ns * (Ns / 2 + 1);
   float *o0 = c->sd_slot[slot_of(types[0])], *o1 = n > 1 ? c->sd_slot[slot_of(types[1])] : NULL;
-  k_sd_fold<<<mgp_blocks_for(total, 8), kThreads, 0, c->stream>>>(
+  k_sd_fold<<<mgp_blocks_for((long long)Ns * Ns * 32, 8), kThreads, 0, c->stream>>>(
       (const float2 *)c->sd_dk[0], (const float2 *)c->sd_dk[1], (const float4 *)c->sd_tab, c->g.N, Ns, c->sd_fold, n,
       (float2 *)o0, (float2 *)o1, c->sd_grid / 2);
   MGP_CHECK_LAUNCH();
