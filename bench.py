@@ -43,6 +43,10 @@ CONFIGS = {
     # |fR0| log-uniform in [1e-6, 1e-4]) in one batch, one graph launch per run
     "fofr_batch_64x64_128": dict(Ns=64, N=128, Box=256.0, model="fofr", nsteps=20, seed=6001, fixed=0, nbins=64,
                                  batch=64),
+    # c1 with the whole 10-step run captured into one CUDA graph (the batch
+    # engine with a single box): at this size the step is launch-bound
+    "lcdm_64_128_graph": dict(Ns=64, N=128, Box=256.0, model="lcdm", nsteps=10, seed=5001, fixed=0, nbins=64,
+                              batch=1),
     # COLA step with the learned force closure applied every step (256^3
     # particles on the 256^3 mesh, Box 256 Mpc/h, 30 steps)
     "closure_lcdm_256": dict(Ns=256, N=256, Box=256.0, model="lcdm", nsteps=30, seed=7017, fixed=0, nbins=128,
@@ -95,6 +99,8 @@ BATCH_FR0_SEED = 20260604
 
 
 def batch_boxes(cfg):
+    if cfg["batch"] == 1:  # one box: the whole run as one graph launch
+        return [dict(Seed=cfg["seed"], inverted=0, fofr0=1e-5)]
     rng = np.random.default_rng(BATCH_FR0_SEED)
     f0 = 10 ** rng.uniform(-6.0, -4.0, cfg["batch"] // 2)
     return [dict(Seed=cfg["seed"] + i, inverted=inv, fofr0=float(f0[i])) for i in range(cfg["batch"] // 2)
@@ -180,9 +186,10 @@ def run_batch(args, cfg):
     wall = float(np.mean(walls))
     N = cfg["N"]
     Nc = N ** 3
-    # minimum HBM bytes per box-step of the f(R) step with screening and P(k)
-    # (FP32): 84 Np particle traffic + 92 Nc grid traffic incl. the six FFTs
-    abytes = (84 * Np + 92 * Nc) * B
+    # minimum HBM bytes per box-step (FP32): 84 Np particle traffic + the grid
+    # traffic incl. the FFTs, 92 Nc with MG screening (six FFTs), 52 Nc for
+    # LCDM (four FFTs and the P(k) pass)
+    abytes = (84 * Np + (92 if cfg["model"] in ("fofr", "dgp") else 52) * Nc) * B
     achieved = abytes / (ms * 1e-3 / nst) / 1e9
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
@@ -191,9 +198,12 @@ def run_batch(args, cfg):
         "metric": "Mparticle-steps/s of a batch of independent boxes", "value": round(value, 3), "unit": UNIT,
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / nst, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (2LPT ICs generated on the device, seeds 6001-6032 normal + inverted)",
+        "data": ("synthetic (2LPT ICs generated on the device, seeds %d-%d normal + inverted)"
+                 % (cfg["seed"], cfg["seed"] + B // 2 - 1) if B > 1 else
+                 "synthetic (2LPT IC generated on the device, seed %d)" % cfg["seed"]),
         "config": {"workload": args.config, "boxes": B, "particles_per_box": Np, "mesh": N, "box_mpc_h": cfg["Box"],
-                   "model": "f(R) Hu-Sawicki n=1, screening, |fR0| log-uniform [1e-6, 1e-4] (seed %d)" % BATCH_FR0_SEED,
+                   "model": ("f(R) Hu-Sawicki n=1, screening, |fR0| log-uniform [1e-6, 1e-4] (seed %d)" % BATCH_FR0_SEED
+                             if B > 1 else model_name(cfg)),
                    "steps_per_run": nst, "pofk_every_step": True, "pofk_bins": cfg["nbins"],
                    "launch_budgets": {"tuned": tuning, "default": default_tuning,
                                       "order": "blocks/SM: CIC deposit, grid passes, kick, P(k) binning",
@@ -481,6 +491,7 @@ def oracle_params(O, cfg):
 
 
 SAMPLE = {"ndgp_512_1024": "ndgp_128_256", "ndgp_256_512": "ndgp_128_256", "lcdm_64_128": "lcdm_64_128",
+          "lcdm_64_128_graph": "lcdm_64_128",
           "fofr_batch_64x64_128": "fofr_64_128", "closure_lcdm_256": "lcdm_128_128",
           "fofr_sd_256_512": "fofr_sd_64_128", "fofr_nu_256_512": "fofr_nu_64_128"}
 CONFIGS["fofr_sd_64_128"] = dict(Ns=64, N=128, Box=128.0, model="fofr", nsteps=30, seed=5002, fixed=0, nbins=64,
