@@ -12,22 +12,36 @@ __device__ __forceinline__ void lattice_ijk(long long p, int Ns, int &i, int &j,
   k = (int)(r - (long long)j * Ns);
 }
 
+// The same for p < 2^32 in unsigned 32-bit arithmetic (a 64-bit division is
+// a long instruction sequence on the GPU; the results are identical).
+__device__ __forceinline__ void lattice_ijk(unsigned p, int Ns, int &i, int &j, int &k) {
+  const unsigned ns = (unsigned)Ns, ns2 = ns * ns;
+  const unsigned ii = p / ns2, r = p - ii * ns2, jj = r / ns;
+  i = (int)ii;
+  j = (int)jj;
+  k = (int)(r - jj * ns);
+}
+
 // Cell index and CIC fraction along one axis for the particle at lattice
 // index `li` with displacement `s` (Mpc/h) and global offset `off_cells`.
 // Position in cells = li*N/Ns + s*N/Box + off; the lattice part is split into
 // integer and fractional parts exactly so the small displacement keeps full
-// FP32 precision.
+// FP32 precision.  li*N < Ns*N stays far below 2^32 for any mesh and lattice
+// that fit in device memory, so the split runs in unsigned 32-bit arithmetic.
 __device__ __forceinline__ void cell_frac(int li, float s, float off_cells, int N, int Ns, float scale,
                                           int &idx, float &frac) {
-  long long qn = (long long)li * N;
-  int qi = (int)(qn / Ns);
-  float qf = (float)(qn - (long long)qi * Ns) / (float)Ns;
+  const unsigned qn = (unsigned)li * (unsigned)N;
+  const unsigned qi = qn / (unsigned)Ns;
+  float qf = (float)(qn - qi * (unsigned)Ns) / (float)Ns;
   float w = fmaf(s, scale, off_cells) + qf;
   float fl = floorf(w);
   float fr = w - fl;
   if (fr >= 1.0f) { fr -= 1.0f; fl += 1.0f; }
-  int ic = (qi + (int)fl) % N;
-  if (ic < 0) ic += N;
+  int ic = (int)qi + (int)fl;
+  if (ic < 0 || ic >= N) {  // a particle more than a cell outside its lattice cell's period
+    ic %= N;
+    if (ic < 0) ic += N;
+  }
   idx = ic;
   frac = fr;
 }

@@ -95,7 +95,10 @@ __global__ void __launch_bounds__(MGP_THREADS) k_cic(const float *__restrict__ s
   long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = p0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += stride) {
     int i, j, k;
-    lattice_ijk(p, Ns, i, j, k);
+    if (np <= 0xffffffffLL)
+      lattice_ijk((unsigned)p, Ns, i, j, k);
+    else
+      lattice_ijk(p, Ns, i, j, k);
     int ix, iy, iz;
     float DX, DY, DZ;
     cell_frac(i, sx[p], ox, N, Ns, scale, ix, DX);
@@ -507,7 +510,10 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
   long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
     int i, j, k;
-    lattice_ijk(p, Ns, i, j, k);
+    if (np <= 0xffffffffLL)
+      lattice_ijk((unsigned)p, Ns, i, j, k);
+    else
+      lattice_ijk(p, Ns, i, j, k);
     float sp[3] = {s[p], s[np + p], s[2 * np + p]};
     int ix, iy, iz;
     float DX, DY, DZ;
