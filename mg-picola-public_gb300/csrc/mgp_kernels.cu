@@ -1219,7 +1219,10 @@ __global__ void k_positions(const float *__restrict__ s, const float *__restrict
   const float cv[3] = {(float)st->cv[0], (float)st->cv[1], (float)st->cv[2]};
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
     int li[3];
-    lattice_ijk(p, Ns, li[0], li[1], li[2]);
+    if (np <= 0xffffffffLL)
+      lattice_ijk((unsigned)p, Ns, li[0], li[1], li[2]);
+    else
+      lattice_ijk(p, Ns, li[0], li[1], li[2]);
     for (int a = 0; a < 3; a++) {
       if (pos) pos[3 * p + a] = wrap_box((float)li[a] * dq + (s[a * np + p] + cx[a]), fbox);
       if (vel) vel[3 * p + a] = v[a * np + p] + cv[a];
@@ -1229,7 +1232,7 @@ __global__ void k_positions(const float *__restrict__ s, const float *__restrict
 
 int mgp_launch_positions(const float *s, const mgp_dstate *dst, long long np, int Ns, double box, float *out_pos,
                          float *out_vel, const float *v, cudaStream_t st) {
-  k_positions<<<blocks_for(np, 4), MGP_THREADS, 0, st>>>(s, v, dst, np, Ns, box, out_pos, out_vel);
+  k_positions<<<blocks_for(np, 8), MGP_THREADS, 0, st>>>(s, v, dst, np, Ns, box, out_pos, out_vel);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -1243,7 +1246,10 @@ __global__ void k_set_state(float *__restrict__ s, float *__restrict__ v, const 
   const float dq = (float)(box / (double)Ns), fbox = (float)box, half = 0.5f * (float)box;
   for (long long p = p0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += stride) {
     int li[3];
-    lattice_ijk(p, Ns, li[0], li[1], li[2]);
+    if (np <= 0xffffffffLL)
+      lattice_ijk((unsigned)p, Ns, li[0], li[1], li[2]);
+    else
+      lattice_ijk(p, Ns, li[0], li[1], li[2]);
     for (int a = 0; a < 3; a++) {
       if (pos) {
         float d = pos[3 * p + a] - (float)li[a] * dq;
@@ -1265,7 +1271,7 @@ int mgp_launch_set_state(float *s, float *v, const float *pos, const float *vel,
 int mgp_launch_set_state_range(float *s, float *v, const float *pos, const float *vel, long long np, int Ns,
                                double box, long long p0, long long p1, cudaStream_t st) {
   if (p1 <= p0) return MGP_OK;
-  k_set_state<<<blocks_for(p1 - p0, 4), MGP_THREADS, 0, st>>>(s, v, pos, vel, np, Ns, box, p0, p1);
+  k_set_state<<<blocks_for(p1 - p0, 8), MGP_THREADS, 0, st>>>(s, v, pos, vel, np, Ns, box, p0, p1);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
