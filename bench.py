@@ -2,18 +2,27 @@
 
 Workload (default): nDGP, rc*H0 = 1, density screening on (Gaussian filter,
 Rsmooth 1 Mpc/h), 512^3 particles on a 1024^3 mesh, Box 1024 Mpc/h, 50
-linear-in-a steps from z = 19, seed 5003, amplitude-fixed 2LPT initial
-conditions, P(k) every step in 512 linear bins over [2 pi/Box, k_Nyquist].
-A step is one KDK step: CIC deposit, R2C, P(k) binning, fifth force (smoothing
-C2R, screening, R2C), force k-space pass, three C2R, fused interpolation +
-kick + drift.  Inputs are synthetic (generated by the IC on the device);
-the working set (~50 GB) is far larger than L2, so no L2 flush is needed.
+linear-in-a steps from z = 19 to z = 0, seed 5003, amplitude-fixed 2LPT
+initial conditions, P(k) every step in 512 linear bins over [2 pi/Box,
+k_Nyquist], RSD multipoles at z = 0.
 
-value: Mparticle-steps/s with the particle state resident in HBM.
+One bench step is one whole run of the workload's schedule: fresh 2LPT
+initial conditions (generated on the device, not timed), then all of its KDK
+steps (50 for the default), so the throughput covers the run from z = 19 to
+z = 0, where clustering slows the particle kernels.  A KDK step is the CIC
+deposit, R2C, P(k) binning, fifth force (smoothing C2R, screening, R2C),
+force k-space pass, three C2R and the fused interpolation + kick + drift.
+Inputs are synthetic; the working set (~50 GB) is far larger than L2, so no
+L2 flush is needed.
+
+value: Mparticle-steps/s with the particle state resident in HBM (CUDA
+       events on the context stream around each run's KDK steps).
 e2e:   the same metric through the host-buffer C-ABI call mgp_step_host
-       (pinned host particle arrays copied in and out every step).
+       (pinned host particle arrays copied in and out every KDK step) over
+       one whole run.
 --impl reference: the FP64 CPU oracle (restatement of the reference's C
-       code) timed on the host cores on a bounded sample of the workload.
+       code, particle loops parallel over x slabs as the reference's MPI
+       tasks) timed on the host cores on a bounded sample of the workload.
 """
 import argparse
 import json
@@ -59,6 +68,11 @@ CONFIGS = {
     "fofr_nu_256_512": dict(Ns=256, N=512, Box=512.0, model="fofr", nsteps=30, seed=5002, fixed=0, nbins=256,
                             sd=True, nu=True),
 }
+
+# the closure network alone (random features on a 192^3 mesh): one forward
+# or one Adam step per bench step; the convolution kernels' profiling workload
+CONFIGS["closure_fwd_192"] = dict(N=192, probe=True)
+CONFIGS["closure_train_192"] = dict(N=192, probe=True, train=True)
 
 SD_GRID = dict(sd_nk=512, sd_kmin=1e-4, sd_kmax=10.0)
 _NU_INFO = []
@@ -150,14 +164,23 @@ def job_value(world, Np, steps, elapsed):
     return world * Np * steps / elapsed / 1e6
 
 
-def run_batch(args, cfg):
+def shard(items, rank, world):
+    """The boxes of rank r: r, r + world, r + 2 world, ... (independent
+    boxes need no collective; each rank runs its share as one batch)."""
+    return items[rank::world]
+
+
+def run_batch(args, cfg, rank=0, world=1, dist=None):
     """A batch of independent boxes: each timed step is one graph launch that
     runs the whole KDK loop of every box; value counts particle-steps of all
-    boxes (drift steps; the final output kick is included in the time)."""
+    boxes (drift steps; the final output kick is included in the time).
+    With several ranks the boxes are split across them (shard) and the job's
+    time is the slowest rank's."""
     import mgpicola as M
 
     p = make_params(M, cfg)
-    boxes = batch_boxes(cfg)
+    all_boxes = batch_boxes(cfg)
+    boxes = shard(all_boxes, rank, world)
     B, Np, nst = len(boxes), cfg["Ns"] ** 3, cfg["nsteps"]
     batch = M.Batch(p, boxes)
     default_tuning = batch.tuning()
@@ -181,9 +204,10 @@ def run_batch(args, cfg):
     ic_ms = batch.ms(1)
     nodes = batch.graph_nodes()
     batch.close()
-    ms = float(np.mean(times))
-    value = B * Np * nst / (ms * 1e-3) / 1e6
-    wall = float(np.mean(walls))
+    ms = reduce_max(float(np.mean(times)), dist)
+    wall = reduce_max(float(np.mean(walls)), dist)
+    B_job = len(all_boxes)
+    value = B_job * Np * nst / (ms * 1e-3) / 1e6
     N = cfg["N"]
     Nc = N ** 3
     # minimum HBM bytes per box-step (FP32): 84 Np particle traffic + the grid
@@ -196,12 +220,13 @@ def run_batch(args, cfg):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     out = {
         "metric": "Mparticle-steps/s of a batch of independent boxes", "value": round(value, 3), "unit": UNIT,
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / nst, 4),
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": ("synthetic (2LPT ICs generated on the device, seeds %d-%d normal + inverted)"
                  % (cfg["seed"], cfg["seed"] + B // 2 - 1) if B > 1 else
                  "synthetic (2LPT IC generated on the device, seed %d)" % cfg["seed"]),
-        "config": {"workload": args.config, "boxes": B, "particles_per_box": Np, "mesh": N, "box_mpc_h": cfg["Box"],
+        "config": {"workload": args.config, "boxes": B_job, "boxes_per_rank": B, "particles_per_box": Np, "mesh": N,
+                   "box_mpc_h": cfg["Box"], "step": "one graph launch: all %d KDK steps of every box" % nst,
                    "model": ("f(R) Hu-Sawicki n=1, screening, |fR0| log-uniform [1e-6, 1e-4] (seed %d)" % BATCH_FR0_SEED
                              if B > 1 else model_name(cfg)),
                    "steps_per_run": nst, "pofk_every_step": True, "pofk_bins": cfg["nbins"],
@@ -210,8 +235,8 @@ def run_batch(args, cfg):
                                       "autotune_s": round(tune_s, 2), "graph_ms_default": round(default_ms, 3),
                                       "graph_ms_tuned": round(tuned_ms, 3)},
                    "l2": "working set %.1f GB > L2" % (B * (6 * 4 * N * N * 2 * (N // 2 + 1) + 48 * Np) / 1e9)},
-        "e2e": {"value": round(B * Np * nst / wall / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": int(B * cfg["nbins"] * 8 / nst), "api": "mgp_batch_run + mgp_batch_pofk",
+        "e2e": {"value": round(B_job * Np * nst / wall / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(B * cfg["nbins"] * 8), "api": "mgp_batch_run + mgp_batch_pofk",
                 "includes": "2LPT ICs of all boxes, graph launch, per-box P(k) read-back"},
         "gpu_launches": int(launches * args.steps),
         "graph": {"launches_per_run": 1, "nodes": nodes, "own_kernels": launches, "ic_ms": round(ic_ms, 3)},
@@ -222,10 +247,13 @@ def run_batch(args, cfg):
                      "algorithmic_bytes_per_step": abytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "clocks": clk.summary(),
     }
-    if not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args)
         out["pofk_check"] = pofk_check(args.config)
-    print(json.dumps(out))
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
 
 
 class ClockSampler:
@@ -301,6 +329,10 @@ def measured_traffic(N, Np, kernel):
     return int(TRAFFIC_256_512[kernel] * (N / 512.0) ** 3)
 
 
+STAGES = ["fill", "cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "lpt_fields", "closure",
+          "closure_conv"]
+
+
 def run_gpu(args):
     import mgpicola as M
 
@@ -310,8 +342,8 @@ def run_gpu(args):
     os.sync()
 
     cfg = CONFIGS[args.config]
-    if cfg.get("batch"):
-        return run_batch(args, cfg)
+    if cfg.get("probe"):
+        return run_closure_probe(args, cfg)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -321,89 +353,109 @@ def run_gpu(args):
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+    if cfg.get("batch"):
+        return run_batch(args, cfg, rank, world, dist)
     p = make_params(M, cfg)
     p.Seed = rank_seed(cfg, rank)
     Np = cfg["Ns"] ** 3
     N = cfg["N"]
+    nst = cfg["nsteps"]
     ctx = M.Context(p, device=local if world > 1 else 0)
     closure = None
     if cfg.get("closure"):
         closure = M.Closure(N, seed=cfg["seed"], device=local if world > 1 else 0)  # He-normal init weights
         closure.attach(ctx)
-    ctx.displacement_fields()
     A0 = 1.0 / (1.0 + p.Init_Redshift)
-    da = (1.0 - A0) / cfg["nsteps"]
-    state = {"A": A0, "AI": A0}
+    da = (1.0 - A0) / nst
 
-    def step():
-        A, AI = state["A"], state["AI"]
-        AF, AFF = A + 0.5 * da, A + da
-        ctx.step(A, AI, AF, AFF)
-        state["A"], state["AI"] = AFF, AF
+    def schedule():
+        """(A, AI, AF, AFF) of the nst linear-in-a KDK steps (src/main.c:394-611)."""
+        A, AI = A0, A0
+        for _ in range(nst):
+            AF, AFF = A + 0.5 * da, A + da
+            yield A, AI, AF, AFF
+            A, AI = AFF, AF
 
-    def sync():
-        # mgp_kernel_ms synchronises the context stream on its last event
-        ctx.kernel_ms("interp_kick_drift")
+    def run(timed=False):
+        """One bench step: the IC (not timed), then the whole schedule
+        bracketed by events on the context stream.  Returns the device ms,
+        this library's launches of the KDK steps and, when timed, the stage
+        ms of every KDK step."""
+        ctx.displacement_fields()
+        if timed:
+            ctx.set_timing(True, history=nst)
+        l0 = ctx.launches()
+        ctx.mark(0)
+        for a in schedule():
+            ctx.step(*a)
+        ctx.mark(1)
+        ms = ctx.mark_ms(0, 1)
+        launches = ctx.launches() - l0
+        stages = None
+        if timed:
+            stages = [{k: max(0.0, ctx.kernel_ms_step(k, i)) for k in STAGES + ["step"]} for i in range(nst)]
+            ctx.set_timing(False)
+        return ms, launches, stages
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
     for _ in range(args.warmup):
-        step()
-    ctx.set_timing(True)
-    sync()
+        run()
     barrier()
-    launches0 = ctx.launches()
-    stage_ms = {k: 0.0 for k in ["fill", "cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "lpt_fields",
-                                 "closure", "closure_conv"]}
+    run_ms, launches, per_step = [], 0, []
     with ClockSampler(local) as clk:
-        t0 = time.perf_counter()
-        dev_ms = 0.0
         for _ in range(args.steps):
-            step()
-            dev_ms += ctx.kernel_ms("step")  # CUDA events around the whole step
-            for k in stage_ms:
-                v = ctx.kernel_ms(k)
-                if v > 0:
-                    stage_ms[k] += v
-        wall = time.perf_counter() - t0
-    elapsed = dev_ms * 1e-3
-    launches = ctx.launches() - launches0
+            ms, nl, st = run(timed=True)
+            run_ms.append(ms)
+            launches += nl
+            per_step.append(st)
     barrier()
-    elapsed = reduce_max(elapsed, dist)
-    ms_per_step = elapsed / args.steps * 1e3
-    value = job_value(world, Np, args.steps, elapsed)
+    elapsed = reduce_max(sum(run_ms) * 1e-3, dist)
+    ms_per_run = elapsed / args.steps * 1e3
+    value = job_value(world, Np, args.steps * nst, elapsed)
+    # stage ms per KDK step, averaged over the timed runs, overall and per
+    # decile of the schedule
+    stage_ms = {k: float(np.mean([[st[i][k] for i in range(nst)] for st in per_step])) for k in STAGES}
+    deciles = []
+    for d in range(10):
+        lo, hi = d * nst // 10, (d + 1) * nst // 10
+        if hi > lo:
+            row = {k: round(float(np.mean([[st[i][k] for i in range(lo, hi)] for st in per_step])), 4)
+                   for k in STAGES + ["step"] if any(st[i][k] > 0 for st in per_step for i in range(lo, hi))}
+            row["steps"] = [lo, hi - 1]
+            deciles.append(row)
 
-    # e2e through the host-buffer C-ABI entry point, pinned host memory
-    ctx.set_timing(False)
+    # e2e through the host-buffer C-ABI entry point, pinned host memory: one
+    # whole run from the IC state
+    ctx.displacement_fields()
     pos, vel, d1, d2 = ctx.get_particles()
     for a in (pos, vel, d1, d2):
         M.pin(a)
-    e2e_steps = max(1, min(args.steps, 10))
 
-    def host_step():
-        A, AI = state["A"], state["AI"]
-        AF, AFF = A + 0.5 * da, A + da
+    def host_step(a):
         t0 = time.perf_counter()
-        ctx.step_host(A, AI, AF, AFF, pos, vel, d1, d2)
-        state["A"], state["AI"] = AFF, AF
+        ctx.step_host(*a, pos, vel, d1, d2)
         return time.perf_counter() - t0
 
-    host_step()  # untimed: allocates the staging buffers and the copy stream
     barrier()
-    e2e_ms = [host_step() * 1e3 for _ in range(e2e_steps)]
+    e2e_ms = [host_step(a) * 1e3 for a in schedule()]
     e2e_t = reduce_max(sum(e2e_ms) * 1e-3, dist)
     for a in (pos, vel, d1, d2):
         M.unpin(a)
-    e2e_val = job_value(world, Np, e2e_steps, e2e_t)
-    # RSD multipoles P0/P2/P4 of the final state (compute_RSD_powerspectrum,
-    # src/compute_pofk.c:403-512: y and z lines of sight, averaged), timed
-    # end to end on the host (two redshift-space deposits, two R2C, binning)
+    e2e_val = job_value(world, Np, nst, e2e_t)
+    # RSD multipoles P0/P2/P4 at z = 0 of that run's final state
+    # (compute_RSD_powerspectrum, src/compute_pofk.c:403-512: y and z lines
+    # of sight, averaged), timed end to end on the host (two
+    # redshift-space deposits, two R2C, binning)
     ctx.kernel_ms("interp_kick_drift")  # synchronise before timing
     t0 = time.perf_counter()
-    rsd = ctx.pofk_rsd(state["A"])
+    rsd = ctx.pofk_rsd(1.0)
     rsd_ms = (time.perf_counter() - t0) * 1e3
+    full_check = None
+    if rank == 0 and not args.no_cpu_baseline:
+        full_check = fullsize_check(ctx, cfg, args.config, schedule)
     ctx.close()
     if closure is not None:
         closure.close()
@@ -411,7 +463,7 @@ def run_gpu(args):
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
     # stages that are one own kernel (the "mg" stage wraps two cuFFT calls)
-    own = {k: v / args.steps for k, v in stage_ms.items() if k in ("cic", "pofk", "forces", "interp_kick_drift")}
+    own = {k: v for k, v in stage_ms.items() if k in ("cic", "pofk", "forces", "interp_kick_drift") and v > 0}
     dom = max(own, key=own.get)
     abytes = algorithmic_bytes(N, Np, dom)
     achieved = abytes / (own[dom] * 1e-3) / 1e9
@@ -421,9 +473,10 @@ def run_gpu(args):
             "frac": round(achieved / peak, 4), "traffic": traffic,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at 256^3 particles / "
                               "512^3 mesh, scaled by particles and cells",
-            "algorithmic_bytes_per_launch": abytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+            "algorithmic_bytes_per_launch": abytes, "mean_launch_ms": round(own[dom], 4),
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
     if closure is not None:
-        conv_ms = stage_ms["closure_conv"] / args.steps
+        conv_ms = stage_ms["closure_conv"]
         fl = closure_flops(N)
         tf = fl / (conv_ms * 1e-3) / 1e12
         bpeak = float(peaks.get("bf16_tflops_sustained", 1700.0))
@@ -431,24 +484,30 @@ def run_gpu(args):
                 "peak": bpeak, "unit": "TFLOP/s", "frac": round(tf / bpeak, 4), "traffic": None,
                 "algorithmic_flops_per_forward": fl, "conv_ms_per_step": round(conv_ms, 4),
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed inside the step)"}
+    h2d = (2 if cfg.get("sd") else 4) * 12 * Np  # scale-dependent growth: the step assigns its own D1/D2
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_run, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (2LPT IC generated on the device, seed 5003)",
+        "data": "synthetic (2LPT IC generated on the device, seed %d)" % cfg["seed"],
         "config": {"workload": args.config, "particles": Np, "mesh": N, "box_mpc_h": cfg["Box"],
                    "model": model_name(cfg)
                    + (" + learned force closure (4x 3^3 conv, 16 ch, BF16/FP32 acc)" if closure is not None else ""),
+                   "step": "one whole run: IC (untimed) + %d KDK steps z = 19 -> 0" % nst,
+                   "kdk_steps_per_step": nst, "ms_per_kdk_step": round(ms_per_run / nst, 4),
                    "pofk_every_step": True, "pofk_bins": cfg["nbins"], "l2": "inputs larger than L2",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas (one box per rank)" if world > 1 else "single GPU"},
         "e2e": {"value": round(e2e_val, 3), "unit": UNIT,
-                # scale-dependent growth: the step assigns its own D1/D2, only pos/vel go up
-                "h2d_bytes_per_step": (2 if cfg.get("sd") else 4) * 12 * Np,
-                "d2h_bytes_per_step": 2 * 12 * Np, "api": "mgp_step_host",
-                "step_ms": [round(x, 2) for x in e2e_ms]},
+                "h2d_bytes_per_step": h2d * nst, "d2h_bytes_per_step": 2 * 12 * Np * nst,
+                "h2d_bytes_per_kdk_step": h2d, "d2h_bytes_per_kdk_step": 2 * 12 * Np,
+                "api": "mgp_step_host", "runs": 1,
+                "kdk_step_ms": {"mean": round(float(np.mean(e2e_ms)), 2), "max": round(float(np.max(e2e_ms)), 2),
+                                "min": round(float(np.min(e2e_ms)), 2)}},
         "gpu_launches": int(launches),
-        "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stage_ms.items()},
-        "rsd_multipoles": {"ms": round(rsd_ms, 3), "bins": int(len(rsd[0])), "a": round(state["A"], 5),
+        "stage_ms_per_kdk_step": {k: round(v, 4) for k, v in stage_ms.items()},
+        "stage_ms_by_decile": deciles,
+        "run_ms": [round(x, 2) for x in run_ms],
+        "rsd_multipoles": {"ms": round(rsd_ms, 3), "bins": int(len(rsd[0])), "a": 1.0,
                            "los": "y and z, averaged (compute_RSD_powerspectrum)"},
         "roofline": roof,
         "clocks": clk.summary(),
@@ -456,10 +515,46 @@ def run_gpu(args):
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args)
         out["pofk_check"] = pofk_check(args.config)
+        if full_check is not None:
+            out["pofk_check_fullsize"] = full_check
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_closure_probe(args, cfg):
+    """The closure network alone on an N^3 mesh (random features): each step
+    is one forward (4 convolution layers) or, with train, one Adam step on
+    N^3 random particles.  Used for the convolution kernels' profiles."""
+    import mgpicola as M
+
+    N = cfg["N"]
+    rng = np.random.default_rng(1)
+    x = rng.normal(0, 1, (N ** 3, 3)).astype(np.float32)
+    with M.Closure(N, seed=3) as cl:
+        cl.set_sample(x, None)
+        if cfg.get("train"):
+            cells = np.minimum(rng.uniform(0, N, (N ** 3, 3)).astype(np.float32), np.float32(N - 1e-3))
+            cl.set_particle_sample(cells, rng.normal(0, 1, (N ** 3, 3)).astype(np.float32))
+            work = lambda: cl.train_step(1e-4)  # noqa: E731
+        else:
+            work = cl.forward
+        for _ in range(args.warmup):
+            work()
+        with ClockSampler(0) as clk:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                work()
+            wall = time.perf_counter() - t0
+    fl = closure_flops(N) * (3 if cfg.get("train") else 1)
+    print(json.dumps({"metric": "closure %s TFLOP/s" % ("training step" if cfg.get("train") else "forward"),
+                      "value": round(fl * args.steps / wall / 1e12, 3), "unit": "TFLOP/s", "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 3),
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+                      "data": "synthetic (random features)", "config": {"workload": args.config, "mesh": N},
+                      "note": "host wall clock per call (each call synchronises); a profiling workload",
+                      "clocks": clk.summary()}))
 
 
 _KEEP = []
@@ -503,14 +598,34 @@ CONFIGS["lcdm_128_128"] = dict(Ns=128, N=128, Box=128.0, model="lcdm", nsteps=30
 CONFIGS["ndgp_128_256"] = dict(Ns=128, N=256, Box=256.0, model="dgp", nsteps=50, seed=5003, fixed=1, nbins=128)
 
 
+FIXTURE_CHECK = {"ndgp_512_1024": "ndgp_256_512_50", "ndgp_256_512": "ndgp_256_512_50"}
+
+
 def pofk_check(config):
-    """P(k) relative error against the FP64 oracle, stated with the throughput:
-    the same model, seed and IC type at 64^3 particles / 128^3 mesh (the
-    512^3/1024^3 run is far beyond what the FP64 oracle can redo on the host),
-    run to z = 0 on the GPU and through the oracle's KDK loop; the maximum
-    |P_gpu / P_oracle - 1| over the bins with k <= 0.5 h/Mpc."""
+    """P(k) relative error against the FP64 oracle, stated with the throughput.
+    For the nDGP workloads: the same model, seed and IC type at the workload's
+    cell size (256^3 particles / 512^3 mesh, Box 512, the full 50-step
+    schedule to z = 0) against the stored FP64 oracle run of that case
+    (tests/golden/orc_ndgp_256_512_50.npz); for the others the same model at
+    64^3 particles / 128^3 mesh, run to z = 0 on the GPU and through the
+    oracle's KDK loop in this job.  The maximum |P_gpu / P_oracle - 1| over
+    the bins with k <= 0.5 h/Mpc."""
     import mgpicola as M
     from oracle import oracle as O
+    from tests.golden import oracle_runs as R
+
+    fx = FIXTURE_CHECK.get(config)
+    ref = R.load(fx) if fx else None
+    if ref is not None:
+        c = R.CASES[fx]
+        with M.Context(R.gpu_params(M, c)) as ctx:
+            k, pk, pos = R.gpu_run(ctx, c)
+        out = R.compare(ref, k, pk, pos)
+        out["case"] = ("%s at 256^3 particles / 512^3 mesh, Box 512, %d steps z = 19 -> 0, seed %d, vs the stored "
+                       "FP64 oracle run (tests/golden/orc_%s.npz)" % (model_name(CONFIGS[config]), c["nsteps"],
+                                                                     c["seed"], fx))
+        out["max_rel_err"] = float("%.3g" % out["max_rel_err"])
+        return out
 
     cfg = dict(CONFIGS[config], Ns=64, N=128, Box=256.0, nsteps=10, nbins=64)
     cfg.pop("closure", None)
@@ -547,6 +662,27 @@ def pofk_check(config):
                     % (model_name(cfg), cfg["seed"], note)}
 
 
+def fullsize_check(ctx, cfg, config, schedule):
+    """The 512^3 / 1024^3 workload itself against the stored FP64 oracle run
+    of its first steps (tests/golden/orc_ndgp_512_1024_3.npz): the bench's
+    own context redoes the IC and those steps."""
+    from tests.golden import oracle_runs as R
+
+    if config != "ndgp_512_1024":
+        return None
+    ref = R.load("ndgp_512_1024_3")
+    if ref is None:
+        return None
+    c = R.CASES["ndgp_512_1024_3"]
+    k, pk, pos = R.gpu_run(ctx, c)
+    out = R.compare(ref, k, pk, pos)
+    out["max_rel_err"] = float("%.3g" % out["max_rel_err"])
+    out["case"] = ("the workload itself (512^3 / 1024^3, seed %d) at the start of step %d of its %d-step schedule vs "
+                   "the stored FP64 oracle run (tests/golden/orc_ndgp_512_1024_3.npz)" % (c["seed"], c["stop"],
+                                                                                         c["nsteps"]))
+    return out
+
+
 def cpu_baseline(args, nsteps=1):
     from oracle import oracle as O
 
@@ -555,9 +691,10 @@ def cpu_baseline(args, nsteps=1):
     dt = O.lib().orc_time_steps(oracle_params(O, cfg), nsteps)
     Np = cfg["Ns"] ** 3
     return {"value": round(Np / dt / 1e6, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d full FP64 KDK step(s) of the same model at %d^3 particles / %d^3 mesh (Box %g), "
-                      "OpenMP FFTs on all host cores, serial CIC/interp as the reference; per-particle cost at "
-                      "512^3/1024^3 is higher (FFT ~ N^3 log N)" % (nsteps, cfg["Ns"], cfg["N"], cfg["Box"])}
+            "sample": "%d full FP64 KDK step(s) of the same model at %d^3 particles / %d^3 mesh (Box %g) on %d "
+                      "threads: OpenMP FFTs, CIC over x slabs with per-thread ghost slices and the other particle "
+                      "and grid loops parallel, the reference's MPI-task shape; per-particle cost at 512^3/1024^3 "
+                      "is higher (FFT ~ N^3 log N)" % (nsteps, cfg["Ns"], cfg["N"], cfg["Box"], os.cpu_count())}
 
 
 def run_reference(args):
@@ -575,7 +712,9 @@ def run_reference(args):
     Np = cfg["Ns"] ** 3
     v = Np / dt / 1e6
     cb = {"value": round(v, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-          "sample": "FP64 oracle KDK steps at %d^3 particles / %d^3 mesh, same model" % (cfg["Ns"], cfg["N"])}
+          "sample": "FP64 oracle KDK steps at %d^3 particles / %d^3 mesh, same model, %d threads (OpenMP FFTs, "
+                    "CIC over x slabs with per-thread ghost slices, parallel particle and grid loops)"
+                    % (cfg["Ns"], cfg["N"], os.cpu_count())}
     print(json.dumps({"metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": 0, "steps": args.steps,
                       "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
                       "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -595,6 +734,12 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one rank per GPU: start them under torch's launcher on this node
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(args.gpus),
+               "--master-addr", "127.0.0.1", "--master-port", os.environ.get("MGP_BENCH_PORT", "29533"),
+               os.path.abspath(__file__)] + sys.argv[1:]
+        sys.exit(subprocess.call(cmd))
     if args.impl == "reference":
         run_reference(args)
     else:

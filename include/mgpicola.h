@@ -429,20 +429,33 @@ int mgp_copy_grid(mgp_ctx *ctx, int which, float *host, size_t count);
  * "mg", "step" = the whole mgp_step); returns -1 if not timed.  Timing is on when enable != 0. */
 int mgp_set_timing(mgp_ctx *ctx, int enable);
 double mgp_kernel_ms(mgp_ctx *ctx, const char *name);
+/* Caller marks (no counterpart in the reference, whose timer.c reads the
+ * host clock): mgp_mark records event `slot` (0..3) on the context's stream;
+ * mgp_mark_ms waits for mark `to` and returns the device milliseconds from
+ * mark `from` to it (-1 on error).  Brackets whole runs without per-step
+ * synchronisation. */
+int mgp_mark(mgp_ctx *ctx, int slot);
+/* With mgp_set_timing(ctx, n) for n > 1 the stage events of the last n
+ * mgp_step calls are kept: milliseconds of stage `name` in step `step`
+ * (counted from that mgp_set_timing call), -1 if not kept or not timed. */
+double mgp_kernel_ms_step(mgp_ctx *ctx, const char *name, int step);
+double mgp_mark_ms(mgp_ctx *ctx, int from, int to);
 /* P(k) binning for callers that cannot allocate (no counterpart in the
  * reference): for code running inside another framework's memory pool or
  * allocator hooks, or that must not let cudaMalloc/cudaFree synchronise the
  * device.  Bins the caller's delta(k) grid (device pointer, complex
  * [Nmesh][Nmesh][Nmesh/2+1] float pairs, the R2C of a CIC density) exactly as
  * mgp_pofk does, with every scratch buffer in one fixed-size device array
- * owned by the library (about 8 MB, held on each device that loads the
+ * owned by the library (about 11.4 MB, held on each device that loads the
  * library until exit); it calls no cudaMalloc, cudaFree or other allocating
- * routine.  Limits: even Nmesh <= 1024, at most 2048 bins after the
+ * routine.  Results are bit-reproducible from call to call.  Limits: even Nmesh <= 1024, at most 2048 bins after the
  * reference's parameter adjustment; larger requests return MGP_EINVAL.  Runs
  * on the current device and on `stream` (NULL = legacy default stream) and
  * returns after the results are in the host arrays.  The first call on a
- * device looks up the array's device address.  All calls share the array:
- * calls whose GPU work overlaps race and must be serialised by the caller. */
+ * device looks up the array's device address and keeps it for the process,
+ * so do not call it on a device after cudaDeviceReset.  All calls share the
+ * array: calls whose GPU work overlaps race and must be serialised by the
+ * caller. */
 int mgp_pofk_noalloc(const float *d_deltak, int Nmesh, int Nsample, double Box, int nbins, int bintype,
                      int subtract_shotnoise, double kmin, double kmax, int cap, int *nbins_out, double *k,
                      double *pk, double *kmean, double *n, void *stream);

@@ -195,24 +195,6 @@ def run_c5(model, Nc=256, r=3, box=256.0, nsteps=30, train_seeds=range(7001, 701
     return out
 
 
-def kernel_probe(N, train=False, reps=3, seed=1):
-    """A fixed closure workload for profiling: random features on an N^3
-    mesh, then `reps` forward passes (or, with train, `reps` Adam steps on a
-    particle sample of N^3 random particles)."""
-    rng = np.random.default_rng(seed)
-    x = rng.normal(0, 1, (N ** 3, 3)).astype(np.float32)
-    with M.Closure(N, seed=3) as cl:
-        cl.set_sample(x, None)
-        if train:
-            cells = np.minimum(rng.uniform(0, N, (N ** 3, 3)).astype(np.float32), np.float32(N - 1e-3))
-            cl.set_particle_sample(cells, rng.normal(0, 1, (N ** 3, 3)).astype(np.float32))
-            for _ in range(reps):
-                cl.train_step(1e-4)
-        else:
-            for _ in range(reps):
-                cl.forward()
-
-
 def main(argv=None):
     import argparse
     import json
@@ -230,12 +212,7 @@ def main(argv=None):
                     help="cutoff wavelength (cells) of the closure output's high-pass")
     ap.add_argument("--out", default=None, help="JSON report")
     ap.add_argument("--weights", default=None, help=".npz for the trained weights")
-    ap.add_argument("--probe", type=int, default=0, help="profiling workload on an N^3 mesh instead of training")
-    ap.add_argument("--probe-train", action="store_true", help="the probe runs Adam steps")
     a = ap.parse_args(argv)
-    if a.probe:
-        kernel_probe(a.probe, train=a.probe_train)
-        return None
     rep = run_c5(a.model, Nc=a.nmesh, box=float(a.nmesh), train_seeds=range(7001, 7001 + a.ntrain),
                  test_seeds=range(7017, 7017 + a.ntest), every=a.every, epochs=a.epochs, lr=a.lr,
                  band=not a.full_target, weights_out=a.weights, highpass=a.highpass)

@@ -41,20 +41,79 @@ static const char *k_timer_names[MGP_NTIMERS] = {"cic",    "r2c",  "pofk",      
                                                    "closure_conv", "fill"};
 
 static void tstart(mgp_ctx *c, int t) {
-  if (c->timing) cudaEventRecord(c->ev[t][0], c->stream);
+  if (c->timing) {
+    cudaEventRecord(c->ev[t][0], c->stream);
+    if (c->hev) {
+      const int slot = c->hstep % c->hcap;
+      cudaEventRecord(c->hev[((size_t)slot * MGP_NTIMERS + t) * 2], c->stream);
+    }
+  }
 }
 static void tstop(mgp_ctx *c, int t) {
   if (c->timing) {
     cudaEventRecord(c->ev[t][1], c->stream);
     c->timed[t] = 1;
+    if (c->hev) {
+      const int slot = c->hstep % c->hcap;
+      cudaEventRecord(c->hev[((size_t)slot * MGP_NTIMERS + t) * 2 + 1], c->stream);
+      c->htimed[(size_t)slot * MGP_NTIMERS + t] = 1;
+    }
   }
+}
+
+static void free_history(mgp_ctx *c) {
+  if (c->hev)
+    for (int i = 0; i < c->hcap * MGP_NTIMERS * 2; i++)
+      if (c->hev[i]) cudaEventDestroy(c->hev[i]);
+  free(c->hev);
+  free(c->htimed);
+  c->hev = NULL;
+  c->htimed = NULL;
+  c->hcap = c->hstep = 0;
 }
 
 extern "C" int mgp_set_timing(mgp_ctx *c, int enable) {
   if (!c) return mgp_set_error(MGP_EINVAL, "null context");
   c->timing = enable ? 1 : 0;
   for (int t = 0; t < MGP_NTIMERS; t++) c->timed[t] = 0;
+  if (enable > 1) {
+    // keep the stage events of the last `enable` steps
+    if (c->hcap != enable) {
+      MGP_CUDA(cudaStreamSynchronize(c->stream));
+      free_history(c);
+      const size_t ne = (size_t)enable * MGP_NTIMERS * 2;
+      c->hev = (cudaEvent_t *)calloc(ne, sizeof(cudaEvent_t));
+      c->htimed = (unsigned char *)calloc((size_t)enable * MGP_NTIMERS, 1);
+      if (!c->hev || !c->htimed) {
+        free_history(c);
+        return mgp_set_error(MGP_ENOMEM, "timing history of %d steps", enable);
+      }
+      c->hcap = enable;
+      for (size_t i = 0; i < ne; i++) MGP_CUDA(cudaEventCreate(&c->hev[i]));
+    }
+    memset(c->htimed, 0, (size_t)c->hcap * MGP_NTIMERS);
+    c->hstep = 0;
+  } else if (c->hev) {
+    MGP_CUDA(cudaStreamSynchronize(c->stream));
+    free_history(c);
+  }
   return MGP_OK;
+}
+
+extern "C" double mgp_kernel_ms_step(mgp_ctx *c, const char *name, int step) {
+  if (!c || !name || !c->hev || step < 0 || step >= c->hstep || step < c->hstep - c->hcap) return -1.0;
+  const int slot = step % c->hcap;
+  for (int t = 0; t < MGP_NTIMERS; t++) {
+    if (strcmp(name, k_timer_names[t]) == 0) {
+      if (!c->htimed[(size_t)slot * MGP_NTIMERS + t]) return -1.0;
+      cudaEvent_t *e = c->hev + ((size_t)slot * MGP_NTIMERS + t) * 2;
+      float ms = 0.f;
+      if (cudaEventSynchronize(e[1]) != cudaSuccess) return -1.0;
+      if (cudaEventElapsedTime(&ms, e[0], e[1]) != cudaSuccess) return -1.0;
+      return ms;
+    }
+  }
+  return -1.0;
 }
 
 extern "C" double mgp_kernel_ms(mgp_ctx *c, const char *name) {
@@ -69,6 +128,20 @@ extern "C" double mgp_kernel_ms(mgp_ctx *c, const char *name) {
     }
   }
   return -1.0;
+}
+
+extern "C" int mgp_mark(mgp_ctx *c, int slot) {
+  if (!c || slot < 0 || slot > 3) return mgp_set_error(MGP_EINVAL, "mark slot %d out of range", slot);
+  MGP_CUDA(cudaEventRecord(c->ev_mark[slot], c->stream));
+  return MGP_OK;
+}
+
+extern "C" double mgp_mark_ms(mgp_ctx *c, int from, int to) {
+  if (!c || from < 0 || from > 3 || to < 0 || to > 3) return -1.0;
+  float ms = 0.f;
+  if (cudaEventSynchronize(c->ev_mark[to]) != cudaSuccess) return -1.0;
+  if (cudaEventElapsedTime(&ms, c->ev_mark[from], c->ev_mark[to]) != cudaSuccess) return -1.0;
+  return ms;
 }
 
 extern "C" long long mgp_launch_count(mgp_ctx *c) { return c ? mgp_kernel_launches() : -1; }
@@ -302,7 +375,9 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
     if (c->nu_ev[q]) cudaEventDestroy(c->nu_ev[q]);
   for (int k = 0; k < MGP_POS_CHUNKS; k++)
     if (c->ev_chunk[k]) cudaEventDestroy(c->ev_chunk[k]);
+  free_history(c);
   for (int t = 0; t < MGP_NTIMERS; t++) {
+    if (t < 4 && c->ev_mark[t]) cudaEventDestroy(c->ev_mark[t]);
     if (c->ev[t][0]) cudaEventDestroy(c->ev[t][0]);
     if (c->ev[t][1]) cudaEventDestroy(c->ev[t][1]);
   }
@@ -388,6 +463,7 @@ static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxe
   TRYCUDA(cudaSetDevice(device));
   TRYCUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   for (int t = 0; t < MGP_NTIMERS; t++) {
+    if (t < 4) TRYCUDA(cudaEventCreate(&c->ev_mark[t]));
     TRYCUDA(cudaEventCreate(&c->ev[t][0]));
     TRYCUDA(cudaEventCreate(&c->ev[t][1]));
   }
@@ -925,6 +1001,10 @@ extern "C" int mgp_step(mgp_ctx *c, double A, double AI, double AF, double AFF) 
   }
   RET_IF(mgp_kick_drift(c, AI, AF, A, AFF, 1));
   tstop(c, T_MISC);
+  if (c->timing && c->hev) {
+    c->hstep++;
+    memset(c->htimed + (size_t)(c->hstep % c->hcap) * MGP_NTIMERS, 0, MGP_NTIMERS);
+  }
   return MGP_OK;
 }
 

@@ -46,4 +46,41 @@ __device__ __forceinline__ void cell_frac(int li, float s, float off_cells, int 
   frac = fr;
 }
 
+// Power-of-two lattices (Ns = 2^ls, the usual set-ups): the same lattice
+// coordinates and cell fractions by shifts and masks.  The results are
+// identical to lattice_ijk / cell_frac: the remainder of qn / Ns is below
+// 2^24, so rem * (1/Ns) is exact in FP32 as rem / Ns is.
+__device__ __forceinline__ void lattice_ijk_p2(unsigned p, int ls, int &i, int &j, int &k) {
+  const unsigned m = (1u << ls) - 1u;
+  i = (int)(p >> (2 * ls));
+  j = (int)((p >> ls) & m);
+  k = (int)(p & m);
+}
+
+__device__ __forceinline__ void cell_frac_p2(int li, float s, float off_cells, int N, int ls, float inv_ns, float scale,
+                                             int &idx, float &frac) {
+  const unsigned qn = (unsigned)li * (unsigned)N;
+  const unsigned qi = qn >> ls;
+  float qf = (float)(qn & ((1u << ls) - 1u)) * inv_ns;
+  float w = fmaf(s, scale, off_cells) + qf;
+  float fl = floorf(w);
+  float fr = w - fl;
+  if (fr >= 1.0f) { fr -= 1.0f; fl += 1.0f; }
+  int ic = (int)qi + (int)fl;
+  if (ic < 0 || ic >= N) {
+    ic %= N;
+    if (ic < 0) ic += N;
+  }
+  idx = ic;
+  frac = fr;
+}
+
+// log2(Ns) when Ns is a power of two, else -1 (host and device).
+__host__ __device__ __forceinline__ int lattice_log2(int Ns) {
+  if (Ns <= 0 || (Ns & (Ns - 1))) return -1;
+  int l = 0;
+  while ((1 << l) < Ns) l++;
+  return l;
+}
+
 #endif

@@ -161,11 +161,18 @@ struct mgp_ctx {
   /* learned force closure added to the force grids (mgp_set_closure) */
   struct mgp_closure *closure;
 
-  /* timing */
+  /* timing: per-stage events of the last call, and caller marks on the
+   * context stream (mgp_mark) that bracket whole runs */
+  cudaEvent_t ev_mark[4];
   int timing;
   cudaEvent_t ev[MGP_NTIMERS][2];
   float ms[MGP_NTIMERS];
   int timed[MGP_NTIMERS];
+  /* timing history (mgp_set_timing with n > 1): the stage events of the
+   * last n mgp_step calls, [slot][timer][start/stop], slot = step % n */
+  cudaEvent_t *hev;
+  unsigned char *htimed;  /* [slot][timer] */
+  int hcap, hstep;
   long long launches;
 };
 

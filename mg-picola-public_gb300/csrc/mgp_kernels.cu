@@ -82,8 +82,13 @@ int mgp_launch_fill(float *p, long long n, float value, cudaStream_t st) {
 // weights, with WPAR = (N/Ns)^3 folded into the y factors (auxPM.c:316-317),
 // to a density grid pre-set to -1; periodic in all three axes (the ghost
 // x-slice exchange of auxPM.c:350-356 is the x wrap).
+// P2: Ns = 2^ls, lattice and cell index arithmetic by shifts (identical
+// results).  IDX: offset type inside one box's grid, 32-bit when the padded
+// grid has fewer than 2^31 floats (N <= 1024), which saves the 64-bit
+// multiplies of the eight addresses.
+template <bool P2, typename IDX>
 __global__ void __launch_bounds__(MGP_THREADS) k_cic(const float *__restrict__ s, const mgp_dstate *__restrict__ st,
-                                                     long long np, int Ns, int N, float scale, float wpar,
+                                                     long long np, int Ns, int ls, int N, float scale, float wpar,
                                                      float *__restrict__ rho, long long P, long long g_bs,
                                                      long long p0, long long p1) {
   // box blockIdx.y of a batch: particles 3 np apart, grids g_bs floats apart
@@ -91,39 +96,65 @@ __global__ void __launch_bounds__(MGP_THREADS) k_cic(const float *__restrict__ s
   st += blockIdx.y;
   rho += blockIdx.y * g_bs;
   const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
+  const float inv_ns = 1.0f / (float)Ns;
   const float *sx = s, *sy = s + np, *sz = s + 2 * np;
+  const IDX Pi = (IDX)P, NPi = (IDX)N * (IDX)P;
   long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = p0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += stride) {
     int i, j, k;
-    if (np <= 0xffffffffLL)
-      lattice_ijk((unsigned)p, Ns, i, j, k);
-    else
-      lattice_ijk(p, Ns, i, j, k);
     int ix, iy, iz;
     float DX, DY, DZ;
-    cell_frac(i, sx[p], ox, N, Ns, scale, ix, DX);
-    cell_frac(j, sy[p], oy, N, Ns, scale, iy, DY);
-    cell_frac(k, sz[p], oz, N, Ns, scale, iz, DZ);
+    if (P2) {
+      lattice_ijk_p2((unsigned)p, ls, i, j, k);
+      cell_frac_p2(i, sx[p], ox, N, ls, inv_ns, scale, ix, DX);
+      cell_frac_p2(j, sy[p], oy, N, ls, inv_ns, scale, iy, DY);
+      cell_frac_p2(k, sz[p], oz, N, ls, inv_ns, scale, iz, DZ);
+    } else {
+      if (np <= 0xffffffffLL)
+        lattice_ijk((unsigned)p, Ns, i, j, k);
+      else
+        lattice_ijk(p, Ns, i, j, k);
+      cell_frac(i, sx[p], ox, N, Ns, scale, ix, DX);
+      cell_frac(j, sy[p], oy, N, Ns, scale, iy, DY);
+      cell_frac(k, sz[p], oz, N, Ns, scale, iz, DZ);
+    }
     float TX = 1.0f - DX, TY = (1.0f - DY) * wpar, TZ = 1.0f - DZ;
     DY *= wpar;
-    int ixn = ix + 1 == N ? 0 : ix + 1, iyn = iy + 1 == N ? 0 : iy + 1, izn = iz + 1 == N ? 0 : iz + 1;
-    long long r00 = ((long long)ix * N + iy) * P, r01 = ((long long)ix * N + iyn) * P;
-    long long r10 = ((long long)ixn * N + iy) * P, r11 = ((long long)ixn * N + iyn) * P;
-    atomicAdd(rho + r00 + iz, TX * TY * TZ);
-    atomicAdd(rho + r00 + izn, TX * TY * DZ);
-    atomicAdd(rho + r01 + iz, TX * DY * TZ);
-    atomicAdd(rho + r01 + izn, TX * DY * DZ);
-    atomicAdd(rho + r10 + iz, DX * TY * TZ);
-    atomicAdd(rho + r10 + izn, DX * TY * DZ);
-    atomicAdd(rho + r11 + iz, DX * DY * TZ);
-    atomicAdd(rho + r11 + izn, DX * DY * DZ);
+    const IDX x0 = (IDX)ix * NPi, x1 = (ix + 1 == N ? 0 : (IDX)(ix + 1) * NPi);
+    const IDX y0 = (IDX)iy * Pi, y1 = (iy + 1 == N ? 0 : (IDX)(iy + 1) * Pi);
+    const IDX z0 = (IDX)iz, z1 = (iz + 1 == N ? 0 : (IDX)(iz + 1));
+    float *r00 = rho + (x0 + y0), *r01 = rho + (x0 + y1), *r10 = rho + (x1 + y0), *r11 = rho + (x1 + y1);
+    atomicAdd(r00 + z0, TX * TY * TZ);
+    atomicAdd(r00 + z1, TX * TY * DZ);
+    atomicAdd(r01 + z0, TX * DY * TZ);
+    atomicAdd(r01 + z1, TX * DY * DZ);
+    atomicAdd(r10 + z0, DX * TY * TZ);
+    atomicAdd(r10 + z1, DX * TY * DZ);
+    atomicAdd(r11 + z0, DX * DY * TZ);
+    atomicAdd(r11 + z1, DX * DY * DZ);
   }
+}
+
+static void launch_cic(dim3 grid, const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box,
+                       float wpar, float *rho, long long P, long long g_bs, long long p0, long long p1,
+                       cudaStream_t stream) {
+  const int ls = lattice_log2(Ns);
+  const bool p2 = ls >= 0 && np <= 0xffffffffLL;
+  const bool i32 = (long long)N * N * P < (1LL << 31);
+  const float sc = (float)(N / box);
+  if (p2 && i32)
+    k_cic<true, int><<<grid, MGP_THREADS, 0, stream>>>(s, st, np, Ns, ls, N, sc, wpar, rho, P, g_bs, p0, p1);
+  else if (p2)
+    k_cic<true, long long><<<grid, MGP_THREADS, 0, stream>>>(s, st, np, Ns, ls, N, sc, wpar, rho, P, g_bs, p0, p1);
+  else if (i32)
+    k_cic<false, int><<<grid, MGP_THREADS, 0, stream>>>(s, st, np, Ns, ls, N, sc, wpar, rho, P, g_bs, p0, p1);
+  else
+    k_cic<false, long long><<<grid, MGP_THREADS, 0, stream>>>(s, st, np, Ns, ls, N, sc, wpar, rho, P, g_bs, p0, p1);
 }
 
 int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, int N, double box, float wpar,
                    float *rho, long long P, cudaStream_t stream, int nbox, long long g_bs) {
-  k_cic<<<grid_boxes(np, g_budget_cic, nbox), MGP_THREADS, 0, stream>>>(s, st, np, Ns, N, (float)(N / box), wpar, rho, P, g_bs,
-                                                                      0, np);
+  launch_cic(grid_boxes(np, g_budget_cic, nbox), s, st, np, Ns, N, box, wpar, rho, P, g_bs, 0, np, stream);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -133,8 +164,7 @@ int mgp_launch_cic(const float *s, const mgp_dstate *st, long long np, int Ns, i
 int mgp_launch_cic_range(const float *s, const mgp_dstate *st, long long np, long long p0, long long p1, int Ns, int N,
                          double box, float wpar, float *rho, long long P, cudaStream_t stream) {
   if (p1 <= p0) return MGP_OK;
-  k_cic<<<grid_boxes(p1 - p0, g_budget_cic, 1), MGP_THREADS, 0, stream>>>(s, st, np, Ns, N, (float)(N / box), wpar, rho, P,
-                                                                        0, p0, p1);
+  launch_cic(grid_boxes(p1 - p0, g_budget_cic, 1), s, st, np, Ns, N, box, wpar, rho, P, 0, p0, p1, stream);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -479,12 +509,14 @@ __device__ __forceinline__ double block_sum_d(double v, double *sh) {
 
 // IDX is the grid offset type: 32-bit when the padded grid has < 2^31
 // floats (N <= 1024), which keeps the 24-point gather in fewer registers.
-template <typename IDX>
+// P2: Ns = 2^ls, lattice and cell index arithmetic by shifts (identical
+// results).
+template <typename IDX, bool P2>
 __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
     const float *__restrict__ frc, long long gf, int N, long long P, int Ns, long long np, float *__restrict__ s,
     float *__restrict__ v, const float *__restrict__ D1, const float *__restrict__ D2,
     const mgp_dstate *__restrict__ st, double *__restrict__ partials, mgp_kd_args a,
-    const mgp_box_scalars *__restrict__ bs) {
+    const mgp_box_scalars *__restrict__ bs, int ls) {
   __shared__ double sh[MGP_THREADS / 32];
   {
     // box blockIdx.y of a batch: force grids 3 gf apart, particle arrays 3 np
@@ -508,18 +540,26 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
   const IDX Pi = (IDX)P, NPi = (IDX)N * (IDX)P;
   float accD[3] = {0.f, 0.f, 0.f}, accV[3] = {0.f, 0.f, 0.f};
   long long stride = (long long)gridDim.x * blockDim.x;
+  const float inv_ns = 1.0f / (float)Ns;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
     int i, j, k;
-    if (np <= 0xffffffffLL)
-      lattice_ijk((unsigned)p, Ns, i, j, k);
-    else
-      lattice_ijk(p, Ns, i, j, k);
     float sp[3] = {s[p], s[np + p], s[2 * np + p]};
     int ix, iy, iz;
     float DX, DY, DZ;
-    cell_frac(i, sp[0], ox, N, Ns, a.scale, ix, DX);
-    cell_frac(j, sp[1], oy, N, Ns, a.scale, iy, DY);
-    cell_frac(k, sp[2], oz, N, Ns, a.scale, iz, DZ);
+    if (P2) {
+      lattice_ijk_p2((unsigned)p, ls, i, j, k);
+      cell_frac_p2(i, sp[0], ox, N, ls, inv_ns, a.scale, ix, DX);
+      cell_frac_p2(j, sp[1], oy, N, ls, inv_ns, a.scale, iy, DY);
+      cell_frac_p2(k, sp[2], oz, N, ls, inv_ns, a.scale, iz, DZ);
+    } else {
+      if (np <= 0xffffffffLL)
+        lattice_ijk((unsigned)p, Ns, i, j, k);
+      else
+        lattice_ijk(p, Ns, i, j, k);
+      cell_frac(i, sp[0], ox, N, Ns, a.scale, ix, DX);
+      cell_frac(j, sp[1], oy, N, Ns, a.scale, iy, DY);
+      cell_frac(k, sp[2], oz, N, Ns, a.scale, iz, DZ);
+    }
     const float TX = 1.0f - DX, TY = 1.0f - DY, TZ = 1.0f - DZ;
     const IDX x0 = (IDX)ix * NPi, x1 = (ix + 1 == N ? 0 : (IDX)(ix + 1) * NPi);
     const IDX y0 = (IDX)iy * Pi, y1 = (iy + 1 == N ? 0 : (IDX)(iy + 1) * Pi);
@@ -536,7 +576,9 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
       disp[ax] = __ldg(F + o000) * w000 + __ldg(F + o001) * w001 + __ldg(F + o010) * w010 + __ldg(F + o011) * w011 +
                  __ldg(F + o100) * w100 + __ldg(F + o101) * w101 + __ldg(F + o110) * w110 + __ldg(F + o111) * w111;
     }
-    const long long od = ((long long)i * Ns + j) * a.lpt_pitch + k;
+    // D1/D2 offsets: the particle index itself for particle arrays
+    // (pitch Ns), the lattice point in the row-padded slot grids otherwise
+    const long long od = a.lpt_pitch == Ns ? p : ((long long)i * Ns + j) * a.lpt_pitch + k;
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
       long long o = ax * np + p;
@@ -595,11 +637,20 @@ int mgp_launch_ikd(const float *frc, long long gf, int N, long long P, int Ns, l
                    const float *D1, const float *D2, mgp_dstate *dst, double *partials, int nblocks,
                    const mgp_kd_args *a, cudaStream_t st, int nbox, const mgp_box_scalars *bs) {
   const dim3 g(nblocks, nbox);
-  if (gf < (1LL << 31))
-    k_interp_kick_drift<int><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a, bs);
+  const int ls = lattice_log2(Ns);
+  const bool p2 = ls >= 0 && np <= 0xffffffffLL;
+  if (gf < (1LL << 31) && p2)
+    k_interp_kick_drift<int, true><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a,
+                                                              bs, ls);
+  else if (gf < (1LL << 31))
+    k_interp_kick_drift<int, false><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a,
+                                                               bs, ls);
+  else if (p2)
+    k_interp_kick_drift<long long, true><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials,
+                                                                    *a, bs, ls);
   else
-    k_interp_kick_drift<long long><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a,
-                                                             bs);
+    k_interp_kick_drift<long long, false><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst,
+                                                                     partials, *a, bs, ls);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   k_finalize_kd<<<nbox, MGP_THREADS, 0, st>>>(dst, partials, nblocks, 1.0 / (double)np, a->dda_omega, a->dyyy_d,

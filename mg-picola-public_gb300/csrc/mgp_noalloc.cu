@@ -15,7 +15,13 @@
 // library until the process exits.  Every call shares it and it keeps the
 // previous call's contents, so each call clears what must start at zero;
 // calls whose GPU work overlaps (other host threads, other streams) race on
-// it and must be serialised by the caller.
+// it and must be serialised by the caller.  The array's device address is
+// looked up by the first call on each device and kept for the process: after
+// a cudaDeviceReset of that device the kept address is stale, so the entry
+// point must not be used on a device that has been reset.
+//
+// Every result is reproducible bit for bit: the mode counts are integer sums,
+// and the mean |k| of a bin is summed over its |k|^2 values in a fixed order.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <mutex>
@@ -32,7 +38,9 @@
 #define NA_ALIGN(x) ((((size_t)(x)) + 255) & ~(size_t)255)
 #define NA_RK_MAX (3 * (MGP_NA_MAX_N / 2) * (MGP_NA_MAX_N / 2))
 #define NA_OFF_RKBIN 0
-#define NA_OFF_WIN NA_ALIGN(NA_OFF_RKBIN + sizeof(int) * (NA_RK_MAX + 1))
+#define NA_OFF_RKCNT NA_ALIGN(NA_OFF_RKBIN + sizeof(int) * (NA_RK_MAX + 1))
+#define NA_OFF_BINRK NA_ALIGN(NA_OFF_RKCNT + sizeof(unsigned) * (NA_RK_MAX + 1))
+#define NA_OFF_WIN NA_ALIGN(NA_OFF_BINRK + sizeof(int) * 2 * MGP_NA_MAX_BINS)
 #define NA_OFF_GEON NA_ALIGN(NA_OFF_WIN + sizeof(float) * (MGP_NA_MAX_N / 2 + 1))
 #define NA_OFF_GEOK NA_ALIGN(NA_OFF_GEON + sizeof(double) * MGP_NA_MAX_BINS)
 #define NA_OFF_PART NA_ALIGN(NA_OFF_GEOK + sizeof(double) * MGP_NA_MAX_BINS)
@@ -64,9 +72,14 @@ static int scratch_for_current_device(unsigned char **out) {
 
 // pofk_bin_index (src/compute_pofk.c:30-46) for every integer |k|^2, and the
 // CIC window 1/sinc^4 per |d| (compute_pofk.c:124-148).
-__global__ void k_na_tables(int N, double kmin, double kmax, int nbins, int bintype, int *rkbin, float *win) {
+// Also clears the per-|k|^2 mode counts and the |k|^2 range of every bin,
+// which the previous call left in the array.
+__global__ void k_na_tables(int N, double kmin, double kmax, int nbins, int bintype, int *rkbin, unsigned *rkcnt,
+                            int *binrk, float *win) {
   const int h = N / 2, rkmax = 3 * h * h;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < 2 * nbins; b += gridDim.x * blockDim.x) binrk[b] = 0;
   for (int rk = blockIdx.x * blockDim.x + threadIdx.x; rk <= rkmax; rk += gridDim.x * blockDim.x) {
+    rkcnt[rk] = 0u;
     double kmag = sqrt((double)rk);
     int nk;
     if (bintype == 0) nk = (int)((kmag - kmin) / (kmax - kmin) * nbins + 0.5);
@@ -79,36 +92,51 @@ __global__ void k_na_tables(int N, double kmin, double kmax, int nbins, int bint
   }
 }
 
-// Mode counts and |k| sums per bin with the reference's weights: |d0|, |d1|
-// stand for 1 or 2 stored indices, kz = 0 and N/2 weigh 1, others 2.
-__global__ void k_na_geometry(int N, const int *rkbin, double *geo_n, double *geo_k) {
-  const int h = N / 2;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)(h + 1) * (h + 1)) return;
-  int d0 = (int)(t / (h + 1)), d1 = (int)(t % (h + 1));
-  double m = ((d0 == 0 || d0 == h) ? 1.0 : 2.0) * ((d1 == 0 || d1 == h) ? 1.0 : 2.0);
-  int run_bin = -1;
-  double run_n = 0.0, run_k = 0.0;
-  for (int d2 = 0; d2 <= h; d2++) {
-    int rk = d0 * d0 + d1 * d1 + d2 * d2;
-    int b = rkbin[rk];
-    double w = m * ((d2 == 0 || d2 == h) ? 1.0 : 2.0);
-    if (b != run_bin) {
-      if (run_bin >= 0) {
-        atomicAdd(&geo_n[run_bin], run_n);
-        atomicAdd(&geo_k[run_bin], run_k);
-      }
-      run_bin = b;
-      run_n = run_k = 0.0;
-    }
-    if (b >= 0) {
-      run_n += w;
-      run_k += w * sqrt((double)rk);
-    }
+// Weighted mode count of every integer |k|^2 with the reference's weights:
+// |d0|, |d1| stand for 1 or 2 stored indices, kz = 0 and N/2 weigh 1, others
+// 2 (compute_pofk.c:124-148).  The counts are integers, so the order of the
+// atomic additions does not matter.  The same threads record the |k|^2
+// range of every bin: rk_bin is non-decreasing in |k|^2 where it is >= 0
+// (the bin index is monotone in |k|), so each bin is one contiguous range.
+__global__ void k_na_geometry(int N, const int *rkbin, unsigned *rkcnt, int *binrk) {
+  const int h = N / 2, rkmax = 3 * h * h;
+  const long long nthr = (long long)gridDim.x * blockDim.x;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (long long t = t0; t < (long long)(h + 1) * (h + 1); t += nthr) {
+    int d0 = (int)(t / (h + 1)), d1 = (int)(t % (h + 1));
+    unsigned m = ((d0 == 0 || d0 == h) ? 1u : 2u) * ((d1 == 0 || d1 == h) ? 1u : 2u);
+    int base = d0 * d0 + d1 * d1;
+    for (int d2 = 0; d2 <= h; d2++) atomicAdd(&rkcnt[base + d2 * d2], m * ((d2 == 0 || d2 == h) ? 1u : 2u));
   }
-  if (run_bin >= 0) {
-    atomicAdd(&geo_n[run_bin], run_n);
-    atomicAdd(&geo_k[run_bin], run_k);
+  for (long long rk = t0; rk <= rkmax; rk += nthr) {
+    int b = rkbin[rk];
+    if (b < 0) continue;
+    if (rk == 0 || rkbin[rk - 1] != b) binrk[2 * b] = (int)rk;
+    if (rk == rkmax || rkbin[rk + 1] != b) binrk[2 * b + 1] = (int)rk + 1;
+  }
+}
+
+// Per bin (one warp each): mode count and sum of |k| over its |k|^2 range,
+// each lane in ascending |k|^2 and the lanes combined by a fixed shuffle
+// tree, so the sums do not depend on scheduling.
+__global__ void k_na_binsum(int nbins, const unsigned *rkcnt, const int *binrk, double *geo_n, double *geo_k) {
+  const int lane = threadIdx.x & 31;
+  const int b = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (b >= nbins) return;
+  const int r0 = binrk[2 * b], r1 = binrk[2 * b + 1];
+  double n = 0.0, k = 0.0;
+  for (int rk = r0 + lane; rk < r1; rk += 32) {
+    double c = (double)rkcnt[rk];
+    n += c;
+    k += c * sqrt((double)rk);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    n += __shfl_xor_sync(0xffffffffu, n, o);
+    k += __shfl_xor_sync(0xffffffffu, k, o);
+  }
+  if (lane == 0) {
+    geo_n[b] = n;
+    geo_k[b] = k;
   }
 }
 
@@ -157,19 +185,23 @@ extern "C" int mgp_pofk_noalloc(const float *d_deltak, int Nmesh, int Nsample, d
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   int *rkbin = (int *)(base + NA_OFF_RKBIN);
+  unsigned *rkcnt = (unsigned *)(base + NA_OFF_RKCNT);
+  int *binrk = (int *)(base + NA_OFF_BINRK);
   float *win = (float *)(base + NA_OFF_WIN);
   double *geo_n = (double *)(base + NA_OFF_GEON), *geo_k = (double *)(base + NA_OFF_GEOK);
   double *part = (double *)(base + NA_OFF_PART), *sums = (double *)(base + NA_OFF_SUMS);
   double *out = (double *)(base + NA_OFF_OUT);
   const int h = Nmesh / 2;
-  // the previous call's counts stay in the array: clear them
-  MGP_CUDA(cudaMemsetAsync(geo_n, 0, sizeof(double) * MGP_NA_MAX_BINS, st));
-  MGP_CUDA(cudaMemsetAsync(geo_k, 0, sizeof(double) * MGP_NA_MAX_BINS, st));
-  k_na_tables<<<(3 * h * h + 256) / 256, 256, 0, st>>>(Nmesh, kmin, kmax, nbins, bintype, rkbin, win);
+  // the tables kernel clears what the previous call left in the array
+  k_na_tables<<<(3 * h * h + 256) / 256, 256, 0, st>>>(Nmesh, kmin, kmax, nbins, bintype, rkbin, rkcnt, binrk, win);
   MGP_CHECK_LAUNCH();
-  long long pairs = (long long)(h + 1) * (h + 1);
-  k_na_geometry<<<(int)((pairs + 255) / 256), 256, 0, st>>>(Nmesh, rkbin, geo_n, geo_k);
+  g_kernel_launches++;
+  k_na_geometry<<<mgp_blocks_for((long long)(h + 1) * (h + 1), 8), 256, 0, st>>>(Nmesh, rkbin, rkcnt, binrk);
   MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  k_na_binsum<<<(nbins * 32 + 255) / 256, 256, 0, st>>>(nbins, rkcnt, binrk, geo_n, geo_k);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
   // the binning kernel of mgp_pofk, writing every block's partials
   int nblocks = MGP_NA_BLOCKS;
   if ((long long)nblocks * 8 > (long long)Nmesh * Nmesh) nblocks = (int)(((long long)Nmesh * Nmesh + 7) / 8);
@@ -179,6 +211,7 @@ extern "C" int mgp_pofk_noalloc(const float *d_deltak, int Nmesh, int Nsample, d
   double shot = subtract_shotnoise ? pow(Box / (double)Nsample, 3) : 0.0;
   k_na_finalize<<<(nbins + 127) / 128, 128, 0, st>>>(nbins, sums, geo_n, geo_k, norm, shot, 2.0 * M_PI / Box, out);
   MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
   MGP_CUDA(cudaMemcpyAsync(pk, out, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
   if (kmean) MGP_CUDA(cudaMemcpyAsync(kmean, out + MGP_NA_MAX_BINS, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));
   if (n) MGP_CUDA(cudaMemcpyAsync(n, out + 2 * MGP_NA_MAX_BINS, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st));

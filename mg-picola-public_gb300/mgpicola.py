@@ -21,7 +21,7 @@ EXPORTS = [
     "mgp_params_default", "mgp_read_parameterfile", "mgp_create", "mgp_destroy", "mgp_last_error",
     "mgp_displacement_fields", "mgp_get_displacements", "mgp_kick_drift", "mgp_step", "mgp_run", "mgp_pofk",
     "mgp_pofk_total", "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
-    "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_launch_count",
+    "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_mark", "mgp_mark_ms", "mgp_kernel_ms_step", "mgp_launch_count",
     "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
     "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_batch_set_tuning",
@@ -172,6 +172,11 @@ def lib():
         L.mgp_set_timing.argtypes = [vp, C.c_int]
         L.mgp_kernel_ms.argtypes = [vp, C.c_char_p]
         L.mgp_kernel_ms.restype = C.c_double
+        L.mgp_kernel_ms_step.argtypes = [vp, C.c_char_p, C.c_int]
+        L.mgp_kernel_ms_step.restype = C.c_double
+        L.mgp_mark.argtypes = [vp, C.c_int]
+        L.mgp_mark_ms.argtypes = [vp, C.c_int, C.c_int]
+        L.mgp_mark_ms.restype = C.c_double
         L.mgp_launch_count.argtypes = [vp]
         L.mgp_launch_count.restype = C.c_longlong
         L.mgp_host_register.argtypes = [vp, C.c_size_t]
@@ -394,11 +399,26 @@ class Context:
     def power(self, k):
         return lib().mgp_power_spectrum(self.h, k)
 
-    def set_timing(self, on=True):
-        _check(lib().mgp_set_timing(self.h, 1 if on else 0))
+    def set_timing(self, on=True, history=0):
+        """Stage timing of the last call; with history = n > 1 the stage
+        events of the last n steps are kept (kernel_ms_step)."""
+        _check(lib().mgp_set_timing(self.h, history if (on and history > 1) else (1 if on else 0)))
 
     def kernel_ms(self, name):
         return lib().mgp_kernel_ms(self.h, name.encode())
+
+    def kernel_ms_step(self, name, step):
+        """Stage milliseconds of step `step` from the timing history
+        (set_timing(n) with n > 1)."""
+        return lib().mgp_kernel_ms_step(self.h, name.encode(), step)
+
+    def mark(self, slot):
+        """Record event `slot` (0..3) on the context's stream."""
+        _check(lib().mgp_mark(self.h, slot))
+
+    def mark_ms(self, a, b):
+        """Device milliseconds from mark a to mark b (waits for b)."""
+        return lib().mgp_mark_ms(self.h, a, b)
 
     def launches(self):
         return lib().mgp_launch_count(self.h)

@@ -47,7 +47,7 @@ class RunParams(C.Structure):
                 ("nsteps", C.c_int), ("final_redshift", C.c_double), ("pofk_nbins", C.c_int),
                 ("pofk_bintype", C.c_int), ("pofk_subtract_shotnoise", C.c_int), ("pofk_kmin", C.c_double),
                 ("pofk_kmax", C.c_double), ("usecola", C.c_int), ("ic_pos01", C.c_void_p), ("ic_n", C.c_long),
-                ("ic_rescale_rk", C.c_void_p)]
+                ("ic_rescale_rk", C.c_void_p), ("stop_step", C.c_int)]
 
 
 def lib():

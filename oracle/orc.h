@@ -267,6 +267,10 @@ typedef struct {
   const double *ic_pos01;
   long ic_n;
   const double *ic_rescale_rk;
+  /* > 0: stop at the start of step stop_step of the schedule, after its
+   * density and P(k); pos/vel out are then the particles there (vel = the
+   * COLA velocity minus its mean, without the LPT part) */
+  int stop_step;
 } orc_run_params;
 /* Runs IC + the KDK loop of src/main.c:394-611 for one output redshift.
  * pos/vel out [Ns^3][3] at the final time (vel incl. LPT part as written by

@@ -21,6 +21,7 @@ static void divide_by_laplacian(const orc_mg *m, double a, int N, double box, co
   const int NH = N / 2 + 1;
   double normfactor = 1.0 / pow((double)N, 3);
   normfactor *= 1.5 * m->omega / a * pow(box / INVERSE_H0_MPCH / (2.0 * PI), 2);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < N; i++)
     for (int j = 0; j < N; j++)
       for (int k = 0; k < NH; k++) {
@@ -39,6 +40,7 @@ static void eff_density_to_phik(const orc_mg *m, double a, int N, double box, do
   const int NH = N / 2 + 1;
   double normfactor = orc_coupling(m, a);
   double massterm2 = pow(a, 2) * orc_mass2_of_a(m, a) / pow((2.0 * PI) * INVERSE_H0_MPCH / box, 2);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < N; i++)
     for (int j = 0; j < N; j++)
       for (int k = 0; k < NH; k++) {
@@ -64,6 +66,7 @@ static double smoothing_filter(int type, double kR) {
 static void smooth_density(const orc_mg *m, int N, double box, const double *dk, double *out) {
   const int NH = N / 2 + 1;
   double normfactor = 1.0 / pow((double)N, 3);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < N; i++)
     for (int j = 0; j < N; j++)
       for (int k = 0; k < NH; k++) {
@@ -93,6 +96,7 @@ void orc_fifth_force(const orc_mg *m, double a, int N, double box, const double 
     divide_by_laplacian(m, a, N, box, deltak, phi);
     orc_fft_c2r(N, phi);
     memcpy(mgk, density_x, sizeof(double) * 2 * total);
+    #pragma omp parallel for schedule(static)
     for (size_t j = 0; j < 2 * total; j++) mgk[j] *= orc_screen_potential(m, a, phi[j]);
     free(phi);
     orc_fft_r2c(N, mgk);
@@ -101,6 +105,7 @@ void orc_fifth_force(const orc_mg *m, double a, int N, double box, const double 
     /* ComputeFifthForce_DensityScreening, src/mg.h:197-260 */
     double coupling = orc_coupling(m, a);
     if (!m->include_screening) {
+      #pragma omp parallel for schedule(static)
       for (size_t i = 0; i < 2 * total; i++) mgk[i] = deltak[i] * coupling;
       return;
     }
@@ -108,12 +113,14 @@ void orc_fifth_force(const orc_mg *m, double a, int N, double box, const double 
     smooth_density(m, N, box, deltak, sm);
     orc_fft_c2r(N, sm);
     memcpy(mgk, density_x, sizeof(double) * 2 * total);
+    #pragma omp parallel for schedule(static)
     for (size_t j = 0; j < 2 * total; j++) mgk[j] *= coupling * orc_screen_density(m, a, sm[j]);
     free(sm);
     orc_fft_r2c(N, mgk);
   } else if (m->model == ORC_JBD_GEFF) {
     /* ComputeFifthForce_TimeDepGeffModels, src/mg.h:127-137 */
     double g = orc_geff(m, a, 0.0);
+    #pragma omp parallel for schedule(static)
     for (size_t j = 0; j < 2 * total; j++) deltak[j] *= g;
   }
 }

@@ -8,6 +8,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <omp.h>
 
 #define PI 3.14159265358979323846 /* src/vars.h:59 */
 
@@ -33,42 +34,83 @@ void orc_lattice_positions(const double *disp, int Ns, double box, double *pos) 
   }
 }
 
-/* PtoMesh, src/auxPM.c:280-357 (one task: the ghost x-slice N is added back
- * onto slice 0, auxPM.c:350-356). */
+/* PtoMesh, src/auxPM.c:280-357, with the reference's parallel shape: the
+ * mesh is split into x slabs, one per thread as one per MPI task; the
+ * particles are handed to the slab of their cell (the exchange of
+ * auxPM.c:108-275), each thread deposits its particles in particle order into
+ * its slab plus one ghost x-slice, and the ghost slices are then added onto
+ * the next slab's first slice (auxPM.c:350-356; the last one wraps to 0). */
+static void deposit_one(double *d, int N, double X, double Y, double Z, double WPAR, size_t ghost_row,
+                        double *ghost) {
+  unsigned IX = (unsigned)X, IY = (unsigned)Y, IZ = (unsigned)Z;
+  double DX = X - (double)IX, DY = Y - (double)IY, DZ = Z - (double)IZ;
+  double TX = 1.0 - DX, TY = 1.0 - DY, TZ = 1.0 - DZ;
+  DY *= WPAR;
+  TY *= WPAR;
+  if (IX >= (unsigned)N) IX -= N; /* X == N from rounding at the box edge: slice N is slice 0 */
+  if (IY >= (unsigned)N) IY = 0;
+  if (IZ >= (unsigned)N) IZ = 0;
+  unsigned IXn = IX + 1, IYn = IY + 1, IZn = IZ + 1;
+  if (IYn >= (unsigned)N) IYn = 0;
+  if (IZn >= (unsigned)N) IZn = 0;
+  d[ridx(N, IX, IY, IZ)] += TX * TY * TZ;
+  d[ridx(N, IX, IY, IZn)] += TX * TY * DZ;
+  d[ridx(N, IX, IYn, IZ)] += TX * DY * TZ;
+  d[ridx(N, IX, IYn, IZn)] += TX * DY * DZ;
+  /* the next x slice: in this slab, or this thread's ghost slice */
+  double *dn = IXn == ghost_row ? ghost : d + ridx(N, IXn, 0, 0);
+  dn[ridx(N, 0, IY, IZ)] += DX * TY * TZ;
+  dn[ridx(N, 0, IY, IZn)] += DX * TY * DZ;
+  dn[ridx(N, 0, IYn, IZ)] += DX * DY * TZ;
+  dn[ridx(N, 0, IYn, IZn)] += DX * DY * DZ;
+}
+
 void orc_cic(const double *pos, long np, int N, int Ns, double box, double *grid) {
   const size_t P = 2 * (size_t)(N / 2 + 1);
-  const size_t total = (size_t)(N + 1) * N * P; /* one extra slice */
-  double *d = malloc(sizeof(double) * total);
+  const size_t slice = (size_t)N * P;
   const double scaleBox = (double)N / box;
   const double WPAR = pow((double)N / (double)Ns, 3);
-  for (size_t i = 0; i < total; i++) d[i] = -1.0;
+  int nt = omp_get_max_threads();
+  if (nt > N) nt = N;
+  if (nt < 1) nt = 1;
+  /* slab of every x slice, and the particles of every slab in particle order */
+  int *slab_of = malloc(sizeof(int) * N);
+  for (int t = 0; t < nt; t++)
+    for (int x = (int)((long)N * t / nt); x < (int)((long)N * (t + 1) / nt); x++) slab_of[x] = t;
+  long *count = calloc(nt + 1, sizeof(long));
+  int *owner = malloc(sizeof(int) * (np > 0 ? np : 1));
   for (long i = 0; i < np; i++) {
-    double X = pos[3 * i + 0] * scaleBox, Y = pos[3 * i + 1] * scaleBox, Z = pos[3 * i + 2] * scaleBox;
-    unsigned IX = (unsigned)X, IY = (unsigned)Y, IZ = (unsigned)Z;
-    double DX = X - (double)IX, DY = Y - (double)IY, DZ = Z - (double)IZ;
-    double TX = 1.0 - DX, TY = 1.0 - DY, TZ = 1.0 - DZ;
-    DY *= WPAR;
-    TY *= WPAR;
-    if (IY >= (unsigned)N) IY = 0;
-    if (IZ >= (unsigned)N) IZ = 0;
-    unsigned IXn = IX + 1, IYn = IY + 1, IZn = IZ + 1;
-    if (IYn >= (unsigned)N) IYn = 0;
-    if (IZn >= (unsigned)N) IZn = 0;
-    d[ridx(N, IX, IY, IZ)] += TX * TY * TZ;
-    d[ridx(N, IX, IY, IZn)] += TX * TY * DZ;
-    d[ridx(N, IX, IYn, IZ)] += TX * DY * TZ;
-    d[ridx(N, IX, IYn, IZn)] += TX * DY * DZ;
-    d[ridx(N, IXn, IY, IZ)] += DX * TY * TZ;
-    d[ridx(N, IXn, IY, IZn)] += DX * TY * DZ;
-    d[ridx(N, IXn, IYn, IZ)] += DX * DY * TZ;
-    d[ridx(N, IXn, IYn, IZn)] += DX * DY * DZ;
+    unsigned IX = (unsigned)(pos[3 * i] * scaleBox);
+    if (IX >= (unsigned)N) IX -= N; /* as deposit_one */
+    owner[i] = slab_of[IX];
+    count[owner[i] + 1]++;
   }
-  /* ghost slice: density[i] += temp[i] + 1 (auxPM.c:352-354) */
-  const size_t slice = (size_t)N * P;
+  for (int t = 0; t < nt; t++) count[t + 1] += count[t];
+  long *list = malloc(sizeof(long) * (np > 0 ? np : 1)), *fillp = malloc(sizeof(long) * nt);
+  memcpy(fillp, count, sizeof(long) * nt);
+  for (long i = 0; i < np; i++) list[fillp[owner[i]]++] = i;
+  double *ghost = malloc(sizeof(double) * slice * nt);
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+  for (int t = 0; t < nt; t++) {
+    const int x0 = (int)((long)N * t / nt), x1 = (int)((long)N * (t + 1) / nt);
+    for (size_t c = (size_t)x0 * slice; c < (size_t)x1 * slice; c++) grid[c] = -1.0;
+    double *g = ghost + (size_t)t * slice;
+    for (size_t c = 0; c < slice; c++) g[c] = 0.0;
+    for (long n = count[t]; n < count[t + 1]; n++) {
+      long i = list[n];
+      double X = pos[3 * i + 0] * scaleBox, Y = pos[3 * i + 1] * scaleBox, Z = pos[3 * i + 2] * scaleBox;
+      deposit_one(grid, N, X, Y, Z, WPAR, (size_t)x1, g);
+    }
+  }
+  /* ghost slices onto the next slab's first slice, in slab order */
   if (np != 0)
-    for (size_t i = 0; i < slice; i++) d[i] += d[(size_t)N * slice + i] + 1.0;
-  memcpy(grid, d, sizeof(double) * (size_t)N * slice);
-  free(d);
+    for (int t = 0; t < nt; t++) {
+      const int x1 = (int)((long)N * (t + 1) / nt);
+      double *dst = grid + (size_t)(x1 == N ? 0 : x1) * slice;
+      const double *g = ghost + (size_t)t * slice;
+      for (size_t c = 0; c < slice; c++) dst[c] += g[c];
+    }
+  free(slab_of); free(count); free(owner); free(list); free(fillp); free(ghost);
 }
 
 /* Forces, src/auxPM.c:437-535. */
@@ -82,6 +124,7 @@ void orc_forces_kspace(const double *deltak, const double *mgk, int N, double bo
   if (mgk)
     for (size_t i = 0; i < Total; i++) { P3D[2 * i] += mgk[2 * i]; P3D[2 * i + 1] += mgk[2 * i + 1]; }
   const double N3 = pow((double)N, 3);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < N; i++) {
     int iglobal = i;
     for (int j = 0; j < NH; j++) {
@@ -123,30 +166,42 @@ void orc_interp(const double *f1, const double *f2, const double *f3, int N, dou
                 const double *pos, long np, double *disp, double mean_out[3]) {
   const double scaleBox = (double)N / box;
   const double *F[3] = {f1, f2, f3};
-  double sum[3] = {0, 0, 0};
-  for (long i = 0; i < np; i++) {
-    double X = pos[3 * i] * scaleBox, Y = pos[3 * i + 1] * scaleBox, Z = pos[3 * i + 2] * scaleBox;
-    unsigned IX = (unsigned)X, IY = (unsigned)Y, IZ = (unsigned)Z;
-    double DX = X - (double)IX, DY = Y - (double)IY, DZ = Z - (double)IZ;
-    double TX = 1.0 - DX, TY = 1.0 - DY, TZ = 1.0 - DZ;
-    if (IY >= (unsigned)N) IY = 0;
-    if (IZ >= (unsigned)N) IZ = 0;
-    unsigned IXn = IX + 1, IYn = IY + 1, IZn = IZ + 1;
-    if (IYn >= (unsigned)N) IYn = 0;
-    if (IZn >= (unsigned)N) IZn = 0;
-    /* ghost slice N holds slice 0 (auxPM.c:546-551) */
-    if (IX >= (unsigned)N) IX -= N;
-    if (IXn >= (unsigned)N) IXn -= N;
-    for (int a = 0; a < 3; a++) {
-      const double *G = F[a];
-      double v = G[ridx(N, IX, IY, IZ)] * TX * TY * TZ + G[ridx(N, IX, IY, IZn)] * TX * TY * DZ +
-                 G[ridx(N, IX, IYn, IZ)] * TX * DY * TZ + G[ridx(N, IX, IYn, IZn)] * TX * DY * DZ +
-                 G[ridx(N, IXn, IY, IZ)] * DX * TY * TZ + G[ridx(N, IXn, IY, IZn)] * DX * TY * DZ +
-                 G[ridx(N, IXn, IYn, IZ)] * DX * DY * TZ + G[ridx(N, IXn, IYn, IZn)] * DX * DY * DZ;
-      disp[3 * i + a] = v;
-      sum[a] += v;
+  const int nt = omp_get_max_threads();
+  double *part = calloc(3 * (size_t)nt, sizeof(double));
+  /* particles in nt contiguous ranges; the sums of the ranges are added in
+   * range order, so the mean does not depend on scheduling */
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+  for (int t = 0; t < nt; t++) {
+    double sum[3] = {0, 0, 0};
+    for (long i = np * t / nt; i < np * (t + 1) / nt; i++) {
+      double X = pos[3 * i] * scaleBox, Y = pos[3 * i + 1] * scaleBox, Z = pos[3 * i + 2] * scaleBox;
+      unsigned IX = (unsigned)X, IY = (unsigned)Y, IZ = (unsigned)Z;
+      double DX = X - (double)IX, DY = Y - (double)IY, DZ = Z - (double)IZ;
+      double TX = 1.0 - DX, TY = 1.0 - DY, TZ = 1.0 - DZ;
+      if (IY >= (unsigned)N) IY = 0;
+      if (IZ >= (unsigned)N) IZ = 0;
+      unsigned IXn = IX + 1, IYn = IY + 1, IZn = IZ + 1;
+      if (IYn >= (unsigned)N) IYn = 0;
+      if (IZn >= (unsigned)N) IZn = 0;
+      /* ghost slice N holds slice 0 (auxPM.c:546-551) */
+      if (IX >= (unsigned)N) IX -= N;
+      if (IXn >= (unsigned)N) IXn -= N;
+      for (int a = 0; a < 3; a++) {
+        const double *G = F[a];
+        double v = G[ridx(N, IX, IY, IZ)] * TX * TY * TZ + G[ridx(N, IX, IY, IZn)] * TX * TY * DZ +
+                   G[ridx(N, IX, IYn, IZ)] * TX * DY * TZ + G[ridx(N, IX, IYn, IZn)] * TX * DY * DZ +
+                   G[ridx(N, IXn, IY, IZ)] * DX * TY * TZ + G[ridx(N, IXn, IY, IZn)] * DX * TY * DZ +
+                   G[ridx(N, IXn, IYn, IZ)] * DX * DY * TZ + G[ridx(N, IXn, IYn, IZn)] * DX * DY * DZ;
+        disp[3 * i + a] = v;
+        sum[a] += v;
+      }
     }
+    for (int a = 0; a < 3; a++) part[3 * t + a] = sum[a];
   }
+  double sum[3] = {0, 0, 0};
+  for (int t = 0; t < nt; t++)
+    for (int a = 0; a < 3; a++) sum[a] += part[3 * t + a];
+  free(part);
   for (int a = 0; a < 3; a++) mean_out[a] = sum[a] / (double)np;
 }
 
@@ -154,21 +209,32 @@ void orc_interp(const double *f1, const double *f2, const double *f3, int N, dou
 void orc_kick(long np, double *vel, double *disp, const double *D1, const double *D2,
               const double sumD[3], double omega, double dda, double ddD, double ddD2,
               double A, int usecola, double sumv_out[3]) {
-  double sumxyz[3] = {0, 0, 0};
-  for (long n = 0; n < np; n++) {
-    for (int ax = 0; ax < 3; ax++) {
-      disp[3 * n + ax] -= sumD[ax];
-      double force = -1.5 * omega * disp[3 * n + ax] - usecola * (D1[3 * n + ax] * ddD + D2[3 * n + ax] * ddD2) / A;
-      vel[3 * n + ax] += force * dda;
-      sumxyz[ax] += vel[3 * n + ax];
+  const int nt = omp_get_max_threads();
+  double *part = calloc(3 * (size_t)nt, sizeof(double));
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+  for (int t = 0; t < nt; t++) {
+    double sumxyz[3] = {0, 0, 0};
+    for (long n = np * t / nt; n < np * (t + 1) / nt; n++) {
+      for (int ax = 0; ax < 3; ax++) {
+        disp[3 * n + ax] -= sumD[ax];
+        double force = -1.5 * omega * disp[3 * n + ax] - usecola * (D1[3 * n + ax] * ddD + D2[3 * n + ax] * ddD2) / A;
+        vel[3 * n + ax] += force * dda;
+        sumxyz[ax] += vel[3 * n + ax];
+      }
     }
+    for (int ax = 0; ax < 3; ax++) part[3 * t + ax] = sumxyz[ax];
   }
+  double sumxyz[3] = {0, 0, 0};
+  for (int t = 0; t < nt; t++)
+    for (int ax = 0; ax < 3; ax++) sumxyz[ax] += part[3 * t + ax];
+  free(part);
   for (int ax = 0; ax < 3; ax++) sumv_out[ax] = sumxyz[ax] / (double)np;
 }
 
 /* Drift, src/main.c:747-787 (non-SCALEDEPENDENT branch 772-783). */
 void orc_drift(long np, double *pos, const double *vel, const double *D1, const double *D2,
                const double sumv[3], double dyyy, double dD, double dD2, int usecola, double box) {
+#pragma omp parallel for schedule(static)
   for (long n = 0; n < np; n++) {
     for (int ax = 0; ax < 3; ax++) {
       pos[3 * n + ax] += (vel[3 * n + ax] - sumv[ax]) * dyyy;
@@ -214,11 +280,11 @@ static double k_from_index(int index, double kmin, double kmax, int nbins, int b
 
 /* Shared mode loop of compute_power_spectrum / bin_up_RSD_power_spectrum
  * (compute_pofk.c:123-223 and 575-690). */
-static void bin_modes(const double *dk, int N, double kmin, double kmax, int nbins, int bintype,
-                      double *p0, double *p2, double *p4, double *kb, double *nb) {
+static void bin_modes_rows(const double *dk, int N, int i0, int i1, double kmin, double kmax, int nbins,
+                           int bintype, double *p0, double *p2, double *p4, double *kb, double *nb) {
   const int NH = N / 2 + 1;
   const double norm = 1.0 / pow((double)N, 6);
-  for (int i = 0; i < N; i++) {
+  for (int i = i0; i < i1; i++) {
     int d0 = i > N / 2 ? N - i : i;
     double gx = d0 == 0 ? 1.0 : sin((PI * d0) / (double)N) / ((PI * d0) / (double)N);
     for (int j = 0; j < NH; j++) {
@@ -262,6 +328,35 @@ static void bin_modes(const double *dk, int N, double kmin, double kmax, int nbi
       }
     }
   }
+}
+
+/* The mode loop over contiguous x ranges, one per thread; the per-range bin
+ * sums are added in range order, so the result does not depend on
+ * scheduling. */
+static void bin_modes(const double *dk, int N, double kmin, double kmax, int nbins, int bintype,
+                      double *p0, double *p2, double *p4, double *kb, double *nb) {
+  int nt = omp_get_max_threads();
+  if (nt > N) nt = N;
+  const size_t nb5 = 5 * (size_t)nbins;
+  double *part = calloc(nb5 * nt, sizeof(double));
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+  for (int t = 0; t < nt; t++) {
+    double *q = part + nb5 * t;
+    bin_modes_rows(dk, N, (int)((long)N * t / nt), (int)((long)N * (t + 1) / nt), kmin, kmax, nbins, bintype, q,
+                   p2 ? q + nbins : NULL, p4 ? q + 2 * (size_t)nbins : NULL, q + 3 * (size_t)nbins,
+                   q + 4 * (size_t)nbins);
+  }
+  for (int t = 0; t < nt; t++) {
+    const double *q = part + nb5 * t;
+    for (int b = 0; b < nbins; b++) {
+      p0[b] += q[b];
+      if (p2) p2[b] += q[nbins + b];
+      if (p4) p4[b] += q[2 * (size_t)nbins + b];
+      kb[b] += q[3 * (size_t)nbins + b];
+      nb[b] += q[4 * (size_t)nbins + b];
+    }
+  }
+  free(part);
 }
 
 int orc_pofk(const double *deltak, int N, int Ns, double box, int *nbins_io, int bintype,

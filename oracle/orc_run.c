@@ -107,6 +107,14 @@ int orc_run(const orc_run_params *rp, double *pos_out, double *vel_out,
         orc_pofk(grid, N, Ns, Box, &nb, rp->pofk_bintype, rp->pofk_subtract_shotnoise, rp->pofk_kmin,
                  rp->pofk_kmax, kbin, pk, kmean, nmodes);
       }
+      if (rp->stop_step > 0 && io == 0 && ts == rp->stop_step) {
+        for (long p = 0; p < np; p++)
+          for (int a = 0; a < 3; a++) {
+            pos_out[3 * p + a] = pos[3 * p + a];
+            vel_out[3 * p + a] = vel[3 * p + a] - sumv[a];
+          }
+        goto done;
+      }
       if (rp->mg.mg_active) orc_fifth_force(&rp->mg, A, N, Box, dens_x, grid, mgk);
       orc_forces_kspace(grid, uses_mgk ? mgk : NULL, N, Box, f[0], f[1], f[2]);
       for (int a = 0; a < 3; a++) orc_fft_c2r(N, f[a]);

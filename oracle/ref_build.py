@@ -14,7 +14,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("MGP_REFERENCE_SRC", "/root/reference/src")
+# the reference's src/ directory; the checker is built only when it is given
+REF_SRC = os.environ.get("MGP_REFERENCE_SRC", "")
 OUT = os.path.join(HERE, "_ref")
 SOURCES = ["main.c", "auxPM.c", "2LPT.c", "cosmo.c", "power.c", "compute_pofk.c", "read_param.c", "vars.c",
            "wrappers.c", "timer.c", "msg.c", "jbd.c"]
@@ -46,7 +47,7 @@ EXTRA_SOURCES = {"FOFR_LCDM_IC": ["readICfromfile.c"]}
 
 
 def available():
-    return os.path.isdir(REF_SRC) and all(os.path.exists(os.path.join(REF_SRC, s)) for s in SOURCES)
+    return bool(REF_SRC) and os.path.isdir(REF_SRC) and all(os.path.exists(os.path.join(REF_SRC, s)) for s in SOURCES)
 
 
 def binary(model):
@@ -55,7 +56,7 @@ def binary(model):
 
 def build(models=None, verbose=False):
     if not available():
-        raise RuntimeError("reference sources not found at " + REF_SRC)
+        raise RuntimeError("reference sources not found (set MGP_REFERENCE_SRC to the reference's src/ directory)")
     os.makedirs(OUT, exist_ok=True)
     inc = ["-I" + os.path.join(HERE, "ref_shim", "include"), "-I" + REF_SRC]
     srcs = [os.path.join(REF_SRC, s) for s in SOURCES] + SHIM

@@ -8,8 +8,10 @@
  * the random stream is the oracle's Philox stream (oracle/orc_rng.c), ODEs
  * are integrated with an adaptive Dormand-Prince 5(4) pair to 1e-12
  * (tighter than the tolerances the reference requests), quadrature is
- * adaptive Gauss-Legendre to 1e-13, splines are natural cubic, 2D
- * interpolation is cubic convolution (R. Keys, IEEE TASSP 29 (1981) 1153).
+ * adaptive Gauss-Legendre to 1e-13, splines are natural cubic, and 2D
+ * interpolation is the bicubic method gsl_interp2d_bicubic documents (node
+ * derivatives from natural cubic splines along the grid lines, Hermite
+ * cells), restated in oracle/orc_interp2d.c.
  */
 #include <math.h>
 #include <stdint.h>

@@ -8,7 +8,8 @@ against these files.  The white-noise stream in both is the project's Philox
 stand-in for GSL's ranlxd1 (the shim's gsl_rng_uniform), so the runs share
 identical initial conditions.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root, with MGP_REFERENCE_SRC set to the reference's
+src/ directory:  MGP_REFERENCE_SRC=<reference>/src python tests/golden/make_golden.py
 """
 import os
 import subprocess

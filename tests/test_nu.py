@@ -159,13 +159,15 @@ def test_neutrino_reader_errors(tmp_path, info):
 # --------------------------------------------------------------------------
 # The reference's own CAMB example tables (camb_data/example_data_nu0.4, the
 # inputs of its f(R)+neutrino test runs) and its own neutrino build, where
-# the reference tree is present.
+# the reference tree is given (MGP_REFERENCE_SRC = its src/ directory).
 REAL_COSMO = dict(Omega=0.3175, OmegaBaryon=0.049, HubbleParam=0.671, Sigma8=0.7656, PrimordialIndex=0.966)
 
 
 @pytest.fixture(scope="module")
 def real_info(tmp_path_factory):
     from oracle import ref_build
+    if not ref_build.available():
+        pytest.skip("reference tree not given (MGP_REFERENCE_SRC)")
     d = os.path.join(os.path.dirname(ref_build.REF_SRC), "camb_data", "example_data_nu0.4")
     if not os.path.isdir(d):
         pytest.skip("reference CAMB example data not present")
