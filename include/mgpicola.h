@@ -185,6 +185,58 @@ int mgp_read_parameterfile(const char *fname, int model, int pofk_keys, int read
 /* Start-up: validate parameters, solve the growth ODEs, normalise the power
  * spectrum, allocate device memory on `device` and plan the FFTs. */
 int mgp_create(const mgp_params *p, int device, mgp_ctx **out);
+
+/* User model hooks: the functions a user of the reference edits in
+ * src/user_defined_functions.h to define a gravity model (lines 413-904),
+ * as host FP64 callbacks.  Every member is optional: NULL keeps the built-in
+ * model that mgp_params selects, and the built-in functions call the other
+ * hooks through the same table (the built-in GeffoverG of f(R) uses a user
+ * mass2_of_a, as in the reference).  `user` is passed to every call.  The
+ * library calls them on the host only: while the growth tables are solved
+ * at mgp_create, and once per step for the step's scalars (coupling, mass
+ * term, phi_crit, Factor_2LPT) and screening tables.
+ *   hubble, dhubbleda     H(a)/H0 and its a-derivative          (:413-452)
+ *   GeffoverG             mu(a, k), k in h/Mpc                  (:618-660)
+ *   beta_of_a, mass2_of_a, dmass2_of_ada
+ *                         coupling strength, m^2(a)/H0^2 and d/da (:462-560)
+ *   coupling_function     the coupling of the fifth-force equation (:587-611)
+ *   phi_of_a              phi_crit(a) of the potential screening (:571-579,
+ *                         the f(R) form of :725-750 for FOFR)
+ *   screening_factor_potential / screening_factor_density
+ *                         the screening factors as functions of the Newtonian
+ *                         potential or the smoothed density (:725-773); the
+ *                         device applies them through a table of 16384
+ *                         values per step over asinh-spaced arguments
+ *                         (linear interpolation, ~1e-6 relative), where the
+ *                         built-in forms are evaluated exactly
+ *   Factor_2LPT           the 2LPT source factor (:814-838)
+ *   second_order_kernel   gamma_2(k, k1, k2, cos theta, a) of the
+ *                         scale-dependent 2LPT growth (:862-904) */
+typedef struct mgp_model_hooks {
+  void *user;
+  double (*hubble)(double a, void *user);
+  double (*dhubbleda)(double a, void *user);
+  double (*GeffoverG)(double a, double k, void *user);
+  double (*beta_of_a)(double a, void *user);
+  double (*mass2_of_a)(double a, void *user);
+  double (*dmass2_of_ada)(double a, void *user);
+  double (*coupling_function)(double a, void *user);
+  double (*phi_of_a)(double a, void *user);
+  double (*screening_factor_potential)(double a, double phinewton, void *user);
+  double (*screening_factor_density)(double a, double density, void *user);
+  double (*Factor_2LPT)(double a, void *user);
+  double (*second_order_kernel)(double k, double k1, double k2, double costheta, double a, void *user);
+} mgp_model_hooks;
+
+/* mgp_create with user model hooks (NULL hooks = mgp_create).  The table is
+ * copied; `user` must stay valid for the context's life. */
+int mgp_create_with_hooks(const mgp_params *p, const mgp_model_hooks *hooks, int device, mgp_ctx **out);
+/* Host-only cosmology of a parameter set with hooks, as mgp_cosmo_eval
+ * (which 0-9); `which` 10-15 give the model functions themselves at a = x
+ * as the library evaluates them (10 hubble, 11 GeffoverG at k = 0.1 h/Mpc,
+ * 12 coupling_function, 13 mass2_of_a, 14 phi_crit, 15 Factor_2LPT). */
+int mgp_cosmo_eval_hooks(const mgp_params *p, const mgp_model_hooks *hooks, int which, const double *x, int n,
+                         double *out);
 int mgp_destroy(mgp_ctx *ctx);
 const char *mgp_last_error(void);
 

@@ -18,6 +18,9 @@ INCLUDE = os.path.join(ROOT, "include")
 OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libmgpicola.so")
+# the command-line driver (MG_PICOLA_<MODEL> <ParameterFile>), linked to the library
+EXE = os.path.join(LIBDIR, "mgpicola_run")
+EXE_SOURCE = "mgpicola_main.c"
 
 CU_SOURCES = ["mgp_kernels.cu", "mgp_api.cu", "mgp_run.cu", "mgp_noalloc.cu", "mgp_sd.cu", "mgp_nn.cu"]
 C_SOURCES = ["mgp_cosmo.c", "mgp_param.c", "mgp_io.c"]
@@ -82,6 +85,16 @@ def build(verbose=False):
             sys.stdout.write(r.stdout + r.stderr)
         if r.returncode:
             raise RuntimeError("link failed")
+    src = os.path.join(CSRC, EXE_SOURCE)
+    if _stale(EXE, [src, LIB, os.path.join(INCLUDE, "mgpicola.h")]):
+        cmd = ["gcc", "-O2", "-std=gnu99", "-Wall", "-o", EXE, src, "-I" + INCLUDE, "-L" + LIBDIR, "-lmgpicola",
+               "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode:
+            print(" ".join(cmd))
+            sys.stdout.write(r.stdout + r.stderr)
+        if r.returncode:
+            raise RuntimeError("driver link failed")
     return LIB
 
 

@@ -367,7 +367,7 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   free(c->box_p);
   void *bufs[] = {c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
                   c->fft_work, c->rk_bin, c->pk_thr, c->win1d, c->pk_block, c->pk_sum, c->rsd_block, c->rsd_sum,
-                  c->pk_sum_tot, c->nu_tab_d, c->nu_row_d, c->nu_x_d, c->nu_den_d};
+                  c->pk_sum_tot, c->nu_tab_d, c->nu_row_d, c->nu_x_d, c->nu_den_d, c->scr_tab};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
     if (bufs[i]) cudaFree(bufs[i]);
   if (c->nu_row_h) cudaFreeHost(c->nu_row_h);
@@ -406,7 +406,8 @@ static mgp_params box_params(const mgp_params *p, const mgp_box_params *bp) {
 
 static const mgp_cosmo *cosmo_of(const mgp_ctx *c, int b) { return b == 0 ? &c->cosmo : &c->box_cosmo[b]; }
 
-static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxes, int device, mgp_ctx **out) {
+static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxes, int device, mgp_ctx **out,
+                       const mgp_model_hooks *hooks = NULL) {
   if (!p || !out) return mgp_set_error(MGP_EINVAL, "null argument");
   *out = NULL;
   RET_IF(validate(p));
@@ -424,7 +425,7 @@ static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxe
   c->p = c->box_p[0];
   c->device = device;
   char err[512] = "";
-  int rc = mgp_cosmo_init(&c->cosmo, &c->box_p[0], err, sizeof(err));
+  int rc = mgp_cosmo_init_hooks(&c->cosmo, &c->box_p[0], hooks, err, sizeof(err));
   if (rc) {
     free(c->box_p);
     free(c);
@@ -513,6 +514,10 @@ static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxe
 
 extern "C" int mgp_create(const mgp_params *p, int device, mgp_ctx **out) {
   return create_impl(p, 1, NULL, device, out);
+}
+
+extern "C" int mgp_create_with_hooks(const mgp_params *p, const mgp_model_hooks *hooks, int device, mgp_ctx **out) {
+  return create_impl(p, 1, NULL, device, out, hooks);
 }
 
 extern "C" int mgp_batch_create(const mgp_params *p, int nbox, const mgp_box_params *boxes, int device,
@@ -739,6 +744,26 @@ static int require_particles(mgp_ctx *c) {
   return MGP_OK;
 }
 
+// A user's screening_factor_potential (density = 0, argument the Newtonian
+// potential of mg1) or screening_factor_density (density = 1, argument the
+// smoothed density of mg1) applied to rho through a table of the function at
+// this a: MGP_SCREEN_TABLE values at t = asinh(u/u_s) uniform in [t0, t1],
+// copied from pageable memory (the copy has been staged when it returns).
+static int user_screening(mgp_ctx *c, double A, int density, double mult, long long nr) {
+  const mgp_model_hooks *h = &c->cosmo.hooks;
+  const int nt = MGP_SCREEN_TABLE;
+  const double us = density ? 1.0 : 1e-8, t0 = density ? -1.5 : -25.0, t1 = density ? 20.0 : 25.0;
+  const double dt = (t1 - t0) / (nt - 1);
+  if (!c->scr_tab) MGP_CUDA(cudaMalloc(&c->scr_tab, sizeof(float) * nt));
+  std::vector<float> tab(nt);
+  for (int j = 0; j < nt; j++) {
+    const double u = us * sinh(t0 + dt * j);
+    tab[j] = (float)(density ? h->screening_factor_density(A, u, h->user) : h->screening_factor_potential(A, u, h->user));
+  }
+  MGP_CUDA(cudaMemcpyAsync(c->scr_tab, tab.data(), sizeof(float) * nt, cudaMemcpyHostToDevice, c->stream));
+  return mgp_launch_screen_table(c->rho, c->mg1, nr, (float)mult, c->scr_tab, nt, us, t0, dt, c->stream);
+}
+
 // MG fifth force (ComputeFifthForce, src/user_defined_functions.h:687-719 and
 // src/mg.h) given delta(x) in rho and delta(k) in dk.  Leaves the MG source
 // for the force pass in rho (as complex) and returns the fused k-space mode.
@@ -756,7 +781,10 @@ static int fifth_force(mgp_ctx *c, double A, int filtered, int *mg_kind, float *
       double norm = 1.0 / pow((double)N, 3) * 1.5 * p->Omega / A * pow(p->Box / 2997.92458 / (2.0 * M_PI), 2);
       if (!filtered) RET_IF(mgp_launch_div_laplacian(c->dk, c->mg1, N, (float)norm, c->stream));
       MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
-      RET_IF(mgp_launch_screen_potential(c->rho, c->mg1, nr, (float)mgp_phicrit(&c->cosmo, A), c->stream));
+      if (mgp_cosmo_user_screening(&c->cosmo, 0))
+        RET_IF(user_screening(c, A, 0, 1.0, nr));
+      else
+        RET_IF(mgp_launch_screen_potential(c->rho, c->mg1, nr, (float)mgp_phicrit(&c->cosmo, A), c->stream));
     }
     MGP_CUFFT(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
     *mg_kind = 1;
@@ -775,8 +803,11 @@ static int fifth_force(mgp_ctx *c, double A, int filtered, int *mg_kind, float *
       RET_IF(mgp_launch_smooth(c->dk, c->mg1, N, p->smoothing_filter, (float)kR1, (float)(1.0 / pow((double)N, 3)),
                                c->stream));
     MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
-    RET_IF(mgp_launch_screen_density(c->rho, c->mg1, nr, (float)coupling_d,
-                                     (float)mgp_dgp_screen_prefactor(&c->cosmo, A), c->stream));
+    if (mgp_cosmo_user_screening(&c->cosmo, 1))
+      RET_IF(user_screening(c, A, 1, coupling_d, nr));
+    else
+      RET_IF(mgp_launch_screen_density(c->rho, c->mg1, nr, (float)coupling_d,
+                                       (float)mgp_dgp_screen_prefactor(&c->cosmo, A), c->stream));
     MGP_CUFFT(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
     *mg_kind = 2;
   } else if (p->model == MGP_MODEL_BRANSDICKE) {

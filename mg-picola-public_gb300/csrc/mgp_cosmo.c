@@ -27,7 +27,14 @@ int mgp_set_error(int code, const char *fmt, ...);
 static double spline_eval(const mgp_spline *s, double x);
 
 /* ------------------------------------------------------------------ hooks */
+/* Each function below is the built-in model of mgp_params unless the user's
+ * hook table replaces it (the hook replaces the whole function, including
+ * its modified_gravity_active checks). */
+#define HOOK1(name, a) \
+  if (c->hooks.name) return c->hooks.name((a), c->hooks.user)
+
 double mgp_hubble(const mgp_cosmo *c, double a) {
+  HOOK1(hubble, a);
   const double om = c->p.Omega;
   if (c->have_jbd) return spline_eval(&c->jbdH, log(a));
   if (c->p.use_w0wa)
@@ -36,6 +43,7 @@ double mgp_hubble(const mgp_cosmo *c, double a) {
 }
 
 double mgp_dhubbleda(const mgp_cosmo *c, double a) {
+  HOOK1(dhubbleda, a);
   const double om = c->p.Omega;
   if (c->have_jbd) return spline_eval(&c->jbddH, log(a));
   double rhs = -3.0 * om / (a * a * a * a);
@@ -48,6 +56,7 @@ double mgp_beta_dgp(const mgp_cosmo *c, double a) {
 }
 
 double mgp_beta_of_a(const mgp_cosmo *c, double a) {
+  HOOK1(beta_of_a, a);
   switch (c->p.model) {
     case MGP_MODEL_FOFR: return 1.0 / sqrt(6.0);
     case MGP_MODEL_MBETA: {
@@ -59,6 +68,7 @@ double mgp_beta_of_a(const mgp_cosmo *c, double a) {
 }
 
 double mgp_mass2_of_a(const mgp_cosmo *c, double a) {
+  HOOK1(mass2_of_a, a);
   if (c->p.model == MGP_MODEL_FOFR) {
     const double om = c->p.Omega, n = c->p.nfofr;
     double fac = om / (a * a * a) + 4.0 * (1.0 - om);
@@ -74,6 +84,7 @@ double mgp_mass2_of_a(const mgp_cosmo *c, double a) {
 }
 
 double mgp_coupling(const mgp_cosmo *c, double a) {
+  HOOK1(coupling_function, a);
   switch (c->p.model) {
     case MGP_MODEL_FOFR:
     case MGP_MODEL_MBETA: {
@@ -87,6 +98,7 @@ double mgp_coupling(const mgp_cosmo *c, double a) {
 }
 
 double mgp_geff(const mgp_cosmo *c, double a, double k) {
+  if (c->hooks.GeffoverG) return c->hooks.GeffoverG(a, k, c->hooks.user);
   if (!c->p.modified_gravity_active || c->p.use_lcdm_growth_factors) return 1.0;
   switch (c->p.model) {
     case MGP_MODEL_FOFR:
@@ -103,6 +115,7 @@ double mgp_geff(const mgp_cosmo *c, double a, double k) {
 }
 
 double mgp_factor_2lpt(const mgp_cosmo *c, double a) {
+  HOOK1(Factor_2LPT, a);
   if (!c->p.modified_gravity_active || c->p.use_lcdm_growth_factors) return 1.0;
   if (c->p.model == MGP_MODEL_DGP) {
     double b = mgp_beta_dgp(c, a), r = c->p.rcH0_DGP;
@@ -113,6 +126,7 @@ double mgp_factor_2lpt(const mgp_cosmo *c, double a) {
 
 /* dm^2/da / H0^2 (user_defined_functions.h:527-560) */
 double mgp_dmass2_of_ada(const mgp_cosmo *c, double a) {
+  HOOK1(dmass2_of_ada, a);
   const double om = c->p.Omega;
   if (c->p.model == MGP_MODEL_FOFR) {
     double a3 = a * a * a, fac = om / a3 + 4.0 * (1.0 - om), fac0 = om + 4.0 * (1.0 - om), n = c->p.nfofr;
@@ -140,6 +154,8 @@ typedef struct {
   int g2kind;              /* 0 none, 1 f(R), 2 DGP, 3 m(a)/beta(a) */
   double g2_pref, g2_pi0;  /* f(R): prefactor and pi(k) = (k c/(H0 a))^2 + pi0; MBETA: pi0 = m2 */
   double inv_a2;           /* (c/H0 / a)^2 multiplier of k^2 in pi(k) */
+  const mgp_model_hooks *h; /* user GeffoverG / second_order_kernel, called per k */
+  double a;
 } mgp_sd_apart;
 
 static void sd_apart(const mgp_cosmo *c, double a, mgp_sd_apart *o) {
@@ -150,6 +166,8 @@ static void sd_apart(const mgp_cosmo *c, double a, mgp_sd_apart *o) {
   o->beta0 = 1.5 * om / (a3 * o->H * o->H);
   o->geff_const = 1.0;
   o->inv_a2 = (INVERSE_H0_MPCH / a) * (INVERSE_H0_MPCH / a);
+  o->a = a;
+  if (c->hooks.GeffoverG || c->hooks.second_order_kernel) o->h = &c->hooks;
   if (!c->p.modified_gravity_active || c->p.use_lcdm_growth_factors) return;
   switch (c->p.model) {
     case MGP_MODEL_FOFR:
@@ -185,6 +203,7 @@ static void sd_apart(const mgp_cosmo *c, double a, mgp_sd_apart *o) {
 }
 
 static double sd_mu(const mgp_sd_apart *o, double k) {
+  if (o->h && o->h->GeffoverG) return o->h->GeffoverG(o->a, k, o->h->user);
   if (!o->kdep) return o->geff_const;
   double k2 = (k * INVERSE_H0_MPCH) * (k * INVERSE_H0_MPCH);
   if (k2 == 0) return 1.0;
@@ -194,6 +213,8 @@ static double sd_mu(const mgp_sd_apart *o, double k) {
 /* second_order_kernel(k, k/sqrt2, k/sqrt2, 0, a): the cos(theta) term of the
  * reference vanishes at cos(theta) = 0. */
 static double sd_gamma2(const mgp_sd_apart *o, double k) {
+  if (o->h && o->h->second_order_kernel)
+    return o->h->second_order_kernel(k, k / sqrt(2.0), k / sqrt(2.0), 0.0, o->a, o->h->user);
   double k2 = k * k * o->inv_a2, k12 = 0.5 * k2;
   switch (o->g2kind) {
     case 1: return o->g2_pref * k * k / ((k2 + o->g2_pi0) * (k12 + o->g2_pi0) * (k12 + o->g2_pi0));
@@ -213,6 +234,7 @@ static double sd_modfac(const mgp_sd_apart *o, double a, double k, double mu, do
 }
 
 double mgp_phicrit(const mgp_cosmo *c, double a) {
+  HOOK1(phi_of_a, a);
   const double om = c->p.Omega;
   if (c->p.model == MGP_MODEL_MBETA) return c->have_phia ? spline_eval(&c->phia, log(a)) : 0.0;
   return 1.5 * c->p.fofr0 * pow((om + 4.0 * (1.0 - om)) / (om / (a * a * a) + 4.0 * (1.0 - om)), c->p.nfofr + 1.0);
@@ -1196,8 +1218,17 @@ static int phia_solve(mgp_cosmo *c) {
 }
 
 int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen) {
+  return mgp_cosmo_init_hooks(c, p, NULL, err, errlen);
+}
+
+int mgp_cosmo_user_screening(const mgp_cosmo *c, int density) {
+  return density ? c->hooks.screening_factor_density != NULL : c->hooks.screening_factor_potential != NULL;
+}
+
+int mgp_cosmo_init_hooks(mgp_cosmo *c, const mgp_params *p, const mgp_model_hooks *hooks, char *err, size_t errlen) {
   memset(c, 0, sizeof(*c));
   c->p = *p;
+  if (hooks) c->hooks = *hooks;
   int rc;
   if (p->massive_neutrinos) {
     if (!p->scaledependent) {
@@ -1274,9 +1305,15 @@ void mgp_cosmo_free(mgp_cosmo *c) {
  * Sq/Sphi are available through mgp_cosmo_coeff. */
 int mgp_cosmo_eval(const mgp_params *p, int which, const double *x, int n, double *out) {
   if (which < 0 || which > 9) return mgp_set_error(MGP_EINVAL, "which = %d out of range", which);
+  return mgp_cosmo_eval_hooks(p, NULL, which, x, n, out);
+}
+
+int mgp_cosmo_eval_hooks(const mgp_params *p, const mgp_model_hooks *hooks, int which, const double *x, int n,
+                         double *out) {
+  if (!p || which < 0 || which > 15) return mgp_set_error(MGP_EINVAL, "which = %d out of range", which);
   char err[512] = "";
   mgp_cosmo c;
-  int rc = mgp_cosmo_init(&c, p, err, sizeof(err));
+  int rc = mgp_cosmo_init_hooks(&c, p, hooks, err, sizeof(err));
   if (rc) {
     mgp_cosmo_free(&c);
     return mgp_set_error(rc, "%s", err);
@@ -1286,6 +1323,12 @@ int mgp_cosmo_eval(const mgp_params *p, int which, const double *x, int n, doubl
       case 7: out[i] = mgp_cosmo_power(&c, x[i]); break;
       case 8: out[i] = mgp_cosmo_pofk_ratio(&c, x[i], 1.0); break;
       case 9: out[i] = mgp_cosmo_sigma8_enh(&c, x[i]); break;
+      case 10: out[i] = mgp_hubble(&c, x[i]); break;
+      case 11: out[i] = mgp_geff(&c, x[i], 0.1); break;
+      case 12: out[i] = mgp_coupling(&c, x[i]); break;
+      case 13: out[i] = mgp_mass2_of_a(&c, x[i]); break;
+      case 14: out[i] = mgp_phicrit(&c, x[i]); break;
+      case 15: out[i] = mgp_factor_2lpt(&c, x[i]); break;
       default: out[i] = mgp_cosmo_growth(&c, which, x[i]);
     }
   }

@@ -24,6 +24,8 @@ typedef struct {
 
 typedef struct mgp_cosmo {
   mgp_params p;
+  /* user model hooks (NULL members: the built-in model) */
+  mgp_model_hooks hooks;
   /* growth splines over x = ln a (src/cosmo.c:54-95) */
   mgp_spline D, dDdy, ddDddy, D2, dD2dy, ddD2ddy;
   mgp_spline DL, dDLdy, ddDLddy, D2L, dD2Ldy, ddD2Lddy;
@@ -54,6 +56,10 @@ typedef struct mgp_cosmo {
 } mgp_cosmo;
 
 int mgp_cosmo_init(mgp_cosmo *c, const mgp_params *p, char *err, size_t errlen);
+/* the same with user model hooks (NULL = none) */
+int mgp_cosmo_init_hooks(mgp_cosmo *c, const mgp_params *p, const mgp_model_hooks *hooks, char *err, size_t errlen);
+/* the user's screening functions, when given (else NULL) */
+int mgp_cosmo_user_screening(const mgp_cosmo *c, int density);
 /* Massive-neutrino density factors per integer |k|^2 = rk of an N^3 mesh
  * (src/auxPM.c:383-421), OmegaNu/Omega N^3 T_nu(k, a) / T_cb(k, 1):
  * mgp_cosmo_nu_den fills den[rk] = T_cb(k, 1), the step-independent

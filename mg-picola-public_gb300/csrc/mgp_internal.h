@@ -119,7 +119,10 @@ struct mgp_ctx {
    *   slot 2 "vel"   FIELD_dDdy for outputs, RSD and the non-COLA IC velocity
    * each the sum of the 1LPT and 2LPT fields (every reader adds them). */
   int sd;
-  int sd_fold;              /* Nmesh / Nsample (alias count per axis) */
+  int sd_fold;              /* Nmesh / Nsample (alias count per axis); 0 when Nmesh is
+                               not a multiple of Nsample (full-mesh path) */
+  float *sd_full;           /* full-mesh path: one padded real N^3 grid */
+  double *sd_part;          /* full-mesh path: read-out partial sums */
   float *sd_dk[2];          /* delta(k), -source(k): complex [N][N][NH] */
   float *sd_slot[3];        /* 3 components x sd_grid floats each */
   long long sd_grid;        /* Ns*Ns*Ps floats */
@@ -157,6 +160,9 @@ struct mgp_ctx {
   cudaStream_t out_stream;
   cudaEvent_t out_ev[2];
   void *out_writer;            /* host writer thread state (mgp_run.cu) */
+
+  /* user screening functions: the device copy of the step's table */
+  float *scr_tab;
 
   /* learned force closure added to the force grids (mgp_set_closure) */
   struct mgp_closure *closure;
@@ -294,6 +300,10 @@ int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float
 int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float coupling, float pref,
                               cudaStream_t st, int nbox = 1, const mgp_box_scalars *bs = NULL);
 int mgp_launch_scale_complex(float *c, long long ncomplex, float factor, cudaStream_t st);
+/* a user's screening function from its per-step table (mgp_model_hooks) */
+#define MGP_SCREEN_TABLE 16384
+int mgp_launch_screen_table(float *rho, const float *arg, long long n, float mult, const float *tab, int nt, double us,
+                            double t0, double dt, cudaStream_t st);
 
 /* IC */
 int mgp_launch_ic_delta(const uint32_t *seedtable, const double *amp_rk, const unsigned char *cut1d,

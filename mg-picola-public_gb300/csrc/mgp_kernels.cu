@@ -821,6 +821,32 @@ int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float c
   return MGP_OK;
 }
 
+// A user's screening function (mgp_model_hooks), tabulated on the host once
+// per step over t = asinh(u / u_s) at nt uniform points from t0: rho *=
+// mult * S(u) with S interpolated linearly in t, u the Newtonian potential
+// or the smoothed density at the cell (clamped to the table's range).
+__global__ void k_screen_table(float *__restrict__ rho, const float *__restrict__ arg, long long n, float mult,
+                               const float *__restrict__ tab, int nt, float inv_us, float t0, float inv_dt) {
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    float x = (asinhf(arg[i] * inv_us) - t0) * inv_dt;
+    x = fminf(fmaxf(x, 0.0f), (float)(nt - 1));
+    int j = min((int)x, nt - 2);
+    float f = x - (float)j;
+    float S = fmaf(f, tab[j + 1] - tab[j], tab[j]);
+    rho[i] *= mult * S;
+  }
+}
+
+int mgp_launch_screen_table(float *rho, const float *arg, long long n, float mult, const float *tab, int nt, double us,
+                            double t0, double dt, cudaStream_t st) {
+  k_screen_table<<<blocks_for(n, g_budget_grid), MGP_THREADS, 0, st>>>(rho, arg, n, mult, tab, nt, (float)(1.0 / us),
+                                                                       (float)t0, (float)(1.0 / dt));
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  return MGP_OK;
+}
+
 // ComputeFifthForce_TimeDepGeffModels (src/mg.h:127-137): P3D *= Geff/G.
 __global__ void k_scale(float *__restrict__ c, long long n, float f) {
   long long stride = (long long)gridDim.x * blockDim.x;

@@ -16,6 +16,11 @@
 //     costs one fold pass over the N^3 spectrum and three Ns^3 C2R instead of
 //     three N^3 C2R per order;
 //   - the mean over the lattice is G(0), so mean removal is G(0) = 0.
+// When Nmesh is not a multiple of Nsample the lattice points fall between mesh
+// points, and the fields follow the reference's algorithm itself: per
+// component the full-mesh spectrum (k_sd_full), an N^3 C2R, the trilinear
+// read-out at the lattice points (k_sd_readout, src/2LPT.c:1642-1704) and the
+// removal of the lattice mean (src/2LPT.c:1714-1728).
 // On the kz = 0 and kz = N/2 planes the C2R keeps only the Hermitian part of
 // its input (FFTW's half-complex semantics); with Hermitian delta and S2
 // that zeroes the derivative components whose own index is the Nyquist one,
@@ -32,6 +37,8 @@
 namespace {
 
 constexpr int kThreads = 256;
+// blocks of the general-ratio read-out (fixed, so its mean sums in a fixed order)
+#define SD_READOUT_BLOCKS 1216
 
 // Integer wave number of index idx (src/2LPT.c:1586-1602): idx < N/2 -> idx,
 // else idx - N, so N/2 maps to -N/2.
@@ -148,6 +155,97 @@ __global__ void __launch_bounds__(kThreads) k_sd_fold(const float2 *__restrict__
   }
 }
 
+// Full-mesh spectrum of component a of field f (table components xy for
+// f = 0, zw for f = 1): i d_a T(|k|^2) . (delta, -S2), one warp per (kx, ky)
+// row (from_cdisp_store_to_ZA, src/2LPT.c:1586-1627), with the Nyquist
+// derivative entries written as zero as in k_sd_fold.
+__global__ void __launch_bounds__(kThreads) k_sd_full(const float2 *__restrict__ d1, const float2 *__restrict__ d2,
+                                                       const float4 *__restrict__ tab, int N, int f, int a,
+                                                       float2 *__restrict__ out) {
+  const int NH = N / 2 + 1;
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < (long long)N * N; row += nw) {
+    const int kx = (int)(row / N), ky = (int)(row - (long long)kx * N);
+    const int dx = sd_d(kx, N), dy = sd_d(ky, N);
+    for (int kz = lane; kz < NH; kz += 32) {
+      const long long c = row * NH + kz;
+      const int dz = sd_d(kz, N);
+      const float4 t = __ldg(tab + ((long long)dx * dx + (long long)dy * dy + (long long)dz * dz));
+      const float T1 = f == 0 ? t.x : t.z, T2 = f == 0 ? t.y : t.w;
+      const float2 u = __ldg(d1 + c), w = __ldg(d2 + c);
+      const float2 S = make_float2(T1 * u.x + T2 * w.x, T1 * u.y + T2 * w.y);
+      float m = a == 0 ? (float)dx : (a == 1 ? (float)dy : (float)dz);
+      if (kz == 0 || 2 * kz == N) {
+        if ((a == 0 && 2 * kx == N) || (a == 1 && 2 * ky == N) || a == 2) m = 0.f;
+      }
+      out[c] = make_float2(-m * S.y, m * S.x);
+    }
+  }
+}
+
+// Trilinear read-out of the real field at the Lagrangian lattice points
+// (i, j, k) N/Ns (src/2LPT.c:1642-1704): fractions from the exact integer
+// split of i N / Ns, periodic neighbours; per-block sums of the values for
+// the mean (fixed order, FP64).
+__global__ void __launch_bounds__(kThreads) k_sd_readout(const float *__restrict__ g, int N, int Ns, long long np,
+                                                          float *__restrict__ out, int pitch,
+                                                          double *__restrict__ partials) {
+  __shared__ double sh[kThreads / 32];
+  const long long P = 2 * (long long)(N / 2 + 1);
+  double acc = 0.0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    const long long ij = p / Ns;
+    const int k = (int)(p - ij * Ns), i = (int)(ij / Ns), j = (int)(ij - (long long)i * Ns);
+    int idx[3], nxt[3];
+    float fr[3];
+    const int l[3] = {i, j, k};
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const long long qn = (long long)l[q] * N;
+      idx[q] = (int)(qn / Ns);
+      fr[q] = (float)(qn - (long long)idx[q] * Ns) / (float)Ns;
+      nxt[q] = idx[q] + 1 >= N ? idx[q] + 1 - N : idx[q] + 1;
+    }
+    const float u = fr[0], v = fr[1], w = fr[2];
+    const long long r00 = ((long long)idx[0] * N + idx[1]) * P, r01 = ((long long)idx[0] * N + nxt[1]) * P;
+    const long long r10 = ((long long)nxt[0] * N + idx[1]) * P, r11 = ((long long)nxt[0] * N + nxt[1]) * P;
+    const float val = g[r00 + idx[2]] * (1 - u) * (1 - v) * (1 - w) + g[r00 + nxt[2]] * (1 - u) * (1 - v) * w +
+                      g[r01 + idx[2]] * (1 - u) * v * (1 - w) + g[r01 + nxt[2]] * (1 - u) * v * w +
+                      g[r10 + idx[2]] * u * (1 - v) * (1 - w) + g[r10 + nxt[2]] * u * (1 - v) * w +
+                      g[r11 + idx[2]] * u * v * (1 - w) + g[r11 + nxt[2]] * u * v * w;
+    out[ij * pitch + k] = val;
+    acc += (double)val;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q];
+    partials[blockIdx.x] = t;
+  }
+}
+
+// Removes the lattice mean (src/2LPT.c:1714-1728): every block sums the
+// read-out partials in the same fixed order, then subtracts.
+__global__ void k_sd_sub_mean(float *__restrict__ out, int pitch, int Ns, long long np,
+                              const double *__restrict__ partials, int nparts) {
+  __shared__ float mean;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < nparts; q++) t += partials[q];
+    mean = (float)(t / (double)np);
+  }
+  __syncthreads();
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    const long long ij = p / Ns;
+    out[ij * pitch + (p - ij * Ns)] -= mean;
+  }
+}
+
 // IC particle state (src/main.c:256-307, SCALEDEPENDENT branch): the
 // displacement from the lattice is the D field (1LPT + 2LPT, already at a_i);
 // the velocity is 0 for COLA, else the dDdy field.
@@ -183,13 +281,15 @@ __global__ void k_sd_store(const float2 *__restrict__ dk, const float2 *__restri
 
 int mgp_sd_alloc(mgp_ctx *c) {
   const int N = c->g.N, Ns = c->Ns;
-  if (N % Ns != 0)
-    return mgp_set_error(MGP_EINVAL,
-                         "scale-dependent growth needs Nmesh to be a multiple of Nsample (Nmesh = %d, Nsample = %d)",
-                         N, Ns);
   if (Ns % 2) return mgp_set_error(MGP_EINVAL, "scale-dependent growth needs an even Nsample (%d)", Ns);
   c->sd = 1;
-  c->sd_fold = N / Ns;
+  // alias fold when the lattice points are mesh points, else the full-mesh
+  // path with the trilinear read-out (0)
+  c->sd_fold = N % Ns == 0 ? N / Ns : 0;
+  if (!c->sd_fold) {
+    MGP_CUDA(cudaMalloc(&c->sd_full, sizeof(float) * (size_t)c->g.nreal));
+    MGP_CUDA(cudaMalloc(&c->sd_part, sizeof(double) * SD_READOUT_BLOCKS));
+  }
   c->sd_pitch = 2 * (Ns / 2 + 1);
   c->sd_grid = (long long)Ns * Ns * c->sd_pitch;
   c->sd_nmax = 3LL * (N / 2) * (N / 2);
@@ -229,6 +329,8 @@ void mgp_sd_free(mgp_ctx *c) {
     if (c->sd_slot[q]) cudaFree(c->sd_slot[q]);
   if (c->sd_cols) cudaFree(c->sd_cols);
   if (c->sd_tab) cudaFree(c->sd_tab);
+  if (c->sd_full) cudaFree(c->sd_full);
+  if (c->sd_part) cudaFree(c->sd_part);
   cufftDestroy(c->plan_c2r_s);
   c->sd = 0;
 }
@@ -298,6 +400,35 @@ static int fields_pass(mgp_ctx *c, double A, double AFF, int n, const int *types
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   const int Ns = c->Ns;
+  if (!c->sd_fold) {
+    // Nmesh not a multiple of Nsample: per field and component the
+    // full-mesh spectrum, an N^3 C2R, the trilinear read-out and the mean
+    const int N = c->g.N;
+    for (int f = 0; f < n; f++) {
+      const int s = slot_of(types[f]);
+      for (int a = 0; a < 3; a++) {
+        k_sd_full<<<mgp_blocks_for((long long)N * N * 32, 8), kThreads, 0, c->stream>>>(
+            (const float2 *)c->sd_dk[0], (const float2 *)c->sd_dk[1], (const float4 *)c->sd_tab, N, f, a,
+            (float2 *)c->sd_full);
+        MGP_CHECK_LAUNCH();
+        g_kernel_launches++;
+        MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->sd_full, (cufftReal *)c->sd_full));
+        float *out = c->sd_slot[s] + a * c->sd_grid;
+        k_sd_readout<<<SD_READOUT_BLOCKS, kThreads, 0, c->stream>>>(c->sd_full, N, Ns, c->np, out, c->sd_pitch,
+                                                                    c->sd_part);
+        MGP_CHECK_LAUNCH();
+        g_kernel_launches++;
+        k_sd_sub_mean<<<SD_READOUT_BLOCKS, kThreads, 0, c->stream>>>(out, c->sd_pitch, Ns, c->np, c->sd_part,
+                                                                     SD_READOUT_BLOCKS);
+        MGP_CHECK_LAUNCH();
+        g_kernel_launches++;
+      }
+      c->sd_kind[s] = types[f];
+      c->sd_a[s] = A;
+      c->sd_aff[s] = AFF;
+    }
+    return MGP_OK;
+  }
   float *o0 = c->sd_slot[slot_of(types[0])], *o1 = n > 1 ? c->sd_slot[slot_of(types[1])] : NULL;
   k_sd_fold<<<mgp_blocks_for((long long)Ns * Ns * 32, 8), kThreads, 0, c->stream>>>(
       (const float2 *)c->sd_dk[0], (const float2 *)c->sd_dk[1], (const float4 *)c->sd_tab, c->g.N, Ns, c->sd_fold, n,

@@ -18,7 +18,8 @@ FILTER_NONE, FILTER_GAUSSIAN, FILTER_TOPHAT, FILTER_SHARPK = 0, 1, 2, 3
 
 # exported symbols of include/mgpicola.h
 EXPORTS = [
-    "mgp_params_default", "mgp_read_parameterfile", "mgp_create", "mgp_destroy", "mgp_last_error",
+    "mgp_params_default", "mgp_read_parameterfile", "mgp_create", "mgp_create_with_hooks", "mgp_cosmo_eval_hooks",
+    "mgp_destroy", "mgp_last_error",
     "mgp_displacement_fields", "mgp_get_displacements", "mgp_kick_drift", "mgp_step", "mgp_run", "mgp_pofk",
     "mgp_pofk_total", "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
     "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_mark", "mgp_mark_ms", "mgp_kernel_ms_step", "mgp_launch_count",
@@ -122,6 +123,8 @@ def lib():
             getattr(L, f).argtypes = [vp, C.c_double, C.c_double, C.c_double]
             getattr(L, f).restype = C.c_double
         L.mgp_cosmo_eval.argtypes = [C.POINTER(Params), C.c_int, dp, C.c_int, dp]
+        L.mgp_cosmo_eval_hooks.argtypes = [C.POINTER(Params), C.POINTER(ModelHooks), C.c_int, dp, C.c_int, dp]
+        L.mgp_create_with_hooks.argtypes = [C.POINTER(Params), C.POINTER(ModelHooks), C.c_int, C.POINTER(vp)]
         L.mgp_cosmo_coeff.argtypes = [C.POINTER(Params), C.c_int, dp, dp, dp, C.c_int, dp]
         L.mgp_growth_scaledependent.argtypes = [C.POINTER(Params), C.c_int, dp, dp, C.c_int, dp]
         L.mgp_assign_displacement_fields.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_int)]
@@ -243,6 +246,46 @@ def cosmo_eval(params, which, x):
     return out
 
 
+_F1 = C.CFUNCTYPE(C.c_double, C.c_double, C.c_void_p)
+_F2 = C.CFUNCTYPE(C.c_double, C.c_double, C.c_double, C.c_void_p)
+_F5 = C.CFUNCTYPE(C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_void_p)
+
+
+class ModelHooks(C.Structure):
+    """struct mgp_model_hooks: the user_defined_functions.h model functions
+    as callbacks (src/user_defined_functions.h:413-904)."""
+    _fields_ = [("user", C.c_void_p), ("hubble", _F1), ("dhubbleda", _F1), ("GeffoverG", _F2), ("beta_of_a", _F1),
+                ("mass2_of_a", _F1), ("dmass2_of_ada", _F1), ("coupling_function", _F1), ("phi_of_a", _F1),
+                ("screening_factor_potential", _F2), ("screening_factor_density", _F2), ("Factor_2LPT", _F1),
+                ("second_order_kernel", _F5)]
+    _SIGS = {"GeffoverG": _F2, "screening_factor_potential": _F2, "screening_factor_density": _F2,
+             "second_order_kernel": _F5}
+
+    @classmethod
+    def from_functions(cls, **fns):
+        """Hooks from Python functions of the reference's arguments (without
+        the user pointer); the callback objects are kept on the table."""
+        h = cls()
+        h._keep = []
+        for name, fn in fns.items():
+            sig = cls._SIGS.get(name, _F1)
+            cb = sig((lambda f: (lambda *a: float(f(*a[:-1]))))(fn))
+            h._keep.append(cb)
+            setattr(h, name, cb)
+        return h
+
+
+def cosmo_eval_hooks(params, hooks, which, x):
+    """cosmo_eval with user model hooks; which 10-15 give hubble,
+    GeffoverG(a, k = 0.1), coupling_function, mass2_of_a, phi_crit and
+    Factor_2LPT at a = x as the library evaluates them."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros_like(x)
+    _check(lib().mgp_cosmo_eval_hooks(C.byref(params), C.byref(hooks) if hooks is not None else None, which, _dptr(x),
+                                      x.size, _dptr(out)))
+    return out
+
+
 def growth_scaledependent(params, which, k, a):
     """growth_*_scaledependent(k, a) of a parameter set (scaledependent = 1)."""
     k = np.ascontiguousarray(k, dtype=np.float64)
@@ -285,10 +328,14 @@ def unpin(arr):
 class Context:
     """One simulation box on one GPU (mgp_ctx)."""
 
-    def __init__(self, params, device=0):
+    def __init__(self, params, device=0, hooks=None):
         self.params = params
+        self.hooks = hooks  # the callbacks must outlive the context
         self.h = C.c_void_p()
-        _check(lib().mgp_create(C.byref(params), device, C.byref(self.h)))
+        if hooks is None:
+            _check(lib().mgp_create(C.byref(params), device, C.byref(self.h)))
+        else:
+            _check(lib().mgp_create_with_hooks(C.byref(params), C.byref(hooks), device, C.byref(self.h)))
         self.N = params.Nmesh
         self.Ns = params.Nsample
         self.np = params.Nsample ** 3
