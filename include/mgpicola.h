@@ -487,6 +487,12 @@ double mgp_kernel_ms(mgp_ctx *ctx, const char *name);
  * mark `from` to it (-1 on error).  Brackets whole runs without per-step
  * synchronisation. */
 int mgp_mark(mgp_ctx *ctx, int slot);
+/* Particle order of the deposit and the kick (no counterpart in the
+ * reference): tiles != 0 (the default for single boxes) buckets the
+ * particles by 16^3-cell tile of the mesh every step, deposits per tile in
+ * shared memory and walks the kick in the same order; 0 keeps the lattice
+ * order.  Both give the same results up to the order of float sums. */
+int mgp_set_particle_order(mgp_ctx *ctx, int tiles);
 /* With mgp_set_timing(ctx, n) for n > 1 the stage events of the last n
  * mgp_step calls are kept: milliseconds of stage `name` in step `step`
  * (counted from that mgp_set_timing call), -1 if not kept or not timed. */

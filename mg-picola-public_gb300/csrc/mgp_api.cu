@@ -38,7 +38,7 @@ extern "C" const char *mgp_last_error(void) { return g_err; }
 // ----------------------------------------------------------------- timing
 static const char *k_timer_names[MGP_NTIMERS] = {"cic",    "r2c",  "pofk",          "mg",         "forces",
                                                    "c2r",    "interp_kick_drift", "step", "lpt_fields", "closure",
-                                                   "closure_conv", "fill"};
+                                                   "closure_conv", "fill", "sort"};
 
 static void tstart(mgp_ctx *c, int t) {
   if (c->timing) {
@@ -128,6 +128,12 @@ extern "C" double mgp_kernel_ms(mgp_ctx *c, const char *name) {
     }
   }
   return -1.0;
+}
+
+extern "C" int mgp_set_particle_order(mgp_ctx *c, int tiles) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  c->tile_mode = tiles ? 1 : 0;
+  return MGP_OK;
 }
 
 extern "C" int mgp_mark(mgp_ctx *c, int slot) {
@@ -376,6 +382,7 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
   for (int k = 0; k < MGP_POS_CHUNKS; k++)
     if (c->ev_chunk[k]) cudaEventDestroy(c->ev_chunk[k]);
   free_history(c);
+  mgp_tiles_free(c);
   for (int t = 0; t < MGP_NTIMERS; t++) {
     if (t < 4 && c->ev_mark[t]) cudaEventDestroy(c->ev_mark[t]);
     if (c->ev[t][0]) cudaEventDestroy(c->ev[t][0]);
@@ -424,6 +431,7 @@ static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxe
   for (int b = 0; b < nbox; b++) c->box_p[b] = boxes ? box_params(p, &boxes[b]) : *p;
   c->p = c->box_p[0];
   c->device = device;
+  c->tile_mode = nbox == 1;
   char err[512] = "";
   int rc = mgp_cosmo_init_hooks(&c->cosmo, &c->box_p[0], hooks, err, sizeof(err));
   if (rc) {
@@ -903,12 +911,23 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   const int N = c->g.N;
   if (c->cosmo.nu) RET_IF(nu_prepare(c, A));
   // PtoMesh, src/auxPM.c:280-432
+  const bool tiles = c->tile_mode && mgp_tile_side(N, c->np) > 0;
+  if (tiles) {
+    // bucket the particles by cell tile (mgp_tiles.cu): the deposit and the
+    // kick of this step walk them in that order
+    tstart(c, T_SORT);
+    RET_IF(mgp_tiles_sort(c));
+    tstop(c, T_SORT);
+  }
   tstart(c, T_FILL);
   RET_IF(mgp_launch_fill(c->rho, c->g.nreal, -1.0f, c->stream));
   tstop(c, T_FILL);
   tstart(c, T_CIC);
   double wpar = pow((double)N / (double)c->Ns, 3);
-  RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, c->p.Box, (float)wpar, c->rho, c->g.P, c->stream));
+  if (tiles)
+    RET_IF(mgp_cic_tiles(c, (float)wpar));
+  else
+    RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, c->p.Box, (float)wpar, c->rho, c->g.P, c->stream));
   tstop(c, T_CIC);
   return fields_from_density(c, A);
 }
@@ -1012,8 +1031,11 @@ extern "C" int mgp_kick_drift(mgp_ctx *c, double AI, double AF, double A, double
   int nblk = mgp_ikd_blocks(c->np);
   const float *D1 = c->sd ? c->sd_slot[0] : c->D1, *D2 = c->sd ? c->sd_slot[1] : c->D2;
   tstart(c, T_IKD);
+  // the cell-tile order of the last deposit, where there is one (any
+  // permutation is correct; that one keeps the force gathers local)
+  const unsigned *order = c->tile_mode && c->tile_ready ? c->tile_order : NULL;
   RET_IF(mgp_launch_ikd(c->frc, c->g.nreal, c->g.N, c->g.P, c->Ns, c->np, c->s, c->v, D1, D2, c->dstate,
-                        c->partials, nblk, &a, c->stream));
+                        c->partials, nblk, &a, c->stream, 1, NULL, order));
   tstop(c, T_IKD);
   if (do_drift) c->have_density = 0;
   return MGP_OK;

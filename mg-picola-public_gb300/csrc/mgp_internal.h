@@ -34,7 +34,7 @@ typedef struct {
   double mean_v[3];    /* mean of the stored v after the last kick */
 } mgp_dstate;
 
-#define MGP_NTIMERS 12
+#define MGP_NTIMERS 13
 
 typedef struct mgp_grid_geom {
   int N, NH;
@@ -161,6 +161,13 @@ struct mgp_ctx {
   cudaEvent_t out_ev[2];
   void *out_writer;            /* host writer thread state (mgp_run.cu) */
 
+  /* cell-tile order of the particles (mgp_tiles.cu): tile of every
+   * particle, particle indices bucketed by tile, tile counts / offsets /
+   * scatter cursors, scan block totals */
+  unsigned *tile_of, *tile_order, *tile_count, *tile_off, *tile_cursor, *tile_bsum;
+  int tile_side, tile_n1, tile_ready;
+  int tile_mode;            /* 1 (default): tile path where it applies; 0: particle order */
+
   /* user screening functions: the device copy of the step's table */
   float *scr_tab;
 
@@ -182,7 +189,7 @@ struct mgp_ctx {
   long long launches;
 };
 
-enum { T_CIC = 0, T_R2C, T_POFK, T_MG, T_FORCES, T_C2R, T_IKD, T_MISC, T_SD, T_NN, T_NNCONV, T_FILL };
+enum { T_CIC = 0, T_R2C, T_POFK, T_MG, T_FORCES, T_C2R, T_IKD, T_MISC, T_SD, T_NN, T_NNCONV, T_FILL, T_SORT };
 
 /* error plumbing (C linkage: also called from the C sources) */
 #ifdef __cplusplus
@@ -280,8 +287,14 @@ int mgp_launch_forces(const float *dk, const float *mgk, float mg_coupling, floa
 int mgp_launch_ikd(const float *frc, long long grid_floats, int N, long long P, int Ns, long long np,
                    float *s, float *v, const float *D1, const float *D2, mgp_dstate *dst,
                    double *partials, int nblocks, const mgp_kd_args *a, cudaStream_t st, int nbox = 1,
-                   const mgp_box_scalars *bs = NULL);
+                   const mgp_box_scalars *bs = NULL, const unsigned *order = NULL);
 int mgp_ikd_blocks(long long np);
+/* cell-tile order (mgp_tiles.cu) */
+int mgp_tile_side(int N, long long np);
+int mgp_tiles_alloc(mgp_ctx *c);
+void mgp_tiles_free(mgp_ctx *c);
+int mgp_tiles_sort(mgp_ctx *c);
+int mgp_cic_tiles(mgp_ctx *c, float wpar);
 int mgp_launch_nu_table(float *tab, int nrk, double kfac, double fac, const double *x, const double *val,
                         const double *dval, int nx, const double *den, cudaStream_t st);
 int mgp_launch_nu_add(float *dk, const float *dk0, int N, double cdmfac, const float *nufac, cudaStream_t st);

@@ -22,7 +22,7 @@ EXPORTS = [
     "mgp_destroy", "mgp_last_error",
     "mgp_displacement_fields", "mgp_get_displacements", "mgp_kick_drift", "mgp_step", "mgp_run", "mgp_pofk",
     "mgp_pofk_total", "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
-    "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_mark", "mgp_mark_ms", "mgp_kernel_ms_step", "mgp_launch_count",
+    "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_mark", "mgp_mark_ms", "mgp_kernel_ms_step", "mgp_set_particle_order", "mgp_launch_count",
     "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
     "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_batch_set_tuning",
@@ -178,6 +178,7 @@ def lib():
         L.mgp_kernel_ms_step.argtypes = [vp, C.c_char_p, C.c_int]
         L.mgp_kernel_ms_step.restype = C.c_double
         L.mgp_mark.argtypes = [vp, C.c_int]
+        L.mgp_set_particle_order.argtypes = [vp, C.c_int]
         L.mgp_mark_ms.argtypes = [vp, C.c_int, C.c_int]
         L.mgp_mark_ms.restype = C.c_double
         L.mgp_launch_count.argtypes = [vp]
@@ -458,6 +459,11 @@ class Context:
         """Stage milliseconds of step `step` from the timing history
         (set_timing(n) with n > 1)."""
         return lib().mgp_kernel_ms_step(self.h, name.encode(), step)
+
+    def set_particle_order(self, tiles):
+        """Cell-tile particle order for the deposit and the kick (default
+        on for single boxes), or the lattice order."""
+        _check(lib().mgp_set_particle_order(self.h, 1 if tiles else 0))
 
     def mark(self, slot):
         """Record event `slot` (0..3) on the context's stream."""

@@ -84,6 +84,61 @@ def test_cic_density_matches_oracle():
     assert err < 2e-5 * np.abs(ref[:, :, :N]).max()
 
 
+@pytest.mark.parametrize("N,Ns,spread", [(32, 16, 0.3), (64, 32, 3.0), (128, 64, 8.0), (48, 32, 1.0)])
+def test_tile_deposit_matches_lattice_order_deposit(N, Ns, spread):
+    """The cell-tile deposit (particles bucketed by 8^3 or 16^3-cell tiles,
+    shared-memory tiles added with float2 reductions) against the deposit in
+    lattice order, and both against the oracle; large displacements put
+    particles far from their lattice tile and on tile faces and box edges."""
+    box = 2.0 * N
+    p = params(N, Ns, box)
+    pos, vel, d1, d2 = random_particles(Ns, box, seed=11, spread=spread)
+    pos[0] = [0.0, 0.0, 0.0]
+    pos[1] = [np.nextafter(np.float32(box), np.float32(0))] * 3
+    pos[2] = [32.0, 32.0, 32.0]  # a tile corner (cell 16)
+    rho = []
+    with M.Context(p) as ctx:
+        ctx.set_particles(pos, vel, d1, d2)
+        for tiles in (True, False):
+            ctx.set_particle_order(tiles)
+            ctx.get_displacements(0.5)
+            rho.append(ctx.grid(0)[:, :, :N].astype(np.float64))
+    ref = O.cic(pos.astype(np.float64), N, Ns, box)[:, :, :N]
+    scale = np.abs(ref).max()
+    assert np.abs(rho[0] - rho[1]).max() < 2e-6 * scale
+    assert np.abs(rho[0] - ref).max() < 2e-5 * scale
+    assert abs(rho[0].mean()) < 1e-6
+
+
+def test_tile_order_run_matches_lattice_order_run():
+    """Five KDK steps with the cell-tile particle order (deposit and kick)
+    against the lattice order: the same run up to float summation order."""
+    N, Ns, box, nsteps = 64, 32, 128.0, 5
+    p = params(N, Ns, box)
+    out = []
+    for tiles in (True, False):
+        with M.Context(p) as ctx:
+            ctx.set_particle_order(tiles)
+            ctx.displacement_fields()
+            A, AI = 0.05, 0.05
+            da = (1.0 - A) / nsteps
+            for _ in range(nsteps):
+                ctx.step(A, AI, A + 0.5 * da, A + da)
+                A, AI = A + da, A + 0.5 * da
+            ctx.get_displacements(A)
+            out.append((ctx.pofk(), ctx.get_particles()))
+    (k0, pk0, _, n0), (pos0, vel0, _, _) = out[0]
+    (k1, pk1, _, n1), (pos1, vel1, _, _) = out[1]
+    np.testing.assert_array_equal(n0, n1)
+    m = n0 > 0
+    m[0] = False
+    assert np.max(np.abs(pk0[m] / pk1[m] - 1)) < 1e-5
+    dx = np.abs(pos0 - pos1)
+    dx = np.minimum(dx, box - dx)
+    assert np.sqrt(np.mean(dx ** 2)) < 1e-5 * box / Ns
+    assert rel_rms(vel0, vel1) < 1e-5
+
+
 @pytest.mark.parametrize("bintype,nbins,kmin,kmax", [(0, 16, 0.0, 0.0), (1, 12, 0.05, 1.5), (0, 40, 0.1, 0.9)])
 def test_pofk_matches_oracle(bintype, nbins, kmin, kmax):
     N, Ns, box = 32, 16, 64.0
