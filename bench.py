@@ -329,7 +329,7 @@ def measured_traffic(N, Np, kernel):
     return int(TRAFFIC_256_512[kernel] * (N / 512.0) ** 3)
 
 
-STAGES = ["fill", "cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "lpt_fields", "closure",
+STAGES = ["sort", "fill", "cic", "r2c", "pofk", "mg", "forces", "c2r", "interp_kick_drift", "lpt_fields", "closure",
           "closure_conv"]
 
 
@@ -430,9 +430,13 @@ def run_gpu(args):
     # e2e through the host-buffer C-ABI entry point, pinned host memory: one
     # whole run from the IC state
     ctx.displacement_fields()
-    pos, vel, d1, d2 = ctx.get_particles()
-    for a in (pos, vel, d1, d2):
-        M.pin(a)
+    arrs = ctx.get_particles()
+    # the P[]-style arrays in page-locked host memory (mgp_host_alloc): on a
+    # busy host, copies from registered pageable arrays slowed down several-fold
+    pos, vel, d1, d2 = (M.host_array(a.shape) for a in arrs)
+    for dst, src in zip((pos, vel, d1, d2), arrs):
+        dst[...] = src
+    del arrs
 
     def host_step(a):
         t0 = time.perf_counter()
@@ -442,8 +446,6 @@ def run_gpu(args):
     barrier()
     e2e_ms = [host_step(a) * 1e3 for a in schedule()]
     e2e_t = reduce_max(sum(e2e_ms) * 1e-3, dist)
-    for a in (pos, vel, d1, d2):
-        M.unpin(a)
     e2e_val = job_value(world, Np, nst, e2e_t)
     # RSD multipoles P0/P2/P4 at z = 0 of that run's final state
     # (compute_RSD_powerspectrum, src/compute_pofk.c:403-512: y and z lines
@@ -453,6 +455,8 @@ def run_gpu(args):
     t0 = time.perf_counter()
     rsd = ctx.pofk_rsd(1.0)
     rsd_ms = (time.perf_counter() - t0) * 1e3
+    for a in (pos, vel, d1, d2):
+        M.host_free(a)
     full_check = None
     if rank == 0 and not args.no_cpu_baseline:
         full_check = fullsize_check(ctx, cfg, args.config, schedule)

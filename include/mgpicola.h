@@ -488,10 +488,15 @@ double mgp_kernel_ms(mgp_ctx *ctx, const char *name);
  * synchronisation. */
 int mgp_mark(mgp_ctx *ctx, int slot);
 /* Particle order of the deposit and the kick (no counterpart in the
- * reference): tiles != 0 (the default for single boxes) buckets the
- * particles by 16^3-cell tile of the mesh every step, deposits per tile in
- * shared memory and walks the kick in the same order; 0 keeps the lattice
- * order.  Both give the same results up to the order of float sums. */
+ * reference).  tiles = 1 (the default for single boxes): every step the
+ * particles are bucketed by 16^3-cell tile of the mesh and deposited per
+ * tile in shared memory, and every 4th step the particle arrays themselves
+ * are permuted into that order (with scale-independent growth), which keeps
+ * the kick's force gathers local as the particles cluster; entry points that
+ * hand particles to the caller restore the lattice order first.  tiles = n
+ * > 1: the permutation every n steps; -1: the tile deposit with the arrays
+ * kept in lattice order; 0: the deposit in lattice order.  All give the same
+ * results up to the order of float sums. */
 int mgp_set_particle_order(mgp_ctx *ctx, int tiles);
 /* With mgp_set_timing(ctx, n) for n > 1 the stage events of the last n
  * mgp_step calls are kept: milliseconds of stage `name` in step `step`
@@ -526,6 +531,12 @@ long long mgp_launch_count(mgp_ctx *ctx);
  * (cudaHostRegister / cudaHostUnregister). */
 int mgp_host_register(void *ptr, size_t bytes);
 int mgp_host_unregister(void *ptr);
+/* Page-locked host allocations (cudaMallocHost / cudaFreeHost) for the
+ * particle arrays of the host-buffer step.  Copies from them stayed at the
+ * link rate on a busy host, where copies from registered pageable memory
+ * (mgp_host_register) slowed down several-fold. */
+int mgp_host_alloc(void **ptr, size_t bytes);
+int mgp_host_free(void *ptr);
 
 #ifdef __cplusplus
 }

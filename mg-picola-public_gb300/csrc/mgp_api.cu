@@ -132,7 +132,11 @@ extern "C" double mgp_kernel_ms(mgp_ctx *c, const char *name) {
 
 extern "C" int mgp_set_particle_order(mgp_ctx *c, int tiles) {
   if (!c) return mgp_set_error(MGP_EINVAL, "null context");
-  c->tile_mode = tiles ? 1 : 0;
+  if (c->nbox != 1 && tiles) return mgp_set_error(MGP_EINVAL, "a batch keeps the lattice order");
+  MGP_CUDA(cudaSetDevice(c->device));
+  RET_IF(mgp_particles_canonical(c));
+  c->tile_mode = tiles != 0;
+  c->tile_resort = tiles > 1 ? tiles : (tiles == 1 ? MGP_TILE_RESORT : 0);
   return MGP_OK;
 }
 
@@ -339,10 +343,8 @@ static int validate(const mgp_params *p) {
   if (p->Nsample < 1 || p->Nsample > 2048) return mgp_set_error(MGP_EINVAL, "Nsample = %d out of range", p->Nsample);
   if (!(p->Box > 0)) return mgp_set_error(MGP_EINVAL, "Box must be positive");
   if (p->model < 0 || p->model > 4) return mgp_set_error(MGP_EINVAL, "unknown model %d", p->model);
-  if (p->scaledependent && (p->Nmesh % p->Nsample != 0 || p->Nsample % 2))
-    return mgp_set_error(MGP_EINVAL,
-                         "scale-dependent growth needs an even Nsample that divides Nmesh (Nmesh = %d, Nsample = %d)",
-                         p->Nmesh, p->Nsample);
+  if (p->scaledependent && p->Nsample % 2)
+    return mgp_set_error(MGP_EINVAL, "scale-dependent growth needs an even Nsample (Nsample = %d)", p->Nsample);
   if ((p->WhichSpectrum != 0) && (p->WhichTransfer != 0))
     return mgp_set_error(MGP_EINVAL, "can't run with both power spectrum and transfer function");
   if ((p->WhichSpectrum == 0) && (p->WhichTransfer == 0))
@@ -432,6 +434,7 @@ static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxe
   c->p = c->box_p[0];
   c->device = device;
   c->tile_mode = nbox == 1;
+  c->tile_resort = MGP_TILE_RESORT;
   char err[512] = "";
   int rc = mgp_cosmo_init_hooks(&c->cosmo, &c->box_p[0], hooks, err, sizeof(err));
   if (rc) {
@@ -715,6 +718,9 @@ extern "C" int mgp_displacement_fields(mgp_ctx *c) {
   if (!c) return mgp_set_error(MGP_EINVAL, "null context");
   if (c->nbox != 1) return mgp_set_error(MGP_ESTATE, "single-box call on a batch of %d boxes", c->nbox);
   MGP_CUDA(cudaSetDevice(c->device));
+  // the IC writes every particle array in lattice order
+  c->permuted = 0;
+  c->tile_age = 0;
   if (c->p.ReadParticlesFromFile) {
     // ReadFilesMakeDisplacementField (src/readICfromfile.c:533-699)
     double *pos = NULL;
@@ -733,6 +739,9 @@ extern "C" int mgp_displacement_fields_from_positions(mgp_ctx *c, const double *
   if (!c || (!pos && n)) return mgp_set_error(MGP_EINVAL, "null argument");
   if (c->nbox != 1) return mgp_set_error(MGP_ESTATE, "single-box call on a batch of %d boxes", c->nbox);
   MGP_CUDA(cudaSetDevice(c->device));
+  // the IC writes every particle array in lattice order
+  c->permuted = 0;
+  c->tile_age = 0;
   std::vector<double> u(3 * n);
   const double inv = 1.0 / c->p.Box;
   for (size_t q = 0; q < 3 * n; q++) {
@@ -912,11 +921,22 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   if (c->cosmo.nu) RET_IF(nu_prepare(c, A));
   // PtoMesh, src/auxPM.c:280-432
   const bool tiles = c->tile_mode && mgp_tile_side(N, c->np) > 0;
+  int identity = 0;
   if (tiles) {
-    // bucket the particles by cell tile (mgp_tiles.cu): the deposit and the
-    // kick of this step walk them in that order
+    // bucket the particles by cell tile (mgp_tiles.cu) for the deposit;
+    // every tile_resort steps the particle arrays themselves are permuted
+    // into that order, so that the kick's force gathers stay local as the
+    // particles cluster (scale-independent growth: the scale-dependent LPT
+    // fields are read at the lattice points)
     tstart(c, T_SORT);
     RET_IF(mgp_tiles_sort(c));
+    if (c->tile_resort > 0 && !c->sd && (!c->permuted || c->tile_age + 1 >= c->tile_resort)) {
+      RET_IF(mgp_tiles_permute(c));
+      identity = 1;
+      c->tile_age = 0;
+    } else {
+      c->tile_age++;
+    }
     tstop(c, T_SORT);
   }
   tstart(c, T_FILL);
@@ -925,7 +945,7 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   tstart(c, T_CIC);
   double wpar = pow((double)N / (double)c->Ns, 3);
   if (tiles)
-    RET_IF(mgp_cic_tiles(c, (float)wpar));
+    RET_IF(mgp_cic_tiles(c, (float)wpar, identity));
   else
     RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, c->p.Box, (float)wpar, c->rho, c->g.P, c->stream));
   tstop(c, T_CIC);
@@ -1031,11 +1051,12 @@ extern "C" int mgp_kick_drift(mgp_ctx *c, double AI, double AF, double A, double
   int nblk = mgp_ikd_blocks(c->np);
   const float *D1 = c->sd ? c->sd_slot[0] : c->D1, *D2 = c->sd ? c->sd_slot[1] : c->D2;
   tstart(c, T_IKD);
-  // the cell-tile order of the last deposit, where there is one (any
-  // permutation is correct; that one keeps the force gathers local)
-  const unsigned *order = c->tile_mode && c->tile_ready ? c->tile_order : NULL;
+  // particles in array order (walking them through the deposit's tile
+  // index order keeps the force gathers local but scatters the 72 bytes of
+  // particle data each one reads and writes, which measured 1.8x slower);
+  // with the arrays permuted into tile order, q gives the lattice points
   RET_IF(mgp_launch_ikd(c->frc, c->g.nreal, c->g.N, c->g.P, c->Ns, c->np, c->s, c->v, D1, D2, c->dstate,
-                        c->partials, nblk, &a, c->stream, 1, NULL, order));
+                        c->partials, nblk, &a, c->stream, 1, NULL, c->permuted ? c->q : NULL));
   tstop(c, T_IKD);
   if (do_drift) c->have_density = 0;
   return MGP_OK;
@@ -1105,6 +1126,7 @@ extern "C" int mgp_pofk_total(mgp_ctx *c, int cap, int *nbins, double *k, double
 extern "C" int mgp_pofk_rsd(mgp_ctx *c, double A, int cap, int *nbins, double *k, double *P0, double *P2, double *P4,
                             double *s0, double *s2, double *s4, double *n) {
   RET_IF(require_particles(c));
+  RET_IF(mgp_particles_canonical(c));  // lattice order for the caller's arrays
   const int nb = c->pk_nbins, N = c->g.N;
   if (nbins) *nbins = nb;
   if (cap < nb) return mgp_set_error(MGP_EINVAL, "RSD capacity %d < %d bins", cap, nb);
@@ -1191,6 +1213,7 @@ static int ensure_stage(mgp_ctx *c, int arrays = 2) {
 
 extern "C" int mgp_get_particles(mgp_ctx *c, float *pos, float *vel, float *D1, float *D2, size_t np) {
   RET_IF(require_particles(c));
+  RET_IF(mgp_particles_canonical(c));  // lattice order for the caller's arrays
   if ((long long)np != c->np) return mgp_set_error(MGP_EINVAL, "np = %zu, context holds %lld", np, c->np);
   RET_IF(ensure_stage(c));
   const size_t bytes = sizeof(float) * 3 * np;
@@ -1235,6 +1258,7 @@ static int reset_offsets(mgp_ctx *c, int pos_set, int vel_set, cudaStream_t st) 
 extern "C" int mgp_set_particles(mgp_ctx *c, const float *pos, const float *vel, const float *D1, const float *D2,
                                  size_t np) {
   RET_IF(require_particles(c));
+  RET_IF(mgp_particles_canonical(c));  // lattice order for the caller's arrays
   if ((long long)np != c->np) return mgp_set_error(MGP_EINVAL, "np = %zu, context holds %lld", np, c->np);
   RET_IF(ensure_stage(c));
   const size_t bytes = sizeof(float) * 3 * np;
@@ -1265,6 +1289,18 @@ extern "C" int mgp_host_register(void *ptr, size_t bytes) {
   return MGP_OK;
 }
 
+extern "C" int mgp_host_alloc(void **ptr, size_t bytes) {
+  if (!ptr) return mgp_set_error(MGP_EINVAL, "null argument");
+  *ptr = NULL;
+  MGP_CUDA(cudaMallocHost(ptr, bytes));
+  return MGP_OK;
+}
+
+extern "C" int mgp_host_free(void *ptr) {
+  if (ptr) MGP_CUDA(cudaFreeHost(ptr));
+  return MGP_OK;
+}
+
 extern "C" int mgp_host_unregister(void *ptr) {
   MGP_CUDA(cudaHostUnregister(ptr));
   return MGP_OK;
@@ -1278,6 +1314,7 @@ extern "C" int mgp_host_unregister(void *ptr) {
 extern "C" int mgp_step_host(mgp_ctx *c, double A, double AI, double AF, double AFF, float *pos, float *vel,
                              const float *D1, const float *D2, size_t np) {
   RET_IF(require_particles(c));
+  RET_IF(mgp_particles_canonical(c));  // lattice order for the caller's arrays
   if ((long long)np != c->np) return mgp_set_error(MGP_EINVAL, "np = %zu, context holds %lld", np, c->np);
   {
     if (!c->side) {

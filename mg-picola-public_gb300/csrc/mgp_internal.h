@@ -167,6 +167,14 @@ struct mgp_ctx {
   unsigned *tile_of, *tile_order, *tile_count, *tile_off, *tile_cursor, *tile_bsum;
   int tile_side, tile_n1, tile_ready;
   int tile_mode;            /* 1 (default): tile path where it applies; 0: particle order */
+  /* particle arrays held in cell-tile order (single box, scale-independent
+   * growth): every tile_resort steps the deposit's sort also permutes s, v,
+   * D1, D2 into tile order; q[p] is then the lattice point of slot p.  Entry
+   * points that read or write particles in lattice order first restore it
+   * (mgp_particles_canonical).  *_alt: the second buffers of the permutation */
+  unsigned *q, *q_alt;
+  float *s_alt, *v_alt, *D1_alt, *D2_alt;
+  int permuted, tile_age, tile_resort;
 
   /* user screening functions: the device copy of the step's table */
   float *scr_tab;
@@ -287,14 +295,20 @@ int mgp_launch_forces(const float *dk, const float *mgk, float mg_coupling, floa
 int mgp_launch_ikd(const float *frc, long long grid_floats, int N, long long P, int Ns, long long np,
                    float *s, float *v, const float *D1, const float *D2, mgp_dstate *dst,
                    double *partials, int nblocks, const mgp_kd_args *a, cudaStream_t st, int nbox = 1,
-                   const mgp_box_scalars *bs = NULL, const unsigned *order = NULL);
+                   const mgp_box_scalars *bs = NULL, const unsigned *qlat = NULL);
 int mgp_ikd_blocks(long long np);
-/* cell-tile order (mgp_tiles.cu) */
+/* cell-tile order (mgp_tiles.cu); the particle arrays are permuted into it
+ * every MGP_TILE_RESORT steps by default */
+#define MGP_TILE_RESORT 4
 int mgp_tile_side(int N, long long np);
 int mgp_tiles_alloc(mgp_ctx *c);
 void mgp_tiles_free(mgp_ctx *c);
 int mgp_tiles_sort(mgp_ctx *c);
-int mgp_cic_tiles(mgp_ctx *c, float wpar);
+int mgp_cic_tiles(mgp_ctx *c, float wpar, int identity);
+/* permute the particle arrays into the order of the last mgp_tiles_sort */
+int mgp_tiles_permute(mgp_ctx *c);
+/* lattice order of the particle arrays (no-op unless permuted) */
+int mgp_particles_canonical(mgp_ctx *c);
 int mgp_launch_nu_table(float *tab, int nrk, double kfac, double fac, const double *x, const double *val,
                         const double *dval, int nx, const double *den, cudaStream_t st);
 int mgp_launch_nu_add(float *dk, const float *dk0, int N, double cdmfac, const float *nufac, cudaStream_t st);

@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
     const float *__restrict__ frc, long long gf, int N, long long P, int Ns, long long np, float *__restrict__ s,
     float *__restrict__ v, const float *__restrict__ D1, const float *__restrict__ D2,
     const mgp_dstate *__restrict__ st, double *__restrict__ partials, mgp_kd_args a,
-    const mgp_box_scalars *__restrict__ bs, int ls, const unsigned *__restrict__ order) {
+    const mgp_box_scalars *__restrict__ bs, int ls, const unsigned *__restrict__ qlat) {
   __shared__ double sh[MGP_THREADS / 32];
   {
     // box blockIdx.y of a batch: force grids 3 gf apart, particle arrays 3 np
@@ -541,24 +541,24 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
   float accD[3] = {0.f, 0.f, 0.f}, accV[3] = {0.f, 0.f, 0.f};
   long long stride = (long long)gridDim.x * blockDim.x;
   const float inv_ns = 1.0f / (float)Ns;
-  for (long long jp = (long long)blockIdx.x * blockDim.x + threadIdx.x; jp < np; jp += stride) {
-    // particles in the given order (the cell-tile order of the step), else
-    // in lattice order
-    const long long p = order ? (long long)order[jp] : jp;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    // lattice point of the particle in slot p: qlat[p] when the arrays are
+    // held in cell-tile order, else p itself
+    const long long lat = qlat ? (long long)qlat[p] : p;
     int i, j, k;
     float sp[3] = {s[p], s[np + p], s[2 * np + p]};
     int ix, iy, iz;
     float DX, DY, DZ;
     if (P2) {
-      lattice_ijk_p2((unsigned)p, ls, i, j, k);
+      lattice_ijk_p2((unsigned)lat, ls, i, j, k);
       cell_frac_p2(i, sp[0], ox, N, ls, inv_ns, a.scale, ix, DX);
       cell_frac_p2(j, sp[1], oy, N, ls, inv_ns, a.scale, iy, DY);
       cell_frac_p2(k, sp[2], oz, N, ls, inv_ns, a.scale, iz, DZ);
     } else {
       if (np <= 0xffffffffLL)
-        lattice_ijk((unsigned)p, Ns, i, j, k);
+        lattice_ijk((unsigned)lat, Ns, i, j, k);
       else
-        lattice_ijk(p, Ns, i, j, k);
+        lattice_ijk(lat, Ns, i, j, k);
       cell_frac(i, sp[0], ox, N, Ns, a.scale, ix, DX);
       cell_frac(j, sp[1], oy, N, Ns, a.scale, iy, DY);
       cell_frac(k, sp[2], oz, N, Ns, a.scale, iz, DZ);
@@ -639,22 +639,22 @@ int mgp_ikd_blocks(long long np) { return blocks_for(np, 8); }
 int mgp_launch_ikd(const float *frc, long long gf, int N, long long P, int Ns, long long np, float *s, float *v,
                    const float *D1, const float *D2, mgp_dstate *dst, double *partials, int nblocks,
                    const mgp_kd_args *a, cudaStream_t st, int nbox, const mgp_box_scalars *bs,
-                   const unsigned *order) {
+                   const unsigned *qlat) {
   const dim3 g(nblocks, nbox);
   const int ls = lattice_log2(Ns);
   const bool p2 = ls >= 0 && np <= 0xffffffffLL;
   if (gf < (1LL << 31) && p2)
     k_interp_kick_drift<int, true><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a,
-                                                              bs, ls, order);
+                                                              bs, ls, qlat);
   else if (gf < (1LL << 31))
     k_interp_kick_drift<int, false><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a,
-                                                               bs, ls, order);
+                                                               bs, ls, qlat);
   else if (p2)
     k_interp_kick_drift<long long, true><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials,
-                                                                    *a, bs, ls, order);
+                                                                    *a, bs, ls, qlat);
   else
     k_interp_kick_drift<long long, false><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst,
-                                                                     partials, *a, bs, ls, order);
+                                                                     partials, *a, bs, ls, qlat);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   k_finalize_kd<<<nbox, MGP_THREADS, 0, st>>>(dst, partials, nblocks, 1.0 / (double)np, a->dda_omega, a->dyyy_d,

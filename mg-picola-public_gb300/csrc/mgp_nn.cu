@@ -1248,6 +1248,9 @@ extern "C" int mgp_closure_target_particles(mgp_closure *cl, mgp_ctx *fine, mgp_
   if (fine->np != coarse->np || fine->Ns != coarse->Ns || fine->p.Box != coarse->p.Box)
     return mgp_set_error(MGP_EINVAL, "fine and coarse contexts hold different particle sets");
   MGP_CUDA(cudaSetDevice(cl->device));
+  // both particle sets in lattice order (the sample pairs them by index)
+  NN_RET(mgp_particles_canonical(fine));
+  NN_RET(mgp_particles_canonical(coarse));
   MGP_CUDA(cudaStreamSynchronize(fine->stream));
   MGP_CUDA(cudaStreamSynchronize(coarse->stream));
   NN_RET(ensure_particles(cl, coarse->np));

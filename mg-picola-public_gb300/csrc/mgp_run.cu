@@ -105,6 +105,7 @@ static int out_buffers(mgp_ctx *c) {
 }
 
 static int output(mgp_ctx *c, double A, double z, int gadget) {
+  RET_IF(mgp_particles_canonical(c));  // snapshots list the particles in lattice order
   // RSD multipoles at output (src/main.c:875-880), not for the IC output
   int first_step = fabs(c->p.Init_Redshift - z) / c->p.Init_Redshift <= 1.0E-6;
   if (c->p.pofk_compute_rsd_pofk >= 1 && !first_step) RET_IF(write_rsd_now(c, A));

@@ -15,11 +15,9 @@
 //                   the mesh with one vector reduction per pair of cells
 //                   (about 1.7 L2 reduction sectors per particle instead of
 //                   ~4.3 for eight scalar reductions per particle);
-// and the fused interpolation + kick + drift walks the particles in the same
-// order, so the warps of a block gather forces from one compact region of the
-// three force grids.  Any permutation gives the same results (up to the
-// order of floating-point sums); the tile order only restores locality that
-// the Lagrangian order loses as the particles cluster.
+// Any order gives the same density (up to the order of floating-point
+// sums); the tile order restores the locality of the deposit that the
+// Lagrangian order loses as the particles cluster.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -33,18 +31,19 @@ constexpr int kScanItems = 16;                     // per thread in a scan block
 constexpr int kScanChunk = kThreads * kScanItems;  // elements per scan block
 
 // CIC base cell of particle p (the same arithmetic as k_cic), and its tile.
+// p is the array slot, lat the lattice point of the particle in it.
 template <bool P2>
-__device__ __forceinline__ void particle_cell(const float *__restrict__ s, long long np, long long p, int Ns, int ls,
-                                              float inv_ns, int N, float scale, float ox, float oy, float oz, int &ix,
-                                              int &iy, int &iz, float &DX, float &DY, float &DZ) {
+__device__ __forceinline__ void particle_cell(const float *__restrict__ s, long long np, long long p, unsigned lat,
+                                              int Ns, int ls, float inv_ns, int N, float scale, float ox, float oy,
+                                              float oz, int &ix, int &iy, int &iz, float &DX, float &DY, float &DZ) {
   int i, j, k;
   if (P2) {
-    lattice_ijk_p2((unsigned)p, ls, i, j, k);
+    lattice_ijk_p2(lat, ls, i, j, k);
     cell_frac_p2(i, s[p], ox, N, ls, inv_ns, scale, ix, DX);
     cell_frac_p2(j, s[np + p], oy, N, ls, inv_ns, scale, iy, DY);
     cell_frac_p2(k, s[2 * np + p], oz, N, ls, inv_ns, scale, iz, DZ);
   } else {
-    lattice_ijk((unsigned)p, Ns, i, j, k);
+    lattice_ijk(lat, Ns, i, j, k);
     cell_frac(i, s[p], ox, N, Ns, scale, ix, DX);
     cell_frac(j, s[np + p], oy, N, Ns, scale, iy, DY);
     cell_frac(k, s[2 * np + p], oz, N, Ns, scale, iz, DZ);
@@ -57,7 +56,8 @@ __device__ __forceinline__ void particle_cell(const float *__restrict__ s, long 
 template <bool P2>
 __global__ void __launch_bounds__(kThreads) k_tile_key(const float *__restrict__ s, const mgp_dstate *__restrict__ st,
                                                        long long np, int Ns, int ls, int N, float scale, int tshift,
-                                                       int ntile1, unsigned *__restrict__ tile_of,
+                                                       int ntile1, const unsigned *__restrict__ q,
+                                                       unsigned *__restrict__ tile_of,
                                                        unsigned *__restrict__ count) {
   const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
   const float inv_ns = 1.0f / (float)Ns;
@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(kThreads) k_tile_key(const float *__restrict__
     if (!on) continue;
     int ix, iy, iz;
     float DX, DY, DZ;
-    particle_cell<P2>(s, np, p, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY, DZ);
+    particle_cell<P2>(s, np, p, q ? q[p] : (unsigned)p, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY,
+                      DZ);
     const unsigned t = ((unsigned)(ix >> tshift) * (unsigned)ntile1 + (unsigned)(iy >> tshift)) * (unsigned)ntile1 +
                        (unsigned)(iz >> tshift);
     tile_of[p] = t;
@@ -191,7 +192,8 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
                                                         long long np, int Ns, int ls, int N, float scale, float wpar,
                                                         float *__restrict__ rho, long long P,
                                                         const unsigned *__restrict__ off,
-                                                        const unsigned *__restrict__ order, int ntile1) {
+                                                        const unsigned *__restrict__ order,
+                                                        const unsigned *__restrict__ q, int ntile1) {
   constexpr int BX = T + 1, BZ = T + 2, BOX = BX * BX * BZ;
   __shared__ float box[BOX];
   const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
@@ -205,10 +207,13 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
     for (int q = threadIdx.x; q < BOX; q += blockDim.x) box[q] = 0.0f;
     __syncthreads();
     for (unsigned j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-      const long long p = order[j];
+      // slot of the j-th particle of the tile order: order[j], or j itself
+      // once the arrays have been permuted into that order
+      const long long p = order ? (long long)order[j] : (long long)j;
       int ix, iy, iz;
       float DX, DY, DZ;
-      particle_cell<P2>(s, np, p, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY, DZ);
+      particle_cell<P2>(s, np, p, q ? q[p] : (unsigned)p, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY,
+                        DZ);
       const float TX = 1.0f - DX, TY = (1.0f - DY) * wpar, TZ = 1.0f - DZ;
       DY *= wpar;
       const int lx = ix - x0, ly = iy - y0, lz = iz - z0;
@@ -253,6 +258,50 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
   }
 }
 
+// Gather of the particle arrays into the tile order: slot j takes the
+// particle of slot order[j] (s, v, D1, D2: [3][np] each) and its lattice
+// point.  Reads come in runs of lattice neighbours, writes are coalesced.
+__global__ void __launch_bounds__(kThreads) k_permute(const unsigned *__restrict__ order, long long np,
+                                                      const float *__restrict__ s, const float *__restrict__ v,
+                                                      const float *__restrict__ D1, const float *__restrict__ D2,
+                                                      const unsigned *__restrict__ q, float *__restrict__ s2,
+                                                      float *__restrict__ v2, float *__restrict__ D12,
+                                                      float *__restrict__ D22, unsigned *__restrict__ q2) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < np; j += stride) {
+    const long long src = order[j];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const long long o = a * np;
+      s2[o + j] = s[o + src];
+      v2[o + j] = v[o + src];
+      D12[o + j] = D1[o + src];
+      D22[o + j] = D2[o + src];
+    }
+    q2[j] = q ? q[src] : (unsigned)src;
+  }
+}
+
+// Back to lattice order: the particle of slot j goes to slot q[j].
+__global__ void __launch_bounds__(kThreads) k_unpermute(long long np, const float *__restrict__ s,
+                                                        const float *__restrict__ v, const float *__restrict__ D1,
+                                                        const float *__restrict__ D2, const unsigned *__restrict__ q,
+                                                        float *__restrict__ s2, float *__restrict__ v2,
+                                                        float *__restrict__ D12, float *__restrict__ D22) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < np; j += stride) {
+    const long long dst = q[j];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const long long o = a * np;
+      s2[o + dst] = s[o + j];
+      v2[o + dst] = v[o + j];
+      D12[o + dst] = D1[o + j];
+      D22[o + dst] = D2[o + j];
+    }
+  }
+}
+
 }  // namespace
 
 // Tile side in cells for the tile path, or 0 when it does not apply (the
@@ -284,11 +333,60 @@ int mgp_tiles_alloc(mgp_ctx *c) {
 }
 
 void mgp_tiles_free(mgp_ctx *c) {
-  void *b[] = {c->tile_of, c->tile_order, c->tile_count, c->tile_off, c->tile_cursor, c->tile_bsum};
+  void *b[] = {c->tile_of, c->tile_order, c->tile_count, c->tile_off, c->tile_cursor, c->tile_bsum,
+               c->q, c->q_alt, c->s_alt, c->v_alt, c->D1_alt, c->D2_alt};
   for (void *x : b)
     if (x) cudaFree(x);
   c->tile_of = c->tile_order = c->tile_count = c->tile_off = c->tile_cursor = c->tile_bsum = NULL;
+  c->q = c->q_alt = NULL;
+  c->s_alt = c->v_alt = c->D1_alt = c->D2_alt = NULL;
   c->tile_ready = 0;
+  c->permuted = 0;
+}
+
+static void swap_arrays(mgp_ctx *c) {
+  float *t;
+  t = c->s; c->s = c->s_alt; c->s_alt = t;
+  t = c->v; c->v = c->v_alt; c->v_alt = t;
+  t = c->D1; c->D1 = c->D1_alt; c->D1_alt = t;
+  t = c->D2; c->D2 = c->D2_alt; c->D2_alt = t;
+}
+
+// Permute the particle arrays into the order of the last mgp_tiles_sort
+// (into the second buffers, then swap); q follows the particles.
+int mgp_tiles_permute(mgp_ctx *c) {
+  const size_t bytes = sizeof(float) * 3 * (size_t)c->np;
+  if (!c->s_alt) {
+    MGP_CUDA(cudaMalloc(&c->s_alt, bytes));
+    MGP_CUDA(cudaMalloc(&c->v_alt, bytes));
+    MGP_CUDA(cudaMalloc(&c->D1_alt, bytes));
+    MGP_CUDA(cudaMalloc(&c->D2_alt, bytes));
+    MGP_CUDA(cudaMalloc(&c->q, sizeof(unsigned) * (size_t)c->np));
+    MGP_CUDA(cudaMalloc(&c->q_alt, sizeof(unsigned) * (size_t)c->np));
+  }
+  k_permute<<<mgp_blocks_for(c->np, 8), kThreads, 0, c->stream>>>(c->tile_order, c->np, c->s, c->v, c->D1, c->D2,
+                                                                  c->permuted ? c->q : NULL, c->s_alt, c->v_alt,
+                                                                  c->D1_alt, c->D2_alt, c->q_alt);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  swap_arrays(c);
+  unsigned *t = c->q;
+  c->q = c->q_alt;
+  c->q_alt = t;
+  c->permuted = 1;
+  return MGP_OK;
+}
+
+int mgp_particles_canonical(mgp_ctx *c) {
+  if (!c->permuted) return MGP_OK;
+  k_unpermute<<<mgp_blocks_for(c->np, 8), kThreads, 0, c->stream>>>(c->np, c->s, c->v, c->D1, c->D2, c->q, c->s_alt,
+                                                                    c->v_alt, c->D1_alt, c->D2_alt);
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  swap_arrays(c);
+  c->permuted = 0;
+  c->tile_age = 0;
+  return MGP_OK;
 }
 
 // Bucket the particles of a single box by tile (their current positions).
@@ -301,13 +399,14 @@ int mgp_tiles_sort(mgp_ctx *c) {
   const float scale = (float)(N / c->p.Box);
   int tshift = 0;
   while ((1 << tshift) < T) tshift++;
+  const unsigned *qp = c->permuted ? c->q : NULL;
   MGP_CUDA(cudaMemsetAsync(c->tile_count, 0, sizeof(unsigned) * (size_t)ntiles, c->stream));
   const int nb = mgp_blocks_for(c->np, 8);
   if (ls >= 0)
-    k_tile_key<true><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, tshift, nt1,
+    k_tile_key<true><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, tshift, nt1, qp,
                                                      c->tile_of, c->tile_count);
   else
-    k_tile_key<false><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, tshift, nt1,
+    k_tile_key<false><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, tshift, nt1, qp,
                                                       c->tile_of, c->tile_count);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
@@ -329,24 +428,26 @@ int mgp_tiles_sort(mgp_ctx *c) {
   return MGP_OK;
 }
 
-// Tile deposit onto a mesh pre-set to -1 (after mgp_tiles_sort).
-int mgp_cic_tiles(mgp_ctx *c, float wpar) {
+// Tile deposit onto a mesh pre-set to -1 (after mgp_tiles_sort; identity:
+// the arrays were just permuted into the sort's order).
+int mgp_cic_tiles(mgp_ctx *c, float wpar, int identity) {
+  const unsigned *ord = identity ? NULL : c->tile_order, *qp = c->permuted ? c->q : NULL;
   const int N = c->g.N, Ns = c->Ns, T = c->tile_side, nt1 = c->tile_n1;
   const int ls = lattice_log2(Ns);
   const float scale = (float)(N / c->p.Box);
   const int nb = mgp_blocks_for((long long)nt1 * nt1 * nt1 * kThreads, 8);
   if (T == 16 && ls >= 0)
     k_cic_tiles<16, true><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                          c->g.P, c->tile_off, c->tile_order, nt1);
+                                                          c->g.P, c->tile_off, ord, qp, nt1);
   else if (T == 16)
     k_cic_tiles<16, false><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                           c->g.P, c->tile_off, c->tile_order, nt1);
+                                                           c->g.P, c->tile_off, ord, qp, nt1);
   else if (ls >= 0)
     k_cic_tiles<8, true><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                         c->g.P, c->tile_off, c->tile_order, nt1);
+                                                         c->g.P, c->tile_off, ord, qp, nt1);
   else
     k_cic_tiles<8, false><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                          c->g.P, c->tile_off, c->tile_order, nt1);
+                                                          c->g.P, c->tile_off, ord, qp, nt1);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;

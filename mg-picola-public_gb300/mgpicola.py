@@ -23,7 +23,7 @@ EXPORTS = [
     "mgp_displacement_fields", "mgp_get_displacements", "mgp_kick_drift", "mgp_step", "mgp_run", "mgp_pofk",
     "mgp_pofk_total", "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
     "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_mark", "mgp_mark_ms", "mgp_kernel_ms_step", "mgp_set_particle_order", "mgp_launch_count",
-    "mgp_host_register", "mgp_host_unregister", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
+    "mgp_host_register", "mgp_host_unregister", "mgp_host_alloc", "mgp_host_free", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
     "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_batch_set_tuning",
     "mgp_batch_get_tuning", "mgp_batch_autotune", "mgp_output_stats", "mgp_displacement_fields_from_positions",
@@ -179,6 +179,8 @@ def lib():
         L.mgp_kernel_ms_step.restype = C.c_double
         L.mgp_mark.argtypes = [vp, C.c_int]
         L.mgp_set_particle_order.argtypes = [vp, C.c_int]
+        L.mgp_host_alloc.argtypes = [C.POINTER(vp), C.c_size_t]
+        L.mgp_host_free.argtypes = [vp]
         L.mgp_mark_ms.argtypes = [vp, C.c_int, C.c_int]
         L.mgp_mark_ms.restype = C.c_double
         L.mgp_launch_count.argtypes = [vp]
@@ -315,6 +317,27 @@ def pofk_noalloc(d_deltak, Nmesh, Nsample, Box, nbins, bintype, subtract_shotnoi
                                   cap, C.byref(nb), _dptr(k), _dptr(pk), _dptr(km), _dptr(n), stream))
     m = nb.value
     return k[:m], pk[:m], km[:m], n[:m]
+
+
+def host_array(shape):
+    """A float32 numpy array in page-locked host memory (mgp_host_alloc);
+    release it with host_free."""
+    n = int(np.prod(shape))
+    ptr = C.c_void_p()
+    _check(lib().mgp_host_alloc(C.byref(ptr), max(4 * n, 4)))
+    buf = (C.c_float * max(n, 1)).from_address(ptr.value)
+    a = np.ctypeslib.as_array(buf)[:n].reshape(shape)
+    _HOST[id(a)] = ptr.value
+    return a
+
+
+_HOST = {}
+
+
+def host_free(a):
+    ptr = _HOST.pop(id(a), None)
+    if ptr:
+        _check(lib().mgp_host_free(ptr))
 
 
 def pin(arr):
@@ -461,9 +484,11 @@ class Context:
         return lib().mgp_kernel_ms_step(self.h, name.encode(), step)
 
     def set_particle_order(self, tiles):
-        """Cell-tile particle order for the deposit and the kick (default
-        on for single boxes), or the lattice order."""
-        _check(lib().mgp_set_particle_order(self.h, 1 if tiles else 0))
+        """Cell-tile particle order (mgp_set_particle_order): True/1 the
+        default (tile deposit, arrays permuted into tile order every 4
+        steps), n > 1 permutation every n steps, -1 tile deposit only,
+        False/0 lattice order."""
+        _check(lib().mgp_set_particle_order(self.h, int(tiles)))
 
     def mark(self, slot):
         """Record event `slot` (0..3) on the context's stream."""

@@ -99,24 +99,39 @@ def test_tile_deposit_matches_lattice_order_deposit(N, Ns, spread):
     rho = []
     with M.Context(p) as ctx:
         ctx.set_particles(pos, vel, d1, d2)
-        for tiles in (True, False):
+        # tile deposit after permuting the arrays, through the index order,
+        # and in lattice order
+        for tiles in (1, -1, 0):
             ctx.set_particle_order(tiles)
             ctx.get_displacements(0.5)
             rho.append(ctx.grid(0)[:, :, :N].astype(np.float64))
+        # the permuted arrays come back in lattice order
+        ctx.set_particle_order(1)
+        ctx.get_displacements(0.5)
+        back = ctx.get_particles()
     ref = O.cic(pos.astype(np.float64), N, Ns, box)[:, :, :N]
     scale = np.abs(ref).max()
-    assert np.abs(rho[0] - rho[1]).max() < 2e-6 * scale
+    for r in rho[:2]:
+        assert np.abs(r - rho[2]).max() < 2e-6 * scale
     assert np.abs(rho[0] - ref).max() < 2e-5 * scale
     assert abs(rho[0].mean()) < 1e-6
+    dx = np.abs(back[0] - pos)
+    assert np.minimum(dx, box - dx).max() < 1e-4 * box / Ns
+    np.testing.assert_array_equal(back[1], vel)
+    np.testing.assert_array_equal(back[2], d1)
+    np.testing.assert_array_equal(back[3], d2)
 
 
-def test_tile_order_run_matches_lattice_order_run():
-    """Five KDK steps with the cell-tile particle order (deposit and kick)
-    against the lattice order: the same run up to float summation order."""
+@pytest.mark.parametrize("tiles", [1, 2, -1])
+def test_tile_order_run_matches_lattice_order_run(tiles):
+    """Five KDK steps with the cell-tile particle order (tile deposit; the
+    arrays permuted into tile order every 4 or 2 steps, or kept in lattice
+    order) against the lattice order: the same run up to float summation
+    order."""
     N, Ns, box, nsteps = 64, 32, 128.0, 5
     p = params(N, Ns, box)
     out = []
-    for tiles in (True, False):
+    for tiles in (tiles, 0):
         with M.Context(p) as ctx:
             ctx.set_particle_order(tiles)
             ctx.displacement_fields()
