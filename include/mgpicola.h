@@ -490,14 +490,21 @@ int mgp_mark(mgp_ctx *ctx, int slot);
 /* Particle order of the deposit and the kick (no counterpart in the
  * reference).  tiles = 1 (the default for single boxes): every step the
  * particles are bucketed by 16^3-cell tile of the mesh and deposited per
- * tile in shared memory, and every 4th step the particle arrays themselves
- * are permuted into that order (with scale-independent growth), which keeps
- * the kick's force gathers local as the particles cluster; entry points that
- * hand particles to the caller restore the lattice order first.  tiles = n
- * > 1: the permutation every n steps; -1: the tile deposit with the arrays
- * kept in lattice order; 0: the deposit in lattice order.  All give the same
- * results up to the order of float sums. */
+ * tile in shared memory; the particle arrays stay in lattice order.
+ * tiles = n > 1: the particle arrays themselves are also permuted into tile
+ * order every n steps (with scale-independent growth; -1: every 4 steps),
+ * and entry points that hand particles to the caller restore the lattice
+ * order first; this kept the kick's force gathers local late in a run but
+ * cost more than it saved over a whole run.  tiles = 0: the deposit in
+ * lattice order.  All give the same results up to the order of float sums. */
 int mgp_set_particle_order(mgp_ctx *ctx, int tiles);
+/* Form of the fused interpolation + kick + drift under the tile order (no
+ * counterpart in the reference): 1 one pass in array order; 2 two passes,
+ * the forces interpolated in the deposit's tile order (local gathers) and
+ * the kick and drift in array order; 0 (default) each step takes the form
+ * that recent CUDA-event timings of both found faster.  Same results up to
+ * the order of float sums. */
+int mgp_set_kick_passes(mgp_ctx *ctx, int passes);
 /* With mgp_set_timing(ctx, n) for n > 1 the stage events of the last n
  * mgp_step calls are kept: milliseconds of stage `name` in step `step`
  * (counted from that mgp_set_timing call), -1 if not kept or not timed. */
