@@ -833,13 +833,20 @@ static int fifth_force(mgp_ctx *c, double A, int filtered, int *mg_kind, float *
       RET_IF(mgp_launch_smooth(c->dk, c->mg1, N, p->smoothing_filter, (float)kR1, (float)(1.0 / pow((double)N, 3)),
                                c->stream));
     MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+    // Without massive neutrinos delta(k) is the transform of rho itself, so
+    // the screening pass writes delta + source, rho (1 + coupling S), and the
+    // force pass reads that one spectrum (mg_kind 4) instead of delta(k) and
+    // the source (the sum P3D + P3D_mg of auxPM.c:450-455, formed in real
+    // space; the transform is linear)
+    const int fold = !c->cosmo.nu && !mgp_cosmo_user_screening(&c->cosmo, 1);
     if (mgp_cosmo_user_screening(&c->cosmo, 1))
       RET_IF(user_screening(c, A, 1, coupling_d, nr));
     else
       RET_IF(mgp_launch_screen_density(c->rho, c->mg1, nr, (float)coupling_d,
-                                       (float)mgp_dgp_screen_prefactor(&c->cosmo, A), c->stream));
+                                       (float)mgp_dgp_screen_prefactor(&c->cosmo, A), c->stream, 1, NULL,
+                                       fold ? 1.0f : 0.0f));
     MGP_CUFFT(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
-    *mg_kind = 2;
+    *mg_kind = fold ? 4 : 2;
   } else if (p->model == MGP_MODEL_BRANSDICKE) {
     // ComputeFifthForce_TimeDepGeffModels (src/mg.h:127-137): the source
     // is delta(k) Geff/G(a), applied inside the force pass
@@ -991,7 +998,10 @@ static int fields_from_density(mgp_ctx *c, double A) {
   tstop(c, T_MG);
   // Forces, src/auxPM.c:437-555
   tstart(c, T_FORCES);
-  RET_IF(mgp_launch_forces(c->dk, c->rho, coupling, mass2, mg_kind, N, c->p.Box, c->frc, c->g.nreal, c->stream));
+  if (mg_kind == 4)  // rho holds delta + the fifth-force source
+    RET_IF(mgp_launch_forces(c->rho, NULL, 0.f, 0.f, 0, N, c->p.Box, c->frc, c->g.nreal, c->stream));
+  else
+    RET_IF(mgp_launch_forces(c->dk, c->rho, coupling, mass2, mg_kind, N, c->p.Box, c->frc, c->g.nreal, c->stream));
   tstop(c, T_FORCES);
   if (c->closure) {  // learned residual force, added to the force transforms
     tstart(c, T_NN);

@@ -335,7 +335,7 @@ int mgp_launch_smooth(const float *dk, float *out, int N, int filter, float kR_p
 int mgp_launch_screen_potential(float *rho, const float *phi, long long n, float phicrit, cudaStream_t st,
                                 int nbox = 1, const mgp_box_scalars *bs = NULL);
 int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float coupling, float pref,
-                              cudaStream_t st, int nbox = 1, const mgp_box_scalars *bs = NULL);
+                              cudaStream_t st, int nbox = 1, const mgp_box_scalars *bs = NULL, float base = 0.0f);
 int mgp_launch_scale_complex(float *c, long long ncomplex, float factor, cudaStream_t st);
 /* a user's screening function from its per-step table (mgp_model_hooks) */
 #define MGP_SCREEN_TABLE 16384

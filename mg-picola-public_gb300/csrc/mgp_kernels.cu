@@ -836,8 +836,10 @@ __device__ __forceinline__ float screen_den(float dsm, float pref) {
   float fac = pref * (1.0f + dsm);
   return fac < 1e-5f ? 1.0f : 2.0f * (sqrtf(1.0f + fac) - 1.0f) / fac;
 }
+// base 1: rho *= 1 + coupling * S, i.e. the density plus its fifth-force
+// source in one field (the force pass then reads one spectrum).
 __global__ void k_screen_density(float *__restrict__ rho, const float *__restrict__ dsm, long long n, float coupling,
-                                 float pref, const mgp_box_scalars *__restrict__ bs) {
+                                 float pref, const mgp_box_scalars *__restrict__ bs, float base) {
   // box blockIdx.y: grids n floats apart
   rho += blockIdx.y * n;
   dsm += blockIdx.y * n;
@@ -849,19 +851,20 @@ __global__ void k_screen_density(float *__restrict__ rho, const float *__restric
   long long n4 = n >> 2;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
     float4 r = reinterpret_cast<float4 *>(rho)[i], d = reinterpret_cast<const float4 *>(dsm)[i];
-    r.x *= coupling * screen_den(d.x, pref);
-    r.y *= coupling * screen_den(d.y, pref);
-    r.z *= coupling * screen_den(d.z, pref);
-    r.w *= coupling * screen_den(d.w, pref);
+    r.x *= fmaf(coupling, screen_den(d.x, pref), base);
+    r.y *= fmaf(coupling, screen_den(d.y, pref), base);
+    r.z *= fmaf(coupling, screen_den(d.z, pref), base);
+    r.w *= fmaf(coupling, screen_den(d.w, pref), base);
     reinterpret_cast<float4 *>(rho)[i] = r;
   }
   for (long long i = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    rho[i] *= coupling * screen_den(dsm[i], pref);
+    rho[i] *= fmaf(coupling, screen_den(dsm[i], pref), base);
 }
 
 int mgp_launch_screen_density(float *rho, const float *dsm, long long n, float coupling, float pref, cudaStream_t st,
-                              int nbox, const mgp_box_scalars *bs) {
-  k_screen_density<<<grid_boxes(n, g_budget_grid, nbox), MGP_THREADS, 0, st>>>(rho, dsm, n, coupling, pref, bs);
+                              int nbox, const mgp_box_scalars *bs, float base) {
+  k_screen_density<<<grid_boxes(n, g_budget_grid, nbox), MGP_THREADS, 0, st>>>(rho, dsm, n, coupling, pref, bs,
+                                                                                base);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
