@@ -498,13 +498,6 @@ int mgp_mark(mgp_ctx *ctx, int slot);
  * cost more than it saved over a whole run.  tiles = 0: the deposit in
  * lattice order.  All give the same results up to the order of float sums. */
 int mgp_set_particle_order(mgp_ctx *ctx, int tiles);
-/* Form of the fused interpolation + kick + drift under the tile order (no
- * counterpart in the reference): 1 one pass in array order; 2 two passes,
- * the forces interpolated in the deposit's tile order (local gathers) and
- * the kick and drift in array order; 0 (default) each step takes the form
- * that recent CUDA-event timings of both found faster.  Same results up to
- * the order of float sums. */
-int mgp_set_kick_passes(mgp_ctx *ctx, int passes);
 /* With mgp_set_timing(ctx, n) for n > 1 the stage events of the last n
  * mgp_step calls are kept: milliseconds of stage `name` in step `step`
  * (counted from that mgp_set_timing call), -1 if not kept or not timed. */

@@ -130,23 +130,13 @@ extern "C" double mgp_kernel_ms(mgp_ctx *c, const char *name) {
   return -1.0;
 }
 
-extern "C" int mgp_set_kick_passes(mgp_ctx *c, int passes) {
-  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
-  if (passes < 0 || passes > 2) return mgp_set_error(MGP_EINVAL, "passes = %d (0 adaptive, 1 fused, 2 two)", passes);
-  c->kd_passes = passes;
-  c->kd_pending = 0;
-  c->kd_ms[0] = c->kd_ms[1] = -1.0f;
-  return MGP_OK;
-}
-
 extern "C" int mgp_set_particle_order(mgp_ctx *c, int tiles) {
   if (!c) return mgp_set_error(MGP_EINVAL, "null context");
   if (c->nbox != 1 && tiles) return mgp_set_error(MGP_EINVAL, "a batch keeps the lattice order");
   MGP_CUDA(cudaSetDevice(c->device));
   RET_IF(mgp_particles_canonical(c));
   c->tile_mode = tiles != 0;
-  c->tile_resort = tiles > 1 ? tiles : 0;
-  if (tiles == -1) c->tile_resort = MGP_TILE_RESORT;
+  c->tile_resort = tiles > 1 ? tiles : (tiles == -1 ? MGP_TILE_RESORT : 0);
   return MGP_OK;
 }
 
@@ -395,9 +385,6 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
     if (c->ev_chunk[k]) cudaEventDestroy(c->ev_chunk[k]);
   free_history(c);
   mgp_tiles_free(c);
-  if (c->kd_pre) cudaFree(c->kd_pre);
-  for (int q = 0; q < 2; q++)
-    if (c->kd_ev[q]) cudaEventDestroy(c->kd_ev[q]);
   for (int t = 0; t < MGP_NTIMERS; t++) {
     if (t < 4 && c->ev_mark[t]) cudaEventDestroy(c->ev_mark[t]);
     if (c->ev[t][0]) cudaEventDestroy(c->ev[t][0]);
@@ -1074,50 +1061,13 @@ extern "C" int mgp_kick_drift(mgp_ctx *c, double AI, double AF, double A, double
   int nblk = mgp_ikd_blocks(c->np);
   const float *D1 = c->sd ? c->sd_slot[0] : c->D1, *D2 = c->sd ? c->sd_slot[1] : c->D2;
   tstart(c, T_IKD);
-  // The fused pass walks the particles in array order (with the arrays
-  // permuted into tile order, q gives the lattice points).  Walking all of it
-  // through the deposit's tile index order keeps the force gathers local but
-  // scatters the 72 bytes of particle data each particle reads and writes
-  // (measured 1.8x slower); the two-pass form scatters only the position
-  // read and one float4 write.  Early in a run the lattice order is already
-  // local and the fused pass wins; as the particles cluster the two-pass form
-  // does, so by default each step takes the faster by recent event timings.
-  int form = 0;
-  if (c->tile_mode && c->tile_ready && !c->permuted && c->nbox == 1) {
-    if (c->kd_passes == 2) {
-      form = 1;
-    } else if (c->kd_passes == 0) {
-      if (!c->kd_ev[0]) {
-        MGP_CUDA(cudaEventCreate(&c->kd_ev[0]));
-        MGP_CUDA(cudaEventCreate(&c->kd_ev[1]));
-        c->kd_ms[0] = c->kd_ms[1] = -1.0f;
-      }
-      if (c->kd_pending && cudaEventQuery(c->kd_ev[1]) == cudaSuccess) {
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, c->kd_ev[0], c->kd_ev[1]) == cudaSuccess) c->kd_ms[c->kd_last] = ms;
-        c->kd_pending = 0;
-      }
-      if (c->kd_ms[0] < 0.f) form = 0;
-      else if (c->kd_ms[1] < 0.f) form = 1;
-      else {
-        form = c->kd_ms[1] < c->kd_ms[0] ? 1 : 0;
-        if (c->kd_count % 8 == 7) form ^= 1;  // re-time the slower form now and then
-      }
-    }
-  }
-  if (form == 1 && !c->kd_pre) MGP_CUDA(cudaMalloc(&c->kd_pre, sizeof(float4) * (size_t)c->np));
-  const bool probe = c->kd_passes == 0 && c->kd_ev[0] && !c->kd_pending && c->tile_mode && c->tile_ready &&
-                     !c->permuted;
-  if (probe) MGP_CUDA(cudaEventRecord(c->kd_ev[0], c->stream));
+  // particles in array order (walking them through the deposit's tile
+  // index order keeps the force gathers local but scatters the 72 bytes of
+  // particle data each one reads and writes, which measured 1.8x slower;
+  // splitting off the force interpolation in tile order, 1.3x slower);
+  // with the arrays permuted into tile order, q gives the lattice points
   RET_IF(mgp_launch_ikd(c->frc, c->g.nreal, c->g.N, c->g.P, c->Ns, c->np, c->s, c->v, D1, D2, c->dstate,
-                        c->partials, nblk, &a, c->stream, 1, NULL, c->permuted ? c->q : NULL,
-                        form ? c->tile_order : NULL, form ? c->kd_pre : NULL));
-  if (probe) {
-    MGP_CUDA(cudaEventRecord(c->kd_ev[1], c->stream));
-    c->kd_pending = 1;
-    c->kd_last = form;
-  }
-  c->kd_count++;
+                        c->partials, nblk, &a, c->stream, 1, NULL, c->permuted ? c->q : NULL));
   tstop(c, T_IKD);
   if (do_drift) c->have_density = 0;
   return MGP_OK;

@@ -175,14 +175,6 @@ struct mgp_ctx {
   unsigned *q, *q_alt;
   float *s_alt, *v_alt, *D1_alt, *D2_alt;
   int permuted, tile_age, tile_resort;
-  /* kick: fused pass (0) or two passes (1: forces in the deposit's tile
-   * order into kd_pre, then kick and drift in lattice order).  kd_passes
-   * 0 chooses per step from event timings of both forms (kd_ms, re-probing
-   * the slower one every 8th step); 1 or 2 fixes the form. */
-  float4 *kd_pre;
-  int kd_passes, kd_last, kd_pending, kd_count;
-  float kd_ms[2];
-  cudaEvent_t kd_ev[2];
 
   /* user screening functions: the device copy of the step's table */
   float *scr_tab;
@@ -303,11 +295,10 @@ int mgp_launch_forces(const float *dk, const float *mgk, float mg_coupling, floa
 int mgp_launch_ikd(const float *frc, long long grid_floats, int N, long long P, int Ns, long long np,
                    float *s, float *v, const float *D1, const float *D2, mgp_dstate *dst,
                    double *partials, int nblocks, const mgp_kd_args *a, cudaStream_t st, int nbox = 1,
-                   const mgp_box_scalars *bs = NULL, const unsigned *qlat = NULL,
-                   const unsigned *order = NULL, float4 *pre = NULL);
+                   const mgp_box_scalars *bs = NULL, const unsigned *qlat = NULL);
 int mgp_ikd_blocks(long long np);
 /* cell-tile order (mgp_tiles.cu); with mgp_set_particle_order(ctx, n > 1)
- * the particle arrays are also permuted into it every n steps (1 selects
+ * the particle arrays are also permuted into it every n steps (-1 selects
  * MGP_TILE_RESORT); by default they stay in lattice order */
 #define MGP_TILE_RESORT 4
 int mgp_tile_side(int N, long long np);

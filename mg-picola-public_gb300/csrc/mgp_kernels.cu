@@ -511,19 +511,12 @@ __device__ __forceinline__ double block_sum_d(double v, double *sh) {
 // floats (N <= 1024), which keeps the 24-point gather in fewer registers.
 // P2: Ns = 2^ls, lattice and cell index arithmetic by shifts (identical
 // results).
-// MODE 0: the fused pass.  The two-pass form splits it for the cell-tile
-// order: MODE 1 interpolates the forces of the particles in the deposit's
-// tile order (order[]; the gathers of a block stay in one tile's region of
-// the force grids) into pre[p] = (disp, 0) and sums disp; MODE 2 then kicks
-// and drifts in lattice order from pre[] and sums the velocities.  Both write
-// their halves of the same per-block partials.
-template <typename IDX, bool P2, int MODE>
+template <typename IDX, bool P2>
 __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
     const float *__restrict__ frc, long long gf, int N, long long P, int Ns, long long np, float *__restrict__ s,
     float *__restrict__ v, const float *__restrict__ D1, const float *__restrict__ D2,
     const mgp_dstate *__restrict__ st, double *__restrict__ partials, mgp_kd_args a,
-    const mgp_box_scalars *__restrict__ bs, int ls, const unsigned *__restrict__ qlat,
-    const unsigned *__restrict__ order, float4 *__restrict__ pre) {
+    const mgp_box_scalars *__restrict__ bs, int ls, const unsigned *__restrict__ qlat) {
   __shared__ double sh[MGP_THREADS / 32];
   {
     // box blockIdx.y of a batch: force grids 3 gf apart, particle arrays 3 np
@@ -548,21 +541,12 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
   float accD[3] = {0.f, 0.f, 0.f}, accV[3] = {0.f, 0.f, 0.f};
   long long stride = (long long)gridDim.x * blockDim.x;
   const float inv_ns = 1.0f / (float)Ns;
-  for (long long jp = (long long)blockIdx.x * blockDim.x + threadIdx.x; jp < np; jp += stride) {
-    const long long p = MODE == 1 ? (long long)order[jp] : jp;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
     // lattice point of the particle in slot p: qlat[p] when the arrays are
     // held in cell-tile order, else p itself
     const long long lat = qlat ? (long long)qlat[p] : p;
-    int i = 0, j = 0, k = 0;
+    int i, j, k;
     float sp[3] = {s[p], s[np + p], s[2 * np + p]};
-    float disp[3];
-    if (MODE == 2) {
-      const float4 d4 = pre[p];
-      disp[0] = d4.x;
-      disp[1] = d4.y;
-      disp[2] = d4.z;
-      if (a.lpt_pitch != Ns) lattice_ijk((unsigned)lat, Ns, i, j, k);
-    } else {
     int ix, iy, iz;
     float DX, DY, DZ;
     if (P2) {
@@ -587,19 +571,13 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
     const IDX o100 = x1 + y0 + z0, o101 = x1 + y0 + z1, o110 = x1 + y1 + z0, o111 = x1 + y1 + z1;
     const float w000 = TX * TY * TZ, w001 = TX * TY * DZ, w010 = TX * DY * TZ, w011 = TX * DY * DZ;
     const float w100 = DX * TY * TZ, w101 = DX * TY * DZ, w110 = DX * DY * TZ, w111 = DX * DY * DZ;
+    float disp[3];
     const float *Fa[3] = {F0, F1, F2};
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
       const float *F = Fa[ax];
       disp[ax] = __ldg(F + o000) * w000 + __ldg(F + o001) * w001 + __ldg(F + o010) * w010 + __ldg(F + o011) * w011 +
                  __ldg(F + o100) * w100 + __ldg(F + o101) * w101 + __ldg(F + o110) * w110 + __ldg(F + o111) * w111;
-    }
-    }
-    if (MODE == 1) {
-      pre[p] = make_float4(disp[0], disp[1], disp[2], 0.0f);
-#pragma unroll
-      for (int ax = 0; ax < 3; ax++) accD[ax] += disp[ax];
-      continue;
     }
     // D1/D2 offsets: the particle index itself for particle arrays
     // (pitch Ns), the lattice point in the row-padded slot grids otherwise
@@ -611,20 +589,16 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
       float vn = v[o] + a.kick_disp * disp[ax] + a.kick_d1 * d1 + a.kick_d2 * d2;
       v[o] = vn;
       if (a.do_drift) s[o] = sp[ax] + vn * a.dyyy + a.dD1 * d1 + a.dD2 * d2;
-      if (MODE == 0) accD[ax] += disp[ax];
+      accD[ax] += disp[ax];
       accV[ax] += vn;
     }
   }
 #pragma unroll
   for (int q = 0; q < 3; q++) {
-    if (MODE != 2) {
-      double t = block_sum_d((double)accD[q], sh);
-      if (threadIdx.x == 0) partials[(long long)blockIdx.x * 6 + q] = t;
-    }
-    if (MODE != 1) {
-      double t = block_sum_d((double)accV[q], sh);
-      if (threadIdx.x == 0) partials[(long long)blockIdx.x * 6 + 3 + q] = t;
-    }
+    double t = block_sum_d((double)accD[q], sh);
+    if (threadIdx.x == 0) partials[(long long)blockIdx.x * 6 + q] = t;
+    t = block_sum_d((double)accV[q], sh);
+    if (threadIdx.x == 0) partials[(long long)blockIdx.x * 6 + 3 + q] = t;
   }
 }
 
@@ -662,41 +636,25 @@ __global__ void k_finalize_kd(mgp_dstate *st, const double *__restrict__ partial
 
 int mgp_ikd_blocks(long long np) { return blocks_for(np, 8); }
 
-template <int MODE>
-static void launch_ikd_mode(dim3 g, cudaStream_t st, const float *frc, long long gf, int N, long long P, int Ns,
-                            long long np, float *s, float *v, const float *D1, const float *D2, mgp_dstate *dst,
-                            double *partials, const mgp_kd_args *a, const mgp_box_scalars *bs, const unsigned *qlat,
-                            const unsigned *order, float4 *pre) {
-  const int ls = lattice_log2(Ns);
-  const bool p2 = ls >= 0 && np <= 0xffffffffLL;
-  if (gf < (1LL << 31) && p2)
-    k_interp_kick_drift<int, true, MODE><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials,
-                                                                    *a, bs, ls, qlat, order, pre);
-  else if (gf < (1LL << 31))
-    k_interp_kick_drift<int, false, MODE><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst,
-                                                                     partials, *a, bs, ls, qlat, order, pre);
-  else if (p2)
-    k_interp_kick_drift<long long, true, MODE><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst,
-                                                                          partials, *a, bs, ls, qlat, order, pre);
-  else
-    k_interp_kick_drift<long long, false, MODE><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst,
-                                                                           partials, *a, bs, ls, qlat, order, pre);
-}
-
 int mgp_launch_ikd(const float *frc, long long gf, int N, long long P, int Ns, long long np, float *s, float *v,
                    const float *D1, const float *D2, mgp_dstate *dst, double *partials, int nblocks,
                    const mgp_kd_args *a, cudaStream_t st, int nbox, const mgp_box_scalars *bs,
-                   const unsigned *qlat, const unsigned *order, float4 *pre) {
+                   const unsigned *qlat) {
   const dim3 g(nblocks, nbox);
-  if (order && pre && nbox == 1) {
-    // two passes: forces in the tile order, then kick and drift
-    launch_ikd_mode<1>(g, st, frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, a, bs, qlat, order, pre);
-    MGP_CHECK_LAUNCH();
-    g_kernel_launches++;
-    launch_ikd_mode<2>(g, st, frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, a, bs, qlat, order, pre);
-  } else {
-    launch_ikd_mode<0>(g, st, frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, a, bs, qlat, NULL, NULL);
-  }
+  const int ls = lattice_log2(Ns);
+  const bool p2 = ls >= 0 && np <= 0xffffffffLL;
+  if (gf < (1LL << 31) && p2)
+    k_interp_kick_drift<int, true><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a,
+                                                              bs, ls, qlat);
+  else if (gf < (1LL << 31))
+    k_interp_kick_drift<int, false><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials, *a,
+                                                               bs, ls, qlat);
+  else if (p2)
+    k_interp_kick_drift<long long, true><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst, partials,
+                                                                    *a, bs, ls, qlat);
+  else
+    k_interp_kick_drift<long long, false><<<g, MGP_THREADS, 0, st>>>(frc, gf, N, P, Ns, np, s, v, D1, D2, dst,
+                                                                     partials, *a, bs, ls, qlat);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   k_finalize_kd<<<nbox, MGP_THREADS, 0, st>>>(dst, partials, nblocks, 1.0 / (double)np, a->dda_omega, a->dyyy_d,

@@ -22,7 +22,7 @@ EXPORTS = [
     "mgp_destroy", "mgp_last_error",
     "mgp_displacement_fields", "mgp_get_displacements", "mgp_kick_drift", "mgp_step", "mgp_run", "mgp_pofk",
     "mgp_pofk_total", "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
-    "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_mark", "mgp_mark_ms", "mgp_kernel_ms_step", "mgp_set_particle_order", "mgp_set_kick_passes", "mgp_launch_count",
+    "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_mark", "mgp_mark_ms", "mgp_kernel_ms_step", "mgp_set_particle_order", "mgp_launch_count",
     "mgp_host_register", "mgp_host_unregister", "mgp_host_alloc", "mgp_host_free", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
     "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_batch_set_tuning",
@@ -179,7 +179,6 @@ def lib():
         L.mgp_kernel_ms_step.restype = C.c_double
         L.mgp_mark.argtypes = [vp, C.c_int]
         L.mgp_set_particle_order.argtypes = [vp, C.c_int]
-        L.mgp_set_kick_passes.argtypes = [vp, C.c_int]
         L.mgp_host_alloc.argtypes = [C.POINTER(vp), C.c_size_t]
         L.mgp_host_free.argtypes = [vp]
         L.mgp_mark_ms.argtypes = [vp, C.c_int, C.c_int]
@@ -490,11 +489,6 @@ class Context:
         also permuted into tile order every n steps (-1: every 4), False/0
         the deposit in lattice order."""
         _check(lib().mgp_set_particle_order(self.h, int(tiles)))
-
-    def set_kick_passes(self, passes):
-        """0 adaptive (default), 1 fused kick pass, 2 two passes (forces in
-        tile order, then kick and drift)."""
-        _check(lib().mgp_set_kick_passes(self.h, passes))
 
     def mark(self, slot):
         """Record event `slot` (0..3) on the context's stream."""

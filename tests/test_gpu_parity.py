@@ -154,33 +154,6 @@ def test_tile_order_run_matches_lattice_order_run(tiles):
     assert rel_rms(vel0, vel1) < 1e-5
 
 
-def test_two_pass_kick_matches_fused_kick():
-    """The kick as two passes (forces interpolated in the deposit's tile
-    order into a float4 array, then kick and drift) and as the adaptive
-    choice, against the fused pass over five KDK steps."""
-    N, Ns, box, nsteps = 64, 32, 128.0, 5
-    p = params(N, Ns, box)
-    out = []
-    for passes in (2, 0, 1):
-        with M.Context(p) as ctx:
-            ctx.set_kick_passes(passes)
-            ctx.displacement_fields()
-            A, AI = 0.05, 0.05
-            da = (1.0 - A) / nsteps
-            for _ in range(nsteps):
-                ctx.step(A, AI, A + 0.5 * da, A + da)
-                A, AI = A + da, A + 0.5 * da
-            ctx.get_displacements(A)
-            out.append((ctx.pofk()[1], ctx.get_particles()))
-    pk_ref, (pos_ref, vel_ref, _, _) = out[2]
-    for pk, (pos, vel, _, _) in out[:2]:
-        assert np.max(np.abs(pk[1:] / pk_ref[1:] - 1)) < 1e-5
-        dx = np.abs(pos - pos_ref)
-        dx = np.minimum(dx, box - dx)
-        assert np.sqrt(np.mean(dx ** 2)) < 1e-5 * box / Ns
-        assert rel_rms(vel, vel_ref) < 1e-5
-
-
 @pytest.mark.parametrize("bintype,nbins,kmin,kmax", [(0, 16, 0.0, 0.0), (1, 12, 0.05, 1.5), (0, 40, 0.1, 0.9)])
 def test_pofk_matches_oracle(bintype, nbins, kmin, kmax):
     N, Ns, box = 32, 16, 64.0
