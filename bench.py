@@ -317,10 +317,11 @@ def algorithmic_bytes(N, Np, kernel):
 
 
 # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
-# nDGP step at 256^3 particles / 512^3 mesh, one launch each from a steady step.  Every term of
-# these kernels scales with the particle count or the cell count, which grow together between
-# the configurations (Nmesh = 2 Nsample), so the figure is scaled by the cell count.
-TRAFFIC_256_512 = {"interp_kick_drift": 3.404e9, "forces": 2.655e9, "cic": 1.466e9, "pofk": 1.040e9}
+# nDGP step at 256^3 particles / 512^3 mesh, one launch each at step 46 of the 50-step run
+# (profiles/deposit_and_kick_late_ndgp_256_512.md; the deposit is the tile deposit).  Every
+# term of these kernels scales with the particle count or the cell count, which grow together
+# between the configurations (Nmesh = 2 Nsample), so the figure is scaled by the cell count.
+TRAFFIC_256_512 = {"interp_kick_drift": 6.307e9, "cic": 1.420e9}
 
 
 def measured_traffic(N, Np, kernel):
@@ -475,8 +476,8 @@ def run_gpu(args):
     traffic = measured_traffic(N, Np, dom)
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at 256^3 particles / "
-                              "512^3 mesh, scaled by particles and cells",
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at step 46 of "
+                              "the 50-step run at 256^3 particles / 512^3 mesh, scaled by particles and cells",
             "algorithmic_bytes_per_launch": abytes, "mean_launch_ms": round(own[dom], 4),
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
     if closure is not None:
