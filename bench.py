@@ -402,17 +402,26 @@ def run_gpu(args):
         if dist is not None:
             dist.barrier()
 
+    warm_ms = 0.0
     for _ in range(args.warmup):
-        run()
+        warm_ms = run()[0]
+    # per-stage events cost ~50 event records per KDK step on the host: with
+    # steps of a few ms that is noise, but a launch-bound step of ~0.3 ms
+    # would be slowed by them, so short steps take their stage times from one
+    # extra run after the timed region instead
+    stages_in_timed = warm_ms / nst >= 2.0
     barrier()
     run_ms, launches, per_step = [], 0, []
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
-            ms, nl, st = run(timed=True)
+            ms, nl, st = run(timed=stages_in_timed)
             run_ms.append(ms)
             launches += nl
-            per_step.append(st)
+            if st is not None:
+                per_step.append(st)
     barrier()
+    if not per_step:
+        per_step.append(run(timed=True)[2])
     elapsed = reduce_max(sum(run_ms) * 1e-3, dist)
     ms_per_run = elapsed / args.steps * 1e3
     value = job_value(world, Np, args.steps * nst, elapsed)
@@ -510,6 +519,8 @@ def run_gpu(args):
                                 "min": round(float(np.min(e2e_ms)), 2)}},
         "gpu_launches": int(launches),
         "stage_ms_per_kdk_step": {k: round(v, 4) for k, v in stage_ms.items()},
+        "stage_timing": "per-step CUDA events in the timed runs" if stages_in_timed else
+                        "per-step CUDA events in one extra run after the timed region (steps < 2 ms)",
         "stage_ms_by_decile": deciles,
         "run_ms": [round(x, 2) for x in run_ms],
         "rsd_multipoles": {"ms": round(rsd_ms, 3), "bins": int(len(rsd[0])), "a": 1.0,

@@ -40,7 +40,7 @@ static const char *k_timer_names[MGP_NTIMERS] = {"cic",    "r2c",  "pofk",      
                                                    "c2r",    "interp_kick_drift", "step", "lpt_fields", "closure",
                                                    "closure_conv", "fill", "sort"};
 
-static void tstart(mgp_ctx *c, int t) {
+void mgp_tstart(mgp_ctx *c, int t) {
   if (c->timing) {
     cudaEventRecord(c->ev[t][0], c->stream);
     if (c->hev) {
@@ -49,7 +49,10 @@ static void tstart(mgp_ctx *c, int t) {
     }
   }
 }
-static void tstop(mgp_ctx *c, int t) {
+void mgp_tstop(mgp_ctx *c, int t);
+static void tstart(mgp_ctx *c, int t) { mgp_tstart(c, t); }
+static void tstop(mgp_ctx *c, int t) { mgp_tstop(c, t); }
+void mgp_tstop(mgp_ctx *c, int t) {
   if (c->timing) {
     cudaEventRecord(c->ev[t][1], c->stream);
     c->timed[t] = 1;

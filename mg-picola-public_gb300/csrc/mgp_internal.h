@@ -198,6 +198,9 @@ struct mgp_ctx {
 };
 
 enum { T_CIC = 0, T_R2C, T_POFK, T_MG, T_FORCES, T_C2R, T_IKD, T_MISC, T_SD, T_NN, T_NNCONV, T_FILL, T_SORT };
+/* stage timer events of a context (current step and, when kept, its history) */
+void mgp_tstart(mgp_ctx *c, int t);
+void mgp_tstop(mgp_ctx *c, int t);
 
 /* error plumbing (C linkage: also called from the C sources) */
 #ifdef __cplusplus

@@ -1451,17 +1451,14 @@ int mgp_closure_apply(mgp_closure *cl, mgp_ctx *c, double A) {
   cl->stream = c->stream;
   int rc = ensure_hp(cl);
   if (rc == MGP_OK) rc = closure_features(cl, c, A);
-  if (c->timing) cudaEventRecord(c->ev[T_NNCONV][0], c->stream);  // the four convolutions
+  mgp_tstart(c, T_NNCONV);  // the four convolutions
   for (int l = 0; l < NN_LAYERS - 1 && rc == MGP_OK; l++)
     rc = conv_fwd(cl, cl->act[l], cl->w16[l], cl->b32[l], NULL, 0, cl->act[l + 1], NULL, NULL, 0, 0, 0.f);
   const long long gf = (long long)cl->N * cl->N * cl->P;
   if (rc == MGP_OK)
     rc = conv_fwd(cl, cl->act[NN_LAYERS - 1], cl->w16[NN_LAYERS - 1], cl->b32[NN_LAYERS - 1], NULL, 3, NULL, NULL,
                   cl->ugrid, gf, cl->P, 0.f);
-  if (c->timing) {
-    cudaEventRecord(c->ev[T_NNCONV][1], c->stream);
-    c->timed[T_NNCONV] = 1;
-  }
+  mgp_tstop(c, T_NNCONV);
   if (rc == MGP_OK && cufftSetStream(cl->plan_r2c, c->stream) != CUFFT_SUCCESS)
     rc = mgp_set_error(MGP_ECUFFT, "closure transform stream");
   for (int q = 0; q < 3 && rc == MGP_OK; q++)
