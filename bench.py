@@ -190,6 +190,7 @@ def run_batch(args, cfg, rank=0, world=1, dist=None):
     tuned_ms = batch.autotune(nst)  # launch budgets picked by timing, before the timed region
     tune_s = time.perf_counter() - tune_t0
     tuning = batch.tuning()
+    deposit_tiles = batch.deposit_tiles()
     for _ in range(args.warmup):
         batch.run(nst)
     launches = batch.graph_kernels()
@@ -232,6 +233,8 @@ def run_batch(args, cfg, rank=0, world=1, dist=None):
                    "steps_per_run": nst, "pofk_every_step": True, "pofk_bins": cfg["nbins"],
                    "launch_budgets": {"tuned": tuning, "default": default_tuning,
                                       "order": "blocks/SM: CIC deposit, grid passes, kick, P(k) binning",
+                                      "deposit_tiles": deposit_tiles,
+                                      "deposit_tiles_meaning": "0 lattice-order deposit, 8/16 tile side in cells",
                                       "autotune_s": round(tune_s, 2), "graph_ms_default": round(default_ms, 3),
                                       "graph_ms_tuned": round(tuned_ms, 3)},
                    "l2": "working set %.1f GB > L2" % (B * (6 * 4 * N * N * 2 * (N // 2 + 1) + 48 * Np) / 1e9)},
@@ -311,17 +314,19 @@ def algorithmic_bytes(N, Np, kernel):
         "cic": 12 * Np + 4 * N ** 3,                 # read s, write the mesh once
         "pofk": 8 * ncomplex,                         # read delta(k)
         "forces": 2 * 8 * ncomplex + 3 * 8 * ncomplex,  # read delta, MG source; write 3 complex grids
-        "interp_kick_drift": 12 * N ** 3 + 72 * Np,   # force grids once; s,v,D1,D2 in, s,v out
+        # force grids once; s,v,D1,D2 in, s,v out (the tile kick also moves the order, q and
+        # D1, D2 in tile order: 108 Np by design, counted as overhead, not as work)
+        "interp_kick_drift": 12 * N ** 3 + 72 * Np,
         "mg": 8 * ncomplex + 4 * nreal + 8 * nreal,   # smoothing pass + screening pass (excl. FFTs)
     }[kernel]
 
 
 # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
 # nDGP step at 256^3 particles / 512^3 mesh, one launch each at step 46 of the 50-step run
-# (profiles/deposit_and_kick_late_ndgp_256_512.md; the deposit is the tile deposit).  Every
-# term of these kernels scales with the particle count or the cell count, which grow together
+# (profiles/deposit_and_kick_late_ndgp_256_512.md; tile deposit and tile kick).  Every term
+# of these kernels scales with the particle count or the cell count, which grow together
 # between the configurations (Nmesh = 2 Nsample), so the figure is scaled by the cell count.
-TRAFFIC_256_512 = {"interp_kick_drift": 6.307e9, "cic": 1.420e9}
+TRAFFIC_256_512 = {"interp_kick_drift": 5.908e9, "cic": 1.364e9}
 
 
 def measured_traffic(N, Np, kernel):

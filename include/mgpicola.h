@@ -399,6 +399,17 @@ int mgp_batch_graph_kernels(mgp_ctx *ctx);
  * set (its graph time in *best_ms). */
 int mgp_batch_set_tuning(mgp_ctx *ctx, const int tune[4]);
 int mgp_batch_get_tuning(mgp_ctx *ctx, int tune[4]);
+/* Deposit form of a batch: 0 (default) one thread per particle in lattice
+ * order; 8 or 16: every step all boxes' particles are bucketed by the
+ * side^3-cell tile of their CIC base cell (a counting sort inside the
+ * graph) and each tile is summed in shared memory before one float2
+ * reduction per pair of mesh cells.  side must divide Nmesh.  The density
+ * agrees up to the order of float sums; the next run captures a new graph.
+ * get returns the side (or a negative error code). */
+int mgp_batch_set_deposit_tiles(mgp_ctx *ctx, int side);
+int mgp_batch_get_deposit_tiles(mgp_ctx *ctx);
+/* The autotuner also picks the deposit form (after the grid budget, before
+ * the deposit budget), timing each side that applies. */
 int mgp_batch_autotune(mgp_ctx *ctx, int nsteps, double z_final, double *best_ms);
 
 /* Learned force closure (no counterpart in the reference): a 3D CNN on the
@@ -488,15 +499,17 @@ double mgp_kernel_ms(mgp_ctx *ctx, const char *name);
  * synchronisation. */
 int mgp_mark(mgp_ctx *ctx, int slot);
 /* Particle order of the deposit and the kick (no counterpart in the
- * reference).  tiles = 1 (the default for single boxes): every step the
- * particles are bucketed by 16^3-cell tile of the mesh and deposited per
- * tile in shared memory; the particle arrays stay in lattice order.
- * tiles = n > 1: the particle arrays themselves are also permuted into tile
- * order every n steps (with scale-independent growth; -1: every 4 steps),
- * and entry points that hand particles to the caller restore the lattice
- * order first; this kept the kick's force gathers local late in a run but
- * cost more than it saved over a whole run.  tiles = 0: the deposit in
- * lattice order.  All give the same results up to the order of float sums. */
+ * reference).  Every step the particles are bucketed by the 16^3-cell (or
+ * 8^3) tile of the mesh holding their CIC base cell and deposited per tile
+ * in shared memory (tiles = 1 or 2).  tiles = 2 (the default for single
+ * boxes): the kick also runs per tile -- the three force grids over the
+ * tile staged in shared memory -- and writes the particles back in the
+ * tile order, so the arrays follow the particles (with scale-independent
+ * growth; the scale-dependent LPT fields keep the array-order kick); entry
+ * points that hand particles to the caller, or take them, restore the
+ * lattice order first.  tiles = 1: the arrays stay in lattice order and the
+ * kick walks them in that order.  tiles = 0: deposit and kick in lattice
+ * order.  All give the same results up to the order of float sums. */
 int mgp_set_particle_order(mgp_ctx *ctx, int tiles);
 /* With mgp_set_timing(ctx, n) for n > 1 the stage events of the last n
  * mgp_step calls are kept: milliseconds of stage `name` in step `step`

@@ -137,9 +137,10 @@ extern "C" int mgp_set_particle_order(mgp_ctx *c, int tiles) {
   if (!c) return mgp_set_error(MGP_EINVAL, "null context");
   if (c->nbox != 1 && tiles) return mgp_set_error(MGP_EINVAL, "a batch keeps the lattice order");
   MGP_CUDA(cudaSetDevice(c->device));
+  if (tiles < 0 || tiles > 2) return mgp_set_error(MGP_EINVAL, "particle order %d (0, 1 or 2)", tiles);
   RET_IF(mgp_particles_canonical(c));
   c->tile_mode = tiles != 0;
-  c->tile_resort = tiles > 1 ? tiles : (tiles == -1 ? MGP_TILE_RESORT : 0);
+  c->tile_kick = tiles == 2;
   return MGP_OK;
 }
 
@@ -437,7 +438,7 @@ static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxe
   c->p = c->box_p[0];
   c->device = device;
   c->tile_mode = nbox == 1;
-  c->tile_resort = 0;
+  c->tile_kick = nbox == 1;
   char err[512] = "";
   int rc = mgp_cosmo_init_hooks(&c->cosmo, &c->box_p[0], hooks, err, sizeof(err));
   if (rc) {
@@ -723,7 +724,7 @@ extern "C" int mgp_displacement_fields(mgp_ctx *c) {
   MGP_CUDA(cudaSetDevice(c->device));
   // the IC writes every particle array in lattice order
   c->permuted = 0;
-  c->tile_age = 0;
+  c->tile_ready = 0;
   if (c->p.ReadParticlesFromFile) {
     // ReadFilesMakeDisplacementField (src/readICfromfile.c:533-699)
     double *pos = NULL;
@@ -744,7 +745,7 @@ extern "C" int mgp_displacement_fields_from_positions(mgp_ctx *c, const double *
   MGP_CUDA(cudaSetDevice(c->device));
   // the IC writes every particle array in lattice order
   c->permuted = 0;
-  c->tile_age = 0;
+  c->tile_ready = 0;
   std::vector<double> u(3 * n);
   const double inv = 1.0 / c->p.Box;
   for (size_t q = 0; q < 3 * n; q++) {
@@ -931,22 +932,11 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   if (c->cosmo.nu) RET_IF(nu_prepare(c, A));
   // PtoMesh, src/auxPM.c:280-432
   const bool tiles = c->tile_mode && mgp_tile_side(N, c->np) > 0;
-  int identity = 0;
   if (tiles) {
-    // bucket the particles by cell tile (mgp_tiles.cu) for the deposit;
-    // every tile_resort steps the particle arrays themselves are permuted
-    // into that order, so that the kick's force gathers stay local as the
-    // particles cluster (scale-independent growth: the scale-dependent LPT
-    // fields are read at the lattice points)
+    // bucket the particles by cell tile (mgp_tiles.cu) for the deposit and
+    // the kick of this step
     tstart(c, T_SORT);
-    RET_IF(mgp_tiles_sort(c));
-    if (c->tile_resort > 0 && !c->sd && (!c->permuted || c->tile_age + 1 >= c->tile_resort)) {
-      RET_IF(mgp_tiles_permute(c));
-      identity = 1;
-      c->tile_age = 0;
-    } else {
-      c->tile_age++;
-    }
+    RET_IF(mgp_tiles_sort(c, mgp_tile_side(N, c->np)));
     tstop(c, T_SORT);
   }
   tstart(c, T_FILL);
@@ -955,7 +945,7 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
   tstart(c, T_CIC);
   double wpar = pow((double)N / (double)c->Ns, 3);
   if (tiles)
-    RET_IF(mgp_cic_tiles(c, (float)wpar, identity));
+    RET_IF(mgp_cic_tiles(c, (float)wpar));
   else
     RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, c->p.Box, (float)wpar, c->rho, c->g.P, c->stream));
   tstop(c, T_CIC);
@@ -1064,13 +1054,18 @@ extern "C" int mgp_kick_drift(mgp_ctx *c, double AI, double AF, double A, double
   int nblk = mgp_ikd_blocks(c->np);
   const float *D1 = c->sd ? c->sd_slot[0] : c->D1, *D2 = c->sd ? c->sd_slot[1] : c->D2;
   tstart(c, T_IKD);
-  // particles in array order (walking them through the deposit's tile
-  // index order keeps the force gathers local but scatters the 72 bytes of
-  // particle data each one reads and writes, which measured 1.8x slower;
-  // splitting off the force interpolation in tile order, 1.3x slower);
-  // with the arrays permuted into tile order, q gives the lattice points
-  RET_IF(mgp_launch_ikd(c->frc, c->g.nreal, c->g.N, c->g.P, c->Ns, c->np, c->s, c->v, D1, D2, c->dstate,
-                        c->partials, nblk, &a, c->stream, 1, NULL, c->permuted ? c->q : NULL));
+  if (c->tile_kick && c->tile_ready && !c->sd) {
+    // per cell tile of this step's deposit sort, forces staged in shared
+    // memory; the particle arrays are rewritten in the tile order
+    RET_IF(mgp_ikd_tiles(c, &a, &nblk));
+    RET_IF(mgp_launch_finalize_kd(c->dstate, c->partials, nblk, c->np, a.dda_omega, a.dyyy_d, a.do_drift,
+                                  c->stream));
+  } else {
+    // particles in array order; with the arrays in tile order, q gives the
+    // lattice points
+    RET_IF(mgp_launch_ikd(c->frc, c->g.nreal, c->g.N, c->g.P, c->Ns, c->np, c->s, c->v, D1, D2, c->dstate,
+                          c->partials, nblk, &a, c->stream, 1, NULL, c->permuted ? c->q : NULL));
+  }
   tstop(c, T_IKD);
   if (do_drift) c->have_density = 0;
   return MGP_OK;
@@ -1507,9 +1502,13 @@ static int batch_step_launch(mgp_ctx *c, const batch_step &q, const mgp_box_scal
   const cufftHandle r2c_ip = B > 1 ? c->plan_r2c_ip_b : c->plan_r2c_ip;
   const cufftHandle c2r = B > 1 ? c->plan_c2r_b : c->plan_c2r_1;
   const cufftHandle c2r_frc = B > 1 ? c->plan_c2r_frc_b : c->plan_c2r_1;
-  RET_IF(mgp_launch_fill(c->rho, gf * B, -1.0f, c->stream));
   const double wpar = pow((double)N / (double)c->Ns, 3);
-  RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, p->Box, (float)wpar, c->rho, c->g.P, c->stream, B, gf));
+  if (c->batch_tile) RET_IF(mgp_tiles_sort(c, c->batch_tile));  // all boxes' particles by tile
+  RET_IF(mgp_launch_fill(c->rho, gf * B, -1.0f, c->stream));
+  if (c->batch_tile)
+    RET_IF(mgp_cic_tiles(c, (float)wpar, c->tune[0]));
+  else
+    RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, p->Box, (float)wpar, c->rho, c->g.P, c->stream, B, gf));
   MGP_CUFFT(cufftExecR2C(r2c_oop, (cufftReal *)c->rho, (cufftComplex *)c->dk));
   const int fused = p->pofk_compute_every_step ? mg_filter_kind(p) : 0;
   const double n3 = pow((double)N, 3);
@@ -1586,6 +1585,7 @@ static int batch_build_graph(mgp_ctx *c, int nsteps, double zf) {
   c->pk_blocks = pk_blocks_for(c, c->tune[3]);
   if (c->pk_blocks > c->pk_blocks_cap) c->pk_blocks = c->pk_blocks_cap;
   mgp_set_launch_budget(c->tune[0], c->tune[1]);
+  if (c->batch_tile) RET_IF(mgp_tiles_alloc(c, c->batch_tile));  // no allocation inside the capture
   MGP_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   const long long k0 = g_kernel_launches;
   int rc = MGP_OK;
@@ -1618,7 +1618,10 @@ extern "C" int mgp_batch_run(mgp_ctx *c, int nsteps, double z_final) {
     MGP_CUDA(cudaEventCreate(&c->bev[1]));
   }
   if (c->sd) return mgp_set_error(MGP_EINVAL, "batch runs use scale-independent growth");
-  // 2LPT ICs of every box (not captured: host-side seed tables)
+  // 2LPT ICs of every box (not captured: host-side seed tables), written
+  // in lattice order
+  c->permuted = 0;
+  c->tile_ready = 0;
   MGP_CUDA(cudaEventRecord(c->bev[0], c->stream));
   for (int b = 0; b < c->nbox; b++) RET_IF(ic_box(c, b));
   MGP_CUDA(cudaEventRecord(c->bev[1], c->stream));
@@ -1656,22 +1659,61 @@ extern "C" int mgp_batch_get_tuning(mgp_ctx *c, int *tune) {
   return MGP_OK;
 }
 
-// Autotuner: coordinate descent over the four budgets (grid passes first,
-// then deposit, kick and P(k)), each over {1, 2, 4, 8, 16, 32} blocks per SM
-// (P(k): {1, 2, 4, 8, 16}); every candidate is timed by one mgp_batch_run of
-// nsteps (fresh ICs, a newly captured graph, the graph timed with CUDA events)
-// and the fastest is kept.  *best_ms receives the graph time of the result.
+// Deposit form of a batch: 0 (default) one thread per particle in lattice
+// order, eight global float reductions each; 8 or 16: every step all boxes'
+// particles are bucketed by the side^3-cell tile of their CIC base cell and
+// each tile is summed in shared memory, then added to the mesh with one
+// float2 reduction per pair of cells.  The density is the same up to the
+// order of float sums; the next mgp_batch_run captures a new graph.
+extern "C" int mgp_batch_set_deposit_tiles(mgp_ctx *c, int side) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  if (side) RET_IF(mgp_tiles_check(c, side));
+  c->batch_tile = side;
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = NULL;
+  c->graph = NULL;
+  return MGP_OK;
+}
+
+extern "C" int mgp_batch_get_deposit_tiles(mgp_ctx *c) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  return c->batch_tile;
+}
+
+// Autotuner: coordinate descent over the deposit form and the four budgets
+// (grid passes first, then the deposit form {lattice order, 8^3 tiles, 16^3
+// tiles}, the deposit budget, kick and P(k)), each budget over {1, 2, 4, 8,
+// 16, 32} blocks per SM (P(k): {1, 2, 4, 8, 16}); every candidate is timed by
+// one mgp_batch_run of nsteps (fresh ICs, a newly captured graph, the graph
+// timed with CUDA events) and the fastest is kept.  *best_ms receives the
+// graph time of the result.
 extern "C" int mgp_batch_autotune(mgp_ctx *c, int nsteps, double z_final, double *best_ms) {
   if (!c) return mgp_set_error(MGP_EINVAL, "null context");
   static const int cand[6] = {1, 2, 4, 8, 16, 32};
-  static const int order[4] = {1, 0, 2, 3};
+  static const int order[5] = {1, -1, 0, 2, 3};  // -1: the deposit form
+  static const int sides[3] = {0, 8, 16};
   int best[4];
   for (int q = 0; q < 4; q++) best[q] = c->tune[q];
   RET_IF(mgp_batch_set_tuning(c, best));
   RET_IF(mgp_batch_run(c, nsteps, z_final));
   double best_t = c->batch_ms;
-  for (int oi = 0; oi < 4; oi++) {
+  for (int oi = 0; oi < 5; oi++) {
     const int q = order[oi];
+    if (q < 0) {
+      int best_side = c->batch_tile;
+      for (int side : sides) {
+        if (side == best_side || (side && mgp_tiles_check(c, side) != MGP_OK)) continue;
+        RET_IF(mgp_batch_set_deposit_tiles(c, side));
+        RET_IF(mgp_batch_run(c, nsteps, z_final));
+        if (c->batch_ms < best_t) {
+          best_t = c->batch_ms;
+          best_side = side;
+        }
+      }
+      RET_IF(mgp_batch_set_deposit_tiles(c, best_side));
+      continue;
+    }
     for (int ci = 0; ci < (q == 3 ? 5 : 6); ci++) {
       if (cand[ci] == best[q]) continue;
       int trial[4] = {best[0], best[1], best[2], best[3]};

@@ -166,15 +166,18 @@ struct mgp_ctx {
    * scatter cursors, scan block totals */
   unsigned *tile_of, *tile_order, *tile_count, *tile_off, *tile_cursor, *tile_bsum;
   int tile_side, tile_n1, tile_ready;
-  int tile_mode;            /* 1 (default): tile path where it applies; 0: particle order */
+  long long tile_cap;       /* tiles the count/offset arrays hold */
+  int batch_tile;           /* batch deposit: tile side (8, 16) or 0 for the lattice-order deposit */
+  int tile_mode;            /* 1 (default): tile deposit where it applies; 0: particle order */
   /* particle arrays held in cell-tile order (single box, scale-independent
-   * growth): every tile_resort steps the deposit's sort also permutes s, v,
-   * D1, D2 into tile order; q[p] is then the lattice point of slot p.  Entry
-   * points that read or write particles in lattice order first restore it
-   * (mgp_particles_canonical).  *_alt: the second buffers of the permutation */
+   * growth): with tile_kick the kick of every step reads the particles in
+   * the deposit's tile order and writes s, v, D1, D2 in that order (into
+   * the *_alt buffers, then swapped); q[p] is then the lattice point of
+   * slot p.  Entry points that read or write particles in lattice order
+   * first restore it (mgp_particles_canonical). */
   unsigned *q, *q_alt;
   float *s_alt, *v_alt, *D1_alt, *D2_alt;
-  int permuted, tile_age, tile_resort;
+  int permuted, tile_kick;
 
   /* user screening functions: the device copy of the step's table */
   float *scr_tab;
@@ -300,17 +303,16 @@ int mgp_launch_ikd(const float *frc, long long grid_floats, int N, long long P, 
                    double *partials, int nblocks, const mgp_kd_args *a, cudaStream_t st, int nbox = 1,
                    const mgp_box_scalars *bs = NULL, const unsigned *qlat = NULL);
 int mgp_ikd_blocks(long long np);
-/* cell-tile order (mgp_tiles.cu); with mgp_set_particle_order(ctx, n > 1)
- * the particle arrays are also permuted into it every n steps (-1 selects
- * MGP_TILE_RESORT); by default they stay in lattice order */
-#define MGP_TILE_RESORT 4
+/* cell-tile order (mgp_tiles.cu) */
 int mgp_tile_side(int N, long long np);
-int mgp_tiles_alloc(mgp_ctx *c);
+int mgp_tiles_check(const mgp_ctx *c, int T);
+int mgp_tiles_alloc(mgp_ctx *c, int T);
 void mgp_tiles_free(mgp_ctx *c);
-int mgp_tiles_sort(mgp_ctx *c);
-int mgp_cic_tiles(mgp_ctx *c, float wpar, int identity);
-/* permute the particle arrays into the order of the last mgp_tiles_sort */
-int mgp_tiles_permute(mgp_ctx *c);
+int mgp_tiles_sort(mgp_ctx *c, int T);
+int mgp_cic_tiles(mgp_ctx *c, float wpar, int per_sm = 0);
+/* kick + drift in the order of the last mgp_tiles_sort, the particle
+ * arrays rewritten in that order */
+int mgp_ikd_tiles(mgp_ctx *c, const mgp_kd_args *a, int *nblocks_out);
 /* lattice order of the particle arrays (no-op unless permuted) */
 int mgp_particles_canonical(mgp_ctx *c);
 int mgp_launch_nu_table(float *tab, int nrk, double kfac, double fac, const double *x, const double *val,

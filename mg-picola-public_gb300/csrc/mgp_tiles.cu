@@ -15,11 +15,25 @@
 //                   the mesh with one vector reduction per pair of cells
 //                   (about 1.7 L2 reduction sectors per particle instead of
 //                   ~4.3 for eight scalar reductions per particle);
-// Any order gives the same density (up to the order of floating-point
-// sums); the tile order restores the locality of the deposit that the
+//   k_ikd_tiles     MtoParticles + Kick + Drift (src/auxPM.c:560-644,
+//                   src/main.c:688-787) per tile: the block copies the three
+//                   force grids over the tile and its +1 halo into shared
+//                   memory, interpolates its particles' forces there, and
+//                   writes every particle (s, v, D1, D2 and its lattice point
+//                   q) to its slot in the tile order, so that the arrays
+//                   follow the particles and the next step's reads stay
+//                   nearly sequential.
+// Any order gives the same density and forces (up to the order of
+// floating-point sums); the tile order restores the locality that the
 // Lagrangian order loses as the particles cluster.
+//
+// A batch of B boxes (particle arrays 3 np floats apart, meshes one real
+// grid apart) sorts and deposits all boxes in the same launches: box b's
+// tiles follow those of boxes 0..b-1 and the order holds the global index
+// b np + p.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "mgp_device.cuh"
 #include "mgp_internal.h"
@@ -30,25 +44,53 @@ constexpr int kThreads = 256;
 constexpr int kScanItems = 16;                     // per thread in a scan block
 constexpr int kScanChunk = kThreads * kScanItems;  // elements per scan block
 
-// CIC base cell of particle p (the same arithmetic as k_cic), and its tile.
-// p is the array slot, lat the lattice point of the particle in it.
+// CIC base cell and fractions of a particle with displacement (sx, sy, sz)
+// at lattice point lat (the same arithmetic as k_cic and the kick).
+template <bool P2>
+__device__ __forceinline__ void cell_of(float sx, float sy, float sz, unsigned lat, int Ns, int ls, float inv_ns, int N,
+                                        float scale, float ox, float oy, float oz, int &ix, int &iy, int &iz,
+                                        float &DX, float &DY, float &DZ) {
+  int i, j, k;
+  if (P2) {
+    lattice_ijk_p2(lat, ls, i, j, k);
+    cell_frac_p2(i, sx, ox, N, ls, inv_ns, scale, ix, DX);
+    cell_frac_p2(j, sy, oy, N, ls, inv_ns, scale, iy, DY);
+    cell_frac_p2(k, sz, oz, N, ls, inv_ns, scale, iz, DZ);
+  } else {
+    lattice_ijk(lat, Ns, i, j, k);
+    cell_frac(i, sx, ox, N, Ns, scale, ix, DX);
+    cell_frac(j, sy, oy, N, Ns, scale, iy, DY);
+    cell_frac(k, sz, oz, N, Ns, scale, iz, DZ);
+  }
+}
+
+// The same for the particle in array slot p.
 template <bool P2>
 __device__ __forceinline__ void particle_cell(const float *__restrict__ s, long long np, long long p, unsigned lat,
                                               int Ns, int ls, float inv_ns, int N, float scale, float ox, float oy,
                                               float oz, int &ix, int &iy, int &iz, float &DX, float &DY, float &DZ) {
-  int i, j, k;
-  if (P2) {
-    lattice_ijk_p2(lat, ls, i, j, k);
-    cell_frac_p2(i, s[p], ox, N, ls, inv_ns, scale, ix, DX);
-    cell_frac_p2(j, s[np + p], oy, N, ls, inv_ns, scale, iy, DY);
-    cell_frac_p2(k, s[2 * np + p], oz, N, ls, inv_ns, scale, iz, DZ);
-  } else {
-    lattice_ijk(lat, Ns, i, j, k);
-    cell_frac(i, s[p], ox, N, Ns, scale, ix, DX);
-    cell_frac(j, s[np + p], oy, N, Ns, scale, iy, DY);
-    cell_frac(k, s[2 * np + p], oz, N, Ns, scale, iz, DZ);
-  }
+  cell_of<P2>(s[p], s[np + p], s[2 * np + p], lat, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY, DZ);
 }
+
+// The L-th tile of a kernel's sweep: with nt1 a multiple of 8 the tiles go
+// in blocks of 8^3 (the blocks, and the tiles inside one, in x, y, z
+// order), so that the tiles in flight at one time are neighbours and the
+// grid lines and particles they share are found in L2; else in index order.
+__device__ __forceinline__ int tile_at(int L, int nt1) {
+  if (nt1 & 7) return L;
+  const int ns = nt1 >> 3, sup = L >> 9, w = L & 511;
+  const int sx = sup / (ns * ns), sy = (sup / ns) % ns, sz = sup % ns;
+  const int tx = (sx << 3) + (w >> 6), ty = (sy << 3) + ((w >> 3) & 7), tz = (sz << 3) + (w & 7);
+  return (tx * nt1 + ty) * nt1 + tz;
+}
+
+// Asynchronous 16-byte global -> shared copies (cp.async, cached in L2
+// only): both addresses 16-byte aligned.
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void cp_async16(float *dst, const float *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Tile of every particle and the per-tile counts.  The loop runs in whole
 // warps (warp-aligned starts, stride a multiple of 32) so that the lanes of
@@ -59,6 +101,12 @@ __global__ void __launch_bounds__(kThreads) k_tile_key(const float *__restrict__
                                                        int ntile1, const unsigned *__restrict__ q,
                                                        unsigned *__restrict__ tile_of,
                                                        unsigned *__restrict__ count) {
+  // box blockIdx.y of a batch: particles 3 np apart, its tiles after those
+  // of the boxes before it, tile_of indexed by the particle's global index
+  const unsigned box = blockIdx.y, ntiles = (unsigned)ntile1 * ntile1 * ntile1;
+  s += (long long)box * 3 * np;
+  st += box;
+  tile_of += (long long)box * np;
   const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
   const float inv_ns = 1.0f / (float)Ns;
   const int lane = threadIdx.x & 31;
@@ -72,7 +120,8 @@ __global__ void __launch_bounds__(kThreads) k_tile_key(const float *__restrict__
     float DX, DY, DZ;
     particle_cell<P2>(s, np, p, q ? q[p] : (unsigned)p, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY,
                       DZ);
-    const unsigned t = ((unsigned)(ix >> tshift) * (unsigned)ntile1 + (unsigned)(iy >> tshift)) * (unsigned)ntile1 +
+    const unsigned t = box * ntiles +
+                       ((unsigned)(ix >> tshift) * (unsigned)ntile1 + (unsigned)(iy >> tshift)) * (unsigned)ntile1 +
                        (unsigned)(iz >> tshift);
     tile_of[p] = t;
     const unsigned same = __match_any_sync(am, t);
@@ -193,23 +242,32 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
                                                         float *__restrict__ rho, long long P,
                                                         const unsigned *__restrict__ off,
                                                         const unsigned *__restrict__ order,
-                                                        const unsigned *__restrict__ q, int ntile1) {
+                                                        const unsigned *__restrict__ q, int ntile1, int nbox,
+                                                        long long g_bs) {
   constexpr int BX = T + 1, BZ = T + 2, BOX = BX * BX * BZ;
   __shared__ float box[BOX];
-  const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
   const float inv_ns = 1.0f / (float)Ns;
   const int ntiles = ntile1 * ntile1 * ntile1;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const unsigned j0 = off[tile], j1 = off[tile + 1];
+  const float *s0 = s;
+  const mgp_dstate *st0 = st;
+  float *rho0 = rho;
+  for (int L = blockIdx.x; L < ntiles * nbox; L += gridDim.x) {
+    // box ib of a batch: particles 3 np apart, grids g_bs floats apart; the
+    // order holds global particle indices ib np + p
+    const int ib = L / ntiles, tile = tile_at(L - ib * ntiles, ntile1), gtile = ib * ntiles + tile;
+    const unsigned j0 = off[gtile], j1 = off[gtile + 1];
     if (j0 == j1) continue;
+    s = s0 + (long long)ib * 3 * np;
+    st = st0 + ib;
+    rho = rho0 + (long long)ib * g_bs;
+    const long long pbase = (long long)ib * np;
+    const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
     const int tz = tile % ntile1, ty = (tile / ntile1) % ntile1, tx = tile / (ntile1 * ntile1);
     const int x0 = tx * T, y0 = ty * T, z0 = tz * T;
-    for (int q = threadIdx.x; q < BOX; q += blockDim.x) box[q] = 0.0f;
+    for (int e = threadIdx.x; e < BOX; e += blockDim.x) box[e] = 0.0f;
     __syncthreads();
     for (unsigned j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-      // slot of the j-th particle of the tile order: order[j], or j itself
-      // once the arrays have been permuted into that order
-      const long long p = order ? (long long)order[j] : (long long)j;
+      const long long p = (long long)order[j] - pbase;  // slot of the j-th particle of the tile order
       int ix, iy, iz;
       float DX, DY, DZ;
       particle_cell<P2>(s, np, p, q ? q[p] : (unsigned)p, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY,
@@ -244,8 +302,8 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
       atomicAdd(box + b + BX * BZ + BZ + 1, DX * DY * DZ);
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < BX * BX * (BZ / 2); q += blockDim.x) {
-      const int zz = q % (BZ / 2), r = q / (BZ / 2), yy = r % BX, xx = r / BX;
+    for (int e = threadIdx.x; e < BX * BX * (BZ / 2); e += blockDim.x) {
+      const int zz = e % (BZ / 2), r = e / (BZ / 2), yy = r % BX, xx = r / BX;
       const float2 v = make_float2(box[r * BZ + 2 * zz], box[r * BZ + 2 * zz + 1]);
       if (v.x == 0.0f && v.y == 0.0f) continue;
       int gx = x0 + xx, gy = y0 + yy, gz = z0 + 2 * zz;
@@ -255,30 +313,6 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
       atomicAdd(reinterpret_cast<float2 *>(rho + ((long long)gx * N + gy) * P + gz), v);
     }
     __syncthreads();
-  }
-}
-
-// Gather of the particle arrays into the tile order: slot j takes the
-// particle of slot order[j] (s, v, D1, D2: [3][np] each) and its lattice
-// point.  Reads come in runs of lattice neighbours, writes are coalesced.
-__global__ void __launch_bounds__(kThreads) k_permute(const unsigned *__restrict__ order, long long np,
-                                                      const float *__restrict__ s, const float *__restrict__ v,
-                                                      const float *__restrict__ D1, const float *__restrict__ D2,
-                                                      const unsigned *__restrict__ q, float *__restrict__ s2,
-                                                      float *__restrict__ v2, float *__restrict__ D12,
-                                                      float *__restrict__ D22, unsigned *__restrict__ q2) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < np; j += stride) {
-    const long long src = order[j];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-      const long long o = a * np;
-      s2[o + j] = s[o + src];
-      v2[o + j] = v[o + src];
-      D12[o + j] = D1[o + src];
-      D22[o + j] = D2[o + src];
-    }
-    q2[j] = q ? q[src] : (unsigned)src;
   }
 }
 
@@ -302,6 +336,164 @@ __global__ void __launch_bounds__(kThreads) k_unpermute(long long np, const floa
   }
 }
 
+// Block sum of one double per thread (the result in thread 0).
+__device__ __forceinline__ double block_sum_tiles(double x, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = x;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += sh[k];
+  return t;
+}
+
+// Force tile in shared memory: three components, each (T+1)^2 rows of
+// R = T + 4 floats.  A grid row (x, y) of N + 2 floats starts on a 16-byte
+// boundary when y is even and 8 bytes past one when y is odd, so row
+// (xx, yy) of the tile is copied as R/4 16-byte pieces from z0 (yy even) or
+// z0 - 2 (yy odd): the tile's z0..z0+T then sit at offset 2 (yy & 1) of the
+// row.  The copied run stays inside the grids: an odd row's starts 2 floats
+// into the previous row's padding, an even row's ends at most 2 floats into
+// the next row (y <= N - 2).  The z halo of the last tile in z lands in the
+// row padding and is patched from z = 0.
+template <int T>
+struct force_tile {
+  static constexpr int X = T + 1, R = T + 4, COMP = X * X * R, FLOATS = 3 * COMP;
+  static constexpr int PIECES = R / 4;  // 16-byte copies per row
+};
+
+// Shared-memory offset of row (xx, yy) of component c of the force tile
+// (the element z0 + zz is at the returned offset + zz).
+template <int T>
+__device__ __forceinline__ int tile_row(int c, int xx, int yy) {
+  using FT = force_tile<T>;
+  return c * FT::COMP + (xx * FT::X + yy) * FT::R + 2 * (yy & 1);
+}
+
+// MtoParticles (src/auxPM.c:560-644) + Kick (src/main.c:688-742) + Drift
+// (src/main.c:747-787) per cell tile, writing the particles in tile order.
+// Tile `tile` holds order[off[tile] .. off[tile+1]), the slots of the
+// particles whose CIC base cell lies in it (k_tile_key, same positions).
+// The block copies fx, fy, fz over the tile's cells and the +1 halo
+// (periodic) into shared memory (force_tile), then for each particle:
+// reads slot p = order[j] of the input arrays, interpolates the forces from
+// shared memory (a base cell outside the tile -- not expected, the key pass
+// rounds identically -- reads the global grids), kicks and drifts as
+// k_interp_kick_drift does (same expressions in the same order), and writes
+// slot j of the output arrays, q2[j] = its lattice point.  D1/D2 are
+// particle arrays (scale-independent growth).  Per-block sums of the
+// interpolated forces and new velocities go to partials for k_finalize_kd.
+// PI: particle-array offset type, 32-bit when 3 np < 2^32 (fewer integer
+// instructions per access); NT: threads per block.
+template <int T, bool P2, typename PI, int NT>
+__global__ void __launch_bounds__(NT) k_ikd_tiles(
+    const float *__restrict__ frc, long long gf, int N, long long P, int Ns, int ls, long long np,
+    const float *__restrict__ s, const float *__restrict__ v, const float *__restrict__ D1,
+    const float *__restrict__ D2, const unsigned *__restrict__ q, const unsigned *__restrict__ off,
+    const unsigned *__restrict__ order, int ntile1, const mgp_dstate *__restrict__ st, float *__restrict__ s2,
+    float *__restrict__ v2, float *__restrict__ D12, float *__restrict__ D22, unsigned *__restrict__ q2,
+    double *__restrict__ partials, mgp_kd_args a) {
+  using FT = force_tile<T>;
+  constexpr int X = FT::X, R = FT::R, COMP = FT::COMP, K = FT::PIECES;
+  constexpr int ROWS = NT / K;  // rows copied per pass of the block
+  extern __shared__ __align__(16) float fs[];  // FT::FLOATS
+  __shared__ double sh[NT / 32];
+  __shared__ long long rowoff[X * X];  // grid offset of row (x0 + xx, y0 + yy), periodic
+  const int sub = threadIdx.x / K, k = threadIdx.x - sub * K;  // this thread's row in a pass, its piece
+  const float ox = (float)(st->cx[0] * a.scale), oy = (float)(st->cx[1] * a.scale), oz = (float)(st->cx[2] * a.scale);
+  const float inv_ns = 1.0f / (float)Ns;
+  const int ntiles = ntile1 * ntile1 * ntile1;
+  float accD[3] = {0.f, 0.f, 0.f}, accV[3] = {0.f, 0.f, 0.f};
+  for (int L = blockIdx.x; L < ntiles; L += gridDim.x) {
+    const int tile = tile_at(L, ntile1);
+    const unsigned j0 = off[tile], j1 = off[tile + 1];
+    if (j0 == j1) continue;
+    const int tz = tile % ntile1, ty = (tile / ntile1) % ntile1, tx = tile / (ntile1 * ntile1);
+    const int x0 = tx * T, y0 = ty * T, z0 = tz * T;
+    __syncthreads();  // the previous tile's reads of fs and rowoff are done
+    for (int r = threadIdx.x; r < X * X; r += NT) {
+      const int xx = r / X, yy = r - xx * X;
+      const int gx = x0 + xx >= N ? x0 + xx - N : x0 + xx, gy = y0 + yy >= N ? y0 + yy - N : y0 + yy;
+      rowoff[r] = ((long long)gx * N + gy) * P + z0 - 2 * (yy & 1);
+    }
+    __syncthreads();
+    if (sub < ROWS) {
+      for (int r = sub; r < 3 * X * X; r += ROWS) {
+        const int c = r >= 2 * X * X ? 2 : (r >= X * X ? 1 : 0), rr = r - c * X * X;
+        cp_async16(fs + c * COMP + rr * R + 4 * k, frc + c * gf + rowoff[rr] + 4 * k);
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (z0 + T == N) {
+      // last tile in z: the halo column z0 + T is z = 0 of the same row
+      for (int r = threadIdx.x; r < 3 * X * X; r += NT) {
+        const int c = r / (X * X), rr = r - c * X * X, yy = rr % X;
+        fs[c * COMP + rr * R + 2 * (yy & 1) + T] = frc[c * gf + rowoff[rr] + 2 * (yy & 1) - z0];
+      }
+      __syncthreads();
+    }
+    const PI npi = (PI)np;
+    for (unsigned j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+      const PI p = (PI)order[j];
+      const unsigned lat = q ? q[p] : (unsigned)p;
+      const float sp[3] = {s[p], s[npi + p], s[2 * npi + p]};
+      int ix, iy, iz;
+      float DX, DY, DZ;
+      cell_of<P2>(sp[0], sp[1], sp[2], lat, Ns, ls, inv_ns, N, a.scale, ox, oy, oz, ix, iy, iz, DX, DY, DZ);
+      const float TX = 1.0f - DX, TY = 1.0f - DY, TZ = 1.0f - DZ;
+      const float w000 = TX * TY * TZ, w001 = TX * TY * DZ, w010 = TX * DY * TZ, w011 = TX * DY * DZ;
+      const float w100 = DX * TY * TZ, w101 = DX * TY * DZ, w110 = DX * DY * TZ, w111 = DX * DY * DZ;
+      const int lx = ix - x0, ly = iy - y0, lz = iz - z0;
+      float disp[3];
+      if ((unsigned)lx < (unsigned)T && (unsigned)ly < (unsigned)T && (unsigned)lz < (unsigned)T) {
+        // row (lx, ly + 1) is in the other parity's box
+        const float *f = fs + tile_row<T>(0, lx, ly) + lz;
+        const int dy = R + ((ly & 1) ? -2 : 2), dx = X * R;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const float *F = f + c * COMP;
+          disp[c] = F[0] * w000 + F[1] * w001 + F[dy] * w010 + F[dy + 1] * w011 + F[dx] * w100 + F[dx + 1] * w101 +
+                    F[dx + dy] * w110 + F[dx + dy + 1] * w111;
+        }
+      } else {
+        const long long xa = (long long)ix * N * P, xb = (ix + 1 == N ? 0 : (long long)(ix + 1) * N * P);
+        const long long ya = (long long)iy * P, yb = (iy + 1 == N ? 0 : (long long)(iy + 1) * P);
+        const long long za = iz, zb = iz + 1 == N ? 0 : iz + 1;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const float *F = frc + c * gf;
+          disp[c] = F[xa + ya + za] * w000 + F[xa + ya + zb] * w001 + F[xa + yb + za] * w010 +
+                    F[xa + yb + zb] * w011 + F[xb + ya + za] * w100 + F[xb + ya + zb] * w101 +
+                    F[xb + yb + za] * w110 + F[xb + yb + zb] * w111;
+        }
+      }
+#pragma unroll
+      for (int ax = 0; ax < 3; ax++) {
+        const PI o = (PI)ax * npi, oj = o + (PI)j;
+        const float d1 = D1[o + p], d2 = D2[o + p];
+        const float vn = v[o + p] + a.kick_disp * disp[ax] + a.kick_d1 * d1 + a.kick_d2 * d2;
+        v2[oj] = vn;
+        s2[oj] = a.do_drift ? sp[ax] + vn * a.dyyy + a.dD1 * d1 + a.dD2 * d2 : sp[ax];
+        D12[oj] = d1;
+        D22[oj] = d2;
+        accD[ax] += disp[ax];
+        accV[ax] += vn;
+      }
+      q2[j] = lat;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double t = block_sum_tiles((double)accD[c], sh);
+    if (threadIdx.x == 0) partials[(long long)blockIdx.x * 6 + c] = t;
+    t = block_sum_tiles((double)accV[c], sh);
+    if (threadIdx.x == 0) partials[(long long)blockIdx.x * 6 + 3 + c] = t;
+  }
+}
+
 }  // namespace
 
 // Tile side in cells for the tile path, or 0 when it does not apply (the
@@ -313,22 +505,43 @@ int mgp_tile_side(int N, long long np) {
   return 0;
 }
 
-int mgp_tiles_alloc(mgp_ctx *c) {
-  if (c->tile_order) return MGP_OK;
-  const int T = mgp_tile_side(c->g.N, c->np);
-  if (!T) return mgp_set_error(MGP_EINVAL, "no tile side for Nmesh = %d", c->g.N);
+// Whether the tile deposit of side T (8 or 16) applies to the context's
+// boxes: whole tiles, particle indices of all boxes in 32 bits, the tiles of
+// all boxes within the two-level scan (kScanChunk^2).
+int mgp_tiles_check(const mgp_ctx *c, int T) {
+  if (T != 8 && T != 16) return mgp_set_error(MGP_EINVAL, "tile side %d (8 or 16)", T);
+  if (c->g.N % T) return mgp_set_error(MGP_EINVAL, "tile side %d does not divide Nmesh = %d", T, c->g.N);
+  const long long nt1 = c->g.N / T, ntiles = nt1 * nt1 * nt1 * c->nbox, nall = c->np * c->nbox;
+  if (nall > 0xffffffffLL) return mgp_set_error(MGP_EINVAL, "%lld particles exceed 32-bit indices", nall);
+  if (ntiles > (long long)kScanChunk * kScanChunk)
+    return mgp_set_error(MGP_EINVAL, "%lld tiles exceed the scan's capacity", ntiles);
+  return MGP_OK;
+}
+
+// Tile arrays for side T over all boxes of the context (the count and
+// offset arrays grow when a batch tries a smaller tile side).
+int mgp_tiles_alloc(mgp_ctx *c, int T) {
+  int rc = mgp_tiles_check(c, T);
+  if (rc != MGP_OK) return rc;
   const int nt1 = c->g.N / T;
-  const long long ntiles = (long long)nt1 * nt1 * nt1;
+  const long long ntiles = (long long)nt1 * nt1 * nt1 * c->nbox, nall = c->np * c->nbox;
+  const long long nblk = (ntiles + kScanChunk - 1) / kScanChunk;
+  if (!c->tile_order) {
+    MGP_CUDA(cudaMalloc(&c->tile_of, sizeof(unsigned) * (size_t)nall));
+    MGP_CUDA(cudaMalloc(&c->tile_order, sizeof(unsigned) * (size_t)nall));
+  }
+  if (ntiles > c->tile_cap) {
+    void *b[] = {c->tile_count, c->tile_off, c->tile_cursor, c->tile_bsum};
+    for (void *x : b)
+      if (x) cudaFree(x);
+    MGP_CUDA(cudaMalloc(&c->tile_count, sizeof(unsigned) * (size_t)ntiles));
+    MGP_CUDA(cudaMalloc(&c->tile_off, sizeof(unsigned) * (size_t)(ntiles + 1)));
+    MGP_CUDA(cudaMalloc(&c->tile_cursor, sizeof(unsigned) * (size_t)ntiles));
+    MGP_CUDA(cudaMalloc(&c->tile_bsum, sizeof(unsigned) * (size_t)nblk));
+    c->tile_cap = ntiles;
+  }
   c->tile_side = T;
   c->tile_n1 = nt1;
-  const long long nblk = (ntiles + kScanChunk - 1) / kScanChunk;
-  if (nblk > kScanChunk) return mgp_set_error(MGP_EINVAL, "%lld tiles exceed the scan's capacity", ntiles);
-  MGP_CUDA(cudaMalloc(&c->tile_of, sizeof(unsigned) * (size_t)c->np));
-  MGP_CUDA(cudaMalloc(&c->tile_order, sizeof(unsigned) * (size_t)c->np));
-  MGP_CUDA(cudaMalloc(&c->tile_count, sizeof(unsigned) * (size_t)ntiles));
-  MGP_CUDA(cudaMalloc(&c->tile_off, sizeof(unsigned) * (size_t)(ntiles + 1)));
-  MGP_CUDA(cudaMalloc(&c->tile_cursor, sizeof(unsigned) * (size_t)ntiles));
-  MGP_CUDA(cudaMalloc(&c->tile_bsum, sizeof(unsigned) * (size_t)nblk));
   return MGP_OK;
 }
 
@@ -341,6 +554,7 @@ void mgp_tiles_free(mgp_ctx *c) {
   c->q = c->q_alt = NULL;
   c->s_alt = c->v_alt = c->D1_alt = c->D2_alt = NULL;
   c->tile_ready = 0;
+  c->tile_cap = 0;
   c->permuted = 0;
 }
 
@@ -352,32 +566,11 @@ static void swap_arrays(mgp_ctx *c) {
   t = c->D2; c->D2 = c->D2_alt; c->D2_alt = t;
 }
 
-// Permute the particle arrays into the order of the last mgp_tiles_sort
-// (into the second buffers, then swap); q follows the particles.
-int mgp_tiles_permute(mgp_ctx *c) {
-  const size_t bytes = sizeof(float) * 3 * (size_t)c->np;
-  if (!c->s_alt) {
-    MGP_CUDA(cudaMalloc(&c->s_alt, bytes));
-    MGP_CUDA(cudaMalloc(&c->v_alt, bytes));
-    MGP_CUDA(cudaMalloc(&c->D1_alt, bytes));
-    MGP_CUDA(cudaMalloc(&c->D2_alt, bytes));
-    MGP_CUDA(cudaMalloc(&c->q, sizeof(unsigned) * (size_t)c->np));
-    MGP_CUDA(cudaMalloc(&c->q_alt, sizeof(unsigned) * (size_t)c->np));
-  }
-  k_permute<<<mgp_blocks_for(c->np, 8), kThreads, 0, c->stream>>>(c->tile_order, c->np, c->s, c->v, c->D1, c->D2,
-                                                                  c->permuted ? c->q : NULL, c->s_alt, c->v_alt,
-                                                                  c->D1_alt, c->D2_alt, c->q_alt);
-  MGP_CHECK_LAUNCH();
-  g_kernel_launches++;
-  swap_arrays(c);
-  unsigned *t = c->q;
-  c->q = c->q_alt;
-  c->q_alt = t;
-  c->permuted = 1;
-  return MGP_OK;
-}
-
+// Lattice order of the particle arrays (the particle of slot j to slot
+// q[j]); every caller of this is about to read or replace the particles, so
+// the last tile sort no longer describes the arrays.
 int mgp_particles_canonical(mgp_ctx *c) {
+  c->tile_ready = 0;
   if (!c->permuted) return MGP_OK;
   k_unpermute<<<mgp_blocks_for(c->np, 8), kThreads, 0, c->stream>>>(c->np, c->s, c->v, c->D1, c->D2, c->q, c->s_alt,
                                                                     c->v_alt, c->D1_alt, c->D2_alt);
@@ -385,28 +578,28 @@ int mgp_particles_canonical(mgp_ctx *c) {
   g_kernel_launches++;
   swap_arrays(c);
   c->permuted = 0;
-  c->tile_age = 0;
   return MGP_OK;
 }
 
-// Bucket the particles of a single box by tile (their current positions).
-int mgp_tiles_sort(mgp_ctx *c) {
-  int rc = mgp_tiles_alloc(c);
+// Bucket the particles of every box by tile of side T (their current
+// positions).
+int mgp_tiles_sort(mgp_ctx *c, int T) {
+  int rc = mgp_tiles_alloc(c, T);
   if (rc != MGP_OK) return rc;
-  const int N = c->g.N, Ns = c->Ns, T = c->tile_side, nt1 = c->tile_n1;
-  const long long ntiles = (long long)nt1 * nt1 * nt1;
+  const int N = c->g.N, Ns = c->Ns, nt1 = c->tile_n1, B = c->nbox;
+  const long long ntiles = (long long)nt1 * nt1 * nt1 * B, nall = c->np * B;
   const int ls = lattice_log2(Ns);
   const float scale = (float)(N / c->p.Box);
   int tshift = 0;
   while ((1 << tshift) < T) tshift++;
   const unsigned *qp = c->permuted ? c->q : NULL;
   MGP_CUDA(cudaMemsetAsync(c->tile_count, 0, sizeof(unsigned) * (size_t)ntiles, c->stream));
-  const int nb = mgp_blocks_for(c->np, 8);
+  const dim3 gk(mgp_blocks_per_box(c->np, 8, B), B);
   if (ls >= 0)
-    k_tile_key<true><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, tshift, nt1, qp,
+    k_tile_key<true><<<gk, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, tshift, nt1, qp,
                                                      c->tile_of, c->tile_count);
   else
-    k_tile_key<false><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, tshift, nt1, qp,
+    k_tile_key<false><<<gk, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, tshift, nt1, qp,
                                                       c->tile_of, c->tile_count);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
@@ -418,37 +611,101 @@ int mgp_tiles_sort(mgp_ctx *c) {
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   k_scan_add<<<mgp_blocks_for(ntiles + 1, 8), kThreads, 0, c->stream>>>(c->tile_off, c->tile_cursor, ntiles,
-                                                                        c->tile_bsum, (unsigned)c->np);
+                                                                        c->tile_bsum, (unsigned)nall);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
-  k_tile_scatter<<<nb, kThreads, 0, c->stream>>>(c->tile_of, c->np, c->tile_cursor, c->tile_order);
+  k_tile_scatter<<<mgp_blocks_for(nall, 8), kThreads, 0, c->stream>>>(c->tile_of, nall, c->tile_cursor,
+                                                                      c->tile_order);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   c->tile_ready = 1;
   return MGP_OK;
 }
 
-// Tile deposit onto a mesh pre-set to -1 (after mgp_tiles_sort; identity:
-// the arrays were just permuted into the sort's order).
-int mgp_cic_tiles(mgp_ctx *c, float wpar, int identity) {
-  const unsigned *ord = identity ? NULL : c->tile_order, *qp = c->permuted ? c->q : NULL;
-  const int N = c->g.N, Ns = c->Ns, T = c->tile_side, nt1 = c->tile_n1;
+// Tile deposit onto meshes pre-set to -1 (after mgp_tiles_sort); per_sm:
+// resident blocks per SM of the launch (0: the default budget).
+int mgp_cic_tiles(mgp_ctx *c, float wpar, int per_sm) {
+  const unsigned *ord = c->tile_order, *qp = c->permuted ? c->q : NULL;
+  const int N = c->g.N, Ns = c->Ns, T = c->tile_side, nt1 = c->tile_n1, B = c->nbox;
+  const long long gbs = c->g.nreal;
   const int ls = lattice_log2(Ns);
   const float scale = (float)(N / c->p.Box);
-  const int nb = mgp_blocks_for((long long)nt1 * nt1 * nt1 * kThreads, 8);
+  const int nb = mgp_blocks_for((long long)nt1 * nt1 * nt1 * B * kThreads, per_sm > 0 ? per_sm : 8);
   if (T == 16 && ls >= 0)
     k_cic_tiles<16, true><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                          c->g.P, c->tile_off, ord, qp, nt1);
+                                                          c->g.P, c->tile_off, ord, qp, nt1, B, gbs);
   else if (T == 16)
     k_cic_tiles<16, false><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                           c->g.P, c->tile_off, ord, qp, nt1);
+                                                           c->g.P, c->tile_off, ord, qp, nt1, B, gbs);
   else if (ls >= 0)
     k_cic_tiles<8, true><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                         c->g.P, c->tile_off, ord, qp, nt1);
+                                                         c->g.P, c->tile_off, ord, qp, nt1, B, gbs);
   else
     k_cic_tiles<8, false><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                          c->g.P, c->tile_off, ord, qp, nt1);
+                                                          c->g.P, c->tile_off, ord, qp, nt1, B, gbs);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Kick + drift per tile in the order of the last mgp_tiles_sort (a single
+// box with particle-array LPT displacements; the positions unchanged since
+// the sort), the particle arrays rewritten in that order into the second
+// buffers, which then become the arrays.  nblocks_out: the grid, whose
+// per-block partial sums k_finalize_kd reduces.
+int mgp_ikd_tiles(mgp_ctx *c, const mgp_kd_args *a, int *nblocks_out) {
+  if (!c->tile_ready || c->nbox != 1) return mgp_set_error(MGP_ESTATE, "tile kick without a current tile sort");
+  const size_t bytes = sizeof(float) * 3 * (size_t)c->np;
+  if (!c->s_alt) {
+    MGP_CUDA(cudaMalloc(&c->s_alt, bytes));
+    MGP_CUDA(cudaMalloc(&c->v_alt, bytes));
+    MGP_CUDA(cudaMalloc(&c->D1_alt, bytes));
+    MGP_CUDA(cudaMalloc(&c->D2_alt, bytes));
+    MGP_CUDA(cudaMalloc(&c->q, sizeof(unsigned) * (size_t)c->np));
+    MGP_CUDA(cudaMalloc(&c->q_alt, sizeof(unsigned) * (size_t)c->np));
+  }
+  const int T = c->tile_side, nt1 = c->tile_n1, N = c->g.N, Ns = c->Ns;
+  const int ls = lattice_log2(Ns);
+  const long long ntiles = (long long)nt1 * nt1 * nt1;
+  const unsigned *qp = c->permuted ? c->q : NULL;
+  // 16^3 tiles: 62 KB of forces per block, three blocks of 256 threads per
+  // SM; 8^3 tiles: 10 KB, eight blocks per SM
+  const size_t smem = sizeof(float) * (T == 16 ? force_tile<16>::FLOATS : force_tile<8>::FLOATS);
+  constexpr int NT16 = 256, NT8 = 256;
+  const int nt = T == 16 ? NT16 : NT8;
+  int nb = mgp_blocks_for(ntiles * nt, T == 16 ? 3 : 8);
+  if (nb > c->max_blocks) nb = c->max_blocks;
+#define MGP_IKD_TILES(TT, PP, PI)                                                                             \
+  do {                                                                                                        \
+    constexpr int NTT = TT == 16 ? NT16 : NT8;                                                                \
+    MGP_CUDA(cudaFuncSetAttribute(k_ikd_tiles<TT, PP, PI, NTT>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                  (int)smem));                                                                \
+    k_ikd_tiles<TT, PP, PI, NTT><<<nb, NTT, smem, c->stream>>>(c->frc, c->g.nreal, N, c->g.P, Ns, ls, c->np,  \
+                                                               c->s, c->v, c->D1, c->D2, qp, c->tile_off,     \
+                                                               c->tile_order, nt1, c->dstate, c->s_alt,       \
+                                                               c->v_alt, c->D1_alt, c->D2_alt, c->q_alt,      \
+                                                               c->partials, *a);                              \
+  } while (0)
+  const bool narrow = 3 * c->np < 0xffffffffLL;
+  if (T == 16 && ls >= 0 && narrow)
+    MGP_IKD_TILES(16, true, unsigned);
+  else if (T == 16 && ls >= 0)
+    MGP_IKD_TILES(16, true, long long);
+  else if (T == 16)
+    MGP_IKD_TILES(16, false, long long);
+  else if (ls >= 0)
+    MGP_IKD_TILES(8, true, long long);
+  else
+    MGP_IKD_TILES(8, false, long long);
+#undef MGP_IKD_TILES
+  MGP_CHECK_LAUNCH();
+  g_kernel_launches++;
+  swap_arrays(c);
+  unsigned *t = c->q;
+  c->q = c->q_alt;
+  c->q_alt = t;
+  c->permuted = 1;
+  c->tile_ready = 0;  // the arrays are in the sort's order now, the positions drifted
+  *nblocks_out = nb;
   return MGP_OK;
 }

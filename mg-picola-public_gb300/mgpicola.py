@@ -26,7 +26,7 @@ EXPORTS = [
     "mgp_host_register", "mgp_host_unregister", "mgp_host_alloc", "mgp_host_free", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
     "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_batch_set_tuning",
-    "mgp_batch_get_tuning", "mgp_batch_autotune", "mgp_output_stats", "mgp_displacement_fields_from_positions",
+    "mgp_batch_get_tuning", "mgp_batch_set_deposit_tiles", "mgp_batch_get_deposit_tiles", "mgp_batch_autotune", "mgp_output_stats", "mgp_displacement_fields_from_positions",
     "mgp_read_particle_files", "mgp_free_particles", "mgp_closure_create", "mgp_closure_destroy",
     "mgp_closure_get_weights", "mgp_closure_set_weights", "mgp_closure_set_sample", "mgp_closure_get_sample",
     "mgp_closure_forward", "mgp_closure_gradients", "mgp_closure_train_step", "mgp_closure_features",
@@ -138,6 +138,8 @@ def lib():
         L.mgp_batch_graph_kernels.argtypes = [vp]
         L.mgp_batch_set_tuning.argtypes = [vp, C.POINTER(C.c_int)]
         L.mgp_batch_get_tuning.argtypes = [vp, C.POINTER(C.c_int)]
+        L.mgp_batch_set_deposit_tiles.argtypes = [vp, C.c_int]
+        L.mgp_batch_get_deposit_tiles.argtypes = [vp]
         L.mgp_batch_autotune.argtypes = [vp, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.mgp_output_stats.argtypes = [vp, C.POINTER(C.c_int)] + [C.POINTER(C.c_double)] * 3
         L.mgp_displacement_fields_from_positions.argtypes = [vp, C.POINTER(C.c_double), C.c_size_t]
@@ -484,10 +486,10 @@ class Context:
         return lib().mgp_kernel_ms_step(self.h, name.encode(), step)
 
     def set_particle_order(self, tiles):
-        """Cell-tile particle order (mgp_set_particle_order): True/1 the
-        default (tile deposit, arrays in lattice order), n > 1 the arrays
-        also permuted into tile order every n steps (-1: every 4), False/0
-        the deposit in lattice order."""
+        """Cell-tile particle order (mgp_set_particle_order): 2 the default
+        for single boxes (tile deposit, kick per tile with the arrays
+        rewritten in tile order every step), 1 the tile deposit with the
+        arrays in lattice order, 0 the deposit and kick in lattice order."""
         _check(lib().mgp_set_particle_order(self.h, int(tiles)))
 
     def mark(self, slot):
@@ -565,8 +567,18 @@ class Batch:
         t = (C.c_int * 4)(*tune)
         _check(lib().mgp_batch_set_tuning(self.h, t))
 
+    def deposit_tiles(self):
+        """Deposit form: 0 lattice order, 8 or 16 the tile side in cells."""
+        r = lib().mgp_batch_get_deposit_tiles(self.h)
+        _check(min(r, 0))
+        return r
+
+    def set_deposit_tiles(self, side):
+        _check(lib().mgp_batch_set_deposit_tiles(self.h, side))
+
     def autotune(self, nsteps, z_final=0.0):
-        """Pick the launch budgets by timing runs; returns the best graph ms."""
+        """Pick the deposit form and the launch budgets by timing runs;
+        returns the best graph ms."""
         ms = C.c_double(0)
         _check(lib().mgp_batch_autotune(self.h, nsteps, z_final, C.byref(ms)))
         return ms.value

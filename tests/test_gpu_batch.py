@@ -118,10 +118,11 @@ def test_batch_autotune_keeps_parity():
     p = params(model=M.MODEL_FOFR, modified_gravity_active=1, include_screening=1, fofr0=1e-5, nfofr=1.0)
     boxes = [dict(Seed=6011, inverted=0, fofr0=1e-5), dict(Seed=6012, inverted=1, fofr0=3e-6)]
     with M.Batch(p, boxes) as batch:
-        assert batch.tuning() == [8, 8, 8, 4]
+        assert batch.tuning() == [8, 8, 8, 4] and batch.deposit_tiles() == 0
         ms = batch.autotune(nsteps)
         t = batch.tuning()
         assert ms > 0 and all(x in (1, 2, 4, 8, 16, 32) for x in t) and t[3] <= 16
+        assert batch.deposit_tiles() in (0, 8, 16)
         batch.run(nsteps)
         for b, box in enumerate(boxes):
             check_box(batch, b, p, O.make_mg(O.FOFR, 0.267, fofr0=box["fofr0"], nfofr=1.0), box, nsteps)
@@ -131,3 +132,38 @@ def test_batch_autotune_keeps_parity():
             check_box(batch, b, p, O.make_mg(O.FOFR, 0.267, fofr0=box["fofr0"], nfofr=1.0), box, nsteps)
         with pytest.raises(M.MGPError):
             batch.set_tuning([0, 8, 8, 4])
+
+
+@pytest.mark.parametrize("side", [8, 16])
+def test_batch_tile_deposit_matches_oracle(side):
+    """The tile deposit of a batch (all boxes' particles counted and bucketed
+    by tile inside the graph, per-tile shared-memory sums) against each box's
+    oracle run, and against the lattice-order deposit of the same batch: the
+    P(k) of the first step agrees to float rounding (the two deposits sum in
+    different orders)."""
+    nsteps = 4
+    p = params(model=M.MODEL_FOFR, modified_gravity_active=1, include_screening=1, fofr0=1e-5, nfofr=1.0)
+    boxes = [dict(Seed=6021, inverted=0, fofr0=1e-5), dict(Seed=6022, inverted=1, fofr0=1e-4),
+             dict(Seed=6023, inverted=0, fofr0=1e-6)]
+    with M.Batch(p, boxes) as batch:
+        batch.run(nsteps)
+        lat = [batch.pofk(b, 0)[1].copy() for b in range(len(boxes))]
+        batch.set_deposit_tiles(side)
+        assert batch.deposit_tiles() == side
+        batch.run(nsteps)
+        for b, box in enumerate(boxes):
+            check_box(batch, b, p, O.make_mg(O.FOFR, 0.267, fofr0=box["fofr0"], nfofr=1.0), box, nsteps)
+            np.testing.assert_allclose(batch.pofk(b, 0)[1][1:], lat[b][1:], rtol=1e-5, atol=0)
+        batch.set_deposit_tiles(0)
+        assert batch.deposit_tiles() == 0
+        for bad in (4, 12, 24, -8):
+            with pytest.raises(M.MGPError):
+                batch.set_deposit_tiles(bad)
+
+
+def test_batch_tile_deposit_rejects_meshes_it_does_not_divide():
+    p = params(Nmesh=40, Nsample=20)
+    with M.Batch(p, [dict(Seed=1), dict(Seed=2)]) as batch:
+        batch.set_deposit_tiles(8)
+        with pytest.raises(M.MGPError, match="divide"):
+            batch.set_deposit_tiles(16)

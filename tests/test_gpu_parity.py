@@ -99,36 +99,42 @@ def test_tile_deposit_matches_lattice_order_deposit(N, Ns, spread):
     rho = []
     with M.Context(p) as ctx:
         ctx.set_particles(pos, vel, d1, d2)
-        # tile deposit after permuting the arrays, through the index order,
-        # and in lattice order
-        for tiles in (-1, 1, 0):
+        # tile deposit with the arrays in lattice order, and the deposit in
+        # lattice order
+        for tiles in (1, 0):
             ctx.set_particle_order(tiles)
             ctx.get_displacements(0.5)
             rho.append(ctx.grid(0)[:, :, :N].astype(np.float64))
-        # the permuted arrays come back in lattice order
-        ctx.set_particle_order(-1)
+        # the tile kick (here over a zero interval, without drift) rewrites
+        # the arrays in the deposit's tile order; the deposit from those
+        # arrays, and the particles handed back in lattice order
+        ctx.set_particle_order(2)
         ctx.get_displacements(0.5)
+        ctx.kick_drift(0.5, 0.5, 0.5, 0.5, drift=False)
+        ctx.get_displacements(0.5)
+        rho.append(ctx.grid(0)[:, :, :N].astype(np.float64))
         back = ctx.get_particles()
     ref = O.cic(pos.astype(np.float64), N, Ns, box)[:, :, :N]
     scale = np.abs(ref).max()
-    for r in rho[:2]:
-        assert np.abs(r - rho[2]).max() < 2e-6 * scale
+    for r in (rho[0], rho[2]):
+        assert np.abs(r - rho[1]).max() < 2e-6 * scale
     assert np.abs(rho[0] - ref).max() < 2e-5 * scale
     assert abs(rho[0].mean()) < 1e-6
     dx = np.abs(back[0] - pos)
     assert np.minimum(dx, box - dx).max() < 1e-4 * box / Ns
-    np.testing.assert_array_equal(back[1], vel)
+    np.testing.assert_allclose(back[1], vel, rtol=1e-6, atol=1e-5)
     np.testing.assert_array_equal(back[2], d1)
     np.testing.assert_array_equal(back[3], d2)
 
 
-@pytest.mark.parametrize("tiles", [1, 2, -1])  # default, permuted every 2 / 4 steps
-def test_tile_order_run_matches_lattice_order_run(tiles):
+@pytest.mark.parametrize("N,Ns", [(64, 32), (48, 24)])  # 16^3 tiles, power-of-two lattice; 8^3 tiles, general
+@pytest.mark.parametrize("tiles", [2, 1])  # tile deposit and kick (the default); tile deposit only
+def test_tile_order_run_matches_lattice_order_run(tiles, N, Ns):
     """Five KDK steps with the cell-tile particle order (tile deposit; the
-    arrays permuted into tile order every 4 or 2 steps, or kept in lattice
-    order) against the lattice order: the same run up to float summation
-    order."""
-    N, Ns, box, nsteps = 64, 32, 128.0, 5
+    kick per tile with the arrays rewritten in tile order every step, or the
+    arrays kept in lattice order) against the lattice order: the same run up
+    to float summation order."""
+    box, nsteps = 2.0 * N, 5
     p = params(N, Ns, box)
     out = []
     for tiles in (tiles, 0):
@@ -195,12 +201,17 @@ def test_forces_match_oracle():
         assert rel_rms(f[a], fo[a][:, :, :N]) < 1e-5
 
 
-def test_kick_drift_matches_oracle():
-    N, Ns, box = 32, 16, 64.0
+@pytest.mark.parametrize("N,Ns,tiles", [(32, 16, 2), (32, 16, 0), (64, 32, 2), (64, 32, 1), (48, 24, 2)])
+def test_kick_drift_matches_oracle(N, Ns, tiles):
+    """MtoParticles + Kick + Drift against the oracle: per cell tile with the
+    forces staged in shared memory (order 2, the default; 8^3 and 16^3
+    tiles), and in array order (orders 0 and 1)."""
+    box = 2.0 * N
     p = params(N, Ns, box)
     pos, vel, d1, d2 = random_particles(Ns, box, seed=6, spread=0.4)
     A, AI, AF, AFF = 0.30, 0.28, 0.32, 0.34
     with M.Context(p) as ctx:
+        ctx.set_particle_order(tiles)
         ctx.set_particles(pos, vel, d1, d2)
         ctx.get_displacements(A)
         ctx.kick_drift(AI, AF, A, AFF, drift=True)
