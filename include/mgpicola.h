@@ -511,6 +511,15 @@ int mgp_mark(mgp_ctx *ctx, int slot);
  * kick walks them in that order.  tiles = 0: deposit and kick in lattice
  * order.  All give the same results up to the order of float sums. */
 int mgp_set_particle_order(mgp_ctx *ctx, int tiles);
+/* Transforms of a single box with Nmesh = 1024 (no counterpart in the
+ * reference, whose FFTW calls are src/wrappers.c:26-96).  mode 1 (the
+ * default there): the z rows with cuFFT's batched 1D transforms and the
+ * strided y and x passes with this library's kernels, the force pass of
+ * Forces (src/auxPM.c:437-555) fused into the inverse passes; mode 0: cuFFT's
+ * 3D plans and the separate force pass.  Both give the same fields up to
+ * float rounding.  Other sizes and batches always use the 3D plans (mode 1
+ * is accepted and has no effect). */
+int mgp_set_fft_mode(mgp_ctx *ctx, int mode);
 /* With mgp_set_timing(ctx, n) for n > 1 the stage events of the last n
  * mgp_step calls are kept: milliseconds of stage `name` in step `step`
  * (counted from that mgp_set_timing call), -1 if not kept or not timed. */

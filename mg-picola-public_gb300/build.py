@@ -22,7 +22,7 @@ LIB = os.path.join(LIBDIR, "libmgpicola.so")
 EXE = os.path.join(LIBDIR, "mgpicola_run")
 EXE_SOURCE = "mgpicola_main.c"
 
-CU_SOURCES = ["mgp_kernels.cu", "mgp_api.cu", "mgp_run.cu", "mgp_noalloc.cu", "mgp_sd.cu", "mgp_nn.cu", "mgp_tiles.cu"]
+CU_SOURCES = ["mgp_kernels.cu", "mgp_api.cu", "mgp_run.cu", "mgp_noalloc.cu", "mgp_sd.cu", "mgp_nn.cu", "mgp_tiles.cu", "mgp_fft.cu"]
 C_SOURCES = ["mgp_cosmo.c", "mgp_param.c", "mgp_io.c"]
 HEADERS = ["mgp_internal.h", "mgp_device.cuh", "mgp_cosmo.h", "mgp_rng.h", "mgp_io.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -144,6 +144,16 @@ extern "C" int mgp_set_particle_order(mgp_ctx *c, int tiles) {
   return MGP_OK;
 }
 
+extern "C" int mgp_set_fft_mode(mgp_ctx *c, int mode) {
+  if (!c) return mgp_set_error(MGP_EINVAL, "null context");
+  if (mode < 0 || mode > 1) return mgp_set_error(MGP_EINVAL, "FFT mode %d (0 or 1)", mode);
+  c->fft_mode = mode;
+  return MGP_OK;
+}
+
+// Whether this context's transforms take the strided passes of mgp_fft.cu.
+static bool own_fft(const mgp_ctx *c) { return c->fft_mode && mgp_fft_supported(c); }
+
 extern "C" int mgp_mark(mgp_ctx *c, int slot) {
   if (!c || slot < 0 || slot > 3) return mgp_set_error(MGP_EINVAL, "mark slot %d out of range", slot);
   MGP_CUDA(cudaEventRecord(c->ev_mark[slot], c->stream));
@@ -365,6 +375,7 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
                           c->plan_c2r_b, c->plan_c2r_frc_b};
   for (int i = 0; i < 7; i++)
     if (plans[i]) cufftDestroy(plans[i]);
+  mgp_fft_free(c);
   mgp_sd_free(c);
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   if (c->graph) cudaGraphDestroy(c->graph);
@@ -439,6 +450,7 @@ static int create_impl(const mgp_params *p, int nbox, const mgp_box_params *boxe
   c->device = device;
   c->tile_mode = nbox == 1;
   c->tile_kick = nbox == 1;
+  c->fft_mode = 1;
   char err[512] = "";
   int rc = mgp_cosmo_init_hooks(&c->cosmo, &c->box_p[0], hooks, err, sizeof(err));
   if (rc) {
@@ -801,13 +813,19 @@ static int fifth_force(mgp_ctx *c, double A, int filtered, int *mg_kind, float *
     if (p->include_screening) {
       double norm = 1.0 / pow((double)N, 3) * 1.5 * p->Omega / A * pow(p->Box / 2997.92458 / (2.0 * M_PI), 2);
       if (!filtered) RET_IF(mgp_launch_div_laplacian(c->dk, c->mg1, N, (float)norm, c->stream));
-      MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+      if (own_fft(c))
+        RET_IF(mgp_fft_c2r(c, c->mg1));
+      else
+        MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
       if (mgp_cosmo_user_screening(&c->cosmo, 0))
         RET_IF(user_screening(c, A, 0, 1.0, nr));
       else
         RET_IF(mgp_launch_screen_potential(c->rho, c->mg1, nr, (float)mgp_phicrit(&c->cosmo, A), c->stream));
     }
-    MGP_CUFFT(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
+    if (own_fft(c))
+      RET_IF(mgp_fft_r2c(c, c->rho, c->rho));
+    else
+      MGP_CUFFT(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
     *mg_kind = 1;
     *coupling = (float)mgp_coupling(&c->cosmo, A);
     *mass2 = (float)(A * A * mgp_mass2_of_a(&c->cosmo, A) / pow(2.0 * M_PI * 2997.92458 / p->Box, 2));
@@ -823,7 +841,10 @@ static int fifth_force(mgp_ctx *c, double A, int filtered, int *mg_kind, float *
     if (!filtered)
       RET_IF(mgp_launch_smooth(c->dk, c->mg1, N, p->smoothing_filter, (float)kR1, (float)(1.0 / pow((double)N, 3)),
                                c->stream));
-    MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+    if (own_fft(c))
+      RET_IF(mgp_fft_c2r(c, c->mg1));
+    else
+      MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
     // Without massive neutrinos delta(k) is the transform of rho itself, so
     // the screening pass writes delta + source, rho (1 + coupling S), and the
     // force pass reads that one spectrum (mg_kind 4) instead of delta(k) and
@@ -836,7 +857,10 @@ static int fifth_force(mgp_ctx *c, double A, int filtered, int *mg_kind, float *
       RET_IF(mgp_launch_screen_density(c->rho, c->mg1, nr, (float)coupling_d,
                                        (float)mgp_dgp_screen_prefactor(&c->cosmo, A), c->stream, 1, NULL,
                                        fold ? 1.0f : 0.0f));
-    MGP_CUFFT(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
+    if (own_fft(c))
+      RET_IF(mgp_fft_r2c(c, c->rho, c->rho));
+    else
+      MGP_CUFFT(cufftExecR2C(c->plan_r2c_ip, (cufftReal *)c->rho, (cufftComplex *)c->rho));
     *mg_kind = fold ? 4 : 2;
   } else if (p->model == MGP_MODEL_BRANSDICKE) {
     // ComputeFifthForce_TimeDepGeffModels (src/mg.h:127-137): the source
@@ -957,7 +981,10 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
 static int fields_from_density(mgp_ctx *c, double A) {
   const int N = c->g.N;
   tstart(c, T_R2C);
-  MGP_CUFFT(cufftExecR2C(c->plan_r2c_oop, (cufftReal *)c->rho, (cufftComplex *)c->dk));
+  if (own_fft(c))
+    RET_IF(mgp_fft_r2c(c, c->rho, c->dk));
+  else
+    MGP_CUFFT(cufftExecR2C(c->plan_r2c_oop, (cufftReal *)c->rho, (cufftComplex *)c->dk));
   tstop(c, T_R2C);
   c->have_density = 1;
   c->last_density_a = A;
@@ -977,6 +1004,14 @@ static int fields_from_density(mgp_ctx *c, double A) {
   RET_IF(fifth_force(c, A, fused, &mg_kind, &coupling, &mass2));
   tstop(c, T_MG);
   // Forces, src/auxPM.c:437-555
+  if (own_fft(c) && !c->closure && (mg_kind == 0 || mg_kind == 3 || mg_kind == 4)) {
+    // one spectrum: the force pass fused into the inverse x and y passes
+    // (mgp_fft.cu); nDGP without screening scales delta by 1 + coupling
+    const float *spec = mg_kind == 4 ? c->rho : c->dk;
+    RET_IF(mgp_fft_forces(c, spec, mg_kind == 3 ? 1.0f + coupling : 1.0f, T_FORCES, T_C2R));
+    c->have_forces = 1;
+    return MGP_OK;
+  }
   tstart(c, T_FORCES);
   if (mg_kind == 4)  // rho holds delta + the fifth-force source
     RET_IF(mgp_launch_forces(c->rho, NULL, 0.f, 0.f, 0, N, c->p.Box, c->frc, c->g.nreal, c->stream));
@@ -989,8 +1024,13 @@ static int fields_from_density(mgp_ctx *c, double A) {
     tstop(c, T_NN);
   }
   tstart(c, T_C2R);
-  for (int g = 0; g < 3; g++)
-    MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(c->frc + g * c->g.nreal), (cufftReal *)(c->frc + g * c->g.nreal)));
+  for (int g = 0; g < 3; g++) {
+    if (own_fft(c))
+      RET_IF(mgp_fft_c2r(c, c->frc + g * c->g.nreal));
+    else
+      MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)(c->frc + g * c->g.nreal),
+                             (cufftReal *)(c->frc + g * c->g.nreal)));
+  }
   tstop(c, T_C2R);
   c->have_forces = 1;
   return MGP_OK;

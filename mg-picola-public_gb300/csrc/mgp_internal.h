@@ -81,6 +81,13 @@ struct mgp_ctx {
   void *fft_work;
   size_t fft_work_bytes;
   cufftHandle plan_r2c_oop, plan_r2c_ip, plan_c2r_1;
+  /* 1024^3 grids (mgp_fft.cu): the y pass by this library's kernel (the
+   * force pass fused into the inverse one), z rows and x lines by cuFFT's
+   * 1D plans.  fft_mode 1 (default where supported) uses them, 0 the 3D
+   * cuFFT plans. */
+  int fft_mode, fft_ready;
+  cufftHandle zplan_r2c_oop, zplan_r2c_ip, zplan_c2r, xplan;
+  float *fft_tw;            /* device: W_1024^m, m = 0..1023 (float2) */
 
   /* P(k) */
   int pk_nbins, pk_bintype, pk_sub;
@@ -268,6 +275,13 @@ typedef struct {
 extern long long g_kernel_launches;
 int mgp_blocks_for(long long n, int per_sm);
 
+/* the y pass of 1024^3 transforms and the fused force pass (mgp_fft.cu) */
+int mgp_fft_supported(const mgp_ctx *c);
+int mgp_fft_setup(mgp_ctx *c);
+void mgp_fft_free(mgp_ctx *c);
+int mgp_fft_r2c(mgp_ctx *c, float *in, float *out);
+int mgp_fft_c2r(mgp_ctx *c, float *grid);
+int mgp_fft_forces(mgp_ctx *c, const float *spec, float mult, int t_x, int t_rest);
 /* learned force closure (mgp_nn.cu): adds its residual to the force grids */
 int mgp_closure_apply(struct mgp_closure *cl, mgp_ctx *c, double A);
 /* waits for a pending snapshot write and frees the output buffers (mgp_destroy) */

@@ -22,7 +22,7 @@ EXPORTS = [
     "mgp_destroy", "mgp_last_error",
     "mgp_displacement_fields", "mgp_get_displacements", "mgp_kick_drift", "mgp_step", "mgp_run", "mgp_pofk",
     "mgp_pofk_total", "mgp_pofk_rsd", "mgp_get_particles", "mgp_set_particles", "mgp_step_host", "mgp_growth", "mgp_Sq",
-    "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_mark", "mgp_mark_ms", "mgp_kernel_ms_step", "mgp_set_particle_order", "mgp_launch_count",
+    "mgp_Sphi", "mgp_power_spectrum", "mgp_cosmo_eval", "mgp_cosmo_coeff", "mgp_copy_grid", "mgp_set_timing", "mgp_kernel_ms", "mgp_mark", "mgp_mark_ms", "mgp_kernel_ms_step", "mgp_set_particle_order", "mgp_set_fft_mode", "mgp_launch_count",
     "mgp_host_register", "mgp_host_unregister", "mgp_host_alloc", "mgp_host_free", "mgp_pofk_noalloc", "mgp_assign_displacement_fields",
     "mgp_growth_scaledependent", "mgp_batch_create", "mgp_batch_run", "mgp_batch_pofk", "mgp_batch_get_particles",
     "mgp_batch_ms", "mgp_batch_graph_nodes", "mgp_batch_graph_kernels", "mgp_batch_set_tuning",
@@ -181,6 +181,7 @@ def lib():
         L.mgp_kernel_ms_step.restype = C.c_double
         L.mgp_mark.argtypes = [vp, C.c_int]
         L.mgp_set_particle_order.argtypes = [vp, C.c_int]
+        L.mgp_set_fft_mode.argtypes = [vp, C.c_int]
         L.mgp_host_alloc.argtypes = [C.POINTER(vp), C.c_size_t]
         L.mgp_host_free.argtypes = [vp]
         L.mgp_mark_ms.argtypes = [vp, C.c_int, C.c_int]
@@ -454,11 +455,13 @@ class Context:
         _check(lib().mgp_step_host(self.h, A, AI, AF, AFF, pos.ctypes.data, vel.ctypes.data, d1.ctypes.data,
                                    d2.ctypes.data, self.np))
 
-    def grid(self, which):
-        n = self.N * self.N * 2 * (self.N // 2 + 1)
+    def grid(self, which, planes=None):
+        """Copy of grid `which` (its first `planes` x planes when given)."""
+        nx = self.N if planes is None else int(planes)
+        n = nx * self.N * 2 * (self.N // 2 + 1)
         out = np.zeros(n, np.float32)
         _check(lib().mgp_copy_grid(self.h, which, out, n))
-        return out.reshape(self.N, self.N, 2 * (self.N // 2 + 1))
+        return out.reshape(nx, self.N, 2 * (self.N // 2 + 1))
 
     def growth(self, which, a):
         return lib().mgp_growth(self.h, which, a)
@@ -491,6 +494,12 @@ class Context:
         rewritten in tile order every step), 1 the tile deposit with the
         arrays in lattice order, 0 the deposit and kick in lattice order."""
         _check(lib().mgp_set_particle_order(self.h, int(tiles)))
+
+    def set_fft_mode(self, mode):
+        """Transforms of a 1024^3 single box (mgp_set_fft_mode): 1 the
+        default, own strided y/x passes with the force pass fused in; 0
+        cuFFT's 3D plans and the separate force pass."""
+        _check(lib().mgp_set_fft_mode(self.h, int(mode)))
 
     def mark(self, slot):
         """Record event `slot` (0..3) on the context's stream."""
