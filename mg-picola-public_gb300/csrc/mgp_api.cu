@@ -812,11 +812,16 @@ static int fifth_force(mgp_ctx *c, double A, int filtered, int *mg_kind, float *
     // ComputeFifthForce_PotentialScreening, src/mg.h:147-189
     if (p->include_screening) {
       double norm = 1.0 / pow((double)N, 3) * 1.5 * p->Omega / A * pow(p->Box / 2997.92458 / (2.0 * M_PI), 2);
-      if (!filtered) RET_IF(mgp_launch_div_laplacian(c->dk, c->mg1, N, (float)norm, c->stream));
-      if (own_fft(c))
-        RET_IF(mgp_fft_c2r(c, c->mg1));
-      else
-        MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+      if (own_fft(c) && !filtered) {
+        // the inverse Laplacian applied in the first inverse pass (mgp_fft.cu)
+        RET_IF(mgp_fft_c2r_filtered(c, c->dk, c->mg1, 2, 0, 0.f, (float)norm));
+      } else {
+        if (!filtered) RET_IF(mgp_launch_div_laplacian(c->dk, c->mg1, N, (float)norm, c->stream));
+        if (own_fft(c))
+          RET_IF(mgp_fft_c2r(c, c->mg1));
+        else
+          MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+      }
       if (mgp_cosmo_user_screening(&c->cosmo, 0))
         RET_IF(user_screening(c, A, 0, 1.0, nr));
       else
@@ -838,13 +843,19 @@ static int fifth_force(mgp_ctx *c, double A, int filtered, int *mg_kind, float *
       return MGP_OK;
     }
     double kR1 = 2.0 * M_PI / p->Box * p->Rsmooth;
-    if (!filtered)
-      RET_IF(mgp_launch_smooth(c->dk, c->mg1, N, p->smoothing_filter, (float)kR1, (float)(1.0 / pow((double)N, 3)),
-                               c->stream));
-    if (own_fft(c))
-      RET_IF(mgp_fft_c2r(c, c->mg1));
-    else
-      MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+    if (own_fft(c) && !filtered) {
+      // the smoothing filter applied in the first inverse pass (mgp_fft.cu)
+      RET_IF(mgp_fft_c2r_filtered(c, c->dk, c->mg1, 1, p->smoothing_filter, (float)kR1,
+                                  (float)(1.0 / pow((double)N, 3))));
+    } else {
+      if (!filtered)
+        RET_IF(mgp_launch_smooth(c->dk, c->mg1, N, p->smoothing_filter, (float)kR1,
+                                 (float)(1.0 / pow((double)N, 3)), c->stream));
+      if (own_fft(c))
+        RET_IF(mgp_fft_c2r(c, c->mg1));
+      else
+        MGP_CUFFT(cufftExecC2R(c->plan_c2r_1, (cufftComplex *)c->mg1, (cufftReal *)c->mg1));
+    }
     // Without massive neutrinos delta(k) is the transform of rho itself, so
     // the screening pass writes delta + source, rho (1 + coupling S), and the
     // force pass reads that one spectrum (mg_kind 4) instead of delta(k) and
@@ -991,8 +1002,10 @@ static int fields_from_density(mgp_ctx *c, double A) {
   int fused = 0;
   if (c->p.pofk_compute_every_step) {
     // with massive neutrinos the fifth-force filter reads the total field:
-    // it is fused into the total P(k) pass instead of the CDM one
-    fused = mg_filter_kind(&c->p);
+    // it is fused into the total P(k) pass instead of the CDM one.  With the
+    // y pass of mgp_fft.cu the filter rides on the first inverse pass of
+    // the solver's transform instead (P(k) then only reads delta(k)).
+    fused = own_fft(c) ? 0 : mg_filter_kind(&c->p);
     tstart(c, T_POFK);
     RET_IF(pofk_now(c, c->cosmo.nu ? 0 : fused, A));
     tstop(c, T_POFK);

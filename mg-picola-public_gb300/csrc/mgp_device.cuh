@@ -83,4 +83,20 @@ __host__ __device__ __forceinline__ int lattice_log2(int Ns) {
   return l;
 }
 
+
+// Fourier-space filter of the fifth-force solvers per integer |k|^2 = rk
+// (grid units): kind 1 SmoothDensityField (src/mg.h:268-309) with the
+// smoothing filters of src/mg.h:318-338 (Gaussian, top-hat, sharp-k), kR =
+// sqrt(rk) kR1, times norm; kind 2 the inverse Laplacian of DivideByLaplacian
+// (src/mg.h:21-64), -norm / rk (0 at k = 0).  filter takes the
+// MGP_FILTER_* values (1 Gaussian, 2 top-hat, 3 sharp-k).
+__device__ __forceinline__ float mg_kfilter(int rk, int kind, int filter, float kR1, float norm) {
+  if (kind == 2) return rk == 0 ? 0.0f : -norm / (float)rk;
+  float kR = sqrtf((float)rk) * kR1, f = 1.0f;
+  if (filter == 1) f = expf(-0.5f * kR * kR);
+  else if (filter == 2) f = kR < 1e-5f ? 1.0f : 3.0f / (kR * kR * kR) * (sinf(kR) - kR * cosf(kR));
+  else if (filter == 3) f = kR < 1.0f ? 1.0f : 0.0f;
+  return f * norm;
+}
+
 #endif

@@ -18,6 +18,12 @@
 //   (The same kernel along x, where a block's rows lie 4.2 MB apart, ran
 //   well below cuFFT's x pass; along y its rows lie 4 KB apart.)
 //
+// The fifth-force solvers' k-space filters (the smoothing of density
+// screening, the inverse Laplacian of potential screening) ride on the first
+// inverse y pass of their transform, so the P(k) pass only reads delta(k);
+// the Gaussian smoothing is a product of per-axis factors (one table of 1024
+// values).
+//
 // The force pass (Forces, src/auxPM.c:437-535) rides on the inverse y pass.
 // F_a(k) = i k_a g(k) S(k), g = -1/(k^2 N^3 Scale), S = delta(k) [+ the MG
 // source].  Along one y line (fixed kx, kz) F_x and F_z are fixed multiples
@@ -36,6 +42,7 @@
 #include <math.h>
 #include <string.h>
 
+#include "mgp_device.cuh"
 #include "mgp_internal.h"
 
 #define RET_IF(x)                  \
@@ -54,7 +61,7 @@ constexpr int FRS = 32 * FW + 8;     // shared-memory row of one k1 (float2), pa
 constexpr int FSMEM = 32 * FRS * 8;  // bytes of the exchange buffer
 constexpr int FBLOCKS = FN * FGR + FN / FW;  // regular groups + Nyquist-column groups
 
-enum { PASS_PLAIN = 0, PASS_FORCE = 1 };
+enum { PASS_PLAIN = 0, PASS_FORCE = 1, PASS_FILTER = 2 };
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -172,14 +179,23 @@ __device__ __forceinline__ void store_column(const float2 (&v)[32], float2 *out,
 //               keeps the kernel within 128 registers).  Phase 0: T =
 //               transform of G = i g S, g = cfac/k^2; fx = k_x T, fz = k_z T.
 //               Phase 1: fy = transform of k_y G.  None of fx, fy, fz is in.
+//   PASS_FILTER: out = DFT(f(|k|^2) in), f = mg_kfilter (the smoothing or
+//               inverse-Laplacian filter of the fifth-force solvers); out is
+//               not in.
+struct yfilter {
+  int kind, filter;  // mg_kfilter's
+  float kR1, norm;
+  const float *gauss;  // Gaussian smoothing: exp(-(kR1 d)^2 / 2) per stored index (d its wave number), or NULL
+};
+
 template <int DIR, int MODE>
 __global__ void __launch_bounds__(FT, 2) k_fft_y(const float2 *in, float2 *out, float2 *fx, float2 *fy, float2 *fz,
-                                                 const float2 *__restrict__ tw, float cfac) {
+                                                 const float2 *__restrict__ tw, float cfac, yfilter yf) {
   extern __shared__ __align__(16) float2 S[];
   constexpr unsigned NH = FN / 2 + 1, OS = FN * NH, ES = NH;
   const int t = threadIdx.x, i = t & 7, b = t >> 3;
-  const int group = MODE == PASS_PLAIN ? (int)blockIdx.x : (int)(blockIdx.x >> 1);
-  const int phase = MODE == PASS_PLAIN ? 0 : (int)(blockIdx.x & 1);
+  const int group = MODE == PASS_FORCE ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+  const int phase = MODE == PASS_FORCE ? (int)(blockIdx.x & 1) : 0;
   int outer, kz;
   unsigned base;
   block_column(group, i, OS, outer, kz, base);
@@ -187,6 +203,27 @@ __global__ void __launch_bounds__(FT, 2) k_fft_y(const float2 *in, float2 *out, 
   if (MODE == PASS_PLAIN) {
 #pragma unroll
     for (int a = 0; a < 32; a++) v[a] = in[base + (unsigned)(32 * a + b) * ES];
+    four_step<DIR>(v, S, tw);
+    store_column(v, out, base, ES, 1.0f, false);
+    return;
+  }
+  if (MODE == PASS_FILTER) {
+    const int dx = wave(outer), r0 = dx * dx + kz * kz;
+#pragma unroll
+    for (int a = 0; a < 32; a++) v[a] = in[base + (unsigned)(32 * a + b) * ES];
+    if (yf.gauss) {
+      // the Gaussian is a product over the axes: norm G(kx) G(kz) per column
+      // times G(ky) per element
+      const float gxz = yf.norm * __ldg(yf.gauss + outer) * __ldg(yf.gauss + kz);
+#pragma unroll
+      for (int a = 0; a < 32; a++) v[a] = cscale(v[a], gxz * __ldg(yf.gauss + 32 * a + b));
+    } else {
+#pragma unroll
+      for (int a = 0; a < 32; a++) {
+        const int dy = wave(32 * a + b);
+        v[a] = cscale(v[a], mg_kfilter(dy * dy + r0, yf.kind, yf.filter, yf.kR1, yf.norm));
+      }
+    }
     four_step<DIR>(v, S, tw);
     store_column(v, out, base, ES, 1.0f, false);
     return;
@@ -215,9 +252,10 @@ __global__ void __launch_bounds__(FT, 2) k_fft_y(const float2 *in, float2 *out, 
 
 template <int DIR, int MODE>
 int launch_y(const float2 *in, float2 *out, float2 *fx, float2 *fy, float2 *fz, const float2 *tw, float cfac,
-             cudaStream_t st) {
+             cudaStream_t st, yfilter yf = yfilter{0, 0, 0.f, 0.f, NULL}) {
   MGP_CUDA(cudaFuncSetAttribute(k_fft_y<DIR, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, FSMEM));
-  k_fft_y<DIR, MODE><<<MODE == PASS_PLAIN ? FBLOCKS : 2 * FBLOCKS, FT, FSMEM, st>>>(in, out, fx, fy, fz, tw, cfac);
+  k_fft_y<DIR, MODE><<<MODE == PASS_FORCE ? 2 * FBLOCKS : FBLOCKS, FT, FSMEM, st>>>(in, out, fx, fy, fz, tw, cfac,
+                                                                                   yf);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -281,7 +319,9 @@ void mgp_fft_free(mgp_ctx *c) {
     if (plans[k]) cufftDestroy(plans[k]);
   c->zplan_r2c_oop = c->zplan_r2c_ip = c->zplan_c2r = c->xplan = 0;
   if (c->fft_tw) cudaFree(c->fft_tw);
+  if (c->fft_gauss) cudaFree(c->fft_gauss);
   c->fft_tw = NULL;
+  c->fft_gauss = NULL;
   c->fft_ready = 0;
 }
 
@@ -305,6 +345,34 @@ int mgp_fft_c2r(mgp_ctx *c, float *grid) {
   MGP_CUFFT(cufftExecC2C(c->xplan, (cufftComplex *)grid, (cufftComplex *)grid, CUFFT_INVERSE));
   RET_IF((launch_y<1, PASS_PLAIN>(g, g, NULL, NULL, NULL, (const float2 *)c->fft_tw, 0.f, c->stream)));
   MGP_CUFFT(cufftExecC2R(c->zplan_c2r, (cufftComplex *)grid, (cufftReal *)grid));
+  return MGP_OK;
+}
+
+// Inverse transform of f(|k|^2) in(k) into `out` (in is kept): the
+// smoothing (kind 1: filter, kR1, norm) or inverse-Laplacian (kind 2: norm)
+// filter of the fifth-force solvers applied in the y pass, then the x lines
+// and z rows of out.
+int mgp_fft_c2r_filtered(mgp_ctx *c, const float *in, float *out, int kind, int filter, float kR1, float norm) {
+  RET_IF(mgp_fft_setup(c));
+  const float *gauss = NULL;
+  if (kind == 1 && filter == MGP_FILTER_GAUSSIAN) {
+    // exp(-(kR1 d)^2 / 2) per stored index, d = its wave number (FP64 on the host)
+    if (!c->fft_gauss) MGP_CUDA(cudaMalloc(&c->fft_gauss, sizeof(float) * FN));
+    if (c->fft_gauss_kR1 != kR1) {
+      float h[FN];
+      for (int i = 0; i < FN; i++) {
+        const double d = i > FN / 2 ? i - FN : i, x = (double)kR1 * d;
+        h[i] = (float)exp(-0.5 * x * x);
+      }
+      MGP_CUDA(cudaMemcpy(c->fft_gauss, h, sizeof(h), cudaMemcpyHostToDevice));
+      c->fft_gauss_kR1 = kR1;
+    }
+    gauss = c->fft_gauss;
+  }
+  RET_IF((launch_y<1, PASS_FILTER>((const float2 *)in, (float2 *)out, NULL, NULL, NULL, (const float2 *)c->fft_tw,
+                                   0.f, c->stream, yfilter{kind, filter, kR1, norm, gauss})));
+  MGP_CUFFT(cufftExecC2C(c->xplan, (cufftComplex *)out, (cufftComplex *)out, CUFFT_INVERSE));
+  MGP_CUFFT(cufftExecC2R(c->zplan_c2r, (cufftComplex *)out, (cufftReal *)out));
   return MGP_OK;
 }
 

@@ -88,6 +88,8 @@ struct mgp_ctx {
   int fft_mode, fft_ready;
   cufftHandle zplan_r2c_oop, zplan_r2c_ip, zplan_c2r, xplan;
   float *fft_tw;            /* device: W_1024^m, m = 0..1023 (float2) */
+  float *fft_gauss;         /* device: Gaussian smoothing factor per stored index (lazy) */
+  float fft_gauss_kR1;      /* the kR1 it was made for */
 
   /* P(k) */
   int pk_nbins, pk_bintype, pk_sub;
@@ -282,6 +284,7 @@ void mgp_fft_free(mgp_ctx *c);
 int mgp_fft_r2c(mgp_ctx *c, float *in, float *out);
 int mgp_fft_c2r(mgp_ctx *c, float *grid);
 int mgp_fft_forces(mgp_ctx *c, const float *spec, float mult, int t_x, int t_rest);
+int mgp_fft_c2r_filtered(mgp_ctx *c, const float *in, float *out, int kind, int filter, float kR1, float norm);
 /* learned force closure (mgp_nn.cu): adds its residual to the force grids */
 int mgp_closure_apply(struct mgp_closure *cl, mgp_ctx *c, double A);
 /* waits for a pending snapshot write and frees the output buffers (mgp_destroy) */

@@ -267,17 +267,7 @@ __global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
         } else {
           bin = a.rk_bin[rk];
         }
-        float f = 0.0f;
-        if (a.fuse_kind == 1) {
-          float kR = sqrtf((float)rk) * a.fuse_a;
-          f = 1.0f;
-          if (a.filter == MGP_FILTER_GAUSSIAN) f = expf(-0.5f * kR * kR);
-          else if (a.filter == MGP_FILTER_TOPHAT) f = kR < 1e-5f ? 1.0f : 3.0f / (kR * kR * kR) * (sinf(kR) - kR * cosf(kR));
-          else if (a.filter == MGP_FILTER_SHARPK) f = kR < 1.0f ? 1.0f : 0.0f;
-          f *= a.fuse_b;
-        } else if (a.fuse_kind == 2) {
-          f = rk == 0 ? 0.0f : -a.fuse_b / (float)rk;
-        }
+        const float f = a.fuse_kind ? mg_kfilter(rk, a.fuse_kind, a.filter, a.fuse_a, a.fuse_b) : 0.0f;
         float2 z[4];
 #pragma unroll
         for (int t = 0; t < 4; t++)
@@ -693,7 +683,7 @@ __global__ void k_div_laplacian(const float2 *__restrict__ dk, float2 *__restric
     int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
     int rk = d0 * d0 + d1 * d1 + kz * kz;
     float2 z = dk[c];
-    float f = rk == 0 ? 0.0f : -norm / (float)rk;
+    const float f = mg_kfilter(rk, 2, 0, 0.0f, norm);
     out[c] = make_float2(f * z.x, f * z.y);
   }
   }
@@ -727,11 +717,7 @@ __global__ void k_smooth(const float2 *__restrict__ dk, float2 *__restrict__ out
     const long long c = r * NH + kz;
     int d0 = i > N / 2 ? N - i : i, d1 = j > N / 2 ? N - j : j;
     int rk = d0 * d0 + d1 * d1 + kz * kz;
-    float kR = sqrtf((float)rk) * kR1, f = 1.0f;
-    if (filter == MGP_FILTER_GAUSSIAN) f = expf(-0.5f * kR * kR);
-    else if (filter == MGP_FILTER_TOPHAT) f = kR < 1e-5f ? 1.0f : 3.0f / (kR * kR * kR) * (sinf(kR) - kR * cosf(kR));
-    else if (filter == MGP_FILTER_SHARPK) f = kR < 1.0f ? 1.0f : 0.0f;
-    f *= norm;
+    const float f = mg_kfilter(rk, 1, filter, kR1, norm);
     float2 z = dk[c];
     out[c] = make_float2(f * z.x, f * z.y);
   }
