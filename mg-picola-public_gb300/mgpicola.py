@@ -452,8 +452,10 @@ class Context:
         _check(lib().mgp_set_particles(self.h, *ptrs, self.np))
 
     def step_host(self, A, AI, AF, AFF, pos, vel, d1, d2):
-        _check(lib().mgp_step_host(self.h, A, AI, AF, AFF, pos.ctypes.data, vel.ctypes.data, d1.ctypes.data,
-                                   d2.ctypes.data, self.np))
+        """Host-buffer step (mgp_step_host).  d1/d2 None: the LPT
+        displacements on the device are kept (they are fixed after the IC)."""
+        ptr = lambda a: None if a is None else a.ctypes.data
+        _check(lib().mgp_step_host(self.h, A, AI, AF, AFF, ptr(pos), ptr(vel), ptr(d1), ptr(d2), self.np))
 
     def grid(self, which, planes=None):
         """Copy of grid `which` (its first `planes` x planes when given)."""

@@ -435,13 +435,16 @@ def test_run_writes_reference_formats(tmp_path):
     assert len(lines) >= 4 and len(lines[0].split()) == 7
 
 
+@pytest.mark.parametrize("lpt_once", [False, True])
 @pytest.mark.parametrize("N,Ns", [(32, 16), (26, 13)])
-def test_step_host_matches_device_step(N, Ns):
+def test_step_host_matches_device_step(N, Ns, lpt_once):
     """mgp_step_host (host buffers: the positions uploaded in chunks, each
     deposited on arrival; velocities and LPT displacements copied on a side
     stream that the kick waits for) against mgp_step on device-resident
     particles from the same state; the CIC's float atomics allow 1e-5 rms.
-    13^3 particles do not split evenly into the upload chunks."""
+    13^3 particles do not split evenly into the upload chunks.  lpt_once:
+    D1, D2 go with the first step only (NULL afterwards keeps the device
+    copy), as a driver does with the fixed LPT displacements."""
     p = params(N, Ns, 128.0, Seed=4242)
     A0 = 1.0 / 20.0
     da = (1.0 - A0) / 5
@@ -450,8 +453,9 @@ def test_step_host_matches_device_step(N, Ns):
         c2.displacement_fields()
         pos, vel, d1, d2 = c1.get_particles()
         A, AI = A0, A0
-        for _ in range(3):
-            c1.step_host(A, AI, A + 0.5 * da, A + da, pos, vel, d1, d2)
+        for i in range(3):
+            keep = lpt_once and i > 0
+            c1.step_host(A, AI, A + 0.5 * da, A + da, pos, vel, None if keep else d1, None if keep else d2)
             c2.step(A, AI, A + 0.5 * da, A + da)
             A, AI = A + da, A + 0.5 * da
         pos2, vel2, _, _ = c2.get_particles()
