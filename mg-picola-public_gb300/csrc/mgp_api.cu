@@ -716,6 +716,7 @@ static int ic_box(mgp_ctx *c, int bx, const double *pos01 = NULL, size_t npos = 
   CK(mgp_launch_ic_readout(g6, gf, N, c->g.P, Ns, c->D1 + po, c->D2 + po, c->partials, nblk, c->stream));
   CK(mgp_launch_ic_finish(c->D1 + po, c->D2 + po, c->s + po, c->v + po, c->np, c->partials, nblk, (float)Di,
                           (float)Di2, (float)vD, (float)vD2, c->stream));
+  c->lpt_ver++;  // new D1/D2
   CKC(cudaMemsetAsync(c->dstate + bx, 0, sizeof(mgp_dstate), c->stream));
   CKC(cudaStreamSynchronize(c->stream));
   c->have_density = c->have_forces = 0;
@@ -1340,6 +1341,7 @@ extern "C" int mgp_set_particles(mgp_ctx *c, const float *pos, const float *vel,
     float *st = q == 0 ? a : b;
     MGP_CUDA(cudaMemcpyAsync(st, srcs[q], bytes, cudaMemcpyHostToDevice, c->stream));
     RET_IF(mgp_launch_aos_to_soa(st, dsts[q], c->np, c->stream));
+    c->lpt_ver++;  // new D1/D2
   }
   MGP_CUDA(cudaStreamSynchronize(c->stream));
   c->have_density = c->have_forces = 0;
@@ -1423,6 +1425,7 @@ extern "C" int mgp_step_host(mgp_ctx *c, double A, double AI, double AF, double 
       if (!src[q]) continue;
       MGP_CUDA(cudaMemcpyAsync(st[1 + q], src[q], bytes, cudaMemcpyHostToDevice, c->side));
       RET_IF(mgp_launch_aos_to_soa(st[1 + q], dst[q], c->np, c->side));
+      if (q > 0) c->lpt_ver++;  // new D1/D2
     }
     MGP_CUDA(cudaEventRecord(c->ev_side[1], c->side));
     c->side_pending = 1;

@@ -180,12 +180,17 @@ struct mgp_ctx {
   int tile_mode;            /* 1 (default): tile deposit where it applies; 0: particle order */
   /* particle arrays held in cell-tile order (single box, scale-independent
    * growth): with tile_kick the kick of every step reads the particles in
-   * the deposit's tile order and writes s, v, D1, D2 in that order (into
-   * the *_alt buffers, then swapped); q[p] is then the lattice point of
+   * the deposit's tile order and writes s, v in that order (into the *_alt
+   * buffers, then swapped); q[p] is then the lattice point of
    * slot p.  Entry points that read or write particles in lattice order
    * first restore it (mgp_particles_canonical). */
   unsigned *q, *q_alt;
-  float *s_alt, *v_alt, *D1_alt, *D2_alt;
+  float *s_alt, *v_alt;
+  /* D1/D2 stay in lattice order; the tile kick reads them packed, 32 bytes
+   * per particle in lattice order (lpt), repacked when lpt_ver (bumped by
+   * every writer of D1/D2) differs from the version packed */
+  float *lpt;
+  long long lpt_ver, lpt_built;
   int permuted, tile_kick;
 
   /* user screening functions: the device copy of the step's table */

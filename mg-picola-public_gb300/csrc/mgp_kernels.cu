@@ -569,9 +569,10 @@ __global__ void __launch_bounds__(MGP_THREADS, 4) k_interp_kick_drift(
       disp[ax] = __ldg(F + o000) * w000 + __ldg(F + o001) * w001 + __ldg(F + o010) * w010 + __ldg(F + o011) * w011 +
                  __ldg(F + o100) * w100 + __ldg(F + o101) * w101 + __ldg(F + o110) * w110 + __ldg(F + o111) * w111;
     }
-    // D1/D2 offsets: the particle index itself for particle arrays
-    // (pitch Ns), the lattice point in the row-padded slot grids otherwise
-    const long long od = a.lpt_pitch == Ns ? p : ((long long)i * Ns + j) * a.lpt_pitch + k;
+    // D1/D2 offsets: the lattice point for particle arrays (pitch Ns; they
+    // stay in lattice order when s and v are in tile order), the lattice
+    // point in the row-padded slot grids otherwise
+    const long long od = a.lpt_pitch == Ns ? lat : ((long long)i * Ns + j) * a.lpt_pitch + k;
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
       long long o = ax * np + p;

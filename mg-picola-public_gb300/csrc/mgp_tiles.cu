@@ -316,12 +316,11 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
   }
 }
 
-// Back to lattice order: the particle of slot j goes to slot q[j].
+// Back to lattice order: the particle of slot j goes to slot q[j] (D1 and
+// D2 are never permuted).
 __global__ void __launch_bounds__(kThreads) k_unpermute(long long np, const float *__restrict__ s,
-                                                        const float *__restrict__ v, const float *__restrict__ D1,
-                                                        const float *__restrict__ D2, const unsigned *__restrict__ q,
-                                                        float *__restrict__ s2, float *__restrict__ v2,
-                                                        float *__restrict__ D12, float *__restrict__ D22) {
+                                                        const float *__restrict__ v, const unsigned *__restrict__ q,
+                                                        float *__restrict__ s2, float *__restrict__ v2) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < np; j += stride) {
     const long long dst = q[j];
@@ -330,9 +329,19 @@ __global__ void __launch_bounds__(kThreads) k_unpermute(long long np, const floa
       const long long o = a * np;
       s2[o + dst] = s[o + j];
       v2[o + dst] = v[o + j];
-      D12[o + dst] = D1[o + j];
-      D22[o + dst] = D2[o + j];
     }
+  }
+}
+
+// The LPT displacements of every particle packed in lattice order, 32 bytes
+// each: (D1x, D1y, D1z, D2x), (D2y, D2z, 0, 0) -- one sector per particle
+// for the tile kick's reads through q.
+__global__ void __launch_bounds__(kThreads) k_pack_lpt(long long np, const float *__restrict__ D1,
+                                                       const float *__restrict__ D2, float4 *__restrict__ lpt) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    lpt[2 * p] = make_float4(D1[p], D1[np + p], D1[2 * np + p], D2[p]);
+    lpt[2 * p + 1] = make_float4(D2[np + p], D2[2 * np + p], 0.0f, 0.0f);
   }
 }
 
@@ -382,18 +391,18 @@ __device__ __forceinline__ int tile_row(int c, int xx, int yy) {
 // shared memory (a base cell outside the tile -- not expected, the key pass
 // rounds identically -- reads the global grids), kicks and drifts as
 // k_interp_kick_drift does (same expressions in the same order), and writes
-// slot j of the output arrays, q2[j] = its lattice point.  D1/D2 are
-// particle arrays (scale-independent growth).  Per-block sums of the
+// slot j of the output arrays (s, v and q2[j] = its lattice point).  D1/D2
+// (scale-independent growth) stay in lattice order, packed 32 bytes per
+// particle in `lpt` and read through the lattice point.  Per-block sums of the
 // interpolated forces and new velocities go to partials for k_finalize_kd.
 // PI: particle-array offset type, 32-bit when 3 np < 2^32 (fewer integer
 // instructions per access); NT: threads per block.
 template <int T, bool P2, typename PI, int NT>
 __global__ void __launch_bounds__(NT) k_ikd_tiles(
     const float *__restrict__ frc, long long gf, int N, long long P, int Ns, int ls, long long np,
-    const float *__restrict__ s, const float *__restrict__ v, const float *__restrict__ D1,
-    const float *__restrict__ D2, const unsigned *__restrict__ q, const unsigned *__restrict__ off,
-    const unsigned *__restrict__ order, int ntile1, const mgp_dstate *__restrict__ st, float *__restrict__ s2,
-    float *__restrict__ v2, float *__restrict__ D12, float *__restrict__ D22, unsigned *__restrict__ q2,
+    const float *__restrict__ s, const float *__restrict__ v, const float4 *__restrict__ lpt,
+    const unsigned *__restrict__ q, const unsigned *__restrict__ off, const unsigned *__restrict__ order, int ntile1,
+    const mgp_dstate *__restrict__ st, float *__restrict__ s2, float *__restrict__ v2, unsigned *__restrict__ q2,
     double *__restrict__ partials, mgp_kd_args a) {
   using FT = force_tile<T>;
   constexpr int X = FT::X, R = FT::R, COMP = FT::COMP, K = FT::PIECES;
@@ -440,6 +449,8 @@ __global__ void __launch_bounds__(NT) k_ikd_tiles(
       const PI p = (PI)order[j];
       const unsigned lat = q ? q[p] : (unsigned)p;
       const float sp[3] = {s[p], s[npi + p], s[2 * npi + p]};
+      const float4 l0 = lpt[2 * (size_t)lat], l1 = lpt[2 * (size_t)lat + 1];
+      const float D1p[3] = {l0.x, l0.y, l0.z}, D2p[3] = {l0.w, l1.x, l1.y};
       int ix, iy, iz;
       float DX, DY, DZ;
       cell_of<P2>(sp[0], sp[1], sp[2], lat, Ns, ls, inv_ns, N, a.scale, ox, oy, oz, ix, iy, iz, DX, DY, DZ);
@@ -473,12 +484,10 @@ __global__ void __launch_bounds__(NT) k_ikd_tiles(
 #pragma unroll
       for (int ax = 0; ax < 3; ax++) {
         const PI o = (PI)ax * npi, oj = o + (PI)j;
-        const float d1 = D1[o + p], d2 = D2[o + p];
+        const float d1 = D1p[ax], d2 = D2p[ax];
         const float vn = v[o + p] + a.kick_disp * disp[ax] + a.kick_d1 * d1 + a.kick_d2 * d2;
         v2[oj] = vn;
         s2[oj] = a.do_drift ? sp[ax] + vn * a.dyyy + a.dD1 * d1 + a.dD2 * d2 : sp[ax];
-        D12[oj] = d1;
-        D22[oj] = d2;
         accD[ax] += disp[ax];
         accV[ax] += vn;
       }
@@ -547,12 +556,13 @@ int mgp_tiles_alloc(mgp_ctx *c, int T) {
 
 void mgp_tiles_free(mgp_ctx *c) {
   void *b[] = {c->tile_of, c->tile_order, c->tile_count, c->tile_off, c->tile_cursor, c->tile_bsum,
-               c->q, c->q_alt, c->s_alt, c->v_alt, c->D1_alt, c->D2_alt};
+               c->q, c->q_alt, c->s_alt, c->v_alt, c->lpt};
   for (void *x : b)
     if (x) cudaFree(x);
   c->tile_of = c->tile_order = c->tile_count = c->tile_off = c->tile_cursor = c->tile_bsum = NULL;
   c->q = c->q_alt = NULL;
-  c->s_alt = c->v_alt = c->D1_alt = c->D2_alt = NULL;
+  c->s_alt = c->v_alt = c->lpt = NULL;
+  c->lpt_built = -1;
   c->tile_ready = 0;
   c->tile_cap = 0;
   c->permuted = 0;
@@ -562,8 +572,6 @@ static void swap_arrays(mgp_ctx *c) {
   float *t;
   t = c->s; c->s = c->s_alt; c->s_alt = t;
   t = c->v; c->v = c->v_alt; c->v_alt = t;
-  t = c->D1; c->D1 = c->D1_alt; c->D1_alt = t;
-  t = c->D2; c->D2 = c->D2_alt; c->D2_alt = t;
 }
 
 // Lattice order of the particle arrays (the particle of slot j to slot
@@ -572,8 +580,7 @@ static void swap_arrays(mgp_ctx *c) {
 int mgp_particles_canonical(mgp_ctx *c) {
   c->tile_ready = 0;
   if (!c->permuted) return MGP_OK;
-  k_unpermute<<<mgp_blocks_for(c->np, 8), kThreads, 0, c->stream>>>(c->np, c->s, c->v, c->D1, c->D2, c->q, c->s_alt,
-                                                                    c->v_alt, c->D1_alt, c->D2_alt);
+  k_unpermute<<<mgp_blocks_for(c->np, 8), kThreads, 0, c->stream>>>(c->np, c->s, c->v, c->q, c->s_alt, c->v_alt);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   swap_arrays(c);
@@ -659,10 +666,17 @@ int mgp_ikd_tiles(mgp_ctx *c, const mgp_kd_args *a, int *nblocks_out) {
   if (!c->s_alt) {
     MGP_CUDA(cudaMalloc(&c->s_alt, bytes));
     MGP_CUDA(cudaMalloc(&c->v_alt, bytes));
-    MGP_CUDA(cudaMalloc(&c->D1_alt, bytes));
-    MGP_CUDA(cudaMalloc(&c->D2_alt, bytes));
     MGP_CUDA(cudaMalloc(&c->q, sizeof(unsigned) * (size_t)c->np));
     MGP_CUDA(cudaMalloc(&c->q_alt, sizeof(unsigned) * (size_t)c->np));
+    MGP_CUDA(cudaMalloc(&c->lpt, sizeof(float) * 8 * (size_t)c->np));
+    c->lpt_built = -1;
+  }
+  if (c->lpt_built != c->lpt_ver) {
+    // D1/D2 changed since the last pack (IC, or set by the caller)
+    k_pack_lpt<<<mgp_blocks_for(c->np, 8), kThreads, 0, c->stream>>>(c->np, c->D1, c->D2, (float4 *)c->lpt);
+    MGP_CHECK_LAUNCH();
+    g_kernel_launches++;
+    c->lpt_built = c->lpt_ver;
   }
   const int T = c->tile_side, nt1 = c->tile_n1, N = c->g.N, Ns = c->Ns;
   const int ls = lattice_log2(Ns);
@@ -681,10 +695,9 @@ int mgp_ikd_tiles(mgp_ctx *c, const mgp_kd_args *a, int *nblocks_out) {
     MGP_CUDA(cudaFuncSetAttribute(k_ikd_tiles<TT, PP, PI, NTT>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                   (int)smem));                                                                \
     k_ikd_tiles<TT, PP, PI, NTT><<<nb, NTT, smem, c->stream>>>(c->frc, c->g.nreal, N, c->g.P, Ns, ls, c->np,  \
-                                                               c->s, c->v, c->D1, c->D2, qp, c->tile_off,     \
-                                                               c->tile_order, nt1, c->dstate, c->s_alt,       \
-                                                               c->v_alt, c->D1_alt, c->D2_alt, c->q_alt,      \
-                                                               c->partials, *a);                              \
+                                                               c->s, c->v, (const float4 *)c->lpt, qp,        \
+                                                               c->tile_off, c->tile_order, nt1, c->dstate,    \
+                                                               c->s_alt, c->v_alt, c->q_alt, c->partials, *a); \
   } while (0)
   const bool narrow = 3 * c->np < 0xffffffffLL;
   if (T == 16 && ls >= 0 && narrow)
