@@ -174,7 +174,7 @@ struct mgp_ctx {
    * particle, particle indices bucketed by tile, tile counts / offsets /
    * scatter cursors, scan block totals */
   unsigned *tile_of, *tile_order, *tile_count, *tile_off, *tile_cursor, *tile_bsum;
-  int tile_side, tile_n1, tile_ready;
+  int tile_side, tile_n1, tile_nz, tile_ready;  /* shape code, tiles along x and y, along z */
   long long tile_cap;       /* tiles the count/offset arrays hold */
   int batch_tile;           /* batch deposit: tile side (8, 16) or 0 for the lattice-order deposit */
   int tile_mode;            /* 1 (default): tile deposit where it applies; 0: particle order */

@@ -2,8 +2,8 @@
 // step (sm_103a).
 //
 // The particle arrays stay in Lagrangian (lattice) order.  Once per step,
-// before the deposit, the particles are counted and bucketed by the T^3-cell
-// tile of their CIC base cell (a counting sort of the particle indices, 8
+// before the deposit, the particles are counted and bucketed by the
+// TX x TX x TZ-cell tile of their CIC base cell (a counting sort of the particle indices, 8
 // bytes per particle of traffic besides one read of the displacements):
 //   k_tile_key      tile of every particle, tile counts (warp-aggregated)
 //   k_scan_*        exclusive prefix sum of the counts = tile offsets
@@ -72,16 +72,23 @@ __device__ __forceinline__ void particle_cell(const float *__restrict__ s, long 
   cell_of<P2>(s[p], s[np + p], s[2 * np + p], lat, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY, DZ);
 }
 
-// The L-th tile of a kernel's sweep: with nt1 a multiple of 8 the tiles go
-// in blocks of 8^3 (the blocks, and the tiles inside one, in x, y, z
-// order), so that the tiles in flight at one time are neighbours and the
-// grid lines and particles they share are found in L2; else in index order.
-__device__ __forceinline__ int tile_at(int L, int nt1) {
-  if (nt1 & 7) return L;
-  const int ns = nt1 >> 3, sup = L >> 9, w = L & 511;
-  const int sx = sup / (ns * ns), sy = (sup / ns) % ns, sz = sup % ns;
+// Tile shapes: T = 8 and 16 are cubic tiles of T^3 cells; T = 64 (kElong)
+// is 8 x 8 x 64 cells, whose rows of 64 cells (256 bytes) make the deposit's
+// flush and the kick's force staging move long contiguous pieces.
+constexpr int kElong = 64;
+__host__ __device__ constexpr int tile_tx(int T) { return T == kElong ? 8 : T; }
+
+// The L-th tile of a kernel's sweep over an ntx x ntx x ntz tile grid: with
+// ntx and ntz multiples of 8 the tiles go in blocks of 8^3 tiles (the
+// blocks, and the tiles inside one, in x, y, z order), so that the tiles in
+// flight at one time are neighbours and the grid lines and particles they
+// share are found in L2; else in index order.
+__device__ __forceinline__ int tile_at(int L, int ntx, int ntz) {
+  if ((ntx & 7) || (ntz & 7)) return L;
+  const int gx = ntx >> 3, gz = ntz >> 3, sup = L >> 9, w = L & 511;
+  const int sx = sup / (gx * gz), sy = (sup / gz) % gx, sz = sup % gz;
   const int tx = (sx << 3) + (w >> 6), ty = (sy << 3) + ((w >> 3) & 7), tz = (sz << 3) + (w & 7);
-  return (tx * nt1 + ty) * nt1 + tz;
+  return (tx * ntx + ty) * ntz + tz;
 }
 
 // Asynchronous 16-byte global -> shared copies (cp.async, cached in L2
@@ -97,13 +104,13 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // a warp can merge their count increments per tile.
 template <bool P2>
 __global__ void __launch_bounds__(kThreads) k_tile_key(const float *__restrict__ s, const mgp_dstate *__restrict__ st,
-                                                       long long np, int Ns, int ls, int N, float scale, int tshift,
-                                                       int ntile1, const unsigned *__restrict__ q,
+                                                       long long np, int Ns, int ls, int N, float scale, int sx,
+                                                       int sz, int ntx, int ntz, const unsigned *__restrict__ q,
                                                        unsigned *__restrict__ tile_of,
                                                        unsigned *__restrict__ count) {
   // box blockIdx.y of a batch: particles 3 np apart, its tiles after those
   // of the boxes before it, tile_of indexed by the particle's global index
-  const unsigned box = blockIdx.y, ntiles = (unsigned)ntile1 * ntile1 * ntile1;
+  const unsigned box = blockIdx.y, ntiles = (unsigned)ntx * ntx * ntz;
   s += (long long)box * 3 * np;
   st += box;
   tile_of += (long long)box * np;
@@ -120,9 +127,8 @@ __global__ void __launch_bounds__(kThreads) k_tile_key(const float *__restrict__
     float DX, DY, DZ;
     particle_cell<P2>(s, np, p, q ? q[p] : (unsigned)p, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY,
                       DZ);
-    const unsigned t = box * ntiles +
-                       ((unsigned)(ix >> tshift) * (unsigned)ntile1 + (unsigned)(iy >> tshift)) * (unsigned)ntile1 +
-                       (unsigned)(iz >> tshift);
+    const unsigned t = box * ntiles + ((unsigned)(ix >> sx) * (unsigned)ntx + (unsigned)(iy >> sx)) * (unsigned)ntz +
+                       (unsigned)(iz >> sz);
     tile_of[p] = t;
     const unsigned same = __match_any_sync(am, t);
     if (lane == __ffs(same) - 1) atomicAdd(count + t, (unsigned)__popc(same));
@@ -230,31 +236,32 @@ __global__ void __launch_bounds__(kThreads) k_tile_scatter(const unsigned *__res
 
 // PtoMesh (src/auxPM.c:280-357) per tile: the weights of the tile's
 // particles (WPAR = (N/Ns)^3 folded into the y factors, auxPM.c:316-317) are
-// summed in shared memory over the tile and its +1 halo, [T+1][T+1][T+2]
-// floats (the z rows padded to an even length), and the copy is added to the
-// mesh (pre-set to -1) with one float2 reduction per pair of cells in z,
-// skipping pairs that received nothing.  Mesh rows have even length and z0
-// is a multiple of T, so every pair is 8-byte aligned; with N a multiple of
-// T a pair never straddles the periodic wrap.
+// summed in shared memory over the tile (TX x TX x TZ cells, tile_tx) and
+// its +1 halo, [TX+1][TX+1][TZ+2] floats (the z rows padded to an even
+// length), and the copy is added to the mesh (pre-set to -1) with one float2
+// reduction per pair of cells in z, skipping pairs that received nothing.
+// Mesh rows have even length and z0 is a multiple of TZ, so every pair is
+// 8-byte aligned; with N a multiple of TZ a pair never straddles the
+// periodic wrap.
 template <int T, bool P2>
 __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict__ s, const mgp_dstate *__restrict__ st,
                                                         long long np, int Ns, int ls, int N, float scale, float wpar,
                                                         float *__restrict__ rho, long long P,
                                                         const unsigned *__restrict__ off,
                                                         const unsigned *__restrict__ order,
-                                                        const unsigned *__restrict__ q, int ntile1, int nbox,
+                                                        const unsigned *__restrict__ q, int ntx, int ntz, int nbox,
                                                         long long g_bs) {
-  constexpr int BX = T + 1, BZ = T + 2, BOX = BX * BX * BZ;
+  constexpr int KX = tile_tx(T), KZ = T, BX = KX + 1, BZ = KZ + 2, BOX = BX * BX * BZ;
   __shared__ float box[BOX];
   const float inv_ns = 1.0f / (float)Ns;
-  const int ntiles = ntile1 * ntile1 * ntile1;
+  const int ntiles = ntx * ntx * ntz;
   const float *s0 = s;
   const mgp_dstate *st0 = st;
   float *rho0 = rho;
   for (int L = blockIdx.x; L < ntiles * nbox; L += gridDim.x) {
     // box ib of a batch: particles 3 np apart, grids g_bs floats apart; the
     // order holds global particle indices ib np + p
-    const int ib = L / ntiles, tile = tile_at(L - ib * ntiles, ntile1), gtile = ib * ntiles + tile;
+    const int ib = L / ntiles, tile = tile_at(L - ib * ntiles, ntx, ntz), gtile = ib * ntiles + tile;
     const unsigned j0 = off[gtile], j1 = off[gtile + 1];
     if (j0 == j1) continue;
     s = s0 + (long long)ib * 3 * np;
@@ -262,8 +269,8 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
     rho = rho0 + (long long)ib * g_bs;
     const long long pbase = (long long)ib * np;
     const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
-    const int tz = tile % ntile1, ty = (tile / ntile1) % ntile1, tx = tile / (ntile1 * ntile1);
-    const int x0 = tx * T, y0 = ty * T, z0 = tz * T;
+    const int tz = tile % ntz, ty = (tile / ntz) % ntx, tx = tile / (ntz * ntx);
+    const int x0 = tx * KX, y0 = ty * KX, z0 = tz * KZ;
     for (int e = threadIdx.x; e < BOX; e += blockDim.x) box[e] = 0.0f;
     __syncthreads();
     for (unsigned j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
@@ -275,7 +282,7 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
       const float TX = 1.0f - DX, TY = (1.0f - DY) * wpar, TZ = 1.0f - DZ;
       DY *= wpar;
       const int lx = ix - x0, ly = iy - y0, lz = iz - z0;
-      if ((unsigned)lx >= (unsigned)T || (unsigned)ly >= (unsigned)T || (unsigned)lz >= (unsigned)T) {
+      if ((unsigned)lx >= (unsigned)KX || (unsigned)ly >= (unsigned)KX || (unsigned)lz >= (unsigned)KZ) {
         // a base cell outside the tile (the key pass rounded differently):
         // straight to the mesh
         const int ixn = ix + 1 == N ? 0 : ix + 1, iyn = iy + 1 == N ? 0 : iy + 1, izn = iz + 1 == N ? 0 : iz + 1;
@@ -358,18 +365,19 @@ __device__ __forceinline__ double block_sum_tiles(double x, double *sh) {
   return t;
 }
 
-// Force tile in shared memory: three components, each (T+1)^2 rows of
-// R = T + 4 floats.  A grid row (x, y) of N + 2 floats starts on a 16-byte
-// boundary when y is even and 8 bytes past one when y is odd, so row
-// (xx, yy) of the tile is copied as R/4 16-byte pieces from z0 (yy even) or
-// z0 - 2 (yy odd): the tile's z0..z0+T then sit at offset 2 (yy & 1) of the
-// row.  The copied run stays inside the grids: an odd row's starts 2 floats
+// Force tile in shared memory: three components, each (TX+1)^2 rows of
+// R = TZ + 4 floats (tile shape TX x TX x TZ, tile_tx).  A grid row (x, y)
+// of N + 2 floats starts on a 16-byte boundary when y is even and 8 bytes
+// past one when y is odd, so row (xx, yy) of the tile is copied as R/4
+// 16-byte pieces from z0 (yy even) or z0 - 2 (yy odd): the tile's
+// z0..z0+TZ then sit at offset 2 (yy & 1) of the row.  The copied run stays inside the grids: an odd row's starts 2 floats
 // into the previous row's padding, an even row's ends at most 2 floats into
 // the next row (y <= N - 2).  The z halo of the last tile in z lands in the
 // row padding and is patched from z = 0.
 template <int T>
 struct force_tile {
-  static constexpr int X = T + 1, R = T + 4, COMP = X * X * R, FLOATS = 3 * COMP;
+  static constexpr int TX = tile_tx(T), TZ = T;
+  static constexpr int X = TX + 1, R = TZ + 4, COMP = X * X * R, FLOATS = 3 * COMP;
   static constexpr int PIECES = R / 4;  // 16-byte copies per row
 };
 
@@ -401,11 +409,12 @@ template <int T, bool P2, typename PI, int NT>
 __global__ void __launch_bounds__(NT) k_ikd_tiles(
     const float *__restrict__ frc, long long gf, int N, long long P, int Ns, int ls, long long np,
     const float *__restrict__ s, const float *__restrict__ v, const float4 *__restrict__ lpt,
-    const unsigned *__restrict__ q, const unsigned *__restrict__ off, const unsigned *__restrict__ order, int ntile1,
+    const unsigned *__restrict__ q, const unsigned *__restrict__ off, const unsigned *__restrict__ order, int ntx,
+    int ntz,
     const mgp_dstate *__restrict__ st, float *__restrict__ s2, float *__restrict__ v2, unsigned *__restrict__ q2,
     double *__restrict__ partials, mgp_kd_args a) {
   using FT = force_tile<T>;
-  constexpr int X = FT::X, R = FT::R, COMP = FT::COMP, K = FT::PIECES;
+  constexpr int X = FT::X, R = FT::R, COMP = FT::COMP, K = FT::PIECES, KX = FT::TX, KZ = FT::TZ;
   constexpr int ROWS = NT / K;  // rows copied per pass of the block
   extern __shared__ __align__(16) float fs[];  // FT::FLOATS
   __shared__ double sh[NT / 32];
@@ -413,14 +422,14 @@ __global__ void __launch_bounds__(NT) k_ikd_tiles(
   const int sub = threadIdx.x / K, k = threadIdx.x - sub * K;  // this thread's row in a pass, its piece
   const float ox = (float)(st->cx[0] * a.scale), oy = (float)(st->cx[1] * a.scale), oz = (float)(st->cx[2] * a.scale);
   const float inv_ns = 1.0f / (float)Ns;
-  const int ntiles = ntile1 * ntile1 * ntile1;
+  const int ntiles = ntx * ntx * ntz;
   float accD[3] = {0.f, 0.f, 0.f}, accV[3] = {0.f, 0.f, 0.f};
   for (int L = blockIdx.x; L < ntiles; L += gridDim.x) {
-    const int tile = tile_at(L, ntile1);
+    const int tile = tile_at(L, ntx, ntz);
     const unsigned j0 = off[tile], j1 = off[tile + 1];
     if (j0 == j1) continue;
-    const int tz = tile % ntile1, ty = (tile / ntile1) % ntile1, tx = tile / (ntile1 * ntile1);
-    const int x0 = tx * T, y0 = ty * T, z0 = tz * T;
+    const int tz = tile % ntz, ty = (tile / ntz) % ntx, tx = tile / (ntz * ntx);
+    const int x0 = tx * KX, y0 = ty * KX, z0 = tz * KZ;
     __syncthreads();  // the previous tile's reads of fs and rowoff are done
     for (int r = threadIdx.x; r < X * X; r += NT) {
       const int xx = r / X, yy = r - xx * X;
@@ -436,11 +445,11 @@ __global__ void __launch_bounds__(NT) k_ikd_tiles(
     }
     cp_async_wait_all();
     __syncthreads();
-    if (z0 + T == N) {
-      // last tile in z: the halo column z0 + T is z = 0 of the same row
+    if (z0 + KZ == N) {
+      // last tile in z: the halo column z0 + KZ is z = 0 of the same row
       for (int r = threadIdx.x; r < 3 * X * X; r += NT) {
         const int c = r / (X * X), rr = r - c * X * X, yy = rr % X;
-        fs[c * COMP + rr * R + 2 * (yy & 1) + T] = frc[c * gf + rowoff[rr] + 2 * (yy & 1) - z0];
+        fs[c * COMP + rr * R + 2 * (yy & 1) + KZ] = frc[c * gf + rowoff[rr] + 2 * (yy & 1) - z0];
       }
       __syncthreads();
     }
@@ -459,7 +468,7 @@ __global__ void __launch_bounds__(NT) k_ikd_tiles(
       const float w100 = DX * TY * TZ, w101 = DX * TY * DZ, w110 = DX * DY * TZ, w111 = DX * DY * DZ;
       const int lx = ix - x0, ly = iy - y0, lz = iz - z0;
       float disp[3];
-      if ((unsigned)lx < (unsigned)T && (unsigned)ly < (unsigned)T && (unsigned)lz < (unsigned)T) {
+      if ((unsigned)lx < (unsigned)KX && (unsigned)ly < (unsigned)KX && (unsigned)lz < (unsigned)KZ) {
         // row (lx, ly + 1) is in the other parity's box
         const float *f = fs + tile_row<T>(0, lx, ly) + lz;
         const int dy = R + ((ly & 1) ? -2 : 2), dx = X * R;
@@ -505,22 +514,27 @@ __global__ void __launch_bounds__(NT) k_ikd_tiles(
 
 }  // namespace
 
-// Tile side in cells for the tile path, or 0 when it does not apply (the
-// mesh must split into whole tiles and the indices fit 32 bits).
+// Tile shape of the single-box tile path, or 0 when it does not apply (the
+// mesh must split into whole tiles and the indices fit 32 bits): 8 x 8 x 64
+// cells (kElong) for meshes of 512 and more (rows of 256 bytes in the
+// deposit's flush and the kick's staging), else 16^3 or 8^3.
 int mgp_tile_side(int N, long long np) {
   if (np <= 0 || np > 0xffffffffLL) return 0;
+  if (N >= 512 && N % kElong == 0) return kElong;
   if (N >= 64 && N % 16 == 0) return 16;
   if (N >= 16 && N % 8 == 0) return 8;
   return 0;
 }
 
-// Whether the tile deposit of side T (8 or 16) applies to the context's
-// boxes: whole tiles, particle indices of all boxes in 32 bits, the tiles of
-// all boxes within the two-level scan (kScanChunk^2).
+// Whether the tile deposit of shape T (8 or 16: T^3 cells; kElong: 8 x 8 x
+// 64) applies to the context's boxes: whole tiles, particle indices of all
+// boxes in 32 bits, the tiles of all boxes within the two-level scan
+// (kScanChunk^2).
 int mgp_tiles_check(const mgp_ctx *c, int T) {
-  if (T != 8 && T != 16) return mgp_set_error(MGP_EINVAL, "tile side %d (8 or 16)", T);
-  if (c->g.N % T) return mgp_set_error(MGP_EINVAL, "tile side %d does not divide Nmesh = %d", T, c->g.N);
-  const long long nt1 = c->g.N / T, ntiles = nt1 * nt1 * nt1 * c->nbox, nall = c->np * c->nbox;
+  if (T != 8 && T != 16 && T != kElong) return mgp_set_error(MGP_EINVAL, "tile shape %d (8, 16 or %d)", T, kElong);
+  if (c->g.N % T) return mgp_set_error(MGP_EINVAL, "tile shape %d does not divide Nmesh = %d", T, c->g.N);
+  const long long ntx = c->g.N / tile_tx(T), ntz = c->g.N / T;
+  const long long ntiles = ntx * ntx * ntz * c->nbox, nall = c->np * c->nbox;
   if (nall > 0xffffffffLL) return mgp_set_error(MGP_EINVAL, "%lld particles exceed 32-bit indices", nall);
   if (ntiles > (long long)kScanChunk * kScanChunk)
     return mgp_set_error(MGP_EINVAL, "%lld tiles exceed the scan's capacity", ntiles);
@@ -532,8 +546,8 @@ int mgp_tiles_check(const mgp_ctx *c, int T) {
 int mgp_tiles_alloc(mgp_ctx *c, int T) {
   int rc = mgp_tiles_check(c, T);
   if (rc != MGP_OK) return rc;
-  const int nt1 = c->g.N / T;
-  const long long ntiles = (long long)nt1 * nt1 * nt1 * c->nbox, nall = c->np * c->nbox;
+  const int nt1 = c->g.N / tile_tx(T), ntz = c->g.N / T;
+  const long long ntiles = (long long)nt1 * nt1 * ntz * c->nbox, nall = c->np * c->nbox;
   const long long nblk = (ntiles + kScanChunk - 1) / kScanChunk;
   if (!c->tile_order) {
     MGP_CUDA(cudaMalloc(&c->tile_of, sizeof(unsigned) * (size_t)nall));
@@ -551,6 +565,7 @@ int mgp_tiles_alloc(mgp_ctx *c, int T) {
   }
   c->tile_side = T;
   c->tile_n1 = nt1;
+  c->tile_nz = ntz;
   return MGP_OK;
 }
 
@@ -593,20 +608,21 @@ int mgp_particles_canonical(mgp_ctx *c) {
 int mgp_tiles_sort(mgp_ctx *c, int T) {
   int rc = mgp_tiles_alloc(c, T);
   if (rc != MGP_OK) return rc;
-  const int N = c->g.N, Ns = c->Ns, nt1 = c->tile_n1, B = c->nbox;
-  const long long ntiles = (long long)nt1 * nt1 * nt1 * B, nall = c->np * B;
+  const int N = c->g.N, Ns = c->Ns, nt1 = c->tile_n1, ntz = c->tile_nz, B = c->nbox;
+  const long long ntiles = (long long)nt1 * nt1 * ntz * B, nall = c->np * B;
   const int ls = lattice_log2(Ns);
   const float scale = (float)(N / c->p.Box);
-  int tshift = 0;
-  while ((1 << tshift) < T) tshift++;
+  int sx = 0, sz = 0;
+  while ((1 << sx) < tile_tx(T)) sx++;
+  while ((1 << sz) < T) sz++;
   const unsigned *qp = c->permuted ? c->q : NULL;
   MGP_CUDA(cudaMemsetAsync(c->tile_count, 0, sizeof(unsigned) * (size_t)ntiles, c->stream));
   const dim3 gk(mgp_blocks_per_box(c->np, 8, B), B);
   if (ls >= 0)
-    k_tile_key<true><<<gk, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, tshift, nt1, qp,
+    k_tile_key<true><<<gk, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, sx, sz, nt1, ntz, qp,
                                                      c->tile_of, c->tile_count);
   else
-    k_tile_key<false><<<gk, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, tshift, nt1, qp,
+    k_tile_key<false><<<gk, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, sx, sz, nt1, ntz, qp,
                                                       c->tile_of, c->tile_count);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
@@ -633,23 +649,27 @@ int mgp_tiles_sort(mgp_ctx *c, int T) {
 // resident blocks per SM of the launch (0: the default budget).
 int mgp_cic_tiles(mgp_ctx *c, float wpar, int per_sm) {
   const unsigned *ord = c->tile_order, *qp = c->permuted ? c->q : NULL;
-  const int N = c->g.N, Ns = c->Ns, T = c->tile_side, nt1 = c->tile_n1, B = c->nbox;
+  const int N = c->g.N, Ns = c->Ns, T = c->tile_side, nt1 = c->tile_n1, ntz = c->tile_nz, B = c->nbox;
   const long long gbs = c->g.nreal;
   const int ls = lattice_log2(Ns);
   const float scale = (float)(N / c->p.Box);
-  const int nb = mgp_blocks_for((long long)nt1 * nt1 * nt1 * B * kThreads, per_sm > 0 ? per_sm : 8);
-  if (T == 16 && ls >= 0)
-    k_cic_tiles<16, true><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                          c->g.P, c->tile_off, ord, qp, nt1, B, gbs);
+  const int nb = mgp_blocks_for((long long)nt1 * nt1 * ntz * B * kThreads, per_sm > 0 ? per_sm : 8);
+#define MGP_CIC_TILES(TT, PP)                                                                                 \
+  k_cic_tiles<TT, PP><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho, \
+                                                      c->g.P, c->tile_off, ord, qp, nt1, ntz, B, gbs)
+  if (T == kElong && ls >= 0)
+    MGP_CIC_TILES(kElong, true);
+  else if (T == kElong)
+    MGP_CIC_TILES(kElong, false);
+  else if (T == 16 && ls >= 0)
+    MGP_CIC_TILES(16, true);
   else if (T == 16)
-    k_cic_tiles<16, false><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                           c->g.P, c->tile_off, ord, qp, nt1, B, gbs);
+    MGP_CIC_TILES(16, false);
   else if (ls >= 0)
-    k_cic_tiles<8, true><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                         c->g.P, c->tile_off, ord, qp, nt1, B, gbs);
+    MGP_CIC_TILES(8, true);
   else
-    k_cic_tiles<8, false><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho,
-                                                          c->g.P, c->tile_off, ord, qp, nt1, B, gbs);
+    MGP_CIC_TILES(8, false);
+#undef MGP_CIC_TILES
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   return MGP_OK;
@@ -678,29 +698,35 @@ int mgp_ikd_tiles(mgp_ctx *c, const mgp_kd_args *a, int *nblocks_out) {
     g_kernel_launches++;
     c->lpt_built = c->lpt_ver;
   }
-  const int T = c->tile_side, nt1 = c->tile_n1, N = c->g.N, Ns = c->Ns;
+  const int T = c->tile_side, nt1 = c->tile_n1, ntz = c->tile_nz, N = c->g.N, Ns = c->Ns;
   const int ls = lattice_log2(Ns);
-  const long long ntiles = (long long)nt1 * nt1 * nt1;
+  const long long ntiles = (long long)nt1 * nt1 * ntz;
   const unsigned *qp = c->permuted ? c->q : NULL;
-  // 16^3 tiles: 62 KB of forces per block, three blocks of 256 threads per
-  // SM; 8^3 tiles: 10 KB, eight blocks per SM
-  const size_t smem = sizeof(float) * (T == 16 ? force_tile<16>::FLOATS : force_tile<8>::FLOATS);
-  constexpr int NT16 = 256, NT8 = 256;
-  const int nt = T == 16 ? NT16 : NT8;
-  int nb = mgp_blocks_for(ntiles * nt, T == 16 ? 3 : 8);
+  // forces per block: 16^3 tiles 68 KB (three blocks of 256 threads per
+  // SM), 8 x 8 x 64 tiles 65 KB (three), 8^3 tiles 12 KB (eight)
+  const size_t smem = sizeof(float) * (T == kElong ? force_tile<kElong>::FLOATS
+                                                   : (T == 16 ? force_tile<16>::FLOATS : force_tile<8>::FLOATS));
+  constexpr int NTT = 256;
+  int nb = mgp_blocks_for(ntiles * NTT, T == 8 ? 8 : 3);
   if (nb > c->max_blocks) nb = c->max_blocks;
 #define MGP_IKD_TILES(TT, PP, PI)                                                                             \
   do {                                                                                                        \
-    constexpr int NTT = TT == 16 ? NT16 : NT8;                                                                \
     MGP_CUDA(cudaFuncSetAttribute(k_ikd_tiles<TT, PP, PI, NTT>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                   (int)smem));                                                                \
     k_ikd_tiles<TT, PP, PI, NTT><<<nb, NTT, smem, c->stream>>>(c->frc, c->g.nreal, N, c->g.P, Ns, ls, c->np,  \
                                                                c->s, c->v, (const float4 *)c->lpt, qp,        \
-                                                               c->tile_off, c->tile_order, nt1, c->dstate,    \
-                                                               c->s_alt, c->v_alt, c->q_alt, c->partials, *a); \
+                                                               c->tile_off, c->tile_order, nt1, ntz,          \
+                                                               c->dstate, c->s_alt, c->v_alt, c->q_alt,       \
+                                                               c->partials, *a);                              \
   } while (0)
   const bool narrow = 3 * c->np < 0xffffffffLL;
-  if (T == 16 && ls >= 0 && narrow)
+  if (T == kElong && ls >= 0 && narrow)
+    MGP_IKD_TILES(kElong, true, unsigned);
+  else if (T == kElong && ls >= 0)
+    MGP_IKD_TILES(kElong, true, long long);
+  else if (T == kElong)
+    MGP_IKD_TILES(kElong, false, long long);
+  else if (T == 16 && ls >= 0 && narrow)
     MGP_IKD_TILES(16, true, unsigned);
   else if (T == 16 && ls >= 0)
     MGP_IKD_TILES(16, true, long long);

@@ -127,7 +127,8 @@ def test_tile_deposit_matches_lattice_order_deposit(N, Ns, spread):
     np.testing.assert_array_equal(back[3], d2)
 
 
-@pytest.mark.parametrize("N,Ns", [(64, 32), (48, 24)])  # 16^3 tiles, power-of-two lattice; 8^3 tiles, general
+# 16^3 tiles, power-of-two lattice; 8^3 tiles, general lattice; 8 x 8 x 64 tiles (meshes of 512 and more)
+@pytest.mark.parametrize("N,Ns", [(64, 32), (48, 24), (512, 64)])
 @pytest.mark.parametrize("tiles", [2, 1])  # tile deposit and kick (the default); tile deposit only
 def test_tile_order_run_matches_lattice_order_run(tiles, N, Ns):
     """Five KDK steps with the cell-tile particle order (tile deposit; the
