@@ -321,12 +321,13 @@ def algorithmic_bytes(N, Np, kernel):
     }[kernel]
 
 
-# DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
-# nDGP step at 256^3 particles / 512^3 mesh, one launch each at step 46 of the 50-step run
-# (profiles/deposit_and_kick_late_ndgp_256_512.md; tile deposit and tile kick).  Every term
-# of these kernels scales with the particle count or the cell count, which grow together
-# between the configurations (Nmesh = 2 Nsample), so the figure is scaled by the cell count.
-TRAFFIC_256_512 = {"interp_kick_drift": 5.908e9, "cic": 1.364e9}
+# DRAM bytes per launch measured by ncu (dram__bytes.sum.per_second x gpu__time_duration.sum)
+# on the nDGP step at 256^3 particles / 512^3 mesh, one launch each at step 46 of the 50-step
+# run (profiles/deposit_and_kick_late_ndgp_256_512.md; tile deposit and tile kick over
+# 8 x 8 x 64-cell tiles).  Every term of these kernels scales with the particle count or the
+# cell count, which grow together between the configurations (Nmesh = 2 Nsample), so the
+# figure is scaled by the cell count.
+TRAFFIC_256_512 = {"interp_kick_drift": 4.246e9, "cic": 1.283e9}
 
 
 def measured_traffic(N, Np, kernel):
@@ -493,8 +494,8 @@ def run_gpu(args):
     traffic = measured_traffic(N, Np, dom)
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at step 46 of "
-                              "the 50-step run at 256^3 particles / 512^3 mesh, scaled by particles and cells",
+            "traffic_source": "ncu DRAM bytes of one launch at step 46 of the 50-step run at 256^3 particles / "
+                              "512^3 mesh (rate x duration), scaled by particles and cells",
             "algorithmic_bytes_per_launch": abytes, "mean_launch_ms": round(own[dom], 4),
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
     if closure is not None:
