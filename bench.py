@@ -415,6 +415,32 @@ def run_gpu(args):
     warm_ms = 0.0
     for _ in range(args.warmup):
         warm_ms = run()[0]
+    # e2e through the host-buffer C-ABI entry point, pinned host memory: one
+    # whole run from the IC state, after the warm-up runs and before the
+    # timed device runs (after tens of seconds of device runs in the process
+    # the downloads of some host-buffer steps were seen to stall for 20-70 ms;
+    # the step times are reported either way)
+    ctx.displacement_fields()
+    arrs = ctx.get_particles()
+    # the P[]-style arrays in page-locked host memory (mgp_host_alloc): on a
+    # busy host, copies from registered pageable arrays slowed down several-fold
+    pos, vel, d1, d2 = (M.host_array(a.shape) for a in arrs)
+    for dst, src in zip((pos, vel, d1, d2), arrs):
+        dst[...] = src
+    del arrs
+
+    def host_step(a, first):
+        # the LPT displacements D1, D2 (P[].D, P[].D2) are fixed after the IC:
+        # they travel with the first step of the run, later steps pass NULL
+        # and the step keeps the device copy (mgp_step_host)
+        t0 = time.perf_counter()
+        ctx.step_host(*a, pos, vel, d1 if first else None, d2 if first else None)
+        return time.perf_counter() - t0
+
+    barrier()
+    e2e_ms = [host_step(a, i == 0) * 1e3 for i, a in enumerate(schedule())]
+    e2e_t = reduce_max(sum(e2e_ms) * 1e-3, dist)
+    e2e_val = job_value(world, Np, nst, e2e_t)
     # per-stage events cost ~50 event records per KDK step on the host: with
     # steps of a few ms that is noise, but a launch-bound step of ~0.3 ms
     # would be slowed by them, so short steps take their stage times from one
@@ -447,29 +473,6 @@ def run_gpu(args):
             row["steps"] = [lo, hi - 1]
             deciles.append(row)
 
-    # e2e through the host-buffer C-ABI entry point, pinned host memory: one
-    # whole run from the IC state
-    ctx.displacement_fields()
-    arrs = ctx.get_particles()
-    # the P[]-style arrays in page-locked host memory (mgp_host_alloc): on a
-    # busy host, copies from registered pageable arrays slowed down several-fold
-    pos, vel, d1, d2 = (M.host_array(a.shape) for a in arrs)
-    for dst, src in zip((pos, vel, d1, d2), arrs):
-        dst[...] = src
-    del arrs
-
-    def host_step(a, first):
-        # the LPT displacements D1, D2 (P[].D, P[].D2) are fixed after the IC:
-        # they travel with the first step of the run, later steps pass NULL
-        # and the step keeps the device copy (mgp_step_host)
-        t0 = time.perf_counter()
-        ctx.step_host(*a, pos, vel, d1 if first else None, d2 if first else None)
-        return time.perf_counter() - t0
-
-    barrier()
-    e2e_ms = [host_step(a, i == 0) * 1e3 for i, a in enumerate(schedule())]
-    e2e_t = reduce_max(sum(e2e_ms) * 1e-3, dist)
-    e2e_val = job_value(world, Np, nst, e2e_t)
     # RSD multipoles P0/P2/P4 at z = 0 of that run's final state
     # (compute_RSD_powerspectrum, src/compute_pofk.c:403-512: y and z lines
     # of sight, averaged), timed end to end on the host (two

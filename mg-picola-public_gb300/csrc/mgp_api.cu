@@ -388,7 +388,7 @@ extern "C" int mgp_destroy(mgp_ctx *c) {
     free(c->box_cosmo);
   }
   free(c->box_p);
-  void *bufs[] = {c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
+  void *bufs[] = {c->ic_scratch, c->s, c->v, c->D1, c->D2, c->dstate, c->partials, c->stage, c->rho, c->dk, c->frc, c->mg1,
                   c->fft_work, c->rk_bin, c->pk_thr, c->win1d, c->pk_block, c->pk_sum, c->rsd_block, c->rsd_sum,
                   c->pk_sum_tot, c->nu_tab_d, c->nu_row_d, c->nu_x_d, c->nu_den_d, c->scr_tab};
   for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
@@ -646,8 +646,11 @@ static int ic_box(mgp_ctx *c, int bx, const double *pos01 = NULL, size_t npos = 
   CKC(cudaMalloc(&d_amp, sizeof(double) * amp.size()));
   CKC(cudaMalloc(&d_cut, cut.size()));
   // six scratch grids for the displacement gradients and the six
-  // displacement fields (2LPT.c:1214-1219, 1300-1306)
-  CKC(cudaMalloc(&g6, sizeof(float) * 6 * (size_t)gf));
+  // displacement fields (2LPT.c:1214-1219, 1300-1306), kept by the context
+  // for its next IC (runs of many ICs -- the boxes of a batch, repeated
+  // runs -- allocate them once)
+  if (!c->ic_scratch) CKC(cudaMalloc(&c->ic_scratch, sizeof(float) * 6 * (size_t)gf));
+  g6 = c->ic_scratch;
   CKC(cudaMemcpyAsync(d_seeds, seeds.data(), sizeof(uint32_t) * seeds.size(), cudaMemcpyHostToDevice, c->stream));
   CKC(cudaMemcpyAsync(d_amp, amp.data(), sizeof(double) * amp.size(), cudaMemcpyHostToDevice, c->stream));
   CKC(cudaMemcpyAsync(d_cut, cut.data(), cut.size(), cudaMemcpyHostToDevice, c->stream));
@@ -724,7 +727,7 @@ cleanup:
   if (d_seeds) cudaFree(d_seeds);
   if (d_amp) cudaFree(d_amp);
   if (d_cut) cudaFree(d_cut);
-  if (g6) cudaFree(g6);
+  (void)g6;  // the context's IC scratch, freed by mgp_destroy
 #undef CK
 #undef CKC
 #undef CKF

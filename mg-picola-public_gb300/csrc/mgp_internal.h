@@ -78,6 +78,7 @@ struct mgp_ctx {
 
   /* grids */
   float *rho, *dk, *frc, *mg1;
+  float *ic_scratch;        /* six grids for the 2LPT IC (lazy, kept for the next IC) */
   void *fft_work;
   size_t fft_work_bytes;
   cufftHandle plan_r2c_oop, plan_r2c_ip, plan_c2r_1;
