@@ -147,7 +147,7 @@ def run_c5(model, Nc=256, r=3, box=256.0, nsteps=30, train_seeds=range(7001, 701
            every=3, epochs=16, lr=2e-3, kmax=1.0, tol=0.01, band=True, net_seed=5, log=print, weights_out=None,
            highpass=None):
     """Learned-closure workload: collect training samples from the fine and
-    coarse meshes of `train_seeds`, train, and judge on `test_seeds` by the
+    coarse meshes of `train_seeds`, train, and evaluate on `test_seeds` by the
     final P(k) against the fine mesh.  The closure is accepted up to the k
     where its error stays within `tol`; beyond that the plain force is the
     result."""
@@ -199,7 +199,7 @@ def main(argv=None):
     import argparse
     import json
 
-    ap = argparse.ArgumentParser(description="train and judge the learned force closure")
+    ap = argparse.ArgumentParser(description="train and evaluate the learned force closure")
     ap.add_argument("--model", default="lcdm", choices=["lcdm", "fofr"])
     ap.add_argument("--nmesh", type=int, default=256)
     ap.add_argument("--ntrain", type=int, default=16)

@@ -3,7 +3,7 @@
  * conditions.
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links, loads or
- * calls this code; it is the checker that the CUDA path is compared against
+ * calls this code; it is the oracle that the CUDA path is compared against
  * (tests/, __graft_entry__.smoke() and the cpu_baseline / reference legs of
  * bench.py).  Every routine restates one reference routine in double
  * precision and cites it (paths are relative to the MG-PICOLA-PUBLIC tree).

@@ -1,5 +1,5 @@
 """Recipe: compile MG-PICOLA's own C sources, unmodified, into single-rank
-checker binaries (test infrastructure only).
+reference binaries (test infrastructure only).
 
 The reference needs FFTW3-MPI, GSL and MPI, which this image does not have;
 the sources are compiled against the project-written shims in
@@ -14,7 +14,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-# the reference's src/ directory; the checker is built only when it is given
+# the reference's src/ directory; the reference binaries are built only when it is given
 REF_SRC = os.environ.get("MGP_REFERENCE_SRC", "")
 OUT = os.path.join(HERE, "_ref")
 SOURCES = ["main.c", "auxPM.c", "2LPT.c", "cosmo.c", "power.c", "compute_pofk.c", "read_param.c", "vars.c",

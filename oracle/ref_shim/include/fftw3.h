@@ -1,4 +1,4 @@
-/* Stand-in for the FFTW3 interface used by MG-PICOLA (checker build only);
+/* Stand-in for the FFTW3 interface used by MG-PICOLA (reference test build only);
  * transforms are the oracle's FFTW-convention FFTs (oracle/orc_fft.c). */
 #ifndef REF_SHIM_FFTW3_H
 #define REF_SHIM_FFTW3_H

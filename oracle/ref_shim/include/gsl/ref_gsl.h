@@ -1,4 +1,4 @@
-/* Stand-in for the GSL interfaces used by MG-PICOLA (checker build only).
+/* Stand-in for the GSL interfaces used by MG-PICOLA (reference test build only).
  * Written from the documented behaviour of each call; numerics are textbook
  * methods (Philox streams, adaptive Dormand-Prince, natural cubic splines,
  * Keys cubic convolution in 2D, adaptive Gauss-Legendre, bisection, the

@@ -1,5 +1,5 @@
-/* Single-rank stand-in for the MPI interface used by MG-PICOLA (checker
- * build only).  Written from the MPI standard's semantics for one process:
+/* Single-rank stand-in for the MPI interface used by MG-PICOLA (reference
+ * test build only).  Written from the MPI standard's semantics for one process:
  * reductions copy, self send/receive copies, everything else is a no-op. */
 #ifndef REF_SHIM_MPI_H
 #define REF_SHIM_MPI_H

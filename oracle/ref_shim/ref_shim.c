@@ -1,7 +1,7 @@
 /*
  * Single-rank implementations of the MPI, FFTW3 and GSL calls made by the
  * MG-PICOLA sources, so that the reference's own code can be compiled into a
- * checker binary (oracle/_ref).  Test infrastructure only.
+ * test binary (oracle/_ref).  Test infrastructure only.
  *
  * Written from each call's documented semantics; none of the libraries'
  * code is reproduced.  Numerics: FFTs are the oracle's (oracle/orc_fft.c),
