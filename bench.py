@@ -417,9 +417,9 @@ def run_gpu(args):
         warm_ms = run()[0]
     # e2e through the host-buffer C-ABI entry point, pinned host memory: one
     # whole run from the IC state, after the warm-up runs and before the
-    # timed device runs (after tens of seconds of device runs in the process
-    # the downloads of some host-buffer steps were seen to stall for 20-70 ms;
-    # the step times are reported either way)
+    # timed device runs (on a host that ran GPU work before this process,
+    # one host-buffer step in every 5-6 was seen to stall for 50-75 ms in its
+    # copies; every step time is reported in e2e.step_ms)
     ctx.displacement_fields()
     arrs = ctx.get_particles()
     # the P[]-style arrays in page-locked host memory (mgp_host_alloc): on a
