@@ -213,10 +213,14 @@ __global__ void k_scan_add(unsigned *__restrict__ off, unsigned *__restrict__ cu
 }
 
 // Particle indices bucketed by tile (order inside a tile: the order in which
-// warps claim their slots).
+// warps claim their slots); with `lat` (a single box), also the lattice
+// point of every slot, lat[slot] = q[p] (p when q is NULL), so that the
+// deposit and the kick read it in slot order instead of through the index.
 __global__ void __launch_bounds__(kThreads) k_tile_scatter(const unsigned *__restrict__ tile_of, long long np,
                                                            unsigned *__restrict__ cursor,
-                                                           unsigned *__restrict__ order) {
+                                                           unsigned *__restrict__ order,
+                                                           const unsigned *__restrict__ q,
+                                                           unsigned *__restrict__ lat) {
   const int lane = threadIdx.x & 31;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np; base += stride) {
@@ -230,7 +234,9 @@ __global__ void __launch_bounds__(kThreads) k_tile_scatter(const unsigned *__res
     unsigned first = 0;
     if (lane == leader) first = atomicAdd(cursor + t, (unsigned)__popc(same));
     first = __shfl_sync(same, first, leader);
-    order[first + __popc(same & ((1u << lane) - 1u))] = (unsigned)p;
+    const unsigned slot = first + __popc(same & ((1u << lane) - 1u));
+    order[slot] = (unsigned)p;
+    if (lat) lat[slot] = q ? q[p] : (unsigned)p;
   }
 }
 
@@ -249,7 +255,7 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
                                                         float *__restrict__ rho, long long P,
                                                         const unsigned *__restrict__ off,
                                                         const unsigned *__restrict__ order,
-                                                        const unsigned *__restrict__ q, int ntx, int ntz, int nbox,
+                                                        const unsigned *__restrict__ qs, int ntx, int ntz, int nbox,
                                                         long long g_bs) {
   constexpr int KX = tile_tx(T), KZ = T, BX = KX + 1, BZ = KZ + 2, BOX = BX * BX * BZ;
   __shared__ float box[BOX];
@@ -277,8 +283,8 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
       const long long p = (long long)order[j] - pbase;  // slot of the j-th particle of the tile order
       int ix, iy, iz;
       float DX, DY, DZ;
-      particle_cell<P2>(s, np, p, q ? q[p] : (unsigned)p, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY,
-                        DZ);
+      particle_cell<P2>(s, np, p, qs ? qs[j] : (unsigned)p, Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX,
+                        DY, DZ);
       const float TX = 1.0f - DX, TY = (1.0f - DY) * wpar, TZ = 1.0f - DZ;
       DY *= wpar;
       const int lx = ix - x0, ly = iy - y0, lz = iz - z0;
@@ -395,11 +401,12 @@ __device__ __forceinline__ int tile_row(int c, int xx, int yy) {
 // particles whose CIC base cell lies in it (k_tile_key, same positions).
 // The block copies fx, fy, fz over the tile's cells and the +1 halo
 // (periodic) into shared memory (force_tile), then for each particle:
-// reads slot p = order[j] of the input arrays, interpolates the forces from
+// reads slot p = order[j] of the input arrays and its lattice point qs[j]
+// (written by the sort's scatter), interpolates the forces from
 // shared memory (a base cell outside the tile -- not expected, the key pass
 // rounds identically -- reads the global grids), kicks and drifts as
 // k_interp_kick_drift does (same expressions in the same order), and writes
-// slot j of the output arrays (s, v and q2[j] = its lattice point).  D1/D2
+// slot j of the output arrays (s, v; qs is the new order's lattice map).  D1/D2
 // (scale-independent growth) stay in lattice order, packed 32 bytes per
 // particle in `lpt` and read through the lattice point.  Per-block sums of the
 // interpolated forces and new velocities go to partials for k_finalize_kd.
@@ -409,9 +416,8 @@ template <int T, bool P2, typename PI, int NT>
 __global__ void __launch_bounds__(NT) k_ikd_tiles(
     const float *__restrict__ frc, long long gf, int N, long long P, int Ns, int ls, long long np,
     const float *__restrict__ s, const float *__restrict__ v, const float4 *__restrict__ lpt,
-    const unsigned *__restrict__ q, const unsigned *__restrict__ off, const unsigned *__restrict__ order, int ntx,
-    int ntz,
-    const mgp_dstate *__restrict__ st, float *__restrict__ s2, float *__restrict__ v2, unsigned *__restrict__ q2,
+    const unsigned *__restrict__ qs, const unsigned *__restrict__ off, const unsigned *__restrict__ order, int ntx,
+    int ntz, const mgp_dstate *__restrict__ st, float *__restrict__ s2, float *__restrict__ v2,
     double *__restrict__ partials, mgp_kd_args a) {
   using FT = force_tile<T>;
   constexpr int X = FT::X, R = FT::R, COMP = FT::COMP, K = FT::PIECES, KX = FT::TX, KZ = FT::TZ;
@@ -456,7 +462,7 @@ __global__ void __launch_bounds__(NT) k_ikd_tiles(
     const PI npi = (PI)np;
     for (unsigned j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
       const PI p = (PI)order[j];
-      const unsigned lat = q ? q[p] : (unsigned)p;
+      const unsigned lat = qs[j];
       const float sp[3] = {s[p], s[npi + p], s[2 * npi + p]};
       const float4 l0 = lpt[2 * (size_t)lat], l1 = lpt[2 * (size_t)lat + 1];
       const float D1p[3] = {l0.x, l0.y, l0.z}, D2p[3] = {l0.w, l1.x, l1.y};
@@ -500,7 +506,6 @@ __global__ void __launch_bounds__(NT) k_ikd_tiles(
         accD[ax] += disp[ax];
         accV[ax] += vn;
       }
-      q2[j] = lat;
     }
   }
 #pragma unroll
@@ -552,6 +557,12 @@ int mgp_tiles_alloc(mgp_ctx *c, int T) {
   if (!c->tile_order) {
     MGP_CUDA(cudaMalloc(&c->tile_of, sizeof(unsigned) * (size_t)nall));
     MGP_CUDA(cudaMalloc(&c->tile_order, sizeof(unsigned) * (size_t)nall));
+  }
+  if (c->nbox == 1 && !c->q) {
+    // q: lattice point of every slot of the particle arrays (in tile order
+    // after a tile kick); q_alt: the same for the slots of the last sort
+    MGP_CUDA(cudaMalloc(&c->q, sizeof(unsigned) * (size_t)c->np));
+    MGP_CUDA(cudaMalloc(&c->q_alt, sizeof(unsigned) * (size_t)c->np));
   }
   if (ntiles > c->tile_cap) {
     void *b[] = {c->tile_count, c->tile_off, c->tile_cursor, c->tile_bsum};
@@ -637,8 +648,8 @@ int mgp_tiles_sort(mgp_ctx *c, int T) {
                                                                         c->tile_bsum, (unsigned)nall);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
-  k_tile_scatter<<<mgp_blocks_for(nall, 8), kThreads, 0, c->stream>>>(c->tile_of, nall, c->tile_cursor,
-                                                                      c->tile_order);
+  k_tile_scatter<<<mgp_blocks_for(nall, 8), kThreads, 0, c->stream>>>(
+      c->tile_of, nall, c->tile_cursor, c->tile_order, qp, c->nbox == 1 ? c->q_alt : NULL);
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
   c->tile_ready = 1;
@@ -648,7 +659,8 @@ int mgp_tiles_sort(mgp_ctx *c, int T) {
 // Tile deposit onto meshes pre-set to -1 (after mgp_tiles_sort); per_sm:
 // resident blocks per SM of the launch (0: the default budget).
 int mgp_cic_tiles(mgp_ctx *c, float wpar, int per_sm) {
-  const unsigned *ord = c->tile_order, *qp = c->permuted ? c->q : NULL;
+  // lattice point of every slot of the sort (single box), else the slot's own
+  const unsigned *ord = c->tile_order, *qs = c->nbox == 1 ? c->q_alt : NULL;
   const int N = c->g.N, Ns = c->Ns, T = c->tile_side, nt1 = c->tile_n1, ntz = c->tile_nz, B = c->nbox;
   const long long gbs = c->g.nreal;
   const int ls = lattice_log2(Ns);
@@ -656,7 +668,7 @@ int mgp_cic_tiles(mgp_ctx *c, float wpar, int per_sm) {
   const int nb = mgp_blocks_for((long long)nt1 * nt1 * ntz * B * kThreads, per_sm > 0 ? per_sm : 8);
 #define MGP_CIC_TILES(TT, PP)                                                                                 \
   k_cic_tiles<TT, PP><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho, \
-                                                      c->g.P, c->tile_off, ord, qp, nt1, ntz, B, gbs)
+                                                      c->g.P, c->tile_off, ord, qs, nt1, ntz, B, gbs)
   if (T == kElong && ls >= 0)
     MGP_CIC_TILES(kElong, true);
   else if (T == kElong)
@@ -686,8 +698,6 @@ int mgp_ikd_tiles(mgp_ctx *c, const mgp_kd_args *a, int *nblocks_out) {
   if (!c->s_alt) {
     MGP_CUDA(cudaMalloc(&c->s_alt, bytes));
     MGP_CUDA(cudaMalloc(&c->v_alt, bytes));
-    MGP_CUDA(cudaMalloc(&c->q, sizeof(unsigned) * (size_t)c->np));
-    MGP_CUDA(cudaMalloc(&c->q_alt, sizeof(unsigned) * (size_t)c->np));
     MGP_CUDA(cudaMalloc(&c->lpt, sizeof(float) * 8 * (size_t)c->np));
     c->lpt_built = -1;
   }
@@ -701,7 +711,6 @@ int mgp_ikd_tiles(mgp_ctx *c, const mgp_kd_args *a, int *nblocks_out) {
   const int T = c->tile_side, nt1 = c->tile_n1, ntz = c->tile_nz, N = c->g.N, Ns = c->Ns;
   const int ls = lattice_log2(Ns);
   const long long ntiles = (long long)nt1 * nt1 * ntz;
-  const unsigned *qp = c->permuted ? c->q : NULL;
   // forces per block: 16^3 tiles 68 KB (three blocks of 256 threads per
   // SM), 8 x 8 x 64 tiles 65 KB (three), 8^3 tiles 12 KB (eight)
   const size_t smem = sizeof(float) * (T == kElong ? force_tile<kElong>::FLOATS
@@ -714,10 +723,10 @@ int mgp_ikd_tiles(mgp_ctx *c, const mgp_kd_args *a, int *nblocks_out) {
     MGP_CUDA(cudaFuncSetAttribute(k_ikd_tiles<TT, PP, PI, NTT>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                   (int)smem));                                                                \
     k_ikd_tiles<TT, PP, PI, NTT><<<nb, NTT, smem, c->stream>>>(c->frc, c->g.nreal, N, c->g.P, Ns, ls, c->np,  \
-                                                               c->s, c->v, (const float4 *)c->lpt, qp,        \
+                                                               c->s, c->v, (const float4 *)c->lpt, c->q_alt,  \
                                                                c->tile_off, c->tile_order, nt1, ntz,          \
-                                                               c->dstate, c->s_alt, c->v_alt, c->q_alt,       \
-                                                               c->partials, *a);                              \
+                                                               c->dstate, c->s_alt, c->v_alt, c->partials,    \
+                                                               *a);                                           \
   } while (0)
   const bool narrow = 3 * c->np < 0xffffffffLL;
   if (T == kElong && ls >= 0 && narrow)
