@@ -978,13 +978,15 @@ extern "C" int mgp_get_displacements(mgp_ctx *c, double A) {
     RET_IF(mgp_tiles_sort(c, mgp_tile_side(N, c->np)));
     tstop(c, T_SORT);
   }
+  // the tile deposit stores every cell of the mesh itself (owner writes),
+  // the particle-order deposit adds to a mesh pre-set to -1
   tstart(c, T_FILL);
-  RET_IF(mgp_launch_fill(c->rho, c->g.nreal, -1.0f, c->stream));
+  if (!tiles) RET_IF(mgp_launch_fill(c->rho, c->g.nreal, -1.0f, c->stream));
   tstop(c, T_FILL);
   tstart(c, T_CIC);
   double wpar = pow((double)N / (double)c->Ns, 3);
   if (tiles)
-    RET_IF(mgp_cic_tiles(c, (float)wpar));
+    RET_IF(mgp_cic_tiles_own(c, (float)wpar));
   else
     RET_IF(mgp_launch_cic(c->s, c->dstate, c->np, c->Ns, N, c->p.Box, (float)wpar, c->rho, c->g.P, c->stream));
   tstop(c, T_CIC);

@@ -177,6 +177,11 @@ struct mgp_ctx {
   unsigned *tile_of, *tile_order, *tile_count, *tile_off, *tile_cursor, *tile_bsum;
   int tile_side, tile_n1, tile_nz, tile_ready;  /* shape code, tiles along x and y, along z */
   long long tile_cap;       /* tiles the count/offset arrays hold */
+  /* owner-writes deposit of a single box: halo pairs of every tile, and the
+   * slots of particles deposited after the interiors (np entries + count) */
+  void *tile_halo;
+  size_t tile_halo_bytes;
+  unsigned *tile_spill;
   int batch_tile;           /* batch deposit: tile side (8, 16) or 0 for the lattice-order deposit */
   int tile_mode;            /* 1 (default): tile deposit where it applies; 0: particle order */
   /* particle arrays held in cell-tile order (single box, scale-independent
@@ -333,6 +338,8 @@ int mgp_tiles_alloc(mgp_ctx *c, int T);
 void mgp_tiles_free(mgp_ctx *c);
 int mgp_tiles_sort(mgp_ctx *c, int T);
 int mgp_cic_tiles(mgp_ctx *c, float wpar, int per_sm = 0);
+/* single-box tile deposit writing every cell itself (no pre-set mesh) */
+int mgp_cic_tiles_own(mgp_ctx *c, float wpar);
 /* kick + drift in the order of the last mgp_tiles_sort, the particle
  * arrays rewritten in that order */
 int mgp_ikd_tiles(mgp_ctx *c, const mgp_kd_args *a, int *nblocks_out);

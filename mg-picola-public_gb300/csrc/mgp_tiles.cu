@@ -329,6 +329,173 @@ __global__ void __launch_bounds__(kThreads) k_cic_tiles(const float *__restrict_
   }
 }
 
+// The single-box deposit writes each tile's interior cells itself: a tile's
+// box [KX+1][KX+1][KZ+2] splits into the interior (x, y < KX, z < KZ), which
+// no other tile's box covers, and the halo, kept as float2 pairs along z
+// (z even): face x = KX (all y, all z), face y = KX (x < KX, all z), and the
+// pair (KZ, KZ+1) of the interior rows.  The last column of the box (z =
+// KZ+1) only pads the rows to an even length and stays zero.
+template <int T>
+struct tile_halo {
+  static constexpr int KX = tile_tx(T), KZ = T, BX = KX + 1, BZ = KZ + 2, RP = BZ / 2;  // pairs per box row
+  static constexpr int FX = BX * RP, FY = KX * RP, FZ = KX * KX, PAIRS = FX + FY + FZ;
+};
+
+// Box cell (xx, yy, zz) of halo pair h (zz even).
+template <int T>
+__device__ __forceinline__ void halo_pair(int h, int &xx, int &yy, int &zz) {
+  using H = tile_halo<T>;
+  if (h < H::FX) {
+    xx = H::KX;
+    yy = h / H::RP;
+    zz = 2 * (h - yy * H::RP);
+  } else if (h < H::FX + H::FY) {
+    const int g = h - H::FX;
+    xx = g / H::RP;
+    yy = H::KX;
+    zz = 2 * (g - xx * H::RP);
+  } else {
+    const int g = h - H::FX - H::FY;
+    xx = g / H::KX;
+    yy = g - xx * H::KX;
+    zz = H::KZ;
+  }
+}
+
+// PtoMesh (src/auxPM.c:280-357) per tile, owner writes (single box): the
+// tile's particles are summed in shared memory as in k_cic_tiles, then the
+// block stores its interior cells as box - 1 with plain stores (the mesh
+// needs no pre-set; every tile stores its interior, empty or not, and the
+// last tile in z also sets the row padding to -1 as a fill would), and writes
+// its halo pairs to `halo` (PAIRS per tile).  k_cic_halo then adds the halos
+// to the neighbours' interiors.  A particle whose base cell falls outside its
+// tile after all (not expected: the key pass rounds identically) is listed in
+// `spill` for k_cic_halo, after every interior has been stored.
+template <int T, bool P2>
+__global__ void __launch_bounds__(kThreads) k_cic_tiles_own(const float *__restrict__ s,
+                                                            const mgp_dstate *__restrict__ st, long long np, int Ns,
+                                                            int ls, int N, float scale, float wpar,
+                                                            float *__restrict__ rho, long long P,
+                                                            const unsigned *__restrict__ off,
+                                                            const unsigned *__restrict__ order,
+                                                            const unsigned *__restrict__ qs, int ntx, int ntz,
+                                                            float2 *__restrict__ halo, unsigned *__restrict__ spill,
+                                                            unsigned *__restrict__ nspill) {
+  using H = tile_halo<T>;
+  constexpr int KX = H::KX, KZ = H::KZ, BX = H::BX, BZ = H::BZ, BOX = BX * BX * BZ;
+  __shared__ __align__(16) float box[BOX];
+  const float inv_ns = 1.0f / (float)Ns;
+  const int ntiles = ntx * ntx * ntz;
+  const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
+  for (int L = blockIdx.x; L < ntiles; L += gridDim.x) {
+    const int tile = tile_at(L, ntx, ntz);
+    const unsigned j0 = off[tile], j1 = off[tile + 1];
+    const int tz = tile % ntz, ty = (tile / ntz) % ntx, tx = tile / (ntz * ntx);
+    const int x0 = tx * KX, y0 = ty * KX, z0 = tz * KZ;
+    for (int e = threadIdx.x; e < BOX; e += blockDim.x) box[e] = 0.0f;
+    __syncthreads();
+    for (unsigned j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+      const long long p = (long long)order[j];
+      int ix, iy, iz;
+      float DX, DY, DZ;
+      particle_cell<P2>(s, np, p, qs[j], Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY, DZ);
+      const float TX = 1.0f - DX, TY = (1.0f - DY) * wpar, TZ = 1.0f - DZ;
+      DY *= wpar;
+      const int lx = ix - x0, ly = iy - y0, lz = iz - z0;
+      if ((unsigned)lx >= (unsigned)KX || (unsigned)ly >= (unsigned)KX || (unsigned)lz >= (unsigned)KZ) {
+        spill[atomicAdd(nspill, 1u)] = j;  // at most np entries: every slot once
+        continue;
+      }
+      const int b = (lx * BX + ly) * BZ + lz;
+      atomicAdd(box + b, TX * TY * TZ);
+      atomicAdd(box + b + 1, TX * TY * DZ);
+      atomicAdd(box + b + BZ, TX * DY * TZ);
+      atomicAdd(box + b + BZ + 1, TX * DY * DZ);
+      atomicAdd(box + b + BX * BZ, DX * TY * TZ);
+      atomicAdd(box + b + BX * BZ + 1, DX * TY * DZ);
+      atomicAdd(box + b + BX * BZ + BZ, DX * DY * TZ);
+      atomicAdd(box + b + BX * BZ + BZ + 1, DX * DY * DZ);
+    }
+    __syncthreads();
+    // interior: rows of the mesh have even length and z0 is even, so every
+    // pair is 8-byte aligned
+    for (int e = threadIdx.x; e < KX * KX * (KZ / 2); e += blockDim.x) {
+      const int zp = e % (KZ / 2), r = e / (KZ / 2), yy = r % KX, xx = r / KX;
+      const float2 v = *reinterpret_cast<const float2 *>(box + (xx * BX + yy) * BZ + 2 * zp);
+      *reinterpret_cast<float2 *>(rho + ((long long)(x0 + xx) * N + (y0 + yy)) * P + z0 + 2 * zp) =
+          make_float2(v.x - 1.0f, v.y - 1.0f);
+    }
+    if (z0 + KZ == N) {
+      for (int r = threadIdx.x; r < KX * KX; r += blockDim.x) {
+        const int yy = r % KX, xx = r / KX;
+        *reinterpret_cast<float2 *>(rho + ((long long)(x0 + xx) * N + (y0 + yy)) * P + N) = make_float2(-1.0f, -1.0f);
+      }
+    }
+    float2 *hp = halo + (long long)tile * H::PAIRS;
+    for (int h = threadIdx.x; h < H::PAIRS; h += blockDim.x) {
+      int xx, yy, zz;
+      halo_pair<T>(h, xx, yy, zz);
+      hp[h] = *reinterpret_cast<const float2 *>(box + (xx * BX + yy) * BZ + zz);
+    }
+    __syncthreads();  // the box is cleared for the next tile
+  }
+}
+
+// The halos of k_cic_tiles_own added to the mesh (float2 reductions, zero
+// pairs skipped; a pair never straddles the periodic wrap: z0 + KZ is even
+// and at most N), then the listed particles straight to the mesh.
+template <int T, bool P2>
+__global__ void __launch_bounds__(kThreads) k_cic_halo(const float2 *__restrict__ halo, int ntx, int ntz,
+                                                       float *__restrict__ rho, long long P,
+                                                       const float *__restrict__ s,
+                                                       const mgp_dstate *__restrict__ st, long long np, int Ns,
+                                                       int ls, int N, float scale, float wpar,
+                                                       const unsigned *__restrict__ order,
+                                                       const unsigned *__restrict__ qs,
+                                                       const unsigned *__restrict__ spill,
+                                                       const unsigned *__restrict__ nspill) {
+  using H = tile_halo<T>;
+  const long long n = (long long)ntx * ntx * ntz * H::PAIRS;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float2 v = halo[i];
+    if (v.x == 0.0f && v.y == 0.0f) continue;
+    const int tile = (int)(i / H::PAIRS), h = (int)(i - (long long)tile * H::PAIRS);
+    int xx, yy, zz;
+    halo_pair<T>(h, xx, yy, zz);
+    const int tz = tile % ntz, ty = (tile / ntz) % ntx, tx = tile / (ntz * ntx);
+    int gx = tx * H::KX + xx, gy = ty * H::KX + yy, gz = tz * H::KZ + zz;
+    if (gx >= N) gx -= N;
+    if (gy >= N) gy -= N;
+    if (gz >= N) gz -= N;
+    atomicAdd(reinterpret_cast<float2 *>(rho + ((long long)gx * N + gy) * P + gz), v);
+  }
+  const unsigned ns = *nspill;
+  if (ns == 0) return;
+  const float inv_ns = 1.0f / (float)Ns;
+  const float ox = (float)(st->cx[0] * scale), oy = (float)(st->cx[1] * scale), oz = (float)(st->cx[2] * scale);
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < (long long)ns; k += stride) {
+    const unsigned j = spill[k];
+    int ix, iy, iz;
+    float DX, DY, DZ;
+    particle_cell<P2>(s, np, (long long)order[j], qs[j], Ns, ls, inv_ns, N, scale, ox, oy, oz, ix, iy, iz, DX, DY,
+                      DZ);
+    const float TX = 1.0f - DX, TY = (1.0f - DY) * wpar, TZ = 1.0f - DZ;
+    DY *= wpar;
+    const int ixn = ix + 1 == N ? 0 : ix + 1, iyn = iy + 1 == N ? 0 : iy + 1, izn = iz + 1 == N ? 0 : iz + 1;
+    float *r00 = rho + ((long long)ix * N + iy) * P, *r01 = rho + ((long long)ix * N + iyn) * P;
+    float *r10 = rho + ((long long)ixn * N + iy) * P, *r11 = rho + ((long long)ixn * N + iyn) * P;
+    atomicAdd(r00 + iz, TX * TY * TZ);
+    atomicAdd(r00 + izn, TX * TY * DZ);
+    atomicAdd(r01 + iz, TX * DY * TZ);
+    atomicAdd(r01 + izn, TX * DY * DZ);
+    atomicAdd(r10 + iz, DX * TY * TZ);
+    atomicAdd(r10 + izn, DX * TY * DZ);
+    atomicAdd(r11 + iz, DX * DY * TZ);
+    atomicAdd(r11 + izn, DX * DY * DZ);
+  }
+}
+
 // Back to lattice order: the particle of slot j goes to slot q[j] (D1 and
 // D2 are never permuted).
 __global__ void __launch_bounds__(kThreads) k_unpermute(long long np, const float *__restrict__ s,
@@ -582,9 +749,12 @@ int mgp_tiles_alloc(mgp_ctx *c, int T) {
 
 void mgp_tiles_free(mgp_ctx *c) {
   void *b[] = {c->tile_of, c->tile_order, c->tile_count, c->tile_off, c->tile_cursor, c->tile_bsum,
-               c->q, c->q_alt, c->s_alt, c->v_alt, c->lpt};
+               c->q, c->q_alt, c->s_alt, c->v_alt, c->lpt, c->tile_halo, c->tile_spill};
   for (void *x : b)
     if (x) cudaFree(x);
+  c->tile_halo = NULL;
+  c->tile_spill = NULL;
+  c->tile_halo_bytes = 0;
   c->tile_of = c->tile_order = c->tile_count = c->tile_off = c->tile_cursor = c->tile_bsum = NULL;
   c->q = c->q_alt = NULL;
   c->s_alt = c->v_alt = c->lpt = NULL;
@@ -684,6 +854,62 @@ int mgp_cic_tiles(mgp_ctx *c, float wpar, int per_sm) {
 #undef MGP_CIC_TILES
   MGP_CHECK_LAUNCH();
   g_kernel_launches++;
+  return MGP_OK;
+}
+
+// Single-box tile deposit with owner writes (after mgp_tiles_sort; the
+// mesh needs no pre-set): k_cic_tiles_own stores every tile's interior and
+// its halo pairs, k_cic_halo adds the halos and the listed particles.
+int mgp_cic_tiles_own(mgp_ctx *c, float wpar) {
+  if (c->nbox != 1 || !c->tile_ready) return mgp_set_error(MGP_ESTATE, "owner-writes deposit without a current tile sort");
+  const int N = c->g.N, Ns = c->Ns, T = c->tile_side, nt1 = c->tile_n1, ntz = c->tile_nz;
+  if (c->g.P != N + 2) return mgp_set_error(MGP_EINVAL, "mesh rows of %lld floats, expected %d", c->g.P, N + 2);
+  const long long ntiles = (long long)nt1 * nt1 * ntz;
+  const int pairs = T == kElong ? tile_halo<kElong>::PAIRS : (T == 16 ? tile_halo<16>::PAIRS : tile_halo<8>::PAIRS);
+  const size_t hbytes = sizeof(float2) * (size_t)ntiles * (size_t)pairs;
+  if (hbytes > c->tile_halo_bytes) {
+    if (c->tile_halo) cudaFree(c->tile_halo);
+    c->tile_halo = NULL;
+    c->tile_halo_bytes = 0;
+    MGP_CUDA(cudaMalloc(&c->tile_halo, hbytes));
+    c->tile_halo_bytes = hbytes;
+  }
+  if (!c->tile_spill) {
+    MGP_CUDA(cudaMalloc(&c->tile_spill, sizeof(unsigned) * ((size_t)c->np + 1)));
+  }
+  unsigned *nspill = c->tile_spill + c->np;
+  MGP_CUDA(cudaMemsetAsync(nspill, 0, sizeof(unsigned), c->stream));
+  const int ls = lattice_log2(Ns);
+  const float scale = (float)(N / c->p.Box);
+  float2 *halo = (float2 *)c->tile_halo;
+  const int nb = mgp_blocks_for(ntiles * kThreads, 8);
+  const int nh = mgp_blocks_for(ntiles * pairs, 8);
+#define MGP_CIC_OWN(TT, PP)                                                                                          \
+  do {                                                                                                               \
+    k_cic_tiles_own<TT, PP><<<nb, kThreads, 0, c->stream>>>(c->s, c->dstate, c->np, Ns, ls, N, scale, wpar, c->rho, \
+                                                            c->g.P, c->tile_off, c->tile_order, c->q_alt, nt1, ntz, \
+                                                            halo, c->tile_spill, nspill);                            \
+    MGP_CHECK_LAUNCH();                                                                                              \
+    g_kernel_launches++;                                                                                             \
+    k_cic_halo<TT, PP><<<nh, kThreads, 0, c->stream>>>(halo, nt1, ntz, c->rho, c->g.P, c->s, c->dstate, c->np, Ns,  \
+                                                       ls, N, scale, wpar, c->tile_order, c->q_alt, c->tile_spill,   \
+                                                       nspill);                                                      \
+    MGP_CHECK_LAUNCH();                                                                                              \
+    g_kernel_launches++;                                                                                             \
+  } while (0)
+  if (T == kElong && ls >= 0)
+    MGP_CIC_OWN(kElong, true);
+  else if (T == kElong)
+    MGP_CIC_OWN(kElong, false);
+  else if (T == 16 && ls >= 0)
+    MGP_CIC_OWN(16, true);
+  else if (T == 16)
+    MGP_CIC_OWN(16, false);
+  else if (ls >= 0)
+    MGP_CIC_OWN(8, true);
+  else
+    MGP_CIC_OWN(8, false);
+#undef MGP_CIC_OWN
   return MGP_OK;
 }
 
