@@ -578,9 +578,10 @@ __device__ __forceinline__ int tile_row(int c, int xx, int yy) {
 // particle in `lpt` and read through the lattice point.  Per-block sums of the
 // interpolated forces and new velocities go to partials for k_finalize_kd.
 // PI: particle-array offset type, 32-bit when 3 np < 2^32 (fewer integer
-// instructions per access); NT: threads per block.
+// instructions per access); NT: threads per block (512: two blocks per SM
+// within 64 registers a thread).
 template <int T, bool P2, typename PI, int NT>
-__global__ void __launch_bounds__(NT) k_ikd_tiles(
+__global__ void __launch_bounds__(NT, NT >= 512 ? 2 : 0) k_ikd_tiles(
     const float *__restrict__ frc, long long gf, int N, long long P, int Ns, int ls, long long np,
     const float *__restrict__ s, const float *__restrict__ v, const float4 *__restrict__ lpt,
     const unsigned *__restrict__ qs, const unsigned *__restrict__ off, const unsigned *__restrict__ order, int ntx,
@@ -938,14 +939,15 @@ int mgp_ikd_tiles(mgp_ctx *c, const mgp_kd_args *a, int *nblocks_out) {
   const int ls = lattice_log2(Ns);
   const long long ntiles = (long long)nt1 * nt1 * ntz;
   // forces per block: 16^3 tiles 68 KB (three blocks of 256 threads per
-  // SM), 8 x 8 x 64 tiles 65 KB (three), 8^3 tiles 12 KB (eight)
+  // SM), 8 x 8 x 64 tiles 65 KB (two blocks of 512), 8^3 tiles 12 KB (eight
+  // of 256)
   const size_t smem = sizeof(float) * (T == kElong ? force_tile<kElong>::FLOATS
                                                    : (T == 16 ? force_tile<16>::FLOATS : force_tile<8>::FLOATS));
-  constexpr int NTT = 256;
-  int nb = mgp_blocks_for(ntiles * NTT, T == 8 ? 8 : 3);
+  int nb = T == kElong ? mgp_blocks_for(ntiles * 256, 2) : mgp_blocks_for(ntiles * 256, T == 8 ? 8 : 3);
   if (nb > c->max_blocks) nb = c->max_blocks;
 #define MGP_IKD_TILES(TT, PP, PI)                                                                             \
   do {                                                                                                        \
+    constexpr int NTT = TT == kElong ? 512 : 256;                                                             \
     MGP_CUDA(cudaFuncSetAttribute(k_ikd_tiles<TT, PP, PI, NTT>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                   (int)smem));                                                                \
     k_ikd_tiles<TT, PP, PI, NTT><<<nb, NTT, smem, c->stream>>>(c->frc, c->g.nreal, N, c->g.P, Ns, ls, c->np,  \
