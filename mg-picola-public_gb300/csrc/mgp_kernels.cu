@@ -248,8 +248,21 @@ __global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
     const long long rows[4] = {(long long)d0 * N + d1, (long long)d0 * N + (N - d1), (long long)(N - d0) * N + d1,
                                (long long)(N - d0) * N + (N - d1)};
     const bool use[4] = {true, mj, mi, mi && mj};
+    // the rows' next 32 modes are loaded while the current ones are binned
+    float2 zn[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+      if (use[t] && lane < NH) zn[t] = dkb[rows[t] * NH + lane];
     for (int k0 = 0; k0 < NH; k0 += 32) {
       const int kz = k0 + lane;
+      float2 z[4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) z[t] = zn[t];
+      if (kz + 32 < NH) {
+#pragma unroll
+        for (int t = 0; t < 4; t++)
+          if (use[t]) zn[t] = dkb[rows[t] * NH + kz + 32];
+      }
       int bin = -1;
       float pk = 0.0f;
       if (kz < NH) {
@@ -268,10 +281,6 @@ __global__ void __launch_bounds__(MGP_THREADS) k_pofk(mgp_pofk_kargs a) {
           bin = a.rk_bin[rk];
         }
         const float f = a.fuse_kind ? mg_kfilter(rk, a.fuse_kind, a.filter, a.fuse_a, a.fuse_b) : 0.0f;
-        float2 z[4];
-#pragma unroll
-        for (int t = 0; t < 4; t++)
-          if (use[t]) z[t] = dkb[rows[t] * NH + kz];
         float p2 = 0.0f;
 #pragma unroll
         for (int t = 0; t < 4; t++)
