@@ -1,28 +1,31 @@
 // Cell-tile order of the particles for the two particle passes of the PM
 // step (sm_103a).
 //
-// The particle arrays stay in Lagrangian (lattice) order.  Once per step,
+// The IC writes the particles in Lagrangian (lattice) order.  Once per step,
 // before the deposit, the particles are counted and bucketed by the
-// TX x TX x TZ-cell tile of their CIC base cell (a counting sort of the particle indices, 8
-// bytes per particle of traffic besides one read of the displacements):
+// TX x TX x TZ-cell tile of their CIC base cell (a counting sort of the
+// particle indices):
 //   k_tile_key      tile of every particle, tile counts (warp-aggregated)
 //   k_scan_*        exclusive prefix sum of the counts = tile offsets
-//   k_tile_scatter  particle indices bucketed by tile
+//   k_tile_scatter  particle indices bucketed by tile and, for a single box,
+//                   the lattice point of every slot beside its index
 // Then
-//   k_cic_tiles     PtoMesh (src/auxPM.c:280-357): one block per tile
-//                   accumulates its particles' CIC weights in a shared-memory
-//                   copy of the tile plus its +1 halo, then adds the copy to
-//                   the mesh with one vector reduction per pair of cells
-//                   (about 1.7 L2 reduction sectors per particle instead of
-//                   ~4.3 for eight scalar reductions per particle);
+//   k_cic_tiles_own PtoMesh (src/auxPM.c:280-357) for a single box: one block
+//   + k_cic_halo    per tile accumulates its particles' CIC weights in a
+//                   shared-memory copy of the tile plus its +1 halo, stores
+//                   the tile's interior cells itself (no pre-set mesh) and
+//                   leaves the halo as float2 pairs, which the second pass
+//                   adds to the neighbouring tiles' cells;
+//   k_cic_tiles     the same sums for batches, added to a mesh pre-set to -1
+//                   with one vector reduction per pair of cells;
 //   k_ikd_tiles     MtoParticles + Kick + Drift (src/auxPM.c:560-644,
 //                   src/main.c:688-787) per tile: the block copies the three
 //                   force grids over the tile and its +1 halo into shared
 //                   memory, interpolates its particles' forces there, and
-//                   writes every particle (s, v, D1, D2 and its lattice point
-//                   q) to its slot in the tile order, so that the arrays
-//                   follow the particles and the next step's reads stay
-//                   nearly sequential.
+//                   writes every particle's s and v to its slot in the tile
+//                   order (the sort's lattice map then describes the arrays),
+//                   so that the arrays follow the particles and the next
+//                   step's reads stay nearly sequential.
 // Any order gives the same density and forces (up to the order of
 // floating-point sums); the tile order restores the locality that the
 // Lagrangian order loses as the particles cluster.
