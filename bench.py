@@ -328,10 +328,11 @@ def algorithmic_bytes(N, Np, kernel):
 # DRAM bytes per launch measured by ncu (dram__bytes.sum.per_second x gpu__time_duration.sum)
 # on the nDGP step at 256^3 particles / 512^3 mesh, one launch each at step 46 of the 50-step
 # run (profiles/deposit_and_kick_late_ndgp_256_512.md; tile deposit and tile kick over
-# 8 x 8 x 64-cell tiles, the kick reading each slot's lattice point from the sort).  Every term of these kernels scales with the particle count or the
+# 8 x 8 x 64-cell tiles, the kick reading each slot's lattice point from the sort; the
+# deposit's figure is its two passes, tile sums with owner writes and the halo pass).  Every term of these kernels scales with the particle count or the
 # cell count, which grow together between the configurations (Nmesh = 2 Nsample), so the
 # figure is scaled by the cell count.
-TRAFFIC_256_512 = {"interp_kick_drift": 4.154e9, "cic": 1.283e9}
+TRAFFIC_256_512 = {"interp_kick_drift": 4.154e9, "cic": 1.420e9}
 
 
 def measured_traffic(N, Np, kernel):
