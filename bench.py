@@ -335,8 +335,10 @@ def algorithmic_bytes(N, Np, kernel):
 TRAFFIC_256_512 = {"interp_kick_drift": 4.154e9, "cic": 1.420e9}
 
 
-def measured_traffic(N, Np, kernel):
-    if kernel not in TRAFFIC_256_512 or Np * 8 != N ** 3:
+def measured_traffic(cfg, N, Np, kernel):
+    # captured on the nDGP step's tile path only (scale-dependent growth and
+    # the closure workloads run other kick or deposit forms)
+    if kernel not in TRAFFIC_256_512 or Np * 8 != N ** 3 or cfg.get("model") != "dgp" or cfg.get("sd"):
         return None
     return int(TRAFFIC_256_512[kernel] * (N / 512.0) ** 3)
 
@@ -499,11 +501,12 @@ def run_gpu(args):
     abytes = algorithmic_bytes(N, Np, dom)
     achieved = abytes / (own[dom] * 1e-3) / 1e9
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = measured_traffic(N, Np, dom)
+    traffic = measured_traffic(cfg, N, Np, dom)
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
-            "traffic_source": "ncu DRAM bytes of one launch at step 46 of the 50-step run at 256^3 particles / "
-                              "512^3 mesh (rate x duration), scaled by particles and cells",
+            "traffic_source": ("ncu DRAM bytes of one launch at step 46 of the 50-step nDGP run at 256^3 particles / "
+                               "512^3 mesh (rate x duration), scaled by particles and cells") if traffic else
+                              "no ncu capture of this kernel for this workload",
             "algorithmic_bytes_per_launch": abytes, "mean_launch_ms": round(own[dom], 4),
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
     if closure is not None:
