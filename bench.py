@@ -318,8 +318,9 @@ def algorithmic_bytes(N, Np, kernel):
         "cic": 12 * Np + 4 * N ** 3,                 # read s, write the mesh once
         "pofk": 8 * ncomplex,                         # read delta(k)
         "forces": 2 * 8 * ncomplex + 3 * 8 * ncomplex,  # read delta, MG source; write 3 complex grids
-        # force grids once; s,v,D1,D2 in, s,v out (the tile kick also moves the order, q and
-        # D1, D2 in tile order: 108 Np by design, counted as overhead, not as work)
+        # force grids once; s,v,D1,D2 in, s,v out (the tile kick also reads the order and each
+        # slot's lattice point, and D1, D2 as a 32-byte record: 88 Np by design, the extra
+        # counted as overhead, not as work)
         "interp_kick_drift": 12 * N ** 3 + 72 * Np,
         "mg": 8 * ncomplex + 4 * nreal + 8 * nreal,   # smoothing pass + screening pass (excl. FFTs)
     }[kernel]
